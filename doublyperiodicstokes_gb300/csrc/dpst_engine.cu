@@ -1,0 +1,858 @@
+// Engine and C ABI of libdpstokes_gb300.so (declared in include/dpstokes_gb300.h).
+//
+// Host side of the operator: validates parameters, reproduces the
+// reference's set-up arithmetic (Chebyshev grid and weights, kernel
+// normalisation and truncation threshold, extended z grid, BC rows,
+// integration matrices, DCT-I matrices; stochasticHydroTools/
+// DoublyPeriodicStokes source/cpu: Chebyshev.py:4-160, Quadrature.cpp:11-46,
+// ParticleList.cpp:211-276 and 394-451, Solvers.py:258-347 and 603-643,
+// FCM.py:211-248), owns the device buffers and cuFFT plans, and runs the
+// Mdot pipeline:
+//   zero grid -> spread F (+ torque curl) -> [fold open-end ghost layers]
+//   -> x-y FFT -> z DCT-I -> per-k BVP -> inverse z DCT-I (+ wall correction)
+//   -> inverse x-y FFT -> interpolate V (+ W).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dpstokes_gb300.h"
+#include "dpst_internal.cuh"
+
+namespace dpst {
+
+// ---- declarations of the kernel launchers (dpst_particles.cu, dpst_kspace.cu)
+template <typename R>
+void launch_locate(bool dipole, const double *pos, int64_t N, const KernelDesc &kd, const double *zext,
+                   const double *wext, const GridArgs &g, const Stencils<R> &st, int *err, int *reach,
+                   cudaStream_t s);
+template <typename R, typename RF>
+void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s);
+template <typename R>
+void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s);
+template <typename R, typename RV>
+void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s);
+
+
+void launch_bvp_factors(const KsArgs &a, cudaStream_t s);
+template <typename R>
+void launch_bvp(const KsArgs &a, R *spec, double2 *corr, double2 *scratch, int64_t nthreads,
+                cudaStream_t s);
+template <typename R>
+cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
+                         cudaStream_t s);
+
+// ---- errors -----------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+#define DPST_CUDA(call)                                                                          \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess)                                                                       \
+      throw Error(e_ == cudaErrorMemoryAllocation ? DPST_ERR_ALLOC : DPST_ERR_CUDA,              \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+  } while (0)
+#define DPST_CUFFT(call)                                                                         \
+  do {                                                                                           \
+    cufftResult r_ = (call);                                                                     \
+    if (r_ != CUFFT_SUCCESS)                                                                     \
+      throw Error(r_ == CUFFT_ALLOC_FAILED ? DPST_ERR_ALLOC : DPST_ERR_CUDA,                     \
+                  std::string(#call) + ": cuFFT error " + std::to_string((int)r_));            \
+  } while (0)
+
+static thread_local std::string g_last_error;
+
+// ---- device memory owned by the engine ---------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void alloc(size_t b) {
+    release();
+    if (b == 0) return;
+    DPST_CUDA(cudaMalloc(&p, b));
+    bytes = b;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+template <typename T>
+static void upload(DevBuf &b, const std::vector<T> &v) {
+  b.alloc(v.size() * sizeof(T));
+  if (!v.empty()) DPST_CUDA(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+// ---- host-side set-up arithmetic ----------------------------------------------
+// Clenshaw-Curtis nodes and weights (Chebyshev.py:4-38 for the z grid,
+// Quadrature.cpp:11-46 for the kernel normalisation; same arithmetic).
+static void clencurt(int Np1, double a, double b, std::vector<double> &x, std::vector<double> &w) {
+  const int N = Np1 - 1;
+  const double H = (b - a) / 2.0, bpad2 = (b + a) / 2.0;
+  x.assign(Np1, 0.0);
+  w.assign(Np1, 0.0);
+  for (int i = 0; i < Np1; ++i) x[i] = H * std::cos(M_PI * i / N) + bpad2;
+  double w1;
+  int end;
+  if (N % 2) { w1 = H / (N * N); end = (N - 1) / 2 + 1; }
+  else { w1 = H / (N * N - 1.0); end = N / 2; }
+  w[0] = w1;
+  w[N] = w1;
+  std::vector<double> v(N > 1 ? N - 1 : 0, 1.0);
+  for (int k = 1; k < end; ++k)
+    for (int ii = 1; ii < N; ++ii) v[ii - 1] -= 2 * std::cos(2.0 * k * M_PI * ii / N) / (4.0 * k * k - 1.0);
+  if (N % 2 == 0)
+    for (int ii = 1; ii < N; ++ii) v[ii - 1] -= std::cos(N * M_PI * ii / N) / (N * N - 1.0);
+  for (int ii = 1; ii < N; ++ii) w[ii] = 2 * H * v[ii - 1] / N;
+}
+
+static double es_norm(double beta, double alpha) {
+  std::vector<double> x, w;
+  clencurt(1000, -alpha, alpha, x, w);
+  double s = 0.0;
+  for (int j = 0; j < 1000; ++j) s += std::exp(beta * (std::sqrt(1 - x[j] * x[j] / (alpha * alpha)) - 1)) * w[j];
+  return s;
+}
+
+// ParticleList.cpp:260-265 (complex principal branches)
+static double dipole_threshold(double bw, double alpha) {
+  typedef std::complex<double> C;
+  C s = std::sqrt(C(-12 * bw * bw + 81, 0.0));
+  C z = (C(8 * bw * bw, 0.0) + 12.0 * s - 108.0) * bw;
+  C t = 6.0 * std::pow(z, 1.0 / 3.0) / bw + 24.0 * bw * std::pow(z, -1.0 / 3.0) + 12.0;
+  return (std::sqrt(t) * alpha / 6.0).real();
+}
+
+static int cround(double v) { return (int)std::floor(v + 0.5); }
+
+struct KernelHost {
+  KernelDesc d;
+  std::vector<double> zext, wext;
+};
+
+// Extended z grid for one kernel (ParticleList.cpp:419-451).
+static KernelHost make_kernel(int w, double beta, double alpha, bool dipole, double hx, double hy, int nx,
+                              int ny, const std::vector<double> &zG, const std::vector<double> &zW,
+                              const char *what) {
+  KernelHost k;
+  KernelDesc &d = k.d;
+  memset(&d, 0, sizeof(d));
+  if (!(alpha > 0) || !(beta > 0) || w < 1)
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": w, beta and alpha must be positive");
+  d.beta = beta;
+  d.alpha = alpha;
+  d.alpha2 = alpha * alpha;
+  d.norm = es_norm(beta, alpha);
+  d.inv_norm3 = 1.0 / (d.norm * d.norm * d.norm);
+  d.thr = dipole ? dipole_threshold(beta, alpha) : alpha;
+  if (!(d.thr > 0) || !(d.thr <= alpha))
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": kernel threshold is not in (0, alpha]");
+  d.wx = cround(2 * d.thr / hx);
+  d.wy = cround(2 * d.thr / hy);
+  if (d.wx < 1 || d.wy < 1 || d.wx > nx || d.wy > ny)
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": kernel support does not fit the grid");
+  d.evenx = 1 - (d.wx % 2);
+  d.eveny = 1 - (d.wy % 2);
+  d.nxeff = nx + d.wx + (d.wx % 2);
+  d.nyeff = ny + d.wy + (d.wy % 2);
+  d.lend = (d.nxeff - nx) / 2;
+  d.bend = (d.nyeff - ny) / 2;
+  const int nz = (int)zG.size();
+  int up = 0, down = 0;
+  for (int i = 1; i < nz && zG[0] - zG[i] <= d.thr; ++i) up++;
+  for (int i = nz - 2; i >= 0 && zG[i] - zG[nz - 1] <= d.thr; --i) down++;
+  if (up != down)
+    throw Error(DPST_ERR_UNSUPPORTED,
+                std::string(what) + ": a Chebyshev node lies exactly at the kernel threshold from one wall "
+                "but not the other (asymmetric ghost extension; the reference overruns its grid here)");
+  if (up >= nz - 1)
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": kernel wider than the z domain");
+  d.dend = up;
+  d.nzeff = nz + up + down;
+  k.zext.assign(d.nzeff, 0.0);
+  k.wext.assign(d.nzeff, 0.0);
+  for (int i = up; i < d.nzeff - down; ++i) {
+    k.zext[i] = zG[i - up];
+    k.wext[i] = zW[i - up];
+  }
+  int j = 0;
+  for (int i = up; i > 0; --i, ++j) {
+    k.zext[j] = 2.0 * zG[0] - zG[i];
+    k.wext[j] = zW[i];
+  }
+  j = d.nzeff - down;
+  for (int i = nz - 2; i > nz - 2 - down; --i, ++j) {
+    k.zext[j] = -1.0 * zG[i];
+    k.wext[j] = zW[i];
+  }
+  // longest possible window: points within a closed interval of length 2 thr
+  int wmax = 1;
+  for (int a = 0; a < d.nzeff; ++a) {
+    int c = 0;
+    for (int b = a; b < d.nzeff && k.zext[a] - k.zext[b] <= 2 * d.thr * (1 + 1e-12); ++b) c++;
+    wmax = std::max(wmax, c);
+  }
+  d.wz_max = wmax + 1;
+  return k;
+}
+
+// ---- the engine -----------------------------------------------------------------
+struct EngineBase {
+  virtual ~EngineBase() {}
+  virtual void set_positions(const void *pos, int dtype, cudaStream_t s) = 0;
+  virtual void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
+  virtual void info(dpst_info *o) const = 0;
+  virtual void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) = 0;
+  virtual void velocity_grid(void *out, cudaStream_t s) = 0;
+  float *stage_ms = nullptr;  // set by dpst_mdot_timed for one call
+  int device = 0;
+  int64_t N = 0;
+  dpst_params p;
+};
+
+template <typename R>
+struct Engine : EngineBase {
+  typedef typename std::conditional<sizeof(R) == 8, cufftDoubleComplex, cufftComplex>::type CR;
+  int nx, ny, nz, nxh, nsm;
+  int64_t nk;
+  double hx, hy, Lz, H;
+  KernelHost km, kd;
+  GridArgs g;
+  KsArgs ks;
+  // device buffers
+  DevBuf grid, spec, corr, scratch, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
+  DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g;
+  DevBuf pos64, flags;
+  DevBuf st_m[8], st_d[8];
+  DevBuf gh_m[2], gh_d[2];
+  DevBuf hF, hT, hV, hW;  // staging for the host-array entry points
+  Stencils<R> stm, std_;
+  Ghosts<R> ghm, ghd;
+  int reach_m[2], reach_d[2];
+  bool positioned = false;
+  int64_t bvp_threads = 0;
+  cufftHandle plan_f = 0, plan_b = 0;
+  bool plans = false;
+
+  Engine(const dpst_params &prm, int64_t n, int dev) {
+    p = prm;
+    N = n;
+    device = dev;
+    DPST_CUDA(cudaSetDevice(dev));
+    DPST_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    nx = p.nx; ny = p.ny; nz = p.nz;
+    nxh = nx / 2 + 1;
+    nk = (int64_t)ny * nxh;
+    hx = p.Lx / nx;
+    hy = p.Ly / ny;
+    Lz = p.zmax - p.zmin;
+    H = Lz / 2;
+    // Chebyshev grid on [0, Lz], descending (Chebyshev.py:4-38, FCM.py:207)
+    std::vector<double> zG, zW;
+    clencurt(nz, 0.0, Lz, zG, zW);
+    km = make_kernel(p.w, p.beta, p.alpha, false, hx, hy, nx, ny, zG, zW, "monopole kernel");
+    if (p.has_torque) kd = make_kernel(p.w_d, p.beta_d, p.alpha_d, true, hx, hy, nx, ny, zG, zW, "dipole kernel");
+    km.d.zext_off = 0;
+    kd.d.zext_off = (int)km.zext.size();
+    std::vector<double> ze = km.zext, we = km.wext;
+    ze.insert(ze.end(), kd.zext.begin(), kd.zext.end());
+    we.insert(we.end(), kd.wext.begin(), kd.wext.end());
+    upload(zext, ze);
+    upload(wext, we);
+    upload(zn, zG);
+    // grid arguments + BC sets (FCM.py:215-248)
+    memset(&g, 0, sizeof(g));
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.hx = hx; g.hy = hy; g.Lx = p.Lx; g.Ly = p.Ly; g.Lz = Lz;
+    if (p.mode == DPST_MODE_BOTTOM) {
+      g.bcA.bot_active = 1; g.bcA.s_bot = -1.0;
+      g.bcB.bot_active = 1; g.bcB.s_bot = 1.0;
+    } else if (p.mode == DPST_MODE_SLIT) {
+      g.bcA.bot_active = g.bcA.top_active = 1; g.bcA.s_bot = g.bcA.s_top = -1.0;
+      g.bcB.bot_active = g.bcB.top_active = 1; g.bcB.s_bot = g.bcB.s_top = 1.0;
+    }
+    // wavenumbers (Solvers.py:292-297)
+    std::vector<double> kx(nx), ky(ny);
+    for (int i = 0; i < nx; ++i) {
+      int n = (i <= nx / 2) ? i : i - nx;
+      kx[i] = 2 * M_PI * (double)n / p.Lx;
+    }
+    for (int i = 0; i < ny; ++i) {
+      int n = (i <= ny / 2) ? i : i - ny;
+      ky[i] = 2 * M_PI * (double)n / p.Ly;
+    }
+    upload(kvx, kx);
+    upload(kvy, ky);
+    // integration matrix bands (Chebyshev.py:119-160), H-scaled
+    std::vector<double> bandv(5 * nz, 0.0);
+    double *s0 = &bandv[0], *sp2 = &bandv[nz], *sm2 = &bandv[2 * nz], *fm1 = &bandv[3 * nz],
+           *fp1 = &bandv[4 * nz];
+    const double H2 = H * H;
+    for (int r = 0; r < nz; ++r) {
+      double c0v, cp2v;
+      if (r == 0) { c0v = 0; cp2v = 0; }
+      else if (r == 1) { c0v = -0.125; cp2v = 0.125; }
+      else if (r == 2) { c0v = -1. / 8. - 1. / 24.; cp2v = 1. / 24.; }
+      else {
+        double jj = r;
+        c0v = -1 / (2 * jj * (2 * jj - 2)) - 1 / (2 * jj * (2 * jj + 2)) * (r < nz - 1 ? 1.0 : 0.0);
+        cp2v = 1 / (2 * jj * (2 * jj + 2)) * (r < nz - 2 ? 1.0 : 0.0);
+      }
+      s0[r] = H2 * c0v;
+      sp2[r] = H2 * cp2v;
+      if (r >= 2) {
+        double cm2v = (r == 2) ? 0.25 : 1 / (2.0 * r * (2.0 * r - 2));
+        sm2[r] = H2 * cm2v;
+      }
+      if (r >= 1) fm1[r] = H * ((r == 1) ? 1.0 : 1 / (2.0 * r));
+      double cp1v = (r == 0) ? 0.0 : (r == 1) ? -0.5 : -1 / (2.0 * r) * (r < nz - 1 ? 1.0 : 0.0);
+      fp1[r] = H * cp1v;
+    }
+    upload(bands, bandv);
+    // BC rows (Solvers.py:603-643)
+    const int N2 = nz + 2;
+    std::vector<double> bc(4 * N2, 0.0);
+    double *R1 = &bc[0], *R2 = &bc[N2], *L1 = &bc[2 * N2], *L2 = &bc[3 * N2];
+    {
+      const int Nn = nz;
+      R1[Nn + 1] = 1; R2[Nn] = 1; R1[0] = 1; R1[2] = -1.0 / 2;
+      R2[Nn + 1] += 1; R2[1] = -1.0 / 8; R2[3] = 1.0 / 8;
+      R1[1] += 1.0 / 4; R1[3] -= 1.0 / 4; R2[0] += 1.0 / 4; R2[2] -= (1.0 / 8 + 1.0 / 24);
+      R2[4] += 1.0 / 24;
+      L1[Nn + 1] = 1; L2[Nn] = -1; L1[0] = -1; L1[2] = 1.0 / 2;
+      L2[Nn + 1] += 1; L2[1] = -1.0 / 8; L2[3] = 1.0 / 8;
+      L1[1] += 1.0 / 4; L1[3] -= 1.0 / 4; L2[0] -= 1.0 / 4; L2[2] += 1.0 / 8 + 1.0 / 24;
+      L2[4] -= 1.0 / 24;
+      for (int jj = 3; jj < Nn; ++jj) {
+        double sg = (jj % 2) ? -1.0 : 1.0;
+        double a1 = 1.0 / (2 * jj), b1 = 1.0 / (2 * jj) * 1.0 / (2 * jj - 2), c1 = 1.0 / (2 * jj) * 1.0 / (2 * jj + 2);
+        R1[jj - 1] += a1;
+        L1[jj - 1] += sg / (2 * jj);
+        if (jj < Nn - 1) { R1[jj + 1] -= a1; L1[jj + 1] -= sg / (2 * jj); }
+        R2[jj - 2] += b1;
+        L2[jj - 2] -= b1 * sg;
+        if (jj < Nn - 2) { R2[jj + 2] += c1; L2[jj + 2] -= c1 * sg; }
+        double m = b1 + (jj < Nn - 1 ? c1 : 0.0);
+        R2[jj] -= m;
+        L2[jj] += m * sg;
+      }
+    }
+    upload(bcrows, bc);
+    // k = 0 velocity correction rows and Gi (Solvers.py:499-504, 582-587)
+    std::vector<double> k0r(2 * nz, 0.0);
+    double k0gi[4] = {0, 0, 0, 0};
+    if (p.mode != DPST_MODE_NOWALL) {
+      const double *top = (p.mode == DPST_MODE_BOTTOM) ? R1 : R2;
+      for (int j = 0; j < nz; ++j) { k0r[j] = top[j]; k0r[nz + j] = L2[j]; }
+      double D00 = -top[nz], D01 = -top[nz + 1], D10 = -L2[nz], D11 = -L2[nz + 1];
+      double det = 1.0 / (D00 * D11 - D01 * D10);
+      k0gi[0] = det * D11; k0gi[1] = det * -D01; k0gi[2] = det * -D10; k0gi[3] = det * D00;
+    }
+    upload(k0rows, k0r);
+    // DCT-I matrices (Transform.cpp:107-304): forward = Chebyshev
+    // coefficients from node values, inverse = node values from coefficients
+    std::vector<double> tf((size_t)nz * nz), ti((size_t)nz * nz);
+    const int Nm = nz - 1, Nu = 2 * Nm;
+    for (int j = 0; j < nz; ++j)
+      for (int m = 0; m < nz; ++m) {
+        int r = (int)(((int64_t)j * m) % Nu);
+        double c = std::cos(M_PI * (double)r / (double)Nm);
+        double wj = (j == 0 || j == Nm) ? 1.0 : 2.0, vm = (m == 0 || m == Nm) ? 1.0 : 2.0;
+        tf[(size_t)j * nz + m] = wj * vm * c / Nu;
+        ti[(size_t)m * nz + j] = c;
+      }
+    std::vector<R> tfr(tf.begin(), tf.end()), tir(ti.begin(), ti.end());
+    upload(Tf, tfr);
+    upload(Ti, tir);
+    // per-wavenumber factors
+    fac_m.alloc(sizeof(double) * nz * nk);
+    fac_i.alloc(sizeof(double) * (nz + 1) * nk);
+    fac_d.alloc(sizeof(double) * nz * nk);
+    fac_a0.alloc(sizeof(double) * nz * nk);
+    fac_a1.alloc(sizeof(double) * nz * nk);
+    fac_c0.alloc(sizeof(double) * nz * nk);
+    fac_c1.alloc(sizeof(double) * nz * nk);
+    fac_g.alloc(sizeof(double) * 4 * nk);
+    memset(&ks, 0, sizeof(ks));
+    ks.nx = nx; ks.ny = ny; ks.nz = nz; ks.nxh = nxh; ks.nk = nk;
+    ks.H = H; ks.eta = p.viscosity; ks.Lz = Lz;
+    ks.mode = p.mode;
+    ks.kvx = kvx.as<double>(); ks.kvy = kvy.as<double>(); ks.zn = zn.as<double>();
+    const double *bd = bands.as<double>();
+    ks.s0 = bd; ks.sp2 = bd + nz; ks.sm2 = bd + 2 * nz; ks.fm1 = bd + 3 * nz; ks.fp1 = bd + 4 * nz;
+    ks.se0 = H2; ks.se1 = H2; ks.fe = H;
+    const double *bcd = bcrows.as<double>();
+    ks.bcr1 = bcd; ks.bcr2 = bcd + N2; ks.bcl1 = bcd + 2 * N2; ks.bcl2 = bcd + 3 * N2;
+    ks.mfac = fac_m.as<double>(); ks.invb = fac_i.as<double>(); ks.dp2 = fac_d.as<double>();
+    ks.ab0 = fac_a0.as<double>(); ks.ab1 = fac_a1.as<double>();
+    ks.c0 = fac_c0.as<double>(); ks.c1 = fac_c1.as<double>(); ks.ginv = fac_g.as<double>();
+    ks.k0c0 = k0rows.as<double>(); ks.k0c1 = k0rows.as<double>() + nz;
+    for (int q = 0; q < 4; ++q) ks.k0gi[q] = k0gi[q];
+    launch_bvp_factors(ks, 0);
+    DPST_CUDA(cudaGetLastError());
+    // grids, spectrum, correction coefficients, BVP scratch
+    grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
+    spec.alloc(sizeof(CR) * 3 * (size_t)nz * nk);
+    if (p.mode != DPST_MODE_NOWALL) corr.alloc(sizeof(double2) * 16 * (size_t)nk);
+    bvp_threads = (int64_t)nsm * 64;
+    scratch.alloc(sizeof(double2) * 3 * (size_t)(nz + 2) * bvp_threads);
+    // particle buffers
+    pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
+    flags.alloc(sizeof(int) * 8);
+    alloc_stencils(km.d, false, st_m, stm);
+    if (p.has_torque) alloc_stencils(kd.d, true, st_d, std_);
+    memset(&ghm, 0, sizeof(ghm));
+    memset(&ghd, 0, sizeof(ghd));
+    // FFT plans: batched 2-D over (y, x) for each (component, z) plane
+    int n2[2] = {ny, nx};
+    int inem[2] = {ny, nx}, onem[2] = {ny, nxh};
+    const int batch = 3 * nz;
+    DPST_CUFFT(cufftPlanMany(&plan_f, 2, n2, inem, 1, ny * nx, onem, 1, (int)nk,
+                             sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, batch));
+    DPST_CUFFT(cufftPlanMany(&plan_b, 2, n2, onem, 1, (int)nk, inem, 1, ny * nx,
+                             sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, batch));
+    plans = true;
+    DPST_CUDA(cudaDeviceSynchronize());
+  }
+
+  ~Engine() override {
+    cudaSetDevice(device);
+    cudaDeviceSynchronize();
+    if (have_events)
+      for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+    if (plans) {
+      cufftDestroy(plan_f);
+      cufftDestroy(plan_b);
+    }
+  }
+
+  void alloc_stencils(const KernelDesc &d, bool dip, DevBuf *b, Stencils<R> &s) {
+    const size_t n = (size_t)std::max<int64_t>(N, 1);
+    b[0].alloc(sizeof(int4) * n);
+    b[1].alloc(sizeof(R) * n * d.wx);
+    b[2].alloc(sizeof(R) * n * d.wy);
+    b[3].alloc(sizeof(R) * n * d.wz_max);
+    b[4].alloc(sizeof(R) * n * d.wz_max);
+    if (dip) {
+      b[5].alloc(sizeof(R) * n * d.wx);
+      b[6].alloc(sizeof(R) * n * d.wy);
+      b[7].alloc(sizeof(R) * n * d.wz_max);
+    }
+    s.cell = b[0].as<int4>();
+    s.phx = b[1].as<R>();
+    s.phy = b[2].as<R>();
+    s.phz = b[3].as<R>();
+    s.phzw = b[4].as<R>();
+    s.dphx = dip ? b[5].as<R>() : nullptr;
+    s.dphy = dip ? b[6].as<R>() : nullptr;
+    s.dphz = dip ? b[7].as<R>() : nullptr;
+    s.dphzw = nullptr;
+    if (dip) {
+      dphzw_buf.alloc(sizeof(R) * n * d.wz_max);
+      s.dphzw = dphzw_buf.as<R>();
+    }
+  }
+  DevBuf dphzw_buf;
+
+  // Ghost layers at open z ends that some particle reaches (see Ghosts).
+  void setup_ghosts(const KernelDesc &d, const ZEnds &ends, const int reach[2], DevBuf *b, Ghosts<R> &gh) {
+    const size_t lev = (size_t)d.nyeff * d.nxeff * 3;
+    gh.top = gh.bot = nullptr;
+    gh.ntop = gh.nbot = 0;
+    if (!ends.top_active && reach[0] < d.dend) {
+      gh.ntop = d.dend;
+      if (b[0].bytes < sizeof(R) * lev * d.dend) b[0].alloc(sizeof(R) * lev * d.dend);
+      gh.top = b[0].as<R>();
+    }
+    const int ubeg = d.dend + nz;
+    if (!ends.bot_active && reach[1] >= ubeg) {
+      gh.nbot = d.dend;
+      if (b[1].bytes < sizeof(R) * lev * d.dend) b[1].alloc(sizeof(R) * lev * d.dend);
+      gh.bot = b[1].as<R>();
+    }
+  }
+
+  void set_positions(const void *pos, int dtype, cudaStream_t s) override {
+    if (N == 0) { positioned = true; return; }
+    if (pos == nullptr) throw Error(DPST_ERR_INVALID_ARG, "positions pointer is NULL");
+    convert_positions(pos, dtype, s);
+    int init[8] = {0, INT_MAX, -1, INT_MAX, -1, 0, 0, 0};
+    int *fl = flags.as<int>();
+    DPST_CUDA(cudaMemcpyAsync(fl, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    launch_locate<R>(false, pos64.as<double>(), N, km.d, zext.as<double>(), wext.as<double>(), g, stm, fl,
+                     fl + 1, s);
+    if (p.has_torque)
+      launch_locate<R>(true, pos64.as<double>(), N, kd.d, zext.as<double>(), wext.as<double>(), g, std_, fl,
+                       fl + 3, s);
+    DPST_CUDA(cudaGetLastError());
+    int out[8];
+    DPST_CUDA(cudaMemcpyAsync(out, fl, sizeof(out), cudaMemcpyDeviceToHost, s));
+    DPST_CUDA(cudaStreamSynchronize(s));
+    if (out[0] & 1) {
+      positioned = false;
+      throw Error(DPST_ERR_OUT_OF_DOMAIN, "a particle lies outside [0,Lx]x[0,Ly]x[zmin,zmax] (or is NaN)");
+    }
+    if (out[0] & 2) {
+      positioned = false;
+      throw Error(DPST_ERR_CUDA, "internal: z window longer than its bound");
+    }
+    reach_m[0] = out[1]; reach_m[1] = out[2];
+    reach_d[0] = out[3]; reach_d[1] = out[4];
+    setup_ghosts(km.d, g.bcA, reach_m, gh_m, ghm);
+    if (p.has_torque) setup_ghosts(kd.d, g.bcB, reach_d, gh_d, ghd);
+    positioned = true;
+  }
+
+  void convert_positions(const void *pos, int dtype, cudaStream_t s);
+
+  cudaEvent_t ev[8] = {};
+  bool have_events = false;
+  void mark(int k, cudaStream_t s) {
+    if (!stage_ms) return;
+    if (!have_events) {
+      for (int i = 0; i < 8; ++i) DPST_CUDA(cudaEventCreate(&ev[i]));
+      have_events = true;
+    }
+    DPST_CUDA(cudaEventRecord(ev[k], s));
+  }
+
+  template <typename RF>
+  void spread_stage(const RF *F, const RF *T, cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    R *gr = grid.as<R>();
+    DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
+    for (Ghosts<R> *gh : {&ghm, &ghd}) {
+      const KernelDesc &d = (gh == &ghm) ? km.d : kd.d;
+      const size_t lev = (size_t)d.nyeff * d.nxeff * 3 * sizeof(R);
+      if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
+      if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
+    }
+    launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s);
+    if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s);
+    launch_ghost_fold<R>(ghm.top, ghm.ntop, nx, ny, km.d, s);
+    launch_ghost_fold<R>(ghm.bot, ghm.nbot, nx, ny, km.d, s);
+    if (torque) {
+      launch_ghost_fold<R>(ghd.top, ghd.ntop, nx, ny, kd.d, s);
+      launch_ghost_fold<R>(ghd.bot, ghd.nbot, nx, ny, kd.d, s);
+    }
+    DPST_CUDA(cudaGetLastError());
+  }
+
+  void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (!F || !out) throw Error(DPST_ERR_INVALID_ARG, "F and grid_out must not be NULL");
+    if (dtype == DPST_F64) spread_stage<double>((const double *)F, (const double *)T, s);
+    else if (dtype == DPST_F32) spread_stage<float>((const float *)F, (const float *)T, s);
+    else throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+    DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
+  }
+
+  void velocity_grid(void *out, cudaStream_t s) override {
+    if (!out) throw Error(DPST_ERR_INVALID_ARG, "grid_out must not be NULL");
+    DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
+  }
+
+  template <typename RF>
+  void run(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    R *gr = grid.as<R>();
+    mark(0, s);
+    spread_stage<RF>(F, T, s);
+    mark(1, s);
+    CR *sp = spec.as<CR>();
+    DPST_CUFFT(cufftSetStream(plan_f, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
+    else
+      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
+    mark(2, s);
+    EpiArgs ef;
+    memset(&ef, 0, sizeof(ef));
+    ef.inverse = 0;
+    ef.scale = 1.0;
+    ef.ks = ks;
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s));
+    mark(3, s);
+    launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), scratch.as<double2>(), bvp_threads, s);
+    DPST_CUDA(cudaGetLastError());
+    mark(4, s);
+    EpiArgs eb = ef;
+    eb.inverse = 1;
+    eb.scale = 1.0 / ((double)nx * (double)ny);
+    eb.corr = corr.as<double2>();
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Ti.as<R>(), eb, nsm, s));
+    mark(5, s);
+    DPST_CUFFT(cufftSetStream(plan_b, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
+    else
+      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
+    mark(6, s);
+    launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s);
+    if (p.has_torque && W != nullptr) {
+      // without torques the reference's torque grid still holds the last
+      // z-derivative spread; with T = NULL it is zero
+      Ghosts<R> gz = ghd;
+      if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
+      launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s);
+    }
+    DPST_CUDA(cudaGetLastError());
+    mark(7, s);
+    if (stage_ms) {
+      DPST_CUDA(cudaEventSynchronize(ev[7]));
+      const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
+      for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
+    }
+  }
+
+  void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (N == 0) return;
+    if (F == nullptr || V == nullptr) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    if (dtype == DPST_F64)
+      run<double>((const double *)F, (const double *)T, (double *)V, (double *)W, s);
+    else if (dtype == DPST_F32)
+      run<float>((const float *)F, (const float *)T, (float *)V, (float *)W, s);
+    else
+      throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+  }
+
+  void info(dpst_info *o) const override {
+    memset(o, 0, sizeof(*o));
+    o->nxh = nxh;
+    o->n_modes = (int)nk;
+    o->nzeff_m = km.d.nzeff;
+    o->nzeff_d = p.has_torque ? kd.d.nzeff : 0;
+    o->ghost_m = km.d.dend;
+    o->ghost_d = p.has_torque ? kd.d.dend : 0;
+    o->wz_max_m = km.d.wz_max;
+    o->wz_max_d = p.has_torque ? kd.d.wz_max : 0;
+    o->thr_m = km.d.thr;
+    o->thr_d = p.has_torque ? kd.d.thr : 0;
+    o->norm_m = km.d.norm;
+    o->norm_d = p.has_torque ? kd.d.norm : 0;
+    o->n_particles = N;
+    int64_t b = 0;
+    const DevBuf *all[] = {&grid, &spec, &corr, &scratch, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
+                           &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1,
+                           &fac_g, &pos64, &flags, &dphzw_buf};
+    for (const DevBuf *d : all) b += d->bytes;
+    for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
+    for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;
+    o->device_bytes = b;
+  }
+};
+
+// positions -> FP64 [N][3] with z relative to zmin
+template <typename RP>
+__global__ void k_prep_pos(const RP *pos, int64_t N, double zmin, double *out) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  out[3 * p] = (double)pos[3 * p];
+  out[3 * p + 1] = (double)pos[3 * p + 1];
+  out[3 * p + 2] = (double)pos[3 * p + 2] - zmin;
+}
+
+template <typename R>
+void Engine<R>::convert_positions(const void *pos, int dtype, cudaStream_t s) {
+  int bs = 256;
+  int64_t nb = (N + bs - 1) / bs;
+  if (dtype == DPST_F64) k_prep_pos<double><<<nb, bs, 0, s>>>((const double *)pos, N, p.zmin, pos64.as<double>());
+  else if (dtype == DPST_F32) k_prep_pos<float><<<nb, bs, 0, s>>>((const float *)pos, N, p.zmin, pos64.as<double>());
+  else throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+  DPST_CUDA(cudaGetLastError());
+}
+
+static void validate(const dpst_params *p, int64_t n) {
+  if (!p) throw Error(DPST_ERR_INVALID_ARG, "params is NULL");
+  if (n < 0) throw Error(DPST_ERR_INVALID_ARG, "n_particles < 0");
+  if (p->mode < 0 || p->mode > 2) throw Error(DPST_ERR_INVALID_ARG, "mode must be NOWALL, BOTTOM or SLIT");
+  if (p->nx < 4 || p->ny < 4) throw Error(DPST_ERR_INVALID_ARG, "nx and ny must be >= 4");
+  if (p->nz < 5) throw Error(DPST_ERR_INVALID_ARG, "nz must be >= 5");
+  if (p->nz > 128) throw Error(DPST_ERR_UNSUPPORTED, "nz > 128 is not supported yet");
+  if ((int64_t)p->ny * (p->nx / 2 + 1) * 3 * p->nz > INT_MAX)
+    throw Error(DPST_ERR_UNSUPPORTED, "grid too large for one FFT plan");
+  if (!(p->Lx > 0) || !(p->Ly > 0)) throw Error(DPST_ERR_INVALID_ARG, "Lx and Ly must be positive");
+  if (!(p->zmax > p->zmin)) throw Error(DPST_ERR_INVALID_ARG, "zmax must exceed zmin");
+  if (!(p->viscosity > 0)) throw Error(DPST_ERR_INVALID_ARG, "viscosity must be positive");
+  if (p->precision != DPST_PREC_FP64 && p->precision != DPST_PREC_MIXED)
+    throw Error(DPST_ERR_INVALID_ARG, "precision must be DPST_PREC_FP64 or DPST_PREC_MIXED");
+}
+
+}  // namespace dpst
+
+struct dpst_engine {
+  std::unique_ptr<dpst::EngineBase> e;
+  // device staging for the host-array entry points
+  void *dpos = nullptr, *dF = nullptr, *dT = nullptr, *dV = nullptr, *dW = nullptr;
+  ~dpst_engine() {
+    for (void *q : {dpos, dF, dT, dV, dW})
+      if (q) cudaFree(q);
+  }
+};
+
+using dpst::Error;
+
+template <typename Fn>
+static int guarded(Fn &&fn) {
+  try {
+    fn();
+    dpst::g_last_error.clear();
+    return DPST_OK;
+  } catch (const Error &e) {
+    dpst::g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    dpst::g_last_error = "host allocation failed";
+    return DPST_ERR_ALLOC;
+  } catch (const std::exception &e) {
+    dpst::g_last_error = e.what();
+    return DPST_ERR_CUDA;
+  } catch (...) {
+    dpst::g_last_error = "unknown error";
+    return DPST_ERR_CUDA;
+  }
+}
+
+extern "C" {
+
+const char *dpst_version(void) { return "dpstokes_gb300 0.1"; }
+
+const char *dpst_last_error(void) { return dpst::g_last_error.c_str(); }
+
+int dpst_create(const dpst_params *p, int64_t n_particles, int device, dpst_handle *out) {
+  return guarded([&] {
+    if (!out) throw Error(DPST_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    dpst::validate(p, n_particles);
+    std::unique_ptr<dpst_engine> h(new dpst_engine());
+    if (p->precision == DPST_PREC_FP64) h->e.reset(new dpst::Engine<double>(*p, n_particles, device));
+    else h->e.reset(new dpst::Engine<float>(*p, n_particles, device));
+    *out = h.release();
+  });
+}
+
+int dpst_destroy(dpst_handle h) {
+  return guarded([&] { delete h; });
+}
+
+int dpst_set_positions(dpst_handle h, const void *pos, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->set_positions(pos, dtype, (cudaStream_t)stream);
+  });
+}
+
+int dpst_mdot(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
+  });
+}
+
+static size_t elem_size(int dtype) {
+  if (dtype == DPST_F64) return 8;
+  if (dtype == DPST_F32) return 4;
+  throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+}
+
+int dpst_set_positions_host(dpst_handle h, const void *pos, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    if (!pos) throw Error(DPST_ERR_INVALID_ARG, "positions pointer is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    const size_t bytes = 3 * (size_t)h->e->N * 8;
+    if (!h->dpos && bytes) DPST_CUDA(cudaMalloc(&h->dpos, bytes));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t b = 3 * (size_t)h->e->N * elem_size(dtype);
+    if (b) DPST_CUDA(cudaMemcpyAsync(h->dpos, pos, b, cudaMemcpyHostToDevice, s));
+    h->e->set_positions(h->dpos, dtype, s);
+  });
+}
+
+int dpst_mdot_host(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    if (!F || !V) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    const size_t b = 3 * (size_t)h->e->N * elem_size(dtype);
+    const size_t cap = 3 * (size_t)h->e->N * 8;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cap) {
+      for (void **q : {&h->dF, &h->dT, &h->dV, &h->dW})
+        if (!*q) DPST_CUDA(cudaMalloc(q, cap));
+      DPST_CUDA(cudaMemcpyAsync(h->dF, F, b, cudaMemcpyHostToDevice, s));
+      if (T) DPST_CUDA(cudaMemcpyAsync(h->dT, T, b, cudaMemcpyHostToDevice, s));
+    }
+    h->e->mdot(h->dF, T ? h->dT : nullptr, h->dV, W ? h->dW : nullptr, dtype, s);
+    if (cap) {
+      DPST_CUDA(cudaMemcpyAsync(V, h->dV, b, cudaMemcpyDeviceToHost, s));
+      if (W) DPST_CUDA(cudaMemcpyAsync(W, h->dW, b, cudaMemcpyDeviceToHost, s));
+    }
+    DPST_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int dpst_spread_grid(dpst_handle h, const void *F, const void *T, int dtype, void *grid_out, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->spread_grid(F, T, dtype, grid_out, (cudaStream_t)stream);
+  });
+}
+
+int dpst_velocity_grid(dpst_handle h, void *grid_out, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->velocity_grid(grid_out, (cudaStream_t)stream);
+  });
+}
+
+int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype, void *stream,
+                    float *stage_ms) {
+  return guarded([&] {
+    if (!h || !stage_ms) throw Error(DPST_ERR_INVALID_ARG, "NULL argument");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->stage_ms = stage_ms;
+    try {
+      h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
+    } catch (...) {
+      h->e->stage_ms = nullptr;
+      throw;
+    }
+    h->e->stage_ms = nullptr;
+  });
+}
+
+int dpst_get_info(dpst_handle h, dpst_info *out) {
+  return guarded([&] {
+    if (!h || !out) throw Error(DPST_ERR_INVALID_ARG, "NULL argument");
+    h->e->info(out);
+  });
+}
+
+}  // extern "C"

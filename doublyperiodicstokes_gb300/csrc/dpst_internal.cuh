@@ -1,0 +1,97 @@
+// Internal types shared by the kernels (dpst_kernels.cu, dpst_kspace.cu) and
+// the engine / C ABI (dpst_engine.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dpst {
+
+// One ES kernel (monopole or dipole) as laid out on the grid.  Mirrors the
+// ParticleList/Grid state of the reference for one particle type
+// (ParticleList.cpp:211-276 normalisation and threshold, :394-451 extended z
+// grid, Grid.h Nxeff/Nyeff).
+struct KernelDesc {
+  int wx, wy;         // stencil widths = round(2 thr / h)
+  int evenx, eveny;   // 1 for even widths (stencil start offset)
+  int nxeff, nyeff;   // extended x-y sizes of the reference grid (ghost buffers)
+  int lend, bend;     // x / y ghost widths
+  int nzeff, dend;    // extended z grid size, ghost layers per end
+  int wz_max;         // upper bound of the z window length
+  int zext_off;       // offset of this kernel's extended z grid in the tables
+  double beta, alpha, alpha2, thr, inv_norm3, norm;
+};
+
+// Boundary handling of the z ends for one BC set (reference BCs / BCst_z,
+// FCM.py:215-248): an active end folds ghost data back with sign s and
+// multiplies the boundary node by (1+s) (BoundaryConditions.h:284-341,
+// 650-729); an inactive end ('none') drops spread data and leaves ghost
+// layers untouched.
+struct ZEnds {
+  int top_active, bot_active;  // top = z max (extended index 0)
+  double s_top, s_bot;
+};
+
+// Everything a particle kernel needs (passed by value).
+struct GridArgs {
+  int nx, ny, nz;
+  double hx, hy, Lx, Ly, Lz;
+  ZEnds bcA;  // BCs  : forces, x/y torque derivatives
+  ZEnds bcB;  // BCst : z torque derivative
+};
+
+// Per-particle stencil data for one kernel type, structure of arrays.
+template <typename R>
+struct Stencils {
+  int4 *cell;   // (xclose, yclose, indl, wz)
+  R *phx;       // [N][wx]  phi(x offsets)
+  R *phy;       // [N][wy]
+  R *phz;       // [N][wz_max] phi(z offsets) / norm^3
+  R *phzw;      // [N][wz_max] phz * hx * hy * w_cc(z)  (interpolation weights)
+  R *dphx;      // dipole only: derivative kernels
+  R *dphy;
+  R *dphz;
+  R *dphzw;
+};
+
+// Ghost-layer buffers for open z ends: the reference leaves spread data in
+// the extended grid's ghost layers at 'none' ends and the next interpolation
+// reads it back (Grid::zeroExtGrid only before a spread, Ghostify copies only
+// active ends).  Layout [level][nyeff][nxeff][3]; top levels are extended
+// indices [0, dend), bottom levels [dend+nz, nzeff).
+template <typename R>
+struct Ghosts {
+  R *top;     // nullptr if no particle reaches the top ghost layers
+  R *bot;
+  int ntop;   // number of levels stored (from the layer nearest the node)
+  int nbot;
+};
+
+// Arguments of the wavenumber-space kernels (dpst_kspace.cu).
+struct KsArgs {
+  int nx, ny, nz, nxh;
+  int64_t nk;
+  double H, eta, Lz;
+  int mode;  // 0 open, 1 bottom wall, 2 slit
+  const double *kvx, *kvy;  // wavenumber tables, length nx / ny (reference ordering)
+  const double *zn;         // Chebyshev nodes in [0, Lz], descending (zn[0] = Lz)
+  // SIMat / FIMat bands (H-scaled), per row m
+  const double *s0, *sp2, *sm2, *fm1, *fp1;
+  double se0, se1, fe;
+  // BC rows (length nz + 2 each) of the reference (Solvers.py:603-643)
+  const double *bcr1, *bcr2, *bcl1, *bcl2;
+  // per-mode factors, [index][nk]
+  double *mfac, *invb, *dp2, *ab0, *ab1, *c0, *c1, *ginv;
+  // k = 0 velocity correction: C rows (length nz) and Gi row-major
+  const double *k0c0, *k0c1;
+  double k0gi[4];
+};
+
+// Epilogue of the z-transform GEMM.
+struct EpiArgs {
+  int inverse;
+  double scale;  // 1/(nx ny) for the inverse
+  const double2 *corr;
+  KsArgs ks;
+};
+
+}  // namespace dpst

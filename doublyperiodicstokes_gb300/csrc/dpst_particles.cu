@@ -1,0 +1,499 @@
+// Particle-side kernels: stencil setup, spreading (forces and the torque
+// curl) and interpolation (velocities and velocity gradients), with the
+// reference's ghost fold / ghost copy semantics applied through index maps
+// instead of an extended grid.
+//
+// Reference behaviour restated (source/cpu of stochasticHydroTools/
+// DoublyPeriodicStokes):
+//   stencil            ParticleList.cpp:394-526 (xclose, clamped offsets,
+//                      z window by lower_bound on the descending extended grid)
+//   kernel             ESKernels.h:8-46 (separable: the product of three 1-D
+//                      factors equals exp of the summed exponents)
+//   spread / interp    SpreadInterp.cpp:302-600, SpreadInterp.h:100-212
+//   ghost fold / copy  BoundaryConditions.h:22-731
+//   torque curl        SpreadInterpWrapper.cpp:66-107, FCM.py:362-371,411-426
+#include "dpst_internal.cuh"
+
+namespace dpst {
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ double es1(double x, double beta, double alpha2) {
+  return exp(beta * (sqrt(1.0 - x * x / alpha2) - 1.0));
+}
+
+__device__ __forceinline__ double des1(double x, double beta, double alpha2) {
+  double s = sqrt(1.0 - x * x / alpha2);
+  return -beta * x * exp(beta * (s - 1.0)) / (alpha2 * s);
+}
+
+// ---------------------------------------------------------------------------
+// Stencil setup: one thread per particle.  pos is [N][3] with z already
+// relative to zmin.  Offsets are computed in FP64 exactly as the reference
+// does (same operation order) and clamped to +thr when outside [-thr, thr].
+// err bit 1: particle outside the unit cell; bit 2: z window longer than the
+// allocated stride.  reach[0] = min indl, reach[1] = max indr (extended z).
+// ---------------------------------------------------------------------------
+template <typename R, bool DIPOLE>
+__global__ void k_locate(const double *__restrict__ pos, int64_t N, KernelDesc kd,
+                         const double *__restrict__ zext, const double *__restrict__ wext,
+                         GridArgs g, Stencils<R> st, int *err, int *reach) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+  if (!(x >= 0.0 && x <= g.Lx && y >= 0.0 && y <= g.Ly && z >= 0.0 && z <= g.Lz)) {
+    atomicOr(err, 1);
+    st.cell[p] = make_int4(0, 0, 0, 0);
+    return;
+  }
+  const double thr = kd.thr;
+  int xclose = (int)(x / g.hx);
+  int yclose = (int)(y / g.hy);
+  if ((kd.wx & 1) && (x / g.hx - xclose > 0.5)) xclose += 1;
+  if ((kd.wy & 1) && (y / g.hy - yclose > 0.5)) yclose += 1;
+  for (int i = 0; i < kd.wx; ++i) {
+    double o = ((double)xclose + i - kd.wx / 2 + kd.evenx) * g.hx - x;
+    if (o > thr || o < -thr) o = thr;
+    st.phx[p * kd.wx + i] = (R)es1(o, kd.beta, kd.alpha2);
+    if (DIPOLE) st.dphx[p * kd.wx + i] = (R)des1(o, kd.beta, kd.alpha2);
+  }
+  for (int j = 0; j < kd.wy; ++j) {
+    double o = ((double)yclose + j - kd.wy / 2 + kd.eveny) * g.hy - y;
+    if (thr < o || o < -thr) o = thr;
+    st.phy[p * kd.wy + j] = (R)es1(o, kd.beta, kd.alpha2);
+    if (DIPOLE) st.dphy[p * kd.wy + j] = (R)des1(o, kd.beta, kd.alpha2);
+  }
+  // z window: zext is strictly descending; indl = #{zext > z + thr},
+  // high = #{zext > z - thr}; indr = high - 1 unless zext[high] == z - thr.
+  const double *ze = zext + kd.zext_off;
+  const double *we = wext + kd.zext_off;
+  const int n = kd.nzeff;
+  auto count_greater = [&](double v) {
+    int lo = 0, hi = n;  // first index with ze[idx] <= v
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (ze[mid] > v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+  };
+  int indl = count_greater(z + thr);
+  int indr = count_greater(z - thr);
+  if (indr == n) indr -= 1;
+  else if (z - thr > ze[indr]) indr -= 1;
+  int wz = indr - indl + 1;
+  if (wz > kd.wz_max) {
+    atomicOr(err, 2);
+    st.cell[p] = make_int4(0, 0, 0, 0);
+    return;
+  }
+  if (wz < 1) wz = 0;  // no node within the support: no z contributions
+  st.cell[p] = make_int4(xclose, yclose, indl, wz);
+  if (wz > 0) {
+    atomicMin(&reach[0], indl);
+    atomicMax(&reach[1], indr);
+  }
+  const double hxy = g.hx * g.hy;
+  for (int k = 0; k < kd.wz_max; ++k) {
+    double v = 0.0, dv = 0.0, wgt = 0.0;
+    if (k < wz) {
+      double o = ze[indl + k] - z;
+      if (thr < o || o < -thr) o = thr;
+      v = es1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
+      if (DIPOLE) dv = des1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
+      wgt = hxy * we[indl + k];
+    }
+    st.phz[p * kd.wz_max + k] = (R)v;
+    st.phzw[p * kd.wz_max + k] = (R)(v * wgt);
+    if (DIPOLE) {
+      st.dphz[p * kd.wz_max + k] = (R)dv;
+      st.dphzw[p * kd.wz_max + k] = (R)(dv * wgt);
+    }
+  }
+}
+
+// Where extended z index kk lands on the interior grid under one BC set.
+// Returns the interior index m (descending z, m = 0 at zmax) and the weight
+// (1 interior, s at a folded ghost, 1+s at an active boundary node).  A
+// ghost layer at an inactive end returns m = -1 (top) or -2 (bottom) and its
+// level in the ghost buffer.
+struct ZMap {
+  int m;
+  int level;
+  double wgt;
+};
+
+__device__ __forceinline__ ZMap zmap(int kk, int dend, int nz, const ZEnds &b) {
+  ZMap r;
+  r.level = 0;
+  const int ubeg = dend + nz;
+  if (kk < dend) {
+    if (b.top_active) { r.m = dend - kk; r.wgt = b.s_top; }
+    else { r.m = -1; r.level = kk; r.wgt = 1.0; }
+  } else if (kk >= ubeg) {
+    if (b.bot_active) { r.m = 2 * nz + dend - 2 - kk; r.wgt = b.s_bot; }
+    else { r.m = -2; r.level = kk - ubeg; r.wgt = 1.0; }
+  } else {
+    r.m = kk - dend;
+    r.wgt = 1.0;
+    if (r.m == 0 && b.top_active) r.wgt = 1.0 + b.s_top;
+    if (r.m == nz - 1 && b.bot_active) r.wgt = 1.0 + b.s_bot;
+  }
+  return r;
+}
+
+template <typename R>
+__device__ __forceinline__ void atomic_add(R *a, R v) { atomicAdd(a, v); }
+
+// ---------------------------------------------------------------------------
+// Monopole spread of forces: one thread per (particle, stencil column).
+// grid layout [3][nz][ny][nx].
+// ---------------------------------------------------------------------------
+template <typename R, typename RF>
+__global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd, GridArgs g,
+                              Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+  const int cols = kd.wx * kd.wy;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * cols) return;
+  int64_t p = t / cols;
+  int c = (int)(t - p * cols);
+  int i = c % kd.wx, j = c / kd.wx;
+  int4 cl = st.cell[p];
+  if (cl.w == 0) return;
+  const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
+  const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
+  const int px = wrapi(ox, g.nx), py = wrapi(oy, g.ny);
+  const int ie = ox + kd.lend, je = oy + kd.bend;  // extended-grid column
+  const R f0 = (R)F[3 * p], f1 = (R)F[3 * p + 1], f2 = (R)F[3 * p + 2];
+  const R cxy = st.phx[p * kd.wx + i] * st.phy[p * kd.wy + j];
+  const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+  const int64_t col = (int64_t)py * g.nx + px;
+  for (int k = 0; k < cl.w; ++k) {
+    const R v = cxy * st.phz[p * kd.wz_max + k];
+    ZMap zm = zmap(cl.z + k, kd.dend, g.nz, g.bcA);
+    if (zm.m >= 0) {
+      if (zm.wgt == 0.0) continue;
+      const R a = v * (R)zm.wgt;
+      R *dst = grid + zm.m * plane + col;
+      atomic_add(dst, a * f0);
+      atomic_add(dst + comp, a * f1);
+      atomic_add(dst + 2 * comp, a * f2);
+    } else {
+      R *buf = (zm.m == -1) ? gh.top : gh.bot;
+      if (buf == nullptr || ie < 0 || ie >= kd.nxeff || je < 0 || je >= kd.nyeff) continue;
+      R *dst = buf + (((int64_t)zm.level * kd.nyeff + je) * kd.nxeff + ie) * 3;
+      atomic_add(dst, v * f0);
+      atomic_add(dst + 1, v * f1);
+      atomic_add(dst + 2, v * f2);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dipole spread of the torque curl, f += 1/2 curl(T delta) with derivative
+// kernels: x and y derivative spreads use BC set A, the z derivative spread
+// BC set B (FCM.py:362-371).  Ghost layers at inactive ends of set B keep the
+// raw z-derivative spread (the last spread the reference does on its torque
+// grid before interpolating).
+// ---------------------------------------------------------------------------
+template <typename R, typename RF>
+__global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd, GridArgs g,
+                             Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+  const int cols = kd.wx * kd.wy;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * cols) return;
+  int64_t p = t / cols;
+  int c = (int)(t - p * cols);
+  int i = c % kd.wx, j = c / kd.wx;
+  int4 cl = st.cell[p];
+  if (cl.w == 0) return;
+  const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
+  const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
+  const int px = wrapi(ox, g.nx), py = wrapi(oy, g.ny);
+  const int ie = ox + kd.lend, je = oy + kd.bend;
+  const R tx = (R)T[3 * p], ty = (R)T[3 * p + 1], tz = (R)T[3 * p + 2];
+  const R fx = st.phx[p * kd.wx + i], fy = st.phy[p * kd.wy + j];
+  const R dfx = st.dphx[p * kd.wx + i], dfy = st.dphy[p * kd.wy + j];
+  const R axy = dfx * fy, bxy = fx * dfy, cxy = fx * fy;
+  const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+  const int64_t col = (int64_t)py * g.nx + px;
+  const R half = (R)0.5;
+  for (int k = 0; k < cl.w; ++k) {
+    const R phz = st.phz[p * kd.wz_max + k];
+    const R ax = axy * phz;                          // d/dx kernel
+    const R ay = bxy * phz;                          // d/dy kernel
+    const R az = cxy * st.dphz[p * kd.wz_max + k];   // d/dz kernel
+    const int kk = cl.z + k;
+    ZMap a = zmap(kk, kd.dend, g.nz, g.bcA);
+    ZMap b = zmap(kk, kd.dend, g.nz, g.bcB);
+    if (a.m >= 0 && a.wgt != 0.0) {
+      R *dst = grid + a.m * plane + col;
+      const R wa = (R)a.wgt * half;
+      atomic_add(dst, wa * (ay * tz));                   // addDy: fx += 1/2 Sy[Tz]
+      atomic_add(dst + comp, -wa * (ax * tz));           // addDx: fy -= 1/2 Sx[Tz]
+      atomic_add(dst + 2 * comp, wa * (ax * ty - ay * tx));  // fz += 1/2 Sx[Ty] - 1/2 Sy[Tx]
+    }
+    if (b.m >= 0) {
+      if (b.wgt != 0.0) {
+        R *dst = grid + b.m * plane + col;
+        const R wb = (R)b.wgt * half;
+        atomic_add(dst, -wb * (az * ty));       // addDz: fx -= 1/2 Sz[Ty]
+        atomic_add(dst + comp, wb * (az * tx)); // fy += 1/2 Sz[Tx]
+      }
+    } else {
+      R *buf = (b.m == -1) ? gh.top : gh.bot;
+      if (buf == nullptr || ie < 0 || ie >= kd.nxeff || je < 0 || je >= kd.nyeff) continue;
+      R *dst = buf + (((int64_t)b.level * kd.nyeff + je) * kd.nxeff + ie) * 3;
+      atomic_add(dst, az * tx);
+      atomic_add(dst + 1, az * ty);
+      atomic_add(dst + 2, az * tz);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Periodic x then y fold of the ghost-layer buffers, applied to every stored
+// level exactly as the reference folds its whole extended grid
+// (BoundaryConditions.h:43-84 then 143-184): x ghosts are added into the
+// interior x range for every row (y ghosts included); then y ghost rows are
+// added into interior rows for every column (x ghosts included).  Ghost
+// cells themselves keep their raw values.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_ghost_fold_x(R *buf, int levels, int nx, KernelDesc kd) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t per = (int64_t)kd.nyeff * kd.lend * 3;
+  if (t >= levels * per * 2) return;
+  int side = (int)(t / (levels * per));
+  int64_t r = t - side * levels * per;
+  int d = (int)(r % 3);
+  int64_t q = r / 3;
+  int i = (int)(q % kd.lend);
+  int64_t q2 = q / kd.lend;
+  int j = (int)(q2 % kd.nyeff);
+  int l = (int)(q2 / kd.nyeff);
+  R *row = buf + ((int64_t)l * kd.nyeff + j) * kd.nxeff * 3;
+  int rbeg = kd.nxeff - kd.lend;
+  if (side == 0) row[(i + nx) * 3 + d] += row[i * 3 + d];
+  else row[(rbeg + i - nx) * 3 + d] += row[(rbeg + i) * 3 + d];
+}
+
+template <typename R>
+__global__ void k_ghost_fold_y(R *buf, int levels, int ny, KernelDesc kd) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t per = (int64_t)kd.bend * kd.nxeff * 3;
+  if (t >= levels * per * 2) return;
+  int side = (int)(t / (levels * per));
+  int64_t r = t - side * levels * per;
+  int d = (int)(r % 3);
+  int64_t q = r / 3;
+  int i = (int)(q % kd.nxeff);
+  int64_t q2 = q / kd.nxeff;
+  int j = (int)(q2 % kd.bend);
+  int l = (int)(q2 / kd.bend);
+  R *lev = buf + (int64_t)l * kd.nyeff * kd.nxeff * 3;
+  int tbeg = kd.nyeff - kd.bend;
+  if (side == 0) lev[((int64_t)(j + ny) * kd.nxeff + i) * 3 + d] += lev[((int64_t)j * kd.nxeff + i) * 3 + d];
+  else lev[((int64_t)(tbeg + j - ny) * kd.nxeff + i) * 3 + d] +=
+      lev[((int64_t)(tbeg + j) * kd.nxeff + i) * 3 + d];
+}
+
+// Value of component d at extended z index kk for a particle column, with the
+// reference's ghost copy applied (BoundaryConditions.h:377-731): interior and
+// active-end layers come from the interior grid (periodic in x, y, mirrored
+// with sign at walls, boundary node times 1+s); inactive-end ghost layers come
+// from the ghost buffer at the extended column (ie, je).
+template <typename R>
+__device__ __forceinline__ void grid_value3(const R *__restrict__ grid, const ZMap &zm, int64_t col,
+                                            int64_t plane, int64_t comp, const Ghosts<R> &gh,
+                                            const KernelDesc &kd, int ie, int je, R out[3]) {
+  if (zm.m >= 0) {
+    const R *src = grid + zm.m * plane + col;
+    const R w = (R)zm.wgt;
+    out[0] = w * src[0];
+    out[1] = w * src[comp];
+    out[2] = w * src[2 * comp];
+  } else {
+    const R *buf = (zm.m == -1) ? gh.top : gh.bot;
+    if (buf == nullptr || ie < 0 || ie >= kd.nxeff || je < 0 || je >= kd.nyeff) {
+      out[0] = out[1] = out[2] = (R)0;
+      return;
+    }
+    const R *src = buf + (((int64_t)zm.level * kd.nyeff + je) * kd.nxeff + ie) * 3;
+    out[0] = src[0];
+    out[1] = src[1];
+    out[2] = src[2];
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R warp_sum(R v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Monopole interpolation: one warp per particle, V = sum u * phi * hx hy w_cc.
+// ---------------------------------------------------------------------------
+template <typename R, typename RV>
+__global__ void k_interp_mono(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
+                              Stencils<R> st, Ghosts<R> gh, RV *__restrict__ V) {
+  int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (p >= N) return;
+  int4 cl = st.cell[p];
+  R s0 = 0, s1 = 0, s2 = 0;
+  if (cl.w > 0) {
+    const int cols = kd.wx * kd.wy;
+    const int tot = cols * cl.w;
+    const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+    for (int t = lane; t < tot; t += 32) {
+      int k = t / cols;
+      int c = t - k * cols;
+      int i = c % kd.wx, j = c / kd.wx;
+      const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
+      const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
+      const int64_t col = (int64_t)wrapi(oy, g.ny) * g.nx + wrapi(ox, g.nx);
+      ZMap zm = zmap(cl.z + k, kd.dend, g.nz, g.bcA);
+      R u[3];
+      grid_value3(grid, zm, col, plane, comp, gh, kd, ox + kd.lend, oy + kd.bend, u);
+      const R wgt = st.phx[p * kd.wx + i] * st.phy[p * kd.wy + j] * st.phzw[p * kd.wz_max + k];
+      s0 += u[0] * wgt;
+      s1 += u[1] * wgt;
+      s2 += u[2] * wgt;
+    }
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if (lane == 0) {
+    V[3 * p] = (RV)s0;
+    V[3 * p + 1] = (RV)s1;
+    V[3 * p + 2] = (RV)s2;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dipole interpolation of the velocity gradient with derivative kernels and
+// W = -1/2 curl v (FCM.py:411-426): d/dx, d/dy use BC set A, d/dz set B.
+// ---------------------------------------------------------------------------
+template <typename R, typename RV>
+__global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
+                             Stencils<R> st, Ghosts<R> gh, RV *__restrict__ W) {
+  int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (p >= N) return;
+  int4 cl = st.cell[p];
+  // gradient terms needed for the curl
+  R dyvz = 0, dzvy = 0, dzvx = 0, dxvz = 0, dxvy = 0, dyvx = 0;
+  if (cl.w > 0) {
+    const int cols = kd.wx * kd.wy;
+    const int tot = cols * cl.w;
+    const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+    for (int t = lane; t < tot; t += 32) {
+      int k = t / cols;
+      int c = t - k * cols;
+      int i = c % kd.wx, j = c / kd.wx;
+      const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
+      const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
+      const int64_t col = (int64_t)wrapi(oy, g.ny) * g.nx + wrapi(ox, g.nx);
+      const int kk = cl.z + k;
+      ZMap za = zmap(kk, kd.dend, g.nz, g.bcA);
+      ZMap zb = zmap(kk, kd.dend, g.nz, g.bcB);
+      R ua[3], ub[3];
+      grid_value3(grid, za, col, plane, comp, gh, kd, ox + kd.lend, oy + kd.bend, ua);
+      grid_value3(grid, zb, col, plane, comp, gh, kd, ox + kd.lend, oy + kd.bend, ub);
+      const R fx = st.phx[p * kd.wx + i], fy = st.phy[p * kd.wy + j];
+      const R dfx = st.dphx[p * kd.wx + i], dfy = st.dphy[p * kd.wy + j];
+      const R zw = st.phzw[p * kd.wz_max + k], dzw = st.dphzw[p * kd.wz_max + k];
+      const R wx = dfx * fy * zw, wy = fx * dfy * zw, wz = fx * fy * dzw;
+      dxvy += ua[1] * wx;
+      dxvz += ua[2] * wx;
+      dyvx += ua[0] * wy;
+      dyvz += ua[2] * wy;
+      dzvx += ub[0] * wz;
+      dzvy += ub[1] * wz;
+    }
+  }
+  dyvz = warp_sum(dyvz);
+  dzvy = warp_sum(dzvy);
+  dzvx = warp_sum(dzvx);
+  dxvz = warp_sum(dxvz);
+  dxvy = warp_sum(dxvy);
+  dyvx = warp_sum(dyvx);
+  if (lane == 0) {
+    W[3 * p] = (RV)(-(R)0.5 * (dyvz - dzvy));
+    W[3 * p + 1] = (RV)(-(R)0.5 * (dzvx - dxvz));
+    W[3 * p + 2] = (RV)(-(R)0.5 * (dxvy - dyvx));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+template <typename R>
+void launch_locate(bool dipole, const double *pos, int64_t N, const KernelDesc &kd,
+                   const double *zext, const double *wext, const GridArgs &g, const Stencils<R> &st,
+                   int *err, int *reach, cudaStream_t s) {
+  if (N == 0) return;
+  int bs = 128;
+  int64_t nb = (N + bs - 1) / bs;
+  if (dipole) k_locate<R, true><<<nb, bs, 0, s>>>(pos, N, kd, zext, wext, g, st, err, reach);
+  else k_locate<R, false><<<nb, bs, 0, s>>>(pos, N, kd, zext, wext, g, st, err, reach);
+}
+
+template <typename R, typename RF>
+void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s) {
+  int64_t tot = N * kd.wx * kd.wy;
+  if (tot == 0) return;
+  int bs = 256;
+  int64_t nb = (tot + bs - 1) / bs;
+  if (dipole) k_spread_dip<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh);
+  else k_spread_mono<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh);
+}
+
+template <typename R>
+void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s) {
+  if (buf == nullptr || levels <= 0) return;
+  int bs = 256;
+  int64_t tx = (int64_t)levels * kd.nyeff * kd.lend * 3 * 2;
+  if (tx > 0) k_ghost_fold_x<R><<<(tx + bs - 1) / bs, bs, 0, s>>>(buf, levels, nx, kd);
+  int64_t ty = (int64_t)levels * kd.bend * kd.nxeff * 3 * 2;
+  if (ty > 0) k_ghost_fold_y<R><<<(ty + bs - 1) / bs, bs, 0, s>>>(buf, levels, ny, kd);
+}
+
+template <typename R, typename RV>
+void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s) {
+  if (N == 0) return;
+  int bs = 256;
+  int64_t nb = (N * 32 + bs - 1) / bs;
+  if (dipole) k_interp_dip<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out);
+  else k_interp_mono<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out);
+}
+
+#define DPST_INST(R)                                                                           \
+  template void launch_locate<R>(bool, const double *, int64_t, const KernelDesc &,             \
+                                 const double *, const double *, const GridArgs &,              \
+                                 const Stencils<R> &, int *, int *, cudaStream_t);              \
+  template void launch_ghost_fold<R>(R *, int, int, int, const KernelDesc &, cudaStream_t);     \
+  template void launch_spread<R, float>(bool, const float *, int64_t, const KernelDesc &,      \
+                                        const GridArgs &, const Stencils<R> &, R *,            \
+                                        const Ghosts<R> &, cudaStream_t);                      \
+  template void launch_spread<R, double>(bool, const double *, int64_t, const KernelDesc &,    \
+                                         const GridArgs &, const Stencils<R> &, R *,           \
+                                         const Ghosts<R> &, cudaStream_t);                     \
+  template void launch_interp<R, float>(bool, const R *, int64_t, const KernelDesc &,          \
+                                        const GridArgs &, const Stencils<R> &,                 \
+                                        const Ghosts<R> &, float *, cudaStream_t);             \
+  template void launch_interp<R, double>(bool, const R *, int64_t, const KernelDesc &,         \
+                                         const GridArgs &, const Stencils<R> &,                \
+                                         const Ghosts<R> &, double *, cudaStream_t);
+
+DPST_INST(float)
+DPST_INST(double)
+
+}  // namespace dpst

@@ -1,0 +1,137 @@
+"""Benchmark and parity workloads: explicit grid/kernel parameters and seeded
+synthetic particle inputs for the five configurations the operator is
+measured on, plus helpers for small parity cases.
+
+All inputs are synthetic (no dataset exists for this operator): positions
+uniform in the periodic box and in a z band, forces/torques i.i.d. standard
+normal, drawn from numpy's PCG64 generator with a fixed seed in a fixed order
+(x, y, z, then forces, then torques), so every machine regenerates the same
+arrays.
+"""
+import math
+from dataclasses import dataclass, asdict, replace
+
+import numpy as np
+
+ETA_DEFAULT = 1.0 / (6.0 * math.pi)
+
+
+@dataclass(frozen=True)
+class Workload:
+    """One Mdot configuration.
+
+    domType: 'DP' (open), 'DPBW' (bottom wall at z0), 'DPSC' (walls at z0 and z0+Lz).
+    The Chebyshev interval is [z0, z0+Lz]; particle heights are drawn from
+    [zlo, zhi].  beta = beta_hat * w for each kernel; alpha = w*h/2 (the
+    reference's UseCbeta convention with c(beta) = R/(w h))."""
+    name: str
+    domType: str
+    N: int
+    Lx: float
+    Ly: float
+    nx: int
+    ny: int
+    nz: int
+    z0: float
+    Lz: float
+    zlo: float
+    zhi: float
+    has_torque: bool
+    wm: int = 6
+    betam_hat: float = 1.714
+    wd: int = 6
+    betad_hat: float = 2.2160
+    eta: float = ETA_DEFAULT
+    radius: float = 1.0
+    seed: int = 0
+
+    def oracle_params(self):
+        """Keyword arguments of the oracle's Params (same field meanings)."""
+        return dict(domType=self.domType, Nx=self.nx, Ny=self.ny, Nz=self.nz, Lx=self.Lx,
+                    Ly=self.Ly, Lz=self.Lz, z0=self.z0, eta=self.eta, wm=self.wm,
+                    betam_hat=self.betam_hat, has_torque=self.has_torque, wd=self.wd,
+                    betad_hat=self.betad_hat, radius=self.radius)
+
+    def to_dict(self):
+        return asdict(self)
+
+
+def make_inputs(w: Workload, dtype=np.float64):
+    """Seeded synthetic positions [N,3], forces [N,3], torques [N,3] (or None)."""
+    rng = np.random.default_rng(w.seed)
+    x = rng.uniform(0.0, w.Lx, w.N)
+    y = rng.uniform(0.0, w.Ly, w.N)
+    z = rng.uniform(w.zlo, w.zhi, w.N)
+    X = np.stack([x, y, z], axis=1)
+    F = rng.standard_normal((w.N, 3))
+    T = rng.standard_normal((w.N, 3)) if w.has_torque else None
+    if dtype != np.float64:
+        F = F.astype(dtype)
+        T = T.astype(dtype) if T is not None else None
+    return X, F, T
+
+
+# The five measured configurations (w = 6 everywhere; with torques the
+# reference's w=6 monopole/dipole pair beta_m = 1.3267*6, beta_d = 2.2160*6).
+C0 = Workload("c0_dpbw_n2048", "DPBW", 2048, 128.0, 128.0, 128, 128, 64, 0.0, 20.0, 1.5, 18.5,
+              False, betam_hat=1.714)
+C1 = Workload("c1_dpsc_n16384", "DPSC", 16384, 256.0, 256.0, 256, 256, 96, 0.0, 32.0, 1.5, 30.5,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+C2 = Workload("c2_dp_n65536", "DP", 65536, 512.0, 512.0, 512, 512, 128, -20.5, 41.0, -16.0, 16.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+C3 = Workload("c3_dpbw_n8192", "DPBW", 8192, 192.0, 192.0, 192, 192, 64, 0.0, 24.0, 1.5, 22.5,
+              False, betam_hat=1.714)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3)}
+
+
+def fft_friendly(n):
+    """Smallest integer >= n whose prime factors are all in {2,3,5,7}."""
+    m = int(n)
+    while True:
+        k = m
+        for p in (2, 3, 5, 7):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m += 1
+
+
+def batched_c4(n_systems=256, seed=1000):
+    """The batched bottom-wall set: N_i log-uniform in [64, 4096], box side
+    L_i ~ U[32, 128], n_i = fft_friendly(round(1.55 L_i)), h_i = L_i/n_i,
+    Lz = 20, nz = 64, inputs drawn as for c0 with seed 1000+i."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_systems):
+        N = int(round(math.exp(rng.uniform(math.log(64), math.log(4096)))))
+        L = float(rng.uniform(32.0, 128.0))
+        n = fft_friendly(int(round(1.55 * L)))
+        out.append(Workload("c4_sys%03d" % i, "DPBW", N, L, L, n, n, 64, 0.0, 20.0, 1.5, 18.5,
+                            False, betam_hat=1.714, seed=seed + i))
+    return out
+
+
+def small(name, domType, N, n, nz, Lz, zlo, zhi, has_torque, ny=None, Ly=None, z0=0.0, seed=0):
+    """A small parity case with h = 1 (Lx = nx)."""
+    ny = n if ny is None else ny
+    Ly = float(ny) if Ly is None else Ly
+    return Workload(name, domType, N, float(n), Ly, n, ny, nz, z0, Lz, zlo, zhi, has_torque,
+                    betam_hat=1.3267 if has_torque else 1.714, seed=seed)
+
+
+# Small parity cases: every geometry with and without torques, particles whose
+# kernels reach open ends (the reference reuses spread data in the ghost
+# layers there), odd and unequal grid sizes (Nyquist handling), a shifted z
+# origin.
+SMALL = [
+    small("s_dpbw_t", "DPBW", 24, 16, 17, 10.0, 1.5, 8.5, True),
+    small("s_dp_t", "DP", 24, 16, 19, 12.4, 3.0, 9.4, True, z0=0.0),
+    small("s_dpsc_t", "DPSC", 24, 16, 21, 10.0, 1.0, 9.0, True),
+    small("s_dpbw_f_top", "DPBW", 20, 20, 24, 12.0, 1.0, 11.5, False, seed=3),
+    small("s_dp_f_ends", "DP", 18, 18, 16, 14.0, 0.5, 13.5, False, seed=4),
+    small("s_dp_t_shift", "DP", 16, 16, 25, 10.0, -4.0, 4.0, True, z0=-5.0, seed=5),
+    small("s_dpbw_t_odd", "DPBW", 20, 15, 22, 11.0, 0.8, 10.5, True, ny=18, Ly=18.0, seed=6),
+    small("s_dpsc_f_odd", "DPSC", 20, 17, 20, 9.0, 0.3, 8.7, False, ny=14, Ly=14.0, seed=7),
+]
+SMALL_BY_NAME = {w.name: w for w in SMALL}

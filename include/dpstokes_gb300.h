@@ -1,0 +1,167 @@
+/*
+ * dpstokes_gb300.h -- C ABI of the GB300 doubly periodic Stokes mobility
+ * operator (libdpstokes_gb300.so).
+ *
+ * Computes [V; W] = M [F; T] for N blobs with exponential-of-semicircle (ES)
+ * kernels in a domain periodic in x, y and open (no wall), bounded below by a
+ * no-slip wall, or bounded by two no-slip walls in z.  Forces F, torques T,
+ * linear velocities V and angular velocities W are [N][3] arrays.
+ *
+ * Drop-in boundary.  Each entry point replaces one call of the reference's
+ * interface for this path (paths are within stochasticHydroTools/
+ * DoublyPeriodicStokes):
+ *   dpst_create        <- DPStokesGlue::initialize(PyParameters, int)
+ *                         (source/gpu/python_wrapper/uammd_interface.h:44-52,
+ *                          uammd_wrapper.cu:182-184) and, on the CPU path,
+ *                         FCM.Initialize (source/cpu/python/FCM.py:149-268)
+ *   dpst_destroy       <- DPStokesGlue::clear (uammd_interface.h:54-56,
+ *                         uammd_wrapper.cu:188-191) / FCM.Clean (FCM.py:443)
+ *   dpst_set_positions <- DPStokesGlue::setPositions(const real*)
+ *                         (uammd_interface.h:58, uammd_wrapper.cu:136-143) /
+ *                         FCM.SetPositions (FCM.py:270-332)
+ *   dpst_mdot          <- DPStokesGlue::Mdot(F, T|nullptr, MF, MT)
+ *                         (uammd_interface.h:60-63, uammd_wrapper.cu:146-170) /
+ *                         FCM.Mdot (FCM.py:334-441)
+ *   dpst_*_host        <- the same calls with host arrays, copied in and out on
+ *                         every call as the reference glue does
+ *                         (uammd_wrapper.cu:139-169)
+ *   dpst_spread_grid,  <- the reference's grid accessors GetData / CopyData
+ *   dpst_velocity_grid    (source/cpu/wrapper/GridWrapper.cpp:66-67), used by
+ *                         FCM.Mdot to hand the spread grid to the transform and
+ *                         the velocity grid to the interpolation (FCM.py:356,406)
+ *   dpst_mdot_timed    <- the stage-timed Mdot of the reference's benchmark
+ *                         (source/cpu/examples/mobility_bench.py:311-442)
+ *   dpst_last_error    <- replaces the C++ exceptions / exit(1) of the
+ *                         reference (uammd_wrapper.cu:106,208-211,
+ *                         source/cpu/include/exceptions.h:30-34)
+ *
+ * Conventions
+ *   - Every function returns DPST_OK (0) or an error code; on error
+ *     dpst_last_error() returns a message (thread-local).  Nothing throws.
+ *   - Device pointers are CUDA device addresses on the handle's device;
+ *     `stream` is a cudaStream_t (NULL = legacy default stream).  Device
+ *     entry points are asynchronous with respect to the host except
+ *     dpst_set_positions, which synchronises the stream once to report
+ *     out-of-domain particles.
+ *   - A handle is not thread-safe; separate handles are independent.
+ *   - Positions: x in [0, Lx], y in [0, Ly] (periodic), z in [zmin, zmax].
+ *   - Kernel: phi(r) = exp(beta (sqrt(1 - r^2/alpha^2) - 1)) per axis, with w
+ *     grid points under it (alpha in physical units; the reference's
+ *     UseCbeta convention gives alpha = w h / 2).  The dipole kernel
+ *     (w_d, beta_d, alpha_d) spreads torques through the curl and
+ *     interpolates the vorticity with kernel derivatives, as the reference
+ *     CPU path does by default.
+ */
+#ifndef DPSTOKES_GB300_H
+#define DPSTOKES_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define DPST_OK 0
+#define DPST_ERR_INVALID_ARG 1   /* bad parameter or pointer */
+#define DPST_ERR_NOT_READY 2     /* positions not set */
+#define DPST_ERR_OUT_OF_DOMAIN 3 /* a particle lies outside the unit cell */
+#define DPST_ERR_CUDA 4          /* CUDA / cuFFT failure */
+#define DPST_ERR_UNSUPPORTED 5   /* configuration the reference cannot run either */
+#define DPST_ERR_ALLOC 6         /* device or host allocation failed */
+
+/* geometry: reference domType DP / DPBW / DPSC (FCM.py:211-229) */
+#define DPST_MODE_NOWALL 0
+#define DPST_MODE_BOTTOM 1
+#define DPST_MODE_SLIT 2
+
+/* arithmetic of the operator */
+#define DPST_PREC_FP64 0  /* every stage in FP64: the drop-in for the reference */
+#define DPST_PREC_MIXED 1 /* FP32 spread/FFT/interp, FP32 z transform, FP64 BVP */
+
+/* element type of the particle arrays passed to mdot */
+#define DPST_F64 0
+#define DPST_F32 1
+
+typedef struct dpst_params {
+  int mode;          /* DPST_MODE_* */
+  int nx, ny, nz;    /* grid: nx*ny Fourier modes, nz Chebyshev points */
+  double Lx, Ly;     /* periodic box */
+  double zmin, zmax; /* Chebyshev interval; walls sit at zmin (bottom) / zmax (slit top) */
+  double viscosity;
+  int w;             /* monopole kernel: points per axis */
+  double beta;       /* monopole ES beta (the reference's beta_hat * w) */
+  double alpha;      /* monopole ES half width, physical units */
+  int has_torque;    /* 1: torques in, angular velocities out */
+  int w_d;           /* dipole kernel (used when has_torque) */
+  double beta_d;
+  double alpha_d;
+  int precision;     /* DPST_PREC_* */
+} dpst_params;
+
+typedef struct dpst_info {
+  int nxh;              /* nx/2 + 1 half-spectrum columns */
+  int n_modes;          /* ny * nxh wavenumbers solved per Mdot */
+  int nzeff_m, nzeff_d; /* extended z grid sizes (monopole, dipole) */
+  int ghost_m, ghost_d; /* ghost layers per z end */
+  int wz_max_m, wz_max_d;
+  double thr_m, thr_d;  /* kernel truncation thresholds */
+  double norm_m, norm_d;/* 1-D kernel integrals */
+  int64_t device_bytes; /* device memory held by the handle */
+  int64_t n_particles;
+} dpst_info;
+
+typedef struct dpst_engine *dpst_handle;
+
+/* Create an operator for n_particles on CUDA device `device`.  Plans FFTs,
+ * precomputes the per-wavenumber BVP factors and allocates all buffers. */
+int dpst_create(const dpst_params *p, int64_t n_particles, int device, dpst_handle *out);
+
+/* Release everything the handle owns.  NULL is accepted. */
+int dpst_destroy(dpst_handle h);
+
+/* Positions: device array [N][3] of `dtype` (DPST_F64 or DPST_F32). */
+int dpst_set_positions(dpst_handle h, const void *pos, int dtype, void *stream);
+
+/* V = M_FF F + M_FT T, W = M_TF F + M_TT T.  F, V: device [N][3]; T, W
+ * device [N][3] or NULL (no torques in / no angular velocities out).  All
+ * four arrays have element type `dtype`. */
+int dpst_mdot(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
+              void *stream);
+
+/* Host-array variants: copy in, run, copy out, synchronise. */
+int dpst_set_positions_host(dpst_handle h, const void *pos, int dtype, void *stream);
+int dpst_mdot_host(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
+                   void *stream);
+
+/* Diagnostics.
+ * dpst_spread_grid: run only the spreading stage (forces and, with T, the
+ *   torque curl, with the boundary fold) and copy the resulting grid to the
+ *   device buffer grid_out, layout [3][nz][ny][nx] (z index 0 at zmax), element
+ *   type double for DPST_PREC_FP64 and float for DPST_PREC_MIXED.
+ * dpst_velocity_grid: copy the fluid velocity on the grid from the last Mdot
+ *   (same layout and type) to grid_out.
+ * dpst_mdot_timed: dpst_mdot that also records CUDA events between stages and
+ *   synchronises; stage_ms[0..7] receive the milliseconds of: zero + spread,
+ *   forward x-y FFT, forward z transform, per-wavenumber solve, inverse z
+ *   transform (+ wall correction), inverse x-y FFT, interpolation, total. */
+int dpst_spread_grid(dpst_handle h, const void *F, const void *T, int dtype, void *grid_out,
+                     void *stream);
+int dpst_velocity_grid(dpst_handle h, void *grid_out, void *stream);
+int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
+                    void *stream, float *stage_ms);
+
+/* Sizes and derived constants of a handle. */
+int dpst_get_info(dpst_handle h, dpst_info *out);
+
+/* Last error message of the calling thread ("" if none). */
+const char *dpst_last_error(void);
+
+/* Library version string. */
+const char *dpst_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DPSTOKES_GB300_H */

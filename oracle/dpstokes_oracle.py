@@ -581,12 +581,13 @@ class DPSolver:
         with np.errstate(divide='ignore', invalid='ignore'):
             AinvB = np.stack([self._penta(B[:, :, c], real=True) for c in range(2)], axis=2)
         G = np.einsum('krj,kjc->krc', C, AinvB) - D
-        det = 1.0 / (G[:, 0, 0] * G[:, 1, 1] - G[:, 0, 1] * G[:, 1, 0])
         Ginv = np.empty_like(G)
-        Ginv[:, 0, 0] = G[:, 1, 1] * det
-        Ginv[:, 1, 0] = -G[:, 1, 0] * det
-        Ginv[:, 0, 1] = -G[:, 0, 1] * det
-        Ginv[:, 1, 1] = G[:, 0, 0] * det
+        with np.errstate(divide='ignore', invalid='ignore'):  # k=0 row is unused
+            det = 1.0 / (G[:, 0, 0] * G[:, 1, 1] - G[:, 0, 1] * G[:, 1, 0])
+            Ginv[:, 0, 0] = G[:, 1, 1] * det
+            Ginv[:, 1, 0] = -G[:, 1, 0] * det
+            Ginv[:, 0, 1] = -G[:, 0, 1] * det
+            Ginv[:, 1, 1] = G[:, 0, 0] * det
         self.AinvB, self.C, self.Ginv = AinvB, C, Ginv
         self.C_k0 = BCs_k0[:, :Nz]
         D_k0 = -BCs_k0[:, Nz:]

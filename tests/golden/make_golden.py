@@ -1,0 +1,68 @@
+"""Generates the golden fixtures in this directory by running the reference
+CPU path itself (source/cpu of stochasticHydroTools/DoublyPeriodicStokes,
+compiled unmodified by oracle/Makefile.ref and driven through its own FCM.py
+by oracle/ref_harness.py).
+
+    make -f oracle/Makefile.ref REF=/root/reference/source/cpu
+    python tests/golden/make_golden.py [--full]
+
+Inputs are not stored: they are regenerated from each workload's seed
+(doublyperiodicstokes_gb300.workloads.make_inputs); a SHA-256 of the input
+bytes is stored with the outputs so a test can detect a generator change.
+Each fixture holds V (and W with torques) from one Mdot, plus V from a second
+Mdot on the same positions (the reference keeps state between calls).
+"""
+import argparse
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from doublyperiodicstokes_gb300 import workloads as W  # noqa: E402
+import ref_harness  # noqa: E402
+
+
+def input_digest(X, F, T):
+    h = hashlib.sha256()
+    for a in (X, F, T):
+        if a is not None:
+            h.update(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
+def make(w, threads=8):
+    X, F, T = W.make_inputs(w)
+    t0 = time.time()
+    r = ref_harness.run_reference(w.oracle_params(), X.ravel(), F.ravel(),
+                                  None if T is None else T.ravel(), repeat=2, threads=threads)
+    dt = time.time() - t0
+    out = dict(V=r["V"], V_repeat=r["V_repeat"])
+    if w.has_torque:
+        out["W"] = r["W"]
+    meta = dict(workload=w.to_dict(), input_sha256=input_digest(X, F, T), ref_seconds=dt,
+                generator="tests/golden/make_golden.py via oracle/ref_harness.py")
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, w.name + ".npz"), **out)
+    print("%-18s %7.1fs |V|=%.3e" % (w.name, dt, np.linalg.norm(r["V"])), flush=True)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--full", action="store_true", help="also the full-size c0, c3, c1 cases")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    todo = list(W.SMALL)
+    if a.full:
+        todo += [W.C0, W.C3, W.C1]
+    for w in todo:
+        if a.only and w.name != a.only:
+            continue
+        make(w)

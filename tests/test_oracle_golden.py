@@ -1,0 +1,69 @@
+"""The oracle (numpy restatement) against outputs of the reference CPU path
+itself (tests/golden, made by tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+import dpstokes_oracle as O
+import golden_io
+from conftest import rel_err
+
+SMALL = [n for n in golden_io.names() if n.startswith("s_")]
+FULL = [n for n in golden_io.names() if not n.startswith("s_")]
+
+
+def _check(name, tol):
+    w, X, F, T, g = golden_io.inputs(name)
+    V, Wv = O.mdot(O.Params(**w.oracle_params()), X, F, T)
+    assert rel_err(V, g["V"]) < tol
+    assert rel_err(g["V_repeat"], g["V"]) == 0.0
+    if w.has_torque:
+        assert rel_err(Wv, g["W"]) < tol
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_oracle_matches_reference_small(name):
+    _check(name, 1e-13)
+
+
+@pytest.mark.parametrize("name", [n for n in FULL if n.startswith("c0")])
+def test_oracle_matches_reference_c0(name):
+    _check(name, 1e-13)
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("name", [n for n in FULL if not n.startswith("c0")])
+def test_oracle_matches_reference_full(name):
+    _check(name, 1e-13)
+
+
+def test_oracle_rejects_asymmetric_ghost_extension():
+    # Nz=19, Lz=12: node 6 sits exactly at distance thr = 3 from the top but
+    # not from the bottom; the reference overruns its interior grid here.
+    p = O.Params("DP", 16, 16, 19, 16.0, 16.0, 12.0, has_torque=False)
+    o = O.Oracle(p)
+    with pytest.raises(ValueError):
+        o.set_positions(np.array([[8.0, 8.0, 6.0]]))
+
+
+def test_oracle_linearity_and_translation():
+    """Mdot is linear in (F, T) and invariant to periodic shifts by whole cells."""
+    from doublyperiodicstokes_gb300 import workloads as W
+    # slit channel: no open ends, so no reuse of ghost-layer spread data, which
+    # the reference folds only partially in x and y (not shift invariant)
+    w = W.SMALL_BY_NAME["s_dpsc_t"]
+    X, F, T = W.make_inputs(w)
+    p = O.Params(**w.oracle_params())
+    o = O.Oracle(p)
+    o.set_positions(X)
+    V1, W1 = o.mdot(F, T)
+    V2, W2 = o.mdot(2.0 * F, 2.0 * T)
+    Vs, Ws = o.mdot(3.0 * F, 3.0 * T)
+    assert rel_err(Vs, V1 + V2) < 1e-13
+    assert rel_err(Ws, W1 + W2) < 1e-13
+    Xs = X.copy()
+    Xs[:, 0] = np.mod(Xs[:, 0] + 3 * p.hx, p.Lx)
+    o2 = O.Oracle(p)
+    o2.set_positions(Xs)
+    V3, W3 = o2.mdot(F, T)
+    assert rel_err(V3, V1) < 1e-12
+    assert rel_err(W3, W1) < 1e-12
