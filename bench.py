@@ -1,0 +1,318 @@
+"""Benchmark of the GB300 doubly periodic Stokes mobility operator.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload c2_dp_n65536] [--precision mixed|fp64]
+
+One step = one Mdot (forces + torques -> linear + angular velocities) of the
+named workload with synthetic seeded inputs (default: the open doubly
+periodic box with 65,536 particles, 512 x 512 x 128 grid, torques; the
+configuration the headline "Mdot particles/s at N=64K" is quoted on).
+Prints one JSON line.
+
+ours      : the mixed-precision operator, inputs resident on the device,
+            K Mdots between CUDA events (barrier + synchronize on both sides,
+            max over ranks); `e2e` is the same metric through the C ABI with
+            host arrays (host->device and device->host copies inside the timed
+            region); the plain FP64 operator is timed alongside for the
+            mixed-vs-FP64 part of the metric; `roofline` is the dominant
+            stage from CUDA events over K timed Mdots.
+reference : the reference CPU path as restated by the oracle (the reference's
+            own compiled CPU code cannot be built on this host: its sources
+            are not shipped here), single-threaded numpy, on a bounded sample
+            of the same workload (see oracle/cpu_sample.py).
+Under torchrun (N > 1) every rank runs an independent replica (one system
+does not shard: replicas only); value aggregates over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mdot particles/s at N=64K, mixed vs FP64 at rel err<=1e-5; bwd/fwd time ratio"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap,power.draw")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.file is None:
+            return None
+        try:
+            rows = [l.strip().split(", ") for l in open(self.file.name) if l.strip()]
+            os.unlink(self.file.name)
+        except Exception:
+            return None
+        sm = [float(r[0]) for r in rows if len(r) >= 7 and r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in rows if len(r) >= 7 and r[1].replace('.', '').isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 7 for i in range(4)
+                          if r[2 + i].strip().lower() == "active"})
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def algorithmic_bytes(stage, w, prec):
+    """Bytes a stage must move at minimum for one Mdot."""
+    s = 4 if prec == "mixed" else 8
+    nxh = w.nx // 2 + 1
+    nk = w.ny * nxh
+    grid = 3 * w.nx * w.ny * w.nz * s
+    spec = 3 * nk * w.nz * 2 * s
+    if stage == "solve":
+        # spectrum in and out, per-wavenumber factors (7 nz + 4 FP64 values)
+        return 2 * spec + nk * (7 * w.nz + 4) * 8
+    if stage in ("ztrans_fwd", "ztrans_inv"):
+        return 2 * spec
+    if stage in ("fft_fwd", "fft_inv"):
+        return grid + spec
+    if stage == "spread":
+        return grid + w.N * (6 if w.has_torque else 3) * s
+    if stage == "interp":
+        return grid + w.N * (6 if w.has_torque else 3) * s
+    return None
+
+
+def run_ours(args, rank, world):
+    import torch
+    import ctypes
+    from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W, _lib
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = W.CONFIGS[args.workload]
+    X, F, T = W.make_inputs(w)
+    prec = args.precision
+    dt = torch.float32 if prec == "mixed" else torch.float64
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    op = DPStokes(StokesParams.from_workload(w, prec), w.N, device=dev)
+    op.set_positions(torch.tensor(X, device=dev))
+    Fd = torch.tensor(F, dtype=dt, device=dev)
+    Td = torch.tensor(T, dtype=dt, device=dev) if T is not None else None
+    V = torch.empty_like(Fd)
+    Wd = torch.empty_like(Fd) if w.has_torque else None
+    for _ in range(args.warmup):
+        op.mdot(Fd, Td, out=(V, Wd))
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as cs:
+        barrier()
+        e0.record()
+        for _ in range(args.steps):
+            op.mdot(Fd, Td, out=(V, Wd))
+        e1.record()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = cs.summary()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * w.N * args.steps / (ms / 1e3)
+
+    # per-stage device times (CUDA events on the operator's stream)
+    stage_runs = []
+    for _ in range(max(3, min(args.steps, 10))):
+        _, _, st = op.mdot_timed(Fd, Td)
+        stage_runs.append(st)
+    stages = {k: statistics.median([s[k] for s in stage_runs]) for k in stage_runs[0]}
+    info = op.info()
+
+    # end to end through the C ABI with pinned host arrays
+    L = _lib.lib()
+    Fh = torch.tensor(F, dtype=dt).pin_memory()
+    Th = torch.tensor(T, dtype=dt).pin_memory() if T is not None else None
+    Vh = torch.empty_like(Fh).pin_memory()
+    Wh = torch.empty_like(Fh).pin_memory() if w.has_torque else None
+    code = _lib.F32 if dt == torch.float32 else _lib.F64
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr() if t is not None else 0)  # noqa: E731
+
+    def e2e_step():
+        _lib.check(L.dpst_mdot_host(op._h, ptr(Fh), ptr(Th), ptr(Vh), ptr(Wh), code, stream))
+
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    nbytes = Fh.numel() * Fh.element_size()
+    e2e = {"value": world * w.N * args.steps / e2e_s, "unit": "particles/s",
+           "h2d_bytes_per_step": nbytes * (2 if T is not None else 1),
+           "d2h_bytes_per_step": nbytes * (2 if w.has_torque else 1)}
+
+    # the plain FP64 operator on the same inputs: speed and error of mixed
+    extra = {}
+    if prec == "mixed" and not args.skip_fp64:
+        op64 = DPStokes(StokesParams.from_workload(w, "fp64"), w.N, device=dev)
+        op64.set_positions(torch.tensor(X, device=dev))
+        F64 = torch.tensor(F, device=dev)
+        T64 = torch.tensor(T, device=dev) if T is not None else None
+        V64, W64 = op64.mdot(F64, T64)
+        barrier()
+        k64 = max(2, args.steps // 5)
+        e0.record()
+        for _ in range(k64):
+            op64.mdot(F64, T64)
+        e1.record()
+        barrier()
+        ms64 = e0.elapsed_time(e1) / k64
+        V32, W32 = op.mdot(Fd, Td)
+        torch.cuda.synchronize()
+        rel = lambda a, b: float(torch.linalg.norm(a.double() - b) / torch.linalg.norm(b))  # noqa: E731
+        extra = {"fp64_particles_per_s": w.N / (ms64 / 1e3), "fp64_ms_per_step": ms64,
+                 "speedup_vs_fp64": ms64 / ms_step, "rel_err_V_vs_fp64": rel(V32, V64)}
+        if W64 is not None:
+            extra["rel_err_W_vs_fp64"] = rel(W32, W64)
+        op64.close()
+
+    # roofline of the dominant stage
+    peaks, peak_kind = load_peaks()
+    stage_names = [k for k in stages if k != "total"]
+    dom = max(stage_names, key=lambda k: stages[k])
+    ab = algorithmic_bytes(dom, w, prec)
+    achieved = ab / (stages[dom] * 1e-3) / 1e9 if ab else None
+    roof = {"bound": "hbm", "stage": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
+            "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
+            "traffic": None, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    if dom == "solve":
+        # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
+        roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "
+                        "its algorithmic bytes")
+    return dict(value=value, ms_step=ms_step, e2e=e2e, stages=stages, info=info, extra=extra,
+                roofline=roof, clocks=clocks, w=w)
+
+
+def cpu_baseline(w):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import dpstokes_oracle as O
+    import cpu_sample
+    from doublyperiodicstokes_gb300 import workloads as W
+    X, F, T = W.make_inputs(w)
+    tot, stages, sample = cpu_sample.sample_mdot_seconds(O.Params(**w.oracle_params()), X, F, T)
+    return {"value": w.N / tot, "unit": "particles/s", "cores": 1, "kind": "port",
+            "sample": sample, "seconds_per_mdot_est": tot,
+            "stage_seconds": {k: round(v, 3) for k, v in stages.items()}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2_dp_n65536")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from doublyperiodicstokes_gb300 import workloads as W
+    w = W.CONFIGS[args.workload]
+    config = {"workload": w.name, "domain": w.domType, "N": w.N, "grid": [w.nx, w.ny, w.nz],
+              "box": [w.Lx, w.Ly, w.Lz], "torques": w.has_torque, "kernel_w": w.wm,
+              "precision": args.precision, "l2": "inputs larger than L2 (grid > 129 MB)",
+              "parallelism": "replicas x%d" % args.gpus}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        t0 = time.time()
+        cb = cpu_baseline(w)
+        line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particles/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * cb["seconds_per_mdot_est"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config, "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "particles/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0},
+                "wall_s": time.time() - t0}
+        print(json.dumps(line), flush=True)
+        return
+    r = run_ours(args, rank, world)
+    if rank != 0:
+        return
+    info = r["info"]
+    line = {"metric": METRIC, "value": r["value"], "unit": "particles/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": config, "e2e": r["e2e"],
+            "gpu_launches": info["kernels_per_mdot"] * args.steps,
+            "roofline": r["roofline"], "clocks": r["clocks"],
+            "stages_ms": {k: round(v, 4) for k, v in r["stages"].items()},
+            "bwd_fwd_ratio": None}
+    line.update(r["extra"])
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(r["w"])
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

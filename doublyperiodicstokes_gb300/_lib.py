@@ -32,7 +32,8 @@ class DpstInfo(ctypes.Structure):
                 ("wz_max_m", ctypes.c_int), ("wz_max_d", ctypes.c_int),
                 ("thr_m", ctypes.c_double), ("thr_d", ctypes.c_double),
                 ("norm_m", ctypes.c_double), ("norm_d", ctypes.c_double),
-                ("device_bytes", ctypes.c_int64), ("n_particles", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("n_particles", ctypes.c_int64),
+                ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int)]
 
 
 # every entry point of include/dpstokes_gb300.h with its signature

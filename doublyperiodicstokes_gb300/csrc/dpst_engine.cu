@@ -47,8 +47,7 @@ void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, 
 
 void launch_bvp_factors(const KsArgs &a, cudaStream_t s);
 template <typename R>
-void launch_bvp(const KsArgs &a, R *spec, double2 *corr, double2 *scratch, int64_t nthreads,
-                cudaStream_t s);
+cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, int nsm, cudaStream_t s);
 template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s);
@@ -241,7 +240,7 @@ struct Engine : EngineBase {
   GridArgs g;
   KsArgs ks;
   // device buffers
-  DevBuf grid, spec, corr, scratch, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
+  DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g;
   DevBuf pos64, flags;
   DevBuf st_m[8], st_d[8];
@@ -251,7 +250,6 @@ struct Engine : EngineBase {
   Ghosts<R> ghm, ghd;
   int reach_m[2], reach_d[2];
   bool positioned = false;
-  int64_t bvp_threads = 0;
   cufftHandle plan_f = 0, plan_b = 0;
   bool plans = false;
 
@@ -415,8 +413,6 @@ struct Engine : EngineBase {
     grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
     spec.alloc(sizeof(CR) * 3 * (size_t)nz * nk);
     if (p.mode != DPST_MODE_NOWALL) corr.alloc(sizeof(double2) * 16 * (size_t)nk);
-    bvp_threads = (int64_t)nsm * 64;
-    scratch.alloc(sizeof(double2) * 3 * (size_t)(nz + 2) * bvp_threads);
     // particle buffers
     pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
     flags.alloc(sizeof(int) * 8);
@@ -594,8 +590,7 @@ struct Engine : EngineBase {
     ef.ks = ks;
     DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s));
     mark(3, s);
-    launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), scratch.as<double2>(), bvp_threads, s);
-    DPST_CUDA(cudaGetLastError());
+    DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), nsm, s));
     mark(4, s);
     EpiArgs eb = ef;
     eb.inverse = 1;
@@ -653,8 +648,13 @@ struct Engine : EngineBase {
     o->norm_m = km.d.norm;
     o->norm_d = p.has_torque ? kd.d.norm : 0;
     o->n_particles = N;
+    // spread (mono [+ dip]), ghost folds (2 kernels per buffer in use),
+    // forward z GEMM, BVP pairs + k=0, inverse z GEMM, interp (mono [+ dip])
+    int nbuf = (ghm.top != nullptr) + (ghm.bot != nullptr) + (ghd.top != nullptr) + (ghd.bot != nullptr);
+    o->ghost_layers_in_use = nbuf;
+    o->kernels_per_mdot = (p.has_torque ? 2 : 1) + 2 * nbuf + 1 + 2 + 1 + (p.has_torque ? 2 : 1);
     int64_t b = 0;
-    const DevBuf *all[] = {&grid, &spec, &corr, &scratch, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
+    const DevBuf *all[] = {&grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1,
                            &fac_g, &pos64, &flags, &dphzw_buf};
     for (const DevBuf *d : all) b += d->bytes;

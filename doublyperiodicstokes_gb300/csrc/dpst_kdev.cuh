@@ -1,0 +1,106 @@
+// Device helpers shared by the wavenumber-space kernels (dpst_kspace.cu,
+// dpst_bvp.cu): complex arithmetic on double2, the Hermitian-partner test of
+// a half-spectrum mode, and the slit-channel correction coefficients.
+#pragma once
+#include "dpst_internal.cuh"
+
+namespace dpst {
+
+static __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+static __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+static __device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+static __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+static __device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+// i*k*a for real k
+static __device__ __forceinline__ double2 cik(double k, double2 a) { return make_double2(-k * a.y, k * a.x); }
+
+static __device__ __forceinline__ bool mode_is_hermitian(const KsArgs &a, int ix, int iy, double kx, double ky,
+                                                  double &kxp, double &kyp) {
+  int ixp = (a.nx - ix) % a.nx, iyp = (a.ny - iy) % a.ny;
+  kxp = a.kvx[ixp];
+  kyp = a.kvy[iyp];
+  return (kxp == -kx) && (kyp == -ky);
+}
+
+// ---------------------------------------------------------------------------
+// 8x8 complex solve with partial pivoting on |re|+|im| (the LAPACK zgesv
+// pivot rule), column-major A.
+// ---------------------------------------------------------------------------
+static __device__ void zsolve8(double2 *A, double2 *x) {
+  for (int k = 0; k < 8; ++k) {
+    int piv = k;
+    double best = -1.0;
+    for (int r = k; r < 8; ++r) {
+      double v = fabs(A[r + 8 * k].x) + fabs(A[r + 8 * k].y);
+      if (v > best) { best = v; piv = r; }
+    }
+    if (piv != k) {
+      for (int c = 0; c < 8; ++c) { double2 t = A[k + 8 * c]; A[k + 8 * c] = A[piv + 8 * c]; A[piv + 8 * c] = t; }
+      double2 t = x[k]; x[k] = x[piv]; x[piv] = t;
+    }
+    double2 p = A[k + 8 * k];
+    double den = p.x * p.x + p.y * p.y;
+    for (int r = k + 1; r < 8; ++r) {
+      double2 ar = A[r + 8 * k];
+      double2 l = make_double2((ar.x * p.x + ar.y * p.y) / den, (ar.y * p.x - ar.x * p.y) / den);
+      for (int c = k + 1; c < 8; ++c) A[r + 8 * c] = csub(A[r + 8 * c], cmul(l, A[k + 8 * c]));
+      x[r] = csub(x[r], cmul(l, x[k]));
+    }
+  }
+  for (int r = 7; r >= 0; --r) {
+    double2 s = x[r];
+    for (int c = r + 1; c < 8; ++c) s = csub(s, cmul(A[r + 8 * c], x[c]));
+    double2 p = A[r + 8 * r];
+    double den = p.x * p.x + p.y * p.y;
+    x[r] = make_double2((s.x * p.x + s.y * p.y) / den, (s.y * p.x - s.x * p.y) / den);
+  }
+}
+
+// Slit correction coefficients for wavevector (kx, ky), wall values fb (z=0)
+// and ft (z=Hs) (DPTools.cpp:731-788).
+static __device__ void slit_coeffs(double kx, double ky, double Hs, double eta, const double2 fb[3],
+                            const double2 ft[3], double2 c[8]) {
+  double2 A[64];
+  for (int q = 0; q < 64; ++q) A[q] = make_double2(0, 0);
+  const double k = sqrt(kx * kx + ky * ky);
+  const double fac = 1.0 / 2.0 / eta;
+  const double enkh = exp(-k * Hs);
+#define AT(r, cc) A[(r) + 8 * (cc)]
+  AT(0, 0) = make_double2(fac, 0);
+  AT(0, 1) = make_double2(enkh * fac, 0);
+  AT(0, 6) = make_double2(-k, 0);
+  AT(0, 7) = make_double2(k * enkh, 0);
+  AT(1, 0) = make_double2((1 - k * Hs) * enkh * fac, 0);
+  AT(1, 1) = make_double2((1 + k * Hs) * fac, 0);
+  AT(1, 6) = make_double2(-k * enkh, 0);
+  AT(1, 7) = make_double2(k, 0);
+  AT(2, 2) = make_double2(1, 0);
+  AT(2, 3) = make_double2(enkh, 0);
+  AT(3, 4) = make_double2(1, 0);
+  AT(3, 5) = make_double2(enkh, 0);
+  AT(4, 6) = make_double2(1, 0);
+  AT(4, 7) = make_double2(enkh, 0);
+  AT(5, 0) = make_double2(0, -(kx * Hs * enkh * fac / k));
+  AT(5, 1) = make_double2(0, kx * Hs * fac / k);
+  AT(5, 2) = make_double2(enkh, 0);
+  AT(5, 3) = make_double2(1, 0);
+  AT(6, 0) = make_double2(0, -(ky * Hs * enkh * fac / k));
+  AT(6, 1) = make_double2(0, ky * Hs * fac / k);
+  AT(6, 4) = make_double2(enkh, 0);
+  AT(6, 5) = make_double2(1, 0);
+  AT(7, 0) = make_double2(Hs * enkh * fac, 0);
+  AT(7, 1) = make_double2(Hs * fac, 0);
+  AT(7, 6) = make_double2(enkh, 0);
+  AT(7, 7) = make_double2(1, 0);
+#undef AT
+  // x0 = -i kx fbx - i ky fby ; x1 likewise for the top
+  c[0] = csub(cik(-kx, fb[0]), cik(ky, fb[1]));
+  c[1] = csub(cik(-kx, ft[0]), cik(ky, ft[1]));
+  c[2] = fb[0]; c[3] = fb[1]; c[4] = fb[2];
+  c[5] = ft[0]; c[6] = ft[1]; c[7] = ft[2];
+  zsolve8(A, c);
+}
+
+}  // namespace dpst

@@ -109,6 +109,9 @@ typedef struct dpst_info {
   double norm_m, norm_d;/* 1-D kernel integrals */
   int64_t device_bytes; /* device memory held by the handle */
   int64_t n_particles;
+  int kernels_per_mdot; /* kernels of this library one dpst_mdot launches (with T
+                           and W given); cuFFT kernels and memsets not counted */
+  int ghost_layers_in_use; /* open-end ghost buffers the current positions need */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

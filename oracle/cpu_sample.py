@@ -1,0 +1,74 @@
+"""Bounded CPU timing sample of the oracle's Mdot (test / benchmark
+infrastructure: bench.py's cpu_baseline and reference arm only).
+
+A full oracle Mdot at the 65,536-particle, 512 x 512 x 128 configuration
+takes minutes and ~15 GB.  The sample times every stage of the same
+configuration on a fixed fraction of its work and scales each stage back up
+(all stages are linear in the sampled quantity):
+  spread + interpolation   first N/pfrac particles            x pfrac
+  forward / backward FFT   one of the three grid components   x 3
+  per-wavenumber solve     every mfrac-th wavenumber (k != 0) x (modes/sampled)
+Single-threaded numpy (cores = 1).
+"""
+import time
+
+import numpy as np
+
+import dpstokes_oracle as O
+
+
+def sample_mdot_seconds(p: O.Params, X, F, T=None, pfrac=16, mfrac=16):
+    X = np.asarray(X, dtype=np.float64).reshape(-1, 3)
+    F = np.asarray(F, dtype=np.float64).reshape(-1, 3)
+    T = None if T is None else np.asarray(T, dtype=np.float64).reshape(-1, 3)
+    N = X.shape[0]
+    ns = max(1, N // pfrac)
+    o = O.Oracle(p)
+    o.set_positions(X[:ns])
+    t0 = time.perf_counter()
+    fG = o.spread_all(F[:ns], None if T is None else T[:ns])
+    t_spread = time.perf_counter() - t0
+    # forward transform of one component
+    one = np.ascontiguousarray(fG[..., :1])
+    del fG
+    t0 = time.perf_counter()
+    fh = O.fc_forward(one)
+    t_fwd = 3 * (time.perf_counter() - t0)
+    # solve on a subset of wavenumbers
+    nk = p.Nx * p.Ny
+    modes = np.arange(1, nk, mfrac)
+    rng = np.random.default_rng(0)
+    fk = (rng.standard_normal((modes.size + 1, p.Nz, 3)) + 1j * rng.standard_normal((modes.size + 1, p.Nz, 3)))
+    sol = O.DPSolver(p.Nx, p.Ny, p.Nz, p.Lx, p.Ly, p.Lz / 2, p.eta,
+                     modes=np.concatenate(([0], modes)))
+    t0 = time.perf_counter()
+    U = sol.solve_no_wall(fk)
+    if p.domType == 'DPBW':
+        sol.correct_bottom(U, o.zpts)
+    elif p.domType == 'DPSC':
+        sol.correct_slit(U, o.zpts, p.Lz)
+    t_solve = (time.perf_counter() - t0) * (nk - 1) / modes.size
+    # backward transform of one component
+    t0 = time.perf_counter()
+    ug = O.fc_backward(fh)
+    t_bwd = 3 * (time.perf_counter() - t0)
+    del fh
+    uG = np.repeat(ug, 3, axis=3)
+    t0 = time.perf_counter()
+    O.ghost_copy(o.g, uG, o.BCs)
+    O.interpolate(o.g, o.km, o.loc)
+    if p.has_torque:
+        O.ghost_copy(o.tg, uG, o.BCs)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=0)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=1)
+        O.ghost_copy(o.tg, uG, o.BCst)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=2)
+    t_interp = time.perf_counter() - t0
+    scale = N / ns
+    stages = dict(spread=t_spread * scale, fft_fwd=t_fwd, solve=t_solve, fft_bwd=t_bwd,
+                  interp=t_interp * scale)
+    total = sum(stages.values())
+    sample = ("oracle stages timed on %d of %d particles (x%.0f), 1 of 3 grid components (x3), "
+              "%d of %d wavenumbers (x%.1f); single-threaded numpy"
+              % (ns, N, scale, modes.size, nk - 1, (nk - 1) / modes.size))
+    return total, stages, sample

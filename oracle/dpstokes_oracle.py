@@ -342,7 +342,7 @@ def spread(g, kern, loc, Fp, deriv=None):
         idx = _ext_indices(g, lc, kern.w).ravel()
         for d in range(3):
             vals = (delta * Fp[sl, d][:, None, None, None]).ravel()
-            ext[:, d] += np.bincount(idx, weights=vals, minlength=ext.shape[0])
+            np.add.at(ext[:, d], idx, vals)
 
 
 def interpolate(g, kern, loc, deriv=None):
@@ -431,11 +431,11 @@ def ghost_copy(g, fG, BCs):
 # --------------------------------------------------------------------------
 def fc_forward(fG):
     """[Ny][Nx][Nz][3] real -> Fourier (unnormalised) x Chebyshev coefficients."""
-    Ny, Nx, Nz, _ = fG.shape
+    Ny, Nx, Nz, nd = fG.shape
     Nu = 2 * Nz - 2
     ext = np.concatenate([fG, fG[:, :, Nz - 2:0:-1, :]], axis=2)
     X = np.fft.fftn(ext, axes=(0, 1, 2))
-    out = np.empty((Ny, Nx, Nz, 3), dtype=np.complex128)
+    out = np.empty((Ny, Nx, Nz, nd), dtype=np.complex128)
     out[:, :, 0] = X[:, :, 0] / Nu
     out[:, :, 1:Nz - 1] = (X[:, :, 1:Nz - 1] + X[:, :, Nu - 1:Nz - 1:-1]) / Nu
     out[:, :, Nz - 1] = X[:, :, Nz - 1] / Nu
@@ -444,9 +444,9 @@ def fc_forward(fG):
 
 def fc_backward(U):
     """Chebyshev coefficients x Fourier -> real grid (real part)."""
-    Ny, Nx, Nz, _ = U.shape
+    Ny, Nx, Nz, nd = U.shape
     Nu = 2 * Nz - 2
-    Y = np.empty((Ny, Nx, Nu, 3), dtype=np.complex128)
+    Y = np.empty((Ny, Nx, Nu, nd), dtype=np.complex128)
     Y[:, :, 0] = Nu * U[:, :, 0]
     Y[:, :, 1:Nz - 1] = Nu * U[:, :, 1:Nz - 1] / 2
     Y[:, :, Nz - 1] = Nu * U[:, :, Nz - 1]
@@ -537,6 +537,7 @@ class DPSolver:
     Ly: float
     H: float
     eta: float
+    modes: np.ndarray = None  # optional subset of flattened wavenumbers (timing samples)
     Kx: np.ndarray = field(init=False)
     Ky: np.ndarray = field(init=False)
 
@@ -547,14 +548,16 @@ class DPSolver:
         ky = 2 * np.pi * np.concatenate((np.arange(0, np.floor(Ny / 2) + 1),
                                          np.arange(-1 * np.ceil(Ny / 2) + 1, 0))) / self.Ly
         Kx, Ky = [K.flatten() for K in np.meshgrid(kx, ky, indexing='xy')]
-        Ksq = Kx ** 2 + Ky ** 2
-        self.Kx, self.Ky, self.K = Kx, Ky, np.sqrt(Ksq)
         Dx = 1j * Kx
         Dy = 1j * Ky
         if Nx % 2 == 0:
             Dx.reshape((Ny, Nx))[:, Nx // 2] = 0
         if Ny % 2 == 0:
             Dy.reshape((Ny, Nx))[Ny // 2, :] = 0
+        if self.modes is not None:
+            Kx, Ky, Dx, Dy = Kx[self.modes], Ky[self.modes], Dx[self.modes], Dy[self.modes]
+        Ksq = Kx ** 2 + Ky ** 2
+        self.Kx, self.Ky, self.K = Kx, Ky, np.sqrt(Ksq)
         self.Dx, self.Dy = Dx, Dy
         self.FIMat = first_integral_matrix(Nz, H)
         self.SIMat = second_integral_matrix(Nz, H)
@@ -571,7 +574,7 @@ class DPSolver:
         B = -Ksq[:, None, None] * S[None, :, Nz:]  # [k, Nz, 2]
         C = BCs_k[:, :, :Nz]  # [k, 2, Nz]
         D = BCs_k[:, :, Nz:]  # [k, 2, 2] (row, col)
-        nk = Nx * Ny
+        nk = Kx.shape[0]
         beta = np.zeros((nk, Nz + 1))
         beta[:, 1] = d0[:, 0]
         beta[:, 2] = d0[:, 1]
