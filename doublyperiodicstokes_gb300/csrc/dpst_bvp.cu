@@ -8,60 +8,78 @@
 // matrices); real and imaginary parts couple only through the products with
 // i kx and i ky.  A pair of adjacent lanes therefore owns one wavenumber:
 // lane 2q the real part, lane 2q+1 the imaginary part, exchanging the few
-// coupled values through shared memory and warp shuffles.  The three working
-// columns of a lane (penta solution / border solution, pressure
-// coefficients, pressure derivative coefficients: 3 nz + 2 doubles) live in
-// shared memory laid out [row][lane], so every access is conflict-free.  A
-// CTA of 64 lanes solves 32 wavenumbers at a time and strides over all of
-// them (persistent).  GB300 executes FP64 at 1/58 of its FP32 rate, so a
-// few warps per SM keep the FP64 pipe busy; the kernel is built to issue
-// nothing but the recurrence arithmetic on that pipe.
+// coupled values through shared memory, global scratch and warp shuffles.
+// The penta / right-hand-side column of a lane (nz + 2 doubles) lives in
+// shared memory laid out [row][lane], so every access is conflict-free; the
+// pressure coefficients (nz doubles per lane, read back by the partner lane)
+// live in an L2-resident global scratch laid out [row][lane of the grid];
+// the pressure derivative is consumed as it is produced (the z velocity is
+// solved first).  A CTA of 192 lanes solves 96 wavenumbers at a time and
+// strides over all of them (persistent).  GB300 executes FP64 at 1/58 of its
+// FP32 rate with the FP64 units split across the four SM sub-partitions, so
+// the CTA is sized for six warps per SM and the per-wavenumber factors stream
+// in through the read-only path ahead of the recurrences.
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
 
 namespace dpst {
 
-constexpr int BVP_LANES = 64;
+constexpr int BVP_LANES = 192;  // 96 wavenumbers per CTA
+constexpr int BVP_MODES = BVP_LANES / 2;
+
+#define LDG(p) __ldg(p)
 
 template <typename R>
 __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
-                                                         double2 *__restrict__ corr) {
+                                                         double2 *__restrict__ corr,
+                                                         double *__restrict__ cp_scratch) {
   extern __shared__ double bvp_sm[];
   const int nz = a.nz;
   const int64_t nk = a.nk;
   const int tid = threadIdx.x, part = tid & 1, q = tid >> 1;
   const int T = BVP_LANES;
-  double *Xs = bvp_sm;                 // [(nz + 2)][T]
-  double *CPs = bvp_sm + (nz + 2) * T;  // [nz][T]
-  double *DPs = CPs + nz * T;           // [nz][T]
+  double *Xs = bvp_sm;  // [(nz + 2)][T] penta / RHS column
+  // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
+  // in global memory (L2 resident: a few tens of MB)
+  const int64_t GT = (int64_t)gridDim.x * T;
+  double *__restrict__ CPs = cp_scratch + (int64_t)blockIdx.x * T;
 #define XS(j) Xs[(j) * T + tid]
-#define CPS(j) CPs[(j) * T + tid]
-#define CPO(j) CPs[(j) * T + (tid ^ 1)]
-#define DPS(j) DPs[(j) * T + tid]
+#define CPS(j) CPs[(int64_t)(j) * GT + tid]
+#define CPO(j) CPs[(int64_t)(j) * GT + (tid ^ 1)]
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
   const double inv_eta = 1.0 / a.eta;
-  const double *s0 = a.s0, *sp2 = a.sp2, *sm2 = a.sm2, *fm1 = a.fm1, *fp1 = a.fp1;
-  const int64_t ntiles = (nk + 31) / 32;
+  const double *__restrict__ s0 = a.s0;
+  const double *__restrict__ sp2 = a.sp2;
+  const double *__restrict__ sm2 = a.sm2;
+  const double *__restrict__ fm1 = a.fm1;
+  const double *__restrict__ fp1 = a.fp1;
+  const int64_t ntiles = (nk + BVP_MODES - 1) / BVP_MODES;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t i_raw = tile * 32 + q;
+    const int64_t i_raw = tile * BVP_MODES + q;
     const int64_t i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0 is solved by k_bvp_k0
-    // element (d, j, mode, part) of the spectrum as a real array
     auto ldp = [&](int d, int j, int pp) -> double {
       return (double)spec[(((int64_t)d * nz + j) * nk + i) * 2 + pp];
     };
     const int ix = (int)(i % a.nxh), iy = (int)(i / a.nxh);
-    const double kx = a.kvx[ix], ky = a.kvy[iy];
+    const double kx = LDG(a.kvx + ix), ky = LDG(a.kvy + iy);
     const double Dx = ((a.nx % 2) == 0 && ix == a.nx / 2) ? 0.0 : kx;
     const double Dy = ((a.ny % 2) == 0 && iy == a.ny / 2) ? 0.0 : ky;
     const double K = sqrt(kx * kx + ky * ky);
-    const double *mf = a.mfac + i, *ib = a.invb + i, *d2 = a.dp2 + i;
-    const double *A0 = a.ab0 + i, *A1 = a.ab1 + i, *C0 = a.c0 + i, *C1 = a.c1 + i;
-    const double G00 = a.ginv[i], G10 = a.ginv[nk + i], G01 = a.ginv[2 * nk + i], G11 = a.ginv[3 * nk + i];
+    const double *__restrict__ mf = a.mfac + i;
+    const double *__restrict__ ib = a.invb + i;
+    const double *__restrict__ d2 = a.dp2 + i;
+    const double *__restrict__ A0 = a.ab0 + i;
+    const double *__restrict__ A1 = a.ab1 + i;
+    const double *__restrict__ C0 = a.c0 + i;
+    const double *__restrict__ C1 = a.c1 + i;
+    const double G00 = LDG(a.ginv + i), G10 = LDG(a.ginv + nk + i);
+    const double G01 = LDG(a.ginv + 2 * nk + i), G11 = LDG(a.ginv + 3 * nk + i);
 
     // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j
     {
       double dfp1 = 0.0, dfp2 = 0.0, fzn = 0.0;
+#pragma unroll 4
       for (int j = nz - 1; j >= 0; --j) {
         const double df = (j == nz - 1) ? 0.0 : dfp2 + ((double)((j + 1) * 2) / a.H) * fzn;
         const double fz = ldp(2, j, part);
@@ -72,66 +90,68 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
         fzn = fz;
       }
     }
-    // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS, with the
+    // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
     // border dots y = C x accumulated during the back sweep
     auto penta = [&](double &y0, double &y1) {
       double xm2 = XS(0), xm1 = XS(1);
-#pragma unroll 4
+#pragma unroll 8
       for (int j = 2; j < nz; ++j) {
-        const double v = XS(j) - mf[j * nk] * xm2;
+        const double v = XS(j) - LDG(mf + j * nk) * xm2;
         XS(j) = v;
         xm2 = xm1;
         xm1 = v;
       }
-      const double xl = ib[nz * nk] * XS(nz - 1);
-      const double xl2 = ib[(nz - 1) * nk] * XS(nz - 2);
+      const double xl = LDG(ib + nz * nk) * xm1;
+      const double xl2 = LDG(ib + (nz - 1) * nk) * xm2;
       XS(nz - 1) = xl;
       XS(nz - 2) = xl2;
-      y0 = C0[(nz - 1) * nk] * xl + C0[(nz - 2) * nk] * xl2;
-      y1 = C1[(nz - 1) * nk] * xl + C1[(nz - 2) * nk] * xl2;
+      y0 = LDG(C0 + (nz - 1) * nk) * xl + LDG(C0 + (nz - 2) * nk) * xl2;
+      y1 = LDG(C1 + (nz - 1) * nk) * xl + LDG(C1 + (nz - 2) * nk) * xl2;
       double xp2 = xl, xp1 = xl2;
-#pragma unroll 4
+#pragma unroll 8
       for (int j = nz - 3; j >= 0; --j) {
-        const double v = ib[(j + 1) * nk] * (XS(j) - d2[j * nk] * xp2);
+        const double v = LDG(ib + (j + 1) * nk) * (XS(j) - LDG(d2 + j * nk) * xp2);
         XS(j) = v;
-        y0 += C0[j * nk] * v;
-        y1 += C1[j * nk] * v;
+        y0 += LDG(C0 + j * nk) * v;
+        y1 += LDG(C1 + j * nk) * v;
         xp2 = xp1;
         xp1 = v;
       }
     };
-    auto border = [&](double g0, double g1) {
-#pragma unroll 4
-      for (int j = 0; j < nz; ++j) XS(j) -= A0[j * nk] * g0 + A1[j * nk] * g1;
-      XS(nz) = g0;
-      XS(nz + 1) = g1;
-    };
-    // S [x; g] for row m (SIMat, Chebyshev.py:139-160)
-    auto srow = [&](int m, double g0, double g1) {
-      double c = s0[m] * XS(m);
-      if (m >= 2) c = sm2[m] * XS(m - 2) + c;
-      c = c + sp2[m] * XS(m + 2);
-      if (m == 0) c += a.se0 * g0;
-      if (m == 1) c += a.se1 * g1;
-      return c;
+    // border-corrected solution x_j = X_j - (A0_j g0 + A1_j g1); x_nz = g0, x_nz+1 = g1
+    auto xcor = [&](int j, double g0, double g1) -> double {
+      if (j < nz) return XS(j) - (LDG(A0 + j * nk) * g0 + LDG(A1 + j * nk) * g1);
+      return j == nz ? g0 : g1;
     };
 
-    // pressure: Schur solve, then cp = S [x; g], dp = F [x; g]
+    // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
+    // once for the z-velocity RHS, which overwrites XS behind the window
     double ssum = 0.0, asum = 0.0;
     {
       double y0, y1;
       penta(y0, y1);
       const double g0 = G00 * y0 + G01 * y1, g1 = G10 * y0 + G11 * y1;
-      border(g0, g1);
+      double xm2 = 0.0, xm1 = 0.0;
+      double x0 = xcor(0, g0, g1), x1 = xcor(1, g0, g1);
+#pragma unroll 4
       for (int m = 0; m < nz; ++m) {
-        const double c = srow(m, g0, g1);
-        double dpv = fp1[m] * XS(m + 1);
-        if (m >= 1) dpv = fm1[m] * XS(m - 1) + dpv;
+        const double x2 = xcor(m + 2, g0, g1);
+        double c = LDG(s0 + m) * x0;
+        if (m >= 2) c = LDG(sm2 + m) * xm2 + c;
+        c = c + LDG(sp2 + m) * x2;
+        if (m == 0) c += a.se0 * g0;
+        if (m == 1) c += a.se1 * g1;
+        double dpv = LDG(fp1 + m) * x1;
+        if (m >= 1) dpv = LDG(fm1 + m) * xm1 + dpv;
         if (m == 0) dpv += a.fe * g1;
         CPS(m) = c;
-        DPS(m) = dpv;
         ssum += c;
         asum += (m & 1) ? -c : c;
+        XS(m) = inv_eta * (dpv - ldp(2, m, part));  // z-velocity RHS (DPTools.cpp:214)
+        xm2 = xm1;
+        xm1 = x0;
+        x0 = x1;
+        x1 = x2;
       }
     }
     // velocity BC right-hand sides (DPTools.cpp:218-234)
@@ -148,28 +168,38 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
     bc[5] = ifac1 * asum;
     __syncwarp();  // the partner's pressure coefficients are read below
 
-    // velocity: three Schur solves (DPTools.cpp:197-216, 287-345)
+    // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
     double wt[3], wb[3];
-    for (int c = 0; c < 3; ++c) {
-      for (int j = 0; j < nz; ++j) {
-        const double f = ldp(c, j, part);
-        double r;
-        if (c == 0) r = (Dx * sp) * CPO(j) - f;
-        else if (c == 1) r = (Dy * sp) * CPO(j) - f;
-        else r = DPS(j) - f;
-        XS(j) = inv_eta * r;
+    for (int cc = 0; cc < 3; ++cc) {
+      const int c = (cc + 2) % 3;  // 2, 0, 1
+      if (c != 2) {
+        const double Dc = (c == 0 ? Dx : Dy) * sp;
+#pragma unroll 4
+        for (int j = 0; j < nz; ++j) XS(j) = inv_eta * (Dc * CPO(j) - ldp(c, j, part));
       }
       double y0, y1;
       penta(y0, y1);
       const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
       const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
-      border(g0, g1);
       double st = 0.0, sb = 0.0;
+      double xm2 = 0.0;
+      double xm1 = 0.0;
+      double x0 = xcor(0, g0, g1), x1 = xcor(1, g0, g1);
+#pragma unroll 4
       for (int m = 0; m < nz; ++m) {
-        const double u = srow(m, g0, g1);
+        const double x2 = xcor(m + 2, g0, g1);
+        double u = LDG(s0 + m) * x0;
+        if (m >= 2) u = LDG(sm2 + m) * xm2 + u;
+        u = u + LDG(sp2 + m) * x2;
+        if (m == 0) u += a.se0 * g0;
+        if (m == 1) u += a.se1 * g1;
         if (store) spec[(((int64_t)c * nz + m) * nk + i) * 2 + part] = (R)u;
         st += u;
         sb += (m & 1) ? -u : u;
+        xm2 = xm1;
+        xm1 = x0;
+        x0 = x1;
+        x1 = x2;
       }
       wt[c] = st;
       wb[c] = sb;
@@ -207,7 +237,6 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
 #undef XS
 #undef CPS
 #undef CPO
-#undef DPS
 }
 
 // k = 0: open domain -> zero; walls -> u, v from the k = 0 BVP with the
@@ -251,26 +280,38 @@ __global__ void k_bvp_k0(KsArgs a, R *__restrict__ spec) {
   for (int j = 0; j < nz; ++j) at(2, j) = (R)0;
 }
 
+// Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
-cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, int nsm, cudaStream_t s) {
-  const size_t smem = sizeof(double) * (size_t)(3 * a.nz + 2) * BVP_LANES;
+cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  const size_t smem = sizeof(double) * (size_t)(a.nz + 2) * BVP_LANES;
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs<R>, BVP_LANES, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int64_t ntiles = (a.nk + 31) / 32;
-  int64_t grid = (int64_t)nsm * per_sm;
-  if (grid > ntiles) grid = ntiles;
-  k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr);
-  err = cudaGetLastError();
+  int64_t ntiles = (a.nk + BVP_MODES - 1) / BVP_MODES;
+  int64_t g = (int64_t)nsm * per_sm;
+  if (g > ntiles) g = ntiles;
+  *grid = g;
+  *scratch_bytes = sizeof(double) * (size_t)a.nz * (size_t)g * BVP_LANES;
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
+                       cudaStream_t s) {
+  const size_t smem = sizeof(double) * (size_t)(a.nz + 2) * BVP_LANES;
+  k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch);
+  cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_bvp_k0<R><<<1, 32, 0, s>>>(a, spec);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_bvp<float>(const KsArgs &, float *, double2 *, int, cudaStream_t);
-template cudaError_t launch_bvp<double>(const KsArgs &, double *, double2 *, int, cudaStream_t);
+template cudaError_t bvp_plan<float>(const KsArgs &, int, int64_t *, size_t *);
+template cudaError_t bvp_plan<double>(const KsArgs &, int, int64_t *, size_t *);
+template cudaError_t launch_bvp<float>(const KsArgs &, float *, double2 *, double *, int64_t, cudaStream_t);
+template cudaError_t launch_bvp<double>(const KsArgs &, double *, double2 *, double *, int64_t, cudaStream_t);
 
 }  // namespace dpst

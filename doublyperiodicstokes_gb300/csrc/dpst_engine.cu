@@ -47,7 +47,10 @@ void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, 
 
 void launch_bvp_factors(const KsArgs &a, cudaStream_t s);
 template <typename R>
-cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, int nsm, cudaStream_t s);
+cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
+                       cudaStream_t s);
 template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s);
@@ -240,6 +243,8 @@ struct Engine : EngineBase {
   GridArgs g;
   KsArgs ks;
   // device buffers
+  DevBuf bvp_scratch;
+  int64_t bvp_grid = 0;
   DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g;
   DevBuf pos64, flags;
@@ -413,6 +418,9 @@ struct Engine : EngineBase {
     grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
     spec.alloc(sizeof(CR) * 3 * (size_t)nz * nk);
     if (p.mode != DPST_MODE_NOWALL) corr.alloc(sizeof(double2) * 16 * (size_t)nk);
+    size_t bvp_bytes = 0;
+    DPST_CUDA(bvp_plan<R>(ks, nsm, &bvp_grid, &bvp_bytes));
+    bvp_scratch.alloc(bvp_bytes);
     // particle buffers
     pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
     flags.alloc(sizeof(int) * 8);
@@ -590,7 +598,7 @@ struct Engine : EngineBase {
     ef.ks = ks;
     DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s));
     mark(3, s);
-    DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), nsm, s));
+    DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
     mark(4, s);
     EpiArgs eb = ef;
     eb.inverse = 1;
@@ -654,7 +662,7 @@ struct Engine : EngineBase {
     o->ghost_layers_in_use = nbuf;
     o->kernels_per_mdot = (p.has_torque ? 2 : 1) + 2 * nbuf + 1 + 2 + 1 + (p.has_torque ? 2 : 1);
     int64_t b = 0;
-    const DevBuf *all[] = {&grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
+    const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1,
                            &fac_g, &pos64, &flags, &dphzw_buf};
     for (const DevBuf *d : all) b += d->bytes;
