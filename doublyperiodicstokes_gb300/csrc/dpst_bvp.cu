@@ -35,93 +35,95 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
                                                          double *__restrict__ cp_scratch) {
   extern __shared__ double bvp_sm[];
   const int nz = a.nz;
-  const int64_t nk = a.nk;
+  const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
   const int tid = threadIdx.x, part = tid & 1, q = tid >> 1;
-  const int T = BVP_LANES;
+  constexpr int T = BVP_LANES;
   double *Xs = bvp_sm;  // [(nz + 2)][T] penta / RHS column
+  // integration-matrix bands, identical for every wavenumber
+  double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
+  for (int t = tid; t < nz; t += T) {
+    S0[t] = a.s0[t];
+    SM2[t] = a.sm2[t];
+    SP2[t] = a.sp2[t];
+    FM1[t] = a.fm1[t];
+    FP1[t] = a.fp1[t];
+  }
+  __syncthreads();
   // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
   // in global memory (L2 resident: a few tens of MB)
-  const int64_t GT = (int64_t)gridDim.x * T;
-  double *__restrict__ CPs = cp_scratch + (int64_t)blockIdx.x * T;
+  const int GT = gridDim.x * T;
+  double *__restrict__ CPs = cp_scratch + blockIdx.x * T + tid;   // row j at CPs[j * GT]
+  const double *__restrict__ CPo = cp_scratch + blockIdx.x * T + (tid ^ 1);
 #define XS(j) Xs[(j) * T + tid]
-#define CPS(j) CPs[(int64_t)(j) * GT + tid]
-#define CPO(j) CPs[(int64_t)(j) * GT + (tid ^ 1)]
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
   const double inv_eta = 1.0 / a.eta;
-  const double *__restrict__ s0 = a.s0;
-  const double *__restrict__ sp2 = a.sp2;
-  const double *__restrict__ sm2 = a.sm2;
-  const double *__restrict__ fm1 = a.fm1;
-  const double *__restrict__ fp1 = a.fp1;
-  const int64_t ntiles = (nk + BVP_MODES - 1) / BVP_MODES;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t i_raw = tile * BVP_MODES + q;
-    const int64_t i = i_raw < nk ? i_raw : nk - 1;
+  const int rs = 2 * nk;  // spectrum row stride (R elements)
+  const int ntiles = (nk + BVP_MODES - 1) / BVP_MODES;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i_raw = tile * BVP_MODES + q;
+    const int i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0 is solved by k_bvp_k0
-    auto ldp = [&](int d, int j, int pp) -> double {
-      return (double)spec[(((int64_t)d * nz + j) * nk + i) * 2 + pp];
-    };
-    const int ix = (int)(i % a.nxh), iy = (int)(i / a.nxh);
-    const double kx = LDG(a.kvx + ix), ky = LDG(a.kvy + iy);
+    // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
+    R *__restrict__ sp_own = spec + 2 * i + part;
+    const R *__restrict__ sp_oth = spec + 2 * i + (part ^ 1);
+    const int ix = i % a.nxh, iy = i / a.nxh;
+    const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
     const double Dx = ((a.nx % 2) == 0 && ix == a.nx / 2) ? 0.0 : kx;
     const double Dy = ((a.ny % 2) == 0 && iy == a.ny / 2) ? 0.0 : ky;
     const double K = sqrt(kx * kx + ky * ky);
-    const double *__restrict__ mf = a.mfac + i;
-    const double *__restrict__ ib = a.invb + i;
-    const double *__restrict__ d2 = a.dp2 + i;
-    const double *__restrict__ A0 = a.ab0 + i;
-    const double *__restrict__ A1 = a.ab1 + i;
-    const double *__restrict__ C0 = a.c0 + i;
-    const double *__restrict__ C1 = a.c1 + i;
-    const double G00 = LDG(a.ginv + i), G10 = LDG(a.ginv + nk + i);
-    const double G01 = LDG(a.ginv + 2 * nk + i), G11 = LDG(a.ginv + 3 * nk + i);
+    const double G00 = __ldg(a.ginv + i), G10 = __ldg(a.ginv + nk + i);
+    const double G01 = __ldg(a.ginv + 2 * nk + i), G11 = __ldg(a.ginv + 3 * nk + i);
+    const double *__restrict__ mf0 = a.mf + i;
+    const double2 *__restrict__ bk0 = reinterpret_cast<const double2 *>(a.bk) + 2 * i;
+    const double *__restrict__ ab0 = a.ab + i;
 
     // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j
     {
       double dfp1 = 0.0, dfp2 = 0.0, fzn = 0.0;
-#pragma unroll 4
+      const R *f0o = sp_oth + (nz - 1) * rs, *f1o = f0o + nz * rs;
+      const R *f2s = sp_own + (2 * nz + nz - 1) * rs;
       for (int j = nz - 1; j >= 0; --j) {
         const double df = (j == nz - 1) ? 0.0 : dfp2 + ((double)((j + 1) * 2) / a.H) * fzn;
-        const double fz = ldp(2, j, part);
+        const double fz = (double)*f2s;
         const double dfv = (j == 0) ? 0.5 * df : df;
-        XS(j) = ((Dx * sp) * ldp(0, j, part ^ 1) + (Dy * sp) * ldp(1, j, part ^ 1)) + dfv;
+        XS(j) = ((Dx * sp) * (double)*f0o + (Dy * sp) * (double)*f1o) + dfv;
         dfp2 = dfp1;
         dfp1 = df;
         fzn = fz;
+        f0o -= rs;
+        f1o -= rs;
+        f2s -= rs;
       }
     }
     // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
-    // border dots y = C x accumulated during the back sweep
+    // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
+    // mf and the dp2 of the last two rows are zero, so both loops are uniform.
     auto penta = [&](double &y0, double &y1) {
-      double xm2 = XS(0), xm1 = XS(1);
+      double xm2 = 0.0, xm1 = 0.0;
+      const double *p = mf0;
 #pragma unroll 8
-      for (int j = 2; j < nz; ++j) {
-        const double v = XS(j) - LDG(mf + j * nk) * xm2;
+      for (int j = 0; j < nz; ++j) {
+        const double v = XS(j) - __ldg(p) * xm2;
         XS(j) = v;
         xm2 = xm1;
         xm1 = v;
+        p += nk;
       }
-      const double xl = LDG(ib + nz * nk) * xm1;
-      const double xl2 = LDG(ib + (nz - 1) * nk) * xm2;
-      XS(nz - 1) = xl;
-      XS(nz - 2) = xl2;
-      y0 = LDG(C0 + (nz - 1) * nk) * xl + LDG(C0 + (nz - 2) * nk) * xl2;
-      y1 = LDG(C1 + (nz - 1) * nk) * xl + LDG(C1 + (nz - 2) * nk) * xl2;
-      double xp2 = xl, xp1 = xl2;
+      double xp2 = 0.0, xp1 = 0.0;
+      y0 = 0.0;
+      y1 = 0.0;
+      const double2 *b = bk0 + (nz - 1) * rs;
 #pragma unroll 8
-      for (int j = nz - 3; j >= 0; --j) {
-        const double v = LDG(ib + (j + 1) * nk) * (XS(j) - LDG(d2 + j * nk) * xp2);
+      for (int j = nz - 1; j >= 0; --j) {
+        const double2 ibd = __ldg(b), cc = __ldg(b + 1);
+        const double v = ibd.x * (XS(j) - ibd.y * xp2);
         XS(j) = v;
-        y0 += LDG(C0 + j * nk) * v;
-        y1 += LDG(C1 + j * nk) * v;
+        y0 += cc.x * v;
+        y1 += cc.y * v;
         xp2 = xp1;
         xp1 = v;
+        b -= rs;
       }
-    };
-    // border-corrected solution x_j = X_j - (A0_j g0 + A1_j g1); x_nz = g0, x_nz+1 = g1
-    auto xcor = [&](int j, double g0, double g1) -> double {
-      if (j < nz) return XS(j) - (LDG(A0 + j * nk) * g0 + LDG(A1 + j * nk) * g1);
-      return j == nz ? g0 : g1;
     };
 
     // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
@@ -131,27 +133,34 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
       double y0, y1;
       penta(y0, y1);
       const double g0 = G00 * y0 + G01 * y1, g1 = G10 * y0 + G11 * y1;
+      // border-corrected x_j = X_j - A^{-1}B_j g (x_nz = g0, x_nz+1 = g1)
+      const double *abp = ab0 + 2 * nk;
       double xm2 = 0.0, xm1 = 0.0;
-      double x0 = xcor(0, g0, g1), x1 = xcor(1, g0, g1);
+      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
+      const R *f2s = sp_own + 2 * nz * rs;
+      double *cpw = CPs;
 #pragma unroll 4
       for (int m = 0; m < nz; ++m) {
-        const double x2 = xcor(m + 2, g0, g1);
-        double c = LDG(s0 + m) * x0;
-        if (m >= 2) c = LDG(sm2 + m) * xm2 + c;
-        c = c + LDG(sp2 + m) * x2;
+        const double x2 = (m + 2 < nz) ? XS(m + 2) - __ldg(abp) * ((m & 1) ? g1 : g0) : ((m + 2 == nz) ? g0 : g1);
+        double c = S0[m] * x0;
+        if (m >= 2) c = SM2[m] * xm2 + c;
+        c = c + SP2[m] * x2;
         if (m == 0) c += a.se0 * g0;
         if (m == 1) c += a.se1 * g1;
-        double dpv = LDG(fp1 + m) * x1;
-        if (m >= 1) dpv = LDG(fm1 + m) * xm1 + dpv;
+        double dpv = FP1[m] * x1;
+        if (m >= 1) dpv = FM1[m] * xm1 + dpv;
         if (m == 0) dpv += a.fe * g1;
-        CPS(m) = c;
+        *cpw = c;
         ssum += c;
         asum += (m & 1) ? -c : c;
-        XS(m) = inv_eta * (dpv - ldp(2, m, part));  // z-velocity RHS (DPTools.cpp:214)
+        XS(m) = inv_eta * (dpv - (double)*f2s);  // z-velocity RHS (DPTools.cpp:214)
         xm2 = xm1;
         xm1 = x0;
         x0 = x1;
         x1 = x2;
+        abp += nk;
+        f2s += rs;
+        cpw += GT;
       }
     }
     // velocity BC right-hand sides (DPTools.cpp:218-234)
@@ -174,32 +183,41 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
       const int c = (cc + 2) % 3;  // 2, 0, 1
       if (c != 2) {
         const double Dc = (c == 0 ? Dx : Dy) * sp;
+        const R *fs = sp_own + c * nz * rs;
+        const double *cpo = CPo;
 #pragma unroll 4
-        for (int j = 0; j < nz; ++j) XS(j) = inv_eta * (Dc * CPO(j) - ldp(c, j, part));
+        for (int j = 0; j < nz; ++j) {
+          XS(j) = inv_eta * (Dc * *cpo - (double)*fs);
+          fs += rs;
+          cpo += GT;
+        }
       }
       double y0, y1;
       penta(y0, y1);
       const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
       const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
       double st = 0.0, sb = 0.0;
-      double xm2 = 0.0;
-      double xm1 = 0.0;
-      double x0 = xcor(0, g0, g1), x1 = xcor(1, g0, g1);
+      const double *abp = ab0 + 2 * nk;
+      double xm2 = 0.0, xm1 = 0.0;
+      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
+      R *us = sp_own + c * nz * rs;
 #pragma unroll 4
       for (int m = 0; m < nz; ++m) {
-        const double x2 = xcor(m + 2, g0, g1);
-        double u = LDG(s0 + m) * x0;
-        if (m >= 2) u = LDG(sm2 + m) * xm2 + u;
-        u = u + LDG(sp2 + m) * x2;
+        const double x2 = (m + 2 < nz) ? XS(m + 2) - __ldg(abp) * ((m & 1) ? g1 : g0) : ((m + 2 == nz) ? g0 : g1);
+        double u = S0[m] * x0;
+        if (m >= 2) u = SM2[m] * xm2 + u;
+        u = u + SP2[m] * x2;
         if (m == 0) u += a.se0 * g0;
         if (m == 1) u += a.se1 * g1;
-        if (store) spec[(((int64_t)c * nz + m) * nk + i) * 2 + part] = (R)u;
+        if (store) *us = (R)u;
         st += u;
         sb += (m & 1) ? -u : u;
         xm2 = xm1;
         xm1 = x0;
         x0 = x1;
         x1 = x2;
+        abp += nk;
+        us += rs;
       }
       wt[c] = st;
       wb[c] = sb;
@@ -235,8 +253,6 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
     }
   }
 #undef XS
-#undef CPS
-#undef CPO
 }
 
 // k = 0: open domain -> zero; walls -> u, v from the k = 0 BVP with the
@@ -283,13 +299,14 @@ __global__ void k_bvp_k0(KsArgs a, R *__restrict__ spec) {
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * (size_t)(a.nz + 2) * BVP_LANES;
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 5 * (size_t)a.nz);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs<R>, BVP_LANES, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if ((int64_t)a.nz * a.nk * 4 >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
   int64_t ntiles = (a.nk + BVP_MODES - 1) / BVP_MODES;
   int64_t g = (int64_t)nsm * per_sm;
   if (g > ntiles) g = ntiles;
@@ -301,7 +318,7 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s) {
-  const size_t smem = sizeof(double) * (size_t)(a.nz + 2) * BVP_LANES;
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 5 * (size_t)a.nz);
   k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;

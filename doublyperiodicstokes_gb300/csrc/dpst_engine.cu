@@ -246,7 +246,7 @@ struct Engine : EngineBase {
   DevBuf bvp_scratch;
   int64_t bvp_grid = 0;
   DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
-  DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g;
+  DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g, fac_pm, fac_pb, fac_pa;
   DevBuf pos64, flags;
   DevBuf st_m[8], st_d[8];
   DevBuf gh_m[2], gh_d[2];
@@ -412,8 +412,18 @@ struct Engine : EngineBase {
     ks.c0 = fac_c0.as<double>(); ks.c1 = fac_c1.as<double>(); ks.ginv = fac_g.as<double>();
     ks.k0c0 = k0rows.as<double>(); ks.k0c1 = k0rows.as<double>() + nz;
     for (int q = 0; q < 4; ++q) ks.k0gi[q] = k0gi[q];
+    fac_pm.alloc(sizeof(double) * nz * nk);
+    fac_pb.alloc(sizeof(double) * 4 * nz * nk);
+    fac_pa.alloc(sizeof(double) * nz * nk);
+    ks.mf = fac_pm.as<double>();
+    ks.bk = fac_pb.as<double>();
+    ks.ab = fac_pa.as<double>();
     launch_bvp_factors(ks, 0);
     DPST_CUDA(cudaGetLastError());
+    DPST_CUDA(cudaDeviceSynchronize());
+    // the unpacked working arrays are no longer needed
+    for (DevBuf *b : {&fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1}) b->release();
+    ks.mfac = ks.invb = ks.dp2 = ks.ab0 = ks.ab1 = ks.c0 = ks.c1 = nullptr;
     // grids, spectrum, correction coefficients, BVP scratch
     grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
     spec.alloc(sizeof(CR) * 3 * (size_t)nz * nk);
@@ -663,7 +673,7 @@ struct Engine : EngineBase {
     o->kernels_per_mdot = (p.has_torque ? 2 : 1) + 2 * nbuf + 1 + 2 + 1 + (p.has_torque ? 2 : 1);
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
-                           &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1,
+                           &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
                            &fac_g, &pos64, &flags, &dphzw_buf};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;

@@ -79,8 +79,16 @@ struct KsArgs {
   double se0, se1, fe;
   // BC rows (length nz + 2 each) of the reference (Solvers.py:603-643)
   const double *bcr1, *bcr2, *bcl1, *bcl2;
-  // per-mode factors, [index][nk]
+  // per-mode factors as computed, [index][nk] (k_bvp_factors' working arrays)
   double *mfac, *invb, *dp2, *ab0, *ab1, *c0, *c1, *ginv;
+  // packed factors read by the solve (k_bvp_pack):
+  //   mf [nz][nk]     forward-sweep multipliers (rows 0, 1 are zero)
+  //   bk [nz][nk][4]  back-sweep row data {1/beta_{j+1}, dp2_j, C0_j, C1_j}
+  //                   (dp2 zero on the last two rows)
+  //   ab [nz][nk]     border column of A^{-1}B: column 0 on even rows, column 1
+  //                   on odd rows (A couples j with j +- 2 only, so each column
+  //                   vanishes exactly on the other parity)
+  double *mf, *bk, *ab;
   // k = 0 velocity correction: C rows (length nz) and Gi row-major
   const double *k0c0, *k0c1;
   double k0gi[4];

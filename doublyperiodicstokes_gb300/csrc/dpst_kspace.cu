@@ -113,6 +113,25 @@ __global__ void k_bvp_factors(KsArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Repack the factors for the solve (layouts documented on KsArgs).
+// ---------------------------------------------------------------------------
+__global__ void k_bvp_pack(KsArgs a) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nk = a.nk;
+  if (t >= (int64_t)a.nz * nk) return;
+  const int j = (int)(t / nk);
+  const int64_t i = t - (int64_t)j * nk;
+  a.mf[t] = (j >= 2) ? a.mfac[t] : 0.0;
+  double4 b;
+  b.x = a.invb[(int64_t)(j + 1) * nk + i];
+  b.y = (j < a.nz - 2) ? a.dp2[t] : 0.0;
+  b.z = a.c0[t];
+  b.w = a.c1[t];
+  reinterpret_cast<double4 *>(a.bk)[t] = b;
+  a.ab[t] = (j & 1) ? a.ab1[t] : a.ab0[t];
+}
+
+// ---------------------------------------------------------------------------
 // z transform GEMM.  OUT[r][col] = sum_m Tm[r][m] IN[m][col] for the real
 // view of spec (per component: nz rows x ncols = 2*nk columns), in place.
 // CTA: 256 threads, tile = all rows x 64 columns; each thread 4 columns x RPT
@@ -264,6 +283,8 @@ __global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, c
 void launch_bvp_factors(const KsArgs &a, cudaStream_t s) {
   int bs = 128;
   k_bvp_factors<<<(a.nk + bs - 1) / bs, bs, 0, s>>>(a);
+  int64_t tot = (int64_t)a.nz * a.nk;
+  k_bvp_pack<<<(tot + 255) / 256, 256, 0, s>>>(a);
 }
 
 
