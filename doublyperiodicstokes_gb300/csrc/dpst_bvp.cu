@@ -22,6 +22,8 @@
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
 
+#include <mutex>
+
 namespace dpst {
 
 constexpr int BVP_LANES = 192;  // 96 wavenumbers per CTA
@@ -326,6 +328,72 @@ cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch,
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free launch of the same solve for dpst_mdot_noalloc.
+//
+// Some callers cannot allocate device memory at the moment they need the
+// operator: code that runs inside a CUDA stream capture in global capture
+// mode (cudaMalloc is not permitted there), or a host whose own allocator has
+// already reserved the device.  For them the solve's scratch (the pressure
+// coefficients of every lane, nz doubles per lane) comes from the file-scope
+// array below instead of memory owned by the handle.  The array is 4 MiB;
+// every GPU that loads the library holds it until the process exits.  The
+// solve writes each lane's scratch before reading it, so nothing needs
+// clearing between calls, but all calls share the one array: calls that
+// overlap on the GPU (other streams, other handles, other threads) race on
+// it and must be serialised by the caller.  The kernel is launched on as many
+// CTAs as the array holds (192 lanes x nz doubles each), at most the grid of
+// the ordinary solve.
+// ---------------------------------------------------------------------------
+constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)1 << 19;  // 4 MiB
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[256];  // device address of the array, per device
+
+// The symbol's device address is looked up once per device, with that
+// device current, on the first call there (so that first call must not be
+// made during a stream capture).  In host code the array's name is only a
+// host-side stand-in and must never be passed to a kernel.
+static cudaError_t noalloc_scratch_ptr(double **out) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void *p = nullptr;
+    err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess) return err;
+    g_noalloc_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+// Returns cudaErrorInvalidValue and sets *too_big when one CTA's scratch
+// (nz x 192 doubles) exceeds the array.
+template <typename R>
+cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t planned_grid,
+                               cudaStream_t s, bool *too_big) {
+  *too_big = false;
+  const size_t per_cta = (size_t)a.nz * BVP_LANES;
+  if (per_cta > NOALLOC_SCRATCH_DOUBLES) {
+    *too_big = true;
+    return cudaErrorInvalidValue;
+  }
+  double *scratch = nullptr;
+  cudaError_t err = noalloc_scratch_ptr(&scratch);
+  if (err != cudaSuccess) return err;
+  int64_t grid = (int64_t)(NOALLOC_SCRATCH_DOUBLES / per_cta);
+  if (grid > planned_grid) grid = planned_grid;
+  return launch_bvp<R>(a, spec, corr, scratch, grid, s);
+}
+
+size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_DOUBLES * sizeof(double); }
+
+template cudaError_t launch_bvp_noalloc<float>(const KsArgs &, float *, double2 *, int64_t, cudaStream_t, bool *);
+template cudaError_t launch_bvp_noalloc<double>(const KsArgs &, double *, double2 *, int64_t, cudaStream_t, bool *);
 template cudaError_t bvp_plan<float>(const KsArgs &, int, int64_t *, size_t *);
 template cudaError_t bvp_plan<double>(const KsArgs &, int, int64_t *, size_t *);
 template cudaError_t launch_bvp<float>(const KsArgs &, float *, double2 *, double *, int64_t, cudaStream_t);

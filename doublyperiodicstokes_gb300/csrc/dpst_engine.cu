@@ -52,6 +52,10 @@ template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s);
 template <typename R>
+cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t planned_grid,
+                               cudaStream_t s, bool *too_big);
+size_t noalloc_scratch_bytes();
+template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s);
 
@@ -224,6 +228,7 @@ struct EngineBase {
   virtual ~EngineBase() {}
   virtual void set_positions(const void *pos, int dtype, cudaStream_t s) = 0;
   virtual void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
+  bool use_static_scratch = false;  // set by dpst_mdot_noalloc for one call
   virtual void info(dpst_info *o) const = 0;
   virtual void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) = 0;
   virtual void velocity_grid(void *out, cudaStream_t s) = 0;
@@ -608,7 +613,18 @@ struct Engine : EngineBase {
     ef.ks = ks;
     DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s));
     mark(3, s);
-    DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
+    if (!use_static_scratch) {
+      DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
+    } else {
+      bool too_big = false;
+      cudaError_t e = launch_bvp_noalloc<R>(ks, (R *)sp, corr.as<double2>(), bvp_grid, s, &too_big);
+      if (too_big)
+        throw Error(DPST_ERR_UNSUPPORTED,
+                    "dpst_mdot_noalloc: one CTA of the solve needs nz*192 = " + std::to_string(nz * 192) +
+                        " doubles of scratch, more than the static array's " +
+                        std::to_string(noalloc_scratch_bytes() / sizeof(double)));
+      DPST_CUDA(e);
+    }
     mark(4, s);
     EpiArgs eb = ef;
     eb.inverse = 1;
@@ -863,6 +879,21 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
       throw;
     }
     h->e->stage_ms = nullptr;
+  });
+}
+
+int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->use_static_scratch = true;
+    try {
+      h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
+    } catch (...) {
+      h->e->use_static_scratch = false;
+      throw;
+    }
+    h->e->use_static_scratch = false;
   });
 }
 

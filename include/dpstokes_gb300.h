@@ -154,6 +154,26 @@ int dpst_velocity_grid(dpst_handle h, void *grid_out, void *stream);
 int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
                     void *stream, float *stage_ms);
 
+/* Allocation-free Mdot.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they call the
+ * operator -- code running inside a CUDA stream capture in global capture
+ * mode, where cudaMalloc is not permitted, or a host whose own allocator has
+ * reserved the device.  Same arguments and results as dpst_mdot; the call
+ * allocates nothing (no cudaMalloc / cudaFree, no allocating library
+ * routine): the per-wavenumber solve takes its scratch from a 4 MiB static
+ * device array compiled into the library (held by every GPU that loads it
+ * until the process exits) instead of memory owned by the handle, and runs
+ * on as many CTAs as that array holds.  Limits and rules:
+ *   - grids needing more than 4 MiB of solve scratch per CTA (nz x 192
+ *     doubles) are rejected with DPST_ERR_UNSUPPORTED; every nz the library
+ *     accepts (<= 128) fits;
+ *   - the first call on a device looks up the array's device address with
+ *     that device current; make that first call before any stream capture;
+ *   - all calls share the one array: calls that overlap on the GPU (other
+ *     streams, handles or threads) race on it and must be serialised. */
+int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
+                      void *stream);
+
 /* Sizes and derived constants of a handle. */
 int dpst_get_info(dpst_handle h, dpst_info *out);
 
