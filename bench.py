@@ -108,8 +108,8 @@ def algorithmic_bytes(stage, w, prec):
     grid = 3 * w.nx * w.ny * w.nz * s
     spec = 3 * nk * w.nz * 2 * s
     if stage == "solve":
-        # spectrum in and out, per-wavenumber factors (7 nz + 4 FP64 values)
-        return 2 * spec + nk * (7 * w.nz + 4) * 8
+        # spectrum in and out, per-wavenumber factors (6 nz + 4 FP64 values)
+        return 2 * spec + nk * (6 * w.nz + 4) * 8
     if stage in ("ztrans_fwd", "ztrans_inv"):
         return 2 * spec
     if stage in ("fft_fwd", "fft_inv"):

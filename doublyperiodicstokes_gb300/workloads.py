@@ -81,7 +81,11 @@ C2 = Workload("c2_dp_n65536", "DP", 65536, 512.0, 512.0, 512, 512, 128, -20.5, 4
               True, betam_hat=1.3267, betad_hat=2.2160)
 C3 = Workload("c3_dpbw_n8192", "DPBW", 8192, 192.0, 192.0, 192, 192, 64, 0.0, 24.0, 1.5, 22.5,
               False, betam_hat=1.714)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3)}
+# The c2 geometry (open domain, nz = 128, Lz = 41, torques) on a 192 x 192 grid:
+# a few-hundred-MB case for ncu captures of the c2 kernels.
+P2 = Workload("p2_dp_n8192_192", "DP", 8192, 192.0, 192.0, 192, 192, 128, -20.5, 41.0, -16.0, 16.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2)}
 
 
 def fft_friendly(n):
