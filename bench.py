@@ -249,6 +249,44 @@ def run_ours(args, rank, world):
                 roofline=roof, clocks=clocks, w=w)
 
 
+def run_backward(args, dev, precision="fp64"):
+    """Forward and backward (dl/dF and dl/dX of l = <g, M(X) F>) of the
+    differentiation configuration: bottom wall, N = 8192, 192^2 x 64, forces
+    only.  Returns device milliseconds per call of each and their ratio."""
+    import torch
+    from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W
+    w = W.C3
+    X, F, _ = W.make_inputs(w)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    g = np.random.default_rng(12).standard_normal((w.N, 3))
+    op = DPStokes(StokesParams.from_workload(w, precision), w.N, device=dev)
+    op.set_positions(torch.tensor(X, device=dev))
+    Fd = torch.tensor(F, dtype=dt, device=dev)
+    gd = torch.tensor(g, dtype=dt, device=dev)
+    V = torch.empty_like(Fd)
+    k = max(3, min(args.steps, 20))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    fwd = timed(lambda: op.mdot(Fd, None, out=(V, None)))
+    bwd = timed(lambda: op.mdot_backward(Fd, None, gd, need_F=True, need_X=True))
+    op.close()
+    return {"workload": w.name, "precision": precision, "grads": ["F", "X"], "calls": k,
+            "fwd_ms": fwd, "bwd_ms": bwd, "bwd_fwd_ratio": bwd / fwd,
+            "note": "backward recomputes the forward's spread and velocity grid"}
+
+
 def cpu_baseline(w):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
@@ -271,6 +309,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-backward", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -309,6 +348,14 @@ def main():
             "stages_ms": {k: round(v, 4) for k, v in r["stages"].items()},
             "bwd_fwd_ratio": None}
     line.update(r["extra"])
+    if not args.skip_backward:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        bw = run_backward(args, dev)
+        line["backward"] = bw
+        line["bwd_fwd_ratio"] = bw["bwd_fwd_ratio"]
+        if args.precision == "mixed":
+            line["backward_mixed"] = run_backward(args, dev, "mixed")
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(r["w"])
     print(json.dumps(line), flush=True)

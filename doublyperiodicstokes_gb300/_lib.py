@@ -59,6 +59,8 @@ SIGNATURES = {
     "dpst_mdot_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                          ctypes.c_void_p]),
+    "dpst_mdot_backward": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 7
+                           + [ctypes.c_int, ctypes.c_void_p]),
     "dpst_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DpstInfo)]),
     "dpst_last_error": (ctypes.c_char_p, []),
     "dpst_version": (ctypes.c_char_p, []),

@@ -1,0 +1,441 @@
+// Transpose of the wavenumber-space stages of Mdot, for the backward pass.
+//
+// The grid operator L of Mdot (spread grid -> velocity grid) is real and
+// translation invariant in x-y.  With the x-y transforms unnormalised and the
+// 1/(nx ny) folded into the per-mode map, L = C2R o B o R2C where, per
+// half-spectrum mode i,
+//     B_i = (1/(nx ny)) [Ti + Zeff_i W] N_i Tf
+// (Tf / Ti the forward / inverse DCT-I matrices, N_i the no-wall solve of
+// DPTools.cpp:81-345, W the wall evaluation with the sign the correction
+// uses, Zeff_i the wall-correction profiles at the nodes of
+// DPTools.cpp:590-877 averaged with the conjugate of the partner mode's on
+// the self-conjugate columns).  The operators of the partner mode are the
+// conjugates of mode i's, so L^T = C2R o B^H o R2C with
+//     B_i^H = (1/(nx ny)) Tf^T N_i^H [Ti^T + W^T Zeff_i^H].
+// This file holds the mode-local pieces:
+//   k_corr_adj       Zeff_i^H applied to the node-space adjoint field
+//   k_bvp_adj_pairs  N_i^H (with the W^T term added to its input); a lane
+//                    pair per wavenumber as in the forward solve; the
+//                    transposed KBPENTA sweeps reuse the forward factors
+//                    (A = L U, so A^{-T} = L^{-T} U^{-T})
+//   k_bvp_adj_k0     the k = 0 mode
+// Every step is the transpose of the forward kernels' arithmetic, so
+// <g, L f> = <L^T g, f> holds to rounding for any f, g.
+#include "dpst_internal.cuh"
+#include "dpst_kdev.cuh"
+
+namespace dpst {
+
+constexpr int ADJ_LANES = 192;
+constexpr int ADJ_MODES = ADJ_LANES / 2;
+
+// ---------------------------------------------------------------------------
+// Zeff_i^H g per wavenumber from the node-space adjoint spectrum (x-y
+// transform of the adjoint grid, before any z transform).  Output per mode:
+// cadj[0..2] the adjoint of the bottom wall values, cadj[3..5] of the top
+// wall values (slit).  One thread per mode, FP64.  For each pass the forward
+// map is Z(q) (main pass, q = (kx, ky)) or conj(Z(q')) (partner pass), so the
+// adjoint applies Z(q)^H or Z(q')^T: the imaginary entries of Z are
+// conjugated on the main pass only.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_corr_adj(KsArgs a, const R *__restrict__ spec, double2 *__restrict__ cadj) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= a.nk || a.mode == 0) return;
+  double2 *out = cadj + i * 6;
+  if (i == 0) {
+    for (int q = 0; q < 6; ++q) out[q] = make_double2(0, 0);
+    return;
+  }
+  const int nz = a.nz;
+  const int64_t nk = a.nk;
+  const int ix = (int)(i % a.nxh), iy = (int)(i / a.nxh);
+  const double kx = a.kvx[ix], ky = a.kvy[iy];
+  const double k = sqrt(kx * kx + ky * ky);
+  double kxp, kyp;
+  const bool herm = mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp);
+  auto g = [&](int d, int m) -> double2 {
+    const R *p = spec + (((int64_t)d * nz + m) * nk + i) * 2;
+    return make_double2((double)p[0], (double)p[1]);
+  };
+  const int npass = herm ? 1 : 2;
+  const double wgt = herm ? 1.0 : 0.5;
+  double2 acc[6];
+  for (int q = 0; q < 6; ++q) acc[q] = make_double2(0, 0);
+  for (int pass = 0; pass < npass; ++pass) {
+    const double qx = pass ? kxp : kx, qy = pass ? kyp : ky;
+    // an entry i c of Z enters as i c (partner pass) or -i c (main pass)
+    const double cs = pass ? 1.0 : -1.0;
+    if (a.mode == 1) {
+      // Z (DPTools.cpp:627-641) per node, symmetric 3x3:
+      //   [e - qx^2 ze/k, -qx qy ze/k, -i qx ze; ., e - qy^2 ze/k, -i qy ze; ., ., e + k ze]
+      for (int m = 0; m < nz; ++m) {
+        const double z = a.zn[m];
+        const double e = exp(-k * z), ze = z * e;
+        const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
+        const double z00 = e - qx * qx * ze / k, z01 = -qx * qy * ze / k;
+        const double z11 = e - qy * qy * ze / k, z22 = e + k * ze;
+        acc[0] = cadd(acc[0], cadd(cadd(cscale(z00, g0), cscale(z01, g1)), cik(cs * (-qx * ze), g2)));
+        acc[1] = cadd(acc[1], cadd(cadd(cscale(z01, g0), cscale(z11, g1)), cik(cs * (-qy * ze), g2)));
+        acc[2] = cadd(acc[2], cadd(cadd(cik(cs * (-qx * ze), g0), cik(cs * (-qy * ze), g1)), cscale(z22, g2)));
+      }
+    } else {
+      // Z = P A^{-1} R (DPTools.cpp:731-815): R maps (fb, ft) to the right
+      // side of the 8x8 system A, P maps its solution to node values
+      const double fac = 1.0 / 2.0 / a.eta, Hs = a.Lz;
+      double2 p[8];
+      for (int q = 0; q < 8; ++q) p[q] = make_double2(0, 0);
+      for (int m = 0; m < nz; ++m) {
+        const double z = a.zn[m];
+        const double e = exp(-k * z), e2 = exp(k * (z - Hs));
+        const double ze = z * e, ze2 = z * e2;
+        const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
+        // P rows: v0 = -i qx ze fac/k c0 + i qx ze2 fac/k c1 + e c2 + e2 c3,
+        // v1 likewise with qy, c4, c5; v2 = ze fac c0 + ze2 fac c1 + e c6 + e2 c7
+        p[0] = cadd(p[0], cadd(cadd(cik(cs * (-qx * ze * fac / k), g0), cik(cs * (-qy * ze * fac / k), g1)),
+                               cscale(ze * fac, g2)));
+        p[1] = cadd(p[1], cadd(cadd(cik(cs * (qx * ze2 * fac / k), g0), cik(cs * (qy * ze2 * fac / k), g1)),
+                               cscale(ze2 * fac, g2)));
+        p[2] = cadd(p[2], cscale(e, g0));
+        p[3] = cadd(p[3], cscale(e2, g0));
+        p[4] = cadd(p[4], cscale(e, g1));
+        p[5] = cadd(p[5], cscale(e2, g1));
+        p[6] = cadd(p[6], cscale(e, g2));
+        p[7] = cadd(p[7], cscale(e2, g2));
+      }
+      // A^{-H} (main) / A^{-T} (partner)
+      double2 A[64], At[64];
+      slit_matrix(qx, qy, Hs, a.eta, A);
+      for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) {
+          const double2 v = A[r + 8 * c];
+          At[c + 8 * r] = pass ? v : cconj(v);
+        }
+      zsolve8(At, p);
+      // R: x0 = -i qx fb0 - i qy fb1, x1 likewise for the top, x2..x4 = fb,
+      // x5..x7 = ft
+      acc[0] = cadd(acc[0], cadd(cik(cs * (-qx), p[0]), p[2]));
+      acc[1] = cadd(acc[1], cadd(cik(cs * (-qy), p[0]), p[3]));
+      acc[2] = cadd(acc[2], p[4]);
+      acc[3] = cadd(acc[3], cadd(cik(cs * (-qx), p[1]), p[5]));
+      acc[4] = cadd(acc[4], cadd(cik(cs * (-qy), p[1]), p[6]));
+      acc[5] = cadd(acc[5], p[7]);
+    }
+  }
+  for (int q = 0; q < 6; ++q) out[q] = cscale(wgt, acc[q]);
+}
+
+// ---------------------------------------------------------------------------
+// N_i^H per wavenumber, in place on the coefficient-space spectrum (in: the
+// adjoint of the velocity coefficients, Ti^T g; out: the adjoint of the force
+// coefficients).  The W^T term is added to the input as it is read: the
+// forward's wall values are fb = -sum_m (-1)^m u_m (z = 0) and
+// ft = -sum_m u_m (z = Lz).  Lane pair per wavenumber (real / imaginary
+// part).  Scratch: cp_bar and dp_bar, each [nz][lanes of the grid].
+//
+// Forward structure (per velocity component c; every operator real):
+//   X = A^{-1} rhs_c, y = C X, g = Ginv (y - bc_c), x = X - AB g,
+//   u_c = S [x; g];  rhs_c = (i D_c cp - f_c)/eta (c = 0, 1),
+//   rhs_2 = (dp - f_2)/eta;
+//   pressure: X = A^{-1} prhs, g = Ginv C X, x = X - AB g, cp = S [x; g],
+//   dp = F [x; g];  prhs = i Dx f0 + i Dy f1 + D f2 (Chebyshev derivative);
+//   bc from ssum = sum cp and asum = sum (-1)^m cp.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__restrict__ spec,
+                                                            const double2 *__restrict__ cadj,
+                                                            double *__restrict__ scratch) {
+  extern __shared__ double adj_sm[];
+  const int nz = a.nz;
+  const int nk = (int)a.nk;
+  const int tid = threadIdx.x, part = tid & 1, q = tid >> 1;
+  constexpr int T = ADJ_LANES;
+  double *Xs = adj_sm;  // [(nz + 2)][T]
+  double *S0 = adj_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
+  for (int t = tid; t < nz; t += T) {
+    S0[t] = a.s0[t];
+    SM2[t] = a.sm2[t];
+    SP2[t] = a.sp2[t];
+    FM1[t] = a.fm1[t];
+    FP1[t] = a.fp1[t];
+  }
+  __syncthreads();
+  const int GT = gridDim.x * T;
+  double *__restrict__ CPb = scratch + blockIdx.x * T + tid;                    // row j at CPb[j * GT]
+  double *__restrict__ DPb = scratch + (size_t)nz * GT + blockIdx.x * T + tid;  // row j at DPb[j * GT]
+#define XS(j) Xs[(j) * T + tid]
+#define XO(j) Xs[(j) * T + (tid ^ 1)]
+  // (i a)_part = sp * a_(other part); (-i a)_part = -sp * a_(other part)
+  const double sp = part ? 1.0 : -1.0;
+  const double inv_eta = 1.0 / a.eta;
+  const int rs = 2 * nk;  // spectrum row stride (R elements) = bk row stride (double2)
+  const int ntiles = (nk + ADJ_MODES - 1) / ADJ_MODES;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int i_raw = tile * ADJ_MODES + q;
+    const int i = i_raw < nk ? i_raw : nk - 1;
+    const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_adj_k0
+    R *__restrict__ own = spec + 2 * i + part;
+    const int ix = i % a.nxh, iy = i / a.nxh;
+    const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
+    const double Dx = ((a.nx % 2) == 0 && ix == a.nx / 2) ? 0.0 : kx;
+    const double Dy = ((a.ny % 2) == 0 && iy == a.ny / 2) ? 0.0 : ky;
+    const double K = sqrt(kx * kx + ky * ky);
+    const double G00 = __ldg(a.ginv + i), G10 = __ldg(a.ginv + nk + i);
+    const double G01 = __ldg(a.ginv + 2 * nk + i), G11 = __ldg(a.ginv + 3 * nk + i);
+    const double *__restrict__ mf0 = a.mf + i;
+    const double2 *__restrict__ bk0 = reinterpret_cast<const double2 *>(a.bk) + 2 * i;
+    const double *__restrict__ ab0 = a.ab + i;
+    double wb_bar[3] = {0, 0, 0}, wt_bar[3] = {0, 0, 0};
+    if (a.mode != 0 && i != 0) {
+      const double *cd = reinterpret_cast<const double *>(cadj + (size_t)i * 6);
+      for (int c = 0; c < 3; ++c) {
+        wb_bar[c] = cd[2 * c + part];
+        if (a.mode == 2) wt_bar[c] = cd[2 * (3 + c) + part];
+      }
+    }
+    // A^{-T} (XS + C^T r) in place on XS: U^T z = b forward, then
+    // L^T x = z backward, with U[j][j] = beta_{j+1}, U[j][j+2] = dp2_j and
+    // L[j][j-2] = mf_j the forward's factors.
+    auto penta_t = [&](double r0, double r1) {
+      double zm2 = 0.0, zm1 = 0.0, d2m2 = 0.0, d2m1 = 0.0;
+      const double2 *b = bk0;
+#pragma unroll 4
+      for (int j = 0; j < nz; ++j) {
+        const double2 ibd = __ldg(b), cc = __ldg(b + 1);
+        const double v = ibd.x * ((XS(j) + (cc.x * r0 + cc.y * r1)) - d2m2 * zm2);
+        XS(j) = v;
+        zm2 = zm1;
+        zm1 = v;
+        d2m2 = d2m1;
+        d2m1 = ibd.y;
+        b += rs;
+      }
+      double xp2 = 0.0, xp1 = 0.0, mp2 = 0.0, mp1 = 0.0;
+      const double *mp = mf0 + (size_t)(nz - 1) * nk;
+#pragma unroll 4
+      for (int j = nz - 1; j >= 0; --j) {
+        const double v = XS(j) - mp2 * xp2;
+        XS(j) = v;
+        xp2 = xp1;
+        xp1 = v;
+        mp2 = mp1;
+        mp1 = __ldg(mp);  // mf_j, used two rows up
+        mp -= nk;
+      }
+    };
+
+    double bcbar[6];
+    for (int c = 0; c < 3; ++c) {
+      R *us = own + c * nz * rs;
+      const double wbb = wb_bar[c], wtb = wt_bar[c];
+      // x_bar = S^T u_bar on the interior rows, then the border adjoints
+      double e0 = 0.0, e1 = 0.0;
+      const double ub0 = (double)us[0] - wbb - wtb, ub1 = (double)us[rs] + wbb - wtb;
+      {
+        double um2 = 0.0, um1 = 0.0, u0 = ub0, u1 = ub1;
+        const R *up = us + 2 * rs;
+        const double *abp = ab0;
+#pragma unroll 4
+        for (int j = 0; j < nz; ++j) {
+          const double u2 = (j + 2 < nz) ? (double)*up - ((j & 1) ? -wbb : wbb) - wtb : 0.0;
+          double x = S0[j] * u0;
+          x += SM2[(j + 2 < nz) ? j + 2 : 0] * u2;
+          x += (j >= 2) ? SP2[j - 2] * um2 : 0.0;
+          XS(j) = x;
+          const double t = __ldg(abp) * x;
+          e0 += (j & 1) ? 0.0 : t;
+          e1 += (j & 1) ? t : 0.0;
+          um2 = um1;
+          um1 = u0;
+          u0 = u1;
+          u1 = u2;
+          up += rs;
+          abp += nk;
+        }
+      }
+      const double gb0 = a.se0 * ub0 - e0, gb1 = a.se1 * ub1 - e1;
+      const double r0 = G00 * gb0 + G10 * gb1, r1 = G01 * gb0 + G11 * gb1;
+      bcbar[2 * c] = -r0;
+      bcbar[2 * c + 1] = -r1;
+      penta_t(r0, r1);  // XS = adjoint of rhs_c
+      __syncwarp();
+      if (c == 2) {
+        double *dpw = DPb;
+        R *fw = us;
+        for (int j = 0; j < nz; ++j) {
+          const double rb = XS(j);
+          *dpw = inv_eta * rb;
+          if (store) *fw = (R)(-inv_eta * rb);
+          dpw += GT;
+          fw += rs;
+        }
+      } else {
+        const double Dc = (c == 0) ? Dx : Dy;
+        double *cpw = CPb;
+        R *fw = us;
+        for (int j = 0; j < nz; ++j) {
+          const double rb = XS(j);
+          const double add = (-sp * Dc * inv_eta) * XO(j);
+          *cpw = (c == 0) ? add : *cpw + add;
+          if (store) *fw = (R)(-inv_eta * rb);
+          cpw += GT;
+          fw += rs;
+        }
+      }
+      __syncwarp();
+    }
+    // bc adjoint -> ssum / asum adjoints; the forward's bc0 = -(i Dx ssum)/fac,
+    // bc1 = (i Dx asum)/fac, bc2, bc3 likewise with Dy, bc4 = ssum/fac1,
+    // bc5 = asum/fac1 (DPTools.cpp:218-234)
+    const double fac1 = 2.0 * a.eta, fac = fac1 * K;
+    const double ifac = 1.0 / fac, ifac1 = 1.0 / fac1;
+    const double b0o = __shfl_xor_sync(0xffffffffu, bcbar[0], 1);
+    const double b1o = __shfl_xor_sync(0xffffffffu, bcbar[1], 1);
+    const double b2o = __shfl_xor_sync(0xffffffffu, bcbar[2], 1);
+    const double b3o = __shfl_xor_sync(0xffffffffu, bcbar[3], 1);
+    const double ssb = (sp * Dx * ifac) * b0o + (sp * Dy * ifac) * b2o + ifac1 * bcbar[4];
+    const double asb = (-sp * Dx * ifac) * b1o + (-sp * Dy * ifac) * b3o + ifac1 * bcbar[5];
+    // pressure: x_bar = S^T cp_bar + F^T dp_bar, border adjoints, A^{-T}
+    {
+      double e0 = 0.0, e1 = 0.0;
+      const double *cpr = CPb, *dpr = DPb;
+      const double c0v = cpr[0] + ssb + asb, c1v = cpr[GT] + ssb - asb;
+      const double d0v = dpr[0];
+      double cm2 = 0.0, cm1 = 0.0, cj = c0v, cj1 = c1v;
+      double dm1 = 0.0, dj = d0v, dj1 = dpr[GT];
+      const double *abp = ab0;
+      cpr += 2 * (size_t)GT;
+      dpr += 2 * (size_t)GT;
+      for (int j = 0; j < nz; ++j) {
+        const double cj2 = (j + 2 < nz) ? *cpr + ssb + ((j & 1) ? -asb : asb) : 0.0;
+        const double dj2 = (j + 2 < nz) ? *dpr : 0.0;
+        double x = S0[j] * cj;
+        x += SM2[(j + 2 < nz) ? j + 2 : 0] * cj2;
+        x += (j >= 2) ? SP2[j - 2] * cm2 : 0.0;
+        x += (j + 1 < nz) ? FM1[j + 1] * dj1 : 0.0;
+        x += (j >= 1) ? FP1[j - 1] * dm1 : 0.0;
+        XS(j) = x;
+        const double t = __ldg(abp) * x;
+        e0 += (j & 1) ? 0.0 : t;
+        e1 += (j & 1) ? t : 0.0;
+        cm2 = cm1;
+        cm1 = cj;
+        cj = cj1;
+        cj1 = cj2;
+        dm1 = dj;
+        dj = dj1;
+        dj1 = dj2;
+        abp += nk;
+        cpr += GT;
+        dpr += GT;
+      }
+      const double gb0 = a.se0 * c0v - e0;
+      const double gb1 = a.se1 * c1v + a.fe * d0v - e1;
+      const double r0 = G00 * gb0 + G10 * gb1, r1 = G01 * gb0 + G11 * gb1;
+      penta_t(r0, r1);  // XS = adjoint of prhs
+    }
+    __syncwarp();
+    // prhs adjoint -> f0 += -i Dx prb, f1 += -i Dy prb, f2 += D^T (df adjoint)
+    // with df_j = sum_{i = j+1, j+3, ...} (2 i / H) f2_i and row 0 halved
+    // (DPTools.cpp:134-174)
+    if (store) {
+      R *f0 = own, *f1 = own + nz * rs, *f2 = own + 2 * nz * rs;
+      double em2 = 0.0, em1 = 0.0;
+      for (int j = 0; j < nz; ++j) {
+        const double prb_o = XO(j);
+        *f0 = (R)((double)*f0 + (-sp * Dx) * prb_o);
+        *f1 = (R)((double)*f1 + (-sp * Dy) * prb_o);
+        double e = 0.0;
+        if (j >= 1) {
+          e = em2 + ((j == 1) ? 0.5 * XS(0) : XS(j - 1));
+          *f2 = (R)((double)*f2 + ((double)(2 * j) / a.H) * e);
+        }
+        em2 = em1;
+        em1 = e;
+        f0 += rs;
+        f1 += rs;
+        f2 += rs;
+      }
+    }
+    __syncwarp();
+  }
+#undef XS
+#undef XO
+}
+
+// k = 0 (walls): U_c = S [r; Gi C r] with r = -f_c/eta (c = 0, 1), U_2 = 0;
+// open domain: zero.  Transposed in place.
+template <typename R>
+__global__ void k_bvp_adj_k0(KsArgs a, R *__restrict__ spec) {
+  const int part = threadIdx.x;
+  if (part > 1) return;
+  const int nz = a.nz;
+  const int64_t nk = a.nk;
+  auto at = [&](int d, int j) -> R & { return spec[(((int64_t)d * nz + j) * nk) * 2 + part]; };
+  if (a.mode == 0) {
+    for (int d = 0; d < 3; ++d)
+      for (int j = 0; j < nz; ++j) at(d, j) = (R)0;
+    return;
+  }
+  double Xb[128];
+  const double inv_eta = 1.0 / a.eta;
+  for (int c = 0; c < 2; ++c) {
+    for (int j = 0; j < nz; ++j) {
+      double x = a.s0[j] * (double)at(c, j);
+      if (j + 2 < nz) x += a.sm2[j + 2] * (double)at(c, j + 2);
+      if (j >= 2) x += a.sp2[j - 2] * (double)at(c, j - 2);
+      Xb[j] = x;
+    }
+    const double gb0 = a.se0 * (double)at(c, 0), gb1 = a.se1 * (double)at(c, 1);
+    // Gi row-major: g0 = Gi00 y0 + Gi01 y1, g1 = Gi10 y0 + Gi11 y1
+    const double t0 = a.k0gi[0] * gb0 + a.k0gi[2] * gb1, t1 = a.k0gi[1] * gb0 + a.k0gi[3] * gb1;
+    for (int j = 0; j < nz; ++j) at(c, j) = (R)(-inv_eta * (Xb[j] + a.k0c0[j] * t0 + a.k0c1[j] * t1));
+  }
+  for (int j = 0; j < nz; ++j) at(2, j) = (R)0;
+}
+
+template <typename R>
+cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 5 * (size_t)a.nz);
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_adj_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_adj_pairs<R>, ADJ_LANES, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t ntiles = (a.nk + ADJ_MODES - 1) / ADJ_MODES;
+  int64_t g = (int64_t)nsm * per_sm;
+  if (g > ntiles) g = ntiles;
+  *grid = g;
+  *scratch_bytes = sizeof(double) * 2 * (size_t)a.nz * (size_t)g * ADJ_LANES;
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_adj_solve(const KsArgs &a, R *spec, const double2 *cadj, double *scratch, int64_t grid,
+                             cudaStream_t s) {
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 5 * (size_t)a.nz);
+  k_bvp_adj_pairs<R><<<(unsigned)grid, ADJ_LANES, smem, s>>>(a, spec, cadj, scratch);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  k_bvp_adj_k0<R><<<1, 32, 0, s>>>(a, spec);
+  return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_corr_adj(const KsArgs &a, const R *spec, double2 *cadj, cudaStream_t s) {
+  if (a.mode == 0) return cudaSuccess;
+  k_corr_adj<R><<<(unsigned)((a.nk + 127) / 128), 128, 0, s>>>(a, spec, cadj);
+  return cudaGetLastError();
+}
+
+template cudaError_t adj_plan<float>(const KsArgs &, int, int64_t *, size_t *);
+template cudaError_t adj_plan<double>(const KsArgs &, int, int64_t *, size_t *);
+template cudaError_t launch_adj_solve<float>(const KsArgs &, float *, const double2 *, double *, int64_t,
+                                             cudaStream_t);
+template cudaError_t launch_adj_solve<double>(const KsArgs &, double *, const double2 *, double *, int64_t,
+                                              cudaStream_t);
+template cudaError_t launch_corr_adj<float>(const KsArgs &, const float *, double2 *, cudaStream_t);
+template cudaError_t launch_corr_adj<double>(const KsArgs &, const double *, double2 *, cudaStream_t);
+
+}  // namespace dpst

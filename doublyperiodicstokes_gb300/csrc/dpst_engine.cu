@@ -58,6 +58,31 @@ size_t noalloc_scratch_bytes();
 template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s);
+// backward pass (dpst_adjoint.cu, dpst_grad.cu)
+template <typename R>
+cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_adj_solve(const KsArgs &a, R *spec, const double2 *cadj, double *scratch, int64_t grid,
+                             cudaStream_t s);
+template <typename R>
+cudaError_t launch_corr_adj(const KsArgs &a, const R *spec, double2 *cadj, cudaStream_t s);
+template <typename R>
+void launch_locate_grad(bool dipole, const double *pos, int64_t N, const KernelDesc &kd, const double *zext,
+                        const double *wext, const GridArgs &g, const Stencils<R> &st, const GradStencils<R> &gs,
+                        cudaStream_t s);
+template <typename R, typename RG>
+void launch_adj_spread_dip(const RG *gW, int64_t N, const KernelDesc &kd, const GridArgs &g, const Stencils<R> &st,
+                           R *grid, const Ghosts<R> &gh, cudaStream_t s);
+template <typename R>
+void launch_ghost_fold_t(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s);
+template <typename R, typename RF>
+void launch_gather_mono(const R *u, const R *psi, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                        const Stencils<R> &st, const GradStencils<R> &gs, const Ghosts<R> &ghu,
+                        const Ghosts<R> &ghp, const RF *F, const RF *gV, RF *gF, RF *gX, cudaStream_t s);
+template <typename R, typename RF>
+void launch_gather_dip(const R *u, const R *psi, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                       const Stencils<R> &st, const GradStencils<R> &gs, const Ghosts<R> &ghu,
+                       const Ghosts<R> &ghp, const RF *T, const RF *gW, RF *gT, RF *gX, cudaStream_t s);
 
 // ---- errors -----------------------------------------------------------------
 struct Error : std::runtime_error {
@@ -223,6 +248,22 @@ static KernelHost make_kernel(int w, double beta, double alpha, bool dipole, dou
   return k;
 }
 
+// DCT-I matrices (Transform.cpp:107-304): tf[j][m] gives Chebyshev
+// coefficient j from node values m, ti[m][j] node value m from coefficient j.
+static void dct_matrices(int nz, std::vector<double> &tf, std::vector<double> &ti) {
+  tf.assign((size_t)nz * nz, 0.0);
+  ti.assign((size_t)nz * nz, 0.0);
+  const int Nm = nz - 1, Nu = 2 * Nm;
+  for (int j = 0; j < nz; ++j)
+    for (int m = 0; m < nz; ++m) {
+      int r = (int)(((int64_t)j * m) % Nu);
+      double c = std::cos(M_PI * (double)r / (double)Nm);
+      double wj = (j == 0 || j == Nm) ? 1.0 : 2.0, vm = (m == 0 || m == Nm) ? 1.0 : 2.0;
+      tf[(size_t)j * nz + m] = wj * vm * c / Nu;
+      ti[(size_t)m * nz + j] = c;
+    }
+}
+
 // ---- the engine -----------------------------------------------------------------
 struct EngineBase {
   virtual ~EngineBase() {}
@@ -232,6 +273,8 @@ struct EngineBase {
   virtual void info(dpst_info *o) const = 0;
   virtual void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) = 0;
   virtual void velocity_grid(void *out, cudaStream_t s) = 0;
+  virtual void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT,
+                        void *gX, int dtype, cudaStream_t s) = 0;
   float *stage_ms = nullptr;  // set by dpst_mdot_timed for one call
   int device = 0;
   int64_t N = 0;
@@ -380,16 +423,8 @@ struct Engine : EngineBase {
     upload(k0rows, k0r);
     // DCT-I matrices (Transform.cpp:107-304): forward = Chebyshev
     // coefficients from node values, inverse = node values from coefficients
-    std::vector<double> tf((size_t)nz * nz), ti((size_t)nz * nz);
-    const int Nm = nz - 1, Nu = 2 * Nm;
-    for (int j = 0; j < nz; ++j)
-      for (int m = 0; m < nz; ++m) {
-        int r = (int)(((int64_t)j * m) % Nu);
-        double c = std::cos(M_PI * (double)r / (double)Nm);
-        double wj = (j == 0 || j == Nm) ? 1.0 : 2.0, vm = (m == 0 || m == Nm) ? 1.0 : 2.0;
-        tf[(size_t)j * nz + m] = wj * vm * c / Nu;
-        ti[(size_t)m * nz + j] = c;
-      }
+    std::vector<double> tf, ti;
+    dct_matrices(nz, tf, ti);
     std::vector<R> tfr(tf.begin(), tf.end()), tir(ti.begin(), ti.end());
     upload(Tf, tfr);
     upload(Ti, tir);
@@ -592,13 +627,10 @@ struct Engine : EngineBase {
     DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
   }
 
-  template <typename RF>
-  void run(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
-    const bool torque = p.has_torque && T != nullptr;
+  // grid (spread forces) -> grid (velocities): x-y FFT, z transform, per-k
+  // solve, inverse z transform with the wall correction, inverse x-y FFT
+  void solve_stage(cudaStream_t s) {
     R *gr = grid.as<R>();
-    mark(0, s);
-    spread_stage<RF>(F, T, s);
-    mark(1, s);
     CR *sp = spec.as<CR>();
     DPST_CUFFT(cufftSetStream(plan_f, s));
     if (sizeof(R) == 8)
@@ -638,6 +670,16 @@ struct Engine : EngineBase {
     else
       DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
     mark(6, s);
+  }
+
+  template <typename RF>
+  void run(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    R *gr = grid.as<R>();
+    mark(0, s);
+    spread_stage<RF>(F, T, s);
+    mark(1, s);
+    solve_stage(s);
     launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s);
     if (p.has_torque && W != nullptr) {
       // without torques the reference's torque grid still holds the last
@@ -653,6 +695,176 @@ struct Engine : EngineBase {
       const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
       for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
     }
+  }
+
+  // ---- backward pass -------------------------------------------------------
+  // Buffers are allocated on the first backward call: the adjoint grid, the
+  // adjoint solve's scratch, the transposed DCT matrices, the position
+  // derivatives of the stencils and the adjoint ghost layers.
+  DevBuf grid2, adj_scratch, TfTn, TiT;
+  int64_t adj_grid = 0;
+  DevBuf gs_m[4], gs_d[8];
+  GradStencils<R> gsm, gsd;
+  DevBuf gha_m[2], gha_d[2];
+  Ghosts<R> gham, ghad;
+  bool grad_ready = false;
+
+  void ensure_grad() {
+    if (!grad_ready) {
+      grid2.alloc(grid.bytes);
+      size_t bytes = 0;
+      DPST_CUDA(adj_plan<R>(ks, nsm, &adj_grid, &bytes));
+      adj_scratch.alloc(bytes);
+      std::vector<double> tf, ti;
+      dct_matrices(nz, tf, ti);
+      const double sc = 1.0 / ((double)nx * (double)ny);
+      std::vector<R> tft((size_t)nz * nz), tit((size_t)nz * nz);
+      for (int r = 0; r < nz; ++r)
+        for (int c = 0; c < nz; ++c) {
+          tft[(size_t)r * nz + c] = (R)(tf[(size_t)c * nz + r] * sc);
+          tit[(size_t)r * nz + c] = (R)ti[(size_t)c * nz + r];
+        }
+      upload(TfTn, tft);
+      upload(TiT, tit);
+      const size_t n = (size_t)std::max<int64_t>(N, 1);
+      memset(&gsm, 0, sizeof(gsm));
+      memset(&gsd, 0, sizeof(gsd));
+      gs_m[0].alloc(sizeof(R) * n * km.d.wx);
+      gs_m[1].alloc(sizeof(R) * n * km.d.wy);
+      gs_m[2].alloc(sizeof(R) * n * km.d.wz_max);
+      gs_m[3].alloc(sizeof(R) * n * km.d.wz_max);
+      gsm.gx = gs_m[0].as<R>();
+      gsm.gy = gs_m[1].as<R>();
+      gsm.gz = gs_m[2].as<R>();
+      gsm.gzw = gs_m[3].as<R>();
+      if (p.has_torque) {
+        const KernelDesc &d = kd.d;
+        const int w[8] = {d.wx, d.wy, d.wz_max, d.wz_max, d.wx, d.wy, d.wz_max, d.wz_max};
+        for (int q = 0; q < 8; ++q) gs_d[q].alloc(sizeof(R) * n * w[q]);
+        gsd.gx = gs_d[0].as<R>();
+        gsd.gy = gs_d[1].as<R>();
+        gsd.gz = gs_d[2].as<R>();
+        gsd.gzw = gs_d[3].as<R>();
+        gsd.gdx = gs_d[4].as<R>();
+        gsd.gdy = gs_d[5].as<R>();
+        gsd.gdz = gs_d[6].as<R>();
+        gsd.gdzw = gs_d[7].as<R>();
+      }
+      grad_ready = true;
+    }
+    // adjoint ghost layers mirror the forward's (which depend on positions)
+    auto mirror = [&](const Ghosts<R> &f, const KernelDesc &d, DevBuf *b, Ghosts<R> &a) {
+      const size_t lev = sizeof(R) * (size_t)d.nyeff * d.nxeff * 3;
+      a = f;
+      if (f.top) {
+        if (b[0].bytes < lev * f.ntop) b[0].alloc(lev * f.ntop);
+        a.top = b[0].as<R>();
+      }
+      if (f.bot) {
+        if (b[1].bytes < lev * f.nbot) b[1].alloc(lev * f.nbot);
+        a.bot = b[1].as<R>();
+      }
+    };
+    mirror(ghm, km.d, gha_m, gham);
+    if (p.has_torque) mirror(ghd, kd.d, gha_d, ghad);
+    else memset(&ghad, 0, sizeof(ghad));
+  }
+
+  // adjoint grid -> psi = L^T (adjoint grid), in place in grid2
+  void adjoint_solve_stage(cudaStream_t s) {
+    R *g2 = grid2.as<R>();
+    CR *sp = spec.as<CR>();
+    DPST_CUFFT(cufftSetStream(plan_f, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)g2, (cufftDoubleComplex *)sp));
+    else
+      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)g2, (cufftComplex *)sp));
+    if (p.mode != DPST_MODE_NOWALL) DPST_CUDA(launch_corr_adj<R>(ks, (const R *)sp, corr.as<double2>(), s));
+    EpiArgs e;
+    memset(&e, 0, sizeof(e));
+    e.inverse = 0;
+    e.scale = 1.0;
+    e.ks = ks;
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TiT.as<R>(), e, nsm, s));
+    DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TfTn.as<R>(), e, nsm, s));
+    DPST_CUFFT(cufftSetStream(plan_b, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)g2));
+    else
+      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)g2));
+  }
+
+  template <typename RF>
+  void run_backward(const RF *F, const RF *T, const RF *gV, const RF *gW, RF *gF, RF *gT, RF *gX,
+                    cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    const bool want_x = gX != nullptr;
+    ensure_grad();
+    R *gr = grid.as<R>(), *g2 = grid2.as<R>();
+    Ghosts<R> none;
+    memset(&none, 0, sizeof(none));
+    // the dipole interpolation reads ghost layers only when torques were spread
+    const Ghosts<R> &ghd_u = torque ? ghd : none;
+    const Ghosts<R> &ghd_a = torque ? ghad : none;
+    if (want_x) {
+      launch_locate_grad<R>(false, pos64.as<double>(), N, km.d, zext.as<double>(), wext.as<double>(), g, stm,
+                            gsm, s);
+      if (p.has_torque)
+        launch_locate_grad<R>(true, pos64.as<double>(), N, kd.d, zext.as<double>(), wext.as<double>(), g, std_,
+                              gsd, s);
+      // velocity grid and ghost layers of the forward, recomputed
+      spread_stage<RF>(F, T, s);
+      solve_stage(s);
+    }
+    // adjoint source J^T (gV, gW) on grid2 and the adjoint ghost layers
+    DPST_CUDA(cudaMemsetAsync(g2, 0, grid2.bytes, s));
+    for (Ghosts<R> *gh : {&gham, &ghad}) {
+      const KernelDesc &d = (gh == &gham) ? km.d : kd.d;
+      const size_t lev = (size_t)d.nyeff * d.nxeff * 3 * sizeof(R);
+      if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
+      if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
+    }
+    Stencils<R> sw = stm;
+    sw.phz = stm.phzw;  // the interpolation's weights
+    launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, gham, s);
+    if (gW) launch_adj_spread_dip<R, RF>(gW, N, kd.d, g, std_, g2, ghd_a, s);
+    launch_ghost_fold_t<R>(gham.top, gham.ntop, nx, ny, km.d, s);
+    launch_ghost_fold_t<R>(gham.bot, gham.nbot, nx, ny, km.d, s);
+    if (torque) {
+      launch_ghost_fold_t<R>(ghad.top, ghad.ntop, nx, ny, kd.d, s);
+      launch_ghost_fold_t<R>(ghad.bot, ghad.nbot, nx, ny, kd.d, s);
+    }
+    DPST_CUDA(cudaGetLastError());
+    adjoint_solve_stage(s);
+    // gathers: S^T psi and the position gradient
+    if (gF || want_x)
+      launch_gather_mono<R, RF>(want_x ? gr : nullptr, g2, N, km.d, g, stm, gsm, ghm, gham, F, gV, gF, gX, s);
+    if (p.has_torque && (gT || (want_x && (torque || gW))))
+      launch_gather_dip<R, RF>(want_x ? gr : nullptr, g2, N, kd.d, g, std_, gsd, ghd_u, ghd_a,
+                               torque ? T : nullptr, gW, gT, gX, s);
+    DPST_CUDA(cudaGetLastError());
+  }
+
+  void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT, void *gX,
+                int dtype, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (N == 0) return;
+    if (gV == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gV must not be NULL");
+    if (gX != nullptr && F == nullptr)
+      throw Error(DPST_ERR_INVALID_ARG, "the position gradient needs the forces F of the forward call");
+    if (gW != nullptr && !p.has_torque)
+      throw Error(DPST_ERR_INVALID_ARG, "gW needs an operator created with torques");
+    if (gT != nullptr && (T == nullptr || !p.has_torque))
+      throw Error(DPST_ERR_INVALID_ARG, "gT needs an operator created with torques and the torques T");
+    if (dtype == DPST_F64)
+      run_backward<double>((const double *)F, (const double *)T, (const double *)gV, (const double *)gW,
+                           (double *)gF, (double *)gT, (double *)gX, s);
+    else if (dtype == DPST_F32)
+      run_backward<float>((const float *)F, (const float *)T, (const float *)gV, (const float *)gW, (float *)gF,
+                          (float *)gT, (float *)gX, s);
+    else
+      throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
   }
 
   void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) override {
@@ -894,6 +1106,15 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
       throw;
     }
     h->e->use_static_scratch = false;
+  });
+}
+
+int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *gV, const void *gW, void *gF,
+                       void *gT, void *gX, int dtype, void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->backward(F, T, gV, gW, gF, gT, gX, dtype, (cudaStream_t)stream);
   });
 }
 

@@ -53,6 +53,17 @@ struct Stencils {
   R *dphzw;
 };
 
+// Derivatives of the stencil factors with respect to the particle's own
+// coordinate, for the position gradient of the backward pass.  Same shapes as
+// the matching Stencils arrays; zero where the forward clamped the offset.
+template <typename R>
+struct GradStencils {
+  R *gx, *gy;     // d phx / d x, d phy / d y
+  R *gz, *gzw;    // d phz / d z, d phzw / d z
+  R *gdx, *gdy;   // dipole kernel: d dphx / d x, d dphy / d y
+  R *gdz, *gdzw;  // dipole kernel: d dphz / d z, d dphzw / d z
+};
+
 // Ghost-layer buffers for open z ends: the reference leaves spread data in
 // the extended grid's ghost layers at 'none' ends and the next interpolation
 // reads it back (Grid::zeroExtGrid only before a spread, Ghostify copies only

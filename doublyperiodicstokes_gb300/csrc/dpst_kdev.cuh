@@ -58,11 +58,9 @@ static __device__ void zsolve8(double2 *A, double2 *x) {
   }
 }
 
-// Slit correction coefficients for wavevector (kx, ky), wall values fb (z=0)
-// and ft (z=Hs) (DPTools.cpp:731-788).
-static __device__ void slit_coeffs(double kx, double ky, double Hs, double eta, const double2 fb[3],
-                            const double2 ft[3], double2 c[8]) {
-  double2 A[64];
+// Matrix of the slit-channel correction system for wavevector (kx, ky),
+// column-major 8x8 (DPTools.cpp:742-768).
+static __device__ void slit_matrix(double kx, double ky, double Hs, double eta, double2 *A) {
   for (int q = 0; q < 64; ++q) A[q] = make_double2(0, 0);
   const double k = sqrt(kx * kx + ky * ky);
   const double fac = 1.0 / 2.0 / eta;
@@ -95,6 +93,14 @@ static __device__ void slit_coeffs(double kx, double ky, double Hs, double eta, 
   AT(7, 6) = make_double2(enkh, 0);
   AT(7, 7) = make_double2(1, 0);
 #undef AT
+}
+
+// Slit correction coefficients for wavevector (kx, ky), wall values fb (z=0)
+// and ft (z=Hs) (DPTools.cpp:731-788).
+static __device__ void slit_coeffs(double kx, double ky, double Hs, double eta, const double2 fb[3],
+                            const double2 ft[3], double2 c[8]) {
+  double2 A[64];
+  slit_matrix(kx, ky, Hs, eta, A);
   // x0 = -i kx fbx - i ky fby ; x1 likewise for the top
   c[0] = csub(cik(-kx, fb[0]), cik(ky, fb[1]));
   c[1] = csub(cik(-kx, ft[0]), cik(ky, ft[1]));

@@ -122,12 +122,12 @@ __global__ void k_bvp_pack(KsArgs a) {
   const int j = (int)(t / nk);
   const int64_t i = t - (int64_t)j * nk;
   a.mf[t] = (j >= 2) ? a.mfac[t] : 0.0;
-  double4 b;
+  double4_32a b;
   b.x = a.invb[(int64_t)(j + 1) * nk + i];
   b.y = (j < a.nz - 2) ? a.dp2[t] : 0.0;
   b.z = a.c0[t];
   b.w = a.c1[t];
-  reinterpret_cast<double4 *>(a.bk)[t] = b;
+  reinterpret_cast<double4_32a *>(a.bk)[t] = b;
   a.ab[t] = (j & 1) ? a.ab1[t] : a.ab0[t];
 }
 

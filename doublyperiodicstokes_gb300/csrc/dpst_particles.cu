@@ -13,22 +13,9 @@
 //   ghost fold / copy  BoundaryConditions.h:22-731
 //   torque curl        SpreadInterpWrapper.cpp:66-107, FCM.py:362-371,411-426
 #include "dpst_internal.cuh"
+#include "dpst_pdev.cuh"
 
 namespace dpst {
-
-__device__ __forceinline__ int wrapi(int i, int n) {
-  int r = i % n;
-  return r < 0 ? r + n : r;
-}
-
-__device__ __forceinline__ double es1(double x, double beta, double alpha2) {
-  return exp(beta * (sqrt(1.0 - x * x / alpha2) - 1.0));
-}
-
-__device__ __forceinline__ double des1(double x, double beta, double alpha2) {
-  double s = sqrt(1.0 - x * x / alpha2);
-  return -beta * x * exp(beta * (s - 1.0)) / (alpha2 * s);
-}
 
 // ---------------------------------------------------------------------------
 // Stencil setup: one thread per particle.  pos is [N][3] with z already
@@ -113,39 +100,6 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t N, KernelDesc k
     }
   }
 }
-
-// Where extended z index kk lands on the interior grid under one BC set.
-// Returns the interior index m (descending z, m = 0 at zmax) and the weight
-// (1 interior, s at a folded ghost, 1+s at an active boundary node).  A
-// ghost layer at an inactive end returns m = -1 (top) or -2 (bottom) and its
-// level in the ghost buffer.
-struct ZMap {
-  int m;
-  int level;
-  double wgt;
-};
-
-__device__ __forceinline__ ZMap zmap(int kk, int dend, int nz, const ZEnds &b) {
-  ZMap r;
-  r.level = 0;
-  const int ubeg = dend + nz;
-  if (kk < dend) {
-    if (b.top_active) { r.m = dend - kk; r.wgt = b.s_top; }
-    else { r.m = -1; r.level = kk; r.wgt = 1.0; }
-  } else if (kk >= ubeg) {
-    if (b.bot_active) { r.m = 2 * nz + dend - 2 - kk; r.wgt = b.s_bot; }
-    else { r.m = -2; r.level = kk - ubeg; r.wgt = 1.0; }
-  } else {
-    r.m = kk - dend;
-    r.wgt = 1.0;
-    if (r.m == 0 && b.top_active) r.wgt = 1.0 + b.s_top;
-    if (r.m == nz - 1 && b.bot_active) r.wgt = 1.0 + b.s_bot;
-  }
-  return r;
-}
-
-template <typename R>
-__device__ __forceinline__ void atomic_add(R *a, R v) { atomicAdd(a, v); }
 
 // ---------------------------------------------------------------------------
 // Monopole spread of forces: one thread per (particle, stencil column).
@@ -298,40 +252,6 @@ __global__ void k_ghost_fold_y(R *buf, int levels, int ny, KernelDesc kd) {
   if (side == 0) lev[((int64_t)(j + ny) * kd.nxeff + i) * 3 + d] += lev[((int64_t)j * kd.nxeff + i) * 3 + d];
   else lev[((int64_t)(tbeg + j - ny) * kd.nxeff + i) * 3 + d] +=
       lev[((int64_t)(tbeg + j) * kd.nxeff + i) * 3 + d];
-}
-
-// Value of component d at extended z index kk for a particle column, with the
-// reference's ghost copy applied (BoundaryConditions.h:377-731): interior and
-// active-end layers come from the interior grid (periodic in x, y, mirrored
-// with sign at walls, boundary node times 1+s); inactive-end ghost layers come
-// from the ghost buffer at the extended column (ie, je).
-template <typename R>
-__device__ __forceinline__ void grid_value3(const R *__restrict__ grid, const ZMap &zm, int64_t col,
-                                            int64_t plane, int64_t comp, const Ghosts<R> &gh,
-                                            const KernelDesc &kd, int ie, int je, R out[3]) {
-  if (zm.m >= 0) {
-    const R *src = grid + zm.m * plane + col;
-    const R w = (R)zm.wgt;
-    out[0] = w * src[0];
-    out[1] = w * src[comp];
-    out[2] = w * src[2 * comp];
-  } else {
-    const R *buf = (zm.m == -1) ? gh.top : gh.bot;
-    if (buf == nullptr || ie < 0 || ie >= kd.nxeff || je < 0 || je >= kd.nyeff) {
-      out[0] = out[1] = out[2] = (R)0;
-      return;
-    }
-    const R *src = buf + (((int64_t)zm.level * kd.nyeff + je) * kd.nxeff + ie) * 3;
-    out[0] = src[0];
-    out[1] = src[1];
-    out[2] = src[2];
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ R warp_sum(R v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
 }
 
 // ---------------------------------------------------------------------------

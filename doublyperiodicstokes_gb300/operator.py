@@ -194,3 +194,34 @@ class DPStokes:
                                           ctypes.c_void_p(W.data_ptr() if W is not None else 0),
                                           _dtype_code(F), _stream_ptr(self.device), ms))
         return V, W, dict(zip(self.STAGES, list(ms)))
+
+    # ---- backward pass -----------------------------------------------------
+    def mdot_backward(self, F, T, gV, gW=None, need_F=True, need_T=False, need_X=True):
+        """Vector-Jacobian product of mdot at the current positions.
+
+        For l = <gV, V> + <gW, W> with (V, W) = mdot(F, T), returns
+        (dl/dF, dl/dT, dl/dX), each [N, 3] or None when not requested.  T is
+        the forward call's torques (None if it had none); F is needed only for
+        dl/dX.  The forward's velocity grid is recomputed, not stored."""
+        gV = self._check_arr(gV, "gV")
+        dt = gV.dtype
+        args = {}
+        for name, t in (("F", F), ("T", T), ("gW", gW)):
+            if t is not None:
+                t = self._check_arr(t, name)
+                if t.dtype != dt:
+                    raise TypeError("%s must have the dtype of gV" % name)
+            args[name] = t
+        if gW is not None and not self.params.has_torque:
+            raise ValueError("gW given but the operator was created without torques")
+        gF = torch.empty_like(gV) if need_F else None
+        gT = torch.empty_like(gV) if (need_T and T is not None) else None
+        gX = torch.empty_like(gV) if need_X else None
+
+        def ptr(t):
+            return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+        _lib.check(self.L.dpst_mdot_backward(self._h, ptr(args["F"]), ptr(args["T"]), ptr(gV),
+                                             ptr(args["gW"]), ptr(gF), ptr(gT), ptr(gX),
+                                             _dtype_code(gV), _stream_ptr(self.device)))
+        return gF, gT, gX

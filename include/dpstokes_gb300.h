@@ -174,6 +174,28 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
 int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
                       void *stream);
 
+/* Backward pass (vector-Jacobian product) of dpst_mdot at the current
+ * positions.  No counterpart in the reference, which has no derivatives;
+ * it differentiates the same discrete operator dpst_mdot applies.
+ * For a scalar loss l with dl/dV = gV and dl/dW = gW it writes
+ *   gF = dl/dF = M_VF^T gV + M_WF^T gW,   gT = dl/dT = M_VT^T gV + M_WT^T gW,
+ *   gX = dl/dX (position gradient; the ES-kernel derivatives enter through
+ *        the spreading and the interpolation weights),
+ * all [N][3] device arrays of `dtype` on the handle's device.
+ *   - F, T: the forward call's forces and torques.  T = NULL means the
+ *     forward had no torques (which also changes which ghost layers the
+ *     vorticity reads).  F is needed only for gX.
+ *   - gV is required; gW may be NULL (zero) and is accepted only by handles
+ *     created with torques.
+ *   - gF, gT, gX may each be NULL (not computed); gT needs T.
+ * The velocity grid of the forward is recomputed (spread + solve), not kept
+ * from dpst_mdot.  Offsets the forward clamps to the kernel threshold and
+ * the stencil's discrete choices (nearest node, z window) have zero
+ * derivative; dl/dX is the gradient of the operator between those events.
+ * Buffers for the backward pass are allocated on its first call. */
+int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *gV, const void *gW,
+                       void *gF, void *gT, void *gX, int dtype, void *stream);
+
 /* Sizes and derived constants of a handle. */
 int dpst_get_info(dpst_handle h, dpst_info *out);
 
