@@ -56,9 +56,9 @@ def _cotangents(w, seed=11):
 
 
 def _loss(V, Wv, gV, gW):
-    l = float(np.sum(gV * V))
+    l = float(np.sum(gV * np.reshape(V, gV.shape)))
     if gW is not None:
-        l += float(np.sum(gW * Wv))
+        l += float(np.sum(gW * np.reshape(Wv, gW.shape)))
     return l
 
 
@@ -145,9 +145,10 @@ def test_autograd_matches_direct():
     l = (V * _dev(gV)).sum() + (Wv * _dev(gW)).sum()
     l.backward()
     dF, dT, dX = _grads(op, X, F, T, gV, gW)
-    assert np.array_equal(_np(Ft.grad), dF)
-    assert np.array_equal(_np(Tt.grad), dT)
-    assert np.array_equal(_np(Xt.grad), dX)
+    # equal up to the order of the spreading's atomic sums
+    assert rel_err(_np(Ft.grad), dF) < 1e-12
+    assert rel_err(_np(Tt.grad), dT) < 1e-12
+    assert rel_err(_np(Xt.grad), dX) < 1e-12
 
 
 @pytest.mark.parametrize("name", ["s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_f_top"])
