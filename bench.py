@@ -310,7 +310,15 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-backward", action="store_true")
+    ap.add_argument("--only-backward", action="store_true",
+                    help="time only the backward pass of the differentiation configuration")
     args = ap.parse_args()
+    if args.only_backward:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"backward": run_backward(args, dev),
+                          "backward_mixed": run_backward(args, dev, "mixed")}), flush=True)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from doublyperiodicstokes_gb300 import workloads as W
