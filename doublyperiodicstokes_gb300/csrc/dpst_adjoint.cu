@@ -33,96 +33,129 @@ constexpr int ADJ_MODES = ADJ_LANES / 2;
 // Zeff_i^H g per wavenumber from the node-space adjoint spectrum (x-y
 // transform of the adjoint grid, before any z transform).  Output per mode:
 // cadj[0..2] the adjoint of the bottom wall values, cadj[3..5] of the top
-// wall values (slit).  One thread per mode, FP64.  For each pass the forward
-// map is Z(q) (main pass, q = (kx, ky)) or conj(Z(q')) (partner pass), so the
+// wall values (slit).  For each pass the forward map is Z(q) (main pass,
+// q = (kx, ky)) or conj(Z(q')) (partner pass, Nyquist lines only), so the
 // adjoint applies Z(q)^H or Z(q')^T: the imaginary entries of Z are
 // conjugated on the main pass only.
+// CADJ_G lanes per mode split the nodes and combine their sums with
+// shuffles; the node profiles are evaluated in the operator's arithmetic CT
+// (as the forward's correction epilogue does), the sums and the slit's 8x8
+// solve in FP64.  Every lane runs both passes so that the shuffles stay
+// warp-uniform; the partner pass contributes only where the mode needs it.
 // ---------------------------------------------------------------------------
-template <typename R>
-__global__ void k_corr_adj(KsArgs a, const R *__restrict__ spec, double2 *__restrict__ cadj) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= a.nk || a.mode == 0) return;
-  double2 *out = cadj + i * 6;
-  if (i == 0) {
-    for (int q = 0; q < 6; ++q) out[q] = make_double2(0, 0);
-    return;
+constexpr int CADJ_G = 8;
+
+static __device__ __forceinline__ double2 group_sum(double2 v) {
+  for (int o = CADJ_G / 2; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
   }
+  return v;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_corr_adj(KsArgs a, const R *__restrict__ spec, double2 *__restrict__ cadj) {
+  typedef R CT;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t i_raw = t / CADJ_G;
+  const int sub = (int)(t % CADJ_G);
   const int nz = a.nz;
   const int64_t nk = a.nk;
+  const int64_t i = i_raw < nk ? i_raw : nk - 1;
+  const bool store = (i_raw < nk) && sub == 0;
   const int ix = (int)(i % a.nxh), iy = (int)(i / a.nxh);
   const double kx = a.kvx[ix], ky = a.kvy[iy];
   const double k = sqrt(kx * kx + ky * ky);
   double kxp, kyp;
   const bool herm = mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp);
+  const CT kc = (CT)k;
   auto g = [&](int d, int m) -> double2 {
     const R *p = spec + (((int64_t)d * nz + m) * nk + i) * 2;
     return make_double2((double)p[0], (double)p[1]);
   };
-  const int npass = herm ? 1 : 2;
-  const double wgt = herm ? 1.0 : 0.5;
   double2 acc[6];
   for (int q = 0; q < 6; ++q) acc[q] = make_double2(0, 0);
-  for (int pass = 0; pass < npass; ++pass) {
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool use = (pass == 0) || !herm;
     const double qx = pass ? kxp : kx, qy = pass ? kyp : ky;
+    const CT qxc = (CT)qx, qyc = (CT)qy;
     // an entry i c of Z enters as i c (partner pass) or -i c (main pass)
     const double cs = pass ? 1.0 : -1.0;
     if (a.mode == 1) {
       // Z (DPTools.cpp:627-641) per node, symmetric 3x3:
       //   [e - qx^2 ze/k, -qx qy ze/k, -i qx ze; ., e - qy^2 ze/k, -i qy ze; ., ., e + k ze]
-      for (int m = 0; m < nz; ++m) {
-        const double z = a.zn[m];
-        const double e = exp(-k * z), ze = z * e;
+      double2 s0 = make_double2(0, 0), s1 = s0, s2 = s0;
+      for (int m = sub; m < nz; m += CADJ_G) {
+        const CT z = (CT)a.zn[m];
+        const CT e = exp(-kc * z), ze = z * e;
         const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
-        const double z00 = e - qx * qx * ze / k, z01 = -qx * qy * ze / k;
-        const double z11 = e - qy * qy * ze / k, z22 = e + k * ze;
-        acc[0] = cadd(acc[0], cadd(cadd(cscale(z00, g0), cscale(z01, g1)), cik(cs * (-qx * ze), g2)));
-        acc[1] = cadd(acc[1], cadd(cadd(cscale(z01, g0), cscale(z11, g1)), cik(cs * (-qy * ze), g2)));
-        acc[2] = cadd(acc[2], cadd(cadd(cik(cs * (-qx * ze), g0), cik(cs * (-qy * ze), g1)), cscale(z22, g2)));
+        const double z00 = (double)(e - qxc * qxc * ze / kc), z01 = (double)(-qxc * qyc * ze / kc);
+        const double z11 = (double)(e - qyc * qyc * ze / kc), z22 = (double)(e + kc * ze);
+        const double ix_ = cs * (double)(-qxc * ze), iy_ = cs * (double)(-qyc * ze);
+        s0 = cadd(s0, cadd(cadd(cscale(z00, g0), cscale(z01, g1)), cik(ix_, g2)));
+        s1 = cadd(s1, cadd(cadd(cscale(z01, g0), cscale(z11, g1)), cik(iy_, g2)));
+        s2 = cadd(s2, cadd(cadd(cik(ix_, g0), cik(iy_, g1)), cscale(z22, g2)));
+      }
+      s0 = group_sum(s0);
+      s1 = group_sum(s1);
+      s2 = group_sum(s2);
+      if (use) {
+        acc[0] = cadd(acc[0], s0);
+        acc[1] = cadd(acc[1], s1);
+        acc[2] = cadd(acc[2], s2);
       }
     } else {
       // Z = P A^{-1} R (DPTools.cpp:731-815): R maps (fb, ft) to the right
       // side of the 8x8 system A, P maps its solution to node values
       const double fac = 1.0 / 2.0 / a.eta, Hs = a.Lz;
+      const CT facc = (CT)fac, Hc = (CT)Hs;
       double2 p[8];
       for (int q = 0; q < 8; ++q) p[q] = make_double2(0, 0);
-      for (int m = 0; m < nz; ++m) {
-        const double z = a.zn[m];
-        const double e = exp(-k * z), e2 = exp(k * (z - Hs));
-        const double ze = z * e, ze2 = z * e2;
+      for (int m = sub; m < nz; m += CADJ_G) {
+        const CT z = (CT)a.zn[m];
+        const CT e = exp(-kc * z), e2 = exp(kc * (z - Hc));
+        const CT ze = z * e, ze2 = z * e2;
         const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
         // P rows: v0 = -i qx ze fac/k c0 + i qx ze2 fac/k c1 + e c2 + e2 c3,
         // v1 likewise with qy, c4, c5; v2 = ze fac c0 + ze2 fac c1 + e c6 + e2 c7
-        p[0] = cadd(p[0], cadd(cadd(cik(cs * (-qx * ze * fac / k), g0), cik(cs * (-qy * ze * fac / k), g1)),
-                               cscale(ze * fac, g2)));
-        p[1] = cadd(p[1], cadd(cadd(cik(cs * (qx * ze2 * fac / k), g0), cik(cs * (qy * ze2 * fac / k), g1)),
-                               cscale(ze2 * fac, g2)));
-        p[2] = cadd(p[2], cscale(e, g0));
-        p[3] = cadd(p[3], cscale(e2, g0));
-        p[4] = cadd(p[4], cscale(e, g1));
-        p[5] = cadd(p[5], cscale(e2, g1));
-        p[6] = cadd(p[6], cscale(e, g2));
-        p[7] = cadd(p[7], cscale(e2, g2));
+        const double a0 = cs * (double)(-qxc * ze * facc / kc), a1 = cs * (double)(-qyc * ze * facc / kc);
+        const double b0 = cs * (double)(qxc * ze2 * facc / kc), b1 = cs * (double)(qyc * ze2 * facc / kc);
+        const double ed = (double)e, e2d = (double)e2;
+        p[0] = cadd(p[0], cadd(cadd(cik(a0, g0), cik(a1, g1)), cscale((double)(ze * facc), g2)));
+        p[1] = cadd(p[1], cadd(cadd(cik(b0, g0), cik(b1, g1)), cscale((double)(ze2 * facc), g2)));
+        p[2] = cadd(p[2], cscale(ed, g0));
+        p[3] = cadd(p[3], cscale(e2d, g0));
+        p[4] = cadd(p[4], cscale(ed, g1));
+        p[5] = cadd(p[5], cscale(e2d, g1));
+        p[6] = cadd(p[6], cscale(ed, g2));
+        p[7] = cadd(p[7], cscale(e2d, g2));
       }
-      // A^{-H} (main) / A^{-T} (partner)
-      double2 A[64], At[64];
-      slit_matrix(qx, qy, Hs, a.eta, A);
-      for (int r = 0; r < 8; ++r)
-        for (int c = 0; c < 8; ++c) {
-          const double2 v = A[r + 8 * c];
-          At[c + 8 * r] = pass ? v : cconj(v);
-        }
-      zsolve8(At, p);
-      // R: x0 = -i qx fb0 - i qy fb1, x1 likewise for the top, x2..x4 = fb,
-      // x5..x7 = ft
-      acc[0] = cadd(acc[0], cadd(cik(cs * (-qx), p[0]), p[2]));
-      acc[1] = cadd(acc[1], cadd(cik(cs * (-qy), p[0]), p[3]));
-      acc[2] = cadd(acc[2], p[4]);
-      acc[3] = cadd(acc[3], cadd(cik(cs * (-qx), p[1]), p[5]));
-      acc[4] = cadd(acc[4], cadd(cik(cs * (-qy), p[1]), p[6]));
-      acc[5] = cadd(acc[5], p[7]);
+      for (int q = 0; q < 8; ++q) p[q] = group_sum(p[q]);
+      if (use && sub == 0) {
+        // A^{-H} (main) / A^{-T} (partner)
+        double2 A[64], At[64];
+        slit_matrix(qx, qy, Hs, a.eta, A);
+        for (int r = 0; r < 8; ++r)
+          for (int c = 0; c < 8; ++c) {
+            const double2 v = A[r + 8 * c];
+            At[c + 8 * r] = pass ? v : cconj(v);
+          }
+        zsolve8(At, p);
+        // R: x0 = -i qx fb0 - i qy fb1, x1 likewise for the top, x2..x4 = fb,
+        // x5..x7 = ft
+        acc[0] = cadd(acc[0], cadd(cik(cs * (-qx), p[0]), p[2]));
+        acc[1] = cadd(acc[1], cadd(cik(cs * (-qy), p[0]), p[3]));
+        acc[2] = cadd(acc[2], p[4]);
+        acc[3] = cadd(acc[3], cadd(cik(cs * (-qx), p[1]), p[5]));
+        acc[4] = cadd(acc[4], cadd(cik(cs * (-qy), p[1]), p[6]));
+        acc[5] = cadd(acc[5], p[7]);
+      }
     }
   }
-  for (int q = 0; q < 6; ++q) out[q] = cscale(wgt, acc[q]);
+  if (!store) return;
+  double2 *out = cadj + i * 6;
+  const double wgt = herm ? 1.0 : 0.5;
+  for (int q = 0; q < 6; ++q) out[q] = (i == 0) ? make_double2(0, 0) : cscale(wgt, acc[q]);  // k = 0: none
 }
 
 // ---------------------------------------------------------------------------
@@ -152,6 +185,7 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
   constexpr int T = ADJ_LANES;
   double *Xs = adj_sm;  // [(nz + 2)][T]
   double *S0 = adj_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
+  double *DH = FP1 + nz;  // 2 j / H, j = 0..nz
   for (int t = tid; t < nz; t += T) {
     S0[t] = a.s0[t];
     SM2[t] = a.sm2[t];
@@ -159,6 +193,7 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
     FM1[t] = a.fm1[t];
     FP1[t] = a.fp1[t];
   }
+  for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
   __syncthreads();
   const int GT = gridDim.x * T;
   double *__restrict__ CPb = scratch + blockIdx.x * T + tid;                    // row j at CPb[j * GT]
@@ -225,6 +260,7 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
     };
 
     double bcbar[6];
+#pragma unroll
     for (int c = 0; c < 3; ++c) {
       R *us = own + c * nz * rs;
       const double wbb = wb_bar[c], wtb = wt_bar[c];
@@ -348,7 +384,7 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
         double e = 0.0;
         if (j >= 1) {
           e = em2 + ((j == 1) ? 0.5 * XS(0) : XS(j - 1));
-          *f2 = (R)((double)*f2 + ((double)(2 * j) / a.H) * e);
+          *f2 = (R)((double)*f2 + DH[j] * e);
         }
         em2 = em1;
         em1 = e;
@@ -364,39 +400,41 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
 }
 
 // k = 0 (walls): U_c = S [r; Gi C r] with r = -f_c/eta (c = 0, 1), U_2 = 0;
-// open domain: zero.  Transposed in place.
+// open domain: zero.  Transposed in place; thread (part, j) owns row j.
+constexpr int ADJ_K0_ROWS = 128;
 template <typename R>
-__global__ void k_bvp_adj_k0(KsArgs a, R *__restrict__ spec) {
-  const int part = threadIdx.x;
-  if (part > 1) return;
+__global__ void __launch_bounds__(2 * ADJ_K0_ROWS) k_bvp_adj_k0(KsArgs a, R *__restrict__ spec) {
+  __shared__ double U[2][ADJ_K0_ROWS];
+  const int part = threadIdx.x / ADJ_K0_ROWS, j = threadIdx.x % ADJ_K0_ROWS;
   const int nz = a.nz;
   const int64_t nk = a.nk;
-  auto at = [&](int d, int j) -> R & { return spec[(((int64_t)d * nz + j) * nk) * 2 + part]; };
+  auto at = [&](int d, int r) -> R & { return spec[(((int64_t)d * nz + r) * nk) * 2 + part]; };
   if (a.mode == 0) {
-    for (int d = 0; d < 3; ++d)
-      for (int j = 0; j < nz; ++j) at(d, j) = (R)0;
+    if (j < nz)
+      for (int d = 0; d < 3; ++d) at(d, j) = (R)0;
     return;
   }
-  double Xb[128];
   const double inv_eta = 1.0 / a.eta;
   for (int c = 0; c < 2; ++c) {
-    for (int j = 0; j < nz; ++j) {
-      double x = a.s0[j] * (double)at(c, j);
-      if (j + 2 < nz) x += a.sm2[j + 2] * (double)at(c, j + 2);
-      if (j >= 2) x += a.sp2[j - 2] * (double)at(c, j - 2);
-      Xb[j] = x;
+    if (j < nz) U[part][j] = (double)at(c, j);
+    __syncthreads();
+    if (j < nz) {
+      double x = a.s0[j] * U[part][j];
+      if (j + 2 < nz) x += a.sm2[j + 2] * U[part][j + 2];
+      if (j >= 2) x += a.sp2[j - 2] * U[part][j - 2];
+      const double gb0 = a.se0 * U[part][0], gb1 = a.se1 * U[part][1];
+      // Gi row-major: g0 = Gi00 y0 + Gi01 y1, g1 = Gi10 y0 + Gi11 y1
+      const double t0 = a.k0gi[0] * gb0 + a.k0gi[2] * gb1, t1 = a.k0gi[1] * gb0 + a.k0gi[3] * gb1;
+      at(c, j) = (R)(-inv_eta * (x + a.k0c0[j] * t0 + a.k0c1[j] * t1));
     }
-    const double gb0 = a.se0 * (double)at(c, 0), gb1 = a.se1 * (double)at(c, 1);
-    // Gi row-major: g0 = Gi00 y0 + Gi01 y1, g1 = Gi10 y0 + Gi11 y1
-    const double t0 = a.k0gi[0] * gb0 + a.k0gi[2] * gb1, t1 = a.k0gi[1] * gb0 + a.k0gi[3] * gb1;
-    for (int j = 0; j < nz; ++j) at(c, j) = (R)(-inv_eta * (Xb[j] + a.k0c0[j] * t0 + a.k0c1[j] * t1));
+    __syncthreads();
   }
-  for (int j = 0; j < nz; ++j) at(2, j) = (R)0;
+  if (j < nz) at(2, j) = (R)0;
 }
 
 template <typename R>
 cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 5 * (size_t)a.nz);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 6 * (size_t)a.nz + 1);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_adj_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -414,18 +452,19 @@ cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
 template <typename R>
 cudaError_t launch_adj_solve(const KsArgs &a, R *spec, const double2 *cadj, double *scratch, int64_t grid,
                              cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 5 * (size_t)a.nz);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 6 * (size_t)a.nz + 1);
   k_bvp_adj_pairs<R><<<(unsigned)grid, ADJ_LANES, smem, s>>>(a, spec, cadj, scratch);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  k_bvp_adj_k0<R><<<1, 32, 0, s>>>(a, spec);
+  k_bvp_adj_k0<R><<<1, 2 * ADJ_K0_ROWS, 0, s>>>(a, spec);
   return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_corr_adj(const KsArgs &a, const R *spec, double2 *cadj, cudaStream_t s) {
   if (a.mode == 0) return cudaSuccess;
-  k_corr_adj<R><<<(unsigned)((a.nk + 127) / 128), 128, 0, s>>>(a, spec, cadj);
+  const int64_t threads = a.nk * CADJ_G;
+  k_corr_adj<R><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a, spec, cadj);
   return cudaGetLastError();
 }
 

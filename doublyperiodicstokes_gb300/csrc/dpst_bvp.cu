@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
   double *Xs = bvp_sm;  // [(nz + 2)][T] penta / RHS column
   // integration-matrix bands, identical for every wavenumber
   double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
+  double *DH = FP1 + nz;  // 2 j / H, j = 0..nz (Chebyshev derivative factors)
   for (int t = tid; t < nz; t += T) {
     S0[t] = a.s0[t];
     SM2[t] = a.sm2[t];
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
     FM1[t] = a.fm1[t];
     FP1[t] = a.fp1[t];
   }
+  for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
   __syncthreads();
   // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
   // in global memory (L2 resident: a few tens of MB)
@@ -85,7 +87,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
       const R *f0o = sp_oth + (nz - 1) * rs, *f1o = f0o + nz * rs;
       const R *f2s = sp_own + (2 * nz + nz - 1) * rs;
       for (int j = nz - 1; j >= 0; --j) {
-        const double df = (j == nz - 1) ? 0.0 : dfp2 + ((double)((j + 1) * 2) / a.H) * fzn;
+        const double df = (j == nz - 1) ? 0.0 : dfp2 + DH[j + 1] * fzn;
         const double fz = (double)*f2s;
         const double dfv = (j == 0) ? 0.5 * df : df;
         XS(j) = ((Dx * sp) * (double)*f0o + (Dy * sp) * (double)*f1o) + dfv;
@@ -259,49 +261,64 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
 
 // k = 0: open domain -> zero; walls -> u, v from the k = 0 BVP with the
 // reference's BC rows (u' = 0 or u = 0 at the top, u = 0 at the bottom), w = 0.
+// One CTA of 2 x 128 threads: thread (part, j) owns row j of the real or
+// imaginary part; the two BC dots are block reductions.
+constexpr int K0_ROWS = 128;
 template <typename R>
-__global__ void k_bvp_k0(KsArgs a, R *__restrict__ spec) {
-  const int part = threadIdx.x;  // 0: real part, 1: imaginary part
-  if (part > 1) return;
+__global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0(KsArgs a, R *__restrict__ spec) {
+  __shared__ double X[2][K0_ROWS + 2];
+  __shared__ double red[2][2][K0_ROWS / 32];
+  const int part = threadIdx.x / K0_ROWS, j = threadIdx.x % K0_ROWS;
   const int nz = a.nz;
   const int64_t nk = a.nk;
-  auto at = [&](int d, int j) -> R & { return spec[(((int64_t)d * nz + j) * nk) * 2 + part]; };
-  double X[130], U[128];
+  auto at = [&](int d, int r) -> R & { return spec[(((int64_t)d * nz + r) * nk) * 2 + part]; };
   if (a.mode == 0) {
-    for (int d = 0; d < 3; ++d)
-      for (int j = 0; j < nz; ++j) at(d, j) = (R)0;
+    if (j < nz)
+      for (int d = 0; d < 3; ++d) at(d, j) = (R)0;
     return;
   }
   const double inv_eta = 1.0 / a.eta;
+  const int lane = j & 31, wid = j >> 5;
   for (int c = 0; c < 2; ++c) {
-    double y0 = 0.0, y1 = 0.0;
-    for (int j = 0; j < nz; ++j) {
-      const double r = -inv_eta * (double)at(c, j);
-      X[j] = r;
-      y0 += a.k0c0[j] * r;
-      y1 += a.k0c1[j] * r;
+    const double r = (j < nz) ? -inv_eta * (double)at(c, j) : 0.0;
+    X[part][j] = r;
+    double y0 = (j < nz) ? a.k0c0[j] * r : 0.0, y1 = (j < nz) ? a.k0c1[j] * r : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      y0 += __shfl_xor_sync(0xffffffffu, y0, o);
+      y1 += __shfl_xor_sync(0xffffffffu, y1, o);
     }
-    const double g0 = a.k0gi[0] * y0 + a.k0gi[1] * y1;
-    const double g1 = a.k0gi[2] * y0 + a.k0gi[3] * y1;
-    X[nz] = g0;
-    X[nz + 1] = g1;
-    for (int m = 0; m < nz; ++m) {
-      double s = a.s0[m] * X[m];
-      if (m >= 2) s = a.sm2[m] * X[m - 2] + s;
-      s = s + a.sp2[m] * X[m + 2];
-      if (m == 0) s += a.se0 * g0;
-      if (m == 1) s += a.se1 * g1;
-      U[m] = s;
+    if (lane == 0) {
+      red[part][0][wid] = y0;
+      red[part][1][wid] = y1;
     }
-    for (int m = 0; m < nz; ++m) at(c, m) = (R)U[m];
+    __syncthreads();
+    if (j == 0) {
+      double s0 = 0.0, s1 = 0.0;
+      for (int q = 0; q < K0_ROWS / 32; ++q) {
+        s0 += red[part][0][q];
+        s1 += red[part][1][q];
+      }
+      X[part][nz] = a.k0gi[0] * s0 + a.k0gi[1] * s1;
+      X[part][nz + 1] = a.k0gi[2] * s0 + a.k0gi[3] * s1;
+    }
+    __syncthreads();
+    if (j < nz) {
+      double u = a.s0[j] * X[part][j];
+      if (j >= 2) u = a.sm2[j] * X[part][j - 2] + u;
+      u = u + a.sp2[j] * X[part][j + 2];
+      if (j == 0) u += a.se0 * X[part][nz];
+      if (j == 1) u += a.se1 * X[part][nz + 1];
+      at(c, j) = (R)u;
+    }
+    __syncthreads();
   }
-  for (int j = 0; j < nz; ++j) at(2, j) = (R)0;
+  if (j < nz) at(2, j) = (R)0;
 }
 
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 5 * (size_t)a.nz);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 6 * (size_t)a.nz + 1);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -320,11 +337,11 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 5 * (size_t)a.nz);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 6 * (size_t)a.nz + 1);
   k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  k_bvp_k0<R><<<1, 32, 0, s>>>(a, spec);
+  k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);
   return cudaGetLastError();
 }
 

@@ -23,43 +23,43 @@
 namespace dpst {
 
 // ---------------------------------------------------------------------------
-// Position derivatives of the stencil factors (one thread per particle), at
-// the stencil k_locate chose (st.cell) and with its offsets and clamping.
+// Position derivatives of the stencil factors, one thread per (particle,
+// stencil entry): entries [0, wx) are x factors, [wx, wx + wy) y factors,
+// then wz_max z factors; at the stencil k_locate chose (st.cell), with its
+// offsets and clamping.
 // ---------------------------------------------------------------------------
 template <typename R, bool DIPOLE>
 __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelDesc kd,
                               const double *__restrict__ zext, const double *__restrict__ wext, GridArgs g,
                               Stencils<R> st, GradStencils<R> gs) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= N) return;
-  const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+  const int E = kd.wx + kd.wy + kd.wz_max;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * E) return;
+  const int64_t p = t / E;
+  const int e = (int)(t - p * E);
   const int4 cl = st.cell[p];
   const double thr = kd.thr;
-  for (int i = 0; i < kd.wx; ++i) {
-    const double o = ((double)cl.x + i - kd.wx / 2 + kd.evenx) * g.hx - x;
-    double g1 = 0.0, g2 = 0.0;
+  double g1 = 0.0, g2 = 0.0;
+  if (e < kd.wx) {
+    const double o = ((double)cl.x + e - kd.wx / 2 + kd.evenx) * g.hx - pos[3 * p];
     if (!(o > thr || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
-    gs.gx[p * kd.wx + i] = (R)g1;
-    if (DIPOLE) gs.gdx[p * kd.wx + i] = (R)g2;
-  }
-  for (int j = 0; j < kd.wy; ++j) {
-    const double o = ((double)cl.y + j - kd.wy / 2 + kd.eveny) * g.hy - y;
-    double g1 = 0.0, g2 = 0.0;
+    gs.gx[p * kd.wx + e] = (R)g1;
+    if (DIPOLE) gs.gdx[p * kd.wx + e] = (R)g2;
+  } else if (e < kd.wx + kd.wy) {
+    const int j = e - kd.wx;
+    const double o = ((double)cl.y + j - kd.wy / 2 + kd.eveny) * g.hy - pos[3 * p + 1];
     if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
     gs.gy[p * kd.wy + j] = (R)g1;
     if (DIPOLE) gs.gdy[p * kd.wy + j] = (R)g2;
-  }
-  const double *ze = zext + kd.zext_off;
-  const double *we = wext + kd.zext_off;
-  const double hxy = g.hx * g.hy;
-  for (int k = 0; k < kd.wz_max; ++k) {
-    double g1 = 0.0, g2 = 0.0, wgt = 0.0;
+  } else {
+    const int k = e - kd.wx - kd.wy;
+    double wgt = 0.0;
     if (k < cl.w) {
-      const double o = ze[cl.z + k] - z;
+      const double o = zext[kd.zext_off + cl.z + k] - pos[3 * p + 2];
       if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
       g1 *= kd.inv_norm3;
       g2 *= kd.inv_norm3;
-      wgt = hxy * we[cl.z + k];
+      wgt = g.hx * g.hy * wext[kd.zext_off + cl.z + k];
     }
     gs.gz[p * kd.wz_max + k] = (R)g1;
     gs.gzw[p * kd.wz_max + k] = (R)(g1 * wgt);
@@ -400,8 +400,8 @@ void launch_locate_grad(bool dipole, const double *pos, int64_t N, const KernelD
                         const double *wext, const GridArgs &g, const Stencils<R> &st, const GradStencils<R> &gs,
                         cudaStream_t s) {
   if (N == 0) return;
-  const int bs = 128;
-  const int64_t nb = (N + bs - 1) / bs;
+  const int bs = 256;
+  const int64_t nb = (N * (kd.wx + kd.wy + kd.wz_max) + bs - 1) / bs;
   if (dipole) k_locate_grad<R, true><<<nb, bs, 0, s>>>(pos, N, kd, zext, wext, g, st, gs);
   else k_locate_grad<R, false><<<nb, bs, 0, s>>>(pos, N, kd, zext, wext, g, st, gs);
 }
