@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(256) k_corr_adj(KsArgs a, const R *__restrict_
 template <typename R>
 __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__restrict__ spec,
                                                             const double2 *__restrict__ cadj,
-                                                            double *__restrict__ scratch) {
+                                                            double *__restrict__ scratch, int per_cta) {
   extern __shared__ double adj_sm[];
   const int nz = a.nz;
   const int nk = (int)a.nk;
@@ -204,11 +204,14 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
   const double sp = part ? 1.0 : -1.0;
   const double inv_eta = 1.0 / a.eta;
   const int rs = 2 * nk;  // spectrum row stride (R elements) = bk row stride (double2)
-  const int ntiles = (nk + ADJ_MODES - 1) / ADJ_MODES;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int i_raw = tile * ADJ_MODES + q;
-    const int i = i_raw < nk ? i_raw : nk - 1;
-    const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_adj_k0
+  // work split as in k_bvp_pairs: contiguous per-CTA ranges, whole warps
+  const int cta_begin = blockIdx.x * per_cta;
+  const int cta_end = min(cta_begin + per_cta, nk);
+  for (int base = cta_begin; base < cta_end; base += ADJ_MODES) {
+    if (base + (tid >> 5) * 16 >= cta_end) continue;  // warp-uniform
+    const int i_raw = base + q;
+    const int i = i_raw < cta_end ? i_raw : cta_end - 1;
+    const bool store = (i_raw < cta_end) && (i != 0);  // mode 0: k_bvp_adj_k0
     R *__restrict__ own = spec + 2 * i + part;
     const int ix = i % a.nxh, iy = i / a.nxh;
     const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
@@ -441,9 +444,9 @@ cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_adj_pairs<R>, ADJ_LANES, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int64_t ntiles = (a.nk + ADJ_MODES - 1) / ADJ_MODES;
   int64_t g = (int64_t)nsm * per_sm;
-  if (g > ntiles) g = ntiles;
+  const int64_t warps_of_modes = (a.nk + 15) / 16;
+  if (g > warps_of_modes) g = warps_of_modes;
   *grid = g;
   *scratch_bytes = sizeof(double) * 2 * (size_t)a.nz * (size_t)g * ADJ_LANES;
   return cudaSuccess;
@@ -453,7 +456,9 @@ template <typename R>
 cudaError_t launch_adj_solve(const KsArgs &a, R *spec, const double2 *cadj, double *scratch, int64_t grid,
                              cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * ADJ_LANES + 6 * (size_t)a.nz + 1);
-  k_bvp_adj_pairs<R><<<(unsigned)grid, ADJ_LANES, smem, s>>>(a, spec, cadj, scratch);
+  const int64_t per = (a.nk + grid - 1) / grid;
+  const int per_cta = (int)((per + 15) / 16 * 16);
+  k_bvp_adj_pairs<R><<<(unsigned)grid, ADJ_LANES, smem, s>>>(a, spec, cadj, scratch, per_cta);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_bvp_adj_k0<R><<<1, 2 * ADJ_K0_ROWS, 0, s>>>(a, spec);

@@ -31,10 +31,14 @@ constexpr int BVP_MODES = BVP_LANES / 2;
 
 #define LDG(p) __ldg(p)
 
+// Work split: CTA b owns the contiguous modes [b per_cta, (b+1) per_cta),
+// per_cta a multiple of 16 (the modes of one warp), and walks them 96 at a
+// time; a warp whose 16 modes lie past the CTA's range skips the tile, so
+// the last, partial tile of every CTA costs only the warps it needs.
 template <typename R>
 __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
                                                          double2 *__restrict__ corr,
-                                                         double *__restrict__ cp_scratch) {
+                                                         double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
   const int nz = a.nz;
   const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
@@ -62,11 +66,13 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
   const double inv_eta = 1.0 / a.eta;
   const int rs = 2 * nk;  // spectrum row stride (R elements)
-  const int ntiles = (nk + BVP_MODES - 1) / BVP_MODES;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int i_raw = tile * BVP_MODES + q;
-    const int i = i_raw < nk ? i_raw : nk - 1;
-    const bool store = (i_raw < nk) && (i != 0);  // mode 0 is solved by k_bvp_k0
+  const int cta_begin = blockIdx.x * per_cta;
+  const int cta_end = min(cta_begin + per_cta, nk);
+  for (int base = cta_begin; base < cta_end; base += BVP_MODES) {
+    if (base + (tid >> 5) * 16 >= cta_end) continue;  // warp-uniform
+    const int i_raw = base + q;
+    const int i = i_raw < cta_end ? i_raw : cta_end - 1;
+    const bool store = (i_raw < cta_end) && (i != 0);  // mode 0 is solved by k_bvp_k0
     // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
     R *__restrict__ sp_own = spec + 2 * i + part;
     const R *__restrict__ sp_oth = spec + 2 * i + (part ^ 1);
@@ -81,23 +87,31 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
     const double2 *__restrict__ bk0 = reinterpret_cast<const double2 *>(a.bk) + 2 * i;
     const double *__restrict__ ab0 = a.ab + i;
 
-    // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j
+    // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j;
+    // the last row (df = 0) and row 0 (halved derivative) are peeled
     {
-      double dfp1 = 0.0, dfp2 = 0.0, fzn = 0.0;
       const R *f0o = sp_oth + (nz - 1) * rs, *f1o = f0o + nz * rs;
       const R *f2s = sp_own + (2 * nz + nz - 1) * rs;
-      for (int j = nz - 1; j >= 0; --j) {
-        const double df = (j == nz - 1) ? 0.0 : dfp2 + DH[j + 1] * fzn;
-        const double fz = (double)*f2s;
-        const double dfv = (j == 0) ? 0.5 * df : df;
-        XS(j) = ((Dx * sp) * (double)*f0o + (Dy * sp) * (double)*f1o) + dfv;
+      const double dxs = Dx * sp, dys = Dy * sp;
+      XS(nz - 1) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.0;
+      double fzn = ld_fp64(f2s);
+      double dfp1 = 0.0, dfp2 = 0.0;
+      f0o -= rs;
+      f1o -= rs;
+      f2s -= rs;
+#pragma unroll 4
+      for (int j = nz - 2; j >= 1; --j) {
+        const double df = dfp2 + DH[j + 1] * fzn;
+        fzn = ld_fp64(f2s);
+        XS(j) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + df;
         dfp2 = dfp1;
         dfp1 = df;
-        fzn = fz;
         f0o -= rs;
         f1o -= rs;
         f2s -= rs;
       }
+      const double df0 = dfp2 + DH[1] * fzn;
+      XS(0) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.5 * df0;
     }
     // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
     // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
@@ -129,6 +143,41 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
         b -= rs;
       }
     };
+    // Window pass over the border-corrected solution x_m = X_m - (A^{-1}B g)_m
+    // (x_nz = g0, x_nz+1 = g1): row m sees x_{m-2} .. x_{m+2} and applies
+    // the SIMat / FIMat bands.  Rows 0, 1 (border columns) and nz-2, nz-1
+    // (x_{m+2} is g) are peeled; the main loop takes rows in (even, odd)
+    // pairs so that the parity of the border column is static.
+    auto window = [&](double g0, double g1, auto &&row) {
+      const double *abp = ab0 + 2 * nk;
+      double xm2 = 0.0, xm1 = 0.0;
+      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
+      auto step = [&](int m, double x2, bool odd, int head) {
+        row(m, xm2, xm1, x0, x1, x2, odd, head);
+        xm2 = xm1;
+        xm1 = x0;
+        x0 = x1;
+        x1 = x2;
+      };
+      step(0, XS(2) - __ldg(abp) * g0, false, 1);
+      abp += nk;
+      step(1, XS(3) - __ldg(abp) * g1, true, 2);
+      abp += nk;
+      int m = 2;
+#pragma unroll 2
+      for (; m + 1 <= nz - 3; m += 2) {
+        step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
+        abp += nk;
+        step(m + 1, XS(m + 3) - __ldg(abp) * g1, true, 0);
+        abp += nk;
+      }
+      if (m <= nz - 3) {  // odd nz: one more even row
+        step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
+        ++m;
+      }
+      step(nz - 2, g0, ((nz - 2) & 1) != 0, 0);
+      step(nz - 1, g1, ((nz - 1) & 1) != 0, 0);
+    };
 
     // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
     // once for the z-velocity RHS, which overwrites XS behind the window
@@ -137,35 +186,24 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
       double y0, y1;
       penta(y0, y1);
       const double g0 = G00 * y0 + G01 * y1, g1 = G10 * y0 + G11 * y1;
-      // border-corrected x_j = X_j - A^{-1}B_j g (x_nz = g0, x_nz+1 = g1)
-      const double *abp = ab0 + 2 * nk;
-      double xm2 = 0.0, xm1 = 0.0;
-      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
       const R *f2s = sp_own + 2 * nz * rs;
       double *cpw = CPs;
-#pragma unroll 4
-      for (int m = 0; m < nz; ++m) {
-        const double x2 = (m + 2 < nz) ? XS(m + 2) - __ldg(abp) * ((m & 1) ? g1 : g0) : ((m + 2 == nz) ? g0 : g1);
+      window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
         double c = S0[m] * x0;
-        if (m >= 2) c = SM2[m] * xm2 + c;
+        if (head == 0) c = SM2[m] * xm2 + c;
         c = c + SP2[m] * x2;
-        if (m == 0) c += a.se0 * g0;
-        if (m == 1) c += a.se1 * g1;
+        if (head == 1) c += a.se0 * g0;
+        if (head == 2) c += a.se1 * g1;
         double dpv = FP1[m] * x1;
-        if (m >= 1) dpv = FM1[m] * xm1 + dpv;
-        if (m == 0) dpv += a.fe * g1;
+        if (head != 1) dpv = FM1[m] * xm1 + dpv;
+        if (head == 1) dpv += a.fe * g1;
         *cpw = c;
         ssum += c;
-        asum += (m & 1) ? -c : c;
-        XS(m) = inv_eta * (dpv - (double)*f2s);  // z-velocity RHS (DPTools.cpp:214)
-        xm2 = xm1;
-        xm1 = x0;
-        x0 = x1;
-        x1 = x2;
-        abp += nk;
+        asum += odd ? -c : c;
+        XS(m) = inv_eta * (dpv - ld_fp64(f2s));  // z-velocity RHS (DPTools.cpp:214)
         f2s += rs;
         cpw += GT;
-      }
+      });
     }
     // velocity BC right-hand sides (DPTools.cpp:218-234)
     const double ssum_o = __shfl_xor_sync(0xffffffffu, ssum, 1);
@@ -183,6 +221,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
 
     // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
     double wt[3], wb[3];
+#pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
       const int c = (cc + 2) % 3;  // 2, 0, 1
       if (c != 2) {
@@ -191,7 +230,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
         const double *cpo = CPo;
 #pragma unroll 4
         for (int j = 0; j < nz; ++j) {
-          XS(j) = inv_eta * (Dc * *cpo - (double)*fs);
+          XS(j) = inv_eta * (Dc * *cpo - ld_fp64(fs));
           fs += rs;
           cpo += GT;
         }
@@ -201,28 +240,18 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
       const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
       const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
       double st = 0.0, sb = 0.0;
-      const double *abp = ab0 + 2 * nk;
-      double xm2 = 0.0, xm1 = 0.0;
-      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
       R *us = sp_own + c * nz * rs;
-#pragma unroll 4
-      for (int m = 0; m < nz; ++m) {
-        const double x2 = (m + 2 < nz) ? XS(m + 2) - __ldg(abp) * ((m & 1) ? g1 : g0) : ((m + 2 == nz) ? g0 : g1);
+      window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
         double u = S0[m] * x0;
-        if (m >= 2) u = SM2[m] * xm2 + u;
+        if (head == 0) u = SM2[m] * xm2 + u;
         u = u + SP2[m] * x2;
-        if (m == 0) u += a.se0 * g0;
-        if (m == 1) u += a.se1 * g1;
-        if (store) *us = (R)u;
+        if (head == 1) u += a.se0 * g0;
+        if (head == 2) u += a.se1 * g1;
+        if (store) *us = to_r<R>(u);
         st += u;
-        sb += (m & 1) ? -u : u;
-        xm2 = xm1;
-        xm1 = x0;
-        x0 = x1;
-        x1 = x2;
-        abp += nk;
+        sb += odd ? -u : u;
         us += rs;
-      }
+      });
       wt[c] = st;
       wb[c] = sb;
     }
@@ -326,9 +355,9 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if ((int64_t)a.nz * a.nk * 4 >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
-  int64_t ntiles = (a.nk + BVP_MODES - 1) / BVP_MODES;
   int64_t g = (int64_t)nsm * per_sm;
-  if (g > ntiles) g = ntiles;
+  const int64_t warps_of_modes = (a.nk + 15) / 16;
+  if (g > warps_of_modes) g = warps_of_modes;
   *grid = g;
   *scratch_bytes = sizeof(double) * (size_t)a.nz * (size_t)g * BVP_LANES;
   return cudaSuccess;
@@ -338,7 +367,9 @@ template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 6 * (size_t)a.nz + 1);
-  k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch);
+  const int64_t per = (a.nk + grid - 1) / grid;
+  const int per_cta = (int)((per + 15) / 16 * 16);
+  k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);

@@ -16,6 +16,45 @@ static __device__ __forceinline__ double2 cconj(double2 a) { return make_double2
 // i*k*a for real k
 static __device__ __forceinline__ double2 cik(double k, double2 a) { return make_double2(-k * a.y, k * a.x); }
 
+// FP32 <-> FP64 conversions with integer instructions, for kernels whose
+// FP64 pipe is the bottleneck (GB300 executes FP64, conversions included, at
+// a small fraction of its integer rate).
+// f2d_int: exact for normal numbers, zeros, infinities and NaNs; FP32
+// subnormals become signed zeros.
+static __device__ __forceinline__ double f2d_int(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned sign = b & 0x80000000u;
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned m = b & 0x7fffffu;
+  const unsigned e2 = (e == 255u) ? 2047u : e + 896u;
+  const unsigned hi = (e == 0u) ? sign : (sign | (e2 << 20) | (m >> 3));
+  const unsigned lo = (e == 0u) ? 0u : (m << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+// d2f_int: round to nearest even, computed with integer instructions when the
+// result is a normal FP32 number or overflows to infinity by rounding;
+// every other input takes the hardware conversion.
+static __device__ __forceinline__ float d2f_int(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+  if (e >= 1 && e <= 254) {
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    unsigned r = ((unsigned)e << 23) | m;
+    r += (rem > 0x10000000u || (rem == 0x10000000u && (m & 1u))) ? 1u : 0u;
+    return __uint_as_float((hi & 0x80000000u) | r);
+  }
+  return __double2float_rn(d);
+}
+template <typename R>
+static __device__ __forceinline__ double ld_fp64(const R *p) { return (double)*p; }
+template <>
+__device__ __forceinline__ double ld_fp64<float>(const float *p) { return f2d_int(*p); }
+template <typename R>
+static __device__ __forceinline__ R to_r(double v) { return (R)v; }
+template <>
+__device__ __forceinline__ float to_r<float>(double v) { return d2f_int(v); }
+
 static __device__ __forceinline__ bool mode_is_hermitian(const KsArgs &a, int ix, int iy, double kx, double ky,
                                                   double &kxp, double &kyp) {
   int ixp = (a.nx - ix) % a.nx, iyp = (a.ny - iy) % a.ny;
