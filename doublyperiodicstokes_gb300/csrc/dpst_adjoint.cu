@@ -262,36 +262,64 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
       }
     };
 
+    // Transposed window: XS(j) = (S^T v)_j [+ (F^T d)_j] on the interior rows
+    // with the border-column dots e0 (even rows: column 0 of A^{-1}B) and e1
+    // (odd rows: column 1).  v_j and d_j are fetched in increasing j.  Rows
+    // 0, 1 and nz-2, nz-1 (incomplete bands) are peeled; the main loop takes
+    // (even, odd) pairs so that the parity is static.
+    auto st_window = [&](auto &&fetch_v, auto &&fetch_d, bool with_d, double &e0, double &e1) {
+      double vm2 = 0.0, vm1 = 0.0, v0 = fetch_v(0), v1 = fetch_v(1);
+      double dm1 = 0.0, d0 = with_d ? fetch_d(0) : 0.0, d1 = with_d ? fetch_d(1) : 0.0;
+      const double *abp = ab0;
+      // kind: 0 interior, 1 row 0, 2 row 1, 3 row nz-2, 4 row nz-1
+      auto row = [&](int j, double v2, double d2, int kind, bool odd) {
+        double x = S0[j] * v0;
+        if (kind <= 2) x += SM2[j + 2] * v2;
+        if (kind == 0 || kind >= 3) x += SP2[j - 2] * vm2;
+        if (with_d) {
+          if (kind != 4) x += FM1[j + 1] * d1;
+          if (kind != 1) x += FP1[j - 1] * dm1;
+        }
+        XS(j) = x;
+        const double t = __ldg(abp) * x;
+        if (odd) e1 += t;
+        else e0 += t;
+        abp += nk;
+        vm2 = vm1;
+        vm1 = v0;
+        v0 = v1;
+        v1 = v2;
+        dm1 = d0;
+        d0 = d1;
+        d1 = d2;
+      };
+      row(0, fetch_v(2), with_d ? fetch_d(2) : 0.0, 1, false);
+      row(1, fetch_v(3), with_d ? fetch_d(3) : 0.0, 2, true);
+      int j = 2;
+#pragma unroll 2
+      for (; j + 1 <= nz - 3; j += 2) {
+        row(j, fetch_v(j + 2), with_d ? fetch_d(j + 2) : 0.0, 0, false);
+        row(j + 1, fetch_v(j + 3), with_d ? fetch_d(j + 3) : 0.0, 0, true);
+      }
+      if (j <= nz - 3) {  // odd nz: one more even row
+        row(j, fetch_v(j + 2), with_d ? fetch_d(j + 2) : 0.0, 0, false);
+        ++j;
+      }
+      row(nz - 2, 0.0, 0.0, 3, ((nz - 2) & 1) != 0);
+      row(nz - 1, 0.0, 0.0, 4, ((nz - 1) & 1) != 0);
+    };
+    auto no_d = [&](int) { return 0.0; };
+
     double bcbar[6];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       R *us = own + c * nz * rs;
       const double wbb = wb_bar[c], wtb = wt_bar[c];
-      // x_bar = S^T u_bar on the interior rows, then the border adjoints
+      // x_bar = S^T u_bar, u_bar including the W^T term, then the border adjoints
       double e0 = 0.0, e1 = 0.0;
-      const double ub0 = (double)us[0] - wbb - wtb, ub1 = (double)us[rs] + wbb - wtb;
-      {
-        double um2 = 0.0, um1 = 0.0, u0 = ub0, u1 = ub1;
-        const R *up = us + 2 * rs;
-        const double *abp = ab0;
-#pragma unroll 4
-        for (int j = 0; j < nz; ++j) {
-          const double u2 = (j + 2 < nz) ? (double)*up - ((j & 1) ? -wbb : wbb) - wtb : 0.0;
-          double x = S0[j] * u0;
-          x += SM2[(j + 2 < nz) ? j + 2 : 0] * u2;
-          x += (j >= 2) ? SP2[j - 2] * um2 : 0.0;
-          XS(j) = x;
-          const double t = __ldg(abp) * x;
-          e0 += (j & 1) ? 0.0 : t;
-          e1 += (j & 1) ? t : 0.0;
-          um2 = um1;
-          um1 = u0;
-          u0 = u1;
-          u1 = u2;
-          up += rs;
-          abp += nk;
-        }
-      }
+      auto fetch_u = [&](int j) { return ld_fp64(us + (size_t)j * rs) - ((j & 1) ? -wbb : wbb) - wtb; };
+      const double ub0 = fetch_u(0), ub1 = fetch_u(1);
+      st_window(fetch_u, no_d, false, e0, e1);
       const double gb0 = a.se0 * ub0 - e0, gb1 = a.se1 * ub1 - e1;
       const double r0 = G00 * gb0 + G10 * gb1, r1 = G01 * gb0 + G11 * gb1;
       bcbar[2 * c] = -r0;
@@ -301,22 +329,23 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
       if (c == 2) {
         double *dpw = DPb;
         R *fw = us;
+#pragma unroll 4
         for (int j = 0; j < nz; ++j) {
-          const double rb = XS(j);
-          *dpw = inv_eta * rb;
-          if (store) *fw = (R)(-inv_eta * rb);
+          const double t = inv_eta * XS(j);
+          *dpw = t;
+          if (store) *fw = to_r<R>(-t);
           dpw += GT;
           fw += rs;
         }
       } else {
-        const double Dc = (c == 0) ? Dx : Dy;
+        const double coef = -sp * (c == 0 ? Dx : Dy) * inv_eta;
         double *cpw = CPb;
         R *fw = us;
+#pragma unroll 4
         for (int j = 0; j < nz; ++j) {
-          const double rb = XS(j);
-          const double add = (-sp * Dc * inv_eta) * XO(j);
+          const double add = coef * XO(j);
           *cpw = (c == 0) ? add : *cpw + add;
-          if (store) *fw = (R)(-inv_eta * rb);
+          if (store) *fw = to_r<R>(-(inv_eta * XS(j)));
           cpw += GT;
           fw += rs;
         }
@@ -337,37 +366,10 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
     // pressure: x_bar = S^T cp_bar + F^T dp_bar, border adjoints, A^{-T}
     {
       double e0 = 0.0, e1 = 0.0;
-      const double *cpr = CPb, *dpr = DPb;
-      const double c0v = cpr[0] + ssb + asb, c1v = cpr[GT] + ssb - asb;
-      const double d0v = dpr[0];
-      double cm2 = 0.0, cm1 = 0.0, cj = c0v, cj1 = c1v;
-      double dm1 = 0.0, dj = d0v, dj1 = dpr[GT];
-      const double *abp = ab0;
-      cpr += 2 * (size_t)GT;
-      dpr += 2 * (size_t)GT;
-      for (int j = 0; j < nz; ++j) {
-        const double cj2 = (j + 2 < nz) ? *cpr + ssb + ((j & 1) ? -asb : asb) : 0.0;
-        const double dj2 = (j + 2 < nz) ? *dpr : 0.0;
-        double x = S0[j] * cj;
-        x += SM2[(j + 2 < nz) ? j + 2 : 0] * cj2;
-        x += (j >= 2) ? SP2[j - 2] * cm2 : 0.0;
-        x += (j + 1 < nz) ? FM1[j + 1] * dj1 : 0.0;
-        x += (j >= 1) ? FP1[j - 1] * dm1 : 0.0;
-        XS(j) = x;
-        const double t = __ldg(abp) * x;
-        e0 += (j & 1) ? 0.0 : t;
-        e1 += (j & 1) ? t : 0.0;
-        cm2 = cm1;
-        cm1 = cj;
-        cj = cj1;
-        cj1 = cj2;
-        dm1 = dj;
-        dj = dj1;
-        dj1 = dj2;
-        abp += nk;
-        cpr += GT;
-        dpr += GT;
-      }
+      auto fetch_c = [&](int j) { return CPb[(size_t)j * GT] + ssb + ((j & 1) ? -asb : asb); };
+      auto fetch_dp = [&](int j) { return DPb[(size_t)j * GT]; };
+      const double c0v = fetch_c(0), c1v = fetch_c(1), d0v = fetch_dp(0);
+      st_window(fetch_c, fetch_dp, true, e0, e1);
       const double gb0 = a.se0 * c0v - e0;
       const double gb1 = a.se1 * c1v + a.fe * d0v - e1;
       const double r0 = G00 * gb0 + G10 * gb1, r1 = G01 * gb0 + G11 * gb1;
@@ -379,21 +381,25 @@ __global__ void __launch_bounds__(ADJ_LANES) k_bvp_adj_pairs(KsArgs a, R *__rest
     // (DPTools.cpp:134-174)
     if (store) {
       R *f0 = own, *f1 = own + nz * rs, *f2 = own + 2 * nz * rs;
-      double em2 = 0.0, em1 = 0.0;
-      for (int j = 0; j < nz; ++j) {
-        const double prb_o = XO(j);
-        *f0 = (R)((double)*f0 + (-sp * Dx) * prb_o);
-        *f1 = (R)((double)*f1 + (-sp * Dy) * prb_o);
-        double e = 0.0;
-        if (j >= 1) {
-          e = em2 + ((j == 1) ? 0.5 * XS(0) : XS(j - 1));
-          *f2 = (R)((double)*f2 + DH[j] * e);
-        }
-        em2 = em1;
-        em1 = e;
+      const double cx = -sp * Dx, cy = -sp * Dy;
+      {
+        const double prb_o = XO(0);
+        *f0 = to_r<R>(ld_fp64(f0) + cx * prb_o);
+        *f1 = to_r<R>(ld_fp64(f1) + cy * prb_o);
+      }
+      double em2 = 0.0, em1 = 0.5 * XS(0);  // e_0 = 0, e_1 = df_bar_0
+#pragma unroll 4
+      for (int j = 1; j < nz; ++j) {
         f0 += rs;
         f1 += rs;
         f2 += rs;
+        const double prb_o = XO(j);
+        *f0 = to_r<R>(ld_fp64(f0) + cx * prb_o);
+        *f1 = to_r<R>(ld_fp64(f1) + cy * prb_o);
+        const double e = em1;  // e_j
+        *f2 = to_r<R>(ld_fp64(f2) + DH[j] * e);
+        em1 = em2 + XS(j);  // e_{j+1} = e_{j-1} + df_bar_j
+        em2 = e;
       }
     }
     __syncwarp();

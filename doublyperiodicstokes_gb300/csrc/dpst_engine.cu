@@ -57,7 +57,7 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
 size_t noalloc_scratch_bytes();
 template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
-                         cudaStream_t s);
+                         cudaStream_t s, bool fold_out);
 // backward pass (dpst_adjoint.cu, dpst_grad.cu)
 template <typename R>
 cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
@@ -643,7 +643,7 @@ struct Engine : EngineBase {
     ef.inverse = 0;
     ef.scale = 1.0;
     ef.ks = ks;
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s));
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s, false));
     mark(3, s);
     if (!use_static_scratch) {
       DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
@@ -662,7 +662,7 @@ struct Engine : EngineBase {
     eb.inverse = 1;
     eb.scale = 1.0 / ((double)nx * (double)ny);
     eb.corr = corr.as<double2>();
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Ti.as<R>(), eb, nsm, s));
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Ti.as<R>(), eb, nsm, s, true));
     mark(5, s);
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
@@ -785,9 +785,9 @@ struct Engine : EngineBase {
     e.inverse = 0;
     e.scale = 1.0;
     e.ks = ks;
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TiT.as<R>(), e, nsm, s));
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TiT.as<R>(), e, nsm, s, false));
     DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TfTn.as<R>(), e, nsm, s));
+    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TfTn.as<R>(), e, nsm, s, true));
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)g2));

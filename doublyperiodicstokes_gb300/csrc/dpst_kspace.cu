@@ -214,17 +214,38 @@ __device__ __forceinline__ void corr_value(const EpiArgs &e, int d, int m, int64
   im = acc.y;
 }
 
-template <typename R, int RPT>
+// Folded z transform.  The DCT-I matrices are symmetric under reversing the
+// node index: T[j][N-1-m] = (-1)^j T[j][m] for the coefficient-from-nodes
+// type (Tf and Ti^T) and T[N-1-m][j] = (-1)^j T[m][j] for the
+// nodes-from-coefficients type (Ti and Tf^T), N = nz.  Either halves the
+// multiply-adds:
+//   ZFOLD_IN  (node-space input): with P_m = x_m + x_{N-1-m},
+//             Q_m = x_m - x_{N-1-m} (m < N/2) and the middle node for odd N,
+//             even rows are T[j][0..h] . P, odd rows T[j][0..h] . Q;
+//   ZFOLD_OUT (node-space output): E_m = sum_{j even} T[m][j] x_j,
+//             O_m = sum_{j odd} T[m][j] x_j for m < ceil(N/2), then
+//             y_m = E_m + O_m and y_{N-1-m} = E_m - O_m.
+// Only the first half of the stored matrix is read.  CTA: 256 threads, tile =
+// all rows x 64 columns, each thread 4 columns x RPT rows; rows of one thread
+// share a parity (r = ty + 16 q).  Persistent grid-stride over tiles; the
+// inverse epilogue adds the wall correction at the node and scales.
+constexpr int ZFOLD_IN = 1, ZFOLD_OUT = 2;
+
+template <typename R, int RPT, int FOLD>
 __global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, const R *__restrict__ Tm,
                                               EpiArgs e) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  R *Ts = reinterpret_cast<R *>(smem_raw);            // [16*RPT][nz+1]
-  const int tstride = nz + 1;
-  R *Bs = Ts + 16 * RPT * tstride;                     // [nz][64]
+  const int h = nz / 2, odd_n = nz & 1;
+  const int kf = h + odd_n;  // folded length (FOLD_IN) / computed rows (FOLD_OUT)
+  const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const int tstride = tcols + 1;
+  R *Ts = reinterpret_cast<R *>(smem_raw);  // [16*RPT][tcols+1]
+  R *Bs = Ts + 16 * RPT * tstride;           // FOLD_IN: P [kf][64] then Q [kf][64]; FOLD_OUT: [nz][64]
   const int tid = threadIdx.x;
+  const int trows = (FOLD == ZFOLD_IN) ? nz : kf;
   for (int idx = tid; idx < 16 * RPT * tstride; idx += 256) {
-    int r = idx / tstride, m = idx % tstride;
-    Ts[idx] = (r < nz && m < nz) ? Tm[r * nz + m] : (R)0;
+    const int r = idx / tstride, m = idx % tstride;
+    Ts[idx] = (r < trows && m < tcols) ? Tm[r * nz + m] : (R)0;
   }
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t tiles_per_comp = (ncols + 63) / 64;
@@ -234,44 +255,126 @@ __global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, c
     const int64_t c0 = (t % tiles_per_comp) * 64;
     R *B = spec + (int64_t)d * nz * ncols;
     __syncthreads();
-    for (int idx = tid; idx < nz * 64; idx += 256) {
-      int m = idx >> 6, c = idx & 63;
-      Bs[idx] = (c0 + c < ncols) ? B[(int64_t)m * ncols + c0 + c] : (R)0;
-    }
-    __syncthreads();
-    R acc[RPT][4];
-#pragma unroll
-    for (int q = 0; q < RPT; ++q)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[q][c] = 0;
-    for (int m = 0; m < nz; ++m) {
-      R b[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = Bs[m * 64 + tx * 4 + c];
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        R av = Ts[(ty + 16 * q) * tstride + m];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[q][c] = fma(av, b[c], acc[q][c]);
+    if (FOLD == ZFOLD_IN) {
+      for (int idx = tid; idx < kf * 64; idx += 256) {
+        const int m = idx >> 6, c = idx & 63;
+        R pv = 0, qv = 0;
+        if (c0 + c < ncols) {
+          const R xa = B[(int64_t)m * ncols + c0 + c];
+          if (m < h) {
+            const R xb = B[(int64_t)(nz - 1 - m) * ncols + c0 + c];
+            pv = xa + xb;
+            qv = xa - xb;
+          } else {
+            pv = xa;  // middle node (odd nz)
+          }
+        }
+        Bs[idx] = pv;
+        Bs[kf * 64 + idx] = qv;
+      }
+    } else {
+      for (int idx = tid; idx < nz * 64; idx += 256) {
+        const int m = idx >> 6, c = idx & 63;
+        Bs[idx] = (c0 + c < ncols) ? B[(int64_t)m * ncols + c0 + c] : (R)0;
       }
     }
+    __syncthreads();
+    if (FOLD == ZFOLD_IN) {
+      R acc[RPT][4];
 #pragma unroll
-    for (int q = 0; q < RPT; ++q) {
-      const int r = ty + 16 * q;
-      if (r >= nz) continue;
+      for (int q = 0; q < RPT; ++q)
 #pragma unroll
-      for (int cp = 0; cp < 2; ++cp) {
-        const int64_t col = c0 + tx * 4 + 2 * cp;  // even: real part of one mode
-        if (col >= ncols) continue;
-        R vr = acc[q][2 * cp], vi = acc[q][2 * cp + 1];
-        if (e.inverse) {
-          R cre, cim;
-          corr_value<R>(e, d, r, col >> 1, cre, cim);
-          vr = (vr + cre) * (R)e.scale;
-          vi = (vi + cim) * (R)e.scale;
+        for (int c = 0; c < 4; ++c) acc[q][c] = 0;
+      const R *Bp = Bs + ((ty & 1) ? kf * 64 : 0);  // odd rows read Q
+      for (int m = 0; m < kf; ++m) {
+        R b[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = Bp[m * 64 + tx * 4 + c];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const R av = Ts[(ty + 16 * q) * tstride + m];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[q][c] = fma(av, b[c], acc[q][c]);
         }
-        B[(int64_t)r * ncols + col] = vr;
-        B[(int64_t)r * ncols + col + 1] = vi;
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int r = ty + 16 * q;
+        if (r >= nz) continue;
+#pragma unroll
+        for (int cp = 0; cp < 2; ++cp) {
+          const int64_t col = c0 + tx * 4 + 2 * cp;
+          if (col >= ncols) continue;
+          R vr = acc[q][2 * cp], vi = acc[q][2 * cp + 1];
+          if (e.inverse) {
+            R cre, cim;
+            corr_value<R>(e, d, r, col >> 1, cre, cim);
+            vr = (vr + cre) * (R)e.scale;
+            vi = (vi + cim) * (R)e.scale;
+          }
+          B[(int64_t)r * ncols + col] = vr;
+          B[(int64_t)r * ncols + col + 1] = vi;
+        }
+      }
+    } else {
+      R ae[RPT][4], ao[RPT][4];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ae[q][c] = ao[q][c] = 0;
+      int j = 0;
+      for (; j + 1 < nz; j += 2) {
+        R be[4], bo[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          be[c] = Bs[j * 64 + tx * 4 + c];
+          bo[c] = Bs[(j + 1) * 64 + tx * 4 + c];
+        }
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const R te = Ts[(ty + 16 * q) * tstride + j], to = Ts[(ty + 16 * q) * tstride + j + 1];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            ae[q][c] = fma(te, be[c], ae[q][c]);
+            ao[q][c] = fma(to, bo[c], ao[q][c]);
+          }
+        }
+      }
+      if (j < nz) {  // odd nz: last (even) coefficient
+        R be[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) be[c] = Bs[j * 64 + tx * 4 + c];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const R te = Ts[(ty + 16 * q) * tstride + j];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) ae[q][c] = fma(te, be[c], ae[q][c]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int m = ty + 16 * q;
+        if (m >= kf) continue;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int r = half ? nz - 1 - m : m;
+          if (half && r == m) continue;  // middle node
+#pragma unroll
+          for (int cp = 0; cp < 2; ++cp) {
+            const int64_t col = c0 + tx * 4 + 2 * cp;
+            if (col >= ncols) continue;
+            R vr = half ? ae[q][2 * cp] - ao[q][2 * cp] : ae[q][2 * cp] + ao[q][2 * cp];
+            R vi = half ? ae[q][2 * cp + 1] - ao[q][2 * cp + 1] : ae[q][2 * cp + 1] + ao[q][2 * cp + 1];
+            if (e.inverse) {
+              R cre, cim;
+              corr_value<R>(e, d, r, col >> 1, cre, cim);
+              vr = (vr + cre) * (R)e.scale;
+              vi = (vi + cim) * (R)e.scale;
+            }
+            B[(int64_t)r * ncols + col] = vr;
+            B[(int64_t)r * ncols + col + 1] = vi;
+          }
+        }
       }
     }
   }
@@ -288,38 +391,51 @@ void launch_bvp_factors(const KsArgs &a, cudaStream_t s) {
 }
 
 
-template <typename R, int RPT>
+template <typename R, int RPT, int FOLD>
 static cudaError_t zgemm_rpt(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                              cudaStream_t s) {
-  size_t smem = (size_t)(16 * RPT * (nz + 1) + nz * 64) * sizeof(R);
-  cudaError_t err = cudaFuncSetAttribute(k_zgemm<R, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  const int kf = nz / 2 + (nz & 1);
+  const size_t tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const size_t bs = (FOLD == ZFOLD_IN) ? 2 * (size_t)kf * 64 : (size_t)nz * 64;
+  size_t smem = (16 * RPT * (tcols + 1) + bs) * sizeof(R);
+  cudaError_t err = cudaFuncSetAttribute(k_zgemm<R, RPT, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
   if (err != cudaSuccess) return err;
   int blocks_per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zgemm<R, RPT>, 256, smem);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zgemm<R, RPT, FOLD>, 256, smem);
   if (err != cudaSuccess) return err;
   if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
   int64_t ntiles = 3 * ((ncols + 63) / 64);
   int64_t grid = (int64_t)nsm * blocks_per_sm;
   if (grid > ntiles) grid = ntiles;
-  k_zgemm<R, RPT><<<(unsigned)grid, 256, smem, s>>>(spec, nz, ncols, Tm, e);
+  k_zgemm<R, RPT, FOLD><<<(unsigned)grid, 256, smem, s>>>(spec, nz, ncols, Tm, e);
   return cudaGetLastError();
 }
 
-template <typename R>
-cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
-                         cudaStream_t s) {
-  int rpt = (nz + 15) / 16;
-  if (rpt <= 2) return zgemm_rpt<R, 2>(spec, nz, ncols, Tm, e, nsm, s);
-  if (rpt <= 4) return zgemm_rpt<R, 4>(spec, nz, ncols, Tm, e, nsm, s);
-  if (rpt <= 6) return zgemm_rpt<R, 6>(spec, nz, ncols, Tm, e, nsm, s);
-  if (rpt <= 8) return zgemm_rpt<R, 8>(spec, nz, ncols, Tm, e, nsm, s);
+// fold_out = false: Tm is of the coefficient-from-nodes type (Tf, Ti^T);
+// true: nodes-from-coefficients (Ti, Tf^T).
+template <typename R, int FOLD>
+static cudaError_t zgemm_fold(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
+                              cudaStream_t s) {
+  const int rows = (FOLD == ZFOLD_IN) ? nz : nz / 2 + (nz & 1);
+  const int rpt = (rows + 15) / 16;
+  if (rpt <= 2) return zgemm_rpt<R, 2, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 4) return zgemm_rpt<R, 4, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 6) return zgemm_rpt<R, 6, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 8) return zgemm_rpt<R, 8, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
   return cudaErrorInvalidValue;
 }
 
+template <typename R>
+cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm, cudaStream_t s,
+                         bool fold_out) {
+  return fold_out ? zgemm_fold<R, ZFOLD_OUT>(spec, nz, ncols, Tm, e, nsm, s)
+                  : zgemm_fold<R, ZFOLD_IN>(spec, nz, ncols, Tm, e, nsm, s);
+}
+
 template cudaError_t launch_zgemm<float>(float *, int, int64_t, const float *, const EpiArgs &, int,
-                                         cudaStream_t);
+                                         cudaStream_t, bool);
 template cudaError_t launch_zgemm<double>(double *, int, int64_t, const double *, const EpiArgs &, int,
-                                          cudaStream_t);
+                                          cudaStream_t, bool);
 
 }  // namespace dpst
