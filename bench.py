@@ -287,6 +287,64 @@ def run_backward(args, dev, precision="fp64"):
             "note": "backward recomputes the forward's spread and velocity grid"}
 
 
+def run_batched(args, dev):
+    """The batched bottom-wall configuration: 256 systems, N_i log-uniform in
+    [64, 4096], L_i ~ U[32, 128], mixed precision.  One batched Mdot (a
+    captured graph over all systems) against a loop of the 256 single-system
+    operators on the same inputs; device milliseconds per pass over all
+    systems."""
+    import torch
+    from doublyperiodicstokes_gb300 import DPStokes, DPStokesBatch, StokesParams, workloads as W
+    ws = W.batched_c4()
+    prm = [StokesParams.from_workload(w, "mixed") for w in ws]
+    ins = [W.make_inputs(w) for w in ws]
+    X = torch.tensor(np.concatenate([a[0] for a in ins]), device=dev)
+    F = torch.tensor(np.concatenate([a[1] for a in ins]), dtype=torch.float32, device=dev)
+    b = DPStokesBatch(prm, [w.N for w in ws], device=dev)
+    b.set_positions(X)
+    V = torch.empty_like(F)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    k = max(3, min(args.steps, 10))
+
+    def timed(fn, reps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    batched = timed(lambda: b.mdot(F, None, out=(V, None)), k)
+    info = b.info()
+    b.close()
+    ops, Fs = [], []
+    for w, p, a in zip(ws, prm, ins):
+        op = DPStokes(p, w.N, device=dev)
+        op.set_positions(torch.tensor(a[0], device=dev))
+        ops.append(op)
+        Fs.append(torch.tensor(a[1], dtype=torch.float32, device=dev))
+    Vs = [torch.empty_like(f) for f in Fs]
+
+    def loop():
+        for op, f, v in zip(ops, Fs, Vs):
+            op.mdot(f, None, out=(v, None))
+
+    looped = timed(loop, max(2, k // 3))
+    for op in ops:
+        op.close()
+    n = sum(w.N for w in ws)
+    return {"workload": "c4_dpbw_256sys", "systems": len(ws), "particles": n,
+            "size_classes": info["n_size_classes"], "modes": info["n_modes"],
+            "batched_ms": batched, "loop_ms": looped, "speedup_vs_loop": looped / batched,
+            "batched_particles_per_s": n / (batched / 1e3), "loop_particles_per_s": n / (looped / 1e3),
+            "kernels_per_batched_mdot": info["kernels_per_mdot"], "fft_plans": info["fft_plans"],
+            "precision": "mixed", "note": "one CUDA graph launch per batched Mdot"}
+
+
 def cpu_baseline(w):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
@@ -312,7 +370,15 @@ def main():
     ap.add_argument("--skip-backward", action="store_true")
     ap.add_argument("--only-backward", action="store_true",
                     help="time only the backward pass of the differentiation configuration")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="time only the batched configuration (256 systems)")
     args = ap.parse_args()
+    if args.only_batched:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"batched": run_batched(args, dev)}), flush=True)
+        return
     if args.only_backward:
         import torch
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -364,6 +430,9 @@ def main():
         line["bwd_fwd_ratio"] = bw["bwd_fwd_ratio"]
         if args.precision == "mixed":
             line["backward_mixed"] = run_backward(args, dev, "mixed")
+    if not args.skip_batched:
+        import torch
+        line["batched"] = run_batched(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(r["w"])
     print(json.dumps(line), flush=True)

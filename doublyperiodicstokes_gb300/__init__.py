@@ -3,8 +3,8 @@
 Hand-written sm_103a CUDA kernels behind a C ABI (libdpstokes_gb300.so,
 include/dpstokes_gb300.h), driven from Python on torch tensors.
 """
-from .operator import DPStokes, StokesParams  # noqa: F401
+from .operator import DPStokes, DPStokesBatch, StokesParams  # noqa: F401
 from .autograd import mdot  # noqa: F401
 from . import workloads  # noqa: F401
 
-__all__ = ["DPStokes", "StokesParams", "mdot", "workloads"]
+__all__ = ["DPStokes", "DPStokesBatch", "StokesParams", "mdot", "workloads"]

@@ -36,6 +36,13 @@ class DpstInfo(ctypes.Structure):
                 ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int)]
 
 
+class DpstBatchInfo(ctypes.Structure):
+    _fields_ = [("n_systems", ctypes.c_int), ("n_size_classes", ctypes.c_int),
+                ("n_particles", ctypes.c_int64), ("n_modes", ctypes.c_int64),
+                ("kernels_per_mdot", ctypes.c_int), ("fft_plans", ctypes.c_int),
+                ("device_bytes", ctypes.c_int64)]
+
+
 # every entry point of include/dpstokes_gb300.h with its signature
 SIGNATURES = {
     "dpst_create": (ctypes.c_int, [ctypes.POINTER(DpstParams), ctypes.c_int64, ctypes.c_int,
@@ -61,6 +68,14 @@ SIGNATURES = {
                                          ctypes.c_void_p]),
     "dpst_mdot_backward": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 7
                            + [ctypes.c_int, ctypes.c_void_p]),
+    "dpst_batched_create": (ctypes.c_int, [ctypes.POINTER(DpstParams), ctypes.POINTER(ctypes.c_int64),
+                                           ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "dpst_batched_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dpst_batched_set_positions": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                  ctypes.c_void_p]),
+    "dpst_batched_mdot": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 4
+                          + [ctypes.c_int, ctypes.c_void_p]),
+    "dpst_batched_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DpstBatchInfo)]),
     "dpst_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DpstInfo)]),
     "dpst_last_error": (ctypes.c_char_p, []),
     "dpst_version": (ctypes.c_char_p, []),

@@ -31,6 +31,279 @@ constexpr int BVP_MODES = BVP_LANES / 2;
 
 #define LDG(p) __ldg(p)
 
+// Shared-memory tables and scratch of one lane of the solve.
+struct BvpCtx {
+  double *Xs;  // [(nz + 2)][BVP_LANES] penta / RHS columns
+  const double *S0, *SM2, *SP2, *FM1, *FP1, *DH;
+  double *CPs;        // this lane's pressure coefficients, row j at CPs[j * GT]
+  const double *CPo;  // the partner lane's
+  int GT, tid;
+};
+
+// Load the integration-matrix bands (identical for every wavenumber) and the
+// Chebyshev derivative factors 2 j / H into shared memory.
+static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm, double *cp_scratch) {
+  const int nz = a.nz, tid = threadIdx.x;
+  constexpr int T = BVP_LANES;
+  BvpCtx c;
+  c.Xs = bvp_sm;
+  double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
+  double *DH = FP1 + nz;
+  for (int t = tid; t < nz; t += T) {
+    S0[t] = a.s0[t];
+    SM2[t] = a.sm2[t];
+    SP2[t] = a.sp2[t];
+    FM1[t] = a.fm1[t];
+    FP1[t] = a.fp1[t];
+  }
+  for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
+  c.S0 = S0;
+  c.SM2 = SM2;
+  c.SP2 = SP2;
+  c.FM1 = FM1;
+  c.FP1 = FP1;
+  c.DH = DH;
+  // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
+  // in global memory (L2 resident: a few tens of MB)
+  c.GT = gridDim.x * T;
+  c.CPs = cp_scratch + blockIdx.x * T + tid;
+  c.CPo = cp_scratch + blockIdx.x * T + (tid ^ 1);
+  c.tid = tid;
+  return c;
+}
+
+// The solve of one wavenumber i for this lane (lane 2q: real part, 2q + 1:
+// imaginary part); both lanes of a pair run it together (shuffles).
+template <typename R>
+static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
+                                                int i, bool store, const BvpCtx &ctx) {
+  const int nz = a.nz;
+  const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
+  constexpr int T = BVP_LANES;
+  const int tid = ctx.tid, part = tid & 1;
+  double *Xs = ctx.Xs;
+  const double *S0 = ctx.S0, *SM2 = ctx.SM2, *SP2 = ctx.SP2, *FM1 = ctx.FM1, *FP1 = ctx.FP1, *DH = ctx.DH;
+  double *__restrict__ CPs = ctx.CPs;
+  const double *__restrict__ CPo = ctx.CPo;
+  const int GT = ctx.GT;
+#define XS(j) Xs[(j) * T + tid]
+  const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
+  const double inv_eta = 1.0 / a.eta;
+  const int rs = 2 * nk;  // spectrum row stride (R elements)
+  // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
+  R *__restrict__ sp_own = spec + 2 * i + part;
+  const R *__restrict__ sp_oth = spec + 2 * i + (part ^ 1);
+  const int ix = i % a.nxh, iy = i / a.nxh;
+  const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
+  const double Dx = ((a.nx % 2) == 0 && ix == a.nx / 2) ? 0.0 : kx;
+  const double Dy = ((a.ny % 2) == 0 && iy == a.ny / 2) ? 0.0 : ky;
+  const double K = sqrt(kx * kx + ky * ky);
+  const double G00 = __ldg(a.ginv + i), G10 = __ldg(a.ginv + nk + i);
+  const double G01 = __ldg(a.ginv + 2 * nk + i), G11 = __ldg(a.ginv + 3 * nk + i);
+  const double *__restrict__ mf0 = a.mf + i;
+  const double2 *__restrict__ bk0 = reinterpret_cast<const double2 *>(a.bk) + 2 * i;
+  const double *__restrict__ ab0 = a.ab + i;
+
+  // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j;
+  // the last row (df = 0) and row 0 (halved derivative) are peeled
+  {
+    const R *f0o = sp_oth + (nz - 1) * rs, *f1o = f0o + nz * rs;
+    const R *f2s = sp_own + (2 * nz + nz - 1) * rs;
+    const double dxs = Dx * sp, dys = Dy * sp;
+    XS(nz - 1) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.0;
+    double fzn = ld_fp64(f2s);
+    double dfp1 = 0.0, dfp2 = 0.0;
+    f0o -= rs;
+    f1o -= rs;
+    f2s -= rs;
+#pragma unroll 4
+    for (int j = nz - 2; j >= 1; --j) {
+      const double df = dfp2 + DH[j + 1] * fzn;
+      fzn = ld_fp64(f2s);
+      XS(j) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + df;
+      dfp2 = dfp1;
+      dfp1 = df;
+      f0o -= rs;
+      f1o -= rs;
+      f2s -= rs;
+    }
+    const double df0 = dfp2 + DH[1] * fzn;
+    XS(0) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.5 * df0;
+  }
+  // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
+  // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
+  // mf and the dp2 of the last two rows are zero, so both loops are uniform.
+  auto penta = [&](double &y0, double &y1) {
+    double xm2 = 0.0, xm1 = 0.0;
+    const double *p = mf0;
+#pragma unroll 8
+    for (int j = 0; j < nz; ++j) {
+      const double v = XS(j) - __ldg(p) * xm2;
+      XS(j) = v;
+      xm2 = xm1;
+      xm1 = v;
+      p += nk;
+    }
+    double xp2 = 0.0, xp1 = 0.0;
+    y0 = 0.0;
+    y1 = 0.0;
+    const double2 *b = bk0 + (nz - 1) * rs;
+#pragma unroll 8
+    for (int j = nz - 1; j >= 0; --j) {
+      const double2 ibd = __ldg(b), cc = __ldg(b + 1);
+      const double v = ibd.x * (XS(j) - ibd.y * xp2);
+      XS(j) = v;
+      y0 += cc.x * v;
+      y1 += cc.y * v;
+      xp2 = xp1;
+      xp1 = v;
+      b -= rs;
+    }
+  };
+  // Window pass over the border-corrected solution x_m = X_m - (A^{-1}B g)_m
+  // (x_nz = g0, x_nz+1 = g1): row m sees x_{m-2} .. x_{m+2} and applies
+  // the SIMat / FIMat bands.  Rows 0, 1 (border columns) and nz-2, nz-1
+  // (x_{m+2} is g) are peeled; the main loop takes rows in (even, odd)
+  // pairs so that the parity of the border column is static.
+  auto window = [&](double g0, double g1, auto &&row) {
+    const double *abp = ab0 + 2 * nk;
+    double xm2 = 0.0, xm1 = 0.0;
+    double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
+    auto step = [&](int m, double x2, bool odd, int head) {
+      row(m, xm2, xm1, x0, x1, x2, odd, head);
+      xm2 = xm1;
+      xm1 = x0;
+      x0 = x1;
+      x1 = x2;
+    };
+    step(0, XS(2) - __ldg(abp) * g0, false, 1);
+    abp += nk;
+    step(1, XS(3) - __ldg(abp) * g1, true, 2);
+    abp += nk;
+    int m = 2;
+#pragma unroll 2
+    for (; m + 1 <= nz - 3; m += 2) {
+      step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
+      abp += nk;
+      step(m + 1, XS(m + 3) - __ldg(abp) * g1, true, 0);
+      abp += nk;
+    }
+    if (m <= nz - 3) {  // odd nz: one more even row
+      step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
+      ++m;
+    }
+    step(nz - 2, g0, ((nz - 2) & 1) != 0, 0);
+    step(nz - 1, g1, ((nz - 1) & 1) != 0, 0);
+  };
+
+  // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
+  // once for the z-velocity RHS, which overwrites XS behind the window
+  double ssum = 0.0, asum = 0.0;
+  {
+    double y0, y1;
+    penta(y0, y1);
+    const double g0 = G00 * y0 + G01 * y1, g1 = G10 * y0 + G11 * y1;
+    const R *f2s = sp_own + 2 * nz * rs;
+    double *cpw = CPs;
+    window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
+      double c = S0[m] * x0;
+      if (head == 0) c = SM2[m] * xm2 + c;
+      c = c + SP2[m] * x2;
+      if (head == 1) c += a.se0 * g0;
+      if (head == 2) c += a.se1 * g1;
+      double dpv = FP1[m] * x1;
+      if (head != 1) dpv = FM1[m] * xm1 + dpv;
+      if (head == 1) dpv += a.fe * g1;
+      *cpw = c;
+      ssum += c;
+      asum += odd ? -c : c;
+      XS(m) = inv_eta * (dpv - ld_fp64(f2s));  // z-velocity RHS (DPTools.cpp:214)
+      f2s += rs;
+      cpw += GT;
+    });
+  }
+  // velocity BC right-hand sides (DPTools.cpp:218-234)
+  const double ssum_o = __shfl_xor_sync(0xffffffffu, ssum, 1);
+  const double asum_o = __shfl_xor_sync(0xffffffffu, asum, 1);
+  const double fac1 = 2.0 * a.eta, fac = fac1 * K;
+  const double ifac = 1.0 / fac, ifac1 = 1.0 / fac1;
+  double bc[6];
+  bc[0] = -ifac * ((Dx * sp) * ssum_o);
+  bc[1] = ifac * ((Dx * sp) * asum_o);
+  bc[2] = -ifac * ((Dy * sp) * ssum_o);
+  bc[3] = ifac * ((Dy * sp) * asum_o);
+  bc[4] = ifac1 * ssum;
+  bc[5] = ifac1 * asum;
+  __syncwarp();  // the partner's pressure coefficients are read below
+
+  // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
+  double wt[3], wb[3];
+#pragma unroll
+  for (int cc = 0; cc < 3; ++cc) {
+    const int c = (cc + 2) % 3;  // 2, 0, 1
+    if (c != 2) {
+      const double Dc = (c == 0 ? Dx : Dy) * sp;
+      const R *fs = sp_own + c * nz * rs;
+      const double *cpo = CPo;
+#pragma unroll 4
+      for (int j = 0; j < nz; ++j) {
+        XS(j) = inv_eta * (Dc * *cpo - ld_fp64(fs));
+        fs += rs;
+        cpo += GT;
+      }
+    }
+    double y0, y1;
+    penta(y0, y1);
+    const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
+    const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
+    double st = 0.0, sb = 0.0;
+    R *us = sp_own + c * nz * rs;
+    window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
+      double u = S0[m] * x0;
+      if (head == 0) u = SM2[m] * xm2 + u;
+      u = u + SP2[m] * x2;
+      if (head == 1) u += a.se0 * g0;
+      if (head == 2) u += a.se1 * g1;
+      if (store) *us = to_r<R>(u);
+      st += u;
+      sb += odd ? -u : u;
+      us += rs;
+    });
+    wt[c] = st;
+    wb[c] = sb;
+  }
+  // wall-correction coefficients (evalTheta at z = 0 and z = Lz)
+  double wto[3], wbo[3];
+  for (int c = 0; c < 3; ++c) {
+    wto[c] = __shfl_xor_sync(0xffffffffu, wt[c], 1);
+    wbo[c] = __shfl_xor_sync(0xffffffffu, wb[c], 1);
+  }
+  __syncwarp();  // XS/CPS reuse in the next tile
+  if (!store) return;
+  double *crd = reinterpret_cast<double *>(corr + i * 16);
+  if (a.mode == 1) {
+    for (int c = 0; c < 3; ++c) crd[2 * c + part] = -wb[c];
+  } else if (a.mode == 2 && part == 0) {
+    double2 fb[3], ft[3], cf[8];
+    for (int c = 0; c < 3; ++c) {
+      fb[c] = make_double2(-wb[c], -wbo[c]);
+      ft[c] = make_double2(-wt[c], -wto[c]);
+    }
+    slit_coeffs(kx, ky, a.Lz, a.eta, fb, ft, cf);
+    for (int r = 0; r < 8; ++r) corr[i * 16 + r] = cf[r];
+    double kxp, kyp;
+    if (!mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp)) {
+      for (int c = 0; c < 3; ++c) {
+        fb[c] = cconj(fb[c]);
+        ft[c] = cconj(ft[c]);
+      }
+      slit_coeffs(kxp, kyp, a.Lz, a.eta, fb, ft, cf);
+      for (int r = 0; r < 8; ++r) corr[i * 16 + 8 + r] = cf[r];
+    }
+  }
+#undef XS
+}
+
 // Work split: CTA b owns the contiguous modes [b per_cta, (b+1) per_cta),
 // per_cta a multiple of 16 (the modes of one warp), and walks them 96 at a
 // time; a warp whose 16 modes lie past the CTA's range skips the tile, so
@@ -40,252 +313,43 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
                                                          double2 *__restrict__ corr,
                                                          double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
-  const int nz = a.nz;
-  const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
-  const int tid = threadIdx.x, part = tid & 1, q = tid >> 1;
-  constexpr int T = BVP_LANES;
-  double *Xs = bvp_sm;  // [(nz + 2)][T] penta / RHS column
-  // integration-matrix bands, identical for every wavenumber
-  double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
-  double *DH = FP1 + nz;  // 2 j / H, j = 0..nz (Chebyshev derivative factors)
-  for (int t = tid; t < nz; t += T) {
-    S0[t] = a.s0[t];
-    SM2[t] = a.sm2[t];
-    SP2[t] = a.sp2[t];
-    FM1[t] = a.fm1[t];
-    FP1[t] = a.fp1[t];
-  }
-  for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
+  const BvpCtx ctx = bvp_ctx(a, bvp_sm, cp_scratch);
   __syncthreads();
-  // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
-  // in global memory (L2 resident: a few tens of MB)
-  const int GT = gridDim.x * T;
-  double *__restrict__ CPs = cp_scratch + blockIdx.x * T + tid;   // row j at CPs[j * GT]
-  const double *__restrict__ CPo = cp_scratch + blockIdx.x * T + (tid ^ 1);
-#define XS(j) Xs[(j) * T + tid]
-  const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
-  const double inv_eta = 1.0 / a.eta;
-  const int rs = 2 * nk;  // spectrum row stride (R elements)
+  const int nk = (int)a.nk;
+  const int tid = threadIdx.x, q = tid >> 1;
   const int cta_begin = blockIdx.x * per_cta;
   const int cta_end = min(cta_begin + per_cta, nk);
   for (int base = cta_begin; base < cta_end; base += BVP_MODES) {
     if (base + (tid >> 5) * 16 >= cta_end) continue;  // warp-uniform
     const int i_raw = base + q;
     const int i = i_raw < cta_end ? i_raw : cta_end - 1;
-    const bool store = (i_raw < cta_end) && (i != 0);  // mode 0 is solved by k_bvp_k0
-    // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
-    R *__restrict__ sp_own = spec + 2 * i + part;
-    const R *__restrict__ sp_oth = spec + 2 * i + (part ^ 1);
-    const int ix = i % a.nxh, iy = i / a.nxh;
-    const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
-    const double Dx = ((a.nx % 2) == 0 && ix == a.nx / 2) ? 0.0 : kx;
-    const double Dy = ((a.ny % 2) == 0 && iy == a.ny / 2) ? 0.0 : ky;
-    const double K = sqrt(kx * kx + ky * ky);
-    const double G00 = __ldg(a.ginv + i), G10 = __ldg(a.ginv + nk + i);
-    const double G01 = __ldg(a.ginv + 2 * nk + i), G11 = __ldg(a.ginv + 3 * nk + i);
-    const double *__restrict__ mf0 = a.mf + i;
-    const double2 *__restrict__ bk0 = reinterpret_cast<const double2 *>(a.bk) + 2 * i;
-    const double *__restrict__ ab0 = a.ab + i;
-
-    // pressure RHS Dx f + Dy g + d/dz h (DPTools.cpp:134-195), backward in j;
-    // the last row (df = 0) and row 0 (halved derivative) are peeled
-    {
-      const R *f0o = sp_oth + (nz - 1) * rs, *f1o = f0o + nz * rs;
-      const R *f2s = sp_own + (2 * nz + nz - 1) * rs;
-      const double dxs = Dx * sp, dys = Dy * sp;
-      XS(nz - 1) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.0;
-      double fzn = ld_fp64(f2s);
-      double dfp1 = 0.0, dfp2 = 0.0;
-      f0o -= rs;
-      f1o -= rs;
-      f2s -= rs;
-#pragma unroll 4
-      for (int j = nz - 2; j >= 1; --j) {
-        const double df = dfp2 + DH[j + 1] * fzn;
-        fzn = ld_fp64(f2s);
-        XS(j) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + df;
-        dfp2 = dfp1;
-        dfp1 = df;
-        f0o -= rs;
-        f1o -= rs;
-        f2s -= rs;
-      }
-      const double df0 = dfp2 + DH[1] * fzn;
-      XS(0) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.5 * df0;
-    }
-    // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
-    // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
-    // mf and the dp2 of the last two rows are zero, so both loops are uniform.
-    auto penta = [&](double &y0, double &y1) {
-      double xm2 = 0.0, xm1 = 0.0;
-      const double *p = mf0;
-#pragma unroll 8
-      for (int j = 0; j < nz; ++j) {
-        const double v = XS(j) - __ldg(p) * xm2;
-        XS(j) = v;
-        xm2 = xm1;
-        xm1 = v;
-        p += nk;
-      }
-      double xp2 = 0.0, xp1 = 0.0;
-      y0 = 0.0;
-      y1 = 0.0;
-      const double2 *b = bk0 + (nz - 1) * rs;
-#pragma unroll 8
-      for (int j = nz - 1; j >= 0; --j) {
-        const double2 ibd = __ldg(b), cc = __ldg(b + 1);
-        const double v = ibd.x * (XS(j) - ibd.y * xp2);
-        XS(j) = v;
-        y0 += cc.x * v;
-        y1 += cc.y * v;
-        xp2 = xp1;
-        xp1 = v;
-        b -= rs;
-      }
-    };
-    // Window pass over the border-corrected solution x_m = X_m - (A^{-1}B g)_m
-    // (x_nz = g0, x_nz+1 = g1): row m sees x_{m-2} .. x_{m+2} and applies
-    // the SIMat / FIMat bands.  Rows 0, 1 (border columns) and nz-2, nz-1
-    // (x_{m+2} is g) are peeled; the main loop takes rows in (even, odd)
-    // pairs so that the parity of the border column is static.
-    auto window = [&](double g0, double g1, auto &&row) {
-      const double *abp = ab0 + 2 * nk;
-      double xm2 = 0.0, xm1 = 0.0;
-      double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
-      auto step = [&](int m, double x2, bool odd, int head) {
-        row(m, xm2, xm1, x0, x1, x2, odd, head);
-        xm2 = xm1;
-        xm1 = x0;
-        x0 = x1;
-        x1 = x2;
-      };
-      step(0, XS(2) - __ldg(abp) * g0, false, 1);
-      abp += nk;
-      step(1, XS(3) - __ldg(abp) * g1, true, 2);
-      abp += nk;
-      int m = 2;
-#pragma unroll 2
-      for (; m + 1 <= nz - 3; m += 2) {
-        step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
-        abp += nk;
-        step(m + 1, XS(m + 3) - __ldg(abp) * g1, true, 0);
-        abp += nk;
-      }
-      if (m <= nz - 3) {  // odd nz: one more even row
-        step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
-        ++m;
-      }
-      step(nz - 2, g0, ((nz - 2) & 1) != 0, 0);
-      step(nz - 1, g1, ((nz - 1) & 1) != 0, 0);
-    };
-
-    // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
-    // once for the z-velocity RHS, which overwrites XS behind the window
-    double ssum = 0.0, asum = 0.0;
-    {
-      double y0, y1;
-      penta(y0, y1);
-      const double g0 = G00 * y0 + G01 * y1, g1 = G10 * y0 + G11 * y1;
-      const R *f2s = sp_own + 2 * nz * rs;
-      double *cpw = CPs;
-      window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
-        double c = S0[m] * x0;
-        if (head == 0) c = SM2[m] * xm2 + c;
-        c = c + SP2[m] * x2;
-        if (head == 1) c += a.se0 * g0;
-        if (head == 2) c += a.se1 * g1;
-        double dpv = FP1[m] * x1;
-        if (head != 1) dpv = FM1[m] * xm1 + dpv;
-        if (head == 1) dpv += a.fe * g1;
-        *cpw = c;
-        ssum += c;
-        asum += odd ? -c : c;
-        XS(m) = inv_eta * (dpv - ld_fp64(f2s));  // z-velocity RHS (DPTools.cpp:214)
-        f2s += rs;
-        cpw += GT;
-      });
-    }
-    // velocity BC right-hand sides (DPTools.cpp:218-234)
-    const double ssum_o = __shfl_xor_sync(0xffffffffu, ssum, 1);
-    const double asum_o = __shfl_xor_sync(0xffffffffu, asum, 1);
-    const double fac1 = 2.0 * a.eta, fac = fac1 * K;
-    const double ifac = 1.0 / fac, ifac1 = 1.0 / fac1;
-    double bc[6];
-    bc[0] = -ifac * ((Dx * sp) * ssum_o);
-    bc[1] = ifac * ((Dx * sp) * asum_o);
-    bc[2] = -ifac * ((Dy * sp) * ssum_o);
-    bc[3] = ifac * ((Dy * sp) * asum_o);
-    bc[4] = ifac1 * ssum;
-    bc[5] = ifac1 * asum;
-    __syncwarp();  // the partner's pressure coefficients are read below
-
-    // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
-    double wt[3], wb[3];
-#pragma unroll
-    for (int cc = 0; cc < 3; ++cc) {
-      const int c = (cc + 2) % 3;  // 2, 0, 1
-      if (c != 2) {
-        const double Dc = (c == 0 ? Dx : Dy) * sp;
-        const R *fs = sp_own + c * nz * rs;
-        const double *cpo = CPo;
-#pragma unroll 4
-        for (int j = 0; j < nz; ++j) {
-          XS(j) = inv_eta * (Dc * *cpo - ld_fp64(fs));
-          fs += rs;
-          cpo += GT;
-        }
-      }
-      double y0, y1;
-      penta(y0, y1);
-      const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
-      const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
-      double st = 0.0, sb = 0.0;
-      R *us = sp_own + c * nz * rs;
-      window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
-        double u = S0[m] * x0;
-        if (head == 0) u = SM2[m] * xm2 + u;
-        u = u + SP2[m] * x2;
-        if (head == 1) u += a.se0 * g0;
-        if (head == 2) u += a.se1 * g1;
-        if (store) *us = to_r<R>(u);
-        st += u;
-        sb += odd ? -u : u;
-        us += rs;
-      });
-      wt[c] = st;
-      wb[c] = sb;
-    }
-    // wall-correction coefficients (evalTheta at z = 0 and z = Lz)
-    double wto[3], wbo[3];
-    for (int c = 0; c < 3; ++c) {
-      wto[c] = __shfl_xor_sync(0xffffffffu, wt[c], 1);
-      wbo[c] = __shfl_xor_sync(0xffffffffu, wb[c], 1);
-    }
-    __syncwarp();  // XS/CPS reuse in the next tile
-    if (!store) continue;
-    double *crd = reinterpret_cast<double *>(corr + i * 16);
-    if (a.mode == 1) {
-      for (int c = 0; c < 3; ++c) crd[2 * c + part] = -wb[c];
-    } else if (a.mode == 2 && part == 0) {
-      double2 fb[3], ft[3], cf[8];
-      for (int c = 0; c < 3; ++c) {
-        fb[c] = make_double2(-wb[c], -wbo[c]);
-        ft[c] = make_double2(-wt[c], -wto[c]);
-      }
-      slit_coeffs(kx, ky, a.Lz, a.eta, fb, ft, cf);
-      for (int r = 0; r < 8; ++r) corr[i * 16 + r] = cf[r];
-      double kxp, kyp;
-      if (!mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp)) {
-        for (int c = 0; c < 3; ++c) {
-          fb[c] = cconj(fb[c]);
-          ft[c] = cconj(ft[c]);
-        }
-        slit_coeffs(kxp, kyp, a.Lz, a.eta, fb, ft, cf);
-        for (int r = 0; r < 8; ++r) corr[i * 16 + 8 + r] = cf[r];
-      }
-    }
+    bvp_mode<R>(a, spec, corr, i, (i_raw < cta_end) && (i != 0), ctx);  // mode 0: k_bvp_k0
   }
-#undef XS
+}
+
+// Batched systems: global mode g of [0, mprefix[S]) belongs to system s with
+// mprefix[s] <= g < mprefix[s+1]; every system has the same nz and H (the
+// shared-memory tables), its own factors, spectrum and corrections.
+template <typename R>
+__global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs_b(const SysK<R> *__restrict__ sys, int S,
+                                                           const int64_t *__restrict__ mprefix,
+                                                           double *__restrict__ cp_scratch, int per_cta) {
+  extern __shared__ double bvp_sm[];
+  const BvpCtx ctx = bvp_ctx(sys[0].ks, bvp_sm, cp_scratch);
+  __syncthreads();
+  const int64_t K = mprefix[S];
+  const int tid = threadIdx.x, q = tid >> 1;
+  const int64_t cta_begin = (int64_t)blockIdx.x * per_cta;
+  const int64_t cta_end = min(cta_begin + per_cta, K);
+  for (int64_t base = cta_begin; base < cta_end; base += BVP_MODES) {
+    if (base + (tid >> 5) * 16 >= cta_end) continue;  // warp-uniform
+    const int64_t g_raw = base + q;
+    const int64_t g = g_raw < cta_end ? g_raw : cta_end - 1;
+    const int s = find_sys(mprefix, S, g);
+    const SysK<R> &y = sys[s];
+    const int i = (int)(g - mprefix[s]);
+    bvp_mode<R>(y.ks, y.spec, y.corr, i, (g_raw < cta_end) && (i != 0), ctx);
+  }
 }
 
 // k = 0: open domain -> zero; walls -> u, v from the k = 0 BVP with the
@@ -294,7 +358,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
 // imaginary part; the two BC dots are block reductions.
 constexpr int K0_ROWS = 128;
 template <typename R>
-__global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0(KsArgs a, R *__restrict__ spec) {
+static __device__ __forceinline__ void bvp_k0_body(const KsArgs &a, R *__restrict__ spec) {
   __shared__ double X[2][K0_ROWS + 2];
   __shared__ double red[2][2][K0_ROWS / 32];
   const int part = threadIdx.x / K0_ROWS, j = threadIdx.x % K0_ROWS;
@@ -344,6 +408,17 @@ __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0(KsArgs a, R *__restrict_
   if (j < nz) at(2, j) = (R)0;
 }
 
+template <typename R>
+__global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0(KsArgs a, R *__restrict__ spec) {
+  bvp_k0_body<R>(a, spec);
+}
+
+// Batched: one CTA per system.
+template <typename R>
+__global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restrict__ sys) {
+  bvp_k0_body<R>(sys[blockIdx.x].ks, sys[blockIdx.x].spec);
+}
+
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
@@ -362,6 +437,45 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
   *scratch_bytes = sizeof(double) * (size_t)a.nz * (size_t)g * BVP_LANES;
   return cudaSuccess;
 }
+
+// Batched solve: grid and scratch for K modes in total with a shared nz.
+template <typename R>
+cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 6 * (size_t)nz + 1);
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs_b<R>, BVP_LANES, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t g = (int64_t)nsm * per_sm;
+  const int64_t warps_of_modes = (K + 15) / 16;
+  if (g > warps_of_modes) g = warps_of_modes;
+  if (g < 1) g = 1;
+  *grid = g;
+  *scratch_bytes = sizeof(double) * (size_t)nz * (size_t)g * BVP_LANES;
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
+                         int64_t grid, cudaStream_t s) {
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 6 * (size_t)nz + 1);
+  const int64_t per = (K + grid - 1) / grid;
+  const int per_cta = (int)((per + 15) / 16 * 16);
+  k_bvp_pairs_b<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  k_bvp_k0_b<R><<<S, 2 * K0_ROWS, 0, s>>>(sys);
+  return cudaGetLastError();
+}
+
+template cudaError_t bvp_plan_b<float>(int, int64_t, int, int64_t *, size_t *);
+template cudaError_t bvp_plan_b<double>(int, int64_t, int, int64_t *, size_t *);
+template cudaError_t launch_bvp_b<float>(const SysK<float> *, int, const int64_t *, int64_t, int, double *, int64_t,
+                                         cudaStream_t);
+template cudaError_t launch_bvp_b<double>(const SysK<double> *, int, const int64_t *, int64_t, int, double *,
+                                          int64_t, cudaStream_t);
 
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,

@@ -77,6 +77,27 @@ struct Ghosts {
   int nbot;
 };
 
+// One system of a batch (dpst_batched_*) as the particle kernels see it.
+// Particles of system s are [pbase, pbase + n) of the concatenated arrays;
+// its stencils, grid and ghost layers are its own slices.
+template <typename R>
+struct SysP {
+  KernelDesc km, kd;  // monopole / dipole kernel
+  GridArgs g;
+  Stencils<R> stm, std_;
+  Ghosts<R> ghm, ghd;
+  R *grid;  // [3][nz][ny][nx]
+  int64_t pbase, n;
+};
+
+// A ghost-layer buffer of one system, for the batched fold.
+template <typename R>
+struct FoldJob {
+  R *buf;
+  int levels, nx, ny;
+  KernelDesc kd;
+};
+
 // Arguments of the wavenumber-space kernels (dpst_kspace.cu).
 struct KsArgs {
   int nx, ny, nz, nxh;
@@ -112,5 +133,33 @@ struct EpiArgs {
   const double2 *corr;
   KsArgs ks;
 };
+
+// One system of a batch as the wavenumber-space kernels see it.
+template <typename R>
+struct SysK {
+  KsArgs ks;
+  R *spec;        // [3][nz][nk] complex
+  double2 *corr;  // [nk][16] wall-correction coefficients (walls only)
+};
+
+// Segment of the batched z transform: one system's spectrum.
+template <typename R>
+struct ZSeg {
+  R *spec;
+  int64_t ncols;  // 2 nk real columns per row
+  EpiArgs e;
+};
+
+// Batched work items: item x of [0, prefix[S]) belongs to entry s with
+// prefix[s] <= x < prefix[s+1] (entries with no items are skipped).
+static __device__ __forceinline__ int find_sys(const int64_t *__restrict__ prefix, int S, int64_t x) {
+  int lo = 0, hi = S;  // prefix[lo] <= x < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(prefix + mid) <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
 
 }  // namespace dpst

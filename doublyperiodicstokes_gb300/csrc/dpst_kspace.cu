@@ -231,81 +231,143 @@ __device__ __forceinline__ void corr_value(const EpiArgs &e, int d, int m, int64
 // inverse epilogue adds the wall correction at the node and scales.
 constexpr int ZFOLD_IN = 1, ZFOLD_OUT = 2;
 
+// Shared-memory state of a z-transform CTA: the (first half of the) matrix
+// and the staged tile.
 template <typename R, int RPT, int FOLD>
-__global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, const R *__restrict__ Tm,
-                                              EpiArgs e) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+static __device__ __forceinline__ void zgemm_load_matrix(int nz, const R *__restrict__ Tm, R *Ts) {
   const int h = nz / 2, odd_n = nz & 1;
-  const int kf = h + odd_n;  // folded length (FOLD_IN) / computed rows (FOLD_OUT)
+  const int kf = h + odd_n;
   const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
   const int tstride = tcols + 1;
-  R *Ts = reinterpret_cast<R *>(smem_raw);  // [16*RPT][tcols+1]
-  R *Bs = Ts + 16 * RPT * tstride;           // FOLD_IN: P [kf][64] then Q [kf][64]; FOLD_OUT: [nz][64]
-  const int tid = threadIdx.x;
   const int trows = (FOLD == ZFOLD_IN) ? nz : kf;
-  for (int idx = tid; idx < 16 * RPT * tstride; idx += 256) {
+  for (int idx = threadIdx.x; idx < 16 * RPT * tstride; idx += 256) {
     const int r = idx / tstride, m = idx % tstride;
     Ts[idx] = (r < trows && m < tcols) ? Tm[r * nz + m] : (R)0;
   }
+}
+
+// One tile: columns [c0, c0 + 64) of component d of the spectrum block B
+// (nz rows, row stride ncols), in place.
+template <typename R, int RPT, int FOLD>
+static __device__ __forceinline__ void zgemm_tile(R *B, int nz, int64_t ncols, int64_t c0, int d, const R *Ts,
+                                                  R *Bs, const EpiArgs &e) {
+  const int h = nz / 2, odd_n = nz & 1;
+  const int kf = h + odd_n;
+  const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const int tstride = tcols + 1;
+  const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  const int64_t tiles_per_comp = (ncols + 63) / 64;
-  const int64_t ntiles = 3 * tiles_per_comp;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int d = (int)(t / tiles_per_comp);
-    const int64_t c0 = (t % tiles_per_comp) * 64;
-    R *B = spec + (int64_t)d * nz * ncols;
-    __syncthreads();
-    if (FOLD == ZFOLD_IN) {
-      for (int idx = tid; idx < kf * 64; idx += 256) {
-        const int m = idx >> 6, c = idx & 63;
-        R pv = 0, qv = 0;
-        if (c0 + c < ncols) {
-          const R xa = B[(int64_t)m * ncols + c0 + c];
-          if (m < h) {
-            const R xb = B[(int64_t)(nz - 1 - m) * ncols + c0 + c];
-            pv = xa + xb;
-            qv = xa - xb;
-          } else {
-            pv = xa;  // middle node (odd nz)
-          }
+  __syncthreads();
+  if (FOLD == ZFOLD_IN) {
+    for (int idx = tid; idx < kf * 64; idx += 256) {
+      const int m = idx >> 6, c = idx & 63;
+      R pv = 0, qv = 0;
+      if (c0 + c < ncols) {
+        const R xa = B[(int64_t)m * ncols + c0 + c];
+        if (m < h) {
+          const R xb = B[(int64_t)(nz - 1 - m) * ncols + c0 + c];
+          pv = xa + xb;
+          qv = xa - xb;
+        } else {
+          pv = xa;  // middle node (odd nz)
         }
-        Bs[idx] = pv;
-        Bs[kf * 64 + idx] = qv;
       }
-    } else {
-      for (int idx = tid; idx < nz * 64; idx += 256) {
-        const int m = idx >> 6, c = idx & 63;
-        Bs[idx] = (c0 + c < ncols) ? B[(int64_t)m * ncols + c0 + c] : (R)0;
+      Bs[idx] = pv;
+      Bs[kf * 64 + idx] = qv;
+    }
+  } else {
+    for (int idx = tid; idx < nz * 64; idx += 256) {
+      const int m = idx >> 6, c = idx & 63;
+      Bs[idx] = (c0 + c < ncols) ? B[(int64_t)m * ncols + c0 + c] : (R)0;
+    }
+  }
+  __syncthreads();
+  if (FOLD == ZFOLD_IN) {
+    R acc[RPT][4];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[q][c] = 0;
+    const R *Bp = Bs + ((ty & 1) ? kf * 64 : 0);  // odd rows read Q
+    for (int m = 0; m < kf; ++m) {
+      R b[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = Bp[m * 64 + tx * 4 + c];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const R av = Ts[(ty + 16 * q) * tstride + m];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[q][c] = fma(av, b[c], acc[q][c]);
       }
     }
-    __syncthreads();
-    if (FOLD == ZFOLD_IN) {
-      R acc[RPT][4];
 #pragma unroll
-      for (int q = 0; q < RPT; ++q)
+    for (int q = 0; q < RPT; ++q) {
+      const int r = ty + 16 * q;
+      if (r >= nz) continue;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[q][c] = 0;
-      const R *Bp = Bs + ((ty & 1) ? kf * 64 : 0);  // odd rows read Q
-      for (int m = 0; m < kf; ++m) {
-        R b[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) b[c] = Bp[m * 64 + tx * 4 + c];
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          const R av = Ts[(ty + 16 * q) * tstride + m];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) acc[q][c] = fma(av, b[c], acc[q][c]);
+      for (int cp = 0; cp < 2; ++cp) {
+        const int64_t col = c0 + tx * 4 + 2 * cp;
+        if (col >= ncols) continue;
+        R vr = acc[q][2 * cp], vi = acc[q][2 * cp + 1];
+        if (e.inverse) {
+          R cre, cim;
+          corr_value<R>(e, d, r, col >> 1, cre, cim);
+          vr = (vr + cre) * (R)e.scale;
+          vi = (vi + cim) * (R)e.scale;
         }
+        B[(int64_t)r * ncols + col] = vr;
+        B[(int64_t)r * ncols + col + 1] = vi;
+      }
+    }
+  } else {
+    R ae[RPT][4], ao[RPT][4];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ae[q][c] = ao[q][c] = 0;
+    int j = 0;
+    for (; j + 1 < nz; j += 2) {
+      R be[4], bo[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        be[c] = Bs[j * 64 + tx * 4 + c];
+        bo[c] = Bs[(j + 1) * 64 + tx * 4 + c];
       }
 #pragma unroll
       for (int q = 0; q < RPT; ++q) {
-        const int r = ty + 16 * q;
-        if (r >= nz) continue;
+        const R te = Ts[(ty + 16 * q) * tstride + j], to = Ts[(ty + 16 * q) * tstride + j + 1];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          ae[q][c] = fma(te, be[c], ae[q][c]);
+          ao[q][c] = fma(to, bo[c], ao[q][c]);
+        }
+      }
+    }
+    if (j < nz) {  // odd nz: last (even) coefficient
+      R be[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) be[c] = Bs[j * 64 + tx * 4 + c];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const R te = Ts[(ty + 16 * q) * tstride + j];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ae[q][c] = fma(te, be[c], ae[q][c]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+      const int m = ty + 16 * q;
+      if (m >= kf) continue;
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int r = half ? nz - 1 - m : m;
+        if (half && r == m) continue;  // middle node
 #pragma unroll
         for (int cp = 0; cp < 2; ++cp) {
           const int64_t col = c0 + tx * 4 + 2 * cp;
           if (col >= ncols) continue;
-          R vr = acc[q][2 * cp], vi = acc[q][2 * cp + 1];
+          R vr = half ? ae[q][2 * cp] - ao[q][2 * cp] : ae[q][2 * cp] + ao[q][2 * cp];
+          R vi = half ? ae[q][2 * cp + 1] - ao[q][2 * cp + 1] : ae[q][2 * cp + 1] + ao[q][2 * cp + 1];
           if (e.inverse) {
             R cre, cim;
             corr_value<R>(e, d, r, col >> 1, cre, cim);
@@ -316,69 +378,52 @@ __global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, c
           B[(int64_t)r * ncols + col + 1] = vi;
         }
       }
-    } else {
-      R ae[RPT][4], ao[RPT][4];
-#pragma unroll
-      for (int q = 0; q < RPT; ++q)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) ae[q][c] = ao[q][c] = 0;
-      int j = 0;
-      for (; j + 1 < nz; j += 2) {
-        R be[4], bo[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          be[c] = Bs[j * 64 + tx * 4 + c];
-          bo[c] = Bs[(j + 1) * 64 + tx * 4 + c];
-        }
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          const R te = Ts[(ty + 16 * q) * tstride + j], to = Ts[(ty + 16 * q) * tstride + j + 1];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            ae[q][c] = fma(te, be[c], ae[q][c]);
-            ao[q][c] = fma(to, bo[c], ao[q][c]);
-          }
-        }
-      }
-      if (j < nz) {  // odd nz: last (even) coefficient
-        R be[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) be[c] = Bs[j * 64 + tx * 4 + c];
-#pragma unroll
-        for (int q = 0; q < RPT; ++q) {
-          const R te = Ts[(ty + 16 * q) * tstride + j];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) ae[q][c] = fma(te, be[c], ae[q][c]);
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < RPT; ++q) {
-        const int m = ty + 16 * q;
-        if (m >= kf) continue;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          const int r = half ? nz - 1 - m : m;
-          if (half && r == m) continue;  // middle node
-#pragma unroll
-          for (int cp = 0; cp < 2; ++cp) {
-            const int64_t col = c0 + tx * 4 + 2 * cp;
-            if (col >= ncols) continue;
-            R vr = half ? ae[q][2 * cp] - ao[q][2 * cp] : ae[q][2 * cp] + ao[q][2 * cp];
-            R vi = half ? ae[q][2 * cp + 1] - ao[q][2 * cp + 1] : ae[q][2 * cp + 1] + ao[q][2 * cp + 1];
-            if (e.inverse) {
-              R cre, cim;
-              corr_value<R>(e, d, r, col >> 1, cre, cim);
-              vr = (vr + cre) * (R)e.scale;
-              vi = (vi + cim) * (R)e.scale;
-            }
-            B[(int64_t)r * ncols + col] = vr;
-            B[(int64_t)r * ncols + col + 1] = vi;
-          }
-        }
-      }
     }
   }
+
 }
+
+template <typename R, int RPT, int FOLD>
+__global__ void __launch_bounds__(256) k_zgemm(R *spec, int nz, int64_t ncols, const R *__restrict__ Tm,
+                                              EpiArgs e) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int kf = nz / 2 + (nz & 1);
+  const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  R *Ts = reinterpret_cast<R *>(smem_raw);  // [16*RPT][tcols+1]
+  R *Bs = Ts + 16 * RPT * (tcols + 1);
+  zgemm_load_matrix<R, RPT, FOLD>(nz, Tm, Ts);
+  const int64_t tiles_per_comp = (ncols + 63) / 64;
+  const int64_t ntiles = 3 * tiles_per_comp;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int d = (int)(t / tiles_per_comp);
+    const int64_t c0 = (t % tiles_per_comp) * 64;
+    zgemm_tile<R, RPT, FOLD>(spec + (int64_t)d * nz * ncols, nz, ncols, c0, d, Ts, Bs, e);
+  }
+}
+
+// Batched: the tiles of every segment (one system's spectrum each), tprefix
+// the first tile of each segment.
+template <typename R, int RPT, int FOLD>
+__global__ void __launch_bounds__(256) k_zgemm_b(const ZSeg<R> *__restrict__ segs, const int64_t *__restrict__ tprefix,
+                                                int S, int nz, const R *__restrict__ Tm) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int kf = nz / 2 + (nz & 1);
+  const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  R *Ts = reinterpret_cast<R *>(smem_raw);
+  R *Bs = Ts + 16 * RPT * (tcols + 1);
+  zgemm_load_matrix<R, RPT, FOLD>(nz, Tm, Ts);
+  const int64_t ntiles = tprefix[S];
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int sg = find_sys(tprefix, S, t);
+    const ZSeg<R> &z = segs[sg];
+    const int64_t lt = t - tprefix[sg];
+    const int64_t tiles_per_comp = (z.ncols + 63) / 64;
+    const int d = (int)(lt / tiles_per_comp);
+    const int64_t c0 = (lt % tiles_per_comp) * 64;
+    zgemm_tile<R, RPT, FOLD>(z.spec + (int64_t)d * nz * z.ncols, nz, z.ncols, c0, d, Ts, Bs, z.e);
+  }
+}
+
 
 // ---------------------------------------------------------------------------
 // Host launchers
@@ -432,6 +477,51 @@ cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiA
   return fold_out ? zgemm_fold<R, ZFOLD_OUT>(spec, nz, ncols, Tm, e, nsm, s)
                   : zgemm_fold<R, ZFOLD_IN>(spec, nz, ncols, Tm, e, nsm, s);
 }
+
+template <typename R, int RPT, int FOLD>
+static cudaError_t zgemm_rpt_b(const ZSeg<R> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                               const R *Tm, int nsm, cudaStream_t s) {
+  const int kf = nz / 2 + (nz & 1);
+  const size_t tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const size_t bs = (FOLD == ZFOLD_IN) ? 2 * (size_t)kf * 64 : (size_t)nz * 64;
+  size_t smem = (16 * RPT * (tcols + 1) + bs) * sizeof(R);
+  cudaError_t err = cudaFuncSetAttribute(k_zgemm_b<R, RPT, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+  if (err != cudaSuccess) return err;
+  int blocks_per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zgemm_b<R, RPT, FOLD>, 256, smem);
+  if (err != cudaSuccess) return err;
+  if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t grid = (int64_t)nsm * blocks_per_sm;
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) return cudaSuccess;
+  k_zgemm_b<R, RPT, FOLD><<<(unsigned)grid, 256, smem, s>>>(segs, tprefix, S, nz, Tm);
+  return cudaGetLastError();
+}
+
+template <typename R, int FOLD>
+static cudaError_t zgemm_fold_b(const ZSeg<R> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                                const R *Tm, int nsm, cudaStream_t s) {
+  const int rows = (FOLD == ZFOLD_IN) ? nz : nz / 2 + (nz & 1);
+  const int rpt = (rows + 15) / 16;
+  if (rpt <= 2) return zgemm_rpt_b<R, 2, FOLD>(segs, tprefix, S, ntiles, nz, Tm, nsm, s);
+  if (rpt <= 4) return zgemm_rpt_b<R, 4, FOLD>(segs, tprefix, S, ntiles, nz, Tm, nsm, s);
+  if (rpt <= 6) return zgemm_rpt_b<R, 6, FOLD>(segs, tprefix, S, ntiles, nz, Tm, nsm, s);
+  if (rpt <= 8) return zgemm_rpt_b<R, 8, FOLD>(segs, tprefix, S, ntiles, nz, Tm, nsm, s);
+  return cudaErrorInvalidValue;
+}
+
+// Batched z transform over the segments' tiles (tprefix[S] = ntiles).
+template <typename R>
+cudaError_t launch_zgemm_b(const ZSeg<R> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz, const R *Tm,
+                           int nsm, cudaStream_t s, bool fold_out) {
+  return fold_out ? zgemm_fold_b<R, ZFOLD_OUT>(segs, tprefix, S, ntiles, nz, Tm, nsm, s)
+                  : zgemm_fold_b<R, ZFOLD_IN>(segs, tprefix, S, ntiles, nz, Tm, nsm, s);
+}
+template cudaError_t launch_zgemm_b<float>(const ZSeg<float> *, const int64_t *, int, int64_t, int, const float *,
+                                           int, cudaStream_t, bool);
+template cudaError_t launch_zgemm_b<double>(const ZSeg<double> *, const int64_t *, int, int64_t, int,
+                                            const double *, int, cudaStream_t, bool);
 
 template cudaError_t launch_zgemm<float>(float *, int, int64_t, const float *, const EpiArgs &, int,
                                          cudaStream_t, bool);

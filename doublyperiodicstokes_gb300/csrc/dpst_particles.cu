@@ -25,11 +25,10 @@ namespace dpst {
 // allocated stride.  reach[0] = min indl, reach[1] = max indr (extended z).
 // ---------------------------------------------------------------------------
 template <typename R, bool DIPOLE>
-__global__ void k_locate(const double *__restrict__ pos, int64_t N, KernelDesc kd,
-                         const double *__restrict__ zext, const double *__restrict__ wext,
-                         GridArgs g, Stencils<R> st, int *err, int *reach) {
-  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= N) return;
+static __device__ __forceinline__ void locate_item(int64_t p, const double *__restrict__ pos, const KernelDesc &kd,
+                                                   const double *__restrict__ zext,
+                                                   const double *__restrict__ wext, const GridArgs &g,
+                                                   const Stencils<R> &st, int *err, int *reach) {
   double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
   if (!(x >= 0.0 && x <= g.Lx && y >= 0.0 && y <= g.Ly && z >= 0.0 && z <= g.Lz)) {
     atomicOr(err, 1);
@@ -101,18 +100,24 @@ __global__ void k_locate(const double *__restrict__ pos, int64_t N, KernelDesc k
   }
 }
 
+template <typename R, bool DIPOLE>
+__global__ void k_locate(const double *__restrict__ pos, int64_t N, KernelDesc kd,
+                         const double *__restrict__ zext, const double *__restrict__ wext,
+                         GridArgs g, Stencils<R> st, int *err, int *reach) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  locate_item<R, DIPOLE>(p, pos, kd, zext, wext, g, st, err, reach);
+}
+
 // ---------------------------------------------------------------------------
 // Monopole spread of forces: one thread per (particle, stencil column).
 // grid layout [3][nz][ny][nx].
 // ---------------------------------------------------------------------------
 template <typename R, typename RF>
-__global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd, GridArgs g,
-                              Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
-  const int cols = kd.wx * kd.wy;
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= N * cols) return;
-  int64_t p = t / cols;
-  int c = (int)(t - p * cols);
+static __device__ __forceinline__ void spread_mono_item(int64_t p, int c, const RF *__restrict__ F,
+                                                     const KernelDesc &kd, const GridArgs &g,
+                                                     const Stencils<R> &st, R *__restrict__ grid,
+                                                     const Ghosts<R> &gh) {
   int i = c % kd.wx, j = c / kd.wx;
   int4 cl = st.cell[p];
   if (cl.w == 0) return;
@@ -145,6 +150,16 @@ __global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd
   }
 }
 
+template <typename R, typename RF>
+__global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd, GridArgs g,
+                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+  const int cols = kd.wx * kd.wy;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * cols) return;
+  const int64_t p = t / cols;
+  spread_mono_item<R, RF>(p, (int)(t - p * cols), F, kd, g, st, grid, gh);
+}
+
 // ---------------------------------------------------------------------------
 // Dipole spread of the torque curl, f += 1/2 curl(T delta) with derivative
 // kernels: x and y derivative spreads use BC set A, the z derivative spread
@@ -153,13 +168,10 @@ __global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd
 // grid before interpolating).
 // ---------------------------------------------------------------------------
 template <typename R, typename RF>
-__global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd, GridArgs g,
-                             Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
-  const int cols = kd.wx * kd.wy;
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= N * cols) return;
-  int64_t p = t / cols;
-  int c = (int)(t - p * cols);
+static __device__ __forceinline__ void spread_dip_item(int64_t p, int c, const RF *__restrict__ T,
+                                                     const KernelDesc &kd, const GridArgs &g,
+                                                     const Stencils<R> &st, R *__restrict__ grid,
+                                                     const Ghosts<R> &gh) {
   int i = c % kd.wx, j = c / kd.wx;
   int4 cl = st.cell[p];
   if (cl.w == 0) return;
@@ -207,6 +219,16 @@ __global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd,
   }
 }
 
+template <typename R, typename RF>
+__global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd, GridArgs g,
+                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+  const int cols = kd.wx * kd.wy;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * cols) return;
+  const int64_t p = t / cols;
+  spread_dip_item<R, RF>(p, (int)(t - p * cols), T, kd, g, st, grid, gh);
+}
+
 // ---------------------------------------------------------------------------
 // Periodic x then y fold of the ghost-layer buffers, applied to every stored
 // level exactly as the reference folds its whole extended grid
@@ -216,8 +238,8 @@ __global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd,
 // cells themselves keep their raw values.
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void k_ghost_fold_x(R *buf, int levels, int nx, KernelDesc kd) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+static __device__ __forceinline__ void ghost_fold_x_item(int64_t t, R *buf, int levels, int nx,
+                                                         const KernelDesc &kd) {
   int64_t per = (int64_t)kd.nyeff * kd.lend * 3;
   if (t >= levels * per * 2) return;
   int side = (int)(t / (levels * per));
@@ -235,8 +257,13 @@ __global__ void k_ghost_fold_x(R *buf, int levels, int nx, KernelDesc kd) {
 }
 
 template <typename R>
-__global__ void k_ghost_fold_y(R *buf, int levels, int ny, KernelDesc kd) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+__global__ void k_ghost_fold_x(R *buf, int levels, int nx, KernelDesc kd) {
+  ghost_fold_x_item<R>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, buf, levels, nx, kd);
+}
+
+template <typename R>
+static __device__ __forceinline__ void ghost_fold_y_item(int64_t t, R *buf, int levels, int ny,
+                                                         const KernelDesc &kd) {
   int64_t per = (int64_t)kd.bend * kd.nxeff * 3;
   if (t >= levels * per * 2) return;
   int side = (int)(t / (levels * per));
@@ -254,15 +281,19 @@ __global__ void k_ghost_fold_y(R *buf, int levels, int ny, KernelDesc kd) {
       lev[((int64_t)(tbeg + j) * kd.nxeff + i) * 3 + d];
 }
 
+template <typename R>
+__global__ void k_ghost_fold_y(R *buf, int levels, int ny, KernelDesc kd) {
+  ghost_fold_y_item<R>(blockIdx.x * (int64_t)blockDim.x + threadIdx.x, buf, levels, ny, kd);
+}
+
 // ---------------------------------------------------------------------------
 // Monopole interpolation: one warp per particle, V = sum u * phi * hx hy w_cc.
 // ---------------------------------------------------------------------------
 template <typename R, typename RV>
-__global__ void k_interp_mono(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
-                              Stencils<R> st, Ghosts<R> gh, RV *__restrict__ V) {
-  int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (p >= N) return;
+static __device__ __forceinline__ void interp_mono_item(int64_t p, int lane, const R *__restrict__ grid,
+                                                     const KernelDesc &kd, const GridArgs &g,
+                                                     const Stencils<R> &st, const Ghosts<R> &gh,
+                                                     RV *__restrict__ V) {
   int4 cl = st.cell[p];
   R s0 = 0, s1 = 0, s2 = 0;
   if (cl.w > 0) {
@@ -295,16 +326,23 @@ __global__ void k_interp_mono(const R *__restrict__ grid, int64_t N, KernelDesc 
   }
 }
 
+template <typename R, typename RV>
+__global__ void k_interp_mono(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
+                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ V) {
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= N) return;
+  interp_mono_item<R, RV>(p, threadIdx.x & 31, grid, kd, g, st, gh, V);
+}
+
 // ---------------------------------------------------------------------------
 // Dipole interpolation of the velocity gradient with derivative kernels and
 // W = -1/2 curl v (FCM.py:411-426): d/dx, d/dy use BC set A, d/dz set B.
 // ---------------------------------------------------------------------------
 template <typename R, typename RV>
-__global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
-                             Stencils<R> st, Ghosts<R> gh, RV *__restrict__ W) {
-  int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (p >= N) return;
+static __device__ __forceinline__ void interp_dip_item(int64_t p, int lane, const R *__restrict__ grid,
+                                                     const KernelDesc &kd, const GridArgs &g,
+                                                     const Stencils<R> &st, const Ghosts<R> &gh,
+                                                     RV *__restrict__ W) {
   int4 cl = st.cell[p];
   // gradient terms needed for the curl
   R dyvz = 0, dzvy = 0, dzvx = 0, dxvz = 0, dxvy = 0, dyvx = 0;
@@ -349,6 +387,133 @@ __global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc k
     W[3 * p + 2] = (RV)(-(R)0.5 * (dxvy - dyvx));
   }
 }
+
+template <typename R, typename RV>
+__global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
+                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ W) {
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= N) return;
+  interp_dip_item<R, RV>(p, threadIdx.x & 31, grid, kd, g, st, gh, W);
+}
+
+// ---------------------------------------------------------------------------
+// Batched systems (dpst_batched_*): one launch over the particles (or
+// particle-columns, or ghost cells) of every system.  prefix[s] is the first
+// work item of system s (prefix[S] = total); an item finds its system by
+// binary search and runs the single-system item with that system's tables.
+// ---------------------------------------------------------------------------
+template <typename R, bool DIPOLE>
+__global__ void k_locate_b(const double *__restrict__ pos, const SysP<R> *__restrict__ sys,
+                           const int64_t *__restrict__ pprefix, int S, const double *__restrict__ zext,
+                           const double *__restrict__ wext, int *err, int *reach) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= __ldg(pprefix + S)) return;
+  const int s = find_sys(pprefix, S, t);
+  const SysP<R> &y = sys[s];
+  locate_item<R, DIPOLE>(t - y.pbase, pos + 3 * y.pbase, DIPOLE ? y.kd : y.km, zext, wext, y.g,
+                         DIPOLE ? y.std_ : y.stm, err, reach + 2 * s);
+}
+
+template <typename R, typename RF, bool DIP>
+__global__ void k_spread_b(const RF *__restrict__ FT, const SysP<R> *__restrict__ sys,
+                           const int64_t *__restrict__ iprefix, int S) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= __ldg(iprefix + S)) return;
+  const int s = find_sys(iprefix, S, t);
+  const SysP<R> &y = sys[s];
+  const int cols = DIP ? y.kd.wx * y.kd.wy : y.km.wx * y.km.wy;
+  const int64_t loc = t - __ldg(iprefix + s);
+  const int64_t p = loc / cols;
+  const int c = (int)(loc - p * cols);
+  if (DIP) spread_dip_item<R, RF>(p, c, FT + 3 * y.pbase, y.kd, y.g, y.std_, y.grid, y.ghd);
+  else spread_mono_item<R, RF>(p, c, FT + 3 * y.pbase, y.km, y.g, y.stm, y.grid, y.ghm);
+}
+
+template <typename R, bool YAXIS>
+__global__ void k_ghost_fold_b(const FoldJob<R> *__restrict__ jobs, const int64_t *__restrict__ jprefix, int J) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= __ldg(jprefix + J)) return;
+  const int j = find_sys(jprefix, J, t);
+  const FoldJob<R> &f = jobs[j];
+  const int64_t loc = t - __ldg(jprefix + j);
+  if (YAXIS) ghost_fold_y_item<R>(loc, f.buf, f.levels, f.ny, f.kd);
+  else ghost_fold_x_item<R>(loc, f.buf, f.levels, f.nx, f.kd);
+}
+
+// One warp per particle of the concatenated arrays.  dip_ghosts = false
+// reads no ghost layers in the vorticity (the forward had no torques).
+template <typename R, typename RV, bool DIP>
+__global__ void k_interp_b(const SysP<R> *__restrict__ sys, const int64_t *__restrict__ pprefix, int S,
+                           RV *__restrict__ out, int dip_ghosts) {
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= __ldg(pprefix + S)) return;
+  const int s = find_sys(pprefix, S, p);
+  const SysP<R> &y = sys[s];
+  if (DIP) {
+    Ghosts<R> gz = y.ghd;
+    if (!dip_ghosts) gz.top = gz.bot = nullptr;
+    interp_dip_item<R, RV>(p - y.pbase, threadIdx.x & 31, y.grid, y.kd, y.g, y.std_, gz, out + 3 * y.pbase);
+  } else {
+    interp_mono_item<R, RV>(p - y.pbase, threadIdx.x & 31, y.grid, y.km, y.g, y.stm, y.ghm, out + 3 * y.pbase);
+  }
+}
+
+template <typename R>
+void launch_locate_b(bool dipole, const double *pos, int64_t total, const SysP<R> *sys, const int64_t *pprefix,
+                     int S, const double *zext, const double *wext, int *err, int *reach, cudaStream_t s) {
+  if (total == 0) return;
+  const int bs = 128;
+  const int64_t nb = (total + bs - 1) / bs;
+  if (dipole) k_locate_b<R, true><<<nb, bs, 0, s>>>(pos, sys, pprefix, S, zext, wext, err, reach);
+  else k_locate_b<R, false><<<nb, bs, 0, s>>>(pos, sys, pprefix, S, zext, wext, err, reach);
+}
+
+template <typename R, typename RF>
+void launch_spread_b(bool dipole, const RF *FT, int64_t items, const SysP<R> *sys, const int64_t *iprefix, int S,
+                     cudaStream_t s) {
+  if (items == 0) return;
+  const int bs = 256;
+  const int64_t nb = (items + bs - 1) / bs;
+  if (dipole) k_spread_b<R, RF, true><<<nb, bs, 0, s>>>(FT, sys, iprefix, S);
+  else k_spread_b<R, RF, false><<<nb, bs, 0, s>>>(FT, sys, iprefix, S);
+}
+
+template <typename R>
+void launch_ghost_fold_b(bool yaxis, const FoldJob<R> *jobs, const int64_t *jprefix, int J, int64_t items,
+                         cudaStream_t s) {
+  if (items == 0 || J == 0) return;
+  const int bs = 256;
+  const int64_t nb = (items + bs - 1) / bs;
+  if (yaxis) k_ghost_fold_b<R, true><<<nb, bs, 0, s>>>(jobs, jprefix, J);
+  else k_ghost_fold_b<R, false><<<nb, bs, 0, s>>>(jobs, jprefix, J);
+}
+
+template <typename R, typename RV>
+void launch_interp_b(bool dipole, int64_t total, const SysP<R> *sys, const int64_t *pprefix, int S, RV *out,
+                     bool dip_ghosts, cudaStream_t s) {
+  if (total == 0) return;
+  const int bs = 256;
+  const int64_t nb = (total * 32 + bs - 1) / bs;
+  if (dipole) k_interp_b<R, RV, true><<<nb, bs, 0, s>>>(sys, pprefix, S, out, dip_ghosts ? 1 : 0);
+  else k_interp_b<R, RV, false><<<nb, bs, 0, s>>>(sys, pprefix, S, out, 0);
+}
+
+#define DPST_BATCH_INST(R, RF)                                                                          \
+  template void launch_spread_b<R, RF>(bool, const RF *, int64_t, const SysP<R> *, const int64_t *, int, \
+                                       cudaStream_t);                                                   \
+  template void launch_interp_b<R, RF>(bool, int64_t, const SysP<R> *, const int64_t *, int, RF *, bool,  \
+                                       cudaStream_t);
+DPST_BATCH_INST(float, float)
+DPST_BATCH_INST(float, double)
+DPST_BATCH_INST(double, float)
+DPST_BATCH_INST(double, double)
+template void launch_locate_b<float>(bool, const double *, int64_t, const SysP<float> *, const int64_t *, int,
+                                     const double *, const double *, int *, int *, cudaStream_t);
+template void launch_locate_b<double>(bool, const double *, int64_t, const SysP<double> *, const int64_t *, int,
+                                      const double *, const double *, int *, int *, cudaStream_t);
+template void launch_ghost_fold_b<float>(bool, const FoldJob<float> *, const int64_t *, int, int64_t, cudaStream_t);
+template void launch_ghost_fold_b<double>(bool, const FoldJob<double> *, const int64_t *, int, int64_t,
+                                          cudaStream_t);
 
 // ---------------------------------------------------------------------------
 // Host launchers

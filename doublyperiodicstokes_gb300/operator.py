@@ -225,3 +225,80 @@ class DPStokes:
                                              ptr(args["gW"]), ptr(gF), ptr(gT), ptr(gX),
                                              _dtype_code(gV), _stream_ptr(self.device)))
         return gF, gT, gX
+
+
+class DPStokesBatch:
+    """Many independent systems in one pipeline (dpst_batched_*): uneven
+    particle counts and box sizes; shared nz, z interval, geometry,
+    viscosity, precision and torque flag.  Arrays are the systems' [N_s, 3]
+    arrays concatenated in the order of `params`."""
+
+    def __init__(self, params, n_particles, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("DPStokesBatch needs a CUDA device")
+        if len(params) != len(n_particles) or not params:
+            raise ValueError("one particle count per system, at least one system")
+        self.L = _lib.lib()
+        self.params = list(params)
+        self.n = [int(v) for v in n_particles]
+        self.N = sum(self.n)
+        self.has_torque = bool(params[0].has_torque)
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None
+                                   else torch.device(device).index or 0)
+        arr = (_lib.DpstParams * len(params))(*[p.to_c() for p in params])
+        cnt = (ctypes.c_int64 * len(params))(*self.n)
+        self._h = ctypes.c_void_p()
+        _lib.check(self.L.dpst_batched_create(arr, cnt, len(params), self.device.index,
+                                              ctypes.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            torch.cuda.synchronize(self.device)
+            _lib.check(self.L.dpst_batched_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        inf = _lib.DpstBatchInfo()
+        _lib.check(self.L.dpst_batched_get_info(self._h, ctypes.byref(inf)))
+        return {f: getattr(inf, f) for f, _ in inf._fields_}
+
+    def _check_arr(self, t, name):
+        if t.device != self.device:
+            raise ValueError("%s must be on %s" % (name, self.device))
+        if t.numel() != 3 * self.N:
+            raise ValueError("%s must hold 3*sum(N) = %d values" % (name, 3 * self.N))
+        return t.contiguous()
+
+    def set_positions(self, X):
+        X = self._check_arr(X, "positions")
+        self._X = X
+        _lib.check(self.L.dpst_batched_set_positions(self._h, ctypes.c_void_p(X.data_ptr()),
+                                                     _dtype_code(X), _stream_ptr(self.device)))
+
+    def mdot(self, F, T=None, out=None):
+        """(V, W) for every system, concatenated; W is None without torques."""
+        F = self._check_arr(F, "forces")
+        if T is not None:
+            if not self.has_torque:
+                raise ValueError("batch was created without torques")
+            T = self._check_arr(T, "torques")
+        V = torch.empty_like(F) if out is None else out[0]
+        W = None
+        if self.has_torque:
+            W = torch.empty_like(F) if out is None else out[1]
+        _lib.check(self.L.dpst_batched_mdot(self._h, ctypes.c_void_p(F.data_ptr()),
+                                            ctypes.c_void_p(T.data_ptr() if T is not None else 0),
+                                            ctypes.c_void_p(V.data_ptr()),
+                                            ctypes.c_void_p(W.data_ptr() if W is not None else 0),
+                                            _dtype_code(F), _stream_ptr(self.device)))
+        return V, W
+
+    def split(self, A):
+        """Split a concatenated [sum N, 3] array into the systems' arrays."""
+        return list(torch.split(A.reshape(-1, 3), self.n))

@@ -139,3 +139,19 @@ SMALL = [
     small("s_dpsc_f_odd", "DPSC", 20, 17, 20, 9.0, 0.3, 8.7, False, ny=14, Ly=14.0, seed=7),
 ]
 SMALL_BY_NAME = {w.name: w for w in SMALL}
+
+
+def small_batch(domType, has_torque, seed=40):
+    """A small batch sharing nz, the z interval and the geometry, with uneven
+    boxes (one size class holding two systems, one non-square grid) and
+    particle counts; h = 1 in every system."""
+    z = {"DPBW": (17, 0.0, 10.0, 1.5, 8.5), "DP": (19, 0.0, 12.4, 3.0, 9.4),
+         "DPSC": (20, 0.0, 9.0, 0.3, 8.7)}[domType]
+    nz, z0, Lz, zlo, zhi = z
+    shapes = [(16, 16, 24), (20, 20, 7), (16, 16, 30), (15, 15, 12), (18, 14, 20)]
+    out = []
+    for k, (nx, ny, N) in enumerate(shapes):
+        out.append(Workload("b_%s_%d" % (domType.lower(), k), domType, N, float(nx), float(ny), nx, ny, nz, z0,
+                            Lz, zlo, zhi, has_torque, betam_hat=1.3267 if has_torque else 1.714,
+                            seed=seed + k))
+    return out

@@ -196,6 +196,36 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
 int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *gV, const void *gW,
                        void *gF, void *gT, void *gX, int dtype, void *stream);
 
+/* ---- Batched systems (no counterpart in the reference, which runs one
+ * system per FCM / DPStokes instance) ------------------------------------
+ * Many independent systems -- uneven particle counts, box sizes and grids --
+ * in one pipeline: one launch per stage over all systems (one cuFFT plan
+ * pair per distinct (nx, ny)), captured into a CUDA graph on the first
+ * dpst_batched_mdot of each (dtype, torques, vorticity) combination and
+ * replayed afterwards.  Each system's V, W equal what dpst_mdot gives for it
+ * alone.  The systems must share nz, zmin, zmax, mode, viscosity, precision
+ * and has_torque; everything else (nx, ny, Lx, Ly, kernels, particle count)
+ * is per system.  Arrays are the systems' [N_s][3] arrays concatenated in
+ * the order of `params`, on the handle's device. */
+typedef struct dpst_batch_engine *dpst_batch;
+
+typedef struct {
+  int n_systems;
+  int n_size_classes;   /* distinct (nx, ny): one cuFFT plan pair each */
+  int64_t n_particles;  /* sum of N_s */
+  int64_t n_modes;      /* sum of ny (nx/2 + 1) */
+  int kernels_per_mdot; /* kernels of this library in one batched Mdot (cuFFT excluded) */
+  int fft_plans;
+  int64_t device_bytes;
+} dpst_batch_info;
+
+int dpst_batched_create(const dpst_params *params, const int64_t *n_particles, int n_systems, int device,
+                        dpst_batch *out);
+int dpst_batched_destroy(dpst_batch b);
+int dpst_batched_set_positions(dpst_batch b, const void *pos, int dtype, void *stream);
+int dpst_batched_mdot(dpst_batch b, const void *F, const void *T, void *V, void *W, int dtype, void *stream);
+int dpst_batched_get_info(dpst_batch b, dpst_batch_info *out);
+
 /* Sizes and derived constants of a handle. */
 int dpst_get_info(dpst_handle h, dpst_info *out);
 

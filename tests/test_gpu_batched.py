@@ -1,0 +1,103 @@
+"""Batched systems (dpst_batched_*, DPStokesBatch) on the GPU: every
+system's V, W from the one-pipeline batch against the single-system
+operator on the same inputs (FP64: 1e-12, equal up to the order of atomic
+sums; mixed: 1e-6), one system against the oracle (1e-10), and a sample of
+the 256-system bottom-wall configuration (mixed)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import dpstokes_oracle as O  # noqa: E402
+from conftest import rel_err  # noqa: E402
+from doublyperiodicstokes_gb300 import DPStokes, DPStokesBatch, StokesParams, _lib, workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(ws, dtype):
+    Xs, Fs, Ts = [], [], []
+    for w in ws:
+        X, F, T = W.make_inputs(w)
+        Xs.append(X)
+        Fs.append(F)
+        Ts.append(T)
+    cat = lambda a: torch.tensor(np.concatenate(a), dtype=dtype, device="cuda")  # noqa: E731
+    return Xs, Fs, Ts, cat(Xs).double(), cat(Fs), (cat(Ts) if Ts[0] is not None else None)
+
+
+def _single(w, X, F, T, precision, dtype):
+    op = DPStokes(StokesParams.from_workload(w, precision), w.N)
+    op.set_positions(torch.tensor(X, device="cuda"))
+    V, Wv = op.mdot(torch.tensor(F, dtype=dtype, device="cuda"),
+                    torch.tensor(T, dtype=dtype, device="cuda") if T is not None else None)
+    torch.cuda.synchronize()
+    out = (V.double().cpu().numpy(), Wv.double().cpu().numpy() if Wv is not None else None)
+    op.close()
+    return out
+
+
+def _run_batch(ws, precision, dtype):
+    b = DPStokesBatch([StokesParams.from_workload(w, precision) for w in ws], [w.N for w in ws])
+    Xs, Fs, Ts, X, F, T = _inputs(ws, dtype)
+    b.set_positions(X)
+    V, Wv = b.mdot(F, T)
+    V2, W2 = b.mdot(F, T)  # graph replay
+    torch.cuda.synchronize()
+    Vs = [v.double().cpu().numpy() for v in b.split(V)]
+    Ws = [v.double().cpu().numpy() for v in b.split(Wv)] if Wv is not None else None
+    # replays agree up to the order of the spreading's atomic sums
+    assert rel_err(V2.double().cpu().numpy(), V.double().cpu().numpy()) < (1e-12 if precision == "fp64" else 1e-6)
+    return b, Xs, Fs, Ts, Vs, Ws
+
+
+@pytest.mark.parametrize("dom,torque", [("DPBW", True), ("DP", True), ("DPSC", False), ("DPBW", False)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_matches_single(dom, torque, precision):
+    ws = W.small_batch(dom, torque)
+    dtype = torch.float64 if precision == "fp64" else torch.float32
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, precision, dtype)
+    info = b.info()
+    assert info["n_systems"] == len(ws) and info["n_size_classes"] == 4
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    for k, w in enumerate(ws):
+        V1, W1 = _single(w, Xs[k], Fs[k], Ts[k], precision, dtype)
+        ev = rel_err(Vs[k], V1)
+        ew = rel_err(Ws[k], W1) if torque else 0.0
+        print("%s %s V %.2e W %.2e" % (w.name, precision, ev, ew))
+        assert ev < tol and ew < tol
+    b.close()
+
+
+def test_batched_system_matches_oracle():
+    ws = W.small_batch("DPBW", True)
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, "fp64", torch.float64)
+    k = 4  # the non-square grid
+    Vo, Wo = O.mdot(O.Params(**ws[k].oracle_params()), Xs[k], Fs[k], Ts[k])
+    assert rel_err(Vs[k], Vo) < 1e-10
+    assert rel_err(Ws[k], Wo) < 1e-10
+    b.close()
+
+
+def test_batched_rejects_mismatched_systems():
+    ws = W.small_batch("DPBW", False)
+    ps = [StokesParams.from_workload(w) for w in ws]
+    ps[2].nz = ps[2].nz + 1
+    with pytest.raises(_lib.DPStokesError) as e:
+        DPStokesBatch(ps, [w.N for w in ws])
+    assert e.value.code == 1
+
+
+def test_batched_c4_sample():
+    """256 bottom-wall systems, N_i log-uniform in [64, 4096], L_i in
+    [32, 128], mixed precision: sampled systems against the single operator."""
+    ws = W.batched_c4()
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, "mixed", torch.float32)
+    print(b.info())
+    rng = np.random.default_rng(3)
+    for k in rng.choice(len(ws), 6, replace=False):
+        V1, _ = _single(ws[k], Xs[k], Fs[k], None, "mixed", torch.float32)
+        e = rel_err(Vs[k], V1)
+        print("%s N %d n %d: %.2e" % (ws[k].name, ws[k].N, ws[k].nx, e))
+        assert e < 1e-6
+    b.close()
