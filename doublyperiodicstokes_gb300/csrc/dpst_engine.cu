@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -59,6 +60,9 @@ size_t noalloc_scratch_bytes();
 template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s, bool fold_out);
+// tensor-core z transform of the mixed operator (dpst_ztc.cu)
+cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
+                            int *err, cudaStream_t s);
 // backward pass (dpst_adjoint.cu, dpst_grad.cu)
 template <typename R>
 cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
@@ -238,6 +242,7 @@ struct Engine : EngineBase {
                              sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, batch));
     plans = true;
     DPST_CUDA(cudaDeviceSynchronize());
+    tune_ztransform();
   }
 
   ~Engine() override {
@@ -377,6 +382,57 @@ struct Engine : EngineBase {
     DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
   }
 
+  // ---- z transform kernel choice (creation-time autotuner) -----------------
+  // 0: SIMT even/odd-folded GEMM (FP32 or FP64); 1: tcgen05 split-TF32 (FP32
+  // data only, nz <= 128).  DPSTOKES_GB300_ZTRANSFORM = simt | tcgen05 | auto
+  // (default) overrides the choice; auto times both on this handle's buffers.
+  int ztc = 0;
+  float ztc_ms[2] = {0.f, 0.f};
+  DevBuf ztc_err;
+
+  cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl) {
+    if (impl == 1 && sizeof(R) == 4)
+      return launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk, reinterpret_cast<const float *>(T), e, nsm,
+                             ztc_err.as<int>(), s);
+    return launch_zgemm<R>(sp, nz, 2 * nk, T, e, nsm, s, fold_out);
+  }
+
+  void tune_ztransform() {
+    ztc_err.alloc(sizeof(int));
+    DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
+    const char *env = getenv("DPSTOKES_GB300_ZTRANSFORM");
+    const std::string want = env ? env : "auto";
+    if (sizeof(R) != 4 || nz > 128 || want == "simt") return;
+    R *sp = reinterpret_cast<R *>(spec.p);
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+    EpiArgs e;
+    memset(&e, 0, sizeof(e));
+    e.scale = 1.0;
+    e.ks = ks;
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    for (int impl = 0; impl < 2; ++impl) {
+      DPST_CUDA(zgemm(sp, Tf.as<R>(), e, false, 0, impl));  // warm-up
+      DPST_CUDA(cudaEventRecord(a, 0));
+      for (int rep = 0; rep < 3; ++rep) DPST_CUDA(zgemm(sp, Tf.as<R>(), e, false, 0, impl));
+      DPST_CUDA(cudaEventRecord(b, 0));
+      DPST_CUDA(cudaEventSynchronize(b));
+      DPST_CUDA(cudaEventElapsedTime(&ztc_ms[impl], a, b));
+      ztc_ms[impl] /= 3.0f;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    int err = 0;
+    DPST_CUDA(cudaMemcpy(&err, ztc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {  // the tensor-core kernel gave up waiting: keep the SIMT kernel
+      ztc = 0;
+      DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
+      return;
+    }
+    ztc = (want == "tcgen05" || ztc_ms[1] < ztc_ms[0]) ? 1 : 0;
+  }
+
   // grid (spread forces) -> grid (velocities): x-y FFT, z transform, per-k
   // solve, inverse z transform with the wall correction, inverse x-y FFT
   void solve_stage(cudaStream_t s) {
@@ -393,7 +449,7 @@ struct Engine : EngineBase {
     ef.inverse = 0;
     ef.scale = 1.0;
     ef.ks = ks;
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Tf.as<R>(), ef, nsm, s, false));
+    DPST_CUDA(zgemm((R *)sp, Tf.as<R>(), ef, false, s, ztc));
     mark(3, s);
     if (!use_static_scratch) {
       DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
@@ -412,7 +468,7 @@ struct Engine : EngineBase {
     eb.inverse = 1;
     eb.scale = 1.0 / ((double)nx * (double)ny);
     eb.corr = corr.as<double2>();
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, Ti.as<R>(), eb, nsm, s, true));
+    DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s, ztc));
     mark(5, s);
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
@@ -535,9 +591,9 @@ struct Engine : EngineBase {
     e.inverse = 0;
     e.scale = 1.0;
     e.ks = ks;
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TiT.as<R>(), e, nsm, s, false));
+    DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s, ztc));
     DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
-    DPST_CUDA(launch_zgemm<R>((R *)sp, nz, 2 * nk, TfTn.as<R>(), e, nsm, s, true));
+    DPST_CUDA(zgemm((R *)sp, TfTn.as<R>(), e, true, s, ztc));
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)g2));
@@ -648,6 +704,9 @@ struct Engine : EngineBase {
     // forward z GEMM, BVP pairs + k=0, inverse z GEMM, interp (mono [+ dip])
     int nbuf = (ghm.top != nullptr) + (ghm.bot != nullptr) + (ghd.top != nullptr) + (ghd.bot != nullptr);
     o->ghost_layers_in_use = nbuf;
+    o->ztransform = ztc;
+    o->ztransform_ms[0] = ztc_ms[0];
+    o->ztransform_ms[1] = ztc_ms[1];
     o->kernels_per_mdot = (p.has_torque ? 2 : 1) + 2 * nbuf + 1 + 2 + 1 + (p.has_torque ? 2 : 1);
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,

@@ -148,4 +148,77 @@ static __device__ void slit_coeffs(double kx, double ky, double Hs, double eta, 
   zsolve8(A, c);
 }
 
+// Wall correction of one mode at node m for component d, evaluated in the
+// operator's arithmetic CT (FP64 for the plain operator, FP32 for the mixed
+// one); the coefficients themselves come from the FP64 solve.
+template <typename CT>
+struct cplx {
+  CT x, y;
+};
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> mk(CT x, CT y) { cplx<CT> r; r.x = x; r.y = y; return r; }
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> operator+(cplx<CT> a, cplx<CT> b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> operator*(CT s, cplx<CT> a) { return mk(s * a.x, s * a.y); }
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> ik(CT k, cplx<CT> a) { return mk(-k * a.y, k * a.x); }
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> conj(cplx<CT> a) { return mk(a.x, -a.y); }
+template <typename CT>
+static __device__ __forceinline__ cplx<CT> ld(const double2 &v) { return mk((CT)v.x, (CT)v.y); }
+
+template <typename R>
+static __device__ __forceinline__ void corr_value(const EpiArgs &e, int d, int m, int64_t mode, R &re, R &im) {
+  typedef R CT;
+  re = 0;
+  im = 0;
+  const KsArgs &a = e.ks;
+  if (a.mode == 0 || mode == 0) return;
+  const int ix = (int)(mode % a.nxh), iy = (int)(mode / a.nxh);
+  const double kxd = a.kvx[ix], kyd = a.kvy[iy];
+  double kxpd, kypd;
+  const bool herm = mode_is_hermitian(a, ix, iy, kxd, kyd, kxpd, kypd);
+  const CT k = (CT)sqrt(kxd * kxd + kyd * kyd);
+  const CT z = (CT)a.zn[m];
+  const double2 *cr = e.corr + mode * 16;
+  const CT enkz = exp(-k * z);
+  const CT zenkz = z * enkz;
+  cplx<CT> acc = mk<CT>(0, 0);
+  const int npass = herm ? 1 : 2;
+  for (int pass = 0; pass < npass; ++pass) {
+    const CT qx = (CT)(pass ? kxpd : kxd), qy = (CT)(pass ? kypd : kyd);
+    cplx<CT> v;
+    if (a.mode == 1) {
+      // DPTools.cpp:627-641, velocity rows
+      cplx<CT> f0 = ld<CT>(cr[0]), f1 = ld<CT>(cr[1]), f2 = ld<CT>(cr[2]);
+      if (pass) { f0 = conj(f0); f1 = conj(f1); f2 = conj(f2); }
+      const cplx<CT> al = (qx * f0 + qy * f1) + ik(k, f2);
+      if (d == 0) v = (-qx * zenkz / k) * al + enkz * f0;
+      else if (d == 1) v = (-qy * zenkz / k) * al + enkz * f1;
+      else v = ik(-zenkz, al) + enkz * f2;
+    } else {
+      // DPTools.cpp:795-815 with e^{k(z-H)} evaluated directly
+      const double2 *c = cr + 8 * pass;
+      const CT fac = (CT)(1.0 / 2.0 / a.eta);
+      const CT ekzmh = exp(k * (z - (CT)a.Lz));
+      const CT zekzmh = z * ekzmh;
+      if (d == 0)
+        v = (ik(-qx * zenkz * fac / k, ld<CT>(c[0])) + ik(qx * zekzmh * fac / k, ld<CT>(c[1]))) +
+            (enkz * ld<CT>(c[2]) + ekzmh * ld<CT>(c[3]));
+      else if (d == 1)
+        v = (ik(-qy * zenkz * fac / k, ld<CT>(c[0])) + ik(qy * zekzmh * fac / k, ld<CT>(c[1]))) +
+            (enkz * ld<CT>(c[4]) + ekzmh * ld<CT>(c[5]));
+      else
+        v = ((zenkz * fac) * ld<CT>(c[0]) + (zekzmh * fac) * ld<CT>(c[1])) +
+            (enkz * ld<CT>(c[6]) + ekzmh * ld<CT>(c[7]));
+    }
+    if (pass) v = conj(v);
+    acc = acc + v;
+  }
+  if (npass == 2) acc = (CT)0.5 * acc;
+  re = acc.x;
+  im = acc.y;
+}
+
 }  // namespace dpst

@@ -112,6 +112,10 @@ typedef struct dpst_info {
   int kernels_per_mdot; /* kernels of this library one dpst_mdot launches (with T
                            and W given); cuFFT kernels and memsets not counted */
   int ghost_layers_in_use; /* open-end ghost buffers the current positions need */
+  int ztransform;          /* z-transform kernel chosen at creation: 0 FP32/FP64 SIMT
+                              (even/odd folded), 1 tcgen05 split-TF32 (mixed only) */
+  float ztransform_ms[2];  /* creation-time timings of one transform: SIMT, tcgen05
+                              (0 if not timed) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

@@ -1,0 +1,80 @@
+"""The tcgen05 split-TF32 z transform of the mixed operator against the SIMT
+transform and the FP64 operator (forced with DPSTOKES_GB300_ZTRANSFORM at
+creation): Mdot outputs within 5e-6 of each other and 1e-5 of FP64, on the
+small cases (odd and even nz, every geometry) and the open-domain c2
+geometry on a 192^2 x 128 grid; the backward pass likewise."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from conftest import rel_err  # noqa: E402
+from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _op(w, precision, impl, monkeypatch):
+    monkeypatch.setenv("DPSTOKES_GB300_ZTRANSFORM", impl)
+    op = DPStokes(StokesParams.from_workload(w, precision), w.N)
+    monkeypatch.delenv("DPSTOKES_GB300_ZTRANSFORM")
+    return op
+
+
+def _mdot(op, X, F, T, dtype):
+    op.set_positions(torch.tensor(X, device="cuda"))
+    V, Wv = op.mdot(torch.tensor(F, dtype=dtype, device="cuda"),
+                    torch.tensor(T, dtype=dtype, device="cuda") if T is not None else None)
+    torch.cuda.synchronize()
+    return V.double().cpu().numpy(), (Wv.double().cpu().numpy() if Wv is not None else None)
+
+
+CASES = [w.name for w in W.SMALL] + ["p2_dp_n8192_192"]
+
+
+def _wl(name):
+    return W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tcgen05_ztransform_matches(name, monkeypatch):
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    tc = _op(w, "mixed", "tcgen05", monkeypatch)
+    info = tc.info()
+    assert info["ztransform"] == 1, info
+    si = _op(w, "mixed", "simt", monkeypatch)
+    assert si.info()["ztransform"] == 0
+    f64 = _op(w, "fp64", "auto", monkeypatch)
+    Vt, Wt = _mdot(tc, X, F, T, torch.float32)
+    Vs, Ws = _mdot(si, X, F, T, torch.float32)
+    Vd, Wd = _mdot(f64, X, F, T, torch.float64)
+    e_ts, e_td, e_sd = rel_err(Vt, Vs), rel_err(Vt, Vd), rel_err(Vs, Vd)
+    print("%s tc-simt %.2e tc-fp64 %.2e simt-fp64 %.2e (ms simt %.3f tc %.3f)" %
+          (name, e_ts, e_td, e_sd, info["ztransform_ms"][0], info["ztransform_ms"][1]))
+    assert e_ts < 5e-6 and e_td < 1e-5
+    if T is not None:
+        assert rel_err(Wt, Ws) < 5e-6 and rel_err(Wt, Wd) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["s_dpbw_t", "s_dpsc_t", "s_dp_t_shift"])
+def test_tcgen05_backward(name, monkeypatch):
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    rng = np.random.default_rng(2)
+    gV = rng.standard_normal((w.N, 3))
+    gW = rng.standard_normal((w.N, 3)) if T is not None else None
+    out = {}
+    for key, prec, impl, dt in (("tc", "mixed", "tcgen05", torch.float32), ("d", "fp64", "auto", torch.float64)):
+        op = _op(w, prec, impl, monkeypatch)
+        op.set_positions(torch.tensor(X, device="cuda"))
+        g = op.mdot_backward(torch.tensor(F, dtype=dt, device="cuda"),
+                             torch.tensor(T, dtype=dt, device="cuda") if T is not None else None,
+                             torch.tensor(gV, dtype=dt, device="cuda"),
+                             torch.tensor(gW, dtype=dt, device="cuda") if gW is not None else None,
+                             need_T=T is not None)
+        torch.cuda.synchronize()
+        out[key] = [x.double().cpu().numpy() if x is not None else None for x in g]
+    for a, b in zip(out["tc"], out["d"]):
+        if a is not None:
+            assert rel_err(a, b) < 1e-4
