@@ -241,6 +241,15 @@ def run_ours(args, rank, world):
     roof = {"bound": "hbm", "stage": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
             "traffic": None, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+    # every stage against HBM from the same CUDA-event stage times
+    roof["stages"] = {}
+    for k in stage_names:
+        b = algorithmic_bytes(k, w, prec)
+        if b and stages[k] > 0:
+            gbs = b / (stages[k] * 1e-3) / 1e9
+            roof["stages"][k] = {"ms": round(stages[k], 4), "algorithmic_bytes": b,
+                                 "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
+    roof["ztransform_kernel"] = "tcgen05 split-TF32" if info.get("ztransform") == 1 else "SIMT folded"
     if dom == "solve":
         # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
         roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "
