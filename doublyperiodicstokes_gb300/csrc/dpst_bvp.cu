@@ -35,6 +35,7 @@ constexpr int BVP_MODES = BVP_LANES / 2;
 struct BvpCtx {
   double *Xs;  // [(nz + 2)][BVP_LANES] penta / RHS columns
   const double *S0, *SM2, *SP2, *FM1, *FP1, *DH;
+  const double *S0e, *SM2e, *SP2e;  // SIMat bands / eta (velocity windows)
   double *CPs;        // this lane's pressure coefficients, row j at CPs[j * GT]
   const double *CPo;  // the partner lane's
   int GT, tid;
@@ -49,12 +50,17 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
   c.Xs = bvp_sm;
   double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
   double *DH = FP1 + nz;
+  double *S0e = DH + nz + 1, *SM2e = S0e + nz, *SP2e = SM2e + nz;
+  const double inv_eta = 1.0 / a.eta;
   for (int t = tid; t < nz; t += T) {
     S0[t] = a.s0[t];
     SM2[t] = a.sm2[t];
     SP2[t] = a.sp2[t];
     FM1[t] = a.fm1[t];
     FP1[t] = a.fp1[t];
+    S0e[t] = a.s0[t] * inv_eta;
+    SM2e[t] = a.sm2[t] * inv_eta;
+    SP2e[t] = a.sp2[t] * inv_eta;
   }
   for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
   c.S0 = S0;
@@ -63,6 +69,9 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
   c.FM1 = FM1;
   c.FP1 = FP1;
   c.DH = DH;
+  c.S0e = S0e;
+  c.SM2e = SM2e;
+  c.SP2e = SP2e;
   // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
   // in global memory (L2 resident: a few tens of MB)
   c.GT = gridDim.x * T;
@@ -73,8 +82,12 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
 }
 
 // The solve of one wavenumber i for this lane (lane 2q: real part, 2q + 1:
-// imaginary part); both lanes of a pair run it together (shuffles).
-template <typename R>
+// imaginary part); both lanes of a pair run it together (shuffles).  The
+// velocity solves run on the right-hand sides times eta (the 1/eta of
+// DPTools.cpp:197-216 moves into the window's SIMat bands and the BC values
+// are scaled by eta), which saves a multiply per row.  WALLS = false (open
+// domain) skips the wall values that only the corrections use.
+template <typename R, bool WALLS>
 static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
                                                 int i, bool store, const BvpCtx &ctx) {
   const int nz = a.nz;
@@ -83,12 +96,12 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   const int tid = ctx.tid, part = tid & 1;
   double *Xs = ctx.Xs;
   const double *S0 = ctx.S0, *SM2 = ctx.SM2, *SP2 = ctx.SP2, *FM1 = ctx.FM1, *FP1 = ctx.FP1, *DH = ctx.DH;
+  const double *S0e = ctx.S0e, *SM2e = ctx.SM2e, *SP2e = ctx.SP2e;
   double *__restrict__ CPs = ctx.CPs;
   const double *__restrict__ CPo = ctx.CPo;
   const int GT = ctx.GT;
 #define XS(j) Xs[(j) * T + tid]
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
-  const double inv_eta = 1.0 / a.eta;
   const int rs = 2 * nk;  // spectrum row stride (R elements)
   // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
   R *__restrict__ sp_own = spec + 2 * i + part;
@@ -217,7 +230,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       *cpw = c;
       ssum += c;
       asum += odd ? -c : c;
-      XS(m) = inv_eta * (dpv - ld_fp64(f2s));  // z-velocity RHS (DPTools.cpp:214)
+      XS(m) = dpv - ld_fp64(f2s);  // eta x z-velocity RHS (DPTools.cpp:214)
       f2s += rs;
       cpw += GT;
     });
@@ -225,8 +238,8 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   // velocity BC right-hand sides (DPTools.cpp:218-234)
   const double ssum_o = __shfl_xor_sync(0xffffffffu, ssum, 1);
   const double asum_o = __shfl_xor_sync(0xffffffffu, asum, 1);
-  const double fac1 = 2.0 * a.eta, fac = fac1 * K;
-  const double ifac = 1.0 / fac, ifac1 = 1.0 / fac1;
+  // eta x the BC values: 1/(2 eta K) -> 1/(2 K), 1/(2 eta) -> 1/2
+  const double ifac = 0.5 / K, ifac1 = 0.5;
   double bc[6];
   bc[0] = -ifac * ((Dx * sp) * ssum_o);
   bc[1] = ifac * ((Dx * sp) * asum_o);
@@ -237,6 +250,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   __syncwarp();  // the partner's pressure coefficients are read below
 
   // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
+  const double inv_eta_w = 1.0 / a.eta;
   double wt[3], wb[3];
 #pragma unroll
   for (int cc = 0; cc < 3; ++cc) {
@@ -247,7 +261,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       const double *cpo = CPo;
 #pragma unroll 4
       for (int j = 0; j < nz; ++j) {
-        XS(j) = inv_eta * (Dc * *cpo - ld_fp64(fs));
+        XS(j) = Dc * *cpo - ld_fp64(fs);
         fs += rs;
         cpo += GT;
       }
@@ -258,19 +272,26 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
     double st = 0.0, sb = 0.0;
     R *us = sp_own + c * nz * rs;
+    const double se0e = a.se0 * inv_eta_w, se1e = a.se1 * inv_eta_w;
     window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
-      double u = S0[m] * x0;
-      if (head == 0) u = SM2[m] * xm2 + u;
-      u = u + SP2[m] * x2;
-      if (head == 1) u += a.se0 * g0;
-      if (head == 2) u += a.se1 * g1;
+      double u = S0e[m] * x0;
+      if (head == 0) u = SM2e[m] * xm2 + u;
+      u = u + SP2e[m] * x2;
+      if (head == 1) u += se0e * g0;
+      if (head == 2) u += se1e * g1;
       if (store) *us = to_r<R>(u);
-      st += u;
-      sb += odd ? -u : u;
+      if (WALLS) {
+        st += u;
+        sb += odd ? -u : u;
+      }
       us += rs;
     });
     wt[c] = st;
     wb[c] = sb;
+  }
+  if (!WALLS) {
+    __syncwarp();  // XS/CPS reuse in the next tile
+    return;
   }
   // wall-correction coefficients (evalTheta at z = 0 and z = Lz)
   double wto[3], wbo[3];
@@ -323,7 +344,9 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
     if (base + (tid >> 5) * 16 >= cta_end) continue;  // warp-uniform
     const int i_raw = base + q;
     const int i = i_raw < cta_end ? i_raw : cta_end - 1;
-    bvp_mode<R>(a, spec, corr, i, (i_raw < cta_end) && (i != 0), ctx);  // mode 0: k_bvp_k0
+    const bool store = (i_raw < cta_end) && (i != 0);  // mode 0: k_bvp_k0
+    if (a.mode != 0) bvp_mode<R, true>(a, spec, corr, i, store, ctx);
+    else bvp_mode<R, false>(a, spec, corr, i, store, ctx);
   }
 }
 
@@ -348,7 +371,9 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs_b(const SysK<R> *__rest
     const int s = find_sys(mprefix, S, g);
     const SysK<R> &y = sys[s];
     const int i = (int)(g - mprefix[s]);
-    bvp_mode<R>(y.ks, y.spec, y.corr, i, (g_raw < cta_end) && (i != 0), ctx);
+    const bool store = (g_raw < cta_end) && (i != 0);
+    if (y.ks.mode != 0) bvp_mode<R, true>(y.ks, y.spec, y.corr, i, store, ctx);
+    else bvp_mode<R, false>(y.ks, y.spec, y.corr, i, store, ctx);
   }
 }
 
@@ -422,7 +447,7 @@ __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restr
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 6 * (size_t)a.nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 9 * (size_t)a.nz + 1);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -441,7 +466,7 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
 // Batched solve: grid and scratch for K modes in total with a shared nz.
 template <typename R>
 cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 6 * (size_t)nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 9 * (size_t)nz + 1);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -460,7 +485,7 @@ cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratc
 template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 6 * (size_t)nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 9 * (size_t)nz + 1);
   const int64_t per = (K + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   k_bvp_pairs_b<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
@@ -480,7 +505,7 @@ template cudaError_t launch_bvp_b<double>(const SysK<double> *, int, const int64
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 6 * (size_t)a.nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 9 * (size_t)a.nz + 1);
   const int64_t per = (a.nk + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
