@@ -39,12 +39,16 @@ void launch_locate(bool dipole, const double *pos, int64_t N, const KernelDesc &
                    cudaStream_t s);
 template <typename R, typename RF>
 void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s);
+                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s, const int *perm = nullptr);
+template <typename R>
+void launch_tile_order(int64_t N, const GridArgs &g, const Stencils<R> &st, int *count, int *start, int *perm,
+                       cudaStream_t s);
+size_t tile_order_tiles(int nx, int ny);
 template <typename R>
 void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s);
 template <typename R, typename RV>
 void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s);
+                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s, const int *perm = nullptr);
 
 
 void launch_bvp_factors(const KsArgs &a, cudaStream_t s);
@@ -123,6 +127,7 @@ struct Engine : EngineBase {
   DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g, fac_pm, fac_pb, fac_pa;
   DevBuf pos64, flags;
+  DevBuf ord_count, ord_start, perm;  // particles sorted by grid tile
   DevBuf st_m[8], st_d[8];
   DevBuf gh_m[2], gh_d[2];
   DevBuf hF, hT, hV, hW;  // staging for the host-array entry points
@@ -230,6 +235,11 @@ struct Engine : EngineBase {
     flags.alloc(sizeof(int) * 8);
     alloc_stencils(km.d, false, st_m, stm);
     if (p.has_torque) alloc_stencils(kd.d, true, st_d, std_);
+    // particle order by grid tile (set_positions), used by the spread and
+    // interpolation kernels
+    ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
+    ord_start.alloc(sizeof(int) * (tile_order_tiles(nx, ny) + 1));
+    perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
     memset(&ghm, 0, sizeof(ghm));
     memset(&ghd, 0, sizeof(ghd));
     // FFT plans: batched 2-D over (y, x) for each (component, z) plane
@@ -316,6 +326,8 @@ struct Engine : EngineBase {
                        fl + 3, s);
     DPST_CUDA(cudaGetLastError());
     int out[8];
+    launch_tile_order<R>(N, g, stm, ord_count.as<int>(), ord_start.as<int>(), perm.as<int>(), s);
+    DPST_CUDA(cudaGetLastError());
     DPST_CUDA(cudaMemcpyAsync(out, fl, sizeof(out), cudaMemcpyDeviceToHost, s));
     DPST_CUDA(cudaStreamSynchronize(s));
     if (out[0] & 1) {
@@ -357,8 +369,8 @@ struct Engine : EngineBase {
       if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
       if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
     }
-    launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s);
-    if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s);
+    launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s, perm.as<int>());
+    if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s, perm.as<int>());
     launch_ghost_fold<R>(ghm.top, ghm.ntop, nx, ny, km.d, s);
     launch_ghost_fold<R>(ghm.bot, ghm.nbot, nx, ny, km.d, s);
     if (torque) {
@@ -486,13 +498,13 @@ struct Engine : EngineBase {
     spread_stage<RF>(F, T, s);
     mark(1, s);
     solve_stage(s);
-    launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s);
+    launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
     if (p.has_torque && W != nullptr) {
       // without torques the reference's torque grid still holds the last
       // z-derivative spread; with T = NULL it is zero
       Ghosts<R> gz = ghd;
       if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
-      launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s);
+      launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s, perm.as<int>());
     }
     DPST_CUDA(cudaGetLastError());
     mark(7, s);
@@ -633,7 +645,7 @@ struct Engine : EngineBase {
     }
     Stencils<R> sw = stm;
     sw.phz = stm.phzw;  // the interpolation's weights
-    launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, gham, s);
+    launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, gham, s, perm.as<int>());
     if (gW) launch_adj_spread_dip<R, RF>(gW, N, kd.d, g, std_, g2, ghd_a, s);
     launch_ghost_fold_t<R>(gham.top, gham.ntop, nx, ny, km.d, s);
     launch_ghost_fold_t<R>(gham.bot, gham.nbot, nx, ny, km.d, s);
@@ -711,7 +723,7 @@ struct Engine : EngineBase {
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
-                           &fac_g, &pos64, &flags, &dphzw_buf};
+                           &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;

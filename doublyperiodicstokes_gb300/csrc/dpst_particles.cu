@@ -150,14 +150,17 @@ static __device__ __forceinline__ void spread_mono_item(int64_t p, int c, const 
   }
 }
 
+// perm (optional): particles taken in this order (sorted by tile, so that
+// neighbouring threads update nearby grid cells).
 template <typename R, typename RF>
 __global__ void k_spread_mono(const RF *__restrict__ F, int64_t N, KernelDesc kd, GridArgs g,
-                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh, const int *__restrict__ perm) {
   const int cols = kd.wx * kd.wy;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N * cols) return;
-  const int64_t p = t / cols;
-  spread_mono_item<R, RF>(p, (int)(t - p * cols), F, kd, g, st, grid, gh);
+  const int64_t q = t / cols;
+  const int64_t p = perm ? (int64_t)perm[q] : q;
+  spread_mono_item<R, RF>(p, (int)(t - q * cols), F, kd, g, st, grid, gh);
 }
 
 // ---------------------------------------------------------------------------
@@ -219,14 +222,17 @@ static __device__ __forceinline__ void spread_dip_item(int64_t p, int c, const R
   }
 }
 
+// perm (optional): particles taken in this order (sorted by tile, so that
+// neighbouring threads update nearby grid cells).
 template <typename R, typename RF>
 __global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd, GridArgs g,
-                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh) {
+                            Stencils<R> st, R *__restrict__ grid, Ghosts<R> gh, const int *__restrict__ perm) {
   const int cols = kd.wx * kd.wy;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= N * cols) return;
-  const int64_t p = t / cols;
-  spread_dip_item<R, RF>(p, (int)(t - p * cols), T, kd, g, st, grid, gh);
+  const int64_t q = t / cols;
+  const int64_t p = perm ? (int64_t)perm[q] : q;
+  spread_dip_item<R, RF>(p, (int)(t - q * cols), T, kd, g, st, grid, gh);
 }
 
 // ---------------------------------------------------------------------------
@@ -326,11 +332,14 @@ static __device__ __forceinline__ void interp_mono_item(int64_t p, int lane, con
   }
 }
 
+// perm (optional): the order in which warps take particles (sorted by tile,
+// for locality of the grid reads).
 template <typename R, typename RV>
 __global__ void k_interp_mono(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
-                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ V) {
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (p >= N) return;
+                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ V, const int *__restrict__ perm) {
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= N) return;
+  const int64_t p = perm ? (int64_t)perm[w] : w;
   interp_mono_item<R, RV>(p, threadIdx.x & 31, grid, kd, g, st, gh, V);
 }
 
@@ -388,11 +397,14 @@ static __device__ __forceinline__ void interp_dip_item(int64_t p, int lane, cons
   }
 }
 
+// perm (optional): the order in which warps take particles (sorted by tile,
+// for locality of the grid reads).
 template <typename R, typename RV>
 __global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc kd, GridArgs g,
-                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ W) {
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (p >= N) return;
+                            Stencils<R> st, Ghosts<R> gh, RV *__restrict__ W, const int *__restrict__ perm) {
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= N) return;
+  const int64_t p = perm ? (int64_t)perm[w] : w;
   interp_dip_item<R, RV>(p, threadIdx.x & 31, grid, kd, g, st, gh, W);
 }
 
@@ -531,13 +543,74 @@ void launch_locate(bool dipole, const double *pos, int64_t N, const KernelDesc &
 
 template <typename R, typename RF>
 void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s) {
+                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s, const int *perm) {
   int64_t tot = N * kd.wx * kd.wy;
   if (tot == 0) return;
   int bs = 256;
   int64_t nb = (tot + bs - 1) / bs;
-  if (dipole) k_spread_dip<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh);
-  else k_spread_mono<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh);
+  if (dipole) k_spread_dip<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh, perm);
+  else k_spread_mono<R, RF><<<nb, bs, 0, s>>>(FT, N, kd, g, st, grid, gh, perm);
+}
+
+// ---------------------------------------------------------------------------
+// Particle order by grid tile (once per set of positions): a counting sort of
+// the particles by the ORDER_TILE x ORDER_TILE column tile of their cell, so
+// that the spread's and the interpolation's neighbouring threads touch
+// neighbouring grid cells.  count holds ntiles ints, start ntiles + 1.
+// ---------------------------------------------------------------------------
+constexpr int ORDER_TILE = 8;
+
+template <typename R, bool FILL>
+__global__ void k_tile_order(int64_t N, GridArgs g, Stencils<R> st, int ntx, int *count, const int *start,
+                             int *perm) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  const int4 cl = st.cell[p];
+  const int t = (wrapi(cl.y, g.ny) / ORDER_TILE) * ntx + wrapi(cl.x, g.nx) / ORDER_TILE;
+  const int pos = atomicAdd(&count[t], 1);
+  if (FILL) perm[start[t] + pos] = (int)p;
+}
+
+// Exclusive prefix sum of n counts in one CTA of 1024 threads: start[0..n].
+__global__ void __launch_bounds__(1024) k_scan_counts(const int *__restrict__ count, int n, int *__restrict__ start) {
+  __shared__ int part[1024];
+  const int tid = threadIdx.x, chunk = (n + 1023) / 1024;
+  const int b = tid * chunk, e = min(b + chunk, n);
+  int sum = 0;
+  for (int i = b; i < e; ++i) sum += count[i];
+  part[tid] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const int v = (tid >= o) ? part[tid - o] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int run = part[tid] - sum;
+  for (int i = b; i < e; ++i) {
+    start[i] = run;
+    run += count[i];
+  }
+  if (tid == 1023) start[n] = part[1023];
+}
+
+template <typename R>
+void launch_tile_order(int64_t N, const GridArgs &g, const Stencils<R> &st, int *count, int *start, int *perm,
+                       cudaStream_t s) {
+  if (N == 0) return;
+  const int ntx = (g.nx + ORDER_TILE - 1) / ORDER_TILE, nty = (g.ny + ORDER_TILE - 1) / ORDER_TILE;
+  const int ntiles = ntx * nty;
+  const int bs = 256;
+  const int64_t nb = (N + bs - 1) / bs;
+  cudaMemsetAsync(count, 0, sizeof(int) * ntiles, s);
+  k_tile_order<R, false><<<nb, bs, 0, s>>>(N, g, st, ntx, count, nullptr, nullptr);
+  k_scan_counts<<<1, 1024, 0, s>>>(count, ntiles, start);
+  cudaMemsetAsync(count, 0, sizeof(int) * ntiles, s);
+  k_tile_order<R, true><<<nb, bs, 0, s>>>(N, g, st, ntx, count, start, perm);
+}
+
+size_t tile_order_tiles(int nx, int ny) {
+  return (size_t)((nx + ORDER_TILE - 1) / ORDER_TILE) * ((ny + ORDER_TILE - 1) / ORDER_TILE);
 }
 
 template <typename R>
@@ -552,12 +625,12 @@ void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd,
 
 template <typename R, typename RV>
 void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s) {
+                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s, const int *perm) {
   if (N == 0) return;
   int bs = 256;
   int64_t nb = (N * 32 + bs - 1) / bs;
-  if (dipole) k_interp_dip<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out);
-  else k_interp_mono<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out);
+  if (dipole) k_interp_dip<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out, perm);
+  else k_interp_mono<R, RV><<<nb, bs, 0, s>>>(grid, N, kd, g, st, gh, out, perm);
 }
 
 #define DPST_INST(R)                                                                           \
@@ -567,16 +640,18 @@ void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, 
   template void launch_ghost_fold<R>(R *, int, int, int, const KernelDesc &, cudaStream_t);     \
   template void launch_spread<R, float>(bool, const float *, int64_t, const KernelDesc &,      \
                                         const GridArgs &, const Stencils<R> &, R *,            \
-                                        const Ghosts<R> &, cudaStream_t);                      \
+                                        const Ghosts<R> &, cudaStream_t, const int *);         \
   template void launch_spread<R, double>(bool, const double *, int64_t, const KernelDesc &,    \
                                          const GridArgs &, const Stencils<R> &, R *,           \
-                                         const Ghosts<R> &, cudaStream_t);                     \
+                                         const Ghosts<R> &, cudaStream_t, const int *);        \
   template void launch_interp<R, float>(bool, const R *, int64_t, const KernelDesc &,          \
                                         const GridArgs &, const Stencils<R> &,                 \
-                                        const Ghosts<R> &, float *, cudaStream_t);             \
+                                        const Ghosts<R> &, float *, cudaStream_t, const int *);\
   template void launch_interp<R, double>(bool, const R *, int64_t, const KernelDesc &,         \
                                          const GridArgs &, const Stencils<R> &,                \
-                                         const Ghosts<R> &, double *, cudaStream_t);
+                                         const Ghosts<R> &, double *, cudaStream_t, const int *);\
+  template void launch_tile_order<R>(int64_t, const GridArgs &, const Stencils<R> &, int *, int *, \
+                                     int *, cudaStream_t);
 
 DPST_INST(float)
 DPST_INST(double)
