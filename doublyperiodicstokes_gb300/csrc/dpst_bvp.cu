@@ -146,42 +146,104 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
   // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
   // mf and the dp2 of the last two rows are zero, so both loops are uniform.
+  // The factor streams are read PF_F / PF_B rows ahead of the recurrence
+  // through register rings (prefetch indices clamped into the table), and
+  // the border dots accumulate in two partial sums (rows of even and odd
+  // distance from the last), which halves their FP64 dependency chains.
   auto penta = [&](double &y0, double &y1) {
+    constexpr int PF_F = 8, PF_B = 4;
     double xm2 = 0.0, xm1 = 0.0;
-    const double *p = mf0;
-#pragma unroll 8
-    for (int j = 0; j < nz; ++j) {
-      const double v = XS(j) - __ldg(p) * xm2;
-      XS(j) = v;
-      xm2 = xm1;
-      xm1 = v;
-      p += nk;
+    double pm[PF_F];
+#pragma unroll
+    for (int k = 0; k < PF_F; ++k) pm[k] = __ldg(mf0 + min(k, nz - 1) * nk);
+    int j = 0;
+    for (; j + PF_F <= nz; j += PF_F) {
+#pragma unroll
+      for (int k = 0; k < PF_F; ++k) {
+        const double m = pm[k];
+        pm[k] = __ldg(mf0 + min(j + PF_F + k, nz - 1) * nk);
+        const double v = XS(j + k) - m * xm2;
+        XS(j + k) = v;
+        xm2 = xm1;
+        xm1 = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PF_F - 1; ++k) {
+      if (j + k < nz) {  // warp-uniform tail
+        const double v = XS(j + k) - pm[k] * xm2;
+        XS(j + k) = v;
+        xm2 = xm1;
+        xm1 = v;
+      }
     }
     double xp2 = 0.0, xp1 = 0.0;
-    y0 = 0.0;
-    y1 = 0.0;
-    const double2 *b = bk0 + (nz - 1) * rs;
-#pragma unroll 8
-    for (int j = nz - 1; j >= 0; --j) {
-      const double2 ibd = __ldg(b), cc = __ldg(b + 1);
-      const double v = ibd.x * (XS(j) - ibd.y * xp2);
-      XS(j) = v;
-      y0 += cc.x * v;
-      y1 += cc.y * v;
-      xp2 = xp1;
-      xp1 = v;
-      b -= rs;
+    double ya0 = 0.0, ya1 = 0.0, yb0 = 0.0, yb1 = 0.0;
+    double2 pi[PF_B], pc[PF_B];
+#pragma unroll
+    for (int k = 0; k < PF_B; ++k) {
+      const double2 *b = bk0 + max(nz - 1 - k, 0) * rs;
+      pi[k] = __ldg(b);
+      pc[k] = __ldg(b + 1);
     }
+    j = nz - 1;
+    for (; j - PF_B + 1 >= 0; j -= PF_B) {
+#pragma unroll
+      for (int k = 0; k < PF_B; ++k) {
+        const double2 ibd = pi[k], cc = pc[k];
+        const double2 *b = bk0 + max(j - k - PF_B, 0) * rs;
+        pi[k] = __ldg(b);
+        pc[k] = __ldg(b + 1);
+        const double v = ibd.x * (XS(j - k) - ibd.y * xp2);
+        XS(j - k) = v;
+        if (k & 1) {
+          yb0 += cc.x * v;
+          yb1 += cc.y * v;
+        } else {
+          ya0 += cc.x * v;
+          ya1 += cc.y * v;
+        }
+        xp2 = xp1;
+        xp1 = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PF_B - 1; ++k) {
+      if (j - k >= 0) {  // warp-uniform tail
+        const double v = pi[k].x * (XS(j - k) - pi[k].y * xp2);
+        XS(j - k) = v;
+        if (k & 1) {
+          yb0 += pc[k].x * v;
+          yb1 += pc[k].y * v;
+        } else {
+          ya0 += pc[k].x * v;
+          ya1 += pc[k].y * v;
+        }
+        xp2 = xp1;
+        xp1 = v;
+      }
+    }
+    y0 = ya0 + yb0;
+    y1 = ya1 + yb1;
   };
   // Window pass over the border-corrected solution x_m = X_m - (A^{-1}B g)_m
   // (x_nz = g0, x_nz+1 = g1): row m sees x_{m-2} .. x_{m+2} and applies
   // the SIMat / FIMat bands.  Rows 0, 1 (border columns) and nz-2, nz-1
   // (x_{m+2} is g) are peeled; the main loop takes rows in (even, odd)
-  // pairs so that the parity of the border column is static.
+  // pairs so that the parity of the border column is static, with the
+  // A^{-1}B column read PF_W pairs ahead through a register ring.
   auto window = [&](double g0, double g1, auto &&row) {
-    const double *abp = ab0 + 2 * nk;
+    constexpr int PF_W = 4;
     double xm2 = 0.0, xm1 = 0.0;
     double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
+    const double ab2 = __ldg(ab0 + min(2, nz - 1) * nk), ab3 = __ldg(ab0 + min(3, nz - 1) * nk);
+    // ring slot q holds the A^{-1}B rows of main-loop pair q: 4 + 2q, 5 + 2q
+    double pa[PF_W][2];
+#pragma unroll
+    for (int q = 0; q < PF_W; ++q) {
+      pa[q][0] = __ldg(ab0 + min(4 + 2 * q, nz - 1) * nk);
+      pa[q][1] = __ldg(ab0 + min(5 + 2 * q, nz - 1) * nk);
+    }
     auto step = [&](int m, double x2, bool odd, int head) {
       row(m, xm2, xm1, x0, x1, x2, odd, head);
       xm2 = xm1;
@@ -189,20 +251,30 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       x0 = x1;
       x1 = x2;
     };
-    step(0, XS(2) - __ldg(abp) * g0, false, 1);
-    abp += nk;
-    step(1, XS(3) - __ldg(abp) * g1, true, 2);
-    abp += nk;
+    step(0, XS(2) - ab2 * g0, false, 1);
+    step(1, XS(3) - ab3 * g1, true, 2);
     int m = 2;
-#pragma unroll 2
-    for (; m + 1 <= nz - 3; m += 2) {
-      step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
-      abp += nk;
-      step(m + 1, XS(m + 3) - __ldg(abp) * g1, true, 0);
-      abp += nk;
+    for (; m + 2 * PF_W - 1 <= nz - 3; m += 2 * PF_W) {
+#pragma unroll
+      for (int q = 0; q < PF_W; ++q) {
+        const int mm = m + 2 * q;
+        const double a0 = pa[q][0], a1 = pa[q][1];
+        pa[q][0] = __ldg(ab0 + min(mm + 2 + 2 * PF_W, nz - 1) * nk);
+        pa[q][1] = __ldg(ab0 + min(mm + 3 + 2 * PF_W, nz - 1) * nk);
+        step(mm, XS(mm + 2) - a0 * g0, false, 0);
+        step(mm + 1, XS(mm + 3) - a1 * g1, true, 0);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < PF_W - 1; ++q) {
+      if (m + 1 <= nz - 3) {  // warp-uniform tail pairs
+        step(m, XS(m + 2) - pa[q][0] * g0, false, 0);
+        step(m + 1, XS(m + 3) - pa[q][1] * g1, true, 0);
+        m += 2;
+      }
     }
     if (m <= nz - 3) {  // odd nz: one more even row
-      step(m, XS(m + 2) - __ldg(abp) * g0, false, 0);
+      step(m, XS(m + 2) - __ldg(ab0 + (m + 2) * nk) * g0, false, 0);
       ++m;
     }
     step(nz - 2, g0, ((nz - 2) & 1) != 0, 0);
@@ -211,7 +283,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
 
   // ---- pressure: Schur solve, cp = S [x; g] (kept), dp = F [x; g] used at
   // once for the z-velocity RHS, which overwrites XS behind the window
-  double ssum = 0.0, asum = 0.0;
+  double se = 0.0, so = 0.0;  // sums of the even and odd coefficients
   {
     double y0, y1;
     penta(y0, y1);
@@ -228,14 +300,16 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       if (head != 1) dpv = FM1[m] * xm1 + dpv;
       if (head == 1) dpv += a.fe * g1;
       *cpw = c;
-      ssum += c;
-      asum += odd ? -c : c;
+      if (odd) so += c;
+      else se += c;
       XS(m) = dpv - ld_fp64(f2s);  // eta x z-velocity RHS (DPTools.cpp:214)
       f2s += rs;
       cpw += GT;
     });
   }
-  // velocity BC right-hand sides (DPTools.cpp:218-234)
+  // velocity BC right-hand sides (DPTools.cpp:218-234): the pressure at
+  // z = +-1 is the sum and the alternating sum of its coefficients
+  const double ssum = se + so, asum = se - so;
   const double ssum_o = __shfl_xor_sync(0xffffffffu, ssum, 1);
   const double asum_o = __shfl_xor_sync(0xffffffffu, asum, 1);
   // eta x the BC values: 1/(2 eta K) -> 1/(2 K), 1/(2 eta) -> 1/2
@@ -270,7 +344,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     penta(y0, y1);
     const double r0 = y0 - bc[2 * c], r1 = y1 - bc[2 * c + 1];
     const double g0 = G00 * r0 + G01 * r1, g1 = G10 * r0 + G11 * r1;
-    double st = 0.0, sb = 0.0;
+    double ue = 0.0, uo = 0.0;  // sums of the even and odd coefficients
     R *us = sp_own + c * nz * rs;
     const double se0e = a.se0 * inv_eta_w, se1e = a.se1 * inv_eta_w;
     window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
@@ -281,13 +355,13 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       if (head == 2) u += se1e * g1;
       if (store) *us = to_r<R>(u);
       if (WALLS) {
-        st += u;
-        sb += odd ? -u : u;
+        if (odd) uo += u;
+        else ue += u;
       }
       us += rs;
     });
-    wt[c] = st;
-    wb[c] = sb;
+    wt[c] = ue + uo;  // u(z = 1), u(z = -1)
+    wb[c] = ue - uo;
   }
   if (!WALLS) {
     __syncwarp();  // XS/CPS reuse in the next tile
@@ -330,7 +404,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
 // time; a warp whose 16 modes lie past the CTA's range skips the tile, so
 // the last, partial tile of every CTA costs only the warps it needs.
 template <typename R>
-__global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
+__global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
                                                          double2 *__restrict__ corr,
                                                          double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
@@ -354,7 +428,7 @@ __global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs(KsArgs a, R *__restrict
 // mprefix[s] <= g < mprefix[s+1]; every system has the same nz and H (the
 // shared-memory tables), its own factors, spectrum and corrections.
 template <typename R>
-__global__ void __launch_bounds__(BVP_LANES) k_bvp_pairs_b(const SysK<R> *__restrict__ sys, int S,
+__global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs_b(const SysK<R> *__restrict__ sys, int S,
                                                            const int64_t *__restrict__ mprefix,
                                                            double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
