@@ -31,47 +31,42 @@ constexpr int BVP_MODES = BVP_LANES / 2;
 
 #define LDG(p) __ldg(p)
 
-// Shared-memory tables and scratch of one lane of the solve.
+// The k-independent tables of the solve live in static shared memory at
+// fixed offsets (nz <= BVP_NZMAX is checked at creation), so that the
+// recurrences address them with immediates: the SIMat bands S0, SM2, SP2,
+// the FIMat bands FM1, FP1, the SIMat bands / eta used by the velocity
+// windows, and the Chebyshev derivative factors 2 j / H (nz + 1 entries).
+constexpr int BVP_NZMAX = 128;
+enum BvpTab { TB_S0, TB_SM2, TB_SP2, TB_FM1, TB_FP1, TB_S0E, TB_SM2E, TB_SP2E, TB_DH };
+__shared__ double bvp_tab[TB_DH * BVP_NZMAX + BVP_NZMAX + 1];
+#define TAB(t, j) bvp_tab[(t) * BVP_NZMAX + (j)]
+
+// Shared-memory column and pressure scratch of one lane of the solve.
 struct BvpCtx {
   double *Xs;  // [(nz + 2)][BVP_LANES] penta / RHS columns
-  const double *S0, *SM2, *SP2, *FM1, *FP1, *DH;
-  const double *S0e, *SM2e, *SP2e;  // SIMat bands / eta (velocity windows)
   double *CPs;        // this lane's pressure coefficients, row j at CPs[j * GT]
   const double *CPo;  // the partner lane's
   int GT, tid;
 };
 
-// Load the integration-matrix bands (identical for every wavenumber) and the
-// Chebyshev derivative factors 2 j / H into shared memory.
+// Load the tables (identical for every wavenumber) into shared memory.
 static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm, double *cp_scratch) {
   const int nz = a.nz, tid = threadIdx.x;
   constexpr int T = BVP_LANES;
   BvpCtx c;
   c.Xs = bvp_sm;
-  double *S0 = bvp_sm + (nz + 2) * T, *SM2 = S0 + nz, *SP2 = SM2 + nz, *FM1 = SP2 + nz, *FP1 = FM1 + nz;
-  double *DH = FP1 + nz;
-  double *S0e = DH + nz + 1, *SM2e = S0e + nz, *SP2e = SM2e + nz;
   const double inv_eta = 1.0 / a.eta;
   for (int t = tid; t < nz; t += T) {
-    S0[t] = a.s0[t];
-    SM2[t] = a.sm2[t];
-    SP2[t] = a.sp2[t];
-    FM1[t] = a.fm1[t];
-    FP1[t] = a.fp1[t];
-    S0e[t] = a.s0[t] * inv_eta;
-    SM2e[t] = a.sm2[t] * inv_eta;
-    SP2e[t] = a.sp2[t] * inv_eta;
+    TAB(TB_S0, t) = a.s0[t];
+    TAB(TB_SM2, t) = a.sm2[t];
+    TAB(TB_SP2, t) = a.sp2[t];
+    TAB(TB_FM1, t) = a.fm1[t];
+    TAB(TB_FP1, t) = a.fp1[t];
+    TAB(TB_S0E, t) = a.s0[t] * inv_eta;
+    TAB(TB_SM2E, t) = a.sm2[t] * inv_eta;
+    TAB(TB_SP2E, t) = a.sp2[t] * inv_eta;
   }
-  for (int t = tid; t <= nz; t += T) DH[t] = (double)(2 * t) / a.H;
-  c.S0 = S0;
-  c.SM2 = SM2;
-  c.SP2 = SP2;
-  c.FM1 = FM1;
-  c.FP1 = FP1;
-  c.DH = DH;
-  c.S0e = S0e;
-  c.SM2e = SM2e;
-  c.SP2e = SP2e;
+  for (int t = tid; t <= nz; t += T) TAB(TB_DH, t) = (double)(2 * t) / a.H;
   // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
   // in global memory (L2 resident: a few tens of MB)
   c.GT = gridDim.x * T;
@@ -95,8 +90,6 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   constexpr int T = BVP_LANES;
   const int tid = ctx.tid, part = tid & 1;
   double *Xs = ctx.Xs;
-  const double *S0 = ctx.S0, *SM2 = ctx.SM2, *SP2 = ctx.SP2, *FM1 = ctx.FM1, *FP1 = ctx.FP1, *DH = ctx.DH;
-  const double *S0e = ctx.S0e, *SM2e = ctx.SM2e, *SP2e = ctx.SP2e;
   double *__restrict__ CPs = ctx.CPs;
   const double *__restrict__ CPo = ctx.CPo;
   const int GT = ctx.GT;
@@ -131,7 +124,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     f2s -= rs;
 #pragma unroll 4
     for (int j = nz - 2; j >= 1; --j) {
-      const double df = dfp2 + DH[j + 1] * fzn;
+      const double df = dfp2 + TAB(TB_DH, j + 1) * fzn;
       fzn = ld_fp64(f2s);
       XS(j) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + df;
       dfp2 = dfp1;
@@ -140,7 +133,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       f1o -= rs;
       f2s -= rs;
     }
-    const double df0 = dfp2 + DH[1] * fzn;
+    const double df0 = dfp2 + TAB(TB_DH, 1) * fzn;
     XS(0) = (dxs * ld_fp64(f0o) + dys * ld_fp64(f1o)) + 0.5 * df0;
   }
   // KBPENTA sweeps (LinearSolvers.h:106-141) in place on XS with the
@@ -151,7 +144,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   // the border dots accumulate in two partial sums (rows of even and odd
   // distance from the last), which halves their FP64 dependency chains.
   auto penta = [&](double &y0, double &y1) {
-    constexpr int PF_F = 8, PF_B = 4;
+    constexpr int PF_F = 16, PF_B = 8;
     double xm2 = 0.0, xm1 = 0.0;
     double pm[PF_F];
 #pragma unroll
@@ -291,13 +284,13 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     const R *f2s = sp_own + 2 * nz * rs;
     double *cpw = CPs;
     window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
-      double c = S0[m] * x0;
-      if (head == 0) c = SM2[m] * xm2 + c;
-      c = c + SP2[m] * x2;
+      double c = TAB(TB_S0, m) * x0;
+      if (head == 0) c = TAB(TB_SM2, m) * xm2 + c;
+      c = c + TAB(TB_SP2, m) * x2;
       if (head == 1) c += a.se0 * g0;
       if (head == 2) c += a.se1 * g1;
-      double dpv = FP1[m] * x1;
-      if (head != 1) dpv = FM1[m] * xm1 + dpv;
+      double dpv = TAB(TB_FP1, m) * x1;
+      if (head != 1) dpv = TAB(TB_FM1, m) * xm1 + dpv;
       if (head == 1) dpv += a.fe * g1;
       *cpw = c;
       if (odd) so += c;
@@ -348,9 +341,9 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     R *us = sp_own + c * nz * rs;
     const double se0e = a.se0 * inv_eta_w, se1e = a.se1 * inv_eta_w;
     window(g0, g1, [&](int m, double xm2, double xm1, double x0, double x1, double x2, bool odd, int head) {
-      double u = S0e[m] * x0;
-      if (head == 0) u = SM2e[m] * xm2 + u;
-      u = u + SP2e[m] * x2;
+      double u = TAB(TB_S0E, m) * x0;
+      if (head == 0) u = TAB(TB_SM2E, m) * xm2 + u;
+      u = u + TAB(TB_SP2E, m) * x2;
       if (head == 1) u += se0e * g0;
       if (head == 2) u += se1e * g1;
       if (store) *us = to_r<R>(u);
@@ -521,7 +514,7 @@ __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restr
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 9 * (size_t)a.nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -540,7 +533,7 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
 // Batched solve: grid and scratch for K modes in total with a shared nz.
 template <typename R>
 cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 9 * (size_t)nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES);
   cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
@@ -559,7 +552,7 @@ cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratc
 template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + 9 * (size_t)nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES);
   const int64_t per = (K + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   k_bvp_pairs_b<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
@@ -579,7 +572,7 @@ template cudaError_t launch_bvp_b<double>(const SysK<double> *, int, const int64
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES + 9 * (size_t)a.nz + 1);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
   const int64_t per = (a.nk + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
