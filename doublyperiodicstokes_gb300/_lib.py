@@ -34,7 +34,8 @@ class DpstInfo(ctypes.Structure):
                 ("norm_m", ctypes.c_double), ("norm_d", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("n_particles", ctypes.c_int64),
                 ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int),
-                ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2)]
+                ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
+                ("fused_particle_passes", ctypes.c_int)]
 
 
 class DpstBatchInfo(ctypes.Structure):

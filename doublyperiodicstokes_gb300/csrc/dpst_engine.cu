@@ -44,6 +44,15 @@ template <typename R>
 void launch_tile_order(int64_t N, const GridArgs &g, const Stencils<R> &st, int *count, int *start, int *perm,
                        cudaStream_t s);
 size_t tile_order_tiles(int nx, int ny);
+bool fused_supports(const KernelDesc &km, const KernelDesc &kd);
+template <typename R, typename RF>
+void launch_spread_fused(const RF *F, const RF *T, int64_t N, const KernelDesc &km, const KernelDesc &kd,
+                         const GridArgs &g, const Stencils<R> &sm, const Stencils<R> &sd, R *grid,
+                         const Ghosts<R> &ghm, const Ghosts<R> &ghd, cudaStream_t s, const int *perm);
+template <typename R, typename RV>
+void launch_interp_fused(const R *grid, int64_t N, const KernelDesc &km, const KernelDesc &kd, const GridArgs &g,
+                         const Stencils<R> &sm, const Stencils<R> &sd, const Ghosts<R> &ghm,
+                         const Ghosts<R> &ghd, RV *V, RV *W, cudaStream_t s, const int *perm);
 template <typename R>
 void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s);
 template <typename R, typename RV>
@@ -119,6 +128,7 @@ struct Engine : EngineBase {
   int64_t nk;
   double hx, hy, Lz, H;
   KernelHost km, kd;
+  bool fused = false;  // monopole and dipole share one spread and one interpolation pass
   GridArgs g;
   KsArgs ks;
   // device buffers
@@ -156,6 +166,7 @@ struct Engine : EngineBase {
     clencurt(nz, 0.0, Lz, zG, zW);
     km = make_kernel(p.w, p.beta, p.alpha, false, hx, hy, nx, ny, zG, zW, "monopole kernel");
     if (p.has_torque) kd = make_kernel(p.w_d, p.beta_d, p.alpha_d, true, hx, hy, nx, ny, zG, zW, "dipole kernel");
+    fused = p.has_torque && fused_supports(km.d, kd.d);
     km.d.zext_off = 0;
     kd.d.zext_off = (int)km.zext.size();
     std::vector<double> ze = km.zext, we = km.wext;
@@ -369,8 +380,12 @@ struct Engine : EngineBase {
       if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
       if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
     }
-    launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s, perm.as<int>());
-    if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s, perm.as<int>());
+    if (torque && fused) {
+      launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, ghm, ghd, s, perm.as<int>());
+    } else {
+      launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s, perm.as<int>());
+      if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s, perm.as<int>());
+    }
     launch_ghost_fold<R>(ghm.top, ghm.ntop, nx, ny, km.d, s);
     launch_ghost_fold<R>(ghm.bot, ghm.nbot, nx, ny, km.d, s);
     if (torque) {
@@ -498,13 +513,19 @@ struct Engine : EngineBase {
     spread_stage<RF>(F, T, s);
     mark(1, s);
     solve_stage(s);
-    launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
     if (p.has_torque && W != nullptr) {
       // without torques the reference's torque grid still holds the last
       // z-derivative spread; with T = NULL it is zero
       Ghosts<R> gz = ghd;
       if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
-      launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s, perm.as<int>());
+      if (fused) {
+        launch_interp_fused<R, RF>(gr, N, km.d, kd.d, g, stm, std_, ghm, gz, V, W, s, perm.as<int>());
+      } else {
+        launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
+        launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s, perm.as<int>());
+      }
+    } else {
+      launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
     }
     DPST_CUDA(cudaGetLastError());
     mark(7, s);
@@ -719,7 +740,9 @@ struct Engine : EngineBase {
     o->ztransform = ztc;
     o->ztransform_ms[0] = ztc_ms[0];
     o->ztransform_ms[1] = ztc_ms[1];
-    o->kernels_per_mdot = (p.has_torque ? 2 : 1) + 2 * nbuf + 1 + 2 + 1 + (p.has_torque ? 2 : 1);
+    const int particle_passes = (p.has_torque && !fused) ? 2 : 1;
+    o->kernels_per_mdot = particle_passes + 2 * nbuf + 1 + 2 + 1 + particle_passes;
+    o->fused_particle_passes = fused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,

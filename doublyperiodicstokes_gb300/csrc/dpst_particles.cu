@@ -236,6 +236,150 @@ __global__ void k_spread_dip(const RF *__restrict__ T, int64_t N, KernelDesc kd,
 }
 
 // ---------------------------------------------------------------------------
+// Fused monopole + dipole spread, for kernel pairs that share the x-y stencil
+// columns and the extended z grid and whose dipole threshold is at most the
+// monopole's (fused_supports): every dipole z window is then a sub-range of
+// the same particle's monopole window, so one pass over the monopole window
+// adds both contributions with one atomic per grid value (the separate
+// passes take three for the forces and five for the torque curl).
+// ---------------------------------------------------------------------------
+template <typename R, typename RF>
+static __device__ __forceinline__ void spread_fused_item(int64_t p, int c, const RF *__restrict__ F,
+                                                         const RF *__restrict__ T, const KernelDesc &km,
+                                                         const KernelDesc &kd, const GridArgs &g,
+                                                         const Stencils<R> &sm, const Stencils<R> &sd,
+                                                         R *__restrict__ grid, const Ghosts<R> &ghm,
+                                                         const Ghosts<R> &ghd) {
+  const int i = c % km.wx, j = c / km.wx;
+  const int4 cm = sm.cell[p];
+  if (cm.w == 0) return;
+  const int4 cd = sd.cell[p];
+  const int ox = cm.x + i - km.wx / 2 + km.evenx;
+  const int oy = cm.y + j - km.wy / 2 + km.eveny;
+  const int px = wrapi(ox, g.nx), py = wrapi(oy, g.ny);
+  const int ie = ox + km.lend, je = oy + km.bend;
+  const R f0 = (R)F[3 * p], f1 = (R)F[3 * p + 1], f2 = (R)F[3 * p + 2];
+  const R tx = (R)T[3 * p], ty = (R)T[3 * p + 1], tz = (R)T[3 * p + 2];
+  const R cm_xy = sm.phx[p * km.wx + i] * sm.phy[p * km.wy + j];
+  const R fx = sd.phx[p * kd.wx + i], fy = sd.phy[p * kd.wy + j];
+  const R dfx = sd.dphx[p * kd.wx + i], dfy = sd.dphy[p * kd.wy + j];
+  const R axy = dfx * fy, bxy = fx * dfy, cxy = fx * fy;
+  const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+  const int64_t col = (int64_t)py * g.nx + px;
+  const R half = (R)0.5;
+  const int m0 = cm.z - km.dend;  // interior node of the window's first entry
+  if (m0 >= 1 && m0 + cm.w <= g.nz - 1) {
+    // every node of the window is an interior node of weight 1 under both
+    // BC sets (zmap): one base pointer, the dipole's sub-range known upfront
+    const int dk = cm.z - cd.z;
+    const int k0 = max(-dk, 0), k1 = min(cd.w - dk, cm.w);
+    const R *__restrict__ pz = sm.phz + p * km.wz_max;
+    const R *__restrict__ pzd = sd.phz + p * kd.wz_max + dk;
+    const R *__restrict__ dpzd = sd.dphz + p * kd.wz_max + dk;
+    R *dst = grid + (int64_t)m0 * plane + col;
+    for (int k = 0; k < cm.w; ++k, dst += plane) {
+      const R v = cm_xy * pz[k];
+      R gx = v * f0, gy = v * f1, gz = v * f2;
+      if (k >= k0 && k < k1) {
+        const R phz = pzd[k];
+        const R ax = axy * phz, ay = bxy * phz, az = cxy * dpzd[k];
+        gx += half * (ay * tz) + (-half) * (az * ty);
+        gy += -half * (ax * tz) + half * (az * tx);
+        gz += half * (ax * ty - ay * tx);
+      }
+      atomic_add(dst, gx);
+      atomic_add(dst + comp, gy);
+      atomic_add(dst + 2 * comp, gz);
+    }
+    return;
+  }
+  for (int k = 0; k < cm.w; ++k) {
+    const int kk = cm.z + k;
+    const R v = cm_xy * sm.phz[p * km.wz_max + k];
+    const int kq = kk - cd.z;  // the dipole window's index of this node
+    const bool dip = kq >= 0 && kq < cd.w;
+    ZMap a = zmap(kk, km.dend, g.nz, g.bcA);
+    // set A: the forces and the x, y derivative spreads of the curl
+    R gx = 0, gy = 0, gz = 0;
+    if (a.m >= 0) {
+      if (a.wgt != 0.0) {
+        const R am = v * (R)a.wgt;
+        gx = am * f0;
+        gy = am * f1;
+        gz = am * f2;
+      }
+    } else {
+      R *buf = (a.m == -1) ? ghm.top : ghm.bot;
+      if (buf != nullptr && ie >= 0 && ie < km.nxeff && je >= 0 && je < km.nyeff) {
+        R *dst = buf + (((int64_t)a.level * km.nyeff + je) * km.nxeff + ie) * 3;
+        atomic_add(dst, v * f0);
+        atomic_add(dst + 1, v * f1);
+        atomic_add(dst + 2, v * f2);
+      }
+    }
+    R bx = 0, by = 0;
+    ZMap b;
+    b.m = a.m;
+    if (dip) {
+      const R phz = sd.phz[p * kd.wz_max + kq];
+      const R ax = axy * phz, ay = bxy * phz;
+      const R az = cxy * sd.dphz[p * kd.wz_max + kq];
+      if (a.m >= 0 && a.wgt != 0.0) {
+        const R wa = (R)a.wgt * half;
+        gx += wa * (ay * tz);
+        gy += -wa * (ax * tz);
+        gz += wa * (ax * ty - ay * tx);
+      }
+      b = zmap(kk, kd.dend, g.nz, g.bcB);
+      if (b.m >= 0) {
+        if (b.wgt != 0.0) {
+          const R wb = (R)b.wgt * half;
+          bx = -wb * (az * ty);
+          by = wb * (az * tx);
+        }
+      } else {
+        R *buf = (b.m == -1) ? ghd.top : ghd.bot;
+        if (buf != nullptr && ie >= 0 && ie < kd.nxeff && je >= 0 && je < kd.nyeff) {
+          R *dst = buf + (((int64_t)b.level * kd.nyeff + je) * kd.nxeff + ie) * 3;
+          atomic_add(dst, az * tx);
+          atomic_add(dst + 1, az * ty);
+          atomic_add(dst + 2, az * tz);
+        }
+      }
+    }
+    if (a.m >= 0 && a.wgt != 0.0) {
+      R *dst = grid + a.m * plane + col;
+      if (dip && b.m == a.m) {  // set B lands on the same node: one atomic each
+        gx += bx;
+        gy += by;
+        bx = 0;
+        by = 0;
+      }
+      atomic_add(dst, gx);
+      atomic_add(dst + comp, gy);
+      atomic_add(dst + 2 * comp, gz);
+    }
+    if (dip && b.m >= 0 && (bx != (R)0 || by != (R)0)) {
+      R *dst = grid + b.m * plane + col;
+      atomic_add(dst, bx);
+      atomic_add(dst + comp, by);
+    }
+  }
+}
+
+template <typename R, typename RF>
+__global__ void k_spread_fused(const RF *__restrict__ F, const RF *__restrict__ T, int64_t N, KernelDesc km,
+                               KernelDesc kd, GridArgs g, Stencils<R> sm, Stencils<R> sd, R *__restrict__ grid,
+                               Ghosts<R> ghm, Ghosts<R> ghd, const int *__restrict__ perm) {
+  const int cols = km.wx * km.wy;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= N * cols) return;
+  const int64_t q = t / cols;
+  const int64_t p = perm ? (int64_t)perm[q] : q;
+  spread_fused_item<R, RF>(p, (int)(t - q * cols), F, T, km, kd, g, sm, sd, grid, ghm, ghd);
+}
+
+// ---------------------------------------------------------------------------
 // Periodic x then y fold of the ghost-layer buffers, applied to every stored
 // level exactly as the reference folds its whole extended grid
 // (BoundaryConditions.h:43-84 then 143-184): x ghosts are added into the
@@ -406,6 +550,199 @@ __global__ void k_interp_dip(const R *__restrict__ grid, int64_t N, KernelDesc k
   if (w >= N) return;
   const int64_t p = perm ? (int64_t)perm[w] : w;
   interp_dip_item<R, RV>(p, threadIdx.x & 31, grid, kd, g, st, gh, W);
+}
+
+// ---------------------------------------------------------------------------
+// Fused monopole + dipole interpolation (kernel pairs as for the fused
+// spread): one warp per particle walks the monopole window once; an interior
+// grid value read for the monopole also serves the dipole's set-A (and, when
+// set B maps the node identically, set-B) derivatives.
+// ---------------------------------------------------------------------------
+template <typename R, typename RV>
+static __device__ __forceinline__ void interp_fused_item(int64_t p, int lane, const R *__restrict__ grid,
+                                                         const KernelDesc &km, const KernelDesc &kd,
+                                                         const GridArgs &g, const Stencils<R> &sm,
+                                                         const Stencils<R> &sd, const Ghosts<R> &ghm,
+                                                         const Ghosts<R> &ghd, RV *__restrict__ V,
+                                                         RV *__restrict__ W) {
+  const int4 cm = sm.cell[p];
+  const int4 cd = sd.cell[p];
+  R s0 = 0, s1 = 0, s2 = 0;
+  R dyvz = 0, dzvy = 0, dzvx = 0, dxvz = 0, dxvy = 0, dyvx = 0;
+  if (cm.w > 0) {
+    const int cols = km.wx * km.wy;
+    const int tot = cols * cm.w;
+    const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+    for (int t = lane; t < tot; t += 32) {
+      const int k = t / cols;
+      const int c = t - k * cols;
+      const int i = c % km.wx, j = c / km.wx;
+      const int ox = cm.x + i - km.wx / 2 + km.evenx;
+      const int oy = cm.y + j - km.wy / 2 + km.eveny;
+      const int64_t col = (int64_t)wrapi(oy, g.ny) * g.nx + wrapi(ox, g.nx);
+      const int kk = cm.z + k;
+      const ZMap za = zmap(kk, km.dend, g.nz, g.bcA);
+      R u[3];
+      grid_value3(grid, za, col, plane, comp, ghm, km, ox + km.lend, oy + km.bend, u);
+      const R wgt = sm.phx[p * km.wx + i] * sm.phy[p * km.wy + j] * sm.phzw[p * km.wz_max + k];
+      s0 += u[0] * wgt;
+      s1 += u[1] * wgt;
+      s2 += u[2] * wgt;
+      const int kq = kk - cd.z;
+      if (kq >= 0 && kq < cd.w) {
+        const ZMap zb = zmap(kk, kd.dend, g.nz, g.bcB);
+        R ua[3], ub[3];
+        if (za.m >= 0) {
+          ua[0] = u[0];
+          ua[1] = u[1];
+          ua[2] = u[2];
+        } else {
+          grid_value3(grid, za, col, plane, comp, ghd, kd, ox + kd.lend, oy + kd.bend, ua);
+        }
+        if (zb.m >= 0 && zb.m == za.m && zb.wgt == za.wgt) {
+          ub[0] = u[0];
+          ub[1] = u[1];
+        } else {
+          grid_value3(grid, zb, col, plane, comp, ghd, kd, ox + kd.lend, oy + kd.bend, ub);
+        }
+        const R fx = sd.phx[p * kd.wx + i], fy = sd.phy[p * kd.wy + j];
+        const R dfx = sd.dphx[p * kd.wx + i], dfy = sd.dphy[p * kd.wy + j];
+        const R zw = sd.phzw[p * kd.wz_max + kq], dzw = sd.dphzw[p * kd.wz_max + kq];
+        const R wx = dfx * fy * zw, wy = fx * dfy * zw, wz = fx * fy * dzw;
+        dxvy += ua[1] * wx;
+        dxvz += ua[2] * wx;
+        dyvx += ua[0] * wy;
+        dyvz += ua[2] * wy;
+        dzvx += ub[0] * wz;
+        dzvy += ub[1] * wz;
+      }
+    }
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  dyvz = warp_sum(dyvz);
+  dzvy = warp_sum(dzvy);
+  dzvx = warp_sum(dzvx);
+  dxvz = warp_sum(dxvz);
+  dxvy = warp_sum(dxvy);
+  dyvx = warp_sum(dyvx);
+  if (lane == 0) {
+    V[3 * p] = (RV)s0;
+    V[3 * p + 1] = (RV)s1;
+    V[3 * p + 2] = (RV)s2;
+    W[3 * p] = (RV)(-(R)0.5 * (dyvz - dzvy));
+    W[3 * p + 1] = (RV)(-(R)0.5 * (dzvx - dxvz));
+    W[3 * p + 2] = (RV)(-(R)0.5 * (dxvy - dyvx));
+  }
+}
+
+// Interior fast path of the fused interpolation (every window node an
+// interior node of weight 1 under both BC sets, at most INTERP_TAB_COLS
+// stencil columns): the warp first tabulates, per stencil column, the wrapped
+// grid column and the x-y weights of both kernels in shared memory, then
+// walks the (z level, column) cells with an incremental index, so that the
+// per-cell work is three grid loads and the weighted sums.
+constexpr int INTERP_TAB_COLS = 64;
+constexpr int INTERP_WARPS = 8;
+
+template <typename R>
+struct InterpTab {
+  int col[INTERP_TAB_COLS];
+  R wm[INTERP_TAB_COLS], wdx[INTERP_TAB_COLS], wdy[INTERP_TAB_COLS], wdz[INTERP_TAB_COLS];
+};
+
+template <typename R, typename RV>
+static __device__ __forceinline__ void interp_fused_interior(int64_t p, int lane, const R *__restrict__ grid,
+                                                             const KernelDesc &km, const KernelDesc &kd,
+                                                             const GridArgs &g, const Stencils<R> &sm,
+                                                             const Stencils<R> &sd, int4 cm, int4 cd,
+                                                             InterpTab<R> &tb, RV *__restrict__ V,
+                                                             RV *__restrict__ W) {
+  const int cols = km.wx * km.wy;
+  for (int c = lane; c < cols; c += 32) {
+    const int i = c % km.wx, j = c / km.wx;
+    const int ox = cm.x + i - km.wx / 2 + km.evenx;
+    const int oy = cm.y + j - km.wy / 2 + km.eveny;
+    tb.col[c] = wrapi(oy, g.ny) * g.nx + wrapi(ox, g.nx);
+    tb.wm[c] = sm.phx[p * km.wx + i] * sm.phy[p * km.wy + j];
+    const R fx = sd.phx[p * kd.wx + i], fy = sd.phy[p * kd.wy + j];
+    tb.wdx[c] = sd.dphx[p * kd.wx + i] * fy;
+    tb.wdy[c] = fx * sd.dphy[p * kd.wy + j];
+    tb.wdz[c] = fx * fy;
+  }
+  __syncwarp();
+  const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
+  const R *__restrict__ base = grid + (int64_t)(cm.z - km.dend) * plane;
+  const R *__restrict__ zwm = sm.phzw + p * km.wz_max;
+  const int dk = cm.z - cd.z;
+  const R *__restrict__ zwd = sd.phzw + p * kd.wz_max + dk;
+  const R *__restrict__ dzwd = sd.dphzw + p * kd.wz_max + dk;
+  const int k0 = max(-dk, 0), k1 = min(cd.w - dk, cm.w);
+  R s0 = 0, s1 = 0, s2 = 0;
+  R dyvz = 0, dzvy = 0, dzvx = 0, dxvz = 0, dxvy = 0, dyvx = 0;
+  const int tot = cols * cm.w;
+  int k = lane / cols, c = lane - k * cols;
+  for (int t = lane; t < tot; t += 32) {
+    const R *src = base + (int64_t)k * plane + tb.col[c];
+    const R u0 = src[0], u1 = src[comp], u2 = src[2 * comp];
+    const R wgt = tb.wm[c] * zwm[k];
+    s0 += u0 * wgt;
+    s1 += u1 * wgt;
+    s2 += u2 * wgt;
+    if (k >= k0 && k < k1) {
+      const R zw = zwd[k];
+      const R wx = tb.wdx[c] * zw, wy = tb.wdy[c] * zw, wz = tb.wdz[c] * dzwd[k];
+      dxvy += u1 * wx;
+      dxvz += u2 * wx;
+      dyvx += u0 * wy;
+      dyvz += u2 * wy;
+      dzvx += u0 * wz;
+      dzvy += u1 * wz;
+    }
+    c += 32;
+    while (c >= cols) {
+      c -= cols;
+      ++k;
+    }
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  dyvz = warp_sum(dyvz);
+  dzvy = warp_sum(dzvy);
+  dzvx = warp_sum(dzvx);
+  dxvz = warp_sum(dxvz);
+  dxvy = warp_sum(dxvy);
+  dyvx = warp_sum(dyvx);
+  if (lane == 0) {
+    V[3 * p] = (RV)s0;
+    V[3 * p + 1] = (RV)s1;
+    V[3 * p + 2] = (RV)s2;
+    W[3 * p] = (RV)(-(R)0.5 * (dyvz - dzvy));
+    W[3 * p + 1] = (RV)(-(R)0.5 * (dzvx - dxvz));
+    W[3 * p + 2] = (RV)(-(R)0.5 * (dxvy - dyvx));
+  }
+}
+
+template <typename R, typename RV>
+__global__ void __launch_bounds__(32 * INTERP_WARPS) k_interp_fused(const R *__restrict__ grid, int64_t N, KernelDesc km,
+                                                                    KernelDesc kd, GridArgs g, Stencils<R> sm,
+                                                                    Stencils<R> sd, Ghosts<R> ghm, Ghosts<R> ghd,
+                                                                    RV *__restrict__ V, RV *__restrict__ W,
+                                                                    const int *__restrict__ perm) {
+  __shared__ InterpTab<R> tabs[INTERP_WARPS];
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= N) return;
+  const int64_t p = perm ? (int64_t)perm[w] : w;
+  const int lane = threadIdx.x & 31;
+  const int4 cm = sm.cell[p];
+  const int m0 = cm.z - km.dend;
+  if (cm.w > 0 && km.wx * km.wy <= INTERP_TAB_COLS && m0 >= 1 && m0 + cm.w <= g.nz - 1) {
+    interp_fused_interior<R, RV>(p, lane, grid, km, kd, g, sm, sd, cm, sd.cell[p], tabs[threadIdx.x >> 5], V, W);
+  } else {
+    interp_fused_item<R, RV>(p, lane, grid, km, kd, g, sm, sd, ghm, ghd, V, W);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -623,6 +960,34 @@ void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd,
   if (ty > 0) k_ghost_fold_y<R><<<(ty + bs - 1) / bs, bs, 0, s>>>(buf, levels, ny, kd);
 }
 
+// The fused spread / interpolation apply to a monopole / dipole kernel pair
+// with the same x-y stencil columns and extended z grid and a dipole
+// threshold no larger than the monopole's.
+bool fused_supports(const KernelDesc &km, const KernelDesc &kd) {
+  return km.wx == kd.wx && km.wy == kd.wy && km.evenx == kd.evenx && km.eveny == kd.eveny &&
+         km.nxeff == kd.nxeff && km.nyeff == kd.nyeff && km.lend == kd.lend && km.bend == kd.bend &&
+         km.nzeff == kd.nzeff && km.dend == kd.dend && kd.thr <= km.thr;
+}
+
+template <typename R, typename RF>
+void launch_spread_fused(const RF *F, const RF *T, int64_t N, const KernelDesc &km, const KernelDesc &kd,
+                         const GridArgs &g, const Stencils<R> &sm, const Stencils<R> &sd, R *grid,
+                         const Ghosts<R> &ghm, const Ghosts<R> &ghd, cudaStream_t s, const int *perm) {
+  const int64_t tot = N * km.wx * km.wy;
+  if (tot == 0) return;
+  const int bs = 256;
+  k_spread_fused<R, RF><<<(tot + bs - 1) / bs, bs, 0, s>>>(F, T, N, km, kd, g, sm, sd, grid, ghm, ghd, perm);
+}
+
+template <typename R, typename RV>
+void launch_interp_fused(const R *grid, int64_t N, const KernelDesc &km, const KernelDesc &kd, const GridArgs &g,
+                         const Stencils<R> &sm, const Stencils<R> &sd, const Ghosts<R> &ghm,
+                         const Ghosts<R> &ghd, RV *V, RV *W, cudaStream_t s, const int *perm) {
+  if (N == 0) return;
+  const int bs = 32 * INTERP_WARPS;
+  k_interp_fused<R, RV><<<(N * 32 + bs - 1) / bs, bs, 0, s>>>(grid, N, km, kd, g, sm, sd, ghm, ghd, V, W, perm);
+}
+
 template <typename R, typename RV>
 void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
                    const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s, const int *perm) {
@@ -651,7 +1016,24 @@ void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, 
                                          const GridArgs &, const Stencils<R> &,                \
                                          const Ghosts<R> &, double *, cudaStream_t, const int *);\
   template void launch_tile_order<R>(int64_t, const GridArgs &, const Stencils<R> &, int *, int *, \
-                                     int *, cudaStream_t);
+                                     int *, cudaStream_t);\
+  template void launch_spread_fused<R, float>(const float *, const float *, int64_t, const KernelDesc &,   \
+                                              const KernelDesc &, const GridArgs &, const Stencils<R> &,  \
+                                              const Stencils<R> &, R *, const Ghosts<R> &,                \
+                                              const Ghosts<R> &, cudaStream_t, const int *);              \
+  template void launch_spread_fused<R, double>(const double *, const double *, int64_t,                   \
+                                               const KernelDesc &, const KernelDesc &, const GridArgs &,  \
+                                               const Stencils<R> &, const Stencils<R> &, R *,             \
+                                               const Ghosts<R> &, const Ghosts<R> &, cudaStream_t,        \
+                                               const int *);                                               \
+  template void launch_interp_fused<R, float>(const R *, int64_t, const KernelDesc &, const KernelDesc &,  \
+                                              const GridArgs &, const Stencils<R> &, const Stencils<R> &, \
+                                              const Ghosts<R> &, const Ghosts<R> &, float *, float *,     \
+                                              cudaStream_t, const int *);                                 \
+  template void launch_interp_fused<R, double>(const R *, int64_t, const KernelDesc &, const KernelDesc &, \
+                                               const GridArgs &, const Stencils<R> &, const Stencils<R> &,\
+                                               const Ghosts<R> &, const Ghosts<R> &, double *, double *,  \
+                                               cudaStream_t, const int *);
 
 DPST_INST(float)
 DPST_INST(double)

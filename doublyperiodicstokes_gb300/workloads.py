@@ -85,7 +85,12 @@ C3 = Workload("c3_dpbw_n8192", "DPBW", 8192, 192.0, 192.0, 192, 192, 64, 0.0, 24
 # a few-hundred-MB case for ncu captures of the c2 kernels.
 P2 = Workload("p2_dp_n8192_192", "DP", 8192, 192.0, 192.0, 192, 192, 128, -20.5, 41.0, -16.0, 16.0,
               True, betam_hat=1.3267, betad_hat=2.2160)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2)}
+# The c2 geometry and particle density on a 320 x 320 grid: a 157 MB grid
+# (larger than L2) in about 1 GB of device memory, for full ncu captures of
+# the particle kernels.
+P3 = Workload("p3_dp_n25600_320", "DP", 25600, 320.0, 320.0, 320, 320, 128, -20.5, 41.0, -16.0, 16.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3)}
 
 
 def fft_friendly(n):

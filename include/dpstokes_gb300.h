@@ -116,6 +116,10 @@ typedef struct dpst_info {
                               (even/odd folded), 1 tcgen05 split-TF32 (mixed only) */
   float ztransform_ms[2];  /* creation-time timings of one transform: SIMT, tcgen05
                               (0 if not timed) */
+  int fused_particle_passes; /* 1: torques spread and interpolate in the same pass as
+                                the forces (the dipole kernel's stencil columns and z
+                                ghost extension equal the monopole's and its threshold
+                                is not larger); 0: separate monopole / dipole passes */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

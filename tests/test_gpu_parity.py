@@ -131,3 +131,28 @@ def test_asymmetric_ghost_extension_is_rejected():
     with pytest.raises(DPStokesError) as e:
         DPStokes(StokesParams.from_workload(w), w.N)
     assert e.value.code == 5
+
+
+def _with_widths(base, wm, wd):
+    import dataclasses
+    return dataclasses.replace(W.SMALL_BY_NAME[base], name="%s_wm%d_wd%d" % (base, wm, wd), wm=wm, wd=wd)
+
+
+@pytest.mark.parametrize("base,wm,wd,fused", [("s_dp_t", 6, 6, 1), ("s_dpsc_t", 6, 6, 1), ("s_dpbw_t", 6, 5, 0),
+                                             ("s_dp_t", 5, 6, 0)])
+def test_fused_and_separate_particle_passes(base, wm, wd, fused):
+    """Equal kernel widths share one spread and one interpolation pass for
+    forces and torques (the dipole's z windows nest in the monopole's);
+    other widths keep separate passes.  Both match the oracle in FP64."""
+    w = _with_widths(base, wm, wd)
+    X, F, T = W.make_inputs(w)
+    op, V, Wv = _run(w, X, F, T)
+    assert op.info()["fused_particle_passes"] == fused
+    Vo, Wo = O.mdot(O.Params(**w.oracle_params()), X, F, T)
+    ev, ew = rel_err(V, Vo), rel_err(Wv, Wo)
+    print("%s fused %d V %.2e W %.2e" % (w.name, fused, ev, ew))
+    assert ev < TOL_FP64
+    assert ew < TOL_FP64
+    _, V32, W32 = _run(w, X, F, T, precision="mixed", dtype=torch.float32)
+    assert rel_err(V32, V) < TOL_MIXED
+    assert rel_err(W32, Wv) < TOL_MIXED
