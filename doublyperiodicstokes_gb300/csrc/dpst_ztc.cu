@@ -4,31 +4,54 @@
 // The transform is OUT[r][col] = sum_m T[r][m] IN[m][col] over every real
 // column of the spectrum (per component: nz rows x 2 nk columns, in place),
 // with the inverse's epilogue adding the wall correction and scaling
-// (corr_value, as k_zgemm does).  Per CTA tile: M = 128 rows (nz padded with
-// zero rows of T), N = 64 columns, K = nz padded to a multiple of 8.  Each
-// FP32 operand x is split as x = hi + lo with hi = tf32(x), lo = tf32(x - hi)
-// and the product is accumulated as hi*hi + hi*lo + lo*hi (three
+// (corr_value, as k_zgemm does).  Per tile: M = 128 rows (nz padded with zero
+// rows of T), N = 128 columns, K = nz padded to a multiple of 8 and streamed
+// through shared memory in stages of 32 rows.  Each FP32
+// operand x is split as x = hi + lo with hi = tf32(x), lo = tf32(x - hi) and
+// the product is accumulated as hi*hi + hi*lo + lo*hi (three
 // tcgen05.mma.kind::tf32 per K step of 8), which keeps the FP32-level
 // accuracy of the SIMT transform.
 //
-// Shared memory holds A = T (hi, lo) for the CTA's lifetime and B = the
-// current tile (hi, lo) in the canonical K-major layout without swizzle:
-// 8-row x 16-byte core matrices, consecutive along K (LBO = 128 B), 8-row
-// groups SBO = (Kp / 4) * 128 B apart.  One thread issues the MMAs and
-// commits them to an mbarrier; every thread waits on it with an iteration
-// limit (on expiry the kernel records the error, stops and still frees its
-// tensor memory).  While the MMAs of tile t run, the threads load tile t+1
-// into registers.  The accumulator (128 lanes x 64 FP32 columns) is read
-// back with tcgen05.ld by the warp owning each lane quadrant.
+// One persistent CTA per SM, warp-specialised so that loads, products and
+// stores of successive tiles overlap:
+//   * 8 producer warps read 32-row x 128-column blocks from HBM (three
+//     blocks in flight per thread in registers), split them into TF32 hi /
+//     lo and write them, in the canonical K-major no-swizzle layout (8-row x
+//     16-byte core matrices, LBO = 128 B along K, SBO = 1 KB along N), into
+//     one of two shared-memory stages, then arrive on the stage's "full"
+//     mbarrier;
+//   * one thread issues the MMAs of a stage (M = 128, N = 128, K = 8: large
+//     enough that the per-instruction issue cost does not bound the kernel)
+//     into one of two tensor-memory accumulators and commits them to the
+//     stage's "empty" mbarrier, and after the tile's last stage to the
+//     accumulator's "full" mbarrier;
+//   * 4 epilogue warps (one per tensor-memory lane quadrant) read the
+//     accumulator 32 columns at a time with tcgen05.ld, release it, transpose
+//     each 32 x 32 block through shared memory and store whole rows.
+// T (hi, lo) stays in shared memory for the CTA's lifetime.  Every wait has
+// an iteration deadline: on expiry the waiting thread records the error and
+// raises a shared abort flag that ends every role; the MMA thread then waits
+// (bounded) for its issued products before the tensor memory is freed.
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
 
 namespace dpst {
 
-constexpr int ZTC_N = 64;         // columns per tile
-constexpr int ZTC_THREADS = 256;  // 8 warps: two per TMEM lane quadrant
-constexpr int ZTC_TMEM_COLS = 64;
-constexpr unsigned long long ZTC_WAIT_NS = 2000000000ull;  // 2 s
+constexpr int ZTC_N = 128;                                     // columns per tile (MMA N)
+constexpr int ZTC_KC = 32;                                     // K rows per shared-memory stage
+constexpr int ZTC_STAGES = 2;                                  // B (hi, lo) stages
+constexpr int ZTC_ACC = 2;                                     // tensor-memory accumulators
+constexpr int ZTC_PROD_WARPS = 8;
+constexpr int ZTC_EPI_WARPS = 4;                               // one per lane quadrant
+constexpr int ZTC_MMA_WARP = ZTC_PROD_WARPS + ZTC_EPI_WARPS;   // warp 12
+constexpr int ZTC_THREADS = 32 * (ZTC_MMA_WARP + 1);
+constexpr int ZTC_TMEM_COLS = ZTC_ACC * ZTC_N;
+constexpr int ZTC_DEPTH = 3;                                   // stages of loads in flight per producer
+constexpr int ZTC_PGROUPS = 32 * ZTC_PROD_WARPS / ZTC_N;       // producer threads per column (2)
+constexpr int ZTC_QPT = ZTC_KC / 4 / ZTC_PGROUPS;              // row quads per producer thread per stage (4)
+constexpr int ZTC_STG = 32 + 4;                                // epilogue staging pitch (floats, 16-B rows)
+constexpr unsigned long long ZTC_WAIT_NS = 2000000000ull;      // 2 s
+static_assert(ZTC_EPI_WARPS == 4 && ZTC_PROD_WARPS % 4 == 0, "epilogue warp w must own lane quadrant w % 4");
 
 static __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -64,31 +87,96 @@ static __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t ad, uin
       "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
 
-// Bytes of the B operand (hi, lo) region, which the epilogue reuses as its
-// [128][ZTC_N + 1] FP32 staging.
-static __host__ __device__ constexpr size_t ztc_b_region(int kp) {
-  return (2 * (size_t)ZTC_N * kp * 4 > (size_t)128 * (ZTC_N + 1) * 4) ? 2 * (size_t)ZTC_N * kp * 4
-                                                                      : (size_t)128 * (ZTC_N + 1) * 4;
-}
-
 // Element offset (in 32-bit words) of (row, k) in the core-matrix layout.
 static __device__ __forceinline__ int cm_off(int row, int k, int kq) {
   return (row >> 3) * (kq * 32) + (k >> 2) * 32 + (row & 7) * 4 + (k & 3);
 }
 
+static __device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+static __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+static __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+static __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+static __device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+// Bounded wait for the completion of the mbarrier phase of the given parity.
+// Returns false once the deadline passes (recording the error and raising
+// the abort flag) or, when watch_abort, once another thread has aborted.
+static __device__ bool ztc_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err,
+                                bool watch_abort = true) {
+  const unsigned long long t0 = globaltimer();
+  for (int spin = 0;; ++spin) {
+    if (mbar_try(bar, parity)) return true;
+    if ((spin & 63) == 63) {
+      if (watch_abort && *abort_flag) return false;
+      if (globaltimer() - t0 > ZTC_WAIT_NS) {
+        *abort_flag = 1;
+        atomicOr(err, 1);
+        return false;
+      }
+    }
+  }
+}
+
+// Shared-memory bytes: T hi / lo, the B stages, the epilogue staging, the
+// mbarriers, the tensor-memory address slot and the abort flag.
+static __host__ __device__ constexpr size_t ztc_off_b(int kp) { return (size_t)2 * 128 * kp * 4; }
+static __host__ __device__ constexpr size_t ztc_off_stg(int kp) {
+  return ztc_off_b(kp) + (size_t)ZTC_STAGES * 2 * ZTC_N * ZTC_KC * 4;
+}
+static __host__ __device__ constexpr size_t ztc_off_bar(int kp) {
+  return ztc_off_stg(kp) + (size_t)ZTC_EPI_WARPS * 32 * ZTC_STG * 4;
+}
+constexpr int ZTC_NBARS = 2 * ZTC_STAGES + 2 * ZTC_ACC + 1;
+
+size_t ztc_smem_bytes(int nz) {
+  const int kp = (nz + 7) & ~7;
+  return ztc_off_bar(kp) + ZTC_NBARS * 8 + 16;
+}
+
 template <bool INVERSE>
-__global__ void __launch_bounds__(ZTC_THREADS) k_zgemm_tc(float *spec, int nz, int64_t ncols,
-                                                          const float *__restrict__ Tm, EpiArgs e, int *err) {
+__global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz, int64_t ncols,
+                                                             const float *__restrict__ Tm, EpiArgs e, int *err) {
   extern __shared__ __align__(1024) unsigned char ztc_sm[];
   const int kp = (nz + 7) & ~7;  // K padded to the MMA step
   const int kq = kp / 4;         // core matrices along K
   uint32_t *Ahi = reinterpret_cast<uint32_t *>(ztc_sm);  // 128 x kp
   uint32_t *Alo = Ahi + 128 * kp;
-  uint32_t *Bhi = Alo + 128 * kp;  // 64 x kp; reused as the epilogue's staging
-  uint32_t *Blo = Bhi + ZTC_N * kp;
-  float *stg = reinterpret_cast<float *>(Bhi);  // [128][ZTC_N + 1]
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(Bhi) + ztc_b_region(kp));
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
+  uint32_t *Bst = reinterpret_cast<uint32_t *>(ztc_sm + ztc_off_b(kp));  // stage s: hi, lo (ZTC_N x kp each)
+  float *stg = reinterpret_cast<float *>(ztc_sm + ztc_off_stg(kp));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(ztc_sm + ztc_off_bar(kp));
+  const uint32_t bar0 = smem_u32(bars);
+  auto full_bar = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(ZTC_STAGES + s); };
+  auto accf_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTC_STAGES + a); };
+  auto acce_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTC_STAGES + ZTC_ACC + a); };
+  const uint32_t drain_bar = bar0 + 8u * (uint32_t)(ZTC_NBARS - 1);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + ZTC_NBARS);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // A = T split into tf32 hi / lo, rows >= nz and columns >= nz zero
@@ -105,7 +193,16 @@ __global__ void __launch_bounds__(ZTC_THREADS) k_zgemm_tc(float *spec, int nz, i
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(1));
+    for (int s = 0; s < ZTC_STAGES; ++s) {
+      mbar_init(full_bar(s), ZTC_PROD_WARPS);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int a = 0; a < ZTC_ACC; ++a) {
+      mbar_init(accf_bar(a), 1);
+      mbar_init(acce_bar(a), ZTC_EPI_WARPS);
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   asm volatile("fence.proxy.async.shared::cta;");
@@ -116,106 +213,79 @@ __global__ void __launch_bounds__(ZTC_THREADS) k_zgemm_tc(float *spec, int nz, i
 
   const int64_t tiles_per_comp = (ncols + ZTC_N - 1) / ZTC_N;
   const int64_t ntiles = 3 * tiles_per_comp;
-  // loader mapping: column n = tid % 64, row quads q = tid / 64 + 4 i
-  const int ln = tid % ZTC_N, lq0 = tid / ZTC_N;
-  constexpr int QPT = 128 / 4 / (ZTC_THREADS / ZTC_N);  // row quads per thread (kp <= 128)
-  // two tiles in flight in registers: tile t (being consumed) and t + G
-  float b0[QPT][4], b1[QPT][4];
-  auto load_tile = [&](int64_t t, float (&br)[QPT][4]) {
-    const int d = (int)(t / tiles_per_comp);
-    const int64_t col = (t % tiles_per_comp) * ZTC_N + ln;
-    const float *B = spec + (int64_t)d * nz * ncols;
-#pragma unroll
-    for (int i = 0; i < QPT; ++i) {
-      const int q = lq0 + 4 * i;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int k = 4 * q + j;
-        br[i][j] = (q < kq && k < nz && col < ncols && t < ntiles) ? __ldcs(B + (int64_t)k * ncols + col) : 0.0f;
-      }
-    }
-  };
-  auto split_tile = [&](const float (&br)[QPT][4]) {
-#pragma unroll
-    for (int i = 0; i < QPT; ++i) {
-      const int q = lq0 + 4 * i;
-      if (q >= kq) continue;
-      uint4 h, l;
-      h.x = to_tf32(br[i][0]);
-      h.y = to_tf32(br[i][1]);
-      h.z = to_tf32(br[i][2]);
-      h.w = to_tf32(br[i][3]);
-      l.x = to_tf32(br[i][0] - __uint_as_float(h.x));
-      l.y = to_tf32(br[i][1] - __uint_as_float(h.y));
-      l.z = to_tf32(br[i][2] - __uint_as_float(h.z));
-      l.w = to_tf32(br[i][3] - __uint_as_float(h.w));
-      const int o = cm_off(ln, 4 * q, kq);
-      *reinterpret_cast<uint4 *>(Bhi + o) = h;
-      *reinterpret_cast<uint4 *>(Blo + o) = l;
-    }
-  };
-  const uint32_t idesc = ztc_idesc(128, ZTC_N);
-  const uint32_t a_hi = smem_u32(Ahi), a_lo = smem_u32(Alo), b_hi = smem_u32(Bhi), b_lo = smem_u32(Blo);
-  const uint32_t sbo = kq * 128;
   const int64_t G = gridDim.x;
-  uint32_t phase = 0;
-  bool ok = true;
-  int64_t t = blockIdx.x;
-  load_tile(t, b0);
-  load_tile(t + G, b1);
-  for (int it = 0; t < ntiles && ok; t += G, ++it) {
-    if (it & 1) split_tile(b1);
-    else split_tile(b0);
-    asm volatile("fence.proxy.async.shared::cta;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      for (int s = 0; s < kp / 8; ++s) {
-        const uint32_t off = (uint32_t)s * 256u;  // two core matrices along K
-        const uint64_t ah = smem_desc(a_hi + off, 128, sbo), al = smem_desc(a_lo + off, 128, sbo);
-        const uint64_t bh = smem_desc(b_hi + off, 128, sbo), bl = smem_desc(b_lo + off, 128, sbo);
-        mma_tf32(tmem, ah, bh, idesc, s > 0 ? 1u : 0u);
-        mma_tf32(tmem, ah, bl, idesc, 1u);
-        mma_tf32(tmem, al, bh, idesc, 1u);
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(mbar)));
-    }
-    // the registers of tile t are free: start tile t + 2G
-    if (it & 1) load_tile(t + 2 * G, b1);
-    else load_tile(t + 2 * G, b0);
-    // wait for the accumulator, at most ZTC_WAIT_NS; the verdict is taken
-    // block-wide so that every thread leaves the loop together
-    uint32_t done = 0;
-    {
-      unsigned long long t0, now;
-      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-      for (int spin = 0; !done; ++spin) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, p;\n\t}\n"
-            : "=r"(done)
-            : "r"(smem_u32(mbar)), "r"(phase));
-        if (!done && (spin & 255) == 255) {
-          asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-          if (now - t0 > ZTC_WAIT_NS) break;
+  const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
+  const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
+  const int my_steps = my_tiles * nkc;         // step u = (tile u / nkc, K chunk u % nkc)
+  constexpr int SKQ = ZTC_KC / 4;              // core matrices along K in a stage
+
+  if (warp < ZTC_PROD_WARPS) {
+    // ---- producers: column n, row quads q = qg + ZTC_PGROUPS i of the chunk
+    const int n = tid % ZTC_N, qg = tid / ZTC_N;
+    float b0[ZTC_QPT][4], b1[ZTC_QPT][4], b2[ZTC_QPT][4];
+    auto load_step = [&](int u, float (&br)[ZTC_QPT][4]) {
+      const bool valid = u < my_steps;
+      const int j = valid ? u / nkc : 0, c = valid ? u - j * nkc : 0;
+      const int64_t t = blockIdx.x + (int64_t)j * G;
+      const int d = valid ? (int)(t / tiles_per_comp) : 0;
+      const int64_t col = valid ? (t % tiles_per_comp) * ZTC_N + n : 0;
+      const float *B = spec + (int64_t)d * nz * ncols;
+#pragma unroll
+      for (int i = 0; i < ZTC_QPT; ++i) {
+        const int q = qg + ZTC_PGROUPS * i;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const int k = ZTC_KC * c + 4 * q + jj;
+          br[i][jj] = (valid && k < nz && col < ncols) ? __ldcs(B + (int64_t)k * ncols + col) : 0.0f;
         }
       }
+    };
+    auto step = [&](int u, float (&br)[ZTC_QPT][4]) -> bool {
+      const int s = u % ZTC_STAGES;
+      bool ok = ztc_wait(empty_bar(s), (uint32_t)(((u / ZTC_STAGES) & 1) ^ 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) return false;
+      uint32_t *Bhi = Bst + (size_t)s * 2 * ZTC_N * ZTC_KC, *Blo = Bhi + ZTC_N * ZTC_KC;
+#pragma unroll
+      for (int i = 0; i < ZTC_QPT; ++i) {
+        const int q = qg + ZTC_PGROUPS * i;
+        uint4 h, l;
+        h.x = to_tf32(br[i][0]);
+        h.y = to_tf32(br[i][1]);
+        h.z = to_tf32(br[i][2]);
+        h.w = to_tf32(br[i][3]);
+        l.x = to_tf32(br[i][0] - __uint_as_float(h.x));
+        l.y = to_tf32(br[i][1] - __uint_as_float(h.y));
+        l.z = to_tf32(br[i][2] - __uint_as_float(h.z));
+        l.w = to_tf32(br[i][3] - __uint_as_float(h.w));
+        const int o = cm_off(n, 4 * q, SKQ);
+        *reinterpret_cast<uint4 *>(Bhi + o) = h;
+        *reinterpret_cast<uint4 *>(Blo + o) = l;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full_bar(s));
+      load_step(u + ZTC_DEPTH, br);
+      return true;
+    };
+    load_step(0, b0);
+    load_step(1, b1);
+    load_step(2, b2);
+    for (int u = 0; u < my_steps; u += 3) {
+      if (!step(u, b0)) break;
+      if (u + 1 < my_steps && !step(u + 1, b1)) break;
+      if (u + 2 < my_steps && !step(u + 2, b2)) break;
     }
-    if (!__syncthreads_and(done != 0)) {
-      if (tid == 0) atomicOr(err, 1);
-      ok = false;
-      break;
-    }
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    // accumulator -> staging (the B operand's shared memory is free now):
-    // warp w reads lanes 32 (w % 4) .. + 31, columns 32 (w / 4) .. + 31
-    {
-      uint32_t v[32];
-      const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(32 * (warp >> 2));
+  } else if (warp < ZTC_MMA_WARP) {
+    // ---- epilogue: warp owns lane quadrant qd = rows 32 qd .. 32 qd + 31.
+    // The accumulator is read 32 columns at a time; the next block's
+    // tcgen05.ld is in flight while the current block is stored.
+    const int qd = warp & 3;
+    float *st = stg + (size_t)(warp - ZTC_PROD_WARPS) * 32 * ZTC_STG;
+    const bool v4 = (ncols & 3) == 0;  // 16-byte aligned rows
+    const bool corr = INVERSE && e.ks.mode != 0 && e.corr != nullptr;
+    const float scale = INVERSE ? (float)e.scale : 1.0f;
+    uint32_t v[32];
+    auto tmem_ld = [&](uint32_t taddr) {
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
           "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
@@ -224,43 +294,116 @@ __global__ void __launch_bounds__(ZTC_THREADS) k_zgemm_tc(float *spec, int nz, i
             "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
             "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
             "=r"(v[30]), "=r"(v[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      float *row = stg + (32 * (warp & 3) + lane) * (ZTC_N + 1) + 32 * (warp >> 2);
-#pragma unroll
-      for (int j = 0; j < 32; ++j) row[j] = __uint_as_float(v[j]);
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    // coalesced epilogue: warp w writes rows w, w + 8, ...; lane = column pair
-    {
+          : "r"(taddr)
+          : "memory");
+    };
+    for (int j = 0; j < my_tiles; ++j) {
+      const int a = j % ZTC_ACC;
+      bool ok = ztc_wait(accf_bar(a), (uint32_t)((j / ZTC_ACC) & 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int64_t t = blockIdx.x + (int64_t)j * G;
       const int d = (int)(t / tiles_per_comp);
-      const int64_t col = (t % tiles_per_comp) * ZTC_N + 2 * lane;
-      if (col < ncols) {
-        for (int r = warp; r < nz; r += ZTC_THREADS / 32) {
-          float vr = stg[r * (ZTC_N + 1) + 2 * lane], vi = stg[r * (ZTC_N + 1) + 2 * lane + 1];
-          if (INVERSE) {
-            float cre, cim;
-            corr_value<float>(e, d, r, col >> 1, cre, cim);
-            vr = (vr + cre) * (float)e.scale;
-            vi = (vi + cim) * (float)e.scale;
+      const uint32_t tbase = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * ZTC_N);
+      tmem_ld(tbase);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int sb = 0; sb < ZTC_N / 32; ++sb) {
+        // row `lane` of the block -> staging (8 x 16 B, conflict-free per quarter warp)
+        float4 *srow = reinterpret_cast<float4 *>(st + lane * ZTC_STG);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          srow[c] = make_float4(__uint_as_float(v[4 * c]), __uint_as_float(v[4 * c + 1]),
+                                __uint_as_float(v[4 * c + 2]), __uint_as_float(v[4 * c + 3]));
+        __syncwarp();
+        if (sb + 1 < ZTC_N / 32) tmem_ld(tbase + (uint32_t)(32 * (sb + 1)));
+        // 4 rows x 128 B per store instruction
+        const int64_t col = (t % tiles_per_comp) * ZTC_N + 32 * sb + 4 * (lane & 7);
+#pragma unroll 4
+        for (int i = 0; i < 8; ++i) {
+          const int rl = 4 * i + (lane >> 3);
+          const int r = 32 * qd + rl;
+          if (r < nz && col < ncols) {
+            float4 q = *reinterpret_cast<const float4 *>(st + rl * ZTC_STG + 4 * (lane & 7));
+            if (corr) {
+              float c0r, c0i, c1r, c1i;
+              corr_value<float>(e, d, r, col >> 1, c0r, c0i);
+              if (col + 2 < ncols) corr_value<float>(e, d, r, (col >> 1) + 1, c1r, c1i);
+              else c1r = c1i = 0.0f;
+              q.x += c0r;
+              q.y += c0i;
+              q.z += c1r;
+              q.w += c1i;
+            }
+            if (INVERSE) {
+              q.x *= scale;
+              q.y *= scale;
+              q.z *= scale;
+              q.w *= scale;
+            }
+            float *g = spec + ((int64_t)d * nz + r) * ncols + col;
+            if (v4) {
+              __stcs(reinterpret_cast<float4 *>(g), q);
+            } else {
+              __stcs(reinterpret_cast<float2 *>(g), make_float2(q.x, q.y));
+              if (col + 2 < ncols) __stcs(reinterpret_cast<float2 *>(g + 2), make_float2(q.z, q.w));
+            }
           }
-          __stcs(reinterpret_cast<float2 *>(spec + ((int64_t)d * nz + r) * ncols + col), make_float2(vr, vi));
         }
+        if (sb + 1 < ZTC_N / 32) {
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (sb + 2 == ZTC_N / 32) {  // the last block is in registers: release the accumulator
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce_bar(a));
+          }
+        }
+        __syncwarp();  // staging reused by the next block
       }
     }
-    __syncthreads();  // staging consumed before the next split overwrites it
+  } else {
+    // ---- MMA warp: every lane takes the waits (warp vote), lane 0 issues
+    const uint32_t idesc = ztc_idesc(128, ZTC_N);
+    const uint32_t a_hi = smem_u32(Ahi), a_lo = smem_u32(Alo);
+    const uint32_t sbo_a = kq * 128, sbo_b = SKQ * 128;
+    for (int u = 0; u < my_steps; ++u) {
+      const int j = u / nkc, c = u - j * nkc;
+      const int s = u % ZTC_STAGES, a = j % ZTC_ACC;
+      bool ok = ztc_wait(full_bar(s), (uint32_t)((u / ZTC_STAGES) & 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      if (c == 0) {
+        ok = ztc_wait(acce_bar(a), (uint32_t)(((j / ZTC_ACC) & 1) ^ 1), abort_flag, err);
+        if (!__all_sync(0xffffffffu, ok)) break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (lane == 0) {
+        const uint32_t b_hi = smem_u32(Bst + (size_t)s * 2 * ZTC_N * ZTC_KC);
+        const uint32_t b_lo = b_hi + (uint32_t)(ZTC_N * ZTC_KC * 4);
+        const uint32_t dt = tmem + (uint32_t)(a * ZTC_N);
+        const int ksteps = min(ZTC_KC, kp - ZTC_KC * c) / 8;
+        for (int ks = 0; ks < ksteps; ++ks) {
+          const uint32_t offa = (uint32_t)(ZTC_KC / 8 * c + ks) * 256u, offb = (uint32_t)ks * 256u;
+          const uint64_t ah = smem_desc(a_hi + offa, 128, sbo_a), al = smem_desc(a_lo + offa, 128, sbo_a);
+          const uint64_t bh = smem_desc(b_hi + offb, 128, sbo_b), bl = smem_desc(b_lo + offb, 128, sbo_b);
+          mma_tf32(dt, ah, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+          mma_tf32(dt, ah, bl, idesc, 1u);
+          mma_tf32(dt, al, bh, idesc, 1u);
+        }
+        tc_commit(empty_bar(s));                     // the stage is free once these products are done
+        if (c == nkc - 1) tc_commit(accf_bar(a));    // and after the last stage, the accumulator
+      }
+      __syncwarp();
+    }
+    // every issued product completes before the tensor memory is freed
+    if (lane == 0) tc_commit(drain_bar);
+    __syncwarp();
+    ztc_wait(drain_bar, 0u, abort_flag, err, false);
+    __syncwarp();
   }
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ZTC_TMEM_COLS));
   }
-}
-
-size_t ztc_smem_bytes(int nz) {
-  const int kp = (nz + 7) & ~7;
-  return (size_t)2 * 128 * kp * 4 + ztc_b_region(kp) + 16;
 }
 
 cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
@@ -277,7 +420,7 @@ cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm,
   else r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<false>, ZTC_THREADS, smem);
   if (r != cudaSuccess) return r;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  if (per_sm > 4) per_sm = 4;  // 4 x 64 tensor-memory columns: allocation never waits
+  if (per_sm > 2) per_sm = 2;  // 2 x 256 tensor-memory columns: allocation never waits
   int64_t grid = (int64_t)nsm * per_sm;
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return cudaSuccess;

@@ -27,7 +27,18 @@ def _inputs(ws, dtype):
 
 
 def _single(w, X, F, T, precision, dtype):
-    op = DPStokes(StokesParams.from_workload(w, precision), w.N)
+    # the batch's z transform is the SIMT one: compare like with like (the
+    # tensor-core transform differs from it by ~1e-6, covered elsewhere)
+    import os
+    old = os.environ.get("DPSTOKES_GB300_ZTRANSFORM")
+    os.environ["DPSTOKES_GB300_ZTRANSFORM"] = "simt"
+    try:
+        op = DPStokes(StokesParams.from_workload(w, precision), w.N)
+    finally:
+        if old is None:
+            del os.environ["DPSTOKES_GB300_ZTRANSFORM"]
+        else:
+            os.environ["DPSTOKES_GB300_ZTRANSFORM"] = old
     op.set_positions(torch.tensor(X, device="cuda"))
     V, Wv = op.mdot(torch.tensor(F, dtype=dtype, device="cuda"),
                     torch.tensor(T, dtype=dtype, device="cuda") if T is not None else None)
