@@ -250,6 +250,8 @@ def run_ours(args, rank, world):
             roof["stages"][k] = {"ms": round(stages[k], 4), "algorithmic_bytes": b,
                                  "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
     roof["ztransform_kernel"] = "tcgen05 split-TF32" if info.get("ztransform") == 1 else "SIMT folded"
+    roof["ztransform_inverse_kernel"] = ("tcgen05 split-TF32" if info.get("ztransform_inverse") == 1
+                                         else "SIMT folded")
     if dom == "solve":
         # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
         roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "

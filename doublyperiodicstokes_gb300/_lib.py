@@ -35,7 +35,8 @@ class DpstInfo(ctypes.Structure):
                 ("device_bytes", ctypes.c_int64), ("n_particles", ctypes.c_int64),
                 ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int),
                 ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
-                ("fused_particle_passes", ctypes.c_int)]
+                ("fused_particle_passes", ctypes.c_int), ("ztransform_inverse", ctypes.c_int),
+                ("ztransform_inverse_ms", ctypes.c_float * 2)]
 
 
 class DpstBatchInfo(ctypes.Structure):

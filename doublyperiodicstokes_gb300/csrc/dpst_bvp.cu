@@ -82,7 +82,7 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
 // DPTools.cpp:197-216 moves into the window's SIMat bands and the BC values
 // are scaled by eta), which saves a multiply per row.  WALLS = false (open
 // domain) skips the wall values that only the corrections use.
-template <typename R, bool WALLS>
+template <typename R, bool WALLS, int PF_F, int PF_B>
 static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
                                                 int i, bool store, const BvpCtx &ctx) {
   const int nz = a.nz;
@@ -140,11 +140,11 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   // border dots y = C x accumulated during the back sweep.  Rows 0, 1 of
   // mf and the dp2 of the last two rows are zero, so both loops are uniform.
   // The factor streams are read PF_F / PF_B rows ahead of the recurrence
-  // through register rings (prefetch indices clamped into the table), and
+  // through register rings (prefetch indices clamped into the table; the
+  // depths follow the kernel's register budget, BvpRings), and
   // the border dots accumulate in two partial sums (rows of even and odd
   // distance from the last), which halves their FP64 dependency chains.
   auto penta = [&](double &y0, double &y1) {
-    constexpr int PF_F = 16, PF_B = 8;
     double xm2 = 0.0, xm1 = 0.0;
     double pm[PF_F];
 #pragma unroll
@@ -371,6 +371,8 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   double *crd = reinterpret_cast<double *>(corr + i * 16);
   if (a.mode == 1) {
     for (int c = 0; c < 3; ++c) crd[2 * c + part] = -wb[c];
+    if (a.corrf)
+      for (int c = 0; c < 3; ++c) reinterpret_cast<float *>(a.corrf + i * 16)[2 * c + part] = (float)(-wb[c]);
   } else if (a.mode == 2 && part == 0) {
     double2 fb[3], ft[3], cf[8];
     for (int c = 0; c < 3; ++c) {
@@ -379,6 +381,8 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
     }
     slit_coeffs(kx, ky, a.Lz, a.eta, fb, ft, cf);
     for (int r = 0; r < 8; ++r) corr[i * 16 + r] = cf[r];
+    if (a.corrf)
+      for (int r = 0; r < 8; ++r) a.corrf[i * 16 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
     double kxp, kyp;
     if (!mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp)) {
       for (int c = 0; c < 3; ++c) {
@@ -387,19 +391,38 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
       }
       slit_coeffs(kxp, kyp, a.Lz, a.eta, fb, ft, cf);
       for (int r = 0; r < 8; ++r) corr[i * 16 + 8 + r] = cf[r];
+      if (a.corrf)
+        for (int r = 0; r < 8; ++r) a.corrf[i * 16 + 8 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
     }
   }
 #undef XS
+}
+
+// Factor-ring depths (forward sweep, back sweep) of the kernel compiled for
+// MINB CTAs per SM: one CTA (large nz, shared memory allows no more) has the
+// whole register file and reads 16 / 8 rows ahead; two CTAs (small nz) keep
+// under half of it with 8 / 2 rows.
+template <int MINB>
+struct BvpRings {
+  static constexpr int F = MINB == 1 ? 16 : 8;
+  static constexpr int B = MINB == 1 ? 8 : 2;
+};
+
+// Two CTAs per SM when their shared memory fits (228 KB per SM, 1 KB of it
+// reserved per CTA).
+static bool bvp_two_per_sm(int nz) {
+  const size_t per_cta = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES + TB_DH * BVP_NZMAX + BVP_NZMAX + 1) + 1024;
+  return 2 * per_cta <= (size_t)228 * 1024;
 }
 
 // Work split: CTA b owns the contiguous modes [b per_cta, (b+1) per_cta),
 // per_cta a multiple of 16 (the modes of one warp), and walks them 96 at a
 // time; a warp whose 16 modes lie past the CTA's range skips the tile, so
 // the last, partial tile of every CTA costs only the warps it needs.
-template <typename R>
-__global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
-                                                         double2 *__restrict__ corr,
-                                                         double *__restrict__ cp_scratch, int per_cta) {
+template <typename R, int MINB>
+__global__ void __launch_bounds__(BVP_LANES, MINB) k_bvp_pairs(KsArgs a, R *__restrict__ spec,
+                                                            double2 *__restrict__ corr,
+                                                            double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
   const BvpCtx ctx = bvp_ctx(a, bvp_sm, cp_scratch);
   __syncthreads();
@@ -412,18 +435,18 @@ __global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs(KsArgs a, R *__restr
     const int i_raw = base + q;
     const int i = i_raw < cta_end ? i_raw : cta_end - 1;
     const bool store = (i_raw < cta_end) && (i != 0);  // mode 0: k_bvp_k0
-    if (a.mode != 0) bvp_mode<R, true>(a, spec, corr, i, store, ctx);
-    else bvp_mode<R, false>(a, spec, corr, i, store, ctx);
+    if (a.mode != 0) bvp_mode<R, true, BvpRings<MINB>::F, BvpRings<MINB>::B>(a, spec, corr, i, store, ctx);
+    else bvp_mode<R, false, BvpRings<MINB>::F, BvpRings<MINB>::B>(a, spec, corr, i, store, ctx);
   }
 }
 
 // Batched systems: global mode g of [0, mprefix[S]) belongs to system s with
 // mprefix[s] <= g < mprefix[s+1]; every system has the same nz and H (the
 // shared-memory tables), its own factors, spectrum and corrections.
-template <typename R>
-__global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs_b(const SysK<R> *__restrict__ sys, int S,
-                                                           const int64_t *__restrict__ mprefix,
-                                                           double *__restrict__ cp_scratch, int per_cta) {
+template <typename R, int MINB>
+__global__ void __launch_bounds__(BVP_LANES, MINB) k_bvp_pairs_b(const SysK<R> *__restrict__ sys, int S,
+                                                              const int64_t *__restrict__ mprefix,
+                                                              double *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
   const BvpCtx ctx = bvp_ctx(sys[0].ks, bvp_sm, cp_scratch);
   __syncthreads();
@@ -439,8 +462,8 @@ __global__ void __launch_bounds__(BVP_LANES, 1) k_bvp_pairs_b(const SysK<R> *__r
     const SysK<R> &y = sys[s];
     const int i = (int)(g - mprefix[s]);
     const bool store = (g_raw < cta_end) && (i != 0);
-    if (y.ks.mode != 0) bvp_mode<R, true>(y.ks, y.spec, y.corr, i, store, ctx);
-    else bvp_mode<R, false>(y.ks, y.spec, y.corr, i, store, ctx);
+    if (y.ks.mode != 0) bvp_mode<R, true, BvpRings<MINB>::F, BvpRings<MINB>::B>(y.ks, y.spec, y.corr, i, store, ctx);
+    else bvp_mode<R, false, BvpRings<MINB>::F, BvpRings<MINB>::B>(y.ks, y.spec, y.corr, i, store, ctx);
   }
 }
 
@@ -512,13 +535,13 @@ __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restr
 }
 
 // Grid of the persistent BVP kernel and the bytes of its pressure scratch.
-template <typename R>
-cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+template <typename R, int MINB>
+static cudaError_t bvp_plan_v(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
-  cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs<R, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs<R>, BVP_LANES, smem);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs<R, MINB>, BVP_LANES, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if ((int64_t)a.nz * a.nk * 4 >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
@@ -530,14 +553,20 @@ cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_by
   return cudaSuccess;
 }
 
-// Batched solve: grid and scratch for K modes in total with a shared nz.
 template <typename R>
-cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
+cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  return bvp_two_per_sm(a.nz) ? bvp_plan_v<R, 2>(a, nsm, grid, scratch_bytes)
+                              : bvp_plan_v<R, 1>(a, nsm, grid, scratch_bytes);
+}
+
+// Batched solve: grid and scratch for K modes in total with a shared nz.
+template <typename R, int MINB>
+static cudaError_t bvp_plan_b_v(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
   const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES);
-  cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs_b<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_pairs_b<R, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs_b<R>, BVP_LANES, smem);
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_pairs_b<R, MINB>, BVP_LANES, smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int64_t g = (int64_t)nsm * per_sm;
@@ -550,12 +579,19 @@ cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratc
 }
 
 template <typename R>
+cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  return bvp_two_per_sm(nz) ? bvp_plan_b_v<R, 2>(nz, K, nsm, grid, scratch_bytes)
+                            : bvp_plan_b_v<R, 1>(nz, K, nsm, grid, scratch_bytes);
+}
+
+template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES);
   const int64_t per = (K + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
-  k_bvp_pairs_b<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  if (bvp_two_per_sm(nz)) k_bvp_pairs_b<R, 2><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  else k_bvp_pairs_b<R, 1><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_bvp_k0_b<R><<<S, 2 * K0_ROWS, 0, s>>>(sys);
@@ -575,7 +611,8 @@ cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch,
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
   const int64_t per = (a.nk + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
-  k_bvp_pairs<R><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
+  if (bvp_two_per_sm(a.nz)) k_bvp_pairs<R, 2><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
+  else k_bvp_pairs<R, 1><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);

@@ -138,6 +138,7 @@ struct Engine : EngineBase {
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g, fac_pm, fac_pb, fac_pa;
   DevBuf pos64, flags;
   DevBuf ord_count, ord_start, perm;  // particles sorted by grid tile
+  DevBuf corrf, cmode, znf;           // FP32 correction tables (mixed operator, walls)
   DevBuf st_m[8], st_d[8];
   DevBuf gh_m[2], gh_d[2];
   DevBuf hF, hT, hV, hW;  // staging for the host-array entry points
@@ -238,6 +239,29 @@ struct Engine : EngineBase {
     grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
     spec.alloc(sizeof(CR) * 3 * (size_t)nz * nk);
     if (p.mode != DPST_MODE_NOWALL) corr.alloc(sizeof(double2) * 16 * (size_t)nk);
+    if (p.mode != DPST_MODE_NOWALL && sizeof(R) == 4) {
+      // FP32 tables of the mixed operator's correction epilogue: the solve's
+      // coefficients in FP32, per mode {k, kx, ky, Hermitian} and the partner
+      // index's {kx', ky'} (as mode_is_hermitian finds them), the nodes
+      corrf.alloc(sizeof(float2) * 16 * (size_t)nk);
+      std::vector<float> cm(8 * (size_t)nk, 0.0f);
+      for (int64_t i = 0; i < nk; ++i) {
+        const int ix = (int)(i % nxh), iy = (int)(i / nxh);
+        const double kxi = kx[ix], kyi = ky[iy];
+        const double kxp = kx[(nx - ix) % nx], kyp = ky[(ny - iy) % ny];
+        float *r = &cm[8 * (size_t)i];
+        r[0] = (float)std::sqrt(kxi * kxi + kyi * kyi);
+        r[1] = (float)kxi;
+        r[2] = (float)kyi;
+        r[3] = (kxp == -kxi && kyp == -kyi) ? 1.0f : 0.0f;
+        r[4] = (float)kxp;
+        r[5] = (float)kyp;
+      }
+      upload(cmode, cm);
+      const std::vector<float> zf(zG.begin(), zG.end());
+      upload(znf, zf);
+      ks.corrf = corrf.as<float2>();
+    }
     size_t bvp_bytes = 0;
     DPST_CUDA(bvp_plan<R>(ks, nsm, &bvp_grid, &bvp_bytes));
     bvp_scratch.alloc(bvp_bytes);
@@ -411,13 +435,29 @@ struct Engine : EngineBase {
 
   // ---- z transform kernel choice (creation-time autotuner) -----------------
   // 0: SIMT even/odd-folded GEMM (FP32 or FP64); 1: tcgen05 split-TF32 (FP32
-  // data only, nz <= 128).  DPSTOKES_GB300_ZTRANSFORM = simt | tcgen05 | auto
-  // (default) overrides the choice; auto times both on this handle's buffers.
-  int ztc = 0;
-  float ztc_ms[2] = {0.f, 0.f};
+  // data only, nz <= 128).  Chosen separately for the plain transforms
+  // (ztc[0]: forward, and the backward's adjoint transforms) and for the
+  // inverse with its wall-correction epilogue (ztc[1]), each timed on this
+  // handle's buffers.  DPSTOKES_GB300_ZTRANSFORM = simt | tcgen05 | auto
+  // (default) overrides the choice.
+  int ztc[2] = {0, 0};
+  float ztc_ms[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [direction][impl]
   DevBuf ztc_err;
 
-  cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl) {
+  // the wall-correction inputs of the inverse transform's epilogue
+  void epi_corr(EpiArgs &e) const {
+    e.corr = corr.as<double2>();
+    if (corrf.p != nullptr) {
+      e.corrf = corrf.as<float2>();
+      e.cmode = cmode.as<float4>();
+      e.znf = znf.as<float>();
+      e.fac = (float)(1.0 / 2.0 / p.viscosity);
+    }
+  }
+
+  // impl < 0: the tuned kernel for e's direction
+  cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl = -1) {
+    if (impl < 0) impl = ztc[e.inverse ? 1 : 0];
     if (impl == 1 && sizeof(R) == 4)
       return launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk, reinterpret_cast<const float *>(T), e, nsm,
                              ztc_err.as<int>(), s);
@@ -432,32 +472,38 @@ struct Engine : EngineBase {
     if (sizeof(R) != 4 || nz > 128 || want == "simt") return;
     R *sp = reinterpret_cast<R *>(spec.p);
     DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
-    EpiArgs e;
-    memset(&e, 0, sizeof(e));
-    e.scale = 1.0;
-    e.ks = ks;
+    DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
     cudaEvent_t a, b;
     DPST_CUDA(cudaEventCreate(&a));
     DPST_CUDA(cudaEventCreate(&b));
-    for (int impl = 0; impl < 2; ++impl) {
-      DPST_CUDA(zgemm(sp, Tf.as<R>(), e, false, 0, impl));  // warm-up
-      DPST_CUDA(cudaEventRecord(a, 0));
-      for (int rep = 0; rep < 3; ++rep) DPST_CUDA(zgemm(sp, Tf.as<R>(), e, false, 0, impl));
-      DPST_CUDA(cudaEventRecord(b, 0));
-      DPST_CUDA(cudaEventSynchronize(b));
-      DPST_CUDA(cudaEventElapsedTime(&ztc_ms[impl], a, b));
-      ztc_ms[impl] /= 3.0f;
+    for (int dir = 0; dir < 2; ++dir) {
+      EpiArgs e;
+      memset(&e, 0, sizeof(e));
+      e.ks = ks;
+      e.inverse = dir;
+      e.scale = dir ? 1.0 / ((double)nx * (double)ny) : 1.0;
+      if (dir) epi_corr(e);
+      const R *T = dir ? Ti.as<R>() : Tf.as<R>();
+      for (int impl = 0; impl < 2; ++impl) {
+        DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));  // warm-up
+        DPST_CUDA(cudaEventRecord(a, 0));
+        for (int rep = 0; rep < 3; ++rep) DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));
+        DPST_CUDA(cudaEventRecord(b, 0));
+        DPST_CUDA(cudaEventSynchronize(b));
+        DPST_CUDA(cudaEventElapsedTime(&ztc_ms[dir][impl], a, b));
+        ztc_ms[dir][impl] /= 3.0f;
+      }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     int err = 0;
     DPST_CUDA(cudaMemcpy(&err, ztc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {  // the tensor-core kernel gave up waiting: keep the SIMT kernel
-      ztc = 0;
+      ztc[0] = ztc[1] = 0;
       DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
       return;
     }
-    ztc = (want == "tcgen05" || ztc_ms[1] < ztc_ms[0]) ? 1 : 0;
+    for (int dir = 0; dir < 2; ++dir) ztc[dir] = (want == "tcgen05" || ztc_ms[dir][1] < ztc_ms[dir][0]) ? 1 : 0;
   }
 
   // grid (spread forces) -> grid (velocities): x-y FFT, z transform, per-k
@@ -476,7 +522,7 @@ struct Engine : EngineBase {
     ef.inverse = 0;
     ef.scale = 1.0;
     ef.ks = ks;
-    DPST_CUDA(zgemm((R *)sp, Tf.as<R>(), ef, false, s, ztc));
+    DPST_CUDA(zgemm((R *)sp, Tf.as<R>(), ef, false, s));
     mark(3, s);
     if (!use_static_scratch) {
       DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
@@ -494,8 +540,8 @@ struct Engine : EngineBase {
     EpiArgs eb = ef;
     eb.inverse = 1;
     eb.scale = 1.0 / ((double)nx * (double)ny);
-    eb.corr = corr.as<double2>();
-    DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s, ztc));
+    epi_corr(eb);
+    DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
     mark(5, s);
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
@@ -624,9 +670,9 @@ struct Engine : EngineBase {
     e.inverse = 0;
     e.scale = 1.0;
     e.ks = ks;
-    DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s, ztc));
+    DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s));
     DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
-    DPST_CUDA(zgemm((R *)sp, TfTn.as<R>(), e, true, s, ztc));
+    DPST_CUDA(zgemm((R *)sp, TfTn.as<R>(), e, true, s));
     DPST_CUFFT(cufftSetStream(plan_b, s));
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)g2));
@@ -737,16 +783,20 @@ struct Engine : EngineBase {
     // forward z GEMM, BVP pairs + k=0, inverse z GEMM, interp (mono [+ dip])
     int nbuf = (ghm.top != nullptr) + (ghm.bot != nullptr) + (ghd.top != nullptr) + (ghd.bot != nullptr);
     o->ghost_layers_in_use = nbuf;
-    o->ztransform = ztc;
-    o->ztransform_ms[0] = ztc_ms[0];
-    o->ztransform_ms[1] = ztc_ms[1];
+    o->ztransform = ztc[0];
+    o->ztransform_ms[0] = ztc_ms[0][0];
+    o->ztransform_ms[1] = ztc_ms[0][1];
+    o->ztransform_inverse = ztc[1];
+    o->ztransform_inverse_ms[0] = ztc_ms[1][0];
+    o->ztransform_inverse_ms[1] = ztc_ms[1][1];
     const int particle_passes = (p.has_torque && !fused) ? 2 : 1;
     o->kernels_per_mdot = particle_passes + 2 * nbuf + 1 + 2 + 1 + particle_passes;
     o->fused_particle_passes = fused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
-                           &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm};
+                           &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm,
+                           &corrf, &cmode, &znf};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;

@@ -124,6 +124,10 @@ struct KsArgs {
   // k = 0 velocity correction: C rows (length nz) and Gi row-major
   const double *k0c0, *k0c1;
   double k0gi[4];
+  // FP32 copy of the wall-correction coefficients [nk][16], written by the
+  // solve beside the FP64 ones for the mixed operator's epilogue (nullptr:
+  // not wanted)
+  float2 *corrf;
 };
 
 // Epilogue of the z-transform GEMM.
@@ -131,6 +135,14 @@ struct EpiArgs {
   int inverse;
   double scale;  // 1/(nx ny) for the inverse
   const double2 *corr;
+  // FP32 form of the correction for the mixed operator (all nullptr: use
+  // corr): the solve's FP32 coefficients [nk][16], per mode {k, kx, ky,
+  // Hermitian ? 1 : 0} and {kx', ky', 0, 0} of the partner index, the nodes
+  // in FP32 and 1 / (2 eta)
+  const float2 *corrf;
+  const float4 *cmode;
+  const float *znf;
+  float fac;
   KsArgs ks;
 };
 

@@ -221,4 +221,73 @@ static __device__ __forceinline__ void corr_value(const EpiArgs &e, int d, int m
   im = acc.y;
 }
 
+// corr_value of the mixed operator from FP32 tables only (EpiArgs' corrf,
+// cmode, znf): the same values as corr_value<float> (every FP64 input there
+// is rounded to FP32 before use), without its per-element FP64 work
+// (wavenumber lookups, square root, conversions), which runs at 1/64 of the
+// FP32 rate on this GPU.
+static __device__ __forceinline__ void corr_value_f(const EpiArgs &e, int d, int m, int64_t mode, float &re,
+                                                    float &im) {
+  typedef float CT;
+  re = 0;
+  im = 0;
+  const KsArgs &a = e.ks;
+  if (a.mode == 0 || mode == 0) return;
+  const float4 m0 = e.cmode[2 * mode];
+  const CT k = m0.x;
+  const CT z = e.znf[m];
+  const float2 *cr = e.corrf + mode * 16;
+  const CT enkz = expf(-k * z);
+  const CT zenkz = z * enkz;
+  cplx<CT> acc = mk<CT>(0, 0);
+  const int npass = m0.w != 0.0f ? 1 : 2;
+  for (int pass = 0; pass < npass; ++pass) {
+    CT qx = m0.y, qy = m0.z;
+    if (pass) {
+      const float4 m1 = e.cmode[2 * mode + 1];
+      qx = m1.x;
+      qy = m1.y;
+    }
+    cplx<CT> v;
+    if (a.mode == 1) {
+      cplx<CT> f0 = mk<CT>(cr[0].x, cr[0].y), f1 = mk<CT>(cr[1].x, cr[1].y), f2 = mk<CT>(cr[2].x, cr[2].y);
+      if (pass) { f0 = conj(f0); f1 = conj(f1); f2 = conj(f2); }
+      const cplx<CT> al = (qx * f0 + qy * f1) + ik(k, f2);
+      if (d == 0) v = (-qx * zenkz / k) * al + enkz * f0;
+      else if (d == 1) v = (-qy * zenkz / k) * al + enkz * f1;
+      else v = ik(-zenkz, al) + enkz * f2;
+    } else {
+      const float2 *c = cr + 8 * pass;
+      auto C = [&](int r) { return mk<CT>(c[r].x, c[r].y); };
+      const CT fac = e.fac;
+      const CT ekzmh = expf(k * (z - (CT)a.Lz));
+      const CT zekzmh = z * ekzmh;
+      if (d == 0)
+        v = (ik(-qx * zenkz * fac / k, C(0)) + ik(qx * zekzmh * fac / k, C(1))) + (enkz * C(2) + ekzmh * C(3));
+      else if (d == 1)
+        v = (ik(-qy * zenkz * fac / k, C(0)) + ik(qy * zekzmh * fac / k, C(1))) + (enkz * C(4) + ekzmh * C(5));
+      else
+        v = ((zenkz * fac) * C(0) + (zekzmh * fac) * C(1)) + (enkz * C(6) + ekzmh * C(7));
+    }
+    if (pass) v = conj(v);
+    acc = acc + v;
+  }
+  if (npass == 2) acc = (CT)0.5 * acc;
+  re = acc.x;
+  im = acc.y;
+}
+
+// The correction at (component d, node m, mode): from the FP32 tables when
+// the epilogue has them (mixed operator), else corr_value.
+template <typename R>
+static __device__ __forceinline__ void corr_any(const EpiArgs &e, int d, int m, int64_t mode, R &re, R &im) {
+  if constexpr (sizeof(R) == 4) {
+    if (e.corrf != nullptr) {
+      corr_value_f(e, d, m, mode, re, im);
+      return;
+    }
+  }
+  corr_value<R>(e, d, m, mode, re, im);
+}
+
 }  // namespace dpst

@@ -238,7 +238,7 @@ static __device__ __forceinline__ void zgemm_tile(R *B, int nz, int64_t ncols, i
         R vr = acc[q][2 * cp], vi = acc[q][2 * cp + 1];
         if (e.inverse) {
           R cre, cim;
-          corr_value<R>(e, d, r, col >> 1, cre, cim);
+          corr_any<R>(e, d, r, col >> 1, cre, cim);
           vr = (vr + cre) * (R)e.scale;
           vi = (vi + cim) * (R)e.scale;
         }
@@ -297,7 +297,7 @@ static __device__ __forceinline__ void zgemm_tile(R *B, int nz, int64_t ncols, i
           R vi = half ? ae[q][2 * cp + 1] - ao[q][2 * cp + 1] : ae[q][2 * cp + 1] + ao[q][2 * cp + 1];
           if (e.inverse) {
             R cre, cim;
-            corr_value<R>(e, d, r, col >> 1, cre, cim);
+            corr_any<R>(e, d, r, col >> 1, cre, cim);
             vr = (vr + cre) * (R)e.scale;
             vi = (vi + cim) * (R)e.scale;
           }

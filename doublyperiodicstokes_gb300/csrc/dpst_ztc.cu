@@ -4,7 +4,7 @@
 // The transform is OUT[r][col] = sum_m T[r][m] IN[m][col] over every real
 // column of the spectrum (per component: nz rows x 2 nk columns, in place),
 // with the inverse's epilogue adding the wall correction and scaling
-// (corr_value, as k_zgemm does).  Per tile: M = 128 rows (nz padded with zero
+// (corr_any, as k_zgemm does).  Per tile: M = 128 rows (nz padded with zero
 // rows of T), N = 128 columns, K = nz padded to a multiple of 8 and streamed
 // through shared memory in stages of 32 rows.  Each FP32
 // operand x is split as x = hi + lo with hi = tf32(x), lo = tf32(x - hi) and
@@ -326,8 +326,8 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
             float4 q = *reinterpret_cast<const float4 *>(st + rl * ZTC_STG + 4 * (lane & 7));
             if (corr) {
               float c0r, c0i, c1r, c1i;
-              corr_value<float>(e, d, r, col >> 1, c0r, c0i);
-              if (col + 2 < ncols) corr_value<float>(e, d, r, (col >> 1) + 1, c1r, c1i);
+              corr_any<float>(e, d, r, col >> 1, c0r, c0i);
+              if (col + 2 < ncols) corr_any<float>(e, d, r, (col >> 1) + 1, c1r, c1i);
               else c1r = c1i = 0.0f;
               q.x += c0r;
               q.y += c0i;

@@ -112,14 +112,19 @@ typedef struct dpst_info {
   int kernels_per_mdot; /* kernels of this library one dpst_mdot launches (with T
                            and W given); cuFFT kernels and memsets not counted */
   int ghost_layers_in_use; /* open-end ghost buffers the current positions need */
-  int ztransform;          /* z-transform kernel chosen at creation: 0 FP32/FP64 SIMT
-                              (even/odd folded), 1 tcgen05 split-TF32 (mixed only) */
+  int ztransform;          /* z-transform kernel chosen at creation for the forward
+                              transform (and the backward's adjoint transforms): 0
+                              FP32/FP64 SIMT (even/odd folded), 1 tcgen05 split-TF32
+                              (mixed only) */
   float ztransform_ms[2];  /* creation-time timings of one transform: SIMT, tcgen05
                               (0 if not timed) */
   int fused_particle_passes; /* 1: torques spread and interpolate in the same pass as
                                 the forces (the dipole kernel's stencil columns and z
                                 ghost extension equal the monopole's and its threshold
                                 is not larger); 0: separate monopole / dipole passes */
+  int ztransform_inverse;          /* kernel of the inverse z transform (with the wall-
+                                      correction epilogue), chosen separately: 0 / 1 */
+  float ztransform_inverse_ms[2];  /* its creation-time timings: SIMT, tcgen05 */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;
