@@ -89,6 +89,7 @@ struct BatchEngine : BatchBase {
   int64_t fold_x_m = 0, fold_y_m = 0, fold_x_d = 0, fold_y_d = 0;
   // device data
   DevBuf grid, spec, corr, zext, wext, zn, bands, bcrows, k0rows, Tf, Ti, kvs;
+  DevBuf corrf, cmode, znf;  // FP32 correction tables (mixed operator, walls)
   DevBuf f_mf, f_bk, f_ab, f_g;
   DevBuf st_cell_m, st_x_m, st_y_m, st_z_m, st_zw_m;
   DevBuf st_cell_d, st_x_d, st_y_d, st_z_d, st_zw_d, st_dx_d, st_dy_d, st_dz_d, st_dzw_d;
@@ -211,6 +212,34 @@ struct BatchEngine : BatchBase {
     grid.alloc(sizeof(R) * gtot);
     spec.alloc(sizeof(CR) * stot);
     if (mode != DPST_MODE_NOWALL) corr.alloc(sizeof(double2) * 16 * (size_t)K);
+    if (mode != DPST_MODE_NOWALL && sizeof(R) == 4) {
+      // FP32 tables of the mixed operator's correction epilogue, per system
+      // at its mode offset: the solve's coefficients in FP32, per mode {k, kx,
+      // ky, Hermitian} and the partner index's {kx', ky'}; the shared nodes
+      corrf.alloc(sizeof(float2) * 16 * (size_t)K);
+      std::vector<float> cm(8 * (size_t)K, 0.0f);
+      for (int s = 0; s < S; ++s) {
+        const dpst_params &p = prm[s];
+        const int nxh = p.nx / 2 + 1;
+        const int64_t nk = (int64_t)p.ny * nxh;
+        const double *kx = kv.data() + kvoff[s], *ky = kx + p.nx;
+        for (int64_t i = 0; i < nk; ++i) {
+          const int ix = (int)(i % nxh), iy = (int)(i / nxh);
+          const double kxi = kx[ix], kyi = ky[iy];
+          const double kxp = kx[(p.nx - ix) % p.nx], kyp = ky[(p.ny - iy) % p.ny];
+          float *r = &cm[8 * (size_t)(moff[s] + i)];
+          r[0] = (float)std::sqrt(kxi * kxi + kyi * kyi);
+          r[1] = (float)kxi;
+          r[2] = (float)kyi;
+          r[3] = (kxp == -kxi && kyp == -kyi) ? 1.0f : 0.0f;
+          r[4] = (float)kxp;
+          r[5] = (float)kyp;
+        }
+      }
+      upload(cmode, cm);
+      const std::vector<float> zf(zG.begin(), zG.end());
+      upload(znf, zf);
+    }
 
     // ---- per-mode factors of every system (working arrays reused)
     int64_t nk_max = 0;
@@ -274,6 +303,7 @@ struct BatchEngine : BatchBase {
         ks.mf = f_mf.as<double>() + nz * moff[s];
         ks.bk = f_bk.as<double>() + 4 * nz * moff[s];
         ks.ab = f_ab.as<double>() + nz * moff[s];
+        ks.corrf = corrf.p != nullptr ? corrf.as<float2>() + 16 * moff[s] : nullptr;
         launch_bvp_factors(ks, 0);
         DPST_CUDA(cudaGetLastError());
         ks.mfac = ks.invb = ks.dp2 = ks.ab0 = ks.ab1 = ks.c0 = ks.c1 = nullptr;
@@ -303,6 +333,12 @@ struct BatchEngine : BatchBase {
       segi[oi].e.inverse = 1;
       segi[oi].e.scale = 1.0 / ((double)prm[s].nx * (double)prm[s].ny);
       segi[oi].e.corr = sysk[s].corr;
+      if (corrf.p != nullptr) {
+        segi[oi].e.corrf = corrf.as<float2>() + 16 * moff[s];
+        segi[oi].e.cmode = cmode.as<float4>() + 2 * moff[s];
+        segi[oi].e.znf = znf.as<float>();
+        segi[oi].e.fac = (float)(1.0 / 2.0 / prm[s].viscosity);
+      }
     }
     ntiles = tprefix[S];
     upload(d_sysk, sysk_sorted);
@@ -622,7 +658,8 @@ struct BatchEngine : BatchBase {
                            &d_jobs_m, &d_jobs_d, &grid, &spec, &corr, &zext, &wext, &zn, &bands, &bcrows, &k0rows,
                            &Tf, &Ti, &kvs, &f_mf, &f_bk, &f_ab, &f_g, &st_cell_m, &st_x_m, &st_y_m, &st_z_m,
                            &st_zw_m, &st_cell_d, &st_x_d, &st_y_d, &st_z_d, &st_zw_d, &st_dx_d, &st_dy_d,
-                           &st_dz_d, &st_dzw_d, &ghost_buf, &pos64, &bvp_scratch, &fft_work, &sF, &sT, &sV, &sW};
+                           &st_dz_d, &st_dzw_d, &ghost_buf, &pos64, &bvp_scratch, &fft_work, &sF, &sT, &sV, &sW,
+                           &corrf, &cmode, &znf};
     for (const DevBuf *d : all) bytes += d->bytes;
     o->device_bytes = bytes;
   }
