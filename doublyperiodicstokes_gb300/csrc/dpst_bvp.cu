@@ -41,22 +41,29 @@ enum BvpTab { TB_S0, TB_SM2, TB_SP2, TB_FM1, TB_FP1, TB_S0E, TB_SM2E, TB_SP2E, T
 __shared__ double bvp_tab[TB_DH * BVP_NZMAX + BVP_NZMAX + 1];
 #define TAB(t, j) bvp_tab[(t) * BVP_NZMAX + (j)]
 
-// Shared-memory column and pressure scratch of one lane of the solve.
+// Column and pressure scratch of one lane of the solve.
 struct BvpCtx {
-  double *Xs;  // [(nz + 2)][BVP_LANES] penta / RHS columns
+  double *Xs;  // [(nz + 2)][BVP_LANES] penta / RHS columns in shared memory
+  double *Xg;  // or this lane's column in global memory, row j at Xg[j * XGT]
   double *CPs;        // this lane's pressure coefficients, row j at CPs[j * GT]
   const double *CPo;  // the partner lane's
-  int GT, tid;
+  int GT, XGT, tid;
 };
 
 // Load the tables (identical for every wavenumber) into shared memory.
-static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm, double *cp_scratch) {
+// LANES = 2 * BVP_LANES (the hybrid kernel): threads BVP_LANES and up keep
+// their columns in xs_scratch, [nz + 2][BVP_LANES x CTAs of the grid].
+template <int LANES = BVP_LANES>
+static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm, double *cp_scratch,
+                                                 double *xs_scratch = nullptr) {
   const int nz = a.nz, tid = threadIdx.x;
   constexpr int T = BVP_LANES;
   BvpCtx c;
   c.Xs = bvp_sm;
+  c.XGT = gridDim.x * T;
+  c.Xg = (LANES > T && tid >= T) ? xs_scratch + blockIdx.x * T + (tid - T) : nullptr;
   const double inv_eta = 1.0 / a.eta;
-  for (int t = tid; t < nz; t += T) {
+  for (int t = tid; t < nz; t += LANES) {
     TAB(TB_S0, t) = a.s0[t];
     TAB(TB_SM2, t) = a.sm2[t];
     TAB(TB_SP2, t) = a.sp2[t];
@@ -66,12 +73,12 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
     TAB(TB_SM2E, t) = a.sm2[t] * inv_eta;
     TAB(TB_SP2E, t) = a.sp2[t] * inv_eta;
   }
-  for (int t = tid; t <= nz; t += T) TAB(TB_DH, t) = (double)(2 * t) / a.H;
+  for (int t = tid; t <= nz; t += LANES) TAB(TB_DH, t) = (double)(2 * t) / a.H;
   // pressure coefficients of every lane of the grid, [nz][lanes of the grid]
   // in global memory (L2 resident: a few tens of MB)
-  c.GT = gridDim.x * T;
-  c.CPs = cp_scratch + blockIdx.x * T + tid;
-  c.CPo = cp_scratch + blockIdx.x * T + (tid ^ 1);
+  c.GT = gridDim.x * LANES;
+  c.CPs = cp_scratch + blockIdx.x * LANES + tid;
+  c.CPo = cp_scratch + blockIdx.x * LANES + (tid ^ 1);
   c.tid = tid;
   return c;
 }
@@ -82,7 +89,7 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
 // DPTools.cpp:197-216 moves into the window's SIMat bands and the BC values
 // are scaled by eta), which saves a multiply per row.  WALLS = false (open
 // domain) skips the wall values that only the corrections use.
-template <typename R, bool WALLS, int PF_F, int PF_B>
+template <typename R, bool WALLS, int PF_F, int PF_B, bool GCOL = false>
 static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
                                                 int i, bool store, const BvpCtx &ctx) {
   const int nz = a.nz;
@@ -90,10 +97,12 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   constexpr int T = BVP_LANES;
   const int tid = ctx.tid, part = tid & 1;
   double *Xs = ctx.Xs;
+  double *__restrict__ Xg = ctx.Xg;
+  const int XGT = ctx.XGT;
   double *__restrict__ CPs = ctx.CPs;
   const double *__restrict__ CPo = ctx.CPo;
   const int GT = ctx.GT;
-#define XS(j) Xs[(j) * T + tid]
+#define XS(j) (*(GCOL ? Xg + (j) * XGT : Xs + (j) * T + tid))
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
   const int rs = 2 * nk;  // spectrum row stride (R elements)
   // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
@@ -440,6 +449,44 @@ __global__ void __launch_bounds__(BVP_LANES, MINB) k_bvp_pairs(KsArgs a, R *__re
   }
 }
 
+// Hybrid kernel for large nz, where shared memory holds the columns of only
+// BVP_LANES lanes per SM: twice the lanes per CTA, the second half keeping
+// their penta columns in an L2-resident global scratch.  More warps per SM
+// keep more factor loads in flight (the solve's limit when one CTA of
+// BVP_LANES fits).  Warps take 16-mode units from a counter (zeroed before
+// the launch), so the two kinds of warps share the work by their own speed.
+template <typename R>
+__global__ void __launch_bounds__(2 * BVP_LANES, 1) k_bvp_hybrid(KsArgs a, R *__restrict__ spec,
+                                                                 double2 *__restrict__ corr,
+                                                                 double *__restrict__ cp_scratch,
+                                                                 double *__restrict__ xs_scratch,
+                                                                 int *__restrict__ counter) {
+  extern __shared__ double bvp_sm[];
+  const BvpCtx ctx = bvp_ctx<2 * BVP_LANES>(a, bvp_sm, cp_scratch, xs_scratch);
+  __syncthreads();
+  const int nk = (int)a.nk;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool gcol = tid >= BVP_LANES;  // warp-uniform
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(counter, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    const int base = u * 16;
+    if (base >= nk) break;
+    const int i_raw = base + (lane >> 1);
+    const int i = i_raw < nk ? i_raw : nk - 1;
+    const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
+    constexpr int F = BvpRings<2>::F, B = BvpRings<2>::B;
+    if (gcol) {
+      if (a.mode != 0) bvp_mode<R, true, F, B, true>(a, spec, corr, i, store, ctx);
+      else bvp_mode<R, false, F, B, true>(a, spec, corr, i, store, ctx);
+    } else {
+      if (a.mode != 0) bvp_mode<R, true, F, B, false>(a, spec, corr, i, store, ctx);
+      else bvp_mode<R, false, F, B, false>(a, spec, corr, i, store, ctx);
+    }
+  }
+}
+
 // Batched systems: global mode g of [0, mprefix[S]) belongs to system s with
 // mprefix[s] <= g < mprefix[s+1]; every system has the same nz and H (the
 // shared-memory tables), its own factors, spectrum and corrections.
@@ -553,10 +600,28 @@ static cudaError_t bvp_plan_v(const KsArgs &a, int nsm, int64_t *grid, size_t *s
   return cudaSuccess;
 }
 
+// Scratch of the hybrid kernel: pressure coefficients of 2 BVP_LANES lanes per
+// CTA, columns of the global-memory half, the work counter.
+static size_t hybrid_cp_doubles(int nz, int64_t grid) { return (size_t)nz * grid * 2 * BVP_LANES; }
+static size_t hybrid_xs_doubles(int nz, int64_t grid) { return (size_t)(nz + 2) * grid * BVP_LANES; }
+
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  return bvp_two_per_sm(a.nz) ? bvp_plan_v<R, 2>(a, nsm, grid, scratch_bytes)
-                              : bvp_plan_v<R, 1>(a, nsm, grid, scratch_bytes);
+  if (bvp_two_per_sm(a.nz)) return bvp_plan_v<R, 2>(a, nsm, grid, scratch_bytes);
+  // one CTA of BVP_LANES per SM fits: the hybrid kernel (the plain one stays
+  // planned for the allocation-free entry point)
+  cudaError_t err = bvp_plan_v<R, 1>(a, nsm, grid, scratch_bytes);
+  if (err != cudaSuccess) return err;
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
+  err = cudaFuncSetAttribute(k_bvp_hybrid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_hybrid<R>, 2 * BVP_LANES, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const size_t hy = sizeof(double) * (hybrid_cp_doubles(a.nz, *grid) + hybrid_xs_doubles(a.nz, *grid)) + 256;
+  if (hy > *scratch_bytes) *scratch_bytes = hy;
+  return cudaSuccess;
 }
 
 // Batched solve: grid and scratch for K modes in total with a shared nz.
@@ -607,8 +672,20 @@ template cudaError_t launch_bvp_b<double>(const SysK<double> *, int, const int64
 
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool hybrid) {
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
+  if (hybrid && !bvp_two_per_sm(a.nz)) {
+    double *cp = scratch;
+    double *xs = cp + hybrid_cp_doubles(a.nz, grid);
+    int *counter = reinterpret_cast<int *>(xs + hybrid_xs_doubles(a.nz, grid));
+    cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), s);
+    if (err != cudaSuccess) return err;
+    k_bvp_hybrid<R><<<(unsigned)grid, 2 * BVP_LANES, smem, s>>>(a, spec, corr, cp, xs, counter);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);
+    return cudaGetLastError();
+  }
   const int64_t per = (a.nk + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   if (bvp_two_per_sm(a.nz)) k_bvp_pairs<R, 2><<<(unsigned)grid, BVP_LANES, smem, s>>>(a, spec, corr, scratch, per_cta);
@@ -678,7 +755,7 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
   if (err != cudaSuccess) return err;
   int64_t grid = (int64_t)(NOALLOC_SCRATCH_DOUBLES / per_cta);
   if (grid > planned_grid) grid = planned_grid;
-  return launch_bvp<R>(a, spec, corr, scratch, grid, s);
+  return launch_bvp<R>(a, spec, corr, scratch, grid, s, false);
 }
 
 size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_DOUBLES * sizeof(double); }
@@ -687,7 +764,7 @@ template cudaError_t launch_bvp_noalloc<float>(const KsArgs &, float *, double2 
 template cudaError_t launch_bvp_noalloc<double>(const KsArgs &, double *, double2 *, int64_t, cudaStream_t, bool *);
 template cudaError_t bvp_plan<float>(const KsArgs &, int, int64_t *, size_t *);
 template cudaError_t bvp_plan<double>(const KsArgs &, int, int64_t *, size_t *);
-template cudaError_t launch_bvp<float>(const KsArgs &, float *, double2 *, double *, int64_t, cudaStream_t);
-template cudaError_t launch_bvp<double>(const KsArgs &, double *, double2 *, double *, int64_t, cudaStream_t);
+template cudaError_t launch_bvp<float>(const KsArgs &, float *, double2 *, double *, int64_t, cudaStream_t, bool);
+template cudaError_t launch_bvp<double>(const KsArgs &, double *, double2 *, double *, int64_t, cudaStream_t, bool);
 
 }  // namespace dpst

@@ -65,7 +65,7 @@ template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
 template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
-                       cudaStream_t s);
+                       cudaStream_t s, bool hybrid = true);
 template <typename R>
 cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t planned_grid,
                                cudaStream_t s, bool *too_big);
