@@ -51,17 +51,17 @@ struct BvpCtx {
 };
 
 // Load the tables (identical for every wavenumber) into shared memory.
-// LANES = 2 * BVP_LANES (the hybrid kernel): threads BVP_LANES and up keep
-// their columns in xs_scratch, [nz + 2][BVP_LANES x CTAs of the grid].
-template <int LANES = BVP_LANES>
+// LANES threads per CTA, the first SL with their columns in shared memory
+// ([nz + 2][SL]); the others (the hybrid kernel) keep theirs in xs_scratch,
+// [nz + 2][(LANES - SL) x CTAs of the grid].
+template <int LANES = BVP_LANES, int SL = BVP_LANES>
 static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm, double *cp_scratch,
                                                  double *xs_scratch = nullptr) {
   const int nz = a.nz, tid = threadIdx.x;
-  constexpr int T = BVP_LANES;
   BvpCtx c;
   c.Xs = bvp_sm;
-  c.XGT = gridDim.x * T;
-  c.Xg = (LANES > T && tid >= T) ? xs_scratch + blockIdx.x * T + (tid - T) : nullptr;
+  c.XGT = gridDim.x * (LANES - SL);
+  c.Xg = (LANES > SL && tid >= SL) ? xs_scratch + blockIdx.x * (LANES - SL) + (tid - SL) : nullptr;
   const double inv_eta = 1.0 / a.eta;
   for (int t = tid; t < nz; t += LANES) {
     TAB(TB_S0, t) = a.s0[t];
@@ -89,7 +89,7 @@ static __device__ __forceinline__ BvpCtx bvp_ctx(const KsArgs &a, double *bvp_sm
 // DPTools.cpp:197-216 moves into the window's SIMat bands and the BC values
 // are scaled by eta), which saves a multiply per row.  WALLS = false (open
 // domain) skips the wall values that only the corrections use.
-template <typename R, bool WALLS, int PF_F, int PF_B, bool GCOL = false>
+template <typename R, bool WALLS, int PF_F, int PF_B, bool GCOL = false, int SL = BVP_LANES, int PF_W = 4>
 static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
                                                 int i, bool store, const BvpCtx &ctx) {
   const int nz = a.nz;
@@ -102,7 +102,7 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   double *__restrict__ CPs = ctx.CPs;
   const double *__restrict__ CPo = ctx.CPo;
   const int GT = ctx.GT;
-#define XS(j) (*(GCOL ? Xg + (j) * XGT : Xs + (j) * T + tid))
+#define XS(j) (*(GCOL ? Xg + (j) * XGT : Xs + (j) * SL + tid))
   const double sp = part ? 1.0 : -1.0;  // (i a)_part = sp * a_(other part)
   const int rs = 2 * nk;  // spectrum row stride (R elements)
   // component d, row j, part pp of the spectrum: spec[(d nz + j) rs + 2 i + pp]
@@ -235,7 +235,6 @@ static __device__ __forceinline__ void bvp_mode(const KsArgs &a, R *__restrict__
   // pairs so that the parity of the border column is static, with the
   // A^{-1}B column read PF_W pairs ahead through a register ring.
   auto window = [&](double g0, double g1, auto &&row) {
-    constexpr int PF_W = 4;
     double xm2 = 0.0, xm1 = 0.0;
     double x0 = XS(0) - __ldg(ab0) * g0, x1 = XS(1) - __ldg(ab0 + nk) * g1;
     const double ab2 = __ldg(ab0 + min(2, nz - 1) * nk), ab3 = __ldg(ab0 + min(3, nz - 1) * nk);
@@ -449,42 +448,58 @@ __global__ void __launch_bounds__(BVP_LANES, MINB) k_bvp_pairs(KsArgs a, R *__re
   }
 }
 
-// Hybrid kernel for large nz, where shared memory holds the columns of only
-// BVP_LANES lanes per SM: twice the lanes per CTA, the second half keeping
-// their penta columns in an L2-resident global scratch.  More warps per SM
-// keep more factor loads in flight (the solve's limit when one CTA of
-// BVP_LANES fits).  Warps take 16-mode units from a counter (zeroed before
-// the launch), so the two kinds of warps share the work by their own speed.
-template <typename R>
-__global__ void __launch_bounds__(2 * BVP_LANES, 1) k_bvp_hybrid(KsArgs a, R *__restrict__ spec,
-                                                                 double2 *__restrict__ corr,
-                                                                 double *__restrict__ cp_scratch,
-                                                                 double *__restrict__ xs_scratch,
-                                                                 int *__restrict__ counter) {
+// Hybrid kernel: BVP_HYB_THREADS lanes per CTA, one CTA per SM; the first SL
+// keep their penta columns in shared memory (SL = 2 BVP_LANES when those
+// fit, else BVP_LANES), the others in an L2-resident global scratch.  The
+// solve's limit is the factor loads in flight per SM, which grows with the
+// warps (24 here: 3.2 ms on c2 against 4.4 ms with the 6 warps whose
+// columns fit in shared memory), so every factor ring is one row deep and
+// the register budget (85 per thread) goes to warps.  CTA b owns the units
+// of 16 modes [b per_cta, (b+1) per_cta) and its warps take them from a
+// shared-memory counter, so shared- and global-column warps share the work by
+// their own speed.  Problems with fewer units than warps keep the plain
+// kernel (deep factor rings, every SM busy).
+constexpr int BVP_HYB_THREADS = 768;
+template <typename R, int SL>
+__global__ void __launch_bounds__(BVP_HYB_THREADS, 1) k_bvp_hybrid(KsArgs a, R *__restrict__ spec,
+                                                                   double2 *__restrict__ corr,
+                                                                   double *__restrict__ cp_scratch,
+                                                                   double *__restrict__ xs_scratch, int per_cta) {
   extern __shared__ double bvp_sm[];
-  const BvpCtx ctx = bvp_ctx<2 * BVP_LANES>(a, bvp_sm, cp_scratch, xs_scratch);
+  __shared__ int next_unit;
+  const BvpCtx ctx = bvp_ctx<BVP_HYB_THREADS, SL>(a, bvp_sm, cp_scratch, xs_scratch);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
   __syncthreads();
   const int nk = (int)a.nk;
+  const int units = (nk + 15) / 16;
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
   const int tid = threadIdx.x, lane = tid & 31;
-  const bool gcol = tid >= BVP_LANES;  // warp-uniform
+  const bool gcol = tid >= SL;  // warp-uniform
   for (;;) {
     int u = 0;
-    if (lane == 0) u = atomicAdd(counter, 1);
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
     u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
     const int base = u * 16;
-    if (base >= nk) break;
     const int i_raw = base + (lane >> 1);
     const int i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
-    constexpr int F = BvpRings<2>::F, B = BvpRings<2>::B;
     if (gcol) {
-      if (a.mode != 0) bvp_mode<R, true, F, B, true>(a, spec, corr, i, store, ctx);
-      else bvp_mode<R, false, F, B, true>(a, spec, corr, i, store, ctx);
+      if (a.mode != 0) bvp_mode<R, true, 1, 1, true, SL, 1>(a, spec, corr, i, store, ctx);
+      else bvp_mode<R, false, 1, 1, true, SL, 1>(a, spec, corr, i, store, ctx);
     } else {
-      if (a.mode != 0) bvp_mode<R, true, F, B, false>(a, spec, corr, i, store, ctx);
-      else bvp_mode<R, false, F, B, false>(a, spec, corr, i, store, ctx);
+      if (a.mode != 0) bvp_mode<R, true, 1, 1, false, SL, 1>(a, spec, corr, i, store, ctx);
+      else bvp_mode<R, false, 1, 1, false, SL, 1>(a, spec, corr, i, store, ctx);
     }
   }
+}
+
+// Shared-memory lanes of the hybrid kernel for nz: 2 BVP_LANES when their
+// columns and the tables fit in one CTA's shared memory, else BVP_LANES.
+static int hybrid_smem_lanes(int nz) {
+  const size_t tabs = sizeof(double) * (TB_DH * BVP_NZMAX + BVP_NZMAX + 1) + 64;  // + static slack
+  return sizeof(double) * (size_t)(nz + 2) * 2 * BVP_LANES + tabs <= (size_t)227 * 1024 ? 2 * BVP_LANES
+                                                                                       : BVP_LANES;
 }
 
 // Batched systems: global mode g of [0, mprefix[S]) belongs to system s with
@@ -600,26 +615,39 @@ static cudaError_t bvp_plan_v(const KsArgs &a, int nsm, int64_t *grid, size_t *s
   return cudaSuccess;
 }
 
-// Scratch of the hybrid kernel: pressure coefficients of 2 BVP_LANES lanes per
-// CTA, columns of the global-memory half, the work counter.
-static size_t hybrid_cp_doubles(int nz, int64_t grid) { return (size_t)nz * grid * 2 * BVP_LANES; }
-static size_t hybrid_xs_doubles(int nz, int64_t grid) { return (size_t)(nz + 2) * grid * BVP_LANES; }
+// Scratch of the hybrid kernel: pressure coefficients of all its lanes, the
+// global-memory columns, the work counter.
+static size_t hybrid_cp_doubles(int nz, int64_t grid) { return (size_t)nz * grid * BVP_HYB_THREADS; }
+static size_t hybrid_xs_doubles(int nz, int64_t grid) {
+  return (size_t)(nz + 2) * grid * (BVP_HYB_THREADS - hybrid_smem_lanes(nz));
+}
 
+template <typename R, int SL>
+static cudaError_t hybrid_setup(size_t smem) {
+  return cudaFuncSetAttribute(k_bvp_hybrid<R, SL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// The planned grid and scratch serve both the hybrid kernel (ordinary calls)
+// and the plain one (the allocation-free entry point).
 template <typename R>
 cudaError_t bvp_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  if (bvp_two_per_sm(a.nz)) return bvp_plan_v<R, 2>(a, nsm, grid, scratch_bytes);
-  // one CTA of BVP_LANES per SM fits: the hybrid kernel (the plain one stays
-  // planned for the allocation-free entry point)
-  cudaError_t err = bvp_plan_v<R, 1>(a, nsm, grid, scratch_bytes);
+  cudaError_t err = bvp_two_per_sm(a.nz) ? bvp_plan_v<R, 2>(a, nsm, grid, scratch_bytes)
+                                         : bvp_plan_v<R, 1>(a, nsm, grid, scratch_bytes);
   if (err != cudaSuccess) return err;
-  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
-  err = cudaFuncSetAttribute(k_bvp_hybrid<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if ((a.nk + 15) / 16 < (int64_t)nsm * (BVP_HYB_THREADS / 32)) return cudaSuccess;  // plain kernel only
+  const int sl = hybrid_smem_lanes(a.nz);
+  const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * sl);
+  err = sl == BVP_LANES ? hybrid_setup<R, BVP_LANES>(smem) : hybrid_setup<R, 2 * BVP_LANES>(smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_hybrid<R>, 2 * BVP_LANES, smem);
+  err = sl == BVP_LANES
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_hybrid<R, BVP_LANES>, BVP_HYB_THREADS, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_hybrid<R, 2 * BVP_LANES>, BVP_HYB_THREADS,
+                                                            smem);
   if (err != cudaSuccess) return err;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const size_t hy = sizeof(double) * (hybrid_cp_doubles(a.nz, *grid) + hybrid_xs_doubles(a.nz, *grid)) + 256;
+  const int64_t hgrid = std::min<int64_t>(nsm, *grid);
+  const size_t hy = sizeof(double) * (hybrid_cp_doubles(a.nz, hgrid) + hybrid_xs_doubles(a.nz, hgrid));
   if (hy > *scratch_bytes) *scratch_bytes = hy;
   return cudaSuccess;
 }
@@ -674,14 +702,23 @@ template <typename R>
 cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch, int64_t grid,
                        cudaStream_t s, bool hybrid) {
   const size_t smem = sizeof(double) * ((size_t)(a.nz + 2) * BVP_LANES);
-  if (hybrid && !bvp_two_per_sm(a.nz)) {
+  int nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // the hybrid kernel when every warp of its grid gets at least one unit
+  if (hybrid && (a.nk + 15) / 16 >= (int64_t)nsm * (BVP_HYB_THREADS / 32)) {
+    const int64_t hgrid = std::min<int64_t>(nsm, grid);
+    const int sl = hybrid_smem_lanes(a.nz);
+    const size_t hsmem = sizeof(double) * ((size_t)(a.nz + 2) * sl);
     double *cp = scratch;
-    double *xs = cp + hybrid_cp_doubles(a.nz, grid);
-    int *counter = reinterpret_cast<int *>(xs + hybrid_xs_doubles(a.nz, grid));
-    cudaError_t err = cudaMemsetAsync(counter, 0, sizeof(int), s);
-    if (err != cudaSuccess) return err;
-    k_bvp_hybrid<R><<<(unsigned)grid, 2 * BVP_LANES, smem, s>>>(a, spec, corr, cp, xs, counter);
-    err = cudaGetLastError();
+    double *xs = cp + hybrid_cp_doubles(a.nz, hgrid);
+    const int64_t units = (a.nk + 15) / 16;
+    const int per_cta = (int)((units + hgrid - 1) / hgrid);
+    if (sl == BVP_LANES)
+      k_bvp_hybrid<R, BVP_LANES><<<(unsigned)hgrid, BVP_HYB_THREADS, hsmem, s>>>(a, spec, corr, cp, xs, per_cta);
+    else
+      k_bvp_hybrid<R, 2 * BVP_LANES><<<(unsigned)hgrid, BVP_HYB_THREADS, hsmem, s>>>(a, spec, corr, cp, xs, per_cta);
+    cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
     k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);
     return cudaGetLastError();
