@@ -494,6 +494,44 @@ __global__ void __launch_bounds__(BVP_HYB_THREADS, 1) k_bvp_hybrid(KsArgs a, R *
   }
 }
 
+// Batched form of the hybrid kernel: units of 16 consecutive modes of the
+// concatenated systems (a lane finds its system by binary search).
+template <typename R, int SL>
+__global__ void __launch_bounds__(BVP_HYB_THREADS, 1) k_bvp_hybrid_b(const SysK<R> *__restrict__ sys, int S,
+                                                                     const int64_t *__restrict__ mprefix,
+                                                                     double *__restrict__ cp_scratch,
+                                                                     double *__restrict__ xs_scratch, int per_cta) {
+  extern __shared__ double bvp_sm[];
+  __shared__ int next_unit;
+  const BvpCtx ctx = bvp_ctx<BVP_HYB_THREADS, SL>(sys[0].ks, bvp_sm, cp_scratch, xs_scratch);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
+  __syncthreads();
+  const int64_t K = mprefix[S];
+  const int units = (int)((K + 15) / 16);
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const bool gcol = tid >= SL;  // warp-uniform
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
+    const int64_t g_raw = (int64_t)u * 16 + (lane >> 1);
+    const int64_t g = g_raw < K ? g_raw : K - 1;
+    const int s = find_sys(mprefix, S, g);
+    const SysK<R> &y = sys[s];
+    const int i = (int)(g - mprefix[s]);
+    const bool store = (g_raw < K) && (i != 0);
+    if (gcol) {
+      if (y.ks.mode != 0) bvp_mode<R, true, 1, 1, true, SL, 1>(y.ks, y.spec, y.corr, i, store, ctx);
+      else bvp_mode<R, false, 1, 1, true, SL, 1>(y.ks, y.spec, y.corr, i, store, ctx);
+    } else {
+      if (y.ks.mode != 0) bvp_mode<R, true, 1, 1, false, SL, 1>(y.ks, y.spec, y.corr, i, store, ctx);
+      else bvp_mode<R, false, 1, 1, false, SL, 1>(y.ks, y.spec, y.corr, i, store, ctx);
+    }
+  }
+}
+
 // Shared-memory lanes of the hybrid kernel for nz: 2 BVP_LANES when their
 // columns and the tables fit in one CTA's shared memory, else BVP_LANES.
 static int hybrid_smem_lanes(int nz) {
@@ -673,14 +711,48 @@ static cudaError_t bvp_plan_b_v(int nz, int64_t K, int nsm, int64_t *grid, size_
 
 template <typename R>
 cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
-  return bvp_two_per_sm(nz) ? bvp_plan_b_v<R, 2>(nz, K, nsm, grid, scratch_bytes)
-                            : bvp_plan_b_v<R, 1>(nz, K, nsm, grid, scratch_bytes);
+  cudaError_t err = bvp_two_per_sm(nz) ? bvp_plan_b_v<R, 2>(nz, K, nsm, grid, scratch_bytes)
+                                       : bvp_plan_b_v<R, 1>(nz, K, nsm, grid, scratch_bytes);
+  if (err != cudaSuccess) return err;
+  if ((K + 15) / 16 < (int64_t)nsm * (BVP_HYB_THREADS / 32)) return cudaSuccess;  // plain kernel only
+  const int sl = hybrid_smem_lanes(nz);
+  const size_t smem = sizeof(double) * ((size_t)(nz + 2) * sl);
+  err = sl == BVP_LANES
+            ? cudaFuncSetAttribute(k_bvp_hybrid_b<R, BVP_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+            : cudaFuncSetAttribute(k_bvp_hybrid_b<R, 2 * BVP_LANES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem);
+  if (err != cudaSuccess) return err;
+  const int64_t hgrid = std::min<int64_t>(nsm, *grid);
+  const size_t hy = sizeof(double) * (hybrid_cp_doubles(nz, hgrid) + hybrid_xs_doubles(nz, hgrid));
+  if (hy > *scratch_bytes) *scratch_bytes = hy;
+  return cudaSuccess;
 }
 
 template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)(nz + 2) * BVP_LANES);
+  int nsm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if ((K + 15) / 16 >= (int64_t)nsm * (BVP_HYB_THREADS / 32)) {
+    const int64_t hgrid = std::min<int64_t>(nsm, grid);
+    const int sl = hybrid_smem_lanes(nz);
+    const size_t hsmem = sizeof(double) * ((size_t)(nz + 2) * sl);
+    double *cp = scratch;
+    double *xs = cp + hybrid_cp_doubles(nz, hgrid);
+    const int64_t units = (K + 15) / 16;
+    const int per_cta = (int)((units + hgrid - 1) / hgrid);
+    if (sl == BVP_LANES)
+      k_bvp_hybrid_b<R, BVP_LANES><<<(unsigned)hgrid, BVP_HYB_THREADS, hsmem, s>>>(sys, S, mprefix, cp, xs, per_cta);
+    else
+      k_bvp_hybrid_b<R, 2 * BVP_LANES><<<(unsigned)hgrid, BVP_HYB_THREADS, hsmem, s>>>(sys, S, mprefix, cp, xs,
+                                                                                     per_cta);
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+    k_bvp_k0_b<R><<<S, 2 * K0_ROWS, 0, s>>>(sys);
+    return cudaGetLastError();
+  }
   const int64_t per = (K + grid - 1) / grid;
   const int per_cta = (int)((per + 15) / 16 * 16);
   if (bvp_two_per_sm(nz)) k_bvp_pairs_b<R, 2><<<(unsigned)grid, BVP_LANES, smem, s>>>(sys, S, mprefix, scratch, per_cta);
