@@ -90,7 +90,12 @@ P2 = Workload("p2_dp_n8192_192", "DP", 8192, 192.0, 192.0, 192, 192, 128, -20.5,
 # the particle kernels.
 P3 = Workload("p3_dp_n25600_320", "DP", 25600, 320.0, 320.0, 320, 320, 128, -20.5, 41.0, -16.0, 16.0,
               True, betam_hat=1.3267, betad_hat=2.2160)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3)}
+# The c2 geometry and particle density on a 384 x 384 grid: 74,112 wavenumbers
+# (enough for the solve's hybrid kernel, which c2 uses) in about 1.2 GB on the
+# device, for full ncu captures of the solve.
+P4 = Workload("p4_dp_n36864_384", "DP", 36864, 384.0, 384.0, 384, 384, 128, -20.5, 41.0, -16.0, 16.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4)}
 
 
 def fft_friendly(n):
