@@ -356,6 +356,54 @@ def run_batched(args, dev):
             "precision": "mixed", "note": "one CUDA graph launch per batched Mdot"}
 
 
+def run_multi_rhs(args, dev):
+    """Multi-RHS Mdot (dpst_mdot_multi): K columns at the same positions against
+    K single Mdots on the same handle; c0 (FP64, K = 16, the mobility-matrix
+    use) and c2 (mixed, K = 4).  Device milliseconds per column."""
+    import torch
+    from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    out = []
+    for w, precision, K in ((W.C0, "fp64", 16), (W.C2, "mixed", 4)):
+        dt = torch.float64 if precision == "fp64" else torch.float32
+        X, _, _ = W.make_inputs(w)
+        rng = np.random.default_rng(3)
+        F = torch.tensor(rng.standard_normal((K, w.N, 3)), dtype=dt, device=dev)
+        T = torch.tensor(rng.standard_normal((K, w.N, 3)), dtype=dt, device=dev) if w.has_torque else None
+        op = DPStokes(StokesParams.from_workload(w, precision), w.N, device=dev)
+        op.set_positions(torch.tensor(X, device=dev))
+        V = torch.empty_like(F)
+        Wt = torch.empty_like(F) if w.has_torque else None
+        multi = timed(lambda: op.mdot_multi(F, T, out=(V, Wt)))
+
+        def loop():
+            for k in range(K):
+                op.mdot(F[k], T[k] if T is not None else None,
+                        out=(V[k], Wt[k] if Wt is not None else None))
+
+        single = timed(loop)
+        op.close()
+        out.append({"workload": w.name, "precision": precision, "columns": K,
+                    "multi_ms_per_column": multi / K, "single_ms_per_column": single / K,
+                    "speedup": single / multi,
+                    "multi_particle_columns_per_s": w.N * K / (multi / 1e3)})
+    return out
+
+
 def cpu_baseline(w):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
@@ -384,7 +432,15 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--only-batched", action="store_true",
                     help="time only the batched configuration (256 systems)")
+    ap.add_argument("--skip-multi", action="store_true")
+    ap.add_argument("--only-multi", action="store_true",
+                    help="time only the multi-RHS Mdot (c0 K = 16, c2 K = 4)")
     args = ap.parse_args()
+    if args.only_multi:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"multi_rhs": run_multi_rhs(args, dev)}), flush=True)
+        return
     if args.only_batched:
         import torch
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -444,6 +500,9 @@ def main():
     if not args.skip_batched:
         import torch
         line["batched"] = run_batched(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
+    if not args.skip_multi:
+        import torch
+        line["multi_rhs"] = run_multi_rhs(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(r["w"])
     print(json.dumps(line), flush=True)

@@ -44,6 +44,11 @@ template <typename R>
 void launch_tile_order(int64_t N, const GridArgs &g, const Stencils<R> &st, int *count, int *start, int *perm,
                        cudaStream_t s);
 size_t tile_order_tiles(int nx, int ny);
+template <typename R>
+cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
+                         int64_t grid, cudaStream_t s);
 bool fused_supports(const KernelDesc &km, const KernelDesc &kd);
 template <typename R, typename RF>
 void launch_spread_fused(const RF *F, const RF *T, int64_t N, const KernelDesc &km, const KernelDesc &kd,
@@ -109,6 +114,7 @@ struct EngineBase {
   virtual ~EngineBase() {}
   virtual void set_positions(const void *pos, int dtype, cudaStream_t s) = 0;
   virtual void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
+  virtual void mdot_multi(int K, const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
   bool use_static_scratch = false;  // set by dpst_mdot_noalloc for one call
   virtual void info(dpst_info *o) const = 0;
   virtual void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) = 0;
@@ -299,6 +305,8 @@ struct Engine : EngineBase {
       cufftDestroy(plan_f);
       cufftDestroy(plan_b);
     }
+    if (planK_f) cufftDestroy(planK_f);
+    if (planK_b) cufftDestroy(planK_b);
   }
 
   void alloc_stencils(const KernelDesc &d, bool dip, DevBuf *b, Stencils<R> &s) {
@@ -395,26 +403,31 @@ struct Engine : EngineBase {
 
   template <typename RF>
   void spread_stage(const RF *F, const RF *T, cudaStream_t s) {
+    spread_into<RF>(F, T, grid.as<R>(), ghm, ghd, s);
+  }
+
+  // spread F (+ the torque curl) into the grid gr with the ghost layers gm, gd
+  template <typename RF>
+  void spread_into(const RF *F, const RF *T, R *gr, const Ghosts<R> &gm, const Ghosts<R> &gd, cudaStream_t s) {
     const bool torque = p.has_torque && T != nullptr;
-    R *gr = grid.as<R>();
     DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
-    for (Ghosts<R> *gh : {&ghm, &ghd}) {
-      const KernelDesc &d = (gh == &ghm) ? km.d : kd.d;
+    for (const Ghosts<R> *gh : {&gm, &gd}) {
+      const KernelDesc &d = (gh == &gm) ? km.d : kd.d;
       const size_t lev = (size_t)d.nyeff * d.nxeff * 3 * sizeof(R);
       if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
       if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
     }
     if (torque && fused) {
-      launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, ghm, ghd, s, perm.as<int>());
+      launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, gm, gd, s, perm.as<int>());
     } else {
-      launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, ghm, s, perm.as<int>());
-      if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, ghd, s, perm.as<int>());
+      launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, gm, s, perm.as<int>());
+      if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, gd, s, perm.as<int>());
     }
-    launch_ghost_fold<R>(ghm.top, ghm.ntop, nx, ny, km.d, s);
-    launch_ghost_fold<R>(ghm.bot, ghm.nbot, nx, ny, km.d, s);
+    launch_ghost_fold<R>(gm.top, gm.ntop, nx, ny, km.d, s);
+    launch_ghost_fold<R>(gm.bot, gm.nbot, nx, ny, km.d, s);
     if (torque) {
-      launch_ghost_fold<R>(ghd.top, ghd.ntop, nx, ny, kd.d, s);
-      launch_ghost_fold<R>(ghd.bot, ghd.nbot, nx, ny, kd.d, s);
+      launch_ghost_fold<R>(gd.top, gd.ntop, nx, ny, kd.d, s);
+      launch_ghost_fold<R>(gd.bot, gd.nbot, nx, ny, kd.d, s);
     }
     DPST_CUDA(cudaGetLastError());
   }
@@ -559,27 +572,157 @@ struct Engine : EngineBase {
     spread_stage<RF>(F, T, s);
     mark(1, s);
     solve_stage(s);
-    if (p.has_torque && W != nullptr) {
-      // without torques the reference's torque grid still holds the last
-      // z-derivative spread; with T = NULL it is zero
-      Ghosts<R> gz = ghd;
-      if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
-      if (fused) {
-        launch_interp_fused<R, RF>(gr, N, km.d, kd.d, g, stm, std_, ghm, gz, V, W, s, perm.as<int>());
-      } else {
-        launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
-        launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s, perm.as<int>());
-      }
-    } else {
-      launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
-    }
-    DPST_CUDA(cudaGetLastError());
+    interp_from<RF>(gr, ghm, ghd, torque, V, W, s);
     mark(7, s);
     if (stage_ms) {
       DPST_CUDA(cudaEventSynchronize(ev[7]));
       const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
       for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
     }
+  }
+
+  // interpolate V (and, with W, the angular velocities) from the grid gr with
+  // the ghost layers gm, gd
+  template <typename RF>
+  void interp_from(const R *gr, const Ghosts<R> &gm, const Ghosts<R> &gd, bool torque, RF *V, RF *W,
+                   cudaStream_t s) {
+    if (p.has_torque && W != nullptr) {
+      // without torques the reference's torque grid still holds the last
+      // z-derivative spread; with T = NULL it is zero
+      Ghosts<R> gz = gd;
+      if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
+      if (fused) {
+        launch_interp_fused<R, RF>(gr, N, km.d, kd.d, g, stm, std_, gm, gz, V, W, s, perm.as<int>());
+      } else {
+        launch_interp<R, RF>(false, gr, N, km.d, g, stm, gm, V, s, perm.as<int>());
+        launch_interp<R, RF>(true, gr, N, kd.d, g, std_, gz, W, s, perm.as<int>());
+      }
+    } else {
+      launch_interp<R, RF>(false, gr, N, km.d, g, stm, gm, V, s, perm.as<int>());
+    }
+    DPST_CUDA(cudaGetLastError());
+  }
+
+  // ---- multi-RHS Mdot (dpst_mdot_multi) -------------------------------------
+  // K force (and torque) columns at the same positions.  Per column: the spread
+  // into its slice of K-column grid and ghost-layer buffers, the z transforms,
+  // the interpolation; across columns: one cuFFT execution per direction over
+  // the K x 3 nz planes and one solve over the K nk wavenumbers (the batched
+  // solve kernels with one table entry per column, sharing the factors).
+  // Buffers are sized on the first call with a given K (a larger K replaces
+  // them).
+  int multi_k = 0;
+  DevBuf gridK, specK, corrK, corrfK, ghostK[4], sysK, mprefK, bvpK_scratch;
+  int64_t bvpK_grid = 0;
+  cufftHandle planK_f = 0, planK_b = 0;
+
+  void ensure_multi(int K) {
+    if (K <= multi_k) return;
+    if (planK_f) cufftDestroy(planK_f);
+    if (planK_b) cufftDestroy(planK_b);
+    planK_f = planK_b = 0;
+    multi_k = 0;
+    gridK.alloc(grid.bytes * K);
+    specK.alloc(spec.bytes * K);
+    if (corr.p) corrK.alloc(corr.bytes * K);
+    if (corrf.p) corrfK.alloc(corrf.bytes * K);
+    int n2[2] = {ny, nx};
+    int inem[2] = {ny, nx}, onem[2] = {ny, nxh};
+    const int batch = 3 * nz * K;
+    DPST_CUFFT(cufftPlanMany(&planK_f, 2, n2, inem, 1, ny * nx, onem, 1, (int)nk,
+                             sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, batch));
+    DPST_CUFFT(cufftPlanMany(&planK_b, 2, n2, onem, 1, (int)nk, inem, 1, ny * nx,
+                             sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, batch));
+    std::vector<SysK<R>> sk(K);
+    std::vector<int64_t> mp(K + 1, 0);
+    for (int k = 0; k < K; ++k) {
+      sk[k].ks = ks;
+      sk[k].ks.corrf = corrf.p ? corrfK.as<float2>() + (size_t)k * 16 * nk : nullptr;
+      sk[k].spec = reinterpret_cast<R *>(specK.as<CR>() + (size_t)k * 3 * nz * nk);
+      sk[k].corr = corr.p ? corrK.as<double2>() + (size_t)k * 16 * nk : nullptr;
+      mp[k + 1] = mp[k] + nk;
+    }
+    upload(sysK, sk);
+    upload(mprefK, mp);
+    size_t bytes = 0;
+    DPST_CUDA(bvp_plan_b<R>(nz, (int64_t)K * nk, nsm, &bvpK_grid, &bytes));
+    bvpK_scratch.alloc(bytes);
+    DPST_CUDA(cudaDeviceSynchronize());
+    multi_k = K;
+  }
+
+  // column k's ghost layers: slices of K-column buffers shaped like the
+  // single-column ones (their sizes follow the current positions)
+  Ghosts<R> ghosts_of(const Ghosts<R> &g1, const KernelDesc &d, DevBuf *b, int k, int K) {
+    Ghosts<R> gk = g1;
+    const size_t lev = (size_t)d.nyeff * d.nxeff * 3;
+    if (g1.top) {
+      if (b[0].bytes < sizeof(R) * lev * g1.ntop * K) b[0].alloc(sizeof(R) * lev * g1.ntop * K);
+      gk.top = b[0].as<R>() + (size_t)k * lev * g1.ntop;
+    }
+    if (g1.bot) {
+      if (b[1].bytes < sizeof(R) * lev * g1.nbot * K) b[1].alloc(sizeof(R) * lev * g1.nbot * K);
+      gk.bot = b[1].as<R>() + (size_t)k * lev * g1.nbot;
+    }
+    return gk;
+  }
+
+  template <typename RF>
+  void run_multi(int K, const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    ensure_multi(K);
+    const bool torque = p.has_torque && T != nullptr;
+    const size_t col = 3 * (size_t)N;
+    const size_t gcol = grid.bytes / sizeof(R), scol = 3 * (size_t)nz * nk;
+    R *gK = gridK.as<R>();
+    CR *sK = specK.as<CR>();
+    std::vector<Ghosts<R>> gm(K), gd(K);
+    for (int k = 0; k < K; ++k) {
+      gm[k] = ghosts_of(ghm, km.d, ghostK, k, K);
+      gd[k] = p.has_torque ? ghosts_of(ghd, kd.d, ghostK + 2, k, K) : ghd;
+      spread_into<RF>(F + k * col, torque ? T + k * col : nullptr, gK + k * gcol, gm[k], gd[k], s);
+    }
+    DPST_CUFFT(cufftSetStream(planK_f, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecD2Z(planK_f, (cufftDoubleReal *)gK, (cufftDoubleComplex *)sK));
+    else
+      DPST_CUFFT(cufftExecR2C(planK_f, (cufftReal *)gK, (cufftComplex *)sK));
+    EpiArgs ef;
+    memset(&ef, 0, sizeof(ef));
+    ef.inverse = 0;
+    ef.scale = 1.0;
+    ef.ks = ks;
+    for (int k = 0; k < K; ++k) DPST_CUDA(zgemm((R *)(sK + k * scol), Tf.as<R>(), ef, false, s));
+    DPST_CUDA(launch_bvp_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz,
+                              bvpK_scratch.as<double>(), bvpK_grid, s));
+    for (int k = 0; k < K; ++k) {
+      EpiArgs eb = ef;
+      eb.inverse = 1;
+      eb.scale = 1.0 / ((double)nx * (double)ny);
+      epi_corr(eb);
+      if (eb.corr) eb.corr = corrK.as<double2>() + (size_t)k * 16 * nk;
+      if (eb.corrf) eb.corrf = corrfK.as<float2>() + (size_t)k * 16 * nk;
+      DPST_CUDA(zgemm((R *)(sK + k * scol), Ti.as<R>(), eb, true, s));
+    }
+    DPST_CUFFT(cufftSetStream(planK_b, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecZ2D(planK_b, (cufftDoubleComplex *)sK, (cufftDoubleReal *)gK));
+    else
+      DPST_CUFFT(cufftExecC2R(planK_b, (cufftComplex *)sK, (cufftReal *)gK));
+    for (int k = 0; k < K; ++k)
+      interp_from<RF>(gK + k * gcol, gm[k], gd[k], torque, V + k * col, W ? W + k * col : nullptr, s);
+  }
+
+  void mdot_multi(int K, const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (K < 1) throw Error(DPST_ERR_INVALID_ARG, "K must be at least 1");
+    if (N == 0) return;
+    if (F == nullptr || V == nullptr) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    if (dtype == DPST_F64)
+      run_multi<double>(K, (const double *)F, (const double *)T, (double *)V, (double *)W, s);
+    else if (dtype == DPST_F32)
+      run_multi<float>(K, (const float *)F, (const float *)T, (float *)V, (float *)W, s);
+    else
+      throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
   }
 
   // ---- backward pass -------------------------------------------------------
@@ -877,6 +1020,15 @@ int dpst_mdot(dpst_handle h, const void *F, const void *T, void *V, void *W, int
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
     h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
+  });
+}
+
+int dpst_mdot_multi(dpst_handle h, int K, const void *F, const void *T, void *V, void *W, int dtype,
+                    void *stream) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    h->e->mdot_multi(K, F, T, V, W, dtype, (cudaStream_t)stream);
   });
 }
 

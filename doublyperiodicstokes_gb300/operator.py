@@ -152,6 +152,38 @@ class DPStokes:
                                     _dtype_code(F), _stream_ptr(self.device)))
         return V, W
 
+    def mdot_multi(self, F, T=None, out=None):
+        """(V, W) = M (F, T) for K columns at once: F, T of shape (K, N, 3) (or
+        (K, 3N)); the result has the same shape.  W is None when the operator
+        has no torques.  Column k equals mdot(F[k], T[k])."""
+        if F.dim() < 2:
+            raise ValueError("forces must have a leading column dimension K")
+        K = F.shape[0]
+        if F.device != self.device:
+            raise ValueError("forces must be on %s" % self.device)
+        if F.numel() != 3 * self.N * K:
+            raise ValueError("forces must hold K*3*N = %d values" % (3 * self.N * K))
+        F = F.contiguous()
+        dt = F.dtype
+        if T is not None:
+            if not self.params.has_torque:
+                raise ValueError("operator was created without torques")
+            if T.device != self.device or T.numel() != F.numel():
+                raise ValueError("torques must match the forces' shape and device")
+            if T.dtype != dt:
+                raise TypeError("forces and torques must have the same dtype")
+            T = T.contiguous()
+        V = torch.empty_like(F) if out is None else out[0]
+        W = None
+        if self.params.has_torque:
+            W = torch.empty_like(F) if out is None else out[1]
+        _lib.check(self.L.dpst_mdot_multi(self._h, K, ctypes.c_void_p(F.data_ptr()),
+                                          ctypes.c_void_p(T.data_ptr() if T is not None else 0),
+                                          ctypes.c_void_p(V.data_ptr()),
+                                          ctypes.c_void_p(W.data_ptr() if W is not None else 0),
+                                          _dtype_code(F), _stream_ptr(self.device)))
+        return V, W
+
     # ---- diagnostics -------------------------------------------------------
     STAGES = ("spread", "fft_fwd", "ztrans_fwd", "solve", "ztrans_inv", "fft_inv", "interp", "total")
 

@@ -145,6 +145,17 @@ int dpst_set_positions(dpst_handle h, const void *pos, int dtype, void *stream);
 int dpst_mdot(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
               void *stream);
 
+/* Multi-RHS Mdot: K force (and torque) columns at the current positions, as the
+ * reference's mobility-matrix and Lanczos drivers apply M (mobility_matrix.py:5-48,
+ * a loop of FCMJoint.Mdot calls there).  F, V: device [K][N][3]; T, W: device
+ * [K][N][3] or NULL.  Column k equals dpst_mdot on column k (up to the order of
+ * the spreading's atomic sums).  The K columns share the stencils and the
+ * per-wavenumber factors; the x-y FFTs and the solve run once over all K.
+ * Buffers for K columns are allocated on the first call with that K (or a
+ * larger one). */
+int dpst_mdot_multi(dpst_handle h, int K, const void *F, const void *T, void *V, void *W, int dtype,
+                    void *stream);
+
 /* Host-array variants: copy in, run, copy out, synchronise. */
 int dpst_set_positions_host(dpst_handle h, const void *pos, int dtype, void *stream);
 int dpst_mdot_host(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,
