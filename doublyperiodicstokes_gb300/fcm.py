@@ -3,15 +3,20 @@
 the CPU path's conventions (FCM.py): positions in [xmin,xmax] x [ymin,ymax] x
 [zmin,zmax], the Chebyshev interval starting at z0, BCs per domain type.
 
-The reference chooses the grid and kernel (h, beta, Nz, z0) from polynomial
-fits in GridAndKernelConfig.py; those tables are not part of this package, so
-Initialize takes the grid explicitly (nx, ny, nz, kernel widths and
-dimensionless betas, z0).  Everything else -- argument names, order, array
-formats ([3N] interleaved xyz), return values -- follows FCMJoint.
+Without an explicit grid, Initialize chooses the grid and kernels exactly as
+the reference does (gridconfig: GridAndKernelConfig.py's (h, beta, N) from the
+hydrodynamic radius, kernel type and optInd; the z extent, Nz and floor from
+the domain type), like the reference's GPU branch
+(common_interface_wrapper.py:78-101) but with the Chebyshev interval at the
+floor it returns, as the CPU path places it.  The keyword-only arguments (nx,
+ny, nz, kernel widths, dimensionless betas, z0) override that choice.
+Everything else -- argument names, order, array formats ([3N] interleaved
+xyz), return values -- follows FCMJoint.
 """
 import numpy as np
 import torch
 
+from . import gridconfig
 from .operator import DPStokes, StokesParams
 
 _MODE = {"DP": "nowall", "DPBW": "bottom", "DPSC": "slit"}
@@ -27,25 +32,41 @@ class FCMJoint:
 
     def Initialize(self, numberParticles, hydrodynamicRadius, viscosity, domType, has_torque,
                    xmax, ymax, zmin, zmax, xmin=0, ymin=0, kernType=0, optInd=0, ref=False, *,
-                   nx, ny, nz, w=6, beta_hat=None, w_d=6, beta_d_hat=2.2160, z0=None,
+                   nx=None, ny=None, nz=None, w=6, beta_hat=None, w_d=6, beta_d_hat=2.2160, z0=None,
                    precision="fp64"):
-        """Explicit-grid version of FCMJoint.Initialize.  beta_hat defaults to
-        the reference's w=6 values (1.714 without torques, 1.3267 with)."""
+        """FCMJoint.Initialize.  With nx = None the grid and kernels are the
+        reference's choice for (hydrodynamicRadius, kernType, optInd, ref);
+        otherwise nx, ny, nz, w, beta_hat (default: the reference's w = 6
+        value, 1.714 without torques, 1.3267 with), w_d, beta_d_hat and z0
+        are taken as given."""
         if domType not in _MODE:
             raise ValueError("domType must be DP, DPBW or DPSC (TP is not provided)")
         self.Clean()
         self.has_torque = bool(has_torque)
         self.N = int(numberParticles)
         self.xmin, self.ymin = xmin, ymin
-        Lx, Ly = xmax - xmin, ymax - ymin
-        self.z0 = zmin if z0 is None else z0
-        if beta_hat is None:
-            beta_hat = 1.3267 if has_torque else 1.714
-        hx = Lx / nx
+        if nx is None:
+            radP = hydrodynamicRadius * np.ones(self.N)
+            kts = kernType * np.ones(self.N, dtype=int)
+            Lx, Ly, hx, _, nx, ny, wm, wd, _, _, bm, bd = gridconfig.configure_grid_and_kernels_xy(
+                xmax - xmin, ymax - ymin, radP, kts, optInd, self.has_torque, ref)
+            Lz, _, nz, self.z0 = gridconfig.configure_grid_and_kernels_z(zmin, zmax, hx, wm, wd, domType,
+                                                                        fac=1.5, ref=ref)
+            w, beta_hat = int(wm[0]), float(bm[0])
+            if self.has_torque:
+                w_d, beta_d_hat = int(wd[0]), float(bd[0])
+        else:
+            if ny is None or nz is None:
+                raise ValueError("an explicit grid needs nx, ny and nz")
+            Lx, Ly = xmax - xmin, ymax - ymin
+            hx = Lx / nx
+            self.z0 = zmin if z0 is None else z0
+            Lz = zmax - self.z0
+            if beta_hat is None:
+                beta_hat = 1.3267 if has_torque else 1.714
         a = StokesParams.kernel_alpha(hydrodynamicRadius, w, hx)
         ad = StokesParams.kernel_alpha(hydrodynamicRadius, w_d, hx)
-        Lz = zmax - self.z0
-        self.params = StokesParams(mode=_MODE[domType], nx=nx, ny=ny, nz=nz, Lx=Lx, Ly=Ly,
+        self.params = StokesParams(mode=_MODE[domType], nx=int(nx), ny=int(ny), nz=int(nz), Lx=Lx, Ly=Ly,
                                    zmin=self.z0, zmax=self.z0 + Lz, viscosity=viscosity, w=w,
                                    beta=beta_hat * w, alpha=a, has_torque=self.has_torque, w_d=w_d,
                                    beta_d=beta_d_hat * w_d, alpha_d=ad, precision=precision)
