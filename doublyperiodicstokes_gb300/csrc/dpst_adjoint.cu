@@ -38,20 +38,38 @@ constexpr int ADJ_MODES = ADJ_LANES / 2;
 // adjoint applies Z(q)^H or Z(q')^T: the imaginary entries of Z are
 // conjugated on the main pass only.
 // CADJ_G lanes per mode split the nodes and combine their sums with
-// shuffles; the node profiles are evaluated in the operator's arithmetic CT
-// (as the forward's correction epilogue does), the sums and the slit's 8x8
-// solve in FP64.  Every lane runs both passes so that the shuffles stay
-// warp-uniform; the partner pass contributes only where the mode needs it.
+// shuffles; the node profiles and the sums are evaluated in the operator's
+// arithmetic CT (as the forward's correction epilogue does; FP32 for the
+// mixed operator, whose FP64 work runs at 1/64 of the FP32 rate here), the
+// slit's 8x8 solve in FP64.  The partner pass runs when any mode of the warp
+// needs it (a warp vote keeps the shuffles warp-uniform) and contributes only
+// where the mode needs it.
 // ---------------------------------------------------------------------------
 constexpr int CADJ_G = 8;
 
-static __device__ __forceinline__ double2 group_sum(double2 v) {
+template <typename V>
+static __device__ __forceinline__ V group_sum(V v) {
   for (int o = CADJ_G / 2; o > 0; o >>= 1) {
     v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
     v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
   }
   return v;
 }
+
+// complex helpers in the sums' type (float2 or double2)
+template <typename V, typename S>
+static __device__ __forceinline__ V vmk(S x, S y) {
+  V r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+template <typename V, typename S>
+static __device__ __forceinline__ V vadd(V a, V b) { return vmk<V, S>(a.x + b.x, a.y + b.y); }
+template <typename V, typename S>
+static __device__ __forceinline__ V vscale(S s, V a) { return vmk<V, S>(s * a.x, s * a.y); }
+template <typename V, typename S>
+static __device__ __forceinline__ V vik(S s, V a) { return vmk<V, S>(-s * a.y, s * a.x); }  // i s a
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_corr_adj(KsArgs a, const R *__restrict__ spec, double2 *__restrict__ cadj) {
@@ -69,13 +87,16 @@ __global__ void __launch_bounds__(256) k_corr_adj(KsArgs a, const R *__restrict_
   double kxp, kyp;
   const bool herm = mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp);
   const CT kc = (CT)k;
-  auto g = [&](int d, int m) -> double2 {
+  typedef typename std::conditional<sizeof(CT) == 4, float2, double2>::type V;  // sums in CT
+  auto g = [&](int d, int m) -> V {
     const R *p = spec + (((int64_t)d * nz + m) * nk + i) * 2;
-    return make_double2((double)p[0], (double)p[1]);
+    return vmk<V, CT>((CT)p[0], (CT)p[1]);
   };
+  auto d2 = [](V v) { return make_double2((double)v.x, (double)v.y); };
   double2 acc[6];
   for (int q = 0; q < 6; ++q) acc[q] = make_double2(0, 0);
-  for (int pass = 0; pass < 2; ++pass) {
+  const bool any_partner = __any_sync(0xffffffffu, !herm && i_raw < nk);
+  for (int pass = 0; pass < (any_partner ? 2 : 1); ++pass) {
     const bool use = (pass == 0) || !herm;
     const double qx = pass ? kxp : kx, qy = pass ? kyp : ky;
     const CT qxc = (CT)qx, qyc = (CT)qy;
@@ -84,53 +105,60 @@ __global__ void __launch_bounds__(256) k_corr_adj(KsArgs a, const R *__restrict_
     if (a.mode == 1) {
       // Z (DPTools.cpp:627-641) per node, symmetric 3x3:
       //   [e - qx^2 ze/k, -qx qy ze/k, -i qx ze; ., e - qy^2 ze/k, -i qy ze; ., ., e + k ze]
-      double2 s0 = make_double2(0, 0), s1 = s0, s2 = s0;
+      V s0 = vmk<V, CT>(0, 0), s1 = s0, s2 = s0;
+      const CT csc = (CT)cs;
       for (int m = sub; m < nz; m += CADJ_G) {
         const CT z = (CT)a.zn[m];
         const CT e = exp(-kc * z), ze = z * e;
-        const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
-        const double z00 = (double)(e - qxc * qxc * ze / kc), z01 = (double)(-qxc * qyc * ze / kc);
-        const double z11 = (double)(e - qyc * qyc * ze / kc), z22 = (double)(e + kc * ze);
-        const double ix_ = cs * (double)(-qxc * ze), iy_ = cs * (double)(-qyc * ze);
-        s0 = cadd(s0, cadd(cadd(cscale(z00, g0), cscale(z01, g1)), cik(ix_, g2)));
-        s1 = cadd(s1, cadd(cadd(cscale(z01, g0), cscale(z11, g1)), cik(iy_, g2)));
-        s2 = cadd(s2, cadd(cadd(cik(ix_, g0), cik(iy_, g1)), cscale(z22, g2)));
+        const V g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
+        const CT z00 = e - qxc * qxc * ze / kc, z01 = -qxc * qyc * ze / kc;
+        const CT z11 = e - qyc * qyc * ze / kc, z22 = e + kc * ze;
+        const CT ix_ = csc * (-qxc * ze), iy_ = csc * (-qyc * ze);
+        s0 = vadd<V, CT>(s0, vadd<V, CT>(vadd<V, CT>(vscale<V, CT>(z00, g0), vscale<V, CT>(z01, g1)),
+                                          vik<V, CT>(ix_, g2)));
+        s1 = vadd<V, CT>(s1, vadd<V, CT>(vadd<V, CT>(vscale<V, CT>(z01, g0), vscale<V, CT>(z11, g1)),
+                                          vik<V, CT>(iy_, g2)));
+        s2 = vadd<V, CT>(s2, vadd<V, CT>(vadd<V, CT>(vik<V, CT>(ix_, g0), vik<V, CT>(iy_, g1)),
+                                          vscale<V, CT>(z22, g2)));
       }
       s0 = group_sum(s0);
       s1 = group_sum(s1);
       s2 = group_sum(s2);
       if (use) {
-        acc[0] = cadd(acc[0], s0);
-        acc[1] = cadd(acc[1], s1);
-        acc[2] = cadd(acc[2], s2);
+        acc[0] = cadd(acc[0], d2(s0));
+        acc[1] = cadd(acc[1], d2(s1));
+        acc[2] = cadd(acc[2], d2(s2));
       }
     } else {
       // Z = P A^{-1} R (DPTools.cpp:731-815): R maps (fb, ft) to the right
       // side of the 8x8 system A, P maps its solution to node values
       const double fac = 1.0 / 2.0 / a.eta, Hs = a.Lz;
       const CT facc = (CT)fac, Hc = (CT)Hs;
-      double2 p[8];
-      for (int q = 0; q < 8; ++q) p[q] = make_double2(0, 0);
+      V pv[8];
+      for (int q = 0; q < 8; ++q) pv[q] = vmk<V, CT>(0, 0);
+      const CT csc = (CT)cs;
       for (int m = sub; m < nz; m += CADJ_G) {
         const CT z = (CT)a.zn[m];
         const CT e = exp(-kc * z), e2 = exp(kc * (z - Hc));
         const CT ze = z * e, ze2 = z * e2;
-        const double2 g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
+        const V g0 = g(0, m), g1 = g(1, m), g2 = g(2, m);
         // P rows: v0 = -i qx ze fac/k c0 + i qx ze2 fac/k c1 + e c2 + e2 c3,
         // v1 likewise with qy, c4, c5; v2 = ze fac c0 + ze2 fac c1 + e c6 + e2 c7
-        const double a0 = cs * (double)(-qxc * ze * facc / kc), a1 = cs * (double)(-qyc * ze * facc / kc);
-        const double b0 = cs * (double)(qxc * ze2 * facc / kc), b1 = cs * (double)(qyc * ze2 * facc / kc);
-        const double ed = (double)e, e2d = (double)e2;
-        p[0] = cadd(p[0], cadd(cadd(cik(a0, g0), cik(a1, g1)), cscale((double)(ze * facc), g2)));
-        p[1] = cadd(p[1], cadd(cadd(cik(b0, g0), cik(b1, g1)), cscale((double)(ze2 * facc), g2)));
-        p[2] = cadd(p[2], cscale(ed, g0));
-        p[3] = cadd(p[3], cscale(e2d, g0));
-        p[4] = cadd(p[4], cscale(ed, g1));
-        p[5] = cadd(p[5], cscale(e2d, g1));
-        p[6] = cadd(p[6], cscale(ed, g2));
-        p[7] = cadd(p[7], cscale(e2d, g2));
+        const CT a0 = csc * (-qxc * ze * facc / kc), a1 = csc * (-qyc * ze * facc / kc);
+        const CT b0 = csc * (qxc * ze2 * facc / kc), b1 = csc * (qyc * ze2 * facc / kc);
+        pv[0] = vadd<V, CT>(pv[0], vadd<V, CT>(vadd<V, CT>(vik<V, CT>(a0, g0), vik<V, CT>(a1, g1)),
+                                                vscale<V, CT>(ze * facc, g2)));
+        pv[1] = vadd<V, CT>(pv[1], vadd<V, CT>(vadd<V, CT>(vik<V, CT>(b0, g0), vik<V, CT>(b1, g1)),
+                                                vscale<V, CT>(ze2 * facc, g2)));
+        pv[2] = vadd<V, CT>(pv[2], vscale<V, CT>(e, g0));
+        pv[3] = vadd<V, CT>(pv[3], vscale<V, CT>(e2, g0));
+        pv[4] = vadd<V, CT>(pv[4], vscale<V, CT>(e, g1));
+        pv[5] = vadd<V, CT>(pv[5], vscale<V, CT>(e2, g1));
+        pv[6] = vadd<V, CT>(pv[6], vscale<V, CT>(e, g2));
+        pv[7] = vadd<V, CT>(pv[7], vscale<V, CT>(e2, g2));
       }
-      for (int q = 0; q < 8; ++q) p[q] = group_sum(p[q]);
+      double2 p[8];
+      for (int q = 0; q < 8; ++q) p[q] = d2(group_sum(pv[q]));
       if (use && sub == 0) {
         // A^{-H} (main) / A^{-T} (partner)
         double2 A[64], At[64];
