@@ -20,7 +20,8 @@ ETA_DEFAULT = 1.0 / (6.0 * math.pi)
 class Workload:
     """One Mdot configuration.
 
-    domType: 'DP' (open), 'DPBW' (bottom wall at z0), 'DPSC' (walls at z0 and z0+Lz).
+    domType: 'DP' (open), 'DPBW' (bottom wall at z0), 'DPSC' (walls at z0 and z0+Lz),
+    'TP' (triply periodic: nz uniform points on the periodic [z0, z0+Lz)).
     The Chebyshev interval is [z0, z0+Lz]; particle heights are drawn from
     [zlo, zhi].  beta = beta_hat * w for each kernel; alpha = w*h/2 (the
     reference's UseCbeta convention with c(beta) = R/(w h))."""
@@ -95,7 +96,14 @@ P3 = Workload("p3_dp_n25600_320", "DP", 25600, 320.0, 320.0, 320, 320, 128, -20.
 # device, for full ncu captures of the solve.
 P4 = Workload("p4_dp_n36864_384", "DP", 36864, 384.0, 384.0, 384, 384, 128, -20.5, 41.0, -16.0, 16.0,
               True, betam_hat=1.3267, betad_hat=2.2160)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4)}
+# Triply periodic configurations (the reference's domType 'TP'): the c0 box
+# and density on a 128 x 128 x 32 grid (reference fixture size), and the c2
+# particle count, kernels and torques in a 512 x 512 x 64 periodic box (h = 1).
+T0 = Workload("t0_tp_n2048", "TP", 2048, 128.0, 128.0, 128, 128, 32, 0.0, 32.0, 0.0, 32.0,
+              False, betam_hat=1.714)
+T1 = Workload("t1_tp_n65536", "TP", 65536, 512.0, 512.0, 512, 512, 64, 0.0, 64.0, 0.0, 64.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4, T0, T1)}
 
 
 def fft_friendly(n):
@@ -148,7 +156,16 @@ SMALL = [
     small("s_dpbw_t_odd", "DPBW", 20, 15, 22, 11.0, 0.8, 10.5, True, ny=18, Ly=18.0, seed=6),
     small("s_dpsc_f_odd", "DPSC", 20, 17, 20, 9.0, 0.3, 8.7, False, ny=14, Ly=14.0, seed=7),
 ]
-SMALL_BY_NAME = {w.name: w for w in SMALL}
+# Small triply periodic cases: torques, odd and unequal grid sizes, a z
+# spacing different from the x-y spacing (wider z stencil), odd-width kernels.
+SMALL_TP = [
+    small("s_tp_t", "TP", 24, 16, 16, 16.0, 0.0, 16.0, True, seed=8),
+    small("s_tp_f_odd", "TP", 20, 15, 13, 13.0, 0.0, 13.0, False, ny=18, Ly=18.0, seed=9),
+    small("s_tp_t_hz", "TP", 24, 16, 20, 16.0, 0.0, 16.0, True, seed=10),
+    replace(small("s_tp_t_w5", "TP", 20, 17, 15, 15.0, 0.0, 15.0, True, seed=11),
+            wm=5, wd=5, betam_hat=1.3055, betad_hat=2.2320),
+]
+SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP}
 
 
 def small_batch(domType, has_torque, seed=40):

@@ -21,7 +21,11 @@ quirks are reproduced exactly:
     (Transform.cpp:107-304);
   * per-wavenumber Schur/KBPENTA solve (DPTools.cpp:81-345,
     LinearSolvers.h:52-141), wall corrections (DPTools.cpp:590-877) and the
-    k=0 corrections (Solvers.py:482-599).
+    k=0 corrections (Solvers.py:482-599);
+  * triply periodic mode (domType 'TP'): uniform periodic z grid located like
+    x and y (ParticleList.cpp:285-366), periodic z fold / copy, unnormalised
+    3-D DFT and the Fourier-space solve (Solvers.py:197-258,
+    TPTools.cpp:6-46).
 Pinned against the reference itself (oracle/_ref, run through
 oracle/ref_harness.py) by tests/golden/make_golden.py.
 """
@@ -44,7 +48,9 @@ class Params:
     beta = beta_hat * w, SpreadInterp.h:123).  With UseCbeta
     (FCM.py:296-307) alpha = R / (2 * R / (w * hx)) = w*hx/2; the same
     floating-point formula is used (ParticleList.cpp:229).
-    z0 is the floor of the Chebyshev interval [z0, z0+Lz] (FCM.py:170)."""
+    z0 is the floor of the Chebyshev interval [z0, z0+Lz] (FCM.py:170).
+    domType 'TP' (triply periodic): Nz uniform points on the periodic
+    interval [z0, z0+Lz), hz = Lz / Nz (GridAndKernelConfig.py:380-393)."""
     domType: str
     Nx: int
     Ny: int
@@ -69,6 +75,10 @@ class Params:
     def hy(self):
         return self.Ly / self.Ny
 
+    @property
+    def hz(self):
+        return self.Lz / self.Nz if self.domType == 'TP' else 0.0
+
     def alpha(self, w):
         cw = self.radius / (w * self.hx)  # GridAndKernelConfig.py:328-329
         return self.radius / (2 * cw)  # ParticleList.cpp:229
@@ -85,6 +95,8 @@ def domain_bcs(domType):
     Returns (BCs, BCst_z) as int arrays of length 18 = 6 ends x 3 dof;
     index 4*3+d is the z end at z=Lz (extended index 0), 5*3+d the end at z=0."""
     BCs = np.full(18, BC_NONE, dtype=np.int64)
+    if domType == 'TP':  # periodic in z: the BCs are not used
+        return BCs, BCs.copy()
     if domType == 'DPBW':
         BCs[15:18] = BC_MIRROR_INV
     elif domType == 'DPSC':
@@ -212,6 +224,23 @@ class GridState:
             j += 1
         self.zext, self.wext = zext, wext
         self.ext_grid = np.zeros((self.Nzeff, self.Nyeff, self.Nxeff, 3))
+        self.periodic_z = False
+
+
+class GridStateTP:
+    """A reference Grid with uniform periodic z (hz > 0, Grid.cpp:26-29):
+    the extended sizes of ParticleList::locateOnGridUnifZ
+    (ParticleList.cpp:307-309), N + w + (w mod 2) on every axis."""
+
+    def __init__(self, p, wmax, wzmax):
+        self.p = p
+        self.Nx, self.Ny, self.Nz = p.Nx, p.Ny, p.Nz
+        self.Nxeff = p.Nx + wmax + (wmax % 2)
+        self.Nyeff = p.Ny + wmax + (wmax % 2)
+        self.Nzeff = p.Nz + wzmax + (wzmax % 2)
+        self.ext = (self.Nzeff - self.Nz) // 2
+        self.ext_grid = np.zeros((self.Nzeff, self.Nyeff, self.Nxeff, 3))
+        self.periodic_z = True
 
 
 @dataclass
@@ -276,6 +305,43 @@ def locate(p, g, kern, X):
     zun = np.where(valid, zun, 0.0)
     ptw = np.where(valid, hx * hy * g.wext[idxc], 0.0)
     return Located(xclose, yclose, xun, yun, indl, wz, zun, ptw)
+
+
+def locate_tp(p, g, kern, X):
+    """Stencil of every particle on the uniform periodic z grid
+    (ParticleList.cpp:285-366): the z window is built like the x and y
+    windows, round(2 thr / hz) points from the nearest node, its first entry
+    at extended index zclose - wz/2 + evenz + (Nzeff - Nz)/2 (the zoffset of
+    :357); interpolation weight hx*hy*hz (SpreadInterp.cpp:168).  X is [N,3]
+    already shifted by (0, 0, z0)."""
+    hx, hy, hz = p.hx, p.hy, p.hz
+    thr = kern.thr
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    if (x < 0).any() or (x > p.Lx).any() or (y < 0).any() or (y > p.Ly).any() \
+            or (z < 0).any() or (z > p.Lz).any():
+        raise ValueError('Particles are outside of the unit cell.')
+    wx, wy, wz = cround(2 * thr / hx), cround(2 * thr / hy), cround(2 * thr / hz)
+    evenx, eveny, evenz = 1 - wx % 2, 1 - wy % 2, 1 - wz % 2
+    xclose = (x / hx).astype(np.int64)
+    yclose = (y / hy).astype(np.int64)
+    zclose = (z / hz).astype(np.int64)
+    xclose += ((wx % 2) & ((x / hx - xclose) > 0.5)).astype(np.int64)
+    yclose += ((wy % 2) & ((y / hy - yclose) > 0.5)).astype(np.int64)
+    zclose += ((wz % 2) & ((z / hz - zclose) > 0.5)).astype(np.int64)
+
+    def offsets(close, w, even, h, c):
+        j = np.arange(w)
+        o = ((close[:, None].astype(np.float64) + j[None, :]) - (w // 2) + even) * h - c[:, None]
+        return np.where((o > thr) | (o < -thr), thr, o)
+
+    xun = offsets(xclose, wx, evenx, hx, x)
+    yun = offsets(yclose, wy, eveny, hy, y)
+    zun = offsets(zclose, wz, evenz, hz, z)
+    n = X.shape[0]
+    indl = zclose - wz // 2 + evenz + (g.Nzeff - g.Nz) // 2
+    wzs = np.full(n, wz, dtype=np.int64)
+    ptw = np.full((n, wz), hx * hy * hz)
+    return Located(xclose, yclose, xun, yun, indl, wzs, zun, ptw)
 
 
 def kernel_weights(kern, loc, deriv=None):
@@ -373,6 +439,11 @@ def fold(g, BCs):
     e[:, :, rbeg - Nx:g.Nxeff - Nx, :] += e[:, :, rbeg:g.Nxeff, :]
     e[:, Ny:Ny + bend, :, :] += e[:, 0:bend, :, :]
     e[:, tbeg - Ny:g.Nyeff - Ny, :, :] += e[:, tbeg:g.Nyeff, :, :]
+    if g.periodic_z:  # BoundaryConditions.h:241-283
+        e[Nz:Nz + dend] += e[0:dend]
+        e[ubeg - Nz:g.Nzeff - Nz] += e[ubeg:g.Nzeff]
+        inner = e[dend:ubeg, bend:tbeg, lend:rbeg, :]
+        return np.ascontiguousarray(inner.transpose(1, 2, 0, 3))
     for d in range(3):
         bc = BCs[12 + d]
         if bc != BC_NONE:
@@ -410,6 +481,10 @@ def ghost_copy(g, fG, BCs):
     e[zs, bend:tbeg, rbeg:g.Nxeff, :] = e[zs, bend:tbeg, rbeg - Nx:g.Nxeff - Nx, :]
     e[zs, tbeg:g.Nyeff, :, :] = e[zs, tbeg - Ny:g.Nyeff - Ny, :, :]
     e[zs, 0:bend, :, :] = e[zs, Ny:Ny + bend, :, :]
+    if g.periodic_z:  # BoundaryConditions.h:608-647
+        e[ubeg:g.Nzeff] = e[ubeg - Nz:g.Nzeff - Nz]
+        e[0:dend] = e[Nz:Nz + dend]
+        return
     for d in range(3):
         bc = BCs[12 + d]
         if bc != BC_NONE:
@@ -757,6 +832,44 @@ class DPSolver:
 
 
 # --------------------------------------------------------------------------
+# Triply periodic solver (Solvers.py:197-258, TPTools.cpp:6-46)
+# --------------------------------------------------------------------------
+def tp_wavenumbers(n, L):
+    """2 pi [0, 1, ..., floor(n/2), -ceil(n/2)+1, ..., -1] / L (Solvers.py:202-209)."""
+    return 2 * np.pi * np.concatenate((np.arange(0, np.floor(n / 2) + 1),
+                                       np.arange(-1 * np.ceil(n / 2) + 1, 0))) / L
+
+
+def tp_solve(fhat, Lx, Ly, Lz, eta):
+    """fhat [Ny,Nx,Nz,3] (unnormalised 3-D DFT) -> velocity coefficients:
+    p = -(Dx f + Dy g + Dz h) / |k|^2, u = (f - Dx p) / (eta |k|^2) per mode,
+    D = i k with the unpaired (Nyquist) plane of an even axis zeroed in D but
+    not in |k|^2, and the k = 0 mode left at zero."""
+    Ny, Nx, Nz, _ = fhat.shape
+    Ky, Kx, Kz = np.meshgrid(tp_wavenumbers(Ny, Ly), tp_wavenumbers(Nx, Lx),
+                             tp_wavenumbers(Nz, Lz), indexing='ij')
+    Ksq = Kx ** 2 + Ky ** 2 + Kz ** 2
+    Dx, Dy, Dz = 1j * Kx, 1j * Ky, 1j * Kz
+    if Nx % 2 == 0:
+        Dx[:, Nx // 2, :] = 0
+    if Ny % 2 == 0:
+        Dy[Ny // 2, :, :] = 0
+    if Nz % 2 == 0:
+        Dz[:, :, Nz // 2] = 0
+    Ksq0 = Ksq.copy()
+    Ksq0[0, 0, 0] = 1.0
+    f, g, h = fhat[..., 0], fhat[..., 1], fhat[..., 2]
+    ph = -(Dx * f + Dy * g + Dz * h) / Ksq0
+    val = 1.0 / (eta * Ksq0)
+    U = np.empty_like(fhat)
+    U[..., 0] = val * (f - Dx * ph)
+    U[..., 1] = val * (g - Dy * ph)
+    U[..., 2] = val * (h - Dz * ph)
+    U[0, 0, 0] = 0
+    return U
+
+
+# --------------------------------------------------------------------------
 # The operator
 # --------------------------------------------------------------------------
 class Oracle:
@@ -766,21 +879,35 @@ class Oracle:
     def __init__(self, p: Params):
         self.p = p
         self.BCs, self.BCst = domain_bcs(p.domType)
-        self.zpts, self.zwts = clencurt(p.Nz, 0, p.Lz)
+        self.tp = p.domType == 'TP'
         self.km = Kernel(p.wm, p.betam_hat, p.alpha(p.wm), dipole=False)
         self.kd = Kernel(p.wd, p.betad_hat, p.alpha(p.wd), dipole=True) if p.has_torque else None
-        self.solver = DPSolver(p.Nx, p.Ny, p.Nz, p.Lx, p.Ly, p.Lz / 2, p.eta)
+        if self.tp:
+            self.zpts = self.zwts = None
+            self.solver = None
+        else:
+            self.zpts, self.zwts = clencurt(p.Nz, 0, p.Lz)
+            self.solver = DPSolver(p.Nx, p.Ny, p.Nz, p.Lx, p.Ly, p.Lz / 2, p.eta)
+
+    def _grid(self, kern):
+        p = self.p
+        if self.tp:
+            return GridStateTP(p, cround(2 * kern.thr / p.hx), cround(2 * kern.thr / p.hz))
+        return GridState(p, self.zpts, self.zwts, kern.thr, cround(2 * kern.thr / p.hx))
+
+    def _locate(self, g, kern, X):
+        return (locate_tp if self.tp else locate)(self.p, g, kern, X)
 
     def set_positions(self, X):
         p = self.p
         X = np.array(X, dtype=np.float64).reshape(-1, 3).copy()
         X[:, 2] -= p.z0
         self.X = X
-        self.g = GridState(p, self.zpts, self.zwts, self.km.thr, cround(2 * self.km.thr / p.hx))
-        self.loc = locate(p, self.g, self.km, X)
+        self.g = self._grid(self.km)
+        self.loc = self._locate(self.g, self.km, X)
         if p.has_torque:
-            self.tg = GridState(p, self.zpts, self.zwts, self.kd.thr, cround(2 * self.kd.thr / p.hx))
-            self.tloc = locate(p, self.tg, self.kd, X)
+            self.tg = self._grid(self.kd)
+            self.tloc = self._locate(self.tg, self.kd, X)
 
     def spread_all(self, F, T=None):
         """Spread grid incl. the torque curl (FCM.py:353-371)."""
@@ -806,6 +933,8 @@ class Oracle:
     def solve(self, fhat):
         """Solvers.py:99-131 for DP / DPBW / DPSC; fhat [Ny,Nx,Nz,3]."""
         p, s = self.p, self.solver
+        if self.tp:
+            return tp_solve(fhat, p.Lx, p.Ly, p.Lz, p.eta)
         fk = fhat.reshape(p.Nx * p.Ny, p.Nz, 3)
         U = s.solve_no_wall(fk)
         if p.domType == 'DPBW':
@@ -819,9 +948,14 @@ class Oracle:
     def mdot(self, F, T=None, stages=None):
         p = self.p
         fG = self.spread_all(F, T)
-        fhat = fc_forward(fG)
-        U = self.solve(fhat)
-        uG = fc_backward(U)
+        if self.tp:  # Transform type fourier (Transform.cpp:109-117, 273-281)
+            fhat = np.fft.fftn(fG, axes=(0, 1, 2))
+            U = self.solve(fhat)
+            uG = np.ascontiguousarray(np.fft.ifftn(U, axes=(0, 1, 2)).real)
+        else:
+            fhat = fc_forward(fG)
+            U = self.solve(fhat)
+            uG = fc_backward(U)
         if stages is not None:
             stages.update(spread_grid=fG, f_hat=fhat, u_hat=U, u_grid=uG)
         ghost_copy(self.g, uG, self.BCs)

@@ -75,7 +75,9 @@ def _child_main(cfg_path, in_path, out_path):
         return (Lx, Ly, hx, hy, Nx, Ny, wm, wd, cbm, cbd, betam, betad)
 
     def cfg_z(*args, **kw):
-        return (Lz, 0.0, Nz, z0)
+        # the triply periodic grid is uniform in z with hz = Lz / Nz
+        # (GridAndKernelConfig.py:380-393); the Chebyshev domains have hz = 0
+        return (Lz, Lz / Nz if cfg["domType"] == "TP" else 0.0, Nz, z0)
 
     fcm_mod.configure_grid_and_kernels_xy = cfg_xy
     fcm_mod.configure_grid_and_kernels_z = cfg_z
@@ -125,7 +127,7 @@ def _child_main(cfg_path, in_path, out_path):
 def run_reference(cfg, X, F, T=None, stages=False, repeat=1, threads=4, timeout=3600):
     """Run the reference Mdot in a child process.
 
-    cfg keys: domType ('DP'|'DPBW'|'DPSC'), Nx, Ny, Nz, Lx, Ly, Lz, z0, eta,
+    cfg keys: domType ('DP'|'DPBW'|'DPSC'|'TP'), Nx, Ny, Nz, Lx, Ly, Lz, z0, eta,
     wm, betam_hat, has_torque, wd, betad_hat, radius.  Returns a dict of numpy
     arrays (V, W and, with stages=True, the intermediate grids)."""
     if not reference_available():

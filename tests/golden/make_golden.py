@@ -56,12 +56,12 @@ def make(w, threads=8):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--full", action="store_true", help="also the full-size c0, c3, c1 cases")
+    ap.add_argument("--full", action="store_true", help="also the full-size c0, c3, c1, t0 cases")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
-    todo = list(W.SMALL)
+    todo = list(W.SMALL) + list(W.SMALL_TP)
     if a.full:
-        todo += [W.C0, W.C3, W.C1]
+        todo += [W.C0, W.C3, W.C1, W.T0]
     for w in todo:
         if a.only and w.name != a.only:
             continue

@@ -25,13 +25,13 @@ def test_oracle_matches_reference_small(name):
     _check(name, 1e-13)
 
 
-@pytest.mark.parametrize("name", [n for n in FULL if n.startswith("c0")])
-def test_oracle_matches_reference_c0(name):
+@pytest.mark.parametrize("name", [n for n in FULL if n.startswith(("c0", "t0"))])
+def test_oracle_matches_reference_c0_t0(name):
     _check(name, 1e-13)
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("name", [n for n in FULL if not n.startswith("c0")])
+@pytest.mark.parametrize("name", [n for n in FULL if not n.startswith(("c0", "t0"))])
 def test_oracle_matches_reference_full(name):
     _check(name, 1e-13)
 
@@ -67,3 +67,19 @@ def test_oracle_linearity_and_translation():
     V3, W3 = o2.mdot(F, T)
     assert rel_err(V3, V1) < 1e-12
     assert rel_err(W3, W1) < 1e-12
+
+
+def test_oracle_tp_shift_invariance():
+    """Triply periodic: shifting every particle by whole cells along any axis
+    (wrapping into the box) leaves Mdot unchanged up to rounding."""
+    from doublyperiodicstokes_gb300 import workloads as W
+    w = W.SMALL_BY_NAME["s_tp_t_hz"]
+    X, F, T = W.make_inputs(w)
+    p = O.Params(**w.oracle_params())
+    V1, W1 = O.mdot(p, X, F, T)
+    Xs = X.copy()
+    Xs[:, 0] = np.mod(Xs[:, 0] + 2 * p.hx, p.Lx)
+    Xs[:, 2] = np.mod(Xs[:, 2] + 7 * p.hz, p.Lz)
+    V2, W2 = O.mdot(p, Xs, F, T)
+    assert rel_err(V2, V1) < 1e-12
+    assert rel_err(W2, W1) < 1e-12
