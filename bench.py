@@ -107,6 +107,9 @@ def algorithmic_bytes(stage, w, prec):
     nk = w.ny * nxh
     grid = 3 * w.nx * w.ny * w.nz * s
     spec = 3 * nk * w.nz * 2 * s
+    if stage == "solve" and w.domType == "TP":
+        # triply periodic: the spectrum in and out (wavenumber tables are cached)
+        return 2 * spec
     if stage == "solve":
         # spectrum in and out, per-wavenumber factors (6 nz + 4 FP64 values)
         return 2 * spec + nk * (6 * w.nz + 4) * 8
@@ -417,6 +420,60 @@ def run_multi_rhs(args, dev):
     return out
 
 
+def run_periodic(args, dev):
+    """Triply periodic Mdot on t1_tp_n65536 (512 x 512 x 64, N = 65,536,
+    torques): mixed and FP64 operators, device milliseconds per Mdot, the
+    CUDA-event stage split with each stage's HBM fraction, mixed vs FP64."""
+    import torch
+    from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W
+    w = W.T1
+    X, F, T = W.make_inputs(w)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+    peaks, _ = load_peaks()
+    out = {"workload": w.name, "grid": [w.nx, w.ny, w.nz], "N": w.N}
+    res = {}
+    for precision in ("mixed", "fp64"):
+        dt = torch.float32 if precision == "mixed" else torch.float64
+        op = DPStokes(StokesParams.from_workload(w, precision), w.N, device=dev)
+        op.set_positions(torch.tensor(X, device=dev))
+        Fd = torch.tensor(F, dtype=dt, device=dev)
+        Td = torch.tensor(T, dtype=dt, device=dev)
+        V = torch.empty_like(Fd)
+        Wd = torch.empty_like(Fd)
+        for _ in range(max(3, args.warmup)):
+            op.mdot(Fd, Td, out=(V, Wd))
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            op.mdot(Fd, Td, out=(V, Wd))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        runs = [op.mdot_timed(Fd, Td)[2] for _ in range(reps)]
+        st = {k: statistics.median([r[k] for r in runs]) for k in runs[0]}
+        st = {k: v for k, v in st.items() if not k.startswith("ztrans")}
+        roof = {}
+        for k, v in st.items():
+            b = algorithmic_bytes(k, w, precision)
+            if b and v > 0:
+                gbs = b / (v * 1e-3) / 1e9
+                roof[k] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
+        res[precision] = (V.double().clone(), Wd.double().clone())
+        out[precision] = {"ms_per_mdot": ms, "particles_per_s": w.N / (ms / 1e3),
+                          "stages_ms": {k: round(v, 4) for k, v in st.items()}, "stage_hbm": roof,
+                          "kernels_per_mdot": op.info()["kernels_per_mdot"]}
+        op.close()
+    rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
+    out["rel_err_V_mixed_vs_fp64"] = rel(res["mixed"][0], res["fp64"][0])
+    out["rel_err_W_mixed_vs_fp64"] = rel(res["mixed"][1], res["fp64"][1])
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_mdot"] / out["mixed"]["ms_per_mdot"]
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(w)
+    return out
+
+
 def cpu_baseline(w):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
@@ -445,10 +502,18 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--only-batched", action="store_true",
                     help="time only the batched configuration (256 systems)")
+    ap.add_argument("--skip-periodic", action="store_true")
+    ap.add_argument("--only-periodic", action="store_true",
+                    help="time only the triply periodic Mdot (t1_tp_n65536)")
     ap.add_argument("--skip-multi", action="store_true")
     ap.add_argument("--only-multi", action="store_true",
                     help="time only the multi-RHS Mdot (c0 K = 16, c2 K = 4)")
     args = ap.parse_args()
+    if args.only_periodic:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"periodic": run_periodic(args, dev)}), flush=True)
+        return
     if args.only_multi:
         import torch
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -516,6 +581,9 @@ def main():
     if not args.skip_multi:
         import torch
         line["multi_rhs"] = run_multi_rhs(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
+    if not args.skip_periodic:
+        import torch
+        line["periodic"] = run_periodic(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(r["w"])
     print(json.dumps(line), flush=True)

@@ -11,7 +11,7 @@ from . import build as _build
 DPST_OK = 0
 ERRORS = {1: "invalid argument", 2: "not ready", 3: "out of domain", 4: "CUDA error",
           5: "unsupported", 6: "allocation failed"}
-MODE = {"nowall": 0, "bottom": 1, "slit": 2}
+MODE = {"nowall": 0, "bottom": 1, "slit": 2, "periodic": 3}
 PREC = {"fp64": 0, "mixed": 1}
 F64, F32 = 0, 1
 

@@ -29,40 +29,16 @@
 #include "../../include/dpstokes_gb300.h"
 #include "dpst_host.cuh"
 #include "dpst_internal.cuh"
+#include "dpst_launch.cuh"
 
 namespace dpst {
 
 // ---- declarations of the kernel launchers (dpst_particles.cu, dpst_kspace.cu)
 template <typename R>
-void launch_locate(bool dipole, const double *pos, int64_t N, const KernelDesc &kd, const double *zext,
-                   const double *wext, const GridArgs &g, const Stencils<R> &st, int *err, int *reach,
-                   cudaStream_t s);
-template <typename R, typename RF>
-void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, R *grid, const Ghosts<R> &gh, cudaStream_t s, const int *perm = nullptr);
-template <typename R>
-void launch_tile_order(int64_t N, const GridArgs &g, const Stencils<R> &st, int *count, int *start, int *perm,
-                       cudaStream_t s);
-size_t tile_order_tiles(int nx, int ny);
-template <typename R>
 cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
 template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s);
-bool fused_supports(const KernelDesc &km, const KernelDesc &kd);
-template <typename R, typename RF>
-void launch_spread_fused(const RF *F, const RF *T, int64_t N, const KernelDesc &km, const KernelDesc &kd,
-                         const GridArgs &g, const Stencils<R> &sm, const Stencils<R> &sd, R *grid,
-                         const Ghosts<R> &ghm, const Ghosts<R> &ghd, cudaStream_t s, const int *perm);
-template <typename R, typename RV>
-void launch_interp_fused(const R *grid, int64_t N, const KernelDesc &km, const KernelDesc &kd, const GridArgs &g,
-                         const Stencils<R> &sm, const Stencils<R> &sd, const Ghosts<R> &ghm,
-                         const Ghosts<R> &ghd, RV *V, RV *W, cudaStream_t s, const int *perm);
-template <typename R>
-void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd, cudaStream_t s);
-template <typename R, typename RV>
-void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, const GridArgs &g,
-                   const Stencils<R> &st, const Ghosts<R> &gh, RV *out, cudaStream_t s, const int *perm = nullptr);
 
 
 void launch_bvp_factors(const KsArgs &a, cudaStream_t s);
@@ -110,22 +86,6 @@ void launch_gather_dip(const R *u, const R *psi, int64_t N, const KernelDesc &kd
 thread_local std::string g_last_error;
 
 // ---- the engine -----------------------------------------------------------------
-struct EngineBase {
-  virtual ~EngineBase() {}
-  virtual void set_positions(const void *pos, int dtype, cudaStream_t s) = 0;
-  virtual void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
-  virtual void mdot_multi(int K, const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) = 0;
-  bool use_static_scratch = false;  // set by dpst_mdot_noalloc for one call
-  virtual void info(dpst_info *o) const = 0;
-  virtual void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) = 0;
-  virtual void velocity_grid(void *out, cudaStream_t s) = 0;
-  virtual void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT,
-                        void *gX, int dtype, cudaStream_t s) = 0;
-  float *stage_ms = nullptr;  // set by dpst_mdot_timed for one call
-  int device = 0;
-  int64_t N = 0;
-  dpst_params p;
-};
 
 template <typename R>
 struct Engine : EngineBase {
@@ -957,14 +917,19 @@ __global__ void k_prep_pos(const RP *pos, int64_t N, double zmin, double *out) {
   out[3 * p + 2] = (double)pos[3 * p + 2] - zmin;
 }
 
-template <typename R>
-void Engine<R>::convert_positions(const void *pos, int dtype, cudaStream_t s) {
+void launch_prep_positions(const void *pos, int dtype, int64_t N, double zmin, double *out, cudaStream_t s) {
   int bs = 256;
   int64_t nb = (N + bs - 1) / bs;
-  if (dtype == DPST_F64) k_prep_pos<double><<<nb, bs, 0, s>>>((const double *)pos, N, p.zmin, pos64.as<double>());
-  else if (dtype == DPST_F32) k_prep_pos<float><<<nb, bs, 0, s>>>((const float *)pos, N, p.zmin, pos64.as<double>());
+  if (N == 0) return;
+  if (dtype == DPST_F64) k_prep_pos<double><<<nb, bs, 0, s>>>((const double *)pos, N, zmin, out);
+  else if (dtype == DPST_F32) k_prep_pos<float><<<nb, bs, 0, s>>>((const float *)pos, N, zmin, out);
   else throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
   DPST_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+void Engine<R>::convert_positions(const void *pos, int dtype, cudaStream_t s) {
+  launch_prep_positions(pos, dtype, N, p.zmin, pos64.as<double>(), s);
 }
 
 
@@ -995,9 +960,10 @@ int dpst_create(const dpst_params *p, int64_t n_particles, int device, dpst_hand
   return guarded([&] {
     if (!out) throw Error(DPST_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    dpst::validate(p, n_particles);
+    dpst::validate(p, n_particles, true);
     std::unique_ptr<dpst_engine> h(new dpst_engine());
-    if (p->precision == DPST_PREC_FP64) h->e.reset(new dpst::Engine<double>(*p, n_particles, device));
+    if (p->mode == DPST_MODE_PERIODIC) h->e.reset(dpst::make_engine_tp(*p, n_particles, device));
+    else if (p->precision == DPST_PREC_FP64) h->e.reset(new dpst::Engine<double>(*p, n_particles, device));
     else h->e.reset(new dpst::Engine<float>(*p, n_particles, device));
     *out = h.release();
   });

@@ -183,6 +183,44 @@ static KernelHost make_kernel(int w, double beta, double alpha, bool dipole, dou
   return k;
 }
 
+// Kernel on a uniform periodic z grid (triply periodic mode): widths
+// round(2 thr / h) on every axis and extended sizes n + w + (w mod 2)
+// (ParticleList.cpp:285-310).  No extended z tables.
+static KernelHost make_kernel_tp(int w, double beta, double alpha, bool dipole, double hx, double hy, double hz,
+                                 int nx, int ny, int nz, const char *what) {
+  KernelHost k;
+  KernelDesc &d = k.d;
+  memset(&d, 0, sizeof(d));
+  if (!(alpha > 0) || !(beta > 0) || w < 1)
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": w, beta and alpha must be positive");
+  d.beta = beta;
+  d.alpha = alpha;
+  d.alpha2 = alpha * alpha;
+  d.norm = es_norm(beta, alpha);
+  d.inv_norm3 = 1.0 / (d.norm * d.norm * d.norm);
+  d.thr = dipole ? dipole_threshold(beta, alpha) : alpha;
+  if (!(d.thr > 0) || !(d.thr <= alpha))
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": kernel threshold is not in (0, alpha]");
+  d.wx = cround(2 * d.thr / hx);
+  d.wy = cround(2 * d.thr / hy);
+  const int wz = cround(2 * d.thr / hz);
+  if (d.wx < 1 || d.wy < 1 || wz < 1 || d.wx > nx || d.wy > ny || wz > nz)
+    throw Error(DPST_ERR_INVALID_ARG, std::string(what) + ": kernel support does not fit the grid");
+  d.evenx = 1 - (d.wx % 2);
+  d.eveny = 1 - (d.wy % 2);
+  d.evenz = 1 - (wz % 2);
+  d.nxeff = nx + d.wx + (d.wx % 2);
+  d.nyeff = ny + d.wy + (d.wy % 2);
+  d.nzeff = nz + wz + (wz % 2);
+  d.lend = (d.nxeff - nx) / 2;
+  d.bend = (d.nyeff - ny) / 2;
+  d.dend = (d.nzeff - nz) / 2;
+  d.wz_max = wz;
+  d.unif_z = 1;
+  d.hz = hz;
+  return k;
+}
+
 // DCT-I matrices (Transform.cpp:107-304): tf[j][m] gives Chebyshev
 // coefficient j from node values m, ti[m][j] node value m from coefficient j.
 static void dct_matrices(int nz, std::vector<double> &tf, std::vector<double> &ti) {
@@ -283,11 +321,14 @@ static ZTables make_ztables(int nz, double H, int mode) {
 }
 
 // Boundary-condition sets of a geometry (FCM.py:215-248): set A for forces
-// and the x/y torque derivatives, set B for the z torque derivative.
+// and the x/y torque derivatives, set B for the z torque derivative.  The
+// triply periodic mode wraps z instead (its BCs are all 'none' and unused).
 static void bc_sets(int mode, GridArgs &g) {
   memset(&g.bcA, 0, sizeof(g.bcA));
   memset(&g.bcB, 0, sizeof(g.bcB));
-  if (mode == DPST_MODE_BOTTOM) {
+  if (mode == DPST_MODE_PERIODIC) {
+    g.bcA.periodic = g.bcB.periodic = 1;
+  } else if (mode == DPST_MODE_BOTTOM) {
     g.bcA.bot_active = 1; g.bcA.s_bot = -1.0;
     g.bcB.bot_active = 1; g.bcB.s_bot = 1.0;
   } else if (mode == DPST_MODE_SLIT) {
@@ -307,15 +348,25 @@ static std::vector<double> wavenumbers(int n, double L) {
 }
 
 // Parameter checks of dpst_create (shared by the batched engine).
-static void validate(const dpst_params *p, int64_t n) {
+// periodic: whether the caller runs the triply periodic mode.
+static void validate(const dpst_params *p, int64_t n, bool periodic_ok = false) {
   if (!p) throw Error(DPST_ERR_INVALID_ARG, "params is NULL");
   if (n < 0) throw Error(DPST_ERR_INVALID_ARG, "n_particles < 0");
-  if (p->mode < 0 || p->mode > 2) throw Error(DPST_ERR_INVALID_ARG, "mode must be NOWALL, BOTTOM or SLIT");
+  if (p->mode == DPST_MODE_PERIODIC && !periodic_ok)
+    throw Error(DPST_ERR_UNSUPPORTED, "mode PERIODIC is available through dpst_create only");
+  if (p->mode < 0 || p->mode > 3)
+    throw Error(DPST_ERR_INVALID_ARG, "mode must be NOWALL, BOTTOM, SLIT or PERIODIC");
   if (p->nx < 4 || p->ny < 4) throw Error(DPST_ERR_INVALID_ARG, "nx and ny must be >= 4");
-  if (p->nz < 5) throw Error(DPST_ERR_INVALID_ARG, "nz must be >= 5");
-  if (p->nz > 128) throw Error(DPST_ERR_UNSUPPORTED, "nz > 128 is not supported yet");
-  if ((int64_t)p->ny * (p->nx / 2 + 1) * 3 * p->nz > INT_MAX)
-    throw Error(DPST_ERR_UNSUPPORTED, "grid too large for one FFT plan");
+  if (p->mode == DPST_MODE_PERIODIC) {
+    if (p->nz < 4) throw Error(DPST_ERR_INVALID_ARG, "nz must be >= 4");
+    if ((int64_t)p->nz * p->ny * p->nx > INT_MAX || (int64_t)p->nz * p->ny * (p->nx / 2 + 1) * 3 > INT_MAX)
+      throw Error(DPST_ERR_UNSUPPORTED, "grid too large for one FFT plan");
+  } else {
+    if (p->nz < 5) throw Error(DPST_ERR_INVALID_ARG, "nz must be >= 5");
+    if (p->nz > 128) throw Error(DPST_ERR_UNSUPPORTED, "nz > 128 is not supported yet");
+    if ((int64_t)p->ny * (p->nx / 2 + 1) * 3 * p->nz > INT_MAX)
+      throw Error(DPST_ERR_UNSUPPORTED, "grid too large for one FFT plan");
+  }
   if (!(p->Lx > 0) || !(p->Ly > 0)) throw Error(DPST_ERR_INVALID_ARG, "Lx and Ly must be positive");
   if (!(p->zmax > p->zmin)) throw Error(DPST_ERR_INVALID_ARG, "zmax must exceed zmin");
   if (!(p->viscosity > 0)) throw Error(DPST_ERR_INVALID_ARG, "viscosity must be positive");

@@ -18,6 +18,10 @@ struct KernelDesc {
   int nzeff, dend;    // extended z grid size, ghost layers per end
   int wz_max;         // upper bound of the z window length
   int zext_off;       // offset of this kernel's extended z grid in the tables
+  int unif_z;         // 1: uniform periodic z grid (triply periodic mode); the
+                      // window is wz_max points around the nearest node
+  int evenz;          // uniform z: 1 for an even z width
+  double hz;          // uniform z: grid spacing
   double beta, alpha, alpha2, thr, inv_norm3, norm;
 };
 
@@ -29,6 +33,7 @@ struct KernelDesc {
 struct ZEnds {
   int top_active, bot_active;  // top = z max (extended index 0)
   double s_top, s_bot;
+  int periodic;                // triply periodic: z wraps like x and y
 };
 
 // Everything a particle kernel needs (passed by value).

@@ -52,6 +52,29 @@ static __device__ __forceinline__ void locate_item(int64_t p, const double *__re
     st.phy[p * kd.wy + j] = (R)es1(o, kd.beta, kd.alpha2);
     if (DIPOLE) st.dphy[p * kd.wy + j] = (R)des1(o, kd.beta, kd.alpha2);
   }
+  if (kd.unif_z) {
+    // uniform periodic z (ParticleList.cpp:285-366): the window is built like
+    // the x and y windows; its first entry sits at extended index
+    // zclose - wz/2 + evenz + dend; interpolation weight hx hy hz
+    const int wz = kd.wz_max;
+    int zclose = (int)(z / kd.hz);
+    if ((wz & 1) && (z / kd.hz - zclose > 0.5)) zclose += 1;
+    st.cell[p] = make_int4(xclose, yclose, zclose - wz / 2 + kd.evenz + kd.dend, wz);
+    const double hxyz = g.hx * g.hy * kd.hz;
+    for (int k = 0; k < wz; ++k) {
+      double o = ((double)zclose + k - wz / 2 + kd.evenz) * kd.hz - z;
+      if (thr < o || o < -thr) o = thr;
+      const double v = es1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
+      st.phz[p * wz + k] = (R)v;
+      st.phzw[p * wz + k] = (R)(v * hxyz);
+      if (DIPOLE) {
+        const double dv = des1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
+        st.dphz[p * wz + k] = (R)dv;
+        st.dphzw[p * wz + k] = (R)(dv * hxyz);
+      }
+    }
+    return;
+  }
   // z window: zext is strictly descending; indl = #{zext > z + thr},
   // high = #{zext > z - thr}; indr = high - 1 unless zext[high] == z - thr.
   const double *ze = zext + kd.zext_off;
@@ -962,11 +985,13 @@ void launch_ghost_fold(R *buf, int levels, int nx, int ny, const KernelDesc &kd,
 
 // The fused spread / interpolation apply to a monopole / dipole kernel pair
 // with the same x-y stencil columns and extended z grid and a dipole
-// threshold no larger than the monopole's.
+// threshold no larger than the monopole's (on a uniform periodic z grid: the
+// same z width, so that both windows start at the same node).
 bool fused_supports(const KernelDesc &km, const KernelDesc &kd) {
   return km.wx == kd.wx && km.wy == kd.wy && km.evenx == kd.evenx && km.eveny == kd.eveny &&
          km.nxeff == kd.nxeff && km.nyeff == kd.nyeff && km.lend == kd.lend && km.bend == kd.bend &&
-         km.nzeff == kd.nzeff && km.dend == kd.dend && kd.thr <= km.thr;
+         km.nzeff == kd.nzeff && km.dend == kd.dend && kd.thr <= km.thr && km.unif_z == kd.unif_z &&
+         (!km.unif_z || (km.wz_max == kd.wz_max && km.evenz == kd.evenz));
 }
 
 template <typename R, typename RF>

@@ -45,7 +45,8 @@ static __device__ __forceinline__ void es_pos_derivs(double o, double beta, doub
 }
 
 // Where extended z index kk lands on the interior grid under one BC set.
-// Returns the interior index m (descending z, m = 0 at zmax) and the weight
+// Returns the interior index m (descending z, m = 0 at zmax; for a periodic
+// uniform z grid ascending, m = 0 at zmin) and the weight
 // (1 interior, s at a folded ghost, 1+s at an active boundary node).  A
 // ghost layer at an inactive end returns m = -1 (top) or -2 (bottom) and its
 // level in the ghost buffer.
@@ -58,6 +59,13 @@ struct ZMap {
 static __device__ __forceinline__ ZMap zmap(int kk, int dend, int nz, const ZEnds &b) {
   ZMap r;
   r.level = 0;
+  if (b.periodic) {  // BoundaryConditions.h:241-283, 608-647: wrap by nz
+    r.m = kk - dend;
+    if (r.m < 0) r.m += nz;
+    else if (r.m >= nz) r.m -= nz;
+    r.wgt = 1.0;
+    return r;
+  }
   const int ubeg = dend + nz;
   if (kk < dend) {
     if (b.top_active) { r.m = dend - kk; r.wgt = b.s_top; }

@@ -1,0 +1,378 @@
+// Triply periodic operator (DPST_MODE_PERIODIC): the reference's CPU domType
+// 'TP' (FCM.py:149-441 with Transformer type fourier and the TP solver) and
+// the mode 'periodic' of its GPU module (uammd_wrapper.cu:122-126).
+//
+// Mdot pipeline:
+//   zero grid -> spread F (+ torque curl) with z wrapped like x and y
+//   -> 3-D real FFT -> Fourier-space Stokes solve (one thread per mode)
+//   -> inverse 3-D real FFT -> interpolate V (+ W).
+// The particle kernels are the ones of the doubly periodic geometries
+// (dpst_particles.cu) with a uniform z window (ParticleList.cpp:285-366) and
+// the periodic z map; the grid layout is [3][nz][ny][nx] with z ascending
+// from zmin (node m at zmin + m hz).
+//
+// Reference behaviour restated (source/cpu of stochasticHydroTools/
+// DoublyPeriodicStokes):
+//   wavenumbers   Solvers.py:197-222 (FFT order, 2 pi m / L; the unpaired
+//                 Nyquist plane of an even axis zeroed in the derivative but
+//                 kept in |k|^2)
+//   solve         TPTools.cpp:6-46: p = -(Dx f + Dy g + Dz h) / |k|^2,
+//                 u = (f - Dx p) / (eta |k|^2), k = 0 left at zero
+//   transforms    Transform.cpp:109-117 (unnormalised forward), 273-281
+//                 (backward divided by Nx Ny Nz); the real part is kept, so
+//                 the Hermitian half spectrum of a real-to-complex transform
+//                 carries the same result.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/dpstokes_gb300.h"
+#include "dpst_host.cuh"
+#include "dpst_internal.cuh"
+#include "dpst_launch.cuh"
+
+namespace dpst {
+
+template <typename R>
+struct Cplx;
+template <>
+struct Cplx<float> {
+  typedef float2 T;
+};
+template <>
+struct Cplx<double> {
+  typedef double2 T;
+};
+
+// One thread per mode of the half spectrum [3][nz][ny][nxh] (component
+// stride M = nz ny nxh), in place.  scale = 1 / (nx ny nz) folds the inverse
+// transform's normalisation into the solve.
+template <typename R>
+__global__ void k_tp_solve(typename Cplx<R>::T *__restrict__ spec, int64_t M, int nx, int ny, int nz, int nxh,
+                           const double *__restrict__ kvx, const double *__restrict__ kvy,
+                           const double *__restrict__ kvz, R eta, R scale) {
+  typedef typename Cplx<R>::T C;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= M) return;
+  C *u = spec + t;
+  if (t == 0) {  // k = 0: the net force on the cell is ignored
+    const C z = {(R)0, (R)0};
+    u[0] = z;
+    u[M] = z;
+    u[2 * M] = z;
+    return;
+  }
+  const int ix = (int)(t % nxh);
+  const int64_t r = t / nxh;
+  const int iy = (int)(r % ny), iz = (int)(r / ny);
+  const R kx = (R)__ldg(kvx + ix), ky = (R)__ldg(kvy + iy), kz = (R)__ldg(kvz + iz);
+  const R dx = (2 * ix == nx) ? (R)0 : kx;
+  const R dy = (2 * iy == ny) ? (R)0 : ky;
+  const R dz = (2 * iz == nz) ? (R)0 : kz;
+  const R ksq = kx * kx + ky * ky + kz * kz;
+  const C f = u[0], g = u[M], h = u[2 * M];
+  // p = -(i dx f + i dy g + i dz h) / ksq
+  const R pr = (dx * f.y + dy * g.y + dz * h.y) / ksq;
+  const R pi = -(dx * f.x + dy * g.x + dz * h.x) / ksq;
+  const R v = scale / (eta * ksq);
+  C a, b, c;
+  a.x = v * (f.x + dx * pi);
+  a.y = v * (f.y - dx * pr);
+  b.x = v * (g.x + dy * pi);
+  b.y = v * (g.y - dy * pr);
+  c.x = v * (h.x + dz * pi);
+  c.y = v * (h.y - dz * pr);
+  u[0] = a;
+  u[M] = b;
+  u[2 * M] = c;
+}
+
+template <typename R>
+struct EngineTP : EngineBase {
+  typedef typename std::conditional<sizeof(R) == 8, cufftDoubleComplex, cufftComplex>::type CR;
+  int nx, ny, nz, nxh;
+  int64_t M;  // modes of the half spectrum
+  double hx, hy, hz, Lz;
+  KernelHost km, kd;
+  bool fused = false;
+  GridArgs g;
+  DevBuf grid, spec, kvx, kvy, kvz, pos64, flags, ord_count, ord_start, perm, dphzw_buf;
+  DevBuf st_m[8], st_d[8];
+  Stencils<R> stm, std_;
+  Ghosts<R> none;  // no ghost layers: z wraps
+  bool positioned = false;
+  cufftHandle plan_f = 0, plan_b = 0;
+  bool plans = false;
+  cudaEvent_t ev[8] = {};
+  bool have_events = false;
+
+  EngineTP(const dpst_params &prm, int64_t n, int dev) {
+    p = prm;
+    N = n;
+    device = dev;
+    DPST_CUDA(cudaSetDevice(dev));
+    nx = p.nx; ny = p.ny; nz = p.nz;
+    nxh = nx / 2 + 1;
+    M = (int64_t)nz * ny * nxh;
+    hx = p.Lx / nx;
+    hy = p.Ly / ny;
+    Lz = p.zmax - p.zmin;
+    hz = Lz / nz;
+    km = make_kernel_tp(p.w, p.beta, p.alpha, false, hx, hy, hz, nx, ny, nz, "monopole kernel");
+    if (p.has_torque) kd = make_kernel_tp(p.w_d, p.beta_d, p.alpha_d, true, hx, hy, hz, nx, ny, nz, "dipole kernel");
+    fused = p.has_torque && fused_supports(km.d, kd.d);
+    memset(&g, 0, sizeof(g));
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.hx = hx; g.hy = hy; g.Lx = p.Lx; g.Ly = p.Ly; g.Lz = Lz;
+    bc_sets(DPST_MODE_PERIODIC, g);
+    memset(&none, 0, sizeof(none));
+    upload(kvx, wavenumbers(nx, p.Lx));
+    upload(kvy, wavenumbers(ny, p.Ly));
+    upload(kvz, wavenumbers(nz, Lz));
+    grid.alloc(sizeof(R) * 3 * (size_t)nz * ny * nx);
+    spec.alloc(sizeof(CR) * 3 * (size_t)M);
+    pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
+    flags.alloc(sizeof(int) * 8);
+    alloc_stencils(km.d, false, st_m, stm);
+    if (p.has_torque) alloc_stencils(kd.d, true, st_d, std_);
+    ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
+    ord_start.alloc(sizeof(int) * (tile_order_tiles(nx, ny) + 1));
+    perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
+    // 3-D real transforms over (z, y, x), one per component
+    int n3[3] = {nz, ny, nx};
+    int inem[3] = {nz, ny, nx}, onem[3] = {nz, ny, nxh};
+    DPST_CUFFT(cufftPlanMany(&plan_f, 3, n3, inem, 1, nz * ny * nx, onem, 1, (int)M,
+                             sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, 3));
+    DPST_CUFFT(cufftPlanMany(&plan_b, 3, n3, onem, 1, (int)M, inem, 1, nz * ny * nx,
+                             sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, 3));
+    plans = true;
+    DPST_CUDA(cudaDeviceSynchronize());
+  }
+
+  ~EngineTP() override {
+    cudaSetDevice(device);
+    cudaDeviceSynchronize();
+    if (have_events)
+      for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+    if (plans) {
+      cufftDestroy(plan_f);
+      cufftDestroy(plan_b);
+    }
+  }
+
+  void alloc_stencils(const KernelDesc &d, bool dip, DevBuf *b, Stencils<R> &s) {
+    const size_t n = (size_t)std::max<int64_t>(N, 1);
+    b[0].alloc(sizeof(int4) * n);
+    b[1].alloc(sizeof(R) * n * d.wx);
+    b[2].alloc(sizeof(R) * n * d.wy);
+    b[3].alloc(sizeof(R) * n * d.wz_max);
+    b[4].alloc(sizeof(R) * n * d.wz_max);
+    memset(&s, 0, sizeof(s));
+    s.cell = b[0].as<int4>();
+    s.phx = b[1].as<R>();
+    s.phy = b[2].as<R>();
+    s.phz = b[3].as<R>();
+    s.phzw = b[4].as<R>();
+    if (dip) {
+      b[5].alloc(sizeof(R) * n * d.wx);
+      b[6].alloc(sizeof(R) * n * d.wy);
+      b[7].alloc(sizeof(R) * n * d.wz_max);
+      dphzw_buf.alloc(sizeof(R) * n * d.wz_max);
+      s.dphx = b[5].as<R>();
+      s.dphy = b[6].as<R>();
+      s.dphz = b[7].as<R>();
+      s.dphzw = dphzw_buf.as<R>();
+    }
+  }
+
+  void set_positions(const void *pos, int dtype, cudaStream_t s) override {
+    if (N == 0) { positioned = true; return; }
+    if (pos == nullptr) throw Error(DPST_ERR_INVALID_ARG, "positions pointer is NULL");
+    launch_prep_positions(pos, dtype, N, p.zmin, pos64.as<double>(), s);
+    int init[8] = {0, INT_MAX, -1, INT_MAX, -1, 0, 0, 0};
+    int *fl = flags.as<int>();
+    DPST_CUDA(cudaMemcpyAsync(fl, init, sizeof(init), cudaMemcpyHostToDevice, s));
+    launch_locate<R>(false, pos64.as<double>(), N, km.d, nullptr, nullptr, g, stm, fl, fl + 1, s);
+    if (p.has_torque) launch_locate<R>(true, pos64.as<double>(), N, kd.d, nullptr, nullptr, g, std_, fl, fl + 3, s);
+    DPST_CUDA(cudaGetLastError());
+    launch_tile_order<R>(N, g, stm, ord_count.as<int>(), ord_start.as<int>(), perm.as<int>(), s);
+    DPST_CUDA(cudaGetLastError());
+    int out[8];
+    DPST_CUDA(cudaMemcpyAsync(out, fl, sizeof(out), cudaMemcpyDeviceToHost, s));
+    DPST_CUDA(cudaStreamSynchronize(s));
+    if (out[0] & 1) {
+      positioned = false;
+      throw Error(DPST_ERR_OUT_OF_DOMAIN, "a particle lies outside [0,Lx]x[0,Ly]x[zmin,zmax] (or is NaN)");
+    }
+    positioned = true;
+  }
+
+  void mark(int k, cudaStream_t s) {
+    if (!stage_ms) return;
+    if (!have_events) {
+      for (int i = 0; i < 8; ++i) DPST_CUDA(cudaEventCreate(&ev[i]));
+      have_events = true;
+    }
+    DPST_CUDA(cudaEventRecord(ev[k], s));
+  }
+
+  template <typename RF>
+  void spread_stage(const RF *F, const RF *T, cudaStream_t s) {
+    R *gr = grid.as<R>();
+    const bool torque = p.has_torque && T != nullptr;
+    DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
+    if (torque && fused) {
+      launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, none, none, s, perm.as<int>());
+    } else {
+      launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, none, s, perm.as<int>());
+      if (torque) launch_spread<R, RF>(true, T, N, kd.d, g, std_, gr, none, s, perm.as<int>());
+    }
+    DPST_CUDA(cudaGetLastError());
+  }
+
+  void solve_stage(cudaStream_t s) {
+    R *gr = grid.as<R>();
+    CR *sp = spec.as<CR>();
+    DPST_CUFFT(cufftSetStream(plan_f, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
+    else
+      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
+    mark(2, s);
+    mark(3, s);  // no z transform in this mode
+    const int bs = 256;
+    k_tp_solve<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<typename Cplx<R>::T *>(sp), M, nx, ny, nz,
+                                                  nxh, kvx.as<double>(), kvy.as<double>(), kvz.as<double>(),
+                                                  (R)p.viscosity, (R)(1.0 / ((double)nx * ny * nz)));
+    DPST_CUDA(cudaGetLastError());
+    mark(4, s);
+    mark(5, s);
+    DPST_CUFFT(cufftSetStream(plan_b, s));
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
+    else
+      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
+    mark(6, s);
+  }
+
+  template <typename RF>
+  void interp_stage(bool torque, RF *V, RF *W, cudaStream_t s) {
+    const R *gr = grid.as<R>();
+    (void)torque;
+    if (p.has_torque && W != nullptr) {
+      if (fused) {
+        launch_interp_fused<R, RF>(gr, N, km.d, kd.d, g, stm, std_, none, none, V, W, s, perm.as<int>());
+      } else {
+        launch_interp<R, RF>(false, gr, N, km.d, g, stm, none, V, s, perm.as<int>());
+        launch_interp<R, RF>(true, gr, N, kd.d, g, std_, none, W, s, perm.as<int>());
+      }
+    } else {
+      launch_interp<R, RF>(false, gr, N, km.d, g, stm, none, V, s, perm.as<int>());
+    }
+    DPST_CUDA(cudaGetLastError());
+  }
+
+  template <typename RF>
+  void run(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    mark(0, s);
+    spread_stage<RF>(F, T, s);
+    mark(1, s);
+    solve_stage(s);
+    interp_stage<RF>(torque, V, W, s);
+    mark(7, s);
+    if (stage_ms) {
+      DPST_CUDA(cudaEventSynchronize(ev[7]));
+      const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
+      for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
+    }
+  }
+
+  void mdot(const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (N == 0) return;
+    if (F == nullptr || V == nullptr) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    if (dtype == DPST_F64)
+      run<double>((const double *)F, (const double *)T, (double *)V, (double *)W, s);
+    else if (dtype == DPST_F32)
+      run<float>((const float *)F, (const float *)T, (float *)V, (float *)W, s);
+    else
+      throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+  }
+
+  // K columns at the same positions: one Mdot per column (the triply
+  // periodic solve has no per-wavenumber factors to share)
+  void mdot_multi(int K, const void *F, const void *T, void *V, void *W, int dtype, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (K < 1) throw Error(DPST_ERR_INVALID_ARG, "K must be at least 1");
+    if (N == 0) return;
+    if (F == nullptr || V == nullptr) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    if (dtype != DPST_F64 && dtype != DPST_F32) throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+    const size_t col = 3 * (size_t)N * (dtype == DPST_F64 ? 8 : 4);
+    for (int k = 0; k < K; ++k) {
+      const char *Fk = (const char *)F + k * col;
+      const char *Tk = T ? (const char *)T + k * col : nullptr;
+      char *Vk = (char *)V + k * col;
+      char *Wk = W ? (char *)W + k * col : nullptr;
+      mdot(Fk, Tk, Vk, Wk, dtype, s);
+    }
+  }
+
+  void spread_grid(const void *F, const void *T, int dtype, void *out, cudaStream_t s) override {
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (!F || !out) throw Error(DPST_ERR_INVALID_ARG, "F and grid_out must not be NULL");
+    if (dtype == DPST_F64) spread_stage<double>((const double *)F, (const double *)T, s);
+    else if (dtype == DPST_F32) spread_stage<float>((const float *)F, (const float *)T, s);
+    else throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+    DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
+  }
+
+  void velocity_grid(void *out, cudaStream_t s) override {
+    if (!out) throw Error(DPST_ERR_INVALID_ARG, "grid_out must not be NULL");
+    DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
+  }
+
+  void backward(const void *, const void *, const void *, const void *, void *, void *, void *, int,
+                cudaStream_t) override {
+    throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the NOWALL, BOTTOM and SLIT geometries");
+  }
+
+  void info(dpst_info *o) const override {
+    memset(o, 0, sizeof(*o));
+    o->nxh = nxh;
+    o->n_modes = (int)M;
+    o->nzeff_m = km.d.nzeff;
+    o->nzeff_d = p.has_torque ? kd.d.nzeff : 0;
+    o->ghost_m = km.d.dend;
+    o->ghost_d = p.has_torque ? kd.d.dend : 0;
+    o->wz_max_m = km.d.wz_max;
+    o->wz_max_d = p.has_torque ? kd.d.wz_max : 0;
+    o->thr_m = km.d.thr;
+    o->thr_d = p.has_torque ? kd.d.thr : 0;
+    o->norm_m = km.d.norm;
+    o->norm_d = p.has_torque ? kd.d.norm : 0;
+    o->n_particles = N;
+    // spread (mono [+ dip]), Fourier solve, interp (mono [+ dip])
+    const int particle_passes = (p.has_torque && !fused) ? 2 : 1;
+    o->kernels_per_mdot = particle_passes + 1 + particle_passes;
+    o->fused_particle_passes = fused ? 1 : 0;
+    int64_t b = 0;
+    const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf};
+    for (const DevBuf *d : all) b += d->bytes;
+    for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
+    o->device_bytes = b;
+  }
+};
+
+EngineBase *make_engine_tp(const dpst_params &p, int64_t n, int device) {
+  if (p.precision == DPST_PREC_FP64) return new EngineTP<double>(p, n, device);
+  return new EngineTP<float>(p, n, device);
+}
+
+}  // namespace dpst

@@ -19,7 +19,7 @@ import torch
 from . import gridconfig
 from .operator import DPStokes, StokesParams
 
-_MODE = {"DP": "nowall", "DPBW": "bottom", "DPSC": "slit"}
+_MODE = {"DP": "nowall", "DPBW": "bottom", "DPSC": "slit", "TP": "periodic"}
 
 
 class FCMJoint:
@@ -40,7 +40,7 @@ class FCMJoint:
         value, 1.714 without torques, 1.3267 with), w_d, beta_d_hat and z0
         are taken as given."""
         if domType not in _MODE:
-            raise ValueError("domType must be DP, DPBW or DPSC (TP is not provided)")
+            raise ValueError("domType must be DP, DPBW, DPSC or TP")
         self.Clean()
         self.has_torque = bool(has_torque)
         self.N = int(numberParticles)

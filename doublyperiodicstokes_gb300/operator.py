@@ -22,8 +22,9 @@ from . import _lib
 class StokesParams:
     """Explicit operator parameters (the fields of dpst_params).
 
-    mode: 'nowall' | 'bottom' | 'slit' (reference domType DP / DPBW / DPSC).
-    z interval [zmin, zmax]; walls at zmin (bottom) and zmax (slit top).
+    mode: 'nowall' | 'bottom' | 'slit' | 'periodic' (reference domType DP /
+    DPBW / DPSC / TP).  z interval [zmin, zmax]; walls at zmin (bottom) and
+    zmax (slit top); 'periodic': nz uniform points on the periodic [zmin, zmax).
     Kernels: w points per axis, ES beta (the reference's beta_hat * w) and
     alpha (physical half width)."""
     mode: str
@@ -64,7 +65,7 @@ class StokesParams:
     @classmethod
     def from_workload(cls, wl, precision="fp64"):
         """Parameters of a doublyperiodicstokes_gb300.workloads.Workload."""
-        mode = {"DP": "nowall", "DPBW": "bottom", "DPSC": "slit"}[wl.domType]
+        mode = {"DP": "nowall", "DPBW": "bottom", "DPSC": "slit", "TP": "periodic"}[wl.domType]
         hx = wl.Lx / wl.nx
         return cls(mode=mode, nx=wl.nx, ny=wl.ny, nz=wl.nz, Lx=wl.Lx, Ly=wl.Ly, zmin=wl.z0,
                    zmax=wl.z0 + wl.Lz, viscosity=wl.eta, w=wl.wm, beta=wl.betam_hat * wl.wm,

@@ -24,9 +24,10 @@ reproduces its CPU path):
     R/(2 c h) = w/2); the operator uses alpha * Lx/nx;
   * zmin, zmax: the Chebyshev interval, taken at face value; walls at zmin
     ('bottom', 'slit') and zmax ('slit');
-  * mode: 'nowall' | 'bottom' | 'slit'; an unknown string means 'nowall'
-    (uammd_wrapper.cu:55-66); 'periodic' (triply periodic FCM) is not
-    provided by this operator and raises;
+  * mode: 'nowall' | 'bottom' | 'slit' | 'periodic'; an unknown string
+    means 'nowall' (uammd_wrapper.cu:55-66); 'periodic' runs the triply
+    periodic operator on nz uniform points of [zmin, zmax) (the reference
+    module hands it to UAMMD's FCM, uammd_wrapper.cu:122-126);
   * torques: the operator is created with the dipole kernel when w_d, beta_d
     and alpha_d are all positive; an Mdot whose torque array holds fewer than
     3N values runs without torques (uammd_python.cpp:51-53).
@@ -72,7 +73,7 @@ class StokesParameters:
                    self.nz, self.mode))
 
 
-_MODES = {"nowall": 0, "bottom": 1, "slit": 2}
+_MODES = {"nowall": 0, "bottom": 1, "slit": 2, "periodic": 3}
 
 
 class DPStokes:
@@ -85,8 +86,6 @@ class DPStokes:
     def initialize(self, Parameters, numberParticles):
         self.clear()
         par = Parameters
-        if par.mode == "periodic":
-            raise RuntimeError("mode 'periodic' (triply periodic) is not provided by dpstokes_gb300")
         if par.nx <= 0 or par.ny <= 0 or par.nz <= 0:
             raise RuntimeError("nx, ny and nz must be given")
         h = par.Lx / par.nx

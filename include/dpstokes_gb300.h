@@ -70,10 +70,15 @@ extern "C" {
 #define DPST_ERR_UNSUPPORTED 5   /* configuration the reference cannot run either */
 #define DPST_ERR_ALLOC 6         /* device or host allocation failed */
 
-/* geometry: reference domType DP / DPBW / DPSC (FCM.py:211-229) */
+/* geometry: reference domType DP / DPBW / DPSC / TP (FCM.py:211-229) */
 #define DPST_MODE_NOWALL 0
 #define DPST_MODE_BOTTOM 1
 #define DPST_MODE_SLIT 2
+#define DPST_MODE_PERIODIC 3 /* triply periodic: nz uniform points on the periodic
+                                [zmin, zmax); the reference GPU module's mode
+                                'periodic' (uammd_wrapper.cu:122-126) and CPU
+                                domType 'TP' (TPTools.cpp:6-46).  dpst_create only:
+                                no batched, multi-column solve sharing or backward */
 
 /* arithmetic of the operator */
 #define DPST_PREC_FP64 0  /* every stage in FP64: the drop-in for the reference */
@@ -85,9 +90,11 @@ extern "C" {
 
 typedef struct dpst_params {
   int mode;          /* DPST_MODE_* */
-  int nx, ny, nz;    /* grid: nx*ny Fourier modes, nz Chebyshev points */
+  int nx, ny, nz;    /* grid: nx*ny Fourier modes, nz Chebyshev points (PERIODIC:
+                        nz uniform points, hz = (zmax - zmin) / nz) */
   double Lx, Ly;     /* periodic box */
-  double zmin, zmax; /* Chebyshev interval; walls sit at zmin (bottom) / zmax (slit top) */
+  double zmin, zmax; /* Chebyshev interval; walls sit at zmin (bottom) / zmax (slit top);
+                        PERIODIC: the periodic z box */
   double viscosity;
   int w;             /* monopole kernel: points per axis */
   double beta;       /* monopole ES beta (the reference's beta_hat * w) */

@@ -28,6 +28,8 @@ def sample_mdot_seconds(p: O.Params, X, F, T=None, pfrac=16, mfrac=16):
     t0 = time.perf_counter()
     fG = o.spread_all(F[:ns], None if T is None else T[:ns])
     t_spread = time.perf_counter() - t0
+    if p.domType == 'TP':
+        return _sample_tp(p, o, fG, N, ns, t_spread)
     # forward transform of one component
     one = np.ascontiguousarray(fG[..., :1])
     del fG
@@ -71,4 +73,40 @@ def sample_mdot_seconds(p: O.Params, X, F, T=None, pfrac=16, mfrac=16):
     sample = ("oracle stages timed on %d of %d particles (x%.0f), 1 of 3 grid components (x3), "
               "%d of %d wavenumbers (x%.1f); single-threaded numpy"
               % (ns, N, scale, modes.size, nk - 1, (nk - 1) / modes.size))
+    return total, stages, sample
+
+
+def _sample_tp(p, o, fG, N, ns, t_spread):
+    """Triply periodic stages: 3-D FFT of one component (x3), the full
+    Fourier-space solve, inverse FFT of one component (x3), interpolation of
+    the sampled particles."""
+    t0 = time.perf_counter()
+    fh1 = np.fft.fftn(np.ascontiguousarray(fG[..., 0]))
+    t_fwd = 3 * (time.perf_counter() - t0)
+    fh = np.repeat(fh1[..., None], 3, axis=3)
+    del fG
+    t0 = time.perf_counter()
+    U = O.tp_solve(fh, p.Lx, p.Ly, p.Lz, p.eta)
+    t_solve = time.perf_counter() - t0
+    del fh
+    t0 = time.perf_counter()
+    ug = np.fft.ifftn(U[..., 0]).real
+    t_bwd = 3 * (time.perf_counter() - t0)
+    del U
+    uG = np.repeat(ug[..., None], 3, axis=3)
+    t0 = time.perf_counter()
+    O.ghost_copy(o.g, uG, o.BCs)
+    O.interpolate(o.g, o.km, o.loc)
+    if p.has_torque:
+        O.ghost_copy(o.tg, uG, o.BCs)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=0)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=1)
+        O.interpolate(o.tg, o.kd, o.tloc, deriv=2)
+    t_interp = time.perf_counter() - t0
+    scale = N / ns
+    stages = dict(spread=t_spread * scale, fft_fwd=t_fwd, solve=t_solve, fft_bwd=t_bwd,
+                  interp=t_interp * scale)
+    total = sum(stages.values())
+    sample = ("oracle stages timed on %d of %d particles (x%.0f), 1 of 3 grid components (x3), "
+              "every wavenumber; single-threaded numpy" % (ns, N, scale))
     return total, stages, sample
