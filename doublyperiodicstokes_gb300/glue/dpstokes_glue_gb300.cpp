@@ -53,10 +53,12 @@ int dtype() { return sizeof(real) == sizeof(double) ? DPST_F64 : DPST_F32; }
 
 void DPStokesGlue::initialize(PyParameters par, int numberParticles) {
   dpstokes.reset();
-  if (par.mode == "periodic") throw std::runtime_error("mode 'periodic' is not provided by dpstokes_gb300");
   if (par.nx <= 0 || par.ny <= 0 || par.nz <= 0) throw std::runtime_error("nx, ny and nz must be given");
   dpst_params p{};
-  p.mode = par.mode == "bottom" ? DPST_MODE_BOTTOM : par.mode == "slit" ? DPST_MODE_SLIT : DPST_MODE_NOWALL;
+  p.mode = par.mode == "bottom"     ? DPST_MODE_BOTTOM
+           : par.mode == "slit"     ? DPST_MODE_SLIT
+           : par.mode == "periodic" ? DPST_MODE_PERIODIC
+                                    : DPST_MODE_NOWALL;
   p.nx = par.nx;
   p.ny = par.ny;
   p.nz = par.nz;
