@@ -23,7 +23,7 @@ class DpstParams(ctypes.Structure):
                 ("viscosity", ctypes.c_double), ("w", ctypes.c_int), ("beta", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("has_torque", ctypes.c_int), ("w_d", ctypes.c_int),
                 ("beta_d", ctypes.c_double), ("alpha_d", ctypes.c_double),
-                ("precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("torque_kernel", ctypes.c_int)]
 
 
 class DpstInfo(ctypes.Structure):

@@ -348,7 +348,8 @@ static std::vector<double> wavenumbers(int n, double L) {
 }
 
 // Parameter checks of dpst_create (shared by the batched engine).
-// periodic: whether the caller runs the triply periodic mode.
+// periodic_ok: the caller (dpst_create) runs the triply periodic mode and the
+// regular-kernel torque coupling; the batched engine does not.
 static void validate(const dpst_params *p, int64_t n, bool periodic_ok = false) {
   if (!p) throw Error(DPST_ERR_INVALID_ARG, "params is NULL");
   if (n < 0) throw Error(DPST_ERR_INVALID_ARG, "n_particles < 0");
@@ -372,6 +373,10 @@ static void validate(const dpst_params *p, int64_t n, bool periodic_ok = false) 
   if (!(p->viscosity > 0)) throw Error(DPST_ERR_INVALID_ARG, "viscosity must be positive");
   if (p->precision != DPST_PREC_FP64 && p->precision != DPST_PREC_MIXED)
     throw Error(DPST_ERR_INVALID_ARG, "precision must be DPST_PREC_FP64 or DPST_PREC_MIXED");
+  if (p->torque_kernel != DPST_TORQUE_DERIV && p->torque_kernel != DPST_TORQUE_REG)
+    throw Error(DPST_ERR_INVALID_ARG, "torque_kernel must be DPST_TORQUE_DERIV or DPST_TORQUE_REG");
+  if (p->torque_kernel == DPST_TORQUE_REG && !periodic_ok)
+    throw Error(DPST_ERR_UNSUPPORTED, "torque_kernel DPST_TORQUE_REG is available through dpst_create only");
 }
 
 // Runs fn and turns exceptions into the C ABI's return codes and message.

@@ -26,7 +26,9 @@ class StokesParams:
     DPBW / DPSC / TP).  z interval [zmin, zmax]; walls at zmin (bottom) and
     zmax (slit top); 'periodic': nz uniform points on the periodic [zmin, zmax).
     Kernels: w points per axis, ES beta (the reference's beta_hat * w) and
-    alpha (physical half width)."""
+    alpha (physical half width).  reg_kernel: torques and angular velocities
+    with the regular ES kernel of (w_d, beta_d, alpha_d) and spectral curls
+    (the reference's useRegKernel=True) instead of the derivative kernels."""
     mode: str
     nx: int
     ny: int
@@ -44,13 +46,14 @@ class StokesParams:
     beta_d: float = 13.296
     alpha_d: float = 3.0
     precision: str = "fp64"
+    reg_kernel: bool = False
 
     def to_c(self):
         return _lib.DpstParams(
             _lib.MODE[self.mode], int(self.nx), int(self.ny), int(self.nz), float(self.Lx),
             float(self.Ly), float(self.zmin), float(self.zmax), float(self.viscosity), int(self.w),
             float(self.beta), float(self.alpha), int(bool(self.has_torque)), int(self.w_d),
-            float(self.beta_d), float(self.alpha_d), _lib.PREC[self.precision])
+            float(self.beta_d), float(self.alpha_d), _lib.PREC[self.precision], int(bool(self.reg_kernel)))
 
     def as_dict(self):
         return asdict(self)
@@ -71,7 +74,8 @@ class StokesParams:
                    zmax=wl.z0 + wl.Lz, viscosity=wl.eta, w=wl.wm, beta=wl.betam_hat * wl.wm,
                    alpha=cls.kernel_alpha(wl.radius, wl.wm, hx), has_torque=wl.has_torque,
                    w_d=wl.wd, beta_d=wl.betad_hat * wl.wd,
-                   alpha_d=cls.kernel_alpha(wl.radius, wl.wd, hx), precision=precision)
+                   alpha_d=cls.kernel_alpha(wl.radius, wl.wd, hx), precision=precision,
+                   reg_kernel=wl.reg_kernel)
 
 
 def _dtype_code(t):

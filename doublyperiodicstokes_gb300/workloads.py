@@ -45,13 +45,14 @@ class Workload:
     eta: float = ETA_DEFAULT
     radius: float = 1.0
     seed: int = 0
+    reg_kernel: bool = False  # torques with the regular kernel and spectral curls (useRegKernel)
 
     def oracle_params(self):
         """Keyword arguments of the oracle's Params (same field meanings)."""
         return dict(domType=self.domType, Nx=self.nx, Ny=self.ny, Nz=self.nz, Lx=self.Lx,
                     Ly=self.Ly, Lz=self.Lz, z0=self.z0, eta=self.eta, wm=self.wm,
                     betam_hat=self.betam_hat, has_torque=self.has_torque, wd=self.wd,
-                    betad_hat=self.betad_hat, radius=self.radius)
+                    betad_hat=self.betad_hat, radius=self.radius, reg_kernel=self.reg_kernel)
 
     def to_dict(self):
         return asdict(self)
@@ -165,7 +166,12 @@ SMALL_TP = [
     replace(small("s_tp_t_w5", "TP", 20, 17, 15, 15.0, 0.0, 15.0, True, seed=11),
             wm=5, wd=5, betam_hat=1.3055, betad_hat=2.2320),
 ]
-SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP}
+# The regular-kernel torque coupling (useRegKernel) on torque cases of every
+# geometry, including open ends reached by the kernels, an odd grid and a
+# shifted z origin.
+SMALL_REG = [replace(w, name=w.name.replace("s_", "s_reg_", 1), reg_kernel=True) for w in SMALL + SMALL_TP
+             if w.name in ("s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_t_odd", "s_dp_t_shift", "s_tp_t", "s_tp_t_hz")]
+SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP + SMALL_REG}
 
 
 def small_batch(domType, has_torque, seed=40):

@@ -84,6 +84,15 @@ extern "C" {
 #define DPST_PREC_FP64 0  /* every stage in FP64: the drop-in for the reference */
 #define DPST_PREC_MIXED 1 /* FP32 spread/FFT/interp, FP32 z transform, FP64 BVP */
 
+/* torque coupling (has_torque) */
+#define DPST_TORQUE_DERIV 0 /* derivative ES kernels spread the torque curl and interpolate the
+                               velocity gradient: the reference's default (FCM.py:362-371,
+                               411-426; useRegKernel = False) */
+#define DPST_TORQUE_REG 1   /* regular ES kernel of the dipole's (w, beta, alpha) for torques and
+                               angular velocities, curls taken spectrally (FCM.py:372-396,
+                               427-439; useRegKernel = True).  dpst_create only: no batched
+                               systems, no backward */
+
 /* element type of the particle arrays passed to mdot */
 #define DPST_F64 0
 #define DPST_F32 1
@@ -104,6 +113,7 @@ typedef struct dpst_params {
   double beta_d;
   double alpha_d;
   int precision;     /* DPST_PREC_* */
+  int torque_kernel; /* DPST_TORQUE_* (0 when the initialiser stops before it) */
 } dpst_params;
 
 typedef struct dpst_info {

@@ -50,7 +50,10 @@ class Params:
     floating-point formula is used (ParticleList.cpp:229).
     z0 is the floor of the Chebyshev interval [z0, z0+Lz] (FCM.py:170).
     domType 'TP' (triply periodic): Nz uniform points on the periodic
-    interval [z0, z0+Lz), hz = Lz / Nz (GridAndKernelConfig.py:380-393)."""
+    interval [z0, z0+Lz), hz = Lz / Nz (GridAndKernelConfig.py:380-393).
+    reg_kernel: the reference's useRegKernel torque coupling (FCM.py:372-396,
+    427-439): torques spread with the regular ES kernel of the dipole's
+    (w, beta, alpha), their curl and the fluid vorticity taken spectrally."""
     domType: str
     Nx: int
     Ny: int
@@ -66,6 +69,7 @@ class Params:
     wd: int = 6
     betad_hat: float = 2.2160
     radius: float = 1.0
+    reg_kernel: bool = False  # torques with the regular kernel and spectral curls (useRegKernel)
 
     @property
     def hx(self):
@@ -87,7 +91,7 @@ class Params:
         return dict(domType=self.domType, Nx=self.Nx, Ny=self.Ny, Nz=self.Nz, Lx=self.Lx,
                     Ly=self.Ly, Lz=self.Lz, z0=self.z0, eta=self.eta, wm=self.wm,
                     betam_hat=self.betam_hat, has_torque=self.has_torque, wd=self.wd,
-                    betad_hat=self.betad_hat, radius=self.radius)
+                    betad_hat=self.betad_hat, radius=self.radius, reg_kernel=self.reg_kernel)
 
 
 def domain_bcs(domType):
@@ -831,6 +835,27 @@ class DPSolver:
         U[0, :, 1] += self.SIMat @ av
 
 
+def cheb_coeff_diff(fh, H):
+    """Chebyshev coefficients of d/dz of fh [..., Nz] (z last): the downward
+    recurrence of chebCoeffDiff_perm
+    (Chebyshev.py:68-94) for z in [a, a + 2H]."""
+    Nz = fh.shape[-1]
+    Df = np.zeros_like(fh)
+    Df[..., Nz - 2] = 2 / H * (Nz - 1) * fh[..., Nz - 1]
+    for j in range(2, Nz):
+        Df[..., Nz - j - 1] = Df[..., Nz - j + 1] + 2 / H * (Nz - j) * fh[..., Nz - j]
+    Df[..., 0] /= 2
+    return Df
+
+
+def spectral_curl(C, Dx, Dy, dz):
+    """(Dy Cz - dz(Cy), dz(Cx) - Dx Cz, Dx Cy - Dy Cx) of the coefficient
+    field C [..., 3] (FCM.py:372-396, Solvers.py:139-177); dz is the z
+    derivative operator on one component."""
+    Cx, Cy, Cz = C[..., 0], C[..., 1], C[..., 2]
+    return np.stack([Dy * Cz - dz(Cy), -Dx * Cz + dz(Cx), Dx * Cy - Dy * Cx], axis=-1)
+
+
 # --------------------------------------------------------------------------
 # Triply periodic solver (Solvers.py:197-258, TPTools.cpp:6-46)
 # --------------------------------------------------------------------------
@@ -840,12 +865,8 @@ def tp_wavenumbers(n, L):
                                        np.arange(-1 * np.ceil(n / 2) + 1, 0))) / L
 
 
-def tp_solve(fhat, Lx, Ly, Lz, eta):
-    """fhat [Ny,Nx,Nz,3] (unnormalised 3-D DFT) -> velocity coefficients:
-    p = -(Dx f + Dy g + Dz h) / |k|^2, u = (f - Dx p) / (eta |k|^2) per mode,
-    D = i k with the unpaired (Nyquist) plane of an even axis zeroed in D but
-    not in |k|^2, and the k = 0 mode left at zero."""
-    Ny, Nx, Nz, _ = fhat.shape
+def tp_derivatives(Ny, Nx, Nz, Lx, Ly, Lz):
+    """Ksq, Dx, Dy, Dz on [Ny, Nx, Nz] (Solvers.py:197-222)."""
     Ky, Kx, Kz = np.meshgrid(tp_wavenumbers(Ny, Ly), tp_wavenumbers(Nx, Lx),
                              tp_wavenumbers(Nz, Lz), indexing='ij')
     Ksq = Kx ** 2 + Ky ** 2 + Kz ** 2
@@ -856,6 +877,16 @@ def tp_solve(fhat, Lx, Ly, Lz, eta):
         Dy[Ny // 2, :, :] = 0
     if Nz % 2 == 0:
         Dz[:, :, Nz // 2] = 0
+    return Ksq, Dx, Dy, Dz
+
+
+def tp_solve(fhat, Lx, Ly, Lz, eta):
+    """fhat [Ny,Nx,Nz,3] (unnormalised 3-D DFT) -> velocity coefficients:
+    p = -(Dx f + Dy g + Dz h) / |k|^2, u = (f - Dx p) / (eta |k|^2) per mode,
+    D = i k with the unpaired (Nyquist) plane of an even axis zeroed in D but
+    not in |k|^2, and the k = 0 mode left at zero."""
+    Ny, Nx, Nz, _ = fhat.shape
+    Ksq, Dx, Dy, Dz = tp_derivatives(Ny, Nx, Nz, Lx, Ly, Lz)
     Ksq0 = Ksq.copy()
     Ksq0[0, 0, 0] = 1.0
     f, g, h = fhat[..., 0], fhat[..., 1], fhat[..., 2]
@@ -881,7 +912,7 @@ class Oracle:
         self.BCs, self.BCst = domain_bcs(p.domType)
         self.tp = p.domType == 'TP'
         self.km = Kernel(p.wm, p.betam_hat, p.alpha(p.wm), dipole=False)
-        self.kd = Kernel(p.wd, p.betad_hat, p.alpha(p.wd), dipole=True) if p.has_torque else None
+        self.kd = Kernel(p.wd, p.betad_hat, p.alpha(p.wd), dipole=not p.reg_kernel) if p.has_torque else None
         if self.tp:
             self.zpts = self.zwts = None
             self.solver = None
@@ -945,8 +976,53 @@ class Oracle:
             s.correct_k0(U, fk[0], slit=True)
         return U.reshape(p.Ny, p.Nx, p.Nz, 3)
 
+    def _mdot_reg(self, F, T, stages):
+        """useRegKernel torque coupling (FCM.py:372-396, 427-439): the torques
+        spread with the regular kernel, 1/2 curl of their transform added to the
+        forces' (Fourier derivatives in x, y; Chebyshev coefficient recurrence
+        or Fourier derivative in z), the solve, the vorticity 1/2 curl u of the
+        solution's coefficients (Solvers.py:134-177), both transformed back and
+        interpolated (V with the monopole kernel, Omega with the regular dipole
+        kernel on the torque grid, whose open-end ghost layers still hold the
+        torque spread)."""
+        p = self.p
+        F = np.asarray(F, dtype=np.float64).reshape(-1, 3)
+        T = np.zeros_like(F) if T is None else np.asarray(T, dtype=np.float64).reshape(-1, 3)
+        spread(self.g, self.km, self.loc, F)
+        fG = fold(self.g, self.BCs)
+        spread(self.tg, self.kd, self.tloc, T)
+        tG = fold(self.tg, self.BCs)
+        if self.tp:
+            _, Dx, Dy, Dz = tp_derivatives(p.Ny, p.Nx, p.Nz, p.Lx, p.Ly, p.Lz)
+            fhat = np.fft.fftn(fG, axes=(0, 1, 2))
+            that = np.fft.fftn(tG, axes=(0, 1, 2))
+            dz = lambda C: Dz * C  # noqa: E731
+        else:
+            Dx = self.solver.Dx.reshape(p.Ny, p.Nx)[:, :, None]
+            Dy = self.solver.Dy.reshape(p.Ny, p.Nx)[:, :, None]
+            fhat = fc_forward(fG)
+            that = fc_forward(tG)
+            dz = lambda C: cheb_coeff_diff(C, p.Lz / 2)  # noqa: E731
+        U = self.solve(fhat + 0.5 * spectral_curl(that, Dx, Dy, dz))
+        Ut = 0.5 * spectral_curl(U, Dx, Dy, dz)
+        if self.tp:
+            uG = np.ascontiguousarray(np.fft.ifftn(U, axes=(0, 1, 2)).real)
+            utG = np.ascontiguousarray(np.fft.ifftn(Ut, axes=(0, 1, 2)).real)
+        else:
+            uG = fc_backward(U)
+            utG = fc_backward(Ut)
+        if stages is not None:
+            stages.update(spread_grid=fG, torque_grid=tG, u_hat=U, u_grid=uG, vort_grid=utG)
+        ghost_copy(self.g, uG, self.BCs)
+        V = interpolate(self.g, self.km, self.loc)
+        ghost_copy(self.tg, utG, self.BCs)
+        W = interpolate(self.tg, self.kd, self.tloc)
+        return V.ravel(), W.ravel()
+
     def mdot(self, F, T=None, stages=None):
         p = self.p
+        if p.has_torque and p.reg_kernel:
+            return self._mdot_reg(F, T, stages)
         fG = self.spread_all(F, T)
         if self.tp:  # Transform type fourier (Transform.cpp:109-117, 273-281)
             fhat = np.fft.fftn(fG, axes=(0, 1, 2))

@@ -107,7 +107,7 @@ def _child_main(cfg_path, in_path, out_path):
     dom = cfg["domType"]
     solver = fcm_mod.FCM(radP, kern, dom, has_torque)
     solver.SetUnitCell([0.0, Lx], [0.0, Ly], [z0, z0 + Lz])
-    solver.Initialize(float(cfg["eta"]), 0)
+    solver.Initialize(float(cfg["eta"]), 0, useRegKernel=bool(cfg.get("reg_kernel", False)))
     X = np.array(data["X"], dtype=np.float64).ravel().copy()
     F = np.array(data["F"], dtype=np.float64).ravel().copy()
     T = np.array(data["T"], dtype=np.float64).ravel().copy() if has_torque else np.empty(0)
@@ -128,7 +128,7 @@ def run_reference(cfg, X, F, T=None, stages=False, repeat=1, threads=4, timeout=
     """Run the reference Mdot in a child process.
 
     cfg keys: domType ('DP'|'DPBW'|'DPSC'|'TP'), Nx, Ny, Nz, Lx, Ly, Lz, z0, eta,
-    wm, betam_hat, has_torque, wd, betad_hat, radius.  Returns a dict of numpy
+    wm, betam_hat, has_torque, wd, betad_hat, radius, reg_kernel (FCM's useRegKernel).  Returns a dict of numpy
     arrays (V, W and, with stages=True, the intermediate grids)."""
     if not reference_available():
         raise RuntimeError("reference sources or oracle/_ref libraries are missing")
