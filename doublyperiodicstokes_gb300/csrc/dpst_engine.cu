@@ -52,6 +52,9 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
                                cudaStream_t s, bool *too_big);
 size_t noalloc_scratch_bytes();
 template <typename R>
+void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
+                      const double *kvx, const double *kvy, double H, cudaStream_t s);
+template <typename R>
 cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiArgs &e, int nsm,
                          cudaStream_t s, bool fold_out);
 // tensor-core z transform of the mixed operator (dpst_ztc.cu)
@@ -95,6 +98,8 @@ struct Engine : EngineBase {
   double hx, hy, Lz, H;
   KernelHost km, kd;
   bool fused = false;  // monopole and dipole share one spread and one interpolation pass
+  bool reg = false;    // torques with the regular kernel and spectral curls (DPST_TORQUE_REG)
+  DevBuf gridT, specT; // reg: torque grid and spectrum, then the vorticity's
   GridArgs g;
   KsArgs ks;
   // device buffers
@@ -132,8 +137,9 @@ struct Engine : EngineBase {
     std::vector<double> zG, zW;
     clencurt(nz, 0.0, Lz, zG, zW);
     km = make_kernel(p.w, p.beta, p.alpha, false, hx, hy, nx, ny, zG, zW, "monopole kernel");
-    if (p.has_torque) kd = make_kernel(p.w_d, p.beta_d, p.alpha_d, true, hx, hy, nx, ny, zG, zW, "dipole kernel");
-    fused = p.has_torque && fused_supports(km.d, kd.d);
+    reg = p.has_torque && p.torque_kernel == DPST_TORQUE_REG;
+    if (p.has_torque) kd = make_kernel(p.w_d, p.beta_d, p.alpha_d, !reg, hx, hy, nx, ny, zG, zW, "dipole kernel");
+    fused = p.has_torque && !reg && fused_supports(km.d, kd.d);
     km.d.zext_off = 0;
     kd.d.zext_off = (int)km.zext.size();
     std::vector<double> ze = km.zext, we = km.wext;
@@ -235,7 +241,11 @@ struct Engine : EngineBase {
     pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
     flags.alloc(sizeof(int) * 8);
     alloc_stencils(km.d, false, st_m, stm);
-    if (p.has_torque) alloc_stencils(kd.d, true, st_d, std_);
+    if (p.has_torque) alloc_stencils(kd.d, !reg, st_d, std_);
+    if (reg) {  // torque grid / spectrum, then the vorticity's
+      gridT.alloc(grid.bytes);
+      specT.alloc(spec.bytes);
+    }
     // particle order by grid tile (set_positions), used by the spread and
     // interpolation kernels
     ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
@@ -325,7 +335,7 @@ struct Engine : EngineBase {
     launch_locate<R>(false, pos64.as<double>(), N, km.d, zext.as<double>(), wext.as<double>(), g, stm, fl,
                      fl + 1, s);
     if (p.has_torque)
-      launch_locate<R>(true, pos64.as<double>(), N, kd.d, zext.as<double>(), wext.as<double>(), g, std_, fl,
+      launch_locate<R>(!reg, pos64.as<double>(), N, kd.d, zext.as<double>(), wext.as<double>(), g, std_, fl,
                        fl + 3, s);
     DPST_CUDA(cudaGetLastError());
     int out[8];
@@ -344,7 +354,7 @@ struct Engine : EngineBase {
     reach_m[0] = out[1]; reach_m[1] = out[2];
     reach_d[0] = out[3]; reach_d[1] = out[4];
     setup_ghosts(km.d, g.bcA, reach_m, gh_m, ghm);
-    if (p.has_torque) setup_ghosts(kd.d, g.bcB, reach_d, gh_d, ghd);
+    if (p.has_torque) setup_ghosts(kd.d, reg ? g.bcA : g.bcB, reach_d, gh_d, ghd);
     positioned = true;
   }
 
@@ -363,7 +373,8 @@ struct Engine : EngineBase {
 
   template <typename RF>
   void spread_stage(const RF *F, const RF *T, cudaStream_t s) {
-    spread_into<RF>(F, T, grid.as<R>(), ghm, ghd, s);
+    // regular-kernel torques are curled in wavenumber space: the grid holds the forces only
+    spread_into<RF>(F, reg ? nullptr : T, grid.as<R>(), ghm, ghd, s);
   }
 
   // spread F (+ the torque curl) into the grid gr with the ghost layers gm, gd
@@ -497,18 +508,7 @@ struct Engine : EngineBase {
     ef.ks = ks;
     DPST_CUDA(zgemm((R *)sp, Tf.as<R>(), ef, false, s));
     mark(3, s);
-    if (!use_static_scratch) {
-      DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
-    } else {
-      bool too_big = false;
-      cudaError_t e = launch_bvp_noalloc<R>(ks, (R *)sp, corr.as<double2>(), bvp_grid, s, &too_big);
-      if (too_big)
-        throw Error(DPST_ERR_UNSUPPORTED,
-                    "dpst_mdot_noalloc: one CTA of the solve needs nz*192 = " + std::to_string(nz * 192) +
-                        " doubles of scratch, more than the static array's " +
-                        std::to_string(noalloc_scratch_bytes() / sizeof(double)));
-      DPST_CUDA(e);
-    }
+    bvp_stage(sp, s);
     mark(4, s);
     EpiArgs eb = ef;
     eb.inverse = 1;
@@ -526,6 +526,10 @@ struct Engine : EngineBase {
 
   template <typename RF>
   void run(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    if (reg) {
+      run_reg<RF>(F, T, V, W, s);
+      return;
+    }
     const bool torque = p.has_torque && T != nullptr;
     R *gr = grid.as<R>();
     mark(0, s);
@@ -539,6 +543,115 @@ struct Engine : EngineBase {
       const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
       for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
     }
+  }
+
+  // ---- regular-kernel torque coupling (DPST_TORQUE_REG) ----------------------
+  // The reference's useRegKernel path (FCM.py:372-396, 427-439): the torques
+  // spread with the regular kernel of (w_d, beta_d, alpha_d) into their own
+  // grid (BC set A, its own open-end ghost layers); after the forward
+  // transforms, 1/2 curl of the torque coefficients is added to the forces'
+  // (k_spec_curl); the solve; the inverse z transform with the wall
+  // correction gives the velocity nodes; their copy is transformed forward
+  // again (coefficients of the corrected velocity, as the reference's U_hat),
+  // replaced by 1/2 curl (the vorticity, Solvers.py:159-177) and transformed
+  // back without correction; both go through the inverse x-y FFT; V is
+  // interpolated with the monopole kernel, Omega with the regular dipole
+  // kernel from the vorticity grid and the torque grid's ghost layers.
+  template <typename RF>
+  void run_reg(const RF *F, const RF *T, RF *V, RF *W, cudaStream_t s) {
+    const bool torque = T != nullptr;
+    R *gr = grid.as<R>(), *gt = gridT.as<R>();
+    CR *sp = spec.as<CR>(), *st = specT.as<CR>();
+    mark(0, s);
+    spread_into<RF>(F, nullptr, gr, ghm, ghd, s);  // also clears the torque ghost layers
+    if (torque) {
+      DPST_CUDA(cudaMemsetAsync(gt, 0, gridT.bytes, s));
+      launch_spread<R, RF>(false, T, N, kd.d, g, std_, gt, ghd, s, perm.as<int>());
+      launch_ghost_fold<R>(ghd.top, ghd.ntop, nx, ny, kd.d, s);
+      launch_ghost_fold<R>(ghd.bot, ghd.nbot, nx, ny, kd.d, s);
+      DPST_CUDA(cudaGetLastError());
+    }
+    mark(1, s);
+    DPST_CUFFT(cufftSetStream(plan_f, s));
+    exec_fwd(gr, sp);
+    if (torque) exec_fwd(gt, st);
+    mark(2, s);
+    EpiArgs ef;
+    memset(&ef, 0, sizeof(ef));
+    ef.inverse = 0;
+    ef.scale = 1.0;
+    ef.ks = ks;
+    DPST_CUDA(zgemm((R *)sp, Tf.as<R>(), ef, false, s));
+    if (torque) {
+      DPST_CUDA(zgemm((R *)st, Tf.as<R>(), ef, false, s));
+      launch_spec_curl<R>((const R *)st, (R *)sp, true, nz, nk, nx, ny, nxh, kvx.as<double>(), kvy.as<double>(),
+                          H, s);
+      DPST_CUDA(cudaGetLastError());
+    }
+    mark(3, s);
+    bvp_stage(sp, s);
+    mark(4, s);
+    EpiArgs eb = ef;
+    eb.inverse = 1;
+    eb.scale = 1.0 / ((double)nx * (double)ny);
+    epi_corr(eb);
+    DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
+    DPST_CUDA(cudaMemcpyAsync(st, sp, spec.bytes, cudaMemcpyDeviceToDevice, s));
+    DPST_CUDA(zgemm((R *)st, Tf.as<R>(), ef, false, s));
+    launch_spec_curl<R>((const R *)st, (R *)st, false, nz, nk, nx, ny, nxh, kvx.as<double>(), kvy.as<double>(), H,
+                        s);
+    DPST_CUDA(cudaGetLastError());
+    EpiArgs ew = ef;
+    ew.inverse = 1;
+    ew.ks.mode = 0;  // no wall correction: it is in the coefficients already
+    DPST_CUDA(zgemm((R *)st, Ti.as<R>(), ew, true, s));
+    mark(5, s);
+    DPST_CUFFT(cufftSetStream(plan_b, s));
+    exec_inv(sp, gr);
+    exec_inv(st, gt);
+    mark(6, s);
+    launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
+    if (W != nullptr) {
+      Ghosts<R> gz = ghd;
+      if (!torque) { gz.top = nullptr; gz.bot = nullptr; }
+      launch_interp<R, RF>(false, gt, N, kd.d, g, std_, gz, W, s, perm.as<int>());
+    }
+    DPST_CUDA(cudaGetLastError());
+    mark(7, s);
+    if (stage_ms) {
+      DPST_CUDA(cudaEventSynchronize(ev[7]));
+      const int from[8] = {0, 1, 2, 3, 4, 5, 6, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
+      for (int k = 0; k < 8; ++k) DPST_CUDA(cudaEventElapsedTime(&stage_ms[k], ev[from[k]], ev[to[k]]));
+    }
+  }
+
+  // per-wavenumber solve (+ k = 0) on the spectrum sp, in place
+  void bvp_stage(CR *sp, cudaStream_t s) {
+    if (!use_static_scratch) {
+      DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
+    } else {
+      bool too_big = false;
+      cudaError_t e = launch_bvp_noalloc<R>(ks, (R *)sp, corr.as<double2>(), bvp_grid, s, &too_big);
+      if (too_big)
+        throw Error(DPST_ERR_UNSUPPORTED,
+                    "dpst_mdot_noalloc: one CTA of the solve needs nz*192 = " + std::to_string(nz * 192) +
+                        " doubles of scratch, more than the static array's " +
+                        std::to_string(noalloc_scratch_bytes() / sizeof(double)));
+      DPST_CUDA(e);
+    }
+  }
+
+  void exec_fwd(R *gr, CR *sp) {
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
+    else
+      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
+  }
+  void exec_inv(CR *sp, R *gr) {
+    if (sizeof(R) == 8)
+      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
+    else
+      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
   }
 
   // interpolate V (and, with W, the angular velocities) from the grid gr with
@@ -677,6 +790,15 @@ struct Engine : EngineBase {
     if (K < 1) throw Error(DPST_ERR_INVALID_ARG, "K must be at least 1");
     if (N == 0) return;
     if (F == nullptr || V == nullptr) throw Error(DPST_ERR_INVALID_ARG, "F and V must not be NULL");
+    if (reg) {  // one Mdot per column
+      if (dtype != DPST_F64 && dtype != DPST_F32)
+        throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
+      const size_t col = 3 * (size_t)N * (dtype == DPST_F64 ? 8 : 4);
+      for (int k = 0; k < K; ++k)
+        mdot((const char *)F + k * col, T ? (const char *)T + k * col : nullptr, (char *)V + k * col,
+             W ? (char *)W + k * col : nullptr, dtype, s);
+      return;
+    }
     if (dtype == DPST_F64)
       run_multi<double>(K, (const double *)F, (const double *)T, (double *)V, (double *)W, s);
     else if (dtype == DPST_F32)
@@ -839,6 +961,8 @@ struct Engine : EngineBase {
     if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
     if (N == 0) return;
     if (gV == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gV must not be NULL");
+    if (reg)
+      throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the derivative-kernel torque coupling");
     if (gX != nullptr && F == nullptr)
       throw Error(DPST_ERR_INVALID_ARG, "the position gradient needs the forces F of the forward call");
     if (gW != nullptr && !p.has_torque)
@@ -894,12 +1018,15 @@ struct Engine : EngineBase {
     o->ztransform_inverse_ms[1] = ztc_ms[1][1];
     const int particle_passes = (p.has_torque && !fused) ? 2 : 1;
     o->kernels_per_mdot = particle_passes + 2 * nbuf + 1 + 2 + 1 + particle_passes;
+    // regular-kernel torques: + the torques' forward z transform and curl, the
+    // vorticity's forward z transform, curl and inverse z transform
+    if (reg) o->kernels_per_mdot += 5;
     o->fused_particle_passes = fused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
                            &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm,
-                           &corrf, &cmode, &znf};
+                           &corrf, &cmode, &znf, &gridT, &specT};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;

@@ -450,6 +450,75 @@ template cudaError_t launch_zgemm_b<float>(const ZSeg<float> *, const int64_t *,
 template cudaError_t launch_zgemm_b<double>(const ZSeg<double> *, const int64_t *, int, int64_t, int,
                                             const double *, int, cudaStream_t, bool);
 
+// ---------------------------------------------------------------------------
+// Spectral curl of a 3-component field in x-y Fourier / z Chebyshev
+// coefficients (the regular-kernel torque coupling, FCM.py:372-396 and
+// Solvers.py:159-177):
+//   c = 1/2 (Dy Sz - dz Sy, dz Sx - Dx Sz, Dx Sy - Dy Sx),
+// D = i k with the unpaired Nyquist line of an even axis zeroed
+// (Solvers.py:300-304), dz the downward coefficient recurrence of
+// chebCoeffDiff_perm (Chebyshev.py:68-94) on [a, a + 2H]:
+//   (dz S)_m = (dz S)_{m+2} + (2/H)(m+1) S_{m+1},  (dz S)_{nz-1} = 0, then / 2 at m = 0.
+// ACC: dst += c (the torque curl added to the forces' coefficients); else
+// dst = c (the vorticity; dst may alias src: level m is read before it is
+// written and the recurrence only looks at levels above).  One thread per
+// wavenumber; spectrum layout [3][nz][nk] complex.
+// ---------------------------------------------------------------------------
+template <typename R, bool ACC>
+__global__ void k_spec_curl(const R *src, R *dst, int nz, int64_t nk, int nx, int ny, int nxh,
+                            const double *__restrict__ kvx, const double *__restrict__ kvy, double H) {
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  const int ix = (int)(k % nxh), iy = (int)(k / nxh);
+  const R dx = (2 * ix == nx) ? (R)0 : (R)kvx[ix];
+  const R dy = (2 * iy == ny) ? (R)0 : (R)kvy[iy];
+  const R half = (R)0.5;
+  auto idx = [&](int d, int m) { return (((int64_t)d * nz + m) * nk + k) * 2; };
+  // f1: S at level m+1 (x, y); g1, g2: dz S at levels m+1, m+2
+  R fxr = 0, fxi = 0, fyr = 0, fyi = 0;
+  R gx1r = 0, gx1i = 0, gy1r = 0, gy1i = 0, gx2r = 0, gx2i = 0, gy2r = 0, gy2i = 0;
+  for (int m = nz - 1; m >= 0; --m) {
+    const R c = (R)(2.0 / H * (double)(m + 1));
+    R gxr = gx2r + c * fxr, gxi = gx2i + c * fxi;
+    R gyr = gy2r + c * fyr, gyi = gy2i + c * fyi;
+    gx2r = gx1r; gx2i = gx1i; gy2r = gy1r; gy2i = gy1i;
+    gx1r = gxr; gx1i = gxi; gy1r = gyr; gy1i = gyi;
+    if (m == 0) {
+      gxr /= 2; gxi /= 2; gyr /= 2; gyi /= 2;
+    }
+    const R sxr = src[idx(0, m)], sxi = src[idx(0, m) + 1];
+    const R syr = src[idx(1, m)], syi = src[idx(1, m) + 1];
+    const R szr = src[idx(2, m)], szi = src[idx(2, m) + 1];
+    // i dy Sz - dz Sy, dz Sx - i dx Sz, i dx Sy - i dy Sx
+    const R cxr = half * (-dy * szi - gyr), cxi = half * (dy * szr - gyi);
+    const R cyr = half * (gxr + dx * szi), cyi = half * (gxi - dx * szr);
+    const R czr = half * (-dx * syi + dy * sxi), czi = half * (dx * syr - dy * sxr);
+    fxr = sxr; fxi = sxi; fyr = syr; fyi = syi;
+    if (ACC) {
+      dst[idx(0, m)] += cxr; dst[idx(0, m) + 1] += cxi;
+      dst[idx(1, m)] += cyr; dst[idx(1, m) + 1] += cyi;
+      dst[idx(2, m)] += czr; dst[idx(2, m) + 1] += czi;
+    } else {
+      dst[idx(0, m)] = cxr; dst[idx(0, m) + 1] = cxi;
+      dst[idx(1, m)] = cyr; dst[idx(1, m) + 1] = cyi;
+      dst[idx(2, m)] = czr; dst[idx(2, m) + 1] = czi;
+    }
+  }
+}
+
+template <typename R>
+void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
+                      const double *kvx, const double *kvy, double H, cudaStream_t s) {
+  const int bs = 128;
+  const int64_t nb = (nk + bs - 1) / bs;
+  if (accumulate) k_spec_curl<R, true><<<nb, bs, 0, s>>>(src, dst, nz, nk, nx, ny, nxh, kvx, kvy, H);
+  else k_spec_curl<R, false><<<nb, bs, 0, s>>>(src, dst, nz, nk, nx, ny, nxh, kvx, kvy, H);
+}
+template void launch_spec_curl<float>(const float *, float *, bool, int, int64_t, int, int, int, const double *,
+                                      const double *, double, cudaStream_t);
+template void launch_spec_curl<double>(const double *, double *, bool, int, int64_t, int, int, int,
+                                       const double *, const double *, double, cudaStream_t);
+
 template cudaError_t launch_zgemm<float>(float *, int, int64_t, const float *, const EpiArgs &, int,
                                          cudaStream_t, bool);
 template cudaError_t launch_zgemm<double>(double *, int, int64_t, const double *, const EpiArgs &, int,

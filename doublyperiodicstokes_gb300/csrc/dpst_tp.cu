@@ -93,6 +93,64 @@ __global__ void k_tp_solve(typename Cplx<R>::T *__restrict__ spec, int64_t M, in
   u[2 * M] = c;
 }
 
+// The regular-kernel torque coupling (FCM.py:372-396, 427-439, Solvers.py:
+// 139-156): with torques, 1/2 curl of the torque spectrum t (tspec) is added
+// to the force spectrum first; after the solve, u goes to spec and the
+// vorticity 1/2 curl u to tspec (both scaled like u).  curl c = (Dy cz - Dz cy,
+// Dz cx - Dx cz, Dx cy - Dy cx) with the same zeroed Nyquist planes.
+template <typename R>
+__global__ void k_tp_solve_reg(typename Cplx<R>::T *__restrict__ spec, typename Cplx<R>::T *__restrict__ tspec,
+                               int torque, int64_t M, int nx, int ny, int nz, int nxh, const double *__restrict__ kvx,
+                               const double *__restrict__ kvy, const double *__restrict__ kvz, R eta, R scale) {
+  typedef typename Cplx<R>::T C;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= M) return;
+  C *u = spec + t, *w = tspec + t;
+  if (t == 0) {
+    const C z = {(R)0, (R)0};
+    u[0] = z; u[M] = z; u[2 * M] = z;
+    w[0] = z; w[M] = z; w[2 * M] = z;
+    return;
+  }
+  const int ix = (int)(t % nxh);
+  const int64_t r = t / nxh;
+  const int iy = (int)(r % ny), iz = (int)(r / ny);
+  const R kx = (R)__ldg(kvx + ix), ky = (R)__ldg(kvy + iy), kz = (R)__ldg(kvz + iz);
+  const R dx = (2 * ix == nx) ? (R)0 : kx;
+  const R dy = (2 * iy == ny) ? (R)0 : ky;
+  const R dz = (2 * iz == nz) ? (R)0 : kz;
+  const R ksq = kx * kx + ky * ky + kz * kz;
+  const R half = (R)0.5;
+  // 1/2 curl of (a, b, c) with D = i k: i (dy c - dz b, dz a - dx c, dx b - dy a) / 2
+  auto curl = [&](const C &a, const C &b, const C &c, C &x, C &y, C &z) {
+    x.x = half * (-dy * c.y - (-dz * b.y)); x.y = half * (dy * c.x - dz * b.x);
+    y.x = half * (-dz * a.y - (-dx * c.y)); y.y = half * (dz * a.x - dx * c.x);
+    z.x = half * (-dx * b.y - (-dy * a.y)); z.y = half * (dx * b.x - dy * a.x);
+  };
+  C f = u[0], g = u[M], h = u[2 * M];
+  if (torque) {
+    C cx, cy, cz;
+    curl(w[0], w[M], w[2 * M], cx, cy, cz);
+    f.x += cx.x; f.y += cx.y;
+    g.x += cy.x; g.y += cy.y;
+    h.x += cz.x; h.y += cz.y;
+  }
+  const R pr = (dx * f.y + dy * g.y + dz * h.y) / ksq;
+  const R pi = -(dx * f.x + dy * g.x + dz * h.x) / ksq;
+  const R v = scale / (eta * ksq);
+  C a, b, c;
+  a.x = v * (f.x + dx * pi);
+  a.y = v * (f.y - dx * pr);
+  b.x = v * (g.x + dy * pi);
+  b.y = v * (g.y - dy * pr);
+  c.x = v * (h.x + dz * pi);
+  c.y = v * (h.y - dz * pr);
+  u[0] = a; u[M] = b; u[2 * M] = c;
+  C ox, oy, oz;
+  curl(a, b, c, ox, oy, oz);
+  w[0] = ox; w[M] = oy; w[2 * M] = oz;
+}
+
 template <typename R>
 struct EngineTP : EngineBase {
   typedef typename std::conditional<sizeof(R) == 8, cufftDoubleComplex, cufftComplex>::type CR;
@@ -101,8 +159,10 @@ struct EngineTP : EngineBase {
   double hx, hy, hz, Lz;
   KernelHost km, kd;
   bool fused = false;
+  bool reg = false;  // torques with the regular kernel and spectral curls (DPST_TORQUE_REG)
   GridArgs g;
   DevBuf grid, spec, kvx, kvy, kvz, pos64, flags, ord_count, ord_start, perm, dphzw_buf;
+  DevBuf gridT, specT;  // reg: torque grid and spectrum, then the vorticity's
   DevBuf st_m[8], st_d[8];
   Stencils<R> stm, std_;
   Ghosts<R> none;  // no ghost layers: z wraps
@@ -125,8 +185,10 @@ struct EngineTP : EngineBase {
     Lz = p.zmax - p.zmin;
     hz = Lz / nz;
     km = make_kernel_tp(p.w, p.beta, p.alpha, false, hx, hy, hz, nx, ny, nz, "monopole kernel");
-    if (p.has_torque) kd = make_kernel_tp(p.w_d, p.beta_d, p.alpha_d, true, hx, hy, hz, nx, ny, nz, "dipole kernel");
-    fused = p.has_torque && fused_supports(km.d, kd.d);
+    reg = p.has_torque && p.torque_kernel == DPST_TORQUE_REG;
+    if (p.has_torque)
+      kd = make_kernel_tp(p.w_d, p.beta_d, p.alpha_d, !reg, hx, hy, hz, nx, ny, nz, "dipole kernel");
+    fused = p.has_torque && !reg && fused_supports(km.d, kd.d);
     memset(&g, 0, sizeof(g));
     g.nx = nx; g.ny = ny; g.nz = nz;
     g.hx = hx; g.hy = hy; g.Lx = p.Lx; g.Ly = p.Ly; g.Lz = Lz;
@@ -140,7 +202,11 @@ struct EngineTP : EngineBase {
     pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
     flags.alloc(sizeof(int) * 8);
     alloc_stencils(km.d, false, st_m, stm);
-    if (p.has_torque) alloc_stencils(kd.d, true, st_d, std_);
+    if (p.has_torque) alloc_stencils(kd.d, !reg, st_d, std_);
+    if (reg) {
+      gridT.alloc(grid.bytes);
+      specT.alloc(spec.bytes);
+    }
     ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
     ord_start.alloc(sizeof(int) * (tile_order_tiles(nx, ny) + 1));
     perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
@@ -199,7 +265,7 @@ struct EngineTP : EngineBase {
     int *fl = flags.as<int>();
     DPST_CUDA(cudaMemcpyAsync(fl, init, sizeof(init), cudaMemcpyHostToDevice, s));
     launch_locate<R>(false, pos64.as<double>(), N, km.d, nullptr, nullptr, g, stm, fl, fl + 1, s);
-    if (p.has_torque) launch_locate<R>(true, pos64.as<double>(), N, kd.d, nullptr, nullptr, g, std_, fl, fl + 3, s);
+    if (p.has_torque) launch_locate<R>(!reg, pos64.as<double>(), N, kd.d, nullptr, nullptr, g, std_, fl, fl + 3, s);
     DPST_CUDA(cudaGetLastError());
     launch_tile_order<R>(N, g, stm, ord_count.as<int>(), ord_start.as<int>(), perm.as<int>(), s);
     DPST_CUDA(cudaGetLastError());
@@ -227,7 +293,13 @@ struct EngineTP : EngineBase {
     R *gr = grid.as<R>();
     const bool torque = p.has_torque && T != nullptr;
     DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
-    if (torque && fused) {
+    if (reg) {  // the torques go to their own grid with the regular kernel
+      launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, none, s, perm.as<int>());
+      if (torque) {
+        DPST_CUDA(cudaMemsetAsync(gridT.p, 0, gridT.bytes, s));
+        launch_spread<R, RF>(false, T, N, kd.d, g, std_, gridT.as<R>(), none, s, perm.as<int>());
+      }
+    } else if (torque && fused) {
       launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, none, none, s, perm.as<int>());
     } else {
       launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, none, s, perm.as<int>());
@@ -236,28 +308,45 @@ struct EngineTP : EngineBase {
     DPST_CUDA(cudaGetLastError());
   }
 
-  void solve_stage(cudaStream_t s) {
-    R *gr = grid.as<R>();
-    CR *sp = spec.as<CR>();
-    DPST_CUFFT(cufftSetStream(plan_f, s));
+  void exec_fwd(R *gr, CR *sp) {
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
     else
       DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
-    mark(2, s);
-    mark(3, s);  // no z transform in this mode
-    const int bs = 256;
-    k_tp_solve<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<typename Cplx<R>::T *>(sp), M, nx, ny, nz,
-                                                  nxh, kvx.as<double>(), kvy.as<double>(), kvz.as<double>(),
-                                                  (R)p.viscosity, (R)(1.0 / ((double)nx * ny * nz)));
-    DPST_CUDA(cudaGetLastError());
-    mark(4, s);
-    mark(5, s);
-    DPST_CUFFT(cufftSetStream(plan_b, s));
+  }
+  void exec_inv(CR *sp, R *gr) {
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
     else
       DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
+  }
+
+  // torque: the torque grid holds spread torques (regular-kernel coupling)
+  void solve_stage(bool torque, cudaStream_t s) {
+    R *gr = grid.as<R>();
+    CR *sp = spec.as<CR>();
+    DPST_CUFFT(cufftSetStream(plan_f, s));
+    exec_fwd(gr, sp);
+    if (reg && torque) exec_fwd(gridT.as<R>(), specT.as<CR>());
+    mark(2, s);
+    mark(3, s);  // no z transform in this mode
+    const int bs = 256;
+    typedef typename Cplx<R>::T C;
+    if (reg)
+      k_tp_solve_reg<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<C *>(sp), specT.as<C>(), torque ? 1 : 0, M,
+                                                        nx, ny, nz, nxh, kvx.as<double>(), kvy.as<double>(),
+                                                        kvz.as<double>(), (R)p.viscosity,
+                                                        (R)(1.0 / ((double)nx * ny * nz)));
+    else
+      k_tp_solve<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<C *>(sp), M, nx, ny, nz, nxh, kvx.as<double>(),
+                                                    kvy.as<double>(), kvz.as<double>(), (R)p.viscosity,
+                                                    (R)(1.0 / ((double)nx * ny * nz)));
+    DPST_CUDA(cudaGetLastError());
+    mark(4, s);
+    mark(5, s);
+    DPST_CUFFT(cufftSetStream(plan_b, s));
+    exec_inv(sp, gr);
+    if (reg) exec_inv(specT.as<CR>(), gridT.as<R>());
     mark(6, s);
   }
 
@@ -265,7 +354,10 @@ struct EngineTP : EngineBase {
   void interp_stage(bool torque, RF *V, RF *W, cudaStream_t s) {
     const R *gr = grid.as<R>();
     (void)torque;
-    if (p.has_torque && W != nullptr) {
+    if (reg) {  // V from the velocity grid, Omega from the vorticity grid (regular kernels)
+      launch_interp<R, RF>(false, gr, N, km.d, g, stm, none, V, s, perm.as<int>());
+      if (W != nullptr) launch_interp<R, RF>(false, gridT.as<R>(), N, kd.d, g, std_, none, W, s, perm.as<int>());
+    } else if (p.has_torque && W != nullptr) {
       if (fused) {
         launch_interp_fused<R, RF>(gr, N, km.d, kd.d, g, stm, std_, none, none, V, W, s, perm.as<int>());
       } else {
@@ -284,7 +376,7 @@ struct EngineTP : EngineBase {
     mark(0, s);
     spread_stage<RF>(F, T, s);
     mark(1, s);
-    solve_stage(s);
+    solve_stage(torque, s);
     interp_stage<RF>(torque, V, W, s);
     mark(7, s);
     if (stage_ms) {
@@ -340,6 +432,7 @@ struct EngineTP : EngineBase {
 
   void backward(const void *, const void *, const void *, const void *, void *, void *, void *, int,
                 cudaStream_t) override {
+    // (neither coupling of the torques has a backward pass in this mode)
     throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the NOWALL, BOTTOM and SLIT geometries");
   }
 
@@ -363,7 +456,8 @@ struct EngineTP : EngineBase {
     o->kernels_per_mdot = particle_passes + 1 + particle_passes;
     o->fused_particle_passes = fused ? 1 : 0;
     int64_t b = 0;
-    const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf};
+    const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf,
+                           &gridT, &specT};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     o->device_bytes = b;
