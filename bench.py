@@ -474,6 +474,47 @@ def run_periodic(args, dev):
     return out
 
 
+def run_regkernel(args, dev):
+    """The regular-kernel torque coupling (the reference's useRegKernel) on c2
+    and t1, mixed: device milliseconds per Mdot and the CUDA-event stage split,
+    beside the derivative-kernel coupling on the same inputs."""
+    import dataclasses
+    import torch
+    from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = max(3, min(args.steps, 10))
+    out = []
+    for base in (W.C2, W.T1):
+        X, F, T = W.make_inputs(base)
+        row = {"workload": base.name, "precision": "mixed"}
+        for reg in (False, True):
+            w = dataclasses.replace(base, reg_kernel=reg)
+            op = DPStokes(StokesParams.from_workload(w, "mixed"), w.N, device=dev)
+            op.set_positions(torch.tensor(X, device=dev))
+            Fd = torch.tensor(F, dtype=torch.float32, device=dev)
+            Td = torch.tensor(T, dtype=torch.float32, device=dev)
+            V, Wd = torch.empty_like(Fd), torch.empty_like(Fd)
+            for _ in range(max(3, args.warmup)):
+                op.mdot(Fd, Td, out=(V, Wd))
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                op.mdot(Fd, Td, out=(V, Wd))
+            e1.record()
+            torch.cuda.synchronize()
+            key = "reg_kernel" if reg else "deriv_kernel"
+            row[key + "_ms"] = e0.elapsed_time(e1) / reps
+            if reg:
+                runs = [op.mdot_timed(Fd, Td)[2] for _ in range(reps)]
+                row["reg_kernel_stages_ms"] = {k: round(statistics.median([r[k] for r in runs]), 4)
+                                               for k in runs[0]}
+                row["reg_kernel_particles_per_s"] = w.N / (row[key + "_ms"] / 1e3)
+            op.close()
+        out.append(row)
+    return out
+
+
 def cpu_baseline(w):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
@@ -505,10 +546,18 @@ def main():
     ap.add_argument("--skip-periodic", action="store_true")
     ap.add_argument("--only-periodic", action="store_true",
                     help="time only the triply periodic Mdot (t1_tp_n65536)")
+    ap.add_argument("--skip-regkernel", action="store_true")
+    ap.add_argument("--only-regkernel", action="store_true",
+                    help="time only the regular-kernel torque coupling (c2, t1)")
     ap.add_argument("--skip-multi", action="store_true")
     ap.add_argument("--only-multi", action="store_true",
                     help="time only the multi-RHS Mdot (c0 K = 16, c2 K = 4)")
     args = ap.parse_args()
+    if args.only_regkernel:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"reg_kernel": run_regkernel(args, dev)}), flush=True)
+        return
     if args.only_periodic:
         import torch
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -581,6 +630,9 @@ def main():
     if not args.skip_multi:
         import torch
         line["multi_rhs"] = run_multi_rhs(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
+    if not args.skip_regkernel:
+        import torch
+        line["reg_kernel"] = run_regkernel(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))
     if not args.skip_periodic:
         import torch
         line["periodic"] = run_periodic(args, torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))))

@@ -550,11 +550,11 @@ struct Engine : EngineBase {
   // spread with the regular kernel of (w_d, beta_d, alpha_d) into their own
   // grid (BC set A, its own open-end ghost layers); after the forward
   // transforms, 1/2 curl of the torque coefficients is added to the forces'
-  // (k_spec_curl); the solve; the inverse z transform with the wall
-  // correction gives the velocity nodes; their copy is transformed forward
-  // again (coefficients of the corrected velocity, as the reference's U_hat),
-  // replaced by 1/2 curl (the vorticity, Solvers.py:159-177) and transformed
-  // back without correction; both go through the inverse x-y FFT; V is
+  // (k_spec_curl); the solve; the vorticity 1/2 curl u (Solvers.py:159-177)
+  // of the solution's coefficients (open domain) or, with walls, of the
+  // corrected velocity's coefficients (the reference's U_hat: the velocity
+  // nodes with the wall correction transformed forward again); both go
+  // through the inverse z and x-y transforms; V is
   // interpolated with the monopole kernel, Omega with the regular dipole
   // kernel from the vorticity grid and the torque grid's ghost layers.
   template <typename RF>
@@ -595,16 +595,28 @@ struct Engine : EngineBase {
     eb.inverse = 1;
     eb.scale = 1.0 / ((double)nx * (double)ny);
     epi_corr(eb);
-    DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
-    DPST_CUDA(cudaMemcpyAsync(st, sp, spec.bytes, cudaMemcpyDeviceToDevice, s));
-    DPST_CUDA(zgemm((R *)st, Tf.as<R>(), ef, false, s));
-    launch_spec_curl<R>((const R *)st, (R *)st, false, nz, nk, nx, ny, nxh, kvx.as<double>(), kvy.as<double>(), H,
-                        s);
-    DPST_CUDA(cudaGetLastError());
     EpiArgs ew = ef;
     ew.inverse = 1;
-    ew.ks.mode = 0;  // no wall correction: it is in the coefficients already
-    DPST_CUDA(zgemm((R *)st, Ti.as<R>(), ew, true, s));
+    ew.ks.mode = 0;  // the vorticity's inverse transform adds no wall correction
+    if (p.mode == DPST_MODE_NOWALL) {
+      // no correction: the vorticity straight from the solution's coefficients
+      launch_spec_curl<R>((const R *)sp, (R *)st, false, nz, nk, nx, ny, nxh, kvx.as<double>(), kvy.as<double>(),
+                          H, s);
+      DPST_CUDA(cudaGetLastError());
+      DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
+      ew.scale = eb.scale;
+      DPST_CUDA(zgemm((R *)st, Ti.as<R>(), ew, true, s));
+    } else {
+      // walls: the correction is added at the nodes; the corrected velocity's
+      // coefficients (the reference's U_hat) come from transforming them forward
+      DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
+      DPST_CUDA(cudaMemcpyAsync(st, sp, spec.bytes, cudaMemcpyDeviceToDevice, s));
+      DPST_CUDA(zgemm((R *)st, Tf.as<R>(), ef, false, s));
+      launch_spec_curl<R>((const R *)st, (R *)st, false, nz, nk, nx, ny, nxh, kvx.as<double>(), kvy.as<double>(),
+                          H, s);
+      DPST_CUDA(cudaGetLastError());
+      DPST_CUDA(zgemm((R *)st, Ti.as<R>(), ew, true, s));
+    }
     mark(5, s);
     DPST_CUFFT(cufftSetStream(plan_b, s));
     exec_inv(sp, gr);
@@ -1020,7 +1032,7 @@ struct Engine : EngineBase {
     o->kernels_per_mdot = particle_passes + 2 * nbuf + 1 + 2 + 1 + particle_passes;
     // regular-kernel torques: + the torques' forward z transform and curl, the
     // vorticity's forward z transform, curl and inverse z transform
-    if (reg) o->kernels_per_mdot += 5;
+    if (reg) o->kernels_per_mdot += (p.mode == DPST_MODE_NOWALL) ? 4 : 5;
     o->fused_particle_passes = fused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,

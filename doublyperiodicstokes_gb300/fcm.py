@@ -33,12 +33,14 @@ class FCMJoint:
     def Initialize(self, numberParticles, hydrodynamicRadius, viscosity, domType, has_torque,
                    xmax, ymax, zmin, zmax, xmin=0, ymin=0, kernType=0, optInd=0, ref=False, *,
                    nx=None, ny=None, nz=None, w=6, beta_hat=None, w_d=6, beta_d_hat=2.2160, z0=None,
-                   precision="fp64"):
+                   precision="fp64", useRegKernel=False):
         """FCMJoint.Initialize.  With nx = None the grid and kernels are the
         reference's choice for (hydrodynamicRadius, kernType, optInd, ref);
         otherwise nx, ny, nz, w, beta_hat (default: the reference's w = 6
         value, 1.714 without torques, 1.3267 with), w_d, beta_d_hat and z0
-        are taken as given."""
+        are taken as given.  useRegKernel selects the reference FCM's
+        regular-kernel torque coupling (FCM.Initialize's argument of that
+        name) instead of the derivative kernels."""
         if domType not in _MODE:
             raise ValueError("domType must be DP, DPBW, DPSC or TP")
         self.Clean()
@@ -69,7 +71,8 @@ class FCMJoint:
         self.params = StokesParams(mode=_MODE[domType], nx=int(nx), ny=int(ny), nz=int(nz), Lx=Lx, Ly=Ly,
                                    zmin=self.z0, zmax=self.z0 + Lz, viscosity=viscosity, w=w,
                                    beta=beta_hat * w, alpha=a, has_torque=self.has_torque, w_d=w_d,
-                                   beta_d=beta_d_hat * w_d, alpha_d=ad, precision=precision)
+                                   beta_d=beta_d_hat * w_d, alpha_d=ad, precision=precision,
+                                   reg_kernel=bool(useRegKernel))
         self.precision = np.float64 if precision == "fp64" else np.float32
         self.op = DPStokes(self.params, self.N)
 
