@@ -46,6 +46,7 @@ class Workload:
     radius: float = 1.0
     seed: int = 0
     reg_kernel: bool = False  # torques with the regular kernel and spectral curls (useRegKernel)
+    layout: str = "uniform"   # particle positions: 'uniform' or 'edge' (edge_positions)
 
     def oracle_params(self):
         """Keyword arguments of the oracle's Params (same field meanings)."""
@@ -58,13 +59,44 @@ class Workload:
         return asdict(self)
 
 
+def edge_positions(w: Workload, rng):
+    """w.N positions at the edges of the unit cell and the grid: the cell's
+    corner and z ends exactly (walls, open ends, the periodic seam), grid
+    nodes exactly (x, y nodes; z Chebyshev nodes or uniform nodes),
+    half-cell points (the rounding tie of odd-width stencils), two
+    particles at one position, one just inside each z end; the rest uniform.
+    x and y stay below Lx, Ly, and z below the top of a triply periodic
+    box (at x = Lx, y = Ly or, uniform z with an even stencil, z = zmax the
+    reference indexes past its extended grid; the wrapped seam is covered by
+    the points at 0)."""
+    hx, hy = w.Lx / w.nx, w.Ly / w.ny
+    a, b = w.z0, w.z0 + w.Lz
+    if w.domType == "TP":
+        zn = w.z0 + np.arange(w.nz) * (w.Lz / w.nz)
+    else:  # Chebyshev nodes on [z0, z0 + Lz] (Chebyshev.py:4-38)
+        zn = w.z0 + w.Lz / 2 * np.cos(np.pi * np.arange(w.nz) / (w.nz - 1)) + w.Lz / 2
+    top = b - 0.25 * (w.Lz / w.nz) if w.domType == "TP" else b
+    pts = [(0.0, 0.0, a), (0.5 * hx, w.Ly - 0.25 * hy, top), (w.Lx / 2, w.Ly / 2, zn[2]),
+           (w.Lx / 2, w.Ly / 2, zn[2]), (3 * hx, 5 * hy, zn[len(zn) // 2]), (2.5 * hx, 7.5 * hy, a + 0.3),
+           (w.Lx - 0.5 * hx, 4 * hy, b - 0.3), (7 * hx, 0.0, zn[-3]), (0.0, 9.5 * hy, (a + b) / 2)]
+    X = np.array(pts[:w.N], dtype=np.float64)
+    n = w.N - X.shape[0]
+    if n > 0:
+        R = np.stack([rng.uniform(0.0, w.Lx, n), rng.uniform(0.0, w.Ly, n), rng.uniform(a, b, n)], axis=1)
+        X = np.concatenate([X, R])
+    return X
+
+
 def make_inputs(w: Workload, dtype=np.float64):
     """Seeded synthetic positions [N,3], forces [N,3], torques [N,3] (or None)."""
     rng = np.random.default_rng(w.seed)
-    x = rng.uniform(0.0, w.Lx, w.N)
-    y = rng.uniform(0.0, w.Ly, w.N)
-    z = rng.uniform(w.zlo, w.zhi, w.N)
-    X = np.stack([x, y, z], axis=1)
+    if w.layout == "edge":
+        X = edge_positions(w, rng)
+    else:
+        x = rng.uniform(0.0, w.Lx, w.N)
+        y = rng.uniform(0.0, w.Ly, w.N)
+        z = rng.uniform(w.zlo, w.zhi, w.N)
+        X = np.stack([x, y, z], axis=1)
     F = rng.standard_normal((w.N, 3))
     T = rng.standard_normal((w.N, 3)) if w.has_torque else None
     if dtype != np.float64:
@@ -171,7 +203,20 @@ SMALL_TP = [
 # shifted z origin.
 SMALL_REG = [replace(w, name=w.name.replace("s_", "s_reg_", 1), reg_kernel=True) for w in SMALL + SMALL_TP
              if w.name in ("s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_t_odd", "s_dp_t_shift", "s_tp_t", "s_tp_t_hz")]
-SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP + SMALL_REG}
+# Edge positions (edge_positions) in every geometry, with torques, an odd
+# kernel width and the regular-kernel coupling among them.
+SMALL_EDGE = [
+    replace(small("e_dpbw_t", "DPBW", 16, 16, 17, 10.0, 0.0, 10.0, True, seed=12), layout="edge"),
+    replace(small("e_dpsc_t", "DPSC", 16, 16, 21, 10.0, 0.0, 10.0, True, seed=13), layout="edge"),
+    replace(small("e_dp_f", "DP", 14, 16, 19, 12.4, 0.0, 12.4, False, seed=14), layout="edge"),
+    replace(small("e_dp_t_shift", "DP", 16, 16, 25, 10.0, -5.0, 5.0, True, z0=-5.0, seed=15), layout="edge"),
+    replace(small("e_tp_t", "TP", 16, 16, 16, 16.0, 0.0, 16.0, True, seed=16), layout="edge"),
+    replace(small("e_tp_t_w5", "TP", 16, 17, 15, 15.0, 0.0, 15.0, True, seed=17), layout="edge",
+            wm=5, wd=5, betam_hat=1.3055, betad_hat=2.2320),
+    replace(small("e_dpbw_t_reg", "DPBW", 16, 16, 17, 10.0, 0.0, 10.0, True, seed=18), layout="edge",
+            reg_kernel=True),
+]
+SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP + SMALL_REG + SMALL_EDGE}
 
 
 def small_batch(domType, has_torque, seed=40):

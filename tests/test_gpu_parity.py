@@ -156,3 +156,22 @@ def test_fused_and_separate_particle_passes(base, wm, wd, fused):
     _, V32, W32 = _run(w, X, F, T, precision="mixed", dtype=torch.float32)
     assert rel_err(V32, V) < TOL_MIXED
     assert rel_err(W32, Wv) < TOL_MIXED
+
+
+@pytest.mark.parametrize("name", ["s_dpbw_t", "s_tp_t"])
+def test_periodic_seam_positions(name):
+    """A particle at x = Lx, y = Ly (and, triply periodic, z = zmax) is the
+    particle at 0 (the reference indexes past its extended grid there; this
+    operator wraps)."""
+    w = W.SMALL_BY_NAME[name]
+    X, F, T = W.make_inputs(w)
+    Xa, Xb = X.copy(), X.copy()
+    Xa[0, :2], Xb[0, :2] = 0.0, (w.Lx, w.Ly)
+    if w.domType == "TP":
+        Xa[1, 2], Xb[1, 2] = w.z0, w.z0 + w.Lz
+    _, Va, Wa = _run(w, Xa, F, T)
+    _, Vb, Wb = _run(w, Xb, F, T)
+    assert rel_err(Vb, Va) < 1e-13
+    assert rel_err(Wb, Wa) < 1e-13
+    Vo, Wo = O.mdot(O.Params(**w.oracle_params()), Xa, F, T)
+    assert rel_err(Va, Vo) < TOL_FP64

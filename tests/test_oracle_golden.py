@@ -7,8 +7,8 @@ import dpstokes_oracle as O
 import golden_io
 from conftest import rel_err
 
-SMALL = [n for n in golden_io.names() if n.startswith("s_")]
-FULL = [n for n in golden_io.names() if not n.startswith("s_")]
+SMALL = [n for n in golden_io.names() if n.startswith(("s_", "e_"))]
+FULL = [n for n in golden_io.names() if not n.startswith(("s_", "e_"))]
 
 
 def _check(name, tol):
