@@ -270,7 +270,18 @@ def run_ours(args, rank, world):
     if dom == "solve":
         # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
         roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "
-                        "its algorithmic bytes")
+                        "its algorithmic bytes; fp64_pipe gives its FP64 issue rate")
+        if w.domType != "TP":
+            # ~46 FP64 instructions per row per lane (2 lanes x nz rows per wavenumber;
+            # ncu's FP64 instruction count of the solve), at 2 FP64 lane-operations
+            # per clock per SM
+            nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = clocks.get("sm_mhz") or 2070.0
+            instr = (w.ny * (w.nx // 2 + 1) - 1) * 2 * w.nz * 46
+            rate = instr / (stages["solve"] * 1e-3)
+            peak = nsm * 2 * mhz * 1e6
+            roof["fp64_pipe"] = {"lane_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
+                                 "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
     extra["set_positions_ms"] = set_positions_ms
     return dict(value=value, ms_step=ms_step, e2e=e2e, stages=stages, info=info, extra=extra,
                 roofline=roof, clocks=clocks, w=w)
