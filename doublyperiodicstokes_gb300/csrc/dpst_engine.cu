@@ -10,7 +10,10 @@
 // Mdot pipeline:
 //   zero grid -> spread F (+ torque curl) -> [fold open-end ghost layers]
 //   -> x-y FFT -> z DCT-I -> per-k BVP -> inverse z DCT-I (+ wall correction)
-//   -> inverse x-y FFT -> interpolate V (+ W).
+//   -> inverse x-y FFT -> interpolate V (+ W);
+// with the regular-kernel torque coupling (run_reg) the torques take their
+// own grid and their curl and the vorticity are taken in wavenumber space.
+// The triply periodic mode has its own engine (dpst_tp.cu).
 #include <cuda_runtime.h>
 #include <cufft.h>
 

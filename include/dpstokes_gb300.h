@@ -4,8 +4,9 @@
  *
  * Computes [V; W] = M [F; T] for N blobs with exponential-of-semicircle (ES)
  * kernels in a domain periodic in x, y and open (no wall), bounded below by a
- * no-slip wall, or bounded by two no-slip walls in z.  Forces F, torques T,
- * linear velocities V and angular velocities W are [N][3] arrays.
+ * no-slip wall, or bounded by two no-slip walls in z, or periodic in z too
+ * (triply periodic).  Forces F, torques T, linear velocities V and angular
+ * velocities W are [N][3] arrays.
  *
  * Drop-in boundary.  Each entry point replaces one call of the reference's
  * interface for this path (paths are within stochasticHydroTools/
@@ -50,7 +51,8 @@
  *     UseCbeta convention gives alpha = w h / 2).  The dipole kernel
  *     (w_d, beta_d, alpha_d) spreads torques through the curl and
  *     interpolates the vorticity with kernel derivatives, as the reference
- *     CPU path does by default.
+ *     CPU path does by default; torque_kernel = DPST_TORQUE_REG selects its
+ *     regular-kernel coupling with spectral curls instead.
  */
 #ifndef DPSTOKES_GB300_H
 #define DPSTOKES_GB300_H

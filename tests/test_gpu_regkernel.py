@@ -145,3 +145,29 @@ def test_multi_columns_and_unsupported_calls():
     n = (ctypes.c_int64 * 1)(w.N)
     b = ctypes.c_void_p()
     assert L.dpst_batched_create(ctypes.byref(prm), n, 1, 0, ctypes.byref(b)) == 5  # DPST_ERR_UNSUPPORTED
+
+
+def test_fcmjoint_use_reg_kernel():
+    """FCMJoint.Initialize(..., useRegKernel=True) with the reference's grid
+    choice against the oracle on the same grid (bottom wall, torques)."""
+    from doublyperiodicstokes_gb300.fcm import FCMJoint
+    N, R, eta, L = 30, 1.0, 1.0 / (6 * np.pi), 24.0
+    rng = np.random.default_rng(21)
+    X = np.column_stack([rng.uniform(0, L, N), rng.uniform(0, L, N), rng.uniform(1.0, 9.0, N)])
+    F, T = rng.standard_normal((N, 3)), rng.standard_normal((N, 3))
+    fj = FCMJoint("gb300")
+    fj.Initialize(N, R, eta, "DPBW", True, L, L, 0.0, 10.0, useRegKernel=True)
+    p = fj.params
+    assert p.reg_kernel
+    fj.SetPositions(X.ravel())
+    MF, MT = fj.Mdot(F.ravel(), T.ravel())
+    h = p.Lx / p.nx
+    op = O.Params("DPBW", p.nx, p.ny, p.nz, p.Lx, p.Ly, p.zmax - p.zmin, z0=p.zmin, eta=eta, wm=p.w,
+                  betam_hat=p.beta / p.w, has_torque=True, wd=p.w_d, betad_hat=p.beta_d / p.w_d, radius=R,
+                  reg_kernel=True)
+    assert abs(op.alpha(p.w) - p.alpha) < 1e-12 * p.alpha and abs(h - op.hx) < 1e-15
+    Xs = X.copy()
+    Vo, Wo = O.mdot(op, Xs, F, T)
+    assert rel_err(MF, Vo) < TOL_FP64
+    assert rel_err(MT, Wo) < TOL_FP64
+    fj.Clean()

@@ -83,3 +83,20 @@ def test_oracle_tp_shift_invariance():
     V2, W2 = O.mdot(p, Xs, F, T)
     assert rel_err(V2, V1) < 1e-12
     assert rel_err(W2, W1) < 1e-12
+
+
+def test_edge_positions_inside_the_cell():
+    """Edge layouts keep x < Lx, y < Ly (and z < zmax in the triply periodic
+    box), and hit the z ends exactly where the reference allows it."""
+    from doublyperiodicstokes_gb300 import workloads as W
+    for w in W.SMALL_EDGE:
+        X, _, _ = W.make_inputs(w)
+        assert X.shape == (w.N, 3)
+        assert (X[:, 0] >= 0).all() and (X[:, 0] < w.Lx).all()
+        assert (X[:, 1] >= 0).all() and (X[:, 1] < w.Ly).all()
+        assert (X[:, 2] >= w.z0).all() and (X[:, 2] <= w.z0 + w.Lz).all()
+        assert (X[:, 2] == w.z0).any()
+        if w.domType == "TP":
+            assert (X[:, 2] < w.z0 + w.Lz).all()
+        else:
+            assert (X[:, 2] == w.z0 + w.Lz).any()
