@@ -36,7 +36,7 @@ class DpstInfo(ctypes.Structure):
                 ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int),
                 ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
                 ("fused_particle_passes", ctypes.c_int), ("ztransform_inverse", ctypes.c_int),
-                ("ztransform_inverse_ms", ctypes.c_float * 2)]
+                ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int)]
 
 
 class DpstBatchInfo(ctypes.Structure):

@@ -26,6 +26,7 @@
 #include <cufft.h>
 
 #include <climits>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -151,6 +152,176 @@ __global__ void k_tp_solve_reg(typename Cplx<R>::T *__restrict__ spec, typename 
   w[0] = ox; w[M] = oy; w[2 * M] = oz;
 }
 
+// ---------------------------------------------------------------------------
+// Fused z transform and solve (nz = R1 x R2, powers of two up to 64): after
+// the x-y real transforms of every z plane, one CTA takes ZF_CB consecutive
+// columns (kx, ky) of all three components into shared memory, transforms
+// each column along z (two passes of small DFTs in registers: n = R2 n1 +
+// n2, k = k1 + R1 k2; pass 1 DFT_R1 over n1 and the twiddle W^(n2 k1), pass
+// 2 DFT_R2 over n2, each thread writing back the slots it read, so the
+// spectrum ends in digit-reversed order: slot R2 k1 + k2 holds kz = k1 + R1
+// k2), solves every (kz, column) mode, transforms back in the reverse order
+// (unnormalised; the 1/(nx ny nz) is in the solve) and stores.  The same
+// arithmetic as the 3-D transform's z passes plus k_tp_solve, with one read
+// and one write of the spectrum instead of three of each.
+// ---------------------------------------------------------------------------
+constexpr int ZF_CB = 32;  // columns per CTA
+
+template <typename C>
+static __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
+template <typename C>
+static __device__ __forceinline__ C csub(C a, C b) { return C{a.x - b.x, a.y - b.y}; }
+template <typename C>
+static __device__ __forceinline__ C cmul(C a, C b) { return C{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+template <typename C>
+static __device__ __forceinline__ C cmulc(C a, C b) { return C{a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y}; }  // a conj(b)
+
+template <int N>
+static constexpr int bitrev(int i) {
+  int r = 0;
+  for (int b = 1; b < N; b <<= 1) r = (r << 1) | ((i & b) ? 1 : 0);
+  return r;
+}
+
+// In-place DFT of N (a power of two) values in registers, natural order in
+// and out; tw[m] = exp(-2 pi i m / NZ), stride = NZ / N.  INV: conjugate
+// twiddles (unnormalised inverse).  Iterative radix-2 with the input taken
+// in bit-reversed order (indices are compile-time constants).
+template <typename C, int N, bool INV>
+static __device__ __forceinline__ void dft_small(C (&v)[N], const C *__restrict__ tw, int stride) {
+  C u[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) u[i] = v[bitrev<N>(i)];
+#pragma unroll
+  for (int len = 2; len <= N; len <<= 1) {
+#pragma unroll
+    for (int i = 0; i < N; i += len) {
+#pragma unroll
+      for (int k = 0; k < len / 2; ++k) {
+        C b = u[i + k + len / 2];
+        if (k != 0) {  // W^0 = 1
+          const C w = tw[k * (N / len) * stride];
+          b = INV ? cmulc(b, w) : cmul(b, w);
+        }
+        const C a = u[i + k];
+        u[i + k] = cadd(a, b);
+        u[i + k + len / 2] = csub(a, b);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = u[i];
+}
+
+template <typename R, int R1, int R2>
+__global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
+    k_tp_zfused(typename Cplx<R>::T *__restrict__ spec, int64_t nk, int nx, int ny, int nxh,
+                const double *__restrict__ kvx, const double *__restrict__ kvy, const double *__restrict__ kvz,
+                const typename Cplx<R>::T *__restrict__ twg, R eta, R scale) {
+  typedef typename Cplx<R>::T C;
+  constexpr int NZ = R1 * R2;
+  constexpr int CB = ZF_CB;
+  extern __shared__ __align__(16) unsigned char zf_smem[];
+  C *buf = reinterpret_cast<C *>(zf_smem);  // [3][NZ][CB]
+  __shared__ C tw[NZ];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int64_t c0 = (int64_t)blockIdx.x * CB;
+  for (int i = tid; i < NZ; i += nth) tw[i] = twg[i];
+  for (int e = tid; e < 3 * NZ * CB; e += nth) {
+    const int col = e % CB, r = e / CB;
+    buf[e] = (c0 + col < nk) ? spec[(int64_t)r * nk + c0 + col] : C{(R)0, (R)0};
+  }
+  __syncthreads();
+  const int col = tid % CB, q = tid / CB, comp = q % 3, j = q / 3;
+  C *s = buf + comp * NZ * CB + col;
+  if (j < R2) {  // pass 1: n2 = j
+    C v[R1];
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) v[n1] = s[(R2 * n1 + j) * CB];
+    dft_small<C, R1, false>(v, tw, NZ / R1);
+    s[j * CB] = v[0];
+#pragma unroll
+    for (int k1 = 1; k1 < R1; ++k1) s[(R2 * k1 + j) * CB] = cmul(v[k1], tw[(j * k1) % NZ]);
+  }
+  __syncthreads();
+  if (j < R1) {  // pass 2: k1 = j
+    C v[R2];
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) v[n2] = s[(R2 * j + n2) * CB];
+    dft_small<C, R2, false>(v, tw, NZ / R2);
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) s[(R2 * j + k2) * CB] = v[k2];
+  }
+  __syncthreads();
+  // solve every (slot, column): slot R2 k1 + k2 holds kz index k1 + R1 k2
+  for (int e = tid; e < NZ * CB; e += nth) {
+    const int cc = e % CB, slot = e / CB;
+    const int64_t kc = c0 + cc;
+    if (kc >= nk) continue;
+    const int iz = slot / R2 + R1 * (slot % R2);
+    C *u = buf + slot * CB + cc;
+    const int ix = (int)(kc % nxh), iy = (int)(kc / nxh);
+    if (ix == 0 && iy == 0 && iz == 0) {
+      u[0] = C{(R)0, (R)0};
+      u[NZ * CB] = C{(R)0, (R)0};
+      u[2 * NZ * CB] = C{(R)0, (R)0};
+      continue;
+    }
+    const R kx = (R)__ldg(kvx + ix), ky = (R)__ldg(kvy + iy), kz = (R)__ldg(kvz + iz);
+    const R dx = (2 * ix == nx) ? (R)0 : kx;
+    const R dy = (2 * iy == ny) ? (R)0 : ky;
+    const R dz = (2 * iz == NZ) ? (R)0 : kz;
+    const R ksq = kx * kx + ky * ky + kz * kz;
+    const C f = u[0], g = u[NZ * CB], h = u[2 * NZ * CB];
+    const R ik = (R)1 / ksq;
+    const R pr = (dx * f.y + dy * g.y + dz * h.y) * ik;
+    const R pi = -(dx * f.x + dy * g.x + dz * h.x) * ik;
+    const R v = scale * ik / eta;
+    u[0] = C{v * (f.x + dx * pi), v * (f.y - dx * pr)};
+    u[NZ * CB] = C{v * (g.x + dy * pi), v * (g.y - dy * pr)};
+    u[2 * NZ * CB] = C{v * (h.x + dz * pi), v * (h.y - dz * pr)};
+  }
+  __syncthreads();
+  if (j < R1) {  // inverse of pass 2
+    C v[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[(R2 * j + k2) * CB];
+    dft_small<C, R2, true>(v, tw, NZ / R2);
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) s[(R2 * j + n2) * CB] = v[n2];
+  }
+  __syncthreads();
+  if (j < R2) {  // inverse of pass 1
+    C v[R1];
+    v[0] = s[j * CB];
+#pragma unroll
+    for (int k1 = 1; k1 < R1; ++k1) v[k1] = cmulc(s[(R2 * k1 + j) * CB], tw[(j * k1) % NZ]);
+    dft_small<C, R1, true>(v, tw, NZ / R1);
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) s[(R2 * n1 + j) * CB] = v[n1];
+  }
+  __syncthreads();
+  for (int e = tid; e < 3 * NZ * CB; e += nth) {
+    const int cc = e % CB, r = e / CB;
+    if (c0 + cc < nk) spec[(int64_t)r * nk + c0 + cc] = buf[e];
+  }
+}
+
+template <typename R, int R1, int R2>
+static void launch_tp_zfused(typename Cplx<R>::T *spec, int64_t nk, int nx, int ny, int nxh, const double *kvx,
+                             const double *kvy, const double *kvz, const typename Cplx<R>::T *tw, R eta, R scale,
+                             cudaStream_t s) {
+  constexpr int threads = ZF_CB * 3 * (R1 > R2 ? R1 : R2);
+  const size_t smem = sizeof(typename Cplx<R>::T) * 3 * R1 * R2 * ZF_CB;
+  static bool attr = false;
+  if (!attr) {
+    DPST_CUDA(cudaFuncSetAttribute(k_tp_zfused<R, R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const int64_t blocks = (nk + ZF_CB - 1) / ZF_CB;
+  k_tp_zfused<R, R1, R2><<<(unsigned)blocks, threads, smem, s>>>(spec, nk, nx, ny, nxh, kvx, kvy, kvz, tw, eta, scale);
+}
+
 template <typename R>
 struct EngineTP : EngineBase {
   typedef typename std::conditional<sizeof(R) == 8, cufftDoubleComplex, cufftComplex>::type CR;
@@ -171,6 +342,14 @@ struct EngineTP : EngineBase {
   bool plans = false;
   cudaEvent_t ev[8] = {};
   bool have_events = false;
+  // fused z transform + solve (k_tp_zfused) for nz = 16, 32, 64 with the
+  // derivative-kernel coupling: x-y transforms by cuFFT, z in the kernel.
+  // Chosen for the mixed operator (HBM-bound there); the FP64 operator keeps
+  // cuFFT's 3-D transforms (its z passes are FP64-pipe bound, and cuFFT's
+  // are the faster of the two).  DPSTOKES_GB300_TP_Z = cufft | fused | auto
+  // (default) overrides the choice.
+  bool zfused = false;
+  DevBuf twz;  // exp(-2 pi i m / nz), m < nz, in R
 
   EngineTP(const dpst_params &prm, int64_t n, int dev) {
     p = prm;
@@ -210,13 +389,34 @@ struct EngineTP : EngineBase {
     ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
     ord_start.alloc(sizeof(int) * (tile_order_tiles(nx, ny) + 1));
     perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
-    // 3-D real transforms over (z, y, x), one per component
-    int n3[3] = {nz, ny, nx};
-    int inem[3] = {nz, ny, nx}, onem[3] = {nz, ny, nxh};
-    DPST_CUFFT(cufftPlanMany(&plan_f, 3, n3, inem, 1, nz * ny * nx, onem, 1, (int)M,
-                             sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, 3));
-    DPST_CUFFT(cufftPlanMany(&plan_b, 3, n3, onem, 1, (int)M, inem, 1, nz * ny * nx,
-                             sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, 3));
+    const char *zenv = getenv("DPSTOKES_GB300_TP_Z");
+    const std::string zwant = zenv ? zenv : "auto";
+    zfused = !reg && (nz == 16 || nz == 32 || nz == 64) &&
+             (zwant == "fused" || (zwant != "cufft" && sizeof(R) == 4));
+    if (zfused) {
+      // 2-D real transforms over (y, x) of every (component, z) plane
+      std::vector<R> t(2 * (size_t)nz);
+      for (int m = 0; m < nz; ++m) {
+        t[2 * m] = (R)std::cos(2.0 * M_PI * m / nz);
+        t[2 * m + 1] = (R)(-std::sin(2.0 * M_PI * m / nz));
+      }
+      upload(twz, t);
+      int n2[2] = {ny, nx};
+      int inem[2] = {ny, nx}, onem[2] = {ny, nxh};
+      const int64_t nk = (int64_t)ny * nxh;
+      DPST_CUFFT(cufftPlanMany(&plan_f, 2, n2, inem, 1, ny * nx, onem, 1, (int)nk,
+                               sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, 3 * nz));
+      DPST_CUFFT(cufftPlanMany(&plan_b, 2, n2, onem, 1, (int)nk, inem, 1, ny * nx,
+                               sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, 3 * nz));
+    } else {
+      // 3-D real transforms over (z, y, x), one per component
+      int n3[3] = {nz, ny, nx};
+      int inem[3] = {nz, ny, nx}, onem[3] = {nz, ny, nxh};
+      DPST_CUFFT(cufftPlanMany(&plan_f, 3, n3, inem, 1, nz * ny * nx, onem, 1, (int)M,
+                               sizeof(R) == 8 ? CUFFT_D2Z : CUFFT_R2C, 3));
+      DPST_CUFFT(cufftPlanMany(&plan_b, 3, n3, onem, 1, (int)M, inem, 1, nz * ny * nx,
+                               sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, 3));
+    }
     plans = true;
     DPST_CUDA(cudaDeviceSynchronize());
   }
@@ -332,7 +532,17 @@ struct EngineTP : EngineBase {
     mark(3, s);  // no z transform in this mode
     const int bs = 256;
     typedef typename Cplx<R>::T C;
-    if (reg)
+    const R scale = (R)(1.0 / ((double)nx * ny * nz));
+    if (zfused) {
+      const int64_t nk = (int64_t)ny * nxh;
+      C *spc = reinterpret_cast<C *>(sp);
+      const double *kx = kvx.as<double>(), *ky = kvy.as<double>(), *kz = kvz.as<double>();
+      const C *tw = twz.as<C>();
+      const R eta = (R)p.viscosity;
+      if (nz == 64) launch_tp_zfused<R, 8, 8>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
+      else if (nz == 32) launch_tp_zfused<R, 8, 4>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
+      else launch_tp_zfused<R, 4, 4>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
+    } else if (reg)
       k_tp_solve_reg<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<C *>(sp), specT.as<C>(), torque ? 1 : 0, M,
                                                         nx, ny, nz, nxh, kvx.as<double>(), kvy.as<double>(),
                                                         kvz.as<double>(), (R)p.viscosity,
@@ -455,9 +665,10 @@ struct EngineTP : EngineBase {
     const int particle_passes = (p.has_torque && !fused) ? 2 : 1;
     o->kernels_per_mdot = particle_passes + 1 + particle_passes;
     o->fused_particle_passes = fused ? 1 : 0;
+    o->z_fused = zfused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf,
-                           &gridT, &specT};
+                           &gridT, &specT, &twz};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     o->device_bytes = b;

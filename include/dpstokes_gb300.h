@@ -144,6 +144,9 @@ typedef struct dpst_info {
   int ztransform_inverse;          /* kernel of the inverse z transform (with the wall-
                                       correction epilogue), chosen separately: 0 / 1 */
   float ztransform_inverse_ms[2];  /* its creation-time timings: SIMT, tcgen05 */
+  int z_fused;                     /* triply periodic: 1 when the z transform and the solve
+                                      run in one kernel after 2-D x-y transforms (nz = 16,
+                                      32, 64), 0 with cuFFT's 3-D transforms */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

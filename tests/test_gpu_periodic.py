@@ -220,3 +220,33 @@ def test_uammd_shim_periodic_mode():
     assert rel_err(MF, Vo) < TOL_FP64
     assert rel_err(MT, Wo) < TOL_FP64
     m.clear()
+
+
+@pytest.mark.parametrize("name", ["s_tp_t", "t0_tp_n2048", "t1_tp_n65536", "s_tp_f_odd"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_z_path_matches_cufft_path(name, precision, monkeypatch):
+    """nz = 16, 32, 64: the fused z transform + solve kernel after 2-D x-y
+    transforms (forced for FP64, the default for mixed) against cuFFT's 3-D
+    transforms and the separate solve (FP64: 1e-12; mixed: 1e-6); nz = 13
+    keeps the 3-D path."""
+    w = W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    X, F, T = W.make_inputs(w)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    if T is not None and precision == "mixed":
+        T = T.astype(np.float32)
+    Fc = F.astype(np.float32) if precision == "mixed" else F
+    out = {}
+    for mode in ("fused", "cufft"):
+        monkeypatch.setenv("DPSTOKES_GB300_TP_Z", mode)
+        op = _op(w, X, precision)
+        out[mode] = (_mdot(op, Fc, T, dt), op.info()["z_fused"])
+        op.close()
+    expect = 1 if w.nz in (16, 32, 64) else 0
+    assert out["fused"][1] == expect and out["cufft"][1] == 0
+    (Vf, Wf), (Vc, Wc) = out["fused"][0], out["cufft"][0]
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    ev = rel_err(Vf, Vc)
+    print("%s %s fused vs cufft V %.2e" % (name, precision, ev))
+    assert ev < tol
+    if Wc is not None:
+        assert rel_err(Wf, Wc) < tol
