@@ -136,7 +136,13 @@ T0 = Workload("t0_tp_n2048", "TP", 2048, 128.0, 128.0, 128, 128, 32, 0.0, 32.0, 
               False, betam_hat=1.714)
 T1 = Workload("t1_tp_n65536", "TP", 65536, 512.0, 512.0, 512, 512, 64, 0.0, 64.0, 0.0, 64.0,
               True, betam_hat=1.3267, betad_hat=2.2160)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4, T0, T1)}
+# Four times c2 (the same density and z geometry on a 1024 x 1024 x 128 grid,
+# N = 262,144): a scale check of the index arithmetic and the solve's
+# scheduling past the headline size (about 20 GB on the device with both
+# operators).
+L1 = Workload("l1_dp_n262144_1024", "DP", 262144, 1024.0, 1024.0, 1024, 1024, 128, -20.5, 41.0, -16.0, 16.0,
+              True, betam_hat=1.3267, betad_hat=2.2160)
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4, T0, T1, L1)}
 
 
 def fft_friendly(n):
