@@ -165,7 +165,7 @@ __global__ void k_tp_solve_reg(typename Cplx<R>::T *__restrict__ spec, typename 
 // arithmetic as the 3-D transform's z passes plus k_tp_solve, with one read
 // and one write of the spectrum instead of three of each.
 // ---------------------------------------------------------------------------
-constexpr int ZF_CB = 32;  // columns per CTA
+constexpr int ZF_CB = 16;  // columns per CTA
 
 template <typename C>
 static __device__ __forceinline__ C cadd(C a, C b) { return C{a.x + b.x, a.y + b.y}; }
@@ -183,12 +183,25 @@ static constexpr int bitrev(int i) {
   return r;
 }
 
-// In-place DFT of N (a power of two) values in registers, natural order in
-// and out; tw[m] = exp(-2 pi i m / NZ), stride = NZ / N.  INV: conjugate
-// twiddles (unnormalised inverse).  Iterative radix-2 with the input taken
-// in bit-reversed order (indices are compile-time constants).
+// b W_8^e (forward) or b conj(W_8^e) (INV) for W_8 = exp(-2 pi i / 8),
+// e = 0..3, without a table: W_8^2 = -i, W_8^(1, 3) = (+-1 - i) / sqrt(2).
+template <typename C, int E, bool INV>
+static __device__ __forceinline__ C mul_w8(C b) {
+  typedef decltype(b.x) R;
+  const R c = (R)0.70710678118654752440;  // 1 / sqrt(2)
+  if (E == 0) return b;
+  if (E == 2) return INV ? C{-b.y, b.x} : C{b.y, -b.x};
+  if (E == 1) return INV ? C{c * (b.x - b.y), c * (b.x + b.y)} : C{c * (b.x + b.y), c * (b.y - b.x)};
+  return INV ? C{-c * (b.x + b.y), c * (b.x - b.y)} : C{c * (b.y - b.x), -c * (b.x + b.y)};
+}
+
+// In-place DFT of N (2, 4 or 8) values in registers, natural order in and
+// out.  INV: the unnormalised inverse.  Iterative radix-2 with the input
+// taken in bit-reversed order; the twiddles W_len^k = W_8^(k 8 / len) are
+// applied by mul_w8 (indices and exponents are compile-time constants).
 template <typename C, int N, bool INV>
-static __device__ __forceinline__ void dft_small(C (&v)[N], const C *__restrict__ tw, int stride) {
+static __device__ __forceinline__ void dft_small(C (&v)[N]) {
+  static_assert(N == 2 || N == 4 || N == 8, "small DFT sizes");
   C u[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) u[i] = v[bitrev<N>(i)];
@@ -198,11 +211,9 @@ static __device__ __forceinline__ void dft_small(C (&v)[N], const C *__restrict_
     for (int i = 0; i < N; i += len) {
 #pragma unroll
       for (int k = 0; k < len / 2; ++k) {
+        const int e = k * (8 / len);
         C b = u[i + k + len / 2];
-        if (k != 0) {  // W^0 = 1
-          const C w = tw[k * (N / len) * stride];
-          b = INV ? cmulc(b, w) : cmul(b, w);
-        }
+        b = (e == 0) ? b : (e == 1) ? mul_w8<C, 1, INV>(b) : (e == 2) ? mul_w8<C, 2, INV>(b) : mul_w8<C, 3, INV>(b);
         const C a = u[i + k];
         u[i + k] = cadd(a, b);
         u[i + k + len / 2] = csub(a, b);
@@ -238,7 +249,7 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     C v[R1];
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) v[n1] = s[(R2 * n1 + j) * CB];
-    dft_small<C, R1, false>(v, tw, NZ / R1);
+    dft_small<C, R1, false>(v);
     s[j * CB] = v[0];
 #pragma unroll
     for (int k1 = 1; k1 < R1; ++k1) s[(R2 * k1 + j) * CB] = cmul(v[k1], tw[(j * k1) % NZ]);
@@ -248,7 +259,7 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     C v[R2];
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) v[n2] = s[(R2 * j + n2) * CB];
-    dft_small<C, R2, false>(v, tw, NZ / R2);
+    dft_small<C, R2, false>(v);
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) s[(R2 * j + k2) * CB] = v[k2];
   }
@@ -286,7 +297,7 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     C v[R2];
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) v[k2] = s[(R2 * j + k2) * CB];
-    dft_small<C, R2, true>(v, tw, NZ / R2);
+    dft_small<C, R2, true>(v);
 #pragma unroll
     for (int n2 = 0; n2 < R2; ++n2) s[(R2 * j + n2) * CB] = v[n2];
   }
@@ -296,7 +307,7 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     v[0] = s[j * CB];
 #pragma unroll
     for (int k1 = 1; k1 < R1; ++k1) v[k1] = cmulc(s[(R2 * k1 + j) * CB], tw[(j * k1) % NZ]);
-    dft_small<C, R1, true>(v, tw, NZ / R1);
+    dft_small<C, R1, true>(v);
 #pragma unroll
     for (int n1 = 0; n1 < R1; ++n1) s[(R2 * n1 + j) * CB] = v[n1];
   }
