@@ -124,6 +124,24 @@ def algorithmic_bytes(stage, w, prec):
     return None
 
 
+def max_over_ranks(x, world, device):
+    """The maximum of a per-rank scalar over the job's ranks (the replicas
+    time the same workload independently; the job's time is the slowest)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(n_particles, steps, seconds, world):
+    """Whole-job particles/s: every rank runs its own replica of the workload
+    (no data-path collective), so the units are world x N x steps over the
+    slowest rank's time."""
+    return world * n_particles * steps / seconds
+
+
 def run_ours(args, rank, world):
     import torch
     import ctypes
@@ -165,12 +183,9 @@ def run_ours(args, rank, world):
         barrier()
     ms = e0.elapsed_time(e1)
     clocks = cs.summary()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     ms_step = ms / args.steps
-    value = world * w.N * args.steps / (ms / 1e3)
+    value = replica_value(w.N, args.steps, ms / 1e3, world)
 
     # per-stage device times (CUDA events on the operator's stream)
     stage_runs = []
@@ -212,13 +227,9 @@ def run_ours(args, rank, world):
     for _ in range(args.steps):
         e2e_step()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
     nbytes = Fh.numel() * Fh.element_size()
-    e2e = {"value": world * w.N * args.steps / e2e_s, "unit": "particles/s",
+    e2e = {"value": replica_value(w.N, args.steps, e2e_s, world), "unit": "particles/s",
            "h2d_bytes_per_step": nbytes * (2 if T is not None else 1),
            "d2h_bytes_per_step": nbytes * (2 if w.has_torque else 1)}
 
