@@ -391,7 +391,7 @@ static __device__ __forceinline__ void spread_fused_item(int64_t p, int c, const
 }
 
 template <typename R, typename RF>
-__global__ void k_spread_fused(const RF *__restrict__ F, const RF *__restrict__ T, int64_t N, KernelDesc km,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_spread_fused(const RF *__restrict__ F, const RF *__restrict__ T, int64_t N, KernelDesc km,
                                KernelDesc kd, GridArgs g, Stencils<R> sm, Stencils<R> sd, R *__restrict__ grid,
                                Ghosts<R> ghm, Ghosts<R> ghd, const int *__restrict__ perm) {
   const int cols = km.wx * km.wy;
@@ -749,7 +749,7 @@ static __device__ __forceinline__ void interp_fused_interior(int64_t p, int lane
 }
 
 template <typename R, typename RV>
-__global__ void __launch_bounds__(32 * INTERP_WARPS) k_interp_fused(const R *__restrict__ grid, int64_t N, KernelDesc km,
+__global__ void __launch_bounds__(32 * INTERP_WARPS, sizeof(R) == 4 ? 4 : 1) k_interp_fused(const R *__restrict__ grid, int64_t N, KernelDesc km,
                                                                     KernelDesc kd, GridArgs g, Stencils<R> sm,
                                                                     Stencils<R> sd, Ghosts<R> ghm, Ghosts<R> ghd,
                                                                     RV *__restrict__ V, RV *__restrict__ W,
