@@ -224,27 +224,34 @@ static __device__ __forceinline__ void dft_small(C (&v)[N]) {
   for (int i = 0; i < N; ++i) v[i] = u[i];
 }
 
-template <typename R, int R1, int R2>
-__global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
-    k_tp_zfused(typename Cplx<R>::T *__restrict__ spec, int64_t nk, int nx, int ny, int nxh,
-                const double *__restrict__ kvx, const double *__restrict__ kvy, const double *__restrict__ kvz,
-                const typename Cplx<R>::T *__restrict__ twg, R eta, R scale) {
+// NS = 3: the force spectrum (derivative-kernel coupling).  NS = 6 (the
+// regular-kernel coupling): the force spectrum in spec and the torque
+// spectrum in tspec; with torques, 1/2 curl of the torque coefficients is
+// added before the solve (k_tp_solve_reg's arithmetic), and the vorticity
+// 1/2 curl u goes back to tspec.
+template <typename R, int R1, int R2, int NS>
+__global__ void __launch_bounds__(ZF_CB * NS * (R1 > R2 ? R1 : R2))
+    k_tp_zfused(typename Cplx<R>::T *__restrict__ spec, typename Cplx<R>::T *__restrict__ tspec, int torque,
+                int64_t nk, int nx, int ny, int nxh, const double *__restrict__ kvx, const double *__restrict__ kvy,
+                const double *__restrict__ kvz, const typename Cplx<R>::T *__restrict__ twg, R eta, R scale) {
   typedef typename Cplx<R>::T C;
   constexpr int NZ = R1 * R2;
   constexpr int CB = ZF_CB;
+  constexpr int CS = NZ * CB;  // component stride in shared memory
   extern __shared__ __align__(16) unsigned char zf_smem[];
-  C *buf = reinterpret_cast<C *>(zf_smem);  // [3][NZ][CB]
+  C *buf = reinterpret_cast<C *>(zf_smem);  // [NS][NZ][CB]
   __shared__ C tw[NZ];
   const int tid = threadIdx.x, nth = blockDim.x;
   const int64_t c0 = (int64_t)blockIdx.x * CB;
   for (int i = tid; i < NZ; i += nth) tw[i] = twg[i];
-  for (int e = tid; e < 3 * NZ * CB; e += nth) {
+  for (int e = tid; e < NS * CS; e += nth) {
     const int col = e % CB, r = e / CB;
-    buf[e] = (c0 + col < nk) ? spec[(int64_t)r * nk + c0 + col] : C{(R)0, (R)0};
+    const C *src = (r < 3 * NZ) ? spec + (int64_t)r * nk : tspec + (int64_t)(r - 3 * NZ) * nk;
+    buf[e] = (c0 + col < nk && (r < 3 * NZ || torque)) ? src[c0 + col] : C{(R)0, (R)0};
   }
   __syncthreads();
-  const int col = tid % CB, q = tid / CB, comp = q % 3, j = q / 3;
-  C *s = buf + comp * NZ * CB + col;
+  const int col = tid % CB, q = tid / CB, comp = q % NS, j = q / NS;
+  C *s = buf + comp * CS + col;
   if (j < R2) {  // pass 1: n2 = j
     C v[R1];
 #pragma unroll
@@ -265,7 +272,7 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
   }
   __syncthreads();
   // solve every (slot, column): slot R2 k1 + k2 holds kz index k1 + R1 k2
-  for (int e = tid; e < NZ * CB; e += nth) {
+  for (int e = tid; e < CS; e += nth) {
     const int cc = e % CB, slot = e / CB;
     const int64_t kc = c0 + cc;
     if (kc >= nk) continue;
@@ -273,9 +280,8 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     C *u = buf + slot * CB + cc;
     const int ix = (int)(kc % nxh), iy = (int)(kc / nxh);
     if (ix == 0 && iy == 0 && iz == 0) {
-      u[0] = C{(R)0, (R)0};
-      u[NZ * CB] = C{(R)0, (R)0};
-      u[2 * NZ * CB] = C{(R)0, (R)0};
+#pragma unroll
+      for (int c = 0; c < NS; ++c) u[c * CS] = C{(R)0, (R)0};
       continue;
     }
     const R kx = (R)__ldg(kvx + ix), ky = (R)__ldg(kvy + iy), kz = (R)__ldg(kvz + iz);
@@ -283,14 +289,29 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     const R dy = (2 * iy == ny) ? (R)0 : ky;
     const R dz = (2 * iz == NZ) ? (R)0 : kz;
     const R ksq = kx * kx + ky * ky + kz * kz;
-    const C f = u[0], g = u[NZ * CB], h = u[2 * NZ * CB];
+    const R half = (R)0.5;
+    C f = u[0], g = u[CS], h = u[2 * CS];
+    if (NS == 6 && torque) {  // + 1/2 curl t, with i k: i (dy tz - dz ty, dz tx - dx tz, dx ty - dy tx)
+      const C a = u[3 * CS], b = u[4 * CS], c = u[5 * CS];
+      f.x += half * (-dy * c.y - (-dz * b.y)); f.y += half * (dy * c.x - dz * b.x);
+      g.x += half * (-dz * a.y - (-dx * c.y)); g.y += half * (dz * a.x - dx * c.x);
+      h.x += half * (-dx * b.y - (-dy * a.y)); h.y += half * (dx * b.x - dy * a.x);
+    }
     const R ik = (R)1 / ksq;
     const R pr = (dx * f.y + dy * g.y + dz * h.y) * ik;
     const R pi = -(dx * f.x + dy * g.x + dz * h.x) * ik;
     const R v = scale * ik / eta;
-    u[0] = C{v * (f.x + dx * pi), v * (f.y - dx * pr)};
-    u[NZ * CB] = C{v * (g.x + dy * pi), v * (g.y - dy * pr)};
-    u[2 * NZ * CB] = C{v * (h.x + dz * pi), v * (h.y - dz * pr)};
+    const C a = C{v * (f.x + dx * pi), v * (f.y - dx * pr)};
+    const C b = C{v * (g.x + dy * pi), v * (g.y - dy * pr)};
+    const C c = C{v * (h.x + dz * pi), v * (h.y - dz * pr)};
+    u[0] = a;
+    u[CS] = b;
+    u[2 * CS] = c;
+    if (NS == 6) {  // vorticity 1/2 curl u
+      u[3 * CS] = C{half * (-dy * c.y - (-dz * b.y)), half * (dy * c.x - dz * b.x)};
+      u[4 * CS] = C{half * (-dz * a.y - (-dx * c.y)), half * (dz * a.x - dx * c.x)};
+      u[5 * CS] = C{half * (-dx * b.y - (-dy * a.y)), half * (dx * b.x - dy * a.x)};
+    }
   }
   __syncthreads();
   if (j < R1) {  // inverse of pass 2
@@ -312,25 +333,38 @@ __global__ void __launch_bounds__(ZF_CB * 3 * (R1 > R2 ? R1 : R2))
     for (int n1 = 0; n1 < R1; ++n1) s[(R2 * n1 + j) * CB] = v[n1];
   }
   __syncthreads();
-  for (int e = tid; e < 3 * NZ * CB; e += nth) {
+  for (int e = tid; e < NS * CS; e += nth) {
     const int cc = e % CB, r = e / CB;
-    if (c0 + cc < nk) spec[(int64_t)r * nk + c0 + cc] = buf[e];
+    if (c0 + cc >= nk) continue;
+    C *dst = (r < 3 * NZ) ? spec + (int64_t)r * nk : tspec + (int64_t)(r - 3 * NZ) * nk;
+    dst[c0 + cc] = buf[e];
   }
 }
 
-template <typename R, int R1, int R2>
-static void launch_tp_zfused(typename Cplx<R>::T *spec, int64_t nk, int nx, int ny, int nxh, const double *kvx,
-                             const double *kvy, const double *kvz, const typename Cplx<R>::T *tw, R eta, R scale,
-                             cudaStream_t s) {
-  constexpr int threads = ZF_CB * 3 * (R1 > R2 ? R1 : R2);
-  const size_t smem = sizeof(typename Cplx<R>::T) * 3 * R1 * R2 * ZF_CB;
+template <typename R, int R1, int R2, int NS>
+static void launch_tp_zfused(typename Cplx<R>::T *spec, typename Cplx<R>::T *tspec, bool torque, int64_t nk, int nx,
+                             int ny, int nxh, const double *kvx, const double *kvy, const double *kvz,
+                             const typename Cplx<R>::T *tw, R eta, R scale, cudaStream_t s) {
+  constexpr int threads = ZF_CB * NS * (R1 > R2 ? R1 : R2);
+  const size_t smem = sizeof(typename Cplx<R>::T) * NS * R1 * R2 * ZF_CB;
   static bool attr = false;
   if (!attr) {
-    DPST_CUDA(cudaFuncSetAttribute(k_tp_zfused<R, R1, R2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DPST_CUDA(cudaFuncSetAttribute(k_tp_zfused<R, R1, R2, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr = true;
   }
   const int64_t blocks = (nk + ZF_CB - 1) / ZF_CB;
-  k_tp_zfused<R, R1, R2><<<(unsigned)blocks, threads, smem, s>>>(spec, nk, nx, ny, nxh, kvx, kvy, kvz, tw, eta, scale);
+  k_tp_zfused<R, R1, R2, NS><<<(unsigned)blocks, threads, smem, s>>>(spec, tspec, torque ? 1 : 0, nk, nx, ny, nxh,
+                                                                     kvx, kvy, kvz, tw, eta, scale);
+}
+
+template <typename R, int NS>
+static void launch_tp_zfused_nz(int nz, typename Cplx<R>::T *spec, typename Cplx<R>::T *tspec, bool torque,
+                                int64_t nk, int nx, int ny, int nxh, const double *kvx, const double *kvy,
+                                const double *kvz, const typename Cplx<R>::T *tw, R eta, R scale, cudaStream_t s) {
+  if (nz == 64) launch_tp_zfused<R, 8, 8, NS>(spec, tspec, torque, nk, nx, ny, nxh, kvx, kvy, kvz, tw, eta, scale, s);
+  else if (nz == 32) launch_tp_zfused<R, 8, 4, NS>(spec, tspec, torque, nk, nx, ny, nxh, kvx, kvy, kvz, tw, eta, scale, s);
+  else launch_tp_zfused<R, 4, 4, NS>(spec, tspec, torque, nk, nx, ny, nxh, kvx, kvy, kvz, tw, eta, scale, s);
 }
 
 template <typename R>
@@ -353,8 +387,9 @@ struct EngineTP : EngineBase {
   bool plans = false;
   cudaEvent_t ev[8] = {};
   bool have_events = false;
-  // fused z transform + solve (k_tp_zfused) for nz = 16, 32, 64 with the
-  // derivative-kernel coupling: x-y transforms by cuFFT, z in the kernel.
+  // fused z transform + solve (k_tp_zfused) for nz = 16, 32, 64: x-y
+  // transforms by cuFFT, z in the kernel (six components with the
+  // regular-kernel coupling).
   // Chosen for the mixed operator (HBM-bound there); the FP64 operator keeps
   // cuFFT's 3-D transforms (its z passes are FP64-pipe bound, and cuFFT's
   // are the faster of the two).  DPSTOKES_GB300_TP_Z = cufft | fused | auto
@@ -402,8 +437,7 @@ struct EngineTP : EngineBase {
     perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
     const char *zenv = getenv("DPSTOKES_GB300_TP_Z");
     const std::string zwant = zenv ? zenv : "auto";
-    zfused = !reg && (nz == 16 || nz == 32 || nz == 64) &&
-             (zwant == "fused" || (zwant != "cufft" && sizeof(R) == 4));
+    zfused = (nz == 16 || nz == 32 || nz == 64) && (zwant == "fused" || (zwant != "cufft" && sizeof(R) == 4));
     if (zfused) {
       // 2-D real transforms over (y, x) of every (component, z) plane
       std::vector<R> t(2 * (size_t)nz);
@@ -550,9 +584,10 @@ struct EngineTP : EngineBase {
       const double *kx = kvx.as<double>(), *ky = kvy.as<double>(), *kz = kvz.as<double>();
       const C *tw = twz.as<C>();
       const R eta = (R)p.viscosity;
-      if (nz == 64) launch_tp_zfused<R, 8, 8>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
-      else if (nz == 32) launch_tp_zfused<R, 8, 4>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
-      else launch_tp_zfused<R, 4, 4>(spc, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
+      if (reg)
+        launch_tp_zfused_nz<R, 6>(nz, spc, specT.as<C>(), torque, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
+      else
+        launch_tp_zfused_nz<R, 3>(nz, spc, nullptr, false, nk, nx, ny, nxh, kx, ky, kz, tw, eta, scale, s);
     } else if (reg)
       k_tp_solve_reg<R><<<(M + bs - 1) / bs, bs, 0, s>>>(reinterpret_cast<C *>(sp), specT.as<C>(), torque ? 1 : 0, M,
                                                         nx, ny, nz, nxh, kvx.as<double>(), kvy.as<double>(),
