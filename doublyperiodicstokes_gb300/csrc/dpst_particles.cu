@@ -43,14 +43,14 @@ static __device__ __forceinline__ void locate_item(int64_t p, const double *__re
   for (int i = 0; i < kd.wx; ++i) {
     double o = ((double)xclose + i - kd.wx / 2 + kd.evenx) * g.hx - x;
     if (o > thr || o < -thr) o = thr;
-    st.phx[p * kd.wx + i] = (R)es1(o, kd.beta, kd.alpha2);
-    if (DIPOLE) st.dphx[p * kd.wx + i] = (R)des1(o, kd.beta, kd.alpha2);
+    st.phx[p * kd.wx + i] = es1r<R>(o, kd);
+    if (DIPOLE) st.dphx[p * kd.wx + i] = des1r<R>(o, kd);
   }
   for (int j = 0; j < kd.wy; ++j) {
     double o = ((double)yclose + j - kd.wy / 2 + kd.eveny) * g.hy - y;
     if (thr < o || o < -thr) o = thr;
-    st.phy[p * kd.wy + j] = (R)es1(o, kd.beta, kd.alpha2);
-    if (DIPOLE) st.dphy[p * kd.wy + j] = (R)des1(o, kd.beta, kd.alpha2);
+    st.phy[p * kd.wy + j] = es1r<R>(o, kd);
+    if (DIPOLE) st.dphy[p * kd.wy + j] = des1r<R>(o, kd);
   }
   if (kd.unif_z) {
     // uniform periodic z (ParticleList.cpp:285-366): the window is built like
@@ -64,13 +64,13 @@ static __device__ __forceinline__ void locate_item(int64_t p, const double *__re
     for (int k = 0; k < wz; ++k) {
       double o = ((double)zclose + k - wz / 2 + kd.evenz) * kd.hz - z;
       if (thr < o || o < -thr) o = thr;
-      const double v = es1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
-      st.phz[p * wz + k] = (R)v;
-      st.phzw[p * wz + k] = (R)(v * hxyz);
+      const R v = es1r<R>(o, kd) * (R)kd.inv_norm3;
+      st.phz[p * wz + k] = v;
+      st.phzw[p * wz + k] = v * (R)hxyz;
       if (DIPOLE) {
-        const double dv = des1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
-        st.dphz[p * wz + k] = (R)dv;
-        st.dphzw[p * wz + k] = (R)(dv * hxyz);
+        const R dv = des1r<R>(o, kd) * (R)kd.inv_norm3;
+        st.dphz[p * wz + k] = dv;
+        st.dphzw[p * wz + k] = dv * (R)hxyz;
       }
     }
     return;
@@ -106,19 +106,19 @@ static __device__ __forceinline__ void locate_item(int64_t p, const double *__re
   }
   const double hxy = g.hx * g.hy;
   for (int k = 0; k < kd.wz_max; ++k) {
-    double v = 0.0, dv = 0.0, wgt = 0.0;
+    R v = 0, dv = 0, wgt = 0;
     if (k < wz) {
       double o = ze[indl + k] - z;
       if (thr < o || o < -thr) o = thr;
-      v = es1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
-      if (DIPOLE) dv = des1(o, kd.beta, kd.alpha2) * kd.inv_norm3;
-      wgt = hxy * we[indl + k];
+      v = es1r<R>(o, kd) * (R)kd.inv_norm3;
+      if (DIPOLE) dv = des1r<R>(o, kd) * (R)kd.inv_norm3;
+      wgt = (R)(hxy * we[indl + k]);
     }
-    st.phz[p * kd.wz_max + k] = (R)v;
-    st.phzw[p * kd.wz_max + k] = (R)(v * wgt);
+    st.phz[p * kd.wz_max + k] = v;
+    st.phzw[p * kd.wz_max + k] = v * wgt;
     if (DIPOLE) {
-      st.dphz[p * kd.wz_max + k] = (R)dv;
-      st.dphzw[p * kd.wz_max + k] = (R)(dv * wgt);
+      st.dphz[p * kd.wz_max + k] = dv;
+      st.dphzw[p * kd.wz_max + k] = dv * wgt;
     }
   }
 }

@@ -22,6 +22,35 @@ static __device__ __forceinline__ double des1(double x, double beta, double alph
   return -beta * x * exp(beta * (s - 1.0)) / (alpha2 * s);
 }
 
+// The factor and its derivative in a stencil's storage type R: FP64 for
+// the FP64 operator (the reference's arithmetic); for the mixed operator the
+// offset (computed in FP64) is rounded to FP32 and the factor evaluated in
+// FP32, as the stored weights are FP32 anyway (FP64 exp and sqrt run at a
+// small fraction of the FP32 rate on this GPU).  The clamped offset of an
+// out-of-support node equals the threshold, so 1 - o^2/alpha^2 may round
+// below 0 in FP32: it is clamped at 0 (the factor there is exp(-beta)).
+template <typename R>
+static __device__ __forceinline__ R es1r(double o, const KernelDesc &kd) {
+  if constexpr (sizeof(R) == 8) {
+    return es1(o, kd.beta, kd.alpha2);
+  } else {
+    const float x = (float)o, a2 = (float)kd.alpha2, b = (float)kd.beta;
+    const float q = fmaxf(0.0f, 1.0f - x * x / a2);
+    return expf(b * (sqrtf(q) - 1.0f));
+  }
+}
+
+template <typename R>
+static __device__ __forceinline__ R des1r(double o, const KernelDesc &kd) {
+  if constexpr (sizeof(R) == 8) {
+    return des1(o, kd.beta, kd.alpha2);
+  } else {
+    const float x = (float)o, a2 = (float)kd.alpha2, b = (float)kd.beta;
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - x * x / a2));
+    return (s > 0.0f) ? -b * x * expf(b * (s - 1.0f)) / (a2 * s) : 0.0f;
+  }
+}
+
 // Position derivatives of one stencil factor.  The forward evaluates
 // phi(o) (and phi'(o) for the dipole kernel) at o = node - x, so
 // d/dx phi(o) = -phi'(o) -> g1 and d/dx phi'(o) = -phi''(o) -> g2, with
