@@ -4,7 +4,9 @@ stream capture in global capture mode, or under an allocator that has
 reserved the device).  Its per-wavenumber solve uses a static device array
 for scratch; here its results are checked, through the C ABI, against the
 ordinary dpst_mdot on the same handle, on two calls in a row (the array
-keeps the previous call's contents, which must not leak into the next).
+keeps the previous call's contents, which must not leak into the next), in
+every geometry, with the regular-kernel coupling and in the triply periodic
+mode (which needs no scratch).
 This file sorts last so that a run stopping at the first failure has run
 every other test first; it also passes alone in a fresh process."""
 import ctypes
@@ -26,7 +28,8 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("name,precision,tol", [("s_dpsc_t", "fp64", 1e-10), ("s_dpbw_t_odd", "fp64", 1e-10),
-                                                ("s_dp_t", "mixed", 1e-5)])
+                                                ("s_dp_t", "mixed", 1e-5), ("s_reg_dpbw_t", "fp64", 1e-10),
+                                                ("s_tp_t", "mixed", 1e-5)])
 def test_noalloc_matches_mdot_on_two_calls(name, precision, tol):
     w = W.SMALL_BY_NAME[name]
     X, F, T = W.make_inputs(w)
