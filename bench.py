@@ -275,6 +275,19 @@ def run_ours(args, rank, world):
             gbs = b / (stages[k] * 1e-3) / 1e9
             roof["stages"][k] = {"ms": round(stages[k], 4), "algorithmic_bytes": b,
                                  "achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
+    # the z transform as a dense contraction: 2 nz^2 flops per real column (3 x 2 nk columns) per
+    # product, three TF32 products (split TF32) on the tensor pipe; TF32 dense rate taken as half
+    # the measured BF16 rate
+    if w.domType != "TP" and info.get("ztransform") == 1 and stages.get("ztrans_fwd", 0) > 0:
+        nk = w.ny * (w.nx // 2 + 1)
+        flops = 3 * 2.0 * w.nz * w.nz * 3 * 2 * nk
+        tf32_peak = peaks["bf16_tflops"] / 2.0
+        roof["ztransform_tensor"] = {
+            "tf32_flops_per_transform": flops,
+            "achieved_tflops_fwd": flops / (stages["ztrans_fwd"] * 1e-3) / 1e12,
+            "achieved_tflops_inv": flops / (stages["ztrans_inv"] * 1e-3) / 1e12,
+            "peak_tflops": tf32_peak, "peak_source": peak_kind + " bf16_tflops / 2 (TF32 dense)",
+            "frac_fwd": flops / (stages["ztrans_fwd"] * 1e-3) / 1e12 / tf32_peak}
     roof["ztransform_kernel"] = "tcgen05 split-TF32" if info.get("ztransform") == 1 else "SIMT folded"
     roof["ztransform_inverse_kernel"] = ("tcgen05 split-TF32" if info.get("ztransform_inverse") == 1
                                          else "SIMT folded")
@@ -282,6 +295,14 @@ def run_ours(args, rank, world):
         # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
         roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "
                         "its algorithmic bytes; fp64_pipe gives its FP64 issue rate")
+        if w.domType == "DP" and w.nz == 128:
+            # DRAM bytes of the hybrid solve per wavenumber from the ncu capture of
+            # k_bvp_hybrid on p4_dp_n36864_384 (same geometry and nz: 3.42 GB read +
+            # 1.32 GB written for 74,112 wavenumbers), scaled by this grid's wavenumbers
+            nk_solve = w.ny * (w.nx // 2 + 1)
+            roof["traffic"] = (3.42e9 + 1.32e9) / 74112 * nk_solve
+            roof["traffic_source"] = ("ncu k_bvp_hybrid on p4_dp_n36864_384, scaled by wavenumbers "
+                                      "(profiles/k_bvp_hybrid_p4_dp_n36864_384.md)")
         if w.domType != "TP":
             # ~46 FP64 instructions per row per lane (2 lanes x nz rows per wavenumber;
             # ncu's FP64 instruction count of the solve), at 2 FP64 lane-operations
