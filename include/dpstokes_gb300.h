@@ -186,14 +186,18 @@ int dpst_mdot_host(dpst_handle h, const void *F, const void *T, void *V, void *W
 /* Diagnostics.
  * dpst_spread_grid: run only the spreading stage (forces and, with T, the
  *   torque curl, with the boundary fold) and copy the resulting grid to the
- *   device buffer grid_out, layout [3][nz][ny][nx] (z index 0 at zmax), element
- *   type double for DPST_PREC_FP64 and float for DPST_PREC_MIXED.
+ *   device buffer grid_out, layout [3][nz][ny][nx] (z index 0 at zmax; in the
+ *   triply periodic mode z index 0 at zmin), element type double for
+ *   DPST_PREC_FP64 and float for DPST_PREC_MIXED.  With DPST_TORQUE_REG the
+ *   grid holds the forces only (the torque curl is added in wavenumber space).
  * dpst_velocity_grid: copy the fluid velocity on the grid from the last Mdot
  *   (same layout and type) to grid_out.
  * dpst_mdot_timed: dpst_mdot that also records CUDA events between stages and
  *   synchronises; stage_ms[0..7] receive the milliseconds of: zero + spread,
  *   forward x-y FFT, forward z transform, per-wavenumber solve, inverse z
- *   transform (+ wall correction), inverse x-y FFT, interpolation, total. */
+ *   transform (+ wall correction), inverse x-y FFT, interpolation, total (in
+ *   the triply periodic mode the transforms are 3-D, or 2-D with the z
+ *   transform inside the solve, and the z-transform entries are ~0). */
 int dpst_spread_grid(dpst_handle h, const void *F, const void *T, int dtype, void *grid_out,
                      void *stream);
 int dpst_velocity_grid(dpst_handle h, void *grid_out, void *stream);
