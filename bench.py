@@ -558,14 +558,21 @@ def run_regkernel(args, dev):
     return out
 
 
-def cpu_baseline(w):
+def cpu_baseline(w, all_cores=False):
+    """The oracle (the reference CPU path restated) timed on a bounded sample
+    of w: single-threaded (this arm's cpu_baseline), or on every core this
+    process may use (the reference arm; oracle/cpu_sample.py)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import dpstokes_oracle as O
     import cpu_sample
     from doublyperiodicstokes_gb300 import workloads as W
     X, F, T = W.make_inputs(w)
-    tot, stages, sample = cpu_sample.sample_mdot_seconds(O.Params(**w.oracle_params()), X, F, T)
-    return {"value": w.N / tot, "unit": "particles/s", "cores": 1, "kind": "port",
+    if all_cores:
+        tot, stages, sample, cores = cpu_sample.sample_mdot_seconds_parallel(O.Params(**w.oracle_params()), X, F, T)
+    else:
+        tot, stages, sample = cpu_sample.sample_mdot_seconds(O.Params(**w.oracle_params()), X, F, T)
+        cores = 1
+    return {"value": w.N / tot, "unit": "particles/s", "cores": cores, "kind": "port",
             "sample": sample, "seconds_per_mdot_est": tot,
             "stage_seconds": {k: round(v, 3) for k, v in stages.items()}}
 
@@ -634,7 +641,7 @@ def main():
         if rank != 0:
             return
         t0 = time.time()
-        cb = cpu_baseline(w)
+        cb = cpu_baseline(w, all_cores=True)
         line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "particles/s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": 1e3 * cb["seconds_per_mdot_est"], "higher_is_better": True,
