@@ -74,15 +74,19 @@ def test_mixed_close_to_fp64(name):
     assert ew < TOL_MIXED
 
 
-def test_without_torques_matches_oracle():
-    w = W.SMALL_BY_NAME["s_reg_dpbw_t"]
+@pytest.mark.parametrize("name", ["s_reg_dpbw_t", "s_reg_tp_t"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_without_torques_matches_oracle(name, precision):
+    w = W.SMALL_BY_NAME[name]
     X, F, _ = W.make_inputs(w)
-    op = _op(w, X)
-    V, Wv = _mdot(op, F, None)
+    op = _op(w, X, precision)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    V, Wv = _mdot(op, F.astype(np.float32) if precision == "mixed" else F, None, dt)
     assert Wv is not None  # the vorticity of the force-driven flow
     Vo, Wo = O.mdot(O.Params(**w.oracle_params()), X, F, np.zeros_like(F))
-    assert rel_err(V, Vo) < TOL_FP64
-    assert rel_err(Wv, Wo) < TOL_FP64
+    tol = TOL_FP64 if precision == "fp64" else TOL_MIXED
+    assert rel_err(V, Vo) < tol
+    assert rel_err(Wv, Wo) < tol
     op.close()
 
 
