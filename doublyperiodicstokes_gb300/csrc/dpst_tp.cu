@@ -686,10 +686,27 @@ struct EngineTP : EngineBase {
     DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
   }
 
-  void backward(const void *, const void *, const void *, const void *, void *, void *, void *, int,
-                cudaStream_t) override {
-    // (neither coupling of the torques has a backward pass in this mode)
-    throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the NOWALL, BOTTOM and SLIT geometries");
+  // The triply periodic mobility with the derivative-kernel coupling is
+  // symmetric (interpolation = hx hy hz x the transpose of spreading, the
+  // Fourier solve and the curl pair self-adjoint), so dl/dF and dl/dT are
+  // the Mdot of (gV, gW).  The position gradient is not provided here.
+  void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT, void *gX,
+                int dtype, cudaStream_t s) override {
+    (void)F;
+    (void)T;
+    if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
+    if (N == 0) return;
+    if (gV == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gV must not be NULL");
+    if (gX != nullptr)
+      throw Error(DPST_ERR_UNSUPPORTED, "the position gradient is available for the NOWALL, BOTTOM and SLIT geometries");
+    if (reg)
+      throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the derivative-kernel torque coupling");
+    if (gW != nullptr && !p.has_torque) throw Error(DPST_ERR_INVALID_ARG, "gW needs an operator created with torques");
+    if (gT != nullptr && !p.has_torque) throw Error(DPST_ERR_INVALID_ARG, "gT needs an operator created with torques");
+    if (gF == nullptr && gT == nullptr) return;
+    // gF is needed as the V output of the Mdot even when not requested
+    if (gF == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gF must be given in the triply periodic mode");
+    mdot(gV, gW, gF, gT, dtype, s);
   }
 
   void info(dpst_info *o) const override {

@@ -151,7 +151,7 @@ def test_info_multi_and_unsupported_calls():
         Vs, Ws = _mdot(op, Fk[k], Tk[k])
         assert rel_err(Vm[k].cpu().numpy(), Vs) < 1e-13
         assert rel_err(Wm[k].cpu().numpy(), Ws) < 1e-13
-    # no backward in this mode
+    # no position gradient in this mode
     gV = torch.ones((w.N, 3), dtype=torch.float64, device=op.device)
     with pytest.raises(DPStokesError):
         op.mdot_backward(torch.tensor(F, device=op.device), torch.tensor(T, device=op.device), gV, gV)
@@ -250,3 +250,37 @@ def test_fused_z_path_matches_cufft_path(name, precision, monkeypatch):
     assert ev < tol
     if Wc is not None:
         assert rel_err(Wf, Wc) < tol
+
+
+@pytest.mark.parametrize("name", ["s_tp_t", "t0_tp_n2048"])
+def test_backward_forces_torques(name):
+    """dl/dF, dl/dT of l = <gV, V> + <gW, W>: the transpose identity
+    <gV, V> + <gW, W> = <dl/dF, F> + <dl/dT, T> (FP64, 1e-12 of the terms'
+    scale) and, per component, the oracle's M (gV, gW) (1e-10)."""
+    w = W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    X, F, T = W.make_inputs(w)
+    op = _op(w, X)
+    d = op.device
+    rng = np.random.default_rng(4)
+    gV = rng.standard_normal(F.shape)
+    gW = rng.standard_normal(F.shape) if T is not None else None
+    V, Wv = _mdot(op, F, T)
+    gF, gT, gX = op.mdot_backward(torch.tensor(F, device=d), torch.tensor(T, device=d) if T is not None else None,
+                                  torch.tensor(gV, device=d), torch.tensor(gW, device=d) if gW is not None else None,
+                                  need_F=True, need_T=T is not None, need_X=False)
+    assert gX is None
+    gF = gF.cpu().numpy()
+    lhs = float(np.sum(gV * V.reshape(gV.shape)))
+    rhs = float(np.sum(gF * F))
+    if T is not None:
+        gT = gT.cpu().numpy()
+        lhs += float(np.sum(gW * Wv.reshape(gW.shape)))
+        rhs += float(np.sum(gT * T))
+    scale = float(np.linalg.norm(gF) * np.linalg.norm(F))
+    print("%s transpose identity %.3e vs %.3e" % (name, lhs, rhs))
+    assert abs(lhs - rhs) <= 1e-12 * scale
+    Vo, Wo = O.mdot(O.Params(**w.oracle_params()), X, gV, gW)
+    assert rel_err(gF, Vo) < TOL_FP64
+    if T is not None:
+        assert rel_err(gT, Wo) < TOL_FP64
+    op.close()
