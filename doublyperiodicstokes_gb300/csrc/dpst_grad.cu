@@ -51,6 +51,21 @@ __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelD
     if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
     gs.gy[p * kd.wy + j] = (R)g1;
     if (DIPOLE) gs.gdy[p * kd.wy + j] = (R)g2;
+  } else if (kd.unif_z) {  // uniform periodic z: the window of locate_item's uniform branch
+    const int k = e - kd.wx - kd.wy;
+    const int wz = kd.wz_max;
+    const int zclose = cl.z - kd.dend + wz / 2 - kd.evenz;
+    const double o = ((double)zclose + k - wz / 2 + kd.evenz) * kd.hz - pos[3 * p + 2];
+    if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+    g1 *= kd.inv_norm3;
+    g2 *= kd.inv_norm3;
+    const double wgt = g.hx * g.hy * kd.hz;
+    gs.gz[p * kd.wz_max + k] = (R)g1;
+    gs.gzw[p * kd.wz_max + k] = (R)(g1 * wgt);
+    if (DIPOLE) {
+      gs.gdz[p * kd.wz_max + k] = (R)g2;
+      gs.gdzw[p * kd.wz_max + k] = (R)(g2 * wgt);
+    }
   } else {
     const int k = e - kd.wx - kd.wy;
     double wgt = 0.0;

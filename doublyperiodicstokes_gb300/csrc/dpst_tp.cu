@@ -40,6 +40,23 @@
 
 namespace dpst {
 
+// backward-pass kernels (dpst_grad.cu)
+template <typename R>
+void launch_locate_grad(bool dipole, const double *pos, int64_t N, const KernelDesc &kd, const double *zext,
+                        const double *wext, const GridArgs &g, const Stencils<R> &st, const GradStencils<R> &gs,
+                        cudaStream_t s);
+template <typename R, typename RG>
+void launch_adj_spread_dip(const RG *gW, int64_t N, const KernelDesc &kd, const GridArgs &g, const Stencils<R> &st,
+                           R *grid, const Ghosts<R> &gh, cudaStream_t s);
+template <typename R, typename RF>
+void launch_gather_mono(const R *u, const R *psi, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                        const Stencils<R> &st, const GradStencils<R> &gs, const Ghosts<R> &ghu,
+                        const Ghosts<R> &ghp, const RF *F, const RF *gV, RF *gF, RF *gX, cudaStream_t s);
+template <typename R, typename RF>
+void launch_gather_dip(const R *u, const R *psi, int64_t N, const KernelDesc &kd, const GridArgs &g,
+                       const Stencils<R> &st, const GradStencils<R> &gs, const Ghosts<R> &ghu,
+                       const Ghosts<R> &ghp, const RF *T, const RF *gW, RF *gT, RF *gX, cudaStream_t s);
+
 template <typename R>
 struct Cplx;
 template <>
@@ -566,9 +583,10 @@ struct EngineTP : EngineBase {
       DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
   }
 
-  // torque: the torque grid holds spread torques (regular-kernel coupling)
-  void solve_stage(bool torque, cudaStream_t s) {
-    R *gr = grid.as<R>();
+  // torque: the torque grid holds spread torques (regular-kernel coupling);
+  // on: the grid to solve in place (default: the operator's grid)
+  void solve_stage(bool torque, cudaStream_t s, R *on = nullptr) {
+    R *gr = on ? on : grid.as<R>();
     CR *sp = spec.as<CR>();
     DPST_CUFFT(cufftSetStream(plan_f, s));
     exec_fwd(gr, sp);
@@ -686,27 +704,96 @@ struct EngineTP : EngineBase {
     DPST_CUDA(cudaMemcpyAsync(out, grid.p, grid.bytes, cudaMemcpyDeviceToDevice, s));
   }
 
-  // The triply periodic mobility with the derivative-kernel coupling is
-  // symmetric (interpolation = hx hy hz x the transpose of spreading, the
-  // Fourier solve and the curl pair self-adjoint), so dl/dF and dl/dT are
-  // the Mdot of (gV, gW).  The position gradient is not provided here.
+  // ---- backward pass ---------------------------------------------------------
+  // The same structure as the doubly periodic backward (dpst_engine.cu): the
+  // adjoint source J^T (gV, gW) spread with the interpolation's weights, the
+  // adjoint of the grid-to-grid map applied to it, the gathers S^T psi (dl/dF,
+  // dl/dT) and, for dl/dX, the derivatives of the stencil factors against the
+  // recomputed forward grid u and psi.  The triply periodic grid-to-grid map
+  // (real transforms, the Fourier solve, 1/(nx ny nz)) is self-adjoint, so psi
+  // is the forward solve of the adjoint source.
+  DevBuf grid2, gs_m[4], gs_d[8];
+  GradStencils<R> gsm, gsd;
+  bool grad_ready = false;
+
+  void ensure_grad() {
+    if (grad_ready) return;
+    grid2.alloc(grid.bytes);
+    const size_t n = (size_t)std::max<int64_t>(N, 1);
+    memset(&gsm, 0, sizeof(gsm));
+    memset(&gsd, 0, sizeof(gsd));
+    gs_m[0].alloc(sizeof(R) * n * km.d.wx);
+    gs_m[1].alloc(sizeof(R) * n * km.d.wy);
+    gs_m[2].alloc(sizeof(R) * n * km.d.wz_max);
+    gs_m[3].alloc(sizeof(R) * n * km.d.wz_max);
+    gsm.gx = gs_m[0].as<R>();
+    gsm.gy = gs_m[1].as<R>();
+    gsm.gz = gs_m[2].as<R>();
+    gsm.gzw = gs_m[3].as<R>();
+    if (p.has_torque) {
+      const KernelDesc &d = kd.d;
+      const int w[8] = {d.wx, d.wy, d.wz_max, d.wz_max, d.wx, d.wy, d.wz_max, d.wz_max};
+      for (int q = 0; q < 8; ++q) gs_d[q].alloc(sizeof(R) * n * w[q]);
+      gsd.gx = gs_d[0].as<R>();
+      gsd.gy = gs_d[1].as<R>();
+      gsd.gz = gs_d[2].as<R>();
+      gsd.gzw = gs_d[3].as<R>();
+      gsd.gdx = gs_d[4].as<R>();
+      gsd.gdy = gs_d[5].as<R>();
+      gsd.gdz = gs_d[6].as<R>();
+      gsd.gdzw = gs_d[7].as<R>();
+    }
+    grad_ready = true;
+  }
+
+  template <typename RF>
+  void run_backward(const RF *F, const RF *T, const RF *gV, const RF *gW, RF *gF, RF *gT, RF *gX,
+                    cudaStream_t s) {
+    const bool torque = p.has_torque && T != nullptr;
+    const bool want_x = gX != nullptr;
+    ensure_grad();
+    R *gr = grid.as<R>(), *g2 = grid2.as<R>();
+    if (want_x) {
+      launch_locate_grad<R>(false, pos64.as<double>(), N, km.d, nullptr, nullptr, g, stm, gsm, s);
+      if (p.has_torque) launch_locate_grad<R>(true, pos64.as<double>(), N, kd.d, nullptr, nullptr, g, std_, gsd, s);
+      spread_stage<RF>(F, T, s);  // the forward's velocity grid, recomputed
+      solve_stage(false, s);
+    }
+    DPST_CUDA(cudaMemsetAsync(g2, 0, grid2.bytes, s));
+    Stencils<R> sw = stm;
+    sw.phz = stm.phzw;  // the interpolation's weights
+    launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, none, s, perm.as<int>());
+    if (gW) launch_adj_spread_dip<R, RF>(gW, N, kd.d, g, std_, g2, none, s);
+    DPST_CUDA(cudaGetLastError());
+    solve_stage(false, s, g2);  // psi
+    if (gF || want_x)
+      launch_gather_mono<R, RF>(want_x ? gr : nullptr, g2, N, km.d, g, stm, gsm, none, none, F, gV, gF, gX, s);
+    if (p.has_torque && (gT || (want_x && (torque || gW))))
+      launch_gather_dip<R, RF>(want_x ? gr : nullptr, g2, N, kd.d, g, std_, gsd, none, none, torque ? T : nullptr, gW,
+                               gT, gX, s);
+    DPST_CUDA(cudaGetLastError());
+  }
+
   void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT, void *gX,
                 int dtype, cudaStream_t s) override {
-    (void)F;
-    (void)T;
     if (!positioned) throw Error(DPST_ERR_NOT_READY, "positions have not been set");
     if (N == 0) return;
     if (gV == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gV must not be NULL");
-    if (gX != nullptr)
-      throw Error(DPST_ERR_UNSUPPORTED, "the position gradient is available for the NOWALL, BOTTOM and SLIT geometries");
     if (reg)
       throw Error(DPST_ERR_UNSUPPORTED, "the backward pass is available for the derivative-kernel torque coupling");
+    if (gX != nullptr && F == nullptr)
+      throw Error(DPST_ERR_INVALID_ARG, "the position gradient needs the forces F of the forward call");
     if (gW != nullptr && !p.has_torque) throw Error(DPST_ERR_INVALID_ARG, "gW needs an operator created with torques");
-    if (gT != nullptr && !p.has_torque) throw Error(DPST_ERR_INVALID_ARG, "gT needs an operator created with torques");
-    if (gF == nullptr && gT == nullptr) return;
-    // gF is needed as the V output of the Mdot even when not requested
-    if (gF == nullptr) throw Error(DPST_ERR_INVALID_ARG, "gF must be given in the triply periodic mode");
-    mdot(gV, gW, gF, gT, dtype, s);
+    if (gT != nullptr && (T == nullptr || !p.has_torque))
+      throw Error(DPST_ERR_INVALID_ARG, "gT needs an operator created with torques and the torques T");
+    if (dtype == DPST_F64)
+      run_backward<double>((const double *)F, (const double *)T, (const double *)gV, (const double *)gW,
+                           (double *)gF, (double *)gT, (double *)gX, s);
+    else if (dtype == DPST_F32)
+      run_backward<float>((const float *)F, (const float *)T, (const float *)gV, (const float *)gW, (float *)gF,
+                          (float *)gT, (float *)gX, s);
+    else
+      throw Error(DPST_ERR_INVALID_ARG, "dtype must be DPST_F64 or DPST_F32");
   }
 
   void info(dpst_info *o) const override {
@@ -731,7 +818,7 @@ struct EngineTP : EngineBase {
     o->z_fused = zfused ? 1 : 0;
     int64_t b = 0;
     const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf,
-                           &gridT, &specT, &twz};
+                           &gridT, &specT, &twz, &grid2};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     o->device_bytes = b;

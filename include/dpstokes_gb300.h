@@ -243,9 +243,9 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
  * the stencil's discrete choices (nearest node, z window) have zero
  * derivative; dl/dX is the gradient of the operator between those events.
  * Buffers for the backward pass are allocated on its first call.
- * Mode PERIODIC: gF (required) and gT only, computed as the Mdot of (gV, gW)
- * (the triply periodic operator is symmetric); gX returns
- * DPST_ERR_UNSUPPORTED, as does torque_kernel = DPST_TORQUE_REG. */
+ * Mode PERIODIC: the same outputs (its grid-to-grid map is self-adjoint, so
+ * the adjoint solve is the forward one).  torque_kernel = DPST_TORQUE_REG
+ * returns DPST_ERR_UNSUPPORTED. */
 int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *gV, const void *gW,
                        void *gF, void *gT, void *gX, int dtype, void *stream);
 

@@ -3,8 +3,9 @@ wrapper doublyperiodicstokes_gb300.mdot).
 
 For l = <gV, V> + <gW, W> with (V, W) = M(X) (F, T):
   * transpose identity <gV, V> + <gW, W> = <dl/dF, F> + <dl/dT, T> on every
-    small case (each geometry, torques, ghost-layer reuse at open ends, odd
-    grids), FP64, to 1e-12 of the terms' scale;
+    small case (each geometry including the triply periodic mode, torques,
+    ghost-layer reuse at open ends, odd grids), FP64, to 1e-12 of the terms'
+    scale;
   * dl/dF, dl/dT against the oracle's M^T g assembled column by column from
     the oracle's own forward (which matches the reference to ~1e-15), 1e-10;
   * dl/dX against central differences of the oracle's forward (step 1e-6),
@@ -62,7 +63,7 @@ def _loss(V, Wv, gV, gW):
     return l
 
 
-@pytest.mark.parametrize("name", [w.name for w in W.SMALL])
+@pytest.mark.parametrize("name", [w.name for w in W.SMALL + W.SMALL_TP])
 def test_transpose_identity(name):
     w = W.SMALL_BY_NAME[name]
     X, F, T = W.make_inputs(w)
@@ -116,7 +117,7 @@ def _oracle_fd(w, X, F, T, gV, gW, coords=None, h=FD_STEP):
     return gX
 
 
-@pytest.mark.parametrize("name", [w.name for w in W.SMALL])
+@pytest.mark.parametrize("name", [w.name for w in W.SMALL + W.SMALL_TP])
 def test_gradients_match_oracle(name):
     w = W.SMALL_BY_NAME[name]
     X, F, T = W.make_inputs(w)

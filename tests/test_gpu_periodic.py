@@ -151,11 +151,15 @@ def test_info_multi_and_unsupported_calls():
         Vs, Ws = _mdot(op, Fk[k], Tk[k])
         assert rel_err(Vm[k].cpu().numpy(), Vs) < 1e-13
         assert rel_err(Wm[k].cpu().numpy(), Ws) < 1e-13
-    # no position gradient in this mode
-    gV = torch.ones((w.N, 3), dtype=torch.float64, device=op.device)
-    with pytest.raises(DPStokesError):
-        op.mdot_backward(torch.tensor(F, device=op.device), torch.tensor(T, device=op.device), gV, gV)
     op.close()
+    # no backward with the regular-kernel coupling
+    import dataclasses
+    wr = dataclasses.replace(w, reg_kernel=True)
+    opr = _op(wr, X)
+    gV = torch.ones((w.N, 3), dtype=torch.float64, device=opr.device)
+    with pytest.raises(DPStokesError):
+        opr.mdot_backward(torch.tensor(F, device=opr.device), torch.tensor(T, device=opr.device), gV, gV)
+    opr.close()
     # no batched systems in this mode
     L = _lib.lib()
     prm = StokesParams.from_workload(w).to_c()
