@@ -465,8 +465,9 @@ def run_multi_rhs(args, dev):
 
 def run_periodic(args, dev):
     """Triply periodic Mdot on t1_tp_n65536 (512 x 512 x 64, N = 65,536,
-    torques): mixed and FP64 operators, device milliseconds per Mdot, the
-    CUDA-event stage split with each stage's HBM fraction, mixed vs FP64."""
+    torques): mixed and FP64 operators, device milliseconds per Mdot and per
+    backward (dl/dF, dl/dT, dl/dX), the CUDA-event stage split with each
+    stage's HBM fraction, mixed vs FP64."""
     import torch
     from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W
     w = W.T1
@@ -504,9 +505,22 @@ def run_periodic(args, dev):
                 gbs = b / (v * 1e-3) / 1e9
                 roof[k] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4)}
         res[precision] = (V.double().clone(), Wd.double().clone())
+        # backward: dl/dF, dl/dT, dl/dX of l = <gV, V> + <gW, W>
+        gVd = torch.tensor(np.random.default_rng(12).standard_normal(F.shape), dtype=dt, device=dev)
+        gWd = torch.tensor(np.random.default_rng(13).standard_normal(F.shape), dtype=dt, device=dev)
+        for _ in range(max(3, args.warmup)):
+            op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True)
+        e1.record()
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1) / reps
         out[precision] = {"ms_per_mdot": ms, "particles_per_s": w.N / (ms / 1e3),
                           "stages_ms": {k: round(v, 4) for k, v in st.items()}, "stage_hbm": roof,
-                          "kernels_per_mdot": op.info()["kernels_per_mdot"]}
+                          "kernels_per_mdot": op.info()["kernels_per_mdot"],
+                          "backward_ms": bms, "bwd_fwd_ratio": bms / ms, "backward_grads": ["F", "T", "X"]}
         op.close()
     rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
     out["rel_err_V_mixed_vs_fp64"] = rel(res["mixed"][0], res["fp64"][0])
