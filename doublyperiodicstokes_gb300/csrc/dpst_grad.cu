@@ -28,6 +28,19 @@ namespace dpst {
 // then wz_max z factors; at the stencil k_locate chose (st.cell), with its
 // offsets and clamping.
 // ---------------------------------------------------------------------------
+// FP64 for the FP64 operator, FP32 transcendentals for the mixed one.
+template <typename R>
+static __device__ __forceinline__ void pos_derivs(double o, const KernelDesc &kd, double &g1, double &g2) {
+  if constexpr (sizeof(R) == 8) {
+    es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+  } else {
+    float f1, f2;
+    es_pos_derivs_f(o, kd.beta, kd.alpha2, f1, f2);
+    g1 = f1;
+    g2 = f2;
+  }
+}
+
 template <typename R, bool DIPOLE>
 __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelDesc kd,
                               const double *__restrict__ zext, const double *__restrict__ wext, GridArgs g,
@@ -42,13 +55,13 @@ __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelD
   double g1 = 0.0, g2 = 0.0;
   if (e < kd.wx) {
     const double o = ((double)cl.x + e - kd.wx / 2 + kd.evenx) * g.hx - pos[3 * p];
-    if (!(o > thr || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+    if (!(o > thr || o < -thr)) pos_derivs<R>(o, kd, g1, g2);
     gs.gx[p * kd.wx + e] = (R)g1;
     if (DIPOLE) gs.gdx[p * kd.wx + e] = (R)g2;
   } else if (e < kd.wx + kd.wy) {
     const int j = e - kd.wx;
     const double o = ((double)cl.y + j - kd.wy / 2 + kd.eveny) * g.hy - pos[3 * p + 1];
-    if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+    if (!(thr < o || o < -thr)) pos_derivs<R>(o, kd, g1, g2);
     gs.gy[p * kd.wy + j] = (R)g1;
     if (DIPOLE) gs.gdy[p * kd.wy + j] = (R)g2;
   } else if (kd.unif_z) {  // uniform periodic z: the window of locate_item's uniform branch
@@ -56,7 +69,7 @@ __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelD
     const int wz = kd.wz_max;
     const int zclose = cl.z - kd.dend + wz / 2 - kd.evenz;
     const double o = ((double)zclose + k - wz / 2 + kd.evenz) * kd.hz - pos[3 * p + 2];
-    if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+    if (!(thr < o || o < -thr)) pos_derivs<R>(o, kd, g1, g2);
     g1 *= kd.inv_norm3;
     g2 *= kd.inv_norm3;
     const double wgt = g.hx * g.hy * kd.hz;
@@ -71,7 +84,7 @@ __global__ void k_locate_grad(const double *__restrict__ pos, int64_t N, KernelD
     double wgt = 0.0;
     if (k < cl.w) {
       const double o = zext[kd.zext_off + cl.z + k] - pos[3 * p + 2];
-      if (!(thr < o || o < -thr)) es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
+      if (!(thr < o || o < -thr)) pos_derivs<R>(o, kd, g1, g2);
       g1 *= kd.inv_norm3;
       g2 *= kd.inv_norm3;
       wgt = g.hx * g.hy * wext[kd.zext_off + cl.z + k];

@@ -51,6 +51,24 @@ static __device__ __forceinline__ R des1r(double o, const KernelDesc &kd) {
   }
 }
 
+// es_pos_derivs for the mixed operator's FP32 stencils: 1 - o^2/alpha^2 in
+// FP64 (it cancels near the support's edge), the square root, exponential
+// and quotients in FP32.
+static __device__ __forceinline__ void es_pos_derivs_f(double o, double beta, double alpha2, float &g1, float &g2) {
+  const double qd = o * o / alpha2;
+  const double s2d = 1.0 - qd;
+  if (!(s2d > 0.0)) {
+    g1 = 0.0f;
+    g2 = 0.0f;
+    return;
+  }
+  const float x = (float)o, a2 = (float)alpha2, b = (float)beta;
+  const float s2 = (float)s2d, q = (float)qd, s = sqrtf(s2);
+  const float phi = expf(b * (s - 1.0f));
+  g1 = b * x * phi / (a2 * s);
+  g2 = (b / a2) * phi * (1.0f / s - b * q / s2 + q / (s2 * s));
+}
+
 // Position derivatives of one stencil factor.  The forward evaluates
 // phi(o) (and phi'(o) for the dipole kernel) at o = node - x, so
 // d/dx phi(o) = -phi'(o) -> g1 and d/dx phi'(o) = -phi''(o) -> g2, with

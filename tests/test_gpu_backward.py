@@ -152,7 +152,7 @@ def test_autograd_matches_direct():
     assert rel_err(_np(Xt.grad), dX) < 1e-12
 
 
-@pytest.mark.parametrize("name", ["s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_f_top"])
+@pytest.mark.parametrize("name", ["s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_f_top", "s_tp_t"])
 def test_mixed_backward_matches_fp64(name):
     w = W.SMALL_BY_NAME[name]
     X, F, T = W.make_inputs(w)
