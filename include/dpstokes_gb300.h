@@ -79,12 +79,14 @@ extern "C" {
 #define DPST_MODE_PERIODIC 3 /* triply periodic: nz uniform points on the periodic
                                 [zmin, zmax); the reference GPU module's mode
                                 'periodic' (uammd_wrapper.cu:122-126) and CPU
-                                domType 'TP' (TPTools.cpp:6-46).  dpst_create only:
-                                no batched, multi-column solve sharing or backward */
+                                domType 'TP' (TPTools.cpp:6-46).  dpst_create only
+                                (no batched systems); multi-column Mdot runs column
+                                by column */
 
 /* arithmetic of the operator */
 #define DPST_PREC_FP64 0  /* every stage in FP64: the drop-in for the reference */
-#define DPST_PREC_MIXED 1 /* FP32 spread/FFT/interp, FP32 z transform, FP64 BVP */
+#define DPST_PREC_MIXED 1 /* FP32 spread/FFT/interp, FP32 z transform, FP64 BVP
+                             (PERIODIC: FP32 throughout; its solve is elementwise) */
 
 /* torque coupling (has_torque) */
 #define DPST_TORQUE_DERIV 0 /* derivative ES kernels spread the torque curl and interpolate the
