@@ -7,10 +7,11 @@
 The backward is the library's dpst_mdot_backward: the transpose of the
 operator applied to the incoming gradients (the adjoint of every stage:
 interpolation, x-y FFT, z transform, per-wavenumber solve, wall correction,
-spreading) for dl/dF and dl/dT, and the ES-kernel derivatives in the
-spreading and interpolation weights for dl/dX.  The forward's velocity grid
-is recomputed in the backward rather than kept.  Second derivatives are not
-provided."""
+spreading; in the triply periodic box the grid-to-grid map is self-adjoint)
+for dl/dF and dl/dT, and the ES-kernel derivatives in the spreading and
+interpolation weights for dl/dX.  The forward's velocity grid is recomputed
+in the backward rather than kept.  Second derivatives and the
+regular-kernel torque coupling are not provided."""
 import torch
 from torch.autograd.function import once_differentiable
 
