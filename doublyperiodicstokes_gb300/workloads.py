@@ -222,7 +222,18 @@ SMALL_EDGE = [
     replace(small("e_dpbw_t_reg", "DPBW", 16, 16, 17, 10.0, 0.0, 10.0, True, seed=18), layout="edge",
             reg_kernel=True),
 ]
-SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP + SMALL_REG + SMALL_EDGE}
+# Unequal monopole / dipole widths (the reference's torque kernel types 3, 4
+# and 5: w_m / w_d = 6/5, 6/4, 5/4 with their betas, GridAndKernelConfig.py):
+# separate monopole and dipole passes.
+SMALL_KT = [
+    replace(small("s_dpbw_t_k3", "DPBW", 24, 16, 17, 10.0, 1.5, 8.5, True, seed=19), wm=6, wd=5,
+            betam_hat=1.3261, betad_hat=1.7584),
+    replace(small("s_dpsc_t_k4", "DPSC", 24, 16, 21, 10.0, 1.0, 9.0, True, seed=20), wm=6, wd=4,
+            betam_hat=1.5728, betad_hat=1.5115),
+    replace(small("s_tp_t_k5", "TP", 24, 16, 16, 16.0, 0.0, 16.0, True, seed=21), wm=5, wd=4,
+            betam_hat=1.3536, betad_hat=1.7147),
+]
+SMALL_BY_NAME = {w.name: w for w in SMALL + SMALL_TP + SMALL_REG + SMALL_EDGE + SMALL_KT}
 
 
 def small_batch(domType, has_torque, seed=40):

@@ -59,7 +59,7 @@ if __name__ == "__main__":
     ap.add_argument("--full", action="store_true", help="also the full-size c0, c3, c1, t0 cases")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
-    todo = list(W.SMALL) + list(W.SMALL_TP) + list(W.SMALL_REG) + list(W.SMALL_EDGE)
+    todo = list(W.SMALL) + list(W.SMALL_TP) + list(W.SMALL_REG) + list(W.SMALL_EDGE) + list(W.SMALL_KT)
     if a.full:
         todo += [W.C0, W.C3, W.C1, W.T0]
     for w in todo:
