@@ -101,7 +101,10 @@ class ClockSampler:
 
 
 def algorithmic_bytes(stage, w, prec):
-    """Bytes a stage must move at minimum for one Mdot."""
+    """Bytes a stage must move at minimum for one Mdot: the grid (3 nx ny nz
+    values) and / or the spectrum (3 nz ny (nx/2+1) complex values) once in
+    and once out, the per-wavenumber factors of the solve, and the particle
+    data."""
     s = 4 if prec == "mixed" else 8
     nxh = w.nx // 2 + 1
     nk = w.ny * nxh
@@ -152,7 +155,7 @@ def run_ours(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = W.CONFIGS[args.workload]
+    w = W.by_name(args.workload)
     X, F, T = W.make_inputs(w)
     prec = args.precision
     dt = torch.float32 if prec == "mixed" else torch.float64
@@ -646,7 +649,7 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     from doublyperiodicstokes_gb300 import workloads as W
-    w = W.CONFIGS[args.workload]
+    w = W.by_name(args.workload)
     config = {"workload": w.name, "domain": w.domType, "N": w.N, "grid": [w.nx, w.ny, w.nz],
               "box": [w.Lx, w.Ly, w.Lz], "torques": w.has_torque, "kernel_w": w.wm,
               "precision": args.precision, "l2": "inputs larger than L2 (grid > 129 MB)",

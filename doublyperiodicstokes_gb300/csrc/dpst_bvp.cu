@@ -809,18 +809,19 @@ cudaError_t launch_bvp(const KsArgs &a, R *spec, double2 *corr, double *scratch,
 // Allocation-free launch of the same solve for dpst_mdot_noalloc.
 //
 // Some callers cannot allocate device memory at the moment they need the
-// operator: code that runs inside a CUDA stream capture in global capture
-// mode (cudaMalloc is not permitted there), or a host whose own allocator has
-// already reserved the device.  For them the solve's scratch (the pressure
-// coefficients of every lane, nz doubles per lane) comes from the file-scope
-// array below instead of memory owned by the handle.  The array is 4 MiB;
-// every GPU that loads the library holds it until the process exits.  The
-// solve writes each lane's scratch before reading it, so nothing needs
-// clearing between calls, but all calls share the one array: calls that
-// overlap on the GPU (other streams, other handles, other threads) race on
-// it and must be serialised by the caller.  The kernel is launched on as many
-// CTAs as the array holds (192 lanes x nz doubles each), at most the grid of
-// the ordinary solve.
+// operator: a host application whose own memory pool has already reserved
+// the device (a cudaMalloc from the library would fail, or take memory the
+// pool counts on), or a time-critical loop that must not pay for cudaMalloc /
+// cudaFree and the device-wide synchronisation cudaFree implies.  For them the
+// solve's scratch (the pressure coefficients of every lane, nz doubles per
+// lane) comes from the file-scope array below instead of memory owned by the
+// handle.  The array is 4 MiB; every GPU that loads the library holds it
+// until the process exits.  The solve writes each lane's scratch before
+// reading it, so nothing needs clearing between calls, but all calls share
+// the one array: calls that overlap on the GPU (other streams, other handles,
+// other threads) race on it and must be serialised by the caller.  The kernel
+// is launched on as many CTAs as the array holds (192 lanes x nz doubles
+// each), at most the grid of the ordinary solve.
 // ---------------------------------------------------------------------------
 constexpr size_t NOALLOC_SCRATCH_DOUBLES = (size_t)1 << 19;  // 4 MiB
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
@@ -828,17 +829,23 @@ static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLE
 static std::mutex g_noalloc_mu;
 static double *g_noalloc_ptr[256];  // device address of the array, per device
 
-// The symbol's device address is looked up once per device, with that
-// device current, on the first call there (so that first call must not be
-// made during a stream capture).  In host code the array's name is only a
-// host-side stand-in and must never be passed to a kernel.
-static cudaError_t noalloc_scratch_ptr(double **out) {
+// The array's device address, looked up with the device current.  In host
+// code the array's name is only a host-side stand-in and must never be
+// passed to a kernel.  The first call on a device does this set-up, so it
+// must come before any stream capture on that device; later calls look the
+// address up again whenever the stream is not capturing (the module may
+// have been reloaded at another address after a device reset) and use the
+// address found last while it is.
+static cudaError_t noalloc_scratch_ptr(cudaStream_t s, double **out) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
   if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  err = cudaStreamIsCapturing(s, &cap);
+  if (err != cudaSuccess) return err;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  if (cap == cudaStreamCaptureStatusNone || g_noalloc_ptr[dev] == nullptr) {
     void *p = nullptr;
     err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (err != cudaSuccess) return err;
@@ -860,7 +867,7 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
     return cudaErrorInvalidValue;
   }
   double *scratch = nullptr;
-  cudaError_t err = noalloc_scratch_ptr(&scratch);
+  cudaError_t err = noalloc_scratch_ptr(s, &scratch);
   if (err != cudaSuccess) return err;
   int64_t grid = (int64_t)(NOALLOC_SCRATCH_DOUBLES / per_cta);
   if (grid > planned_grid) grid = planned_grid;

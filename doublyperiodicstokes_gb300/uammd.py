@@ -11,7 +11,8 @@ source/gpu/python_wrapper/uammd_python.cpp:59-129:
     uammd.DPStokes().initialize(par, N) / .setPositions(pos)
         / .Mdot(forces, torques, velocities, angularVelocities) / .clear()
 
-Importing this module as `uammd` makes that wrapper run
+Importing this module as `uammd` (put this package's directory first on
+sys.path, or alias it in sys.modules) makes that wrapper run
 on libdpstokes_gb300.so through its host-array C entry points, with host
 NumPy arrays in and out exactly as the reference glue copies them
 (uammd_wrapper.cu:136-170).  No torch is needed.

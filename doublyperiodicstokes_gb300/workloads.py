@@ -115,20 +115,6 @@ C2 = Workload("c2_dp_n65536", "DP", 65536, 512.0, 512.0, 512, 512, 128, -20.5, 4
               True, betam_hat=1.3267, betad_hat=2.2160)
 C3 = Workload("c3_dpbw_n8192", "DPBW", 8192, 192.0, 192.0, 192, 192, 64, 0.0, 24.0, 1.5, 22.5,
               False, betam_hat=1.714)
-# The c2 geometry (open domain, nz = 128, Lz = 41, torques) on a 192 x 192 grid:
-# a few-hundred-MB case for ncu captures of the c2 kernels.
-P2 = Workload("p2_dp_n8192_192", "DP", 8192, 192.0, 192.0, 192, 192, 128, -20.5, 41.0, -16.0, 16.0,
-              True, betam_hat=1.3267, betad_hat=2.2160)
-# The c2 geometry and particle density on a 320 x 320 grid: a 157 MB grid
-# (larger than L2) in about 1 GB of device memory, for full ncu captures of
-# the particle kernels.
-P3 = Workload("p3_dp_n25600_320", "DP", 25600, 320.0, 320.0, 320, 320, 128, -20.5, 41.0, -16.0, 16.0,
-              True, betam_hat=1.3267, betad_hat=2.2160)
-# The c2 geometry and particle density on a 384 x 384 grid: 74,112 wavenumbers
-# (enough for the solve's hybrid kernel, which c2 uses) in about 1.2 GB on the
-# device, for full ncu captures of the solve.
-P4 = Workload("p4_dp_n36864_384", "DP", 36864, 384.0, 384.0, 384, 384, 128, -20.5, 41.0, -16.0, 16.0,
-              True, betam_hat=1.3267, betad_hat=2.2160)
 # Triply periodic configurations (the reference's domType 'TP'): the c0 box
 # and density on a 128 x 128 x 32 grid (reference fixture size), and the c2
 # particle count, kernels and torques in a 512 x 512 x 64 periodic box (h = 1).
@@ -142,7 +128,25 @@ T1 = Workload("t1_tp_n65536", "TP", 65536, 512.0, 512.0, 512, 512, 64, 0.0, 64.0
 # operators).
 L1 = Workload("l1_dp_n262144_1024", "DP", 262144, 1024.0, 1024.0, 1024, 1024, 128, -20.5, 41.0, -16.0, 16.0,
               True, betam_hat=1.3267, betad_hat=2.2160)
-CONFIGS = {w.name: w for w in (C0, C1, C2, C3, P2, P3, P4, T0, T1, L1)}
+CONFIGS = {w.name: w for w in (C0, C1, C2, C3, T0, T1, L1)}
+
+
+def scaled(w: Workload, n: int) -> Workload:
+    """w with the same z geometry, grid spacing and particle density on an
+    n x n grid (box side n h, N scaled by the area), named
+    '<w.name>@<n>'; e.g. scaled(C2, 384) is the open 384 x 384 x 128 box with
+    36,864 particles."""
+    h = w.Lx / w.nx
+    N = int(round(w.N * (n * n) / (w.nx * w.ny)))
+    return replace(w, name="%s@%d" % (w.name, n), N=N, Lx=n * h, Ly=n * h, nx=n, ny=n)
+
+
+def by_name(name: str) -> Workload:
+    """A named configuration, or '<name>@<n>' for scaled(CONFIGS[name], n)."""
+    if "@" in name:
+        base, n = name.split("@", 1)
+        return scaled(CONFIGS[base], int(n))
+    return CONFIGS[name]
 
 
 def fft_friendly(n):

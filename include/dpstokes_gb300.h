@@ -208,9 +208,11 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
 
 /* Allocation-free Mdot.  No counterpart in the reference.
  * For callers that cannot allocate device memory when they call the
- * operator -- code running inside a CUDA stream capture in global capture
- * mode, where cudaMalloc is not permitted, or a host whose own allocator has
- * reserved the device.  Same arguments and results as dpst_mdot; the call
+ * operator: a host application whose own memory pool has already reserved
+ * the device (a cudaMalloc from the library would fail, or take memory the
+ * pool counts on), or a time-critical loop that must not pay for cudaMalloc /
+ * cudaFree and the device-wide synchronisation cudaFree implies.  Same
+ * arguments and results as dpst_mdot; the call
  * allocates nothing (no cudaMalloc / cudaFree, no allocating library
  * routine): the per-wavenumber solve takes its scratch from a 4 MiB static
  * device array compiled into the library (held by every GPU that loads it
@@ -220,7 +222,8 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
  *     doubles) are rejected with DPST_ERR_UNSUPPORTED; every nz the library
  *     accepts (<= 128) fits;
  *   - the first call on a device looks up the array's device address with
- *     that device current; make that first call before any stream capture;
+ *     that device current; make that first call before any stream capture
+ *     (later calls look it up again whenever their stream is not capturing);
  *   - all calls share the one array: calls that overlap on the GPU (other
  *     streams, handles or threads) race on it and must be serialised. */
 int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void *W, int dtype,

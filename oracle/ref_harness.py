@@ -31,7 +31,7 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("DPST_REFERENCE_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("DPST_REFERENCE_ROOT", "")
 REF_LIB = os.path.join(HERE, "_ref")
 
 

@@ -12,7 +12,7 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("DPST_REFERENCE_ROOT", "/root/reference")
+REF = os.environ["DPST_REFERENCE_ROOT"]
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 XY = [  # Lx, Ly, radii, kernel types, optInd, has_torque, ref

@@ -38,3 +38,12 @@ def inputs(name):
     if h.hexdigest() != g["meta"]["input_sha256"]:
         raise AssertionError("regenerated inputs differ from the ones the fixture was made with")
     return w, X, F, T, g
+
+
+def restrict(g, A):
+    """A [N][3] (or flat 3N) output restricted to the particles the fixture
+    stores: all of them, or the subset g['idx'] of a full-size run."""
+    A = np.asarray(A).reshape(-1, 3)
+    if "idx" in g:
+        A = A[g["idx"]]
+    return A.ravel()

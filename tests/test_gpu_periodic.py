@@ -66,7 +66,7 @@ def test_fp64_stages_match_oracle(name):
 
 @pytest.mark.parametrize("name", [w.name for w in W.SMALL_TP] + ["t0_tp_n2048"])
 def test_mixed_close_to_fp64(name):
-    w = W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    w = W.SMALL_BY_NAME.get(name) or W.by_name(name)
     X, F, T = W.make_inputs(w)
     V64, W64 = _mdot(_op(w, X), F, T)
     V32, W32 = _mdot(_op(w, X, "mixed"), F.astype(np.float32), None if T is None else T.astype(np.float32),
@@ -233,7 +233,7 @@ def test_fused_z_path_matches_cufft_path(name, precision, monkeypatch):
     transforms (forced for FP64, the default for mixed) against cuFFT's 3-D
     transforms and the separate solve (FP64: 1e-12; mixed: 1e-6); nz = 13
     keeps the 3-D path."""
-    w = W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    w = W.SMALL_BY_NAME.get(name) or W.by_name(name)
     X, F, T = W.make_inputs(w)
     dt = torch.float64 if precision == "fp64" else torch.float32
     if T is not None and precision == "mixed":
@@ -261,7 +261,7 @@ def test_backward_forces_torques(name):
     """dl/dF, dl/dT of l = <gV, V> + <gW, W>: the transpose identity
     <gV, V> + <gW, W> = <dl/dF, F> + <dl/dT, T> (FP64, 1e-12 of the terms'
     scale) and, per component, the oracle's M (gV, gW) (1e-10)."""
-    w = W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    w = W.SMALL_BY_NAME.get(name) or W.by_name(name)
     X, F, T = W.make_inputs(w)
     op = _op(w, X)
     d = op.device

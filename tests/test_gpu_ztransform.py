@@ -29,11 +29,11 @@ def _mdot(op, X, F, T, dtype):
     return V.double().cpu().numpy(), (Wv.double().cpu().numpy() if Wv is not None else None)
 
 
-CASES = [w.name for w in W.SMALL] + ["p2_dp_n8192_192"]
+CASES = [w.name for w in W.SMALL] + ["c2_dp_n65536@192"]
 
 
 def _wl(name):
-    return W.SMALL_BY_NAME.get(name) or W.CONFIGS[name]
+    return W.SMALL_BY_NAME.get(name) or W.by_name(name)
 
 
 @pytest.mark.parametrize("name", CASES)

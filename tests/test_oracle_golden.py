@@ -14,10 +14,11 @@ FULL = [n for n in golden_io.names() if not n.startswith(("s_", "e_"))]
 def _check(name, tol):
     w, X, F, T, g = golden_io.inputs(name)
     V, Wv = O.mdot(O.Params(**w.oracle_params()), X, F, T)
-    assert rel_err(V, g["V"]) < tol
-    assert rel_err(g["V_repeat"], g["V"]) == 0.0
+    assert rel_err(golden_io.restrict(g, V), g["V"]) < tol
+    if "V_repeat" in g:
+        assert rel_err(g["V_repeat"], g["V"]) == 0.0
     if w.has_torque:
-        assert rel_err(Wv, g["W"]) < tol
+        assert rel_err(golden_io.restrict(g, Wv), g["W"]) < tol
 
 
 @pytest.mark.parametrize("name", SMALL)

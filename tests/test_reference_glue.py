@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("DPST_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("DPST_REFERENCE_ROOT", "")
 WRAP = os.path.join(REF, "source", "gpu", "python_wrapper")
 LIBDIR = os.path.join(ROOT, "doublyperiodicstokes_gb300", "lib")
 
