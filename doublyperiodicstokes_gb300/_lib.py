@@ -13,6 +13,7 @@ ERRORS = {1: "invalid argument", 2: "not ready", 3: "out of domain", 4: "CUDA er
           5: "unsupported", 6: "allocation failed"}
 MODE = {"nowall": 0, "bottom": 1, "slit": 2, "periodic": 3}
 PREC = {"fp64": 0, "mixed": 1}
+SOLVE = {"default": 0, "fp64": 1, "df64": 2}
 F64, F32 = 0, 1
 
 
@@ -23,7 +24,8 @@ class DpstParams(ctypes.Structure):
                 ("viscosity", ctypes.c_double), ("w", ctypes.c_int), ("beta", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("has_torque", ctypes.c_int), ("w_d", ctypes.c_int),
                 ("beta_d", ctypes.c_double), ("alpha_d", ctypes.c_double),
-                ("precision", ctypes.c_int), ("torque_kernel", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("torque_kernel", ctypes.c_int),
+                ("solve_arith", ctypes.c_int)]
 
 
 class DpstInfo(ctypes.Structure):
@@ -36,7 +38,8 @@ class DpstInfo(ctypes.Structure):
                 ("kernels_per_mdot", ctypes.c_int), ("ghost_layers_in_use", ctypes.c_int),
                 ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
                 ("fused_particle_passes", ctypes.c_int), ("ztransform_inverse", ctypes.c_int),
-                ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int)]
+                ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int),
+                ("solve_arith", ctypes.c_int)]
 
 
 class DpstBatchInfo(ctypes.Structure):

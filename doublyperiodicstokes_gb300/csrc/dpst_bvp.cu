@@ -628,6 +628,15 @@ __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0(KsArgs a, R *__restrict_
   bvp_k0_body<R>(a, spec);
 }
 
+// the k = 0 mode alone (after the double-float solve of the other modes)
+template <typename R>
+cudaError_t launch_bvp_k0(const KsArgs &a, R *spec, cudaStream_t s) {
+  k_bvp_k0<R><<<1, 2 * K0_ROWS, 0, s>>>(a, spec);
+  return cudaGetLastError();
+}
+template cudaError_t launch_bvp_k0<float>(const KsArgs &, float *, cudaStream_t);
+template cudaError_t launch_bvp_k0<double>(const KsArgs &, double *, cudaStream_t);
+
 // Batched: one CTA per system.
 template <typename R>
 __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restrict__ sys) {

@@ -1,0 +1,409 @@
+// Per-wavenumber Stokes BVP of the mixed operator in double-float arithmetic
+// (the no-wall Schur/KBPENTA solve of DPTools.cpp:81-345 and the wall values
+// the corrections of DPTools.cpp:590-877 start from), on the FP32 pipe.
+//
+// Same algorithm, factors and operation order as the FP64 solve (dpst_bvp.cu,
+// bvp_mode): pressure right-hand side Dx f + Dy g + d/dz h, the KBPENTA
+// forward and back sweeps with the border dots, the Schur correction with
+// Ginv, the SIMat / FIMat window for the pressure coefficients and its z
+// derivative, then the three velocity solves (z first) with the BC values
+// from the pressure at z = +-1.  Every value is a double-float (dpst_df64.cuh,
+// about 48 significant bits); only the wall-correction coefficients of the
+// slit channel (an 8 x 8 complex solve per mode) stay FP64.
+//
+// Work decomposition: four lanes per wavenumber.  The banded matrix couples
+// row j with j +- 2 only, and its border columns act on rows of one parity
+// each, so the sweeps split into an even and an odd chain; all operators
+// have real coefficients, so real and imaginary parts split too.  Lane
+// (part, parity) = (lane & 1, (lane >> 1) & 1) of a quad owns the rows of
+// its parity of the real or imaginary part: a column of ceil(nz / 2)
+// double-floats in shared memory ([row][lane], conflict-free).  The chains
+// meet only in the border dots and coefficient sums (one shuffle each) and in
+// the pressure window, whose z-derivative band reads the other parity's
+// neighbours (the two lanes of a parity pair walk their rows in lockstep and
+// exchange them by shuffles).  The pressure coefficients, read back by the
+// other part's lane for the x and y velocity right-hand sides, go to an
+// L2-resident global scratch [row][lane of the grid].  With half-length
+// columns, 13 warps per SM fit at nz = 128 (the FP64 solve fits 6), enough to
+// keep the FP32 pipe issuing through the double-float dependency chains.
+#include "dpst_internal.cuh"
+#include "dpst_kdev.cuh"
+#include "dpst_df64.cuh"
+
+namespace dpst {
+
+constexpr int DFS_NZMAX = 128;
+constexpr int DFS_ROWS = DFS_NZMAX / 2;  // rows of one parity chain
+constexpr int DFS_MAXT = 512;            // threads per CTA (register budget 128)
+enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_DH };
+// k-independent tables as double-floats, at fixed offsets; then the scalars
+// se0, se1, fe, se0 / eta, se1 / eta
+__shared__ float2 dfs_tab[DT_DH * DFS_NZMAX + DFS_NZMAX + 1 + 5];
+#define DTAB(t, j) df_lds(dfs_tab[(t) * DFS_NZMAX + (j)])
+constexpr int DT_SCAL = DT_DH * DFS_NZMAX + DFS_NZMAX + 1;
+
+struct DfCtx {
+  float2 *Xs;         // this lane's column, row t at Xs[t * NT]
+  float2 *CPs;        // this lane's pressure coefficients, row t at CPs[t * GT]
+  const float2 *CPo;  // the other part's (same parity)
+  int NT, GT;
+};
+
+// Solve of wavenumber i by the quad of lanes this lane belongs to.
+template <typename R, bool WALLS>
+static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
+                                                int i, bool store, const DfCtx &c) {
+  const int nz = a.nz;
+  const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
+  const int lane = threadIdx.x & 31;
+  const int part = lane & 1, par = (lane >> 1) & 1;
+  const int nzp = (nz + 1 - par) >> 1;  // rows of this parity
+  const int nsteps = (nz + 1) >> 1;     // rows of parity 0: the lockstep length
+  float2 *__restrict__ Xs = c.Xs;
+  const int NT = c.NT, GT = c.GT;
+#define XS(t) Xs[(t) * NT]
+  const int rs = 2 * nk;  // spectrum row stride (R elements)
+  R *__restrict__ sp_own = spec + 2 * i + part;
+  const R *__restrict__ sp_oth = spec + 2 * i + (part ^ 1);
+  const int ix = i % a.nxh, iy = i / a.nxh;
+  // (i a)_part = sp a_(other part), sp = -1 for the real part
+  const df64 dxs = part ? df_ld(a.dx2 + ix) : df_neg(df_ld(a.dx2 + ix));
+  const df64 dys = part ? df_ld(a.dy2 + iy) : df_neg(df_ld(a.dy2 + iy));
+  const float4 kk = __ldg(a.km2 + i);
+  const df64 hK = df_make(kk.z, kk.w);  // 1 / (2 K)
+  const df64 G00 = df_ld(a.gi2 + i), G10 = df_ld(a.gi2 + nk + i);
+  const df64 G01 = df_ld(a.gi2 + 2 * nk + i), G11 = df_ld(a.gi2 + 3 * nk + i);
+  const float2 *__restrict__ mf0 = a.mf2 + i;
+  const float4 *__restrict__ bk0 = a.bk2 + 2 * i;
+  const float2 *__restrict__ ab0 = a.ab2 + i;
+  const df64 se0 = df_lds(dfs_tab[DT_SCAL]), se1 = df_lds(dfs_tab[DT_SCAL + 1]);
+  const df64 fe = df_lds(dfs_tab[DT_SCAL + 2]);
+  const df64 se0e = df_lds(dfs_tab[DT_SCAL + 3]), se1e = df_lds(dfs_tab[DT_SCAL + 4]);
+
+  // ---- pressure right-hand side over this chain, backward (DPTools.cpp:134-195):
+  // X_j = Dx f + Dy g (other part) + d_j dh_j, with the Chebyshev derivative
+  // dh_j = dh_{j+2} + (2 (j+1) / H) h_{j+1} (dh = 0 past the last row) and
+  // d_0 = 1/2, d_j = 1 otherwise
+  {
+    df64 dh = df_zero();
+    for (int t = nzp - 1; t >= 0; --t) {
+      const int j = par + 2 * t;
+      if (j + 1 < nz) dh = df_fma(DTAB(DT_DH, j + 1), df_in(sp_own + (2 * nz + j + 1) * rs), dh);
+      df64 X = df_mul(dxs, df_in(sp_oth + j * rs));
+      X = df_fma(dys, df_in(sp_oth + (nz + j) * rs), X);
+      X = df_add(X, j == 0 ? df_scale2(dh, 0.5f) : dh);
+      XS(t) = df_f2(X);
+    }
+  }
+
+  // KBPENTA sweeps (LinearSolvers.h:106-141) on this chain, in place, with
+  // the forward sweep reading its right-hand side from rhs(t, j); the border
+  // dots y = C x are summed over both chains
+  auto penta = [&](auto &&rhs, df64 &y0, df64 &y1) {
+    df64 vm = df_zero();
+    for (int t = 0; t < nzp; ++t) {
+      const int j = par + 2 * t;
+      const df64 v = df_fnma(df_ld(mf0 + j * nk), vm, rhs(t, j));
+      XS(t) = df_f2(v);
+      vm = v;
+    }
+    df64 vp = df_zero();
+    y0 = df_zero();
+    y1 = df_zero();
+    for (int t = nzp - 1; t >= 0; --t) {
+      const int j = par + 2 * t;
+      const float4 b0 = __ldg(bk0 + j * rs), b1 = __ldg(bk0 + j * rs + 1);
+      const df64 v = df_mul(df_make(b0.x, b0.y), df_fnma(df_make(b0.z, b0.w), vp, df_lds(XS(t))));
+      XS(t) = df_f2(v);
+      vp = v;
+      y0 = df_fma(df_make(b1.x, b1.y), v, y0);
+      y1 = df_fma(df_make(b1.z, b1.w), v, y1);
+    }
+    y0 = df_add(y0, df_shfl_xor(y0, 2));
+    y1 = df_add(y1, df_shfl_xor(y1, 2));
+  };
+  // the border-corrected solution of this chain, x_j = X_j - (A^{-1}B)_j g_par
+  // (column 0 on even rows, column 1 on odd rows), extended by the border
+  // unknown that follows its last row (x_nz = g0, x_nz+1 = g1)
+  auto xat = [&](int t, df64 gown, df64 gext) -> df64 {
+    if (t < nzp) return df_fnma(df_ld(ab0 + (par + 2 * t) * nk), gown, df_lds(XS(t)));
+    return gext;
+  };
+  const bool ext0 = (par + 2 * nzp == nz);  // this chain's extension is g0 (else g1)
+
+  // ---- pressure: Schur solve, cp = S [x; g] (kept for the other part's x, y
+  // velocity right-hand sides), dp = F [x; g] -> z-velocity right-hand side
+  df64 pacc = df_zero();  // sum of this chain's pressure coefficients
+  {
+    df64 y0, y1;
+    penta([&](int t, int) { return df_lds(XS(t)); }, y0, y1);
+    const df64 g0 = df_fma(G00, y0, df_mul(G01, y1)), g1 = df_fma(G10, y0, df_mul(G11, y1));
+    const df64 gown = par ? g1 : g0, gext = ext0 ? g0 : g1;
+    df64 xm = df_zero(), x0 = xat(0, gown, gext);
+    float2 *cpw = c.CPs;
+    for (int t = 0; t < nsteps; ++t) {
+      const int m = par + 2 * t;
+      const df64 xp = (t + 1 <= nzp) ? xat(t + 1, gown, gext) : df_zero();
+      // the other chain's neighbours x_{m-1}, x_{m+1}: parity 0 takes the
+      // partner's x(t - 1), x(t); parity 1 its x(t), x(t + 1)
+      const df64 px0 = df_shfl_xor(x0, 2), pside = df_shfl_xor(par ? xm : xp, 2);
+      const df64 xl = par ? px0 : pside, xr = par ? pside : px0;
+      if (t < nzp) {
+        df64 cp = df_mul(DTAB(DT_S0, m), x0);
+        if (m >= 2) cp = df_fma(DTAB(DT_SM2, m), xm, cp);
+        cp = df_fma(DTAB(DT_SP2, m), xp, cp);
+        if (m == 0) cp = df_fma(se0, g0, cp);
+        if (m == 1) cp = df_fma(se1, g1, cp);
+        df64 dp = df_mul(DTAB(DT_FP1, m), xr);
+        if (m >= 1) dp = df_fma(DTAB(DT_FM1, m), xl, dp);
+        if (m == 0) dp = df_fma(fe, g1, dp);
+        *cpw = df_f2(cp);
+        cpw += GT;
+        pacc = df_add(pacc, cp);
+        XS(t) = df_f2(df_sub(dp, df_in(sp_own + (2 * nz + m) * rs)));  // eta x z-velocity RHS (DPTools.cpp:214)
+      }
+      xm = x0;
+      x0 = xp;
+    }
+  }
+  // velocity BC right-hand sides (DPTools.cpp:218-234): the pressure at
+  // z = +-1 is the sum and the alternating sum of its coefficients; the
+  // velocity solves run on eta x their right-hand sides (1/eta sits in the
+  // window's SIMat bands), so the BC values are scaled by eta too
+  const df64 poth = df_shfl_xor(pacc, 2);
+  const df64 pe = par ? poth : pacc, po = par ? pacc : poth;
+  const df64 ssum = df_add(pe, po), asum = df_sub(pe, po);
+  const df64 ssum_o = df_shfl_xor(ssum, 1), asum_o = df_shfl_xor(asum, 1);
+  df64 bc[6];
+  bc[0] = df_neg(df_mul(hK, df_mul(dxs, ssum_o)));
+  bc[1] = df_mul(hK, df_mul(dxs, asum_o));
+  bc[2] = df_neg(df_mul(hK, df_mul(dys, ssum_o)));
+  bc[3] = df_mul(hK, df_mul(dys, asum_o));
+  bc[4] = df_scale2(ssum, 0.5f);
+  bc[5] = df_scale2(asum, 0.5f);
+  __syncwarp();  // the other part's pressure coefficients are read below
+
+  // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
+  df64 wt[3], wb[3];
+#pragma unroll
+  for (int cc = 0; cc < 3; ++cc) {
+    const int comp = (cc + 2) % 3;  // 2, 0, 1
+    df64 y0, y1;
+    if (comp == 2) {
+      penta([&](int t, int) { return df_lds(XS(t)); }, y0, y1);
+    } else {
+      const df64 dcs = comp == 0 ? dxs : dys;
+      const R *fs = sp_own + comp * nz * rs;
+      const float2 *cpo = c.CPo;
+      penta([&](int t, int j) { return df_sub(df_mul(dcs, df_lds(cpo[t * GT])), df_in(fs + j * rs)); }, y0, y1);
+    }
+    const df64 r0 = df_sub(y0, bc[2 * comp]), r1 = df_sub(y1, bc[2 * comp + 1]);
+    const df64 g0 = df_fma(G00, r0, df_mul(G01, r1)), g1 = df_fma(G10, r0, df_mul(G11, r1));
+    const df64 gown = par ? g1 : g0, gext = ext0 ? g0 : g1;
+    df64 uacc = df_zero();
+    R *us = sp_own + (comp * nz + par) * rs;
+    df64 xm = df_zero(), x0 = xat(0, gown, gext);
+    for (int t = 0; t < nzp; ++t) {
+      const int m = par + 2 * t;
+      const df64 xp = xat(t + 1, gown, gext);
+      df64 u = df_mul(DTAB(DT_S0E, m), x0);
+      if (m >= 2) u = df_fma(DTAB(DT_SM2E, m), xm, u);
+      u = df_fma(DTAB(DT_SP2E, m), xp, u);
+      if (m == 0) u = df_fma(se0e, g0, u);
+      if (m == 1) u = df_fma(se1e, g1, u);
+      if (store) df_out(us, u);
+      if (WALLS) uacc = df_add(uacc, u);
+      us += 2 * rs;
+      xm = x0;
+      x0 = xp;
+    }
+    if (WALLS) {
+      const df64 uoth = df_shfl_xor(uacc, 2);
+      const df64 ue = par ? uoth : uacc, uo = par ? uacc : uoth;
+      wt[comp] = df_add(ue, uo);  // u(z = 1), u(z = -1)
+      wb[comp] = df_sub(ue, uo);
+    }
+  }
+  if (!WALLS) {
+    __syncwarp();  // column / pressure scratch reuse in the next mode
+    return;
+  }
+  // wall-correction coefficients (evalTheta at z = 0 and z = Lz), FP64
+  double wto[3], wbo[3], wtd[3], wbd[3];
+  for (int q = 0; q < 3; ++q) {
+    wtd[q] = df_to_d(wt[q]);
+    wbd[q] = df_to_d(wb[q]);
+    wto[q] = __shfl_xor_sync(0xffffffffu, wtd[q], 1);
+    wbo[q] = __shfl_xor_sync(0xffffffffu, wbd[q], 1);
+  }
+  __syncwarp();  // column / pressure scratch reuse in the next mode
+  if (!store || par != 0) return;
+  double *crd = reinterpret_cast<double *>(corr + i * 16);
+  if (a.mode == 1) {
+    for (int q = 0; q < 3; ++q) crd[2 * q + part] = -wbd[q];
+    if (a.corrf)
+      for (int q = 0; q < 3; ++q) reinterpret_cast<float *>(a.corrf + i * 16)[2 * q + part] = (float)(-wbd[q]);
+  } else if (a.mode == 2 && part == 0) {
+    const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
+    double2 fb[3], ft[3], cf[8];
+    for (int q = 0; q < 3; ++q) {
+      fb[q] = make_double2(-wbd[q], -wbo[q]);
+      ft[q] = make_double2(-wtd[q], -wto[q]);
+    }
+    slit_coeffs(kx, ky, a.Lz, a.eta, fb, ft, cf);
+    for (int r = 0; r < 8; ++r) corr[i * 16 + r] = cf[r];
+    if (a.corrf)
+      for (int r = 0; r < 8; ++r) a.corrf[i * 16 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
+    double kxp, kyp;
+    if (!mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp)) {
+      for (int q = 0; q < 3; ++q) {
+        fb[q] = cconj(fb[q]);
+        ft[q] = cconj(ft[q]);
+      }
+      slit_coeffs(kxp, kyp, a.Lz, a.eta, fb, ft, cf);
+      for (int r = 0; r < 8; ++r) corr[i * 16 + 8 + r] = cf[r];
+      if (a.corrf)
+        for (int r = 0; r < 8; ++r) a.corrf[i * 16 + 8 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
+    }
+  }
+#undef XS
+}
+
+// Persistent kernel: CTA b owns the units of 8 wavenumbers [b per_cta,
+// (b+1) per_cta) and its warps take them from a shared-memory counter.
+template <typename R>
+__global__ void __launch_bounds__(DFS_MAXT, 1) k_bvp_df(KsArgs a, R *__restrict__ spec, double2 *__restrict__ corr,
+                                                        float2 *__restrict__ cp_scratch, int per_cta) {
+  extern __shared__ float2 dfs_cols[];
+  __shared__ int next_unit;
+  const int nz = a.nz, tid = threadIdx.x, NT = blockDim.x;
+  const double inv_eta = 1.0 / a.eta;
+  for (int t = tid; t < nz; t += NT) {
+    dfs_tab[DT_S0 * DFS_NZMAX + t] = df_f2(df_from_d(a.s0[t]));
+    dfs_tab[DT_SM2 * DFS_NZMAX + t] = df_f2(df_from_d(a.sm2[t]));
+    dfs_tab[DT_SP2 * DFS_NZMAX + t] = df_f2(df_from_d(a.sp2[t]));
+    dfs_tab[DT_FM1 * DFS_NZMAX + t] = df_f2(df_from_d(a.fm1[t]));
+    dfs_tab[DT_FP1 * DFS_NZMAX + t] = df_f2(df_from_d(a.fp1[t]));
+    dfs_tab[DT_S0E * DFS_NZMAX + t] = df_f2(df_from_d(a.s0[t] * inv_eta));
+    dfs_tab[DT_SM2E * DFS_NZMAX + t] = df_f2(df_from_d(a.sm2[t] * inv_eta));
+    dfs_tab[DT_SP2E * DFS_NZMAX + t] = df_f2(df_from_d(a.sp2[t] * inv_eta));
+  }
+  for (int t = tid; t <= nz; t += NT) dfs_tab[DT_DH * DFS_NZMAX + t] = df_f2(df_from_d((double)(2 * t) / a.H));
+  if (tid == 0) {
+    dfs_tab[DT_SCAL] = df_f2(df_from_d(a.se0));
+    dfs_tab[DT_SCAL + 1] = df_f2(df_from_d(a.se1));
+    dfs_tab[DT_SCAL + 2] = df_f2(df_from_d(a.fe));
+    dfs_tab[DT_SCAL + 3] = df_f2(df_from_d(a.se0 * inv_eta));
+    dfs_tab[DT_SCAL + 4] = df_f2(df_from_d(a.se1 * inv_eta));
+    next_unit = blockIdx.x * per_cta;
+  }
+  __syncthreads();
+  DfCtx c;
+  c.NT = NT;
+  c.GT = gridDim.x * NT;
+  c.Xs = dfs_cols + tid;
+  c.CPs = cp_scratch + (size_t)blockIdx.x * NT + tid;
+  c.CPo = cp_scratch + (size_t)blockIdx.x * NT + (tid ^ 1);
+  const int nk = (int)a.nk;
+  const int units = (nk + 7) / 8;
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
+  const int lane = tid & 31;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
+    const int i_raw = u * 8 + (lane >> 2);
+    const int i = i_raw < nk ? i_raw : nk - 1;
+    const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
+    if (a.mode != 0) dfs_mode<R, true>(a, spec, corr, i, store, c);
+    else dfs_mode<R, false>(a, spec, corr, i, store, c);
+  }
+}
+
+// Double-float copies of the packed factors (one thread per table entry).
+__global__ void k_bvp_pack_df(KsArgs a) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nk = a.nk;
+  if (t < (int64_t)a.nz * nk) {
+    a.mf2[t] = df_f2(df_from_d(a.mf[t]));
+    a.ab2[t] = df_f2(df_from_d(a.ab[t]));
+    const double *b = a.bk + 4 * t;
+    const df64 b0 = df_from_d(b[0]), b1 = df_from_d(b[1]), b2 = df_from_d(b[2]), b3 = df_from_d(b[3]);
+    a.bk2[2 * t] = make_float4(b0.hi, b0.lo, b1.hi, b1.lo);
+    a.bk2[2 * t + 1] = make_float4(b2.hi, b2.lo, b3.hi, b3.lo);
+  }
+  if (t < 4 * nk) a.gi2[t] = df_f2(df_from_d(a.ginv[t]));
+  if (t < nk) {
+    const int ix = (int)(t % a.nxh), iy = (int)(t / a.nxh);
+    const double kx = a.kvx[ix], ky = a.kvy[iy];
+    const double K = sqrt(kx * kx + ky * ky);
+    const df64 k = df_from_d(K), h = df_from_d(K > 0.0 ? 0.5 / K : 0.0);
+    a.km2[t] = make_float4(k.hi, k.lo, h.hi, h.lo);
+  }
+  if (t < a.nxh) {
+    const double kx = a.kvx[t];
+    a.dx2[t] = df_f2(df_from_d(((a.nx % 2) == 0 && t == a.nx / 2) ? 0.0 : kx));
+  }
+  if (t < a.ny) {
+    const double ky = a.kvy[t];
+    a.dy2[t] = df_f2(df_from_d(((a.ny % 2) == 0 && t == a.ny / 2) ? 0.0 : ky));
+  }
+}
+
+void launch_bvp_pack_df(const KsArgs &a, cudaStream_t s) {
+  int64_t tot = std::max<int64_t>((int64_t)a.nz * a.nk, 4 * a.nk);
+  tot = std::max<int64_t>(tot, std::max(a.nxh, a.ny));
+  k_bvp_pack_df<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(a);
+}
+
+// Threads per CTA of k_bvp_df for nz: as many warps as the columns
+// (ceil(nz / 2) double-floats per lane) allow next to the static tables in
+// 227 KB of shared memory, at most DFS_MAXT / 32.
+static int bvp_df_threads(int nz) {
+  const size_t per_warp = sizeof(float2) * (size_t)((nz + 1) / 2) * 32;
+  const size_t stat = sizeof(dfs_tab) + 64;
+  const size_t avail = (size_t)227 * 1024 - stat;
+  int w = (int)(avail / per_warp);
+  if (w > DFS_MAXT / 32) w = DFS_MAXT / 32;
+  return w * 32;
+}
+
+// Grid (one CTA per SM, at most one per unit of 8 wavenumbers) and the bytes
+// of the pressure scratch.
+cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  if (a.nz > DFS_NZMAX) return cudaErrorInvalidValue;
+  if ((int64_t)a.nz * a.nk * 4 >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  const int nt = bvp_df_threads(a.nz);
+  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_df<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(k_bvp_df<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_df<float>, nt, smem);
+  if (err != cudaSuccess) return err;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t g = nsm;
+  const int64_t units = (a.nk + 7) / 8;
+  const int64_t warps = nt / 32;
+  if (g * warps > units) g = std::max<int64_t>(1, (units + warps - 1) / warps);
+  *grid = g;
+  *scratch_bytes = sizeof(float2) * (size_t)((a.nz + 1) / 2) * (size_t)g * nt;
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, cudaStream_t s) {
+  const int nt = bvp_df_threads(a.nz);
+  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
+  const int64_t units = (a.nk + 7) / 8;
+  const int per_cta = (int)((units + grid - 1) / grid);
+  k_bvp_df<R><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_bvp_df<float>(const KsArgs &, float *, double2 *, float2 *, int64_t, cudaStream_t);
+template cudaError_t launch_bvp_df<double>(const KsArgs &, double *, double2 *, float2 *, int64_t, cudaStream_t);
+
+}  // namespace dpst

@@ -55,6 +55,13 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
                                cudaStream_t s, bool *too_big);
 size_t noalloc_scratch_bytes();
 template <typename R>
+cudaError_t launch_bvp_k0(const KsArgs &a, R *spec, cudaStream_t s);
+// double-float solve of the mixed operator (dpst_bvp_df.cu)
+void launch_bvp_pack_df(const KsArgs &a, cudaStream_t s);
+cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, cudaStream_t s);
+template <typename R>
 void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
                       const double *kvx, const double *kvy, double H, cudaStream_t s);
 template <typename R>
@@ -108,6 +115,10 @@ struct Engine : EngineBase {
   // device buffers
   DevBuf bvp_scratch;
   int64_t bvp_grid = 0;
+  // double-float solve (DPST_SOLVE_DF64): factor copies and pressure scratch
+  bool dfsolve = false;
+  DevBuf df_mf, df_bk, df_ab, df_gi, df_km, df_dx, df_dy, bvp_df_scratch;
+  int64_t bvp_df_grid = 0;
   DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g, fac_pm, fac_pb, fac_pa;
   DevBuf pos64, flags;
@@ -240,6 +251,30 @@ struct Engine : EngineBase {
     size_t bvp_bytes = 0;
     DPST_CUDA(bvp_plan<R>(ks, nsm, &bvp_grid, &bvp_bytes));
     bvp_scratch.alloc(bvp_bytes);
+    // the double-float solve: by default for the mixed operator
+    dfsolve = p.solve_arith == DPST_SOLVE_DF64 || (p.solve_arith == DPST_SOLVE_DEFAULT && sizeof(R) == 4);
+    if (dfsolve) {
+      df_mf.alloc(sizeof(float2) * nz * nk);
+      df_ab.alloc(sizeof(float2) * nz * nk);
+      df_bk.alloc(sizeof(float4) * 2 * nz * nk);
+      df_gi.alloc(sizeof(float2) * 4 * nk);
+      df_km.alloc(sizeof(float4) * nk);
+      df_dx.alloc(sizeof(float2) * nxh);
+      df_dy.alloc(sizeof(float2) * ny);
+      ks.mf2 = df_mf.as<float2>();
+      ks.ab2 = df_ab.as<float2>();
+      ks.bk2 = df_bk.as<float4>();
+      ks.gi2 = df_gi.as<float2>();
+      ks.km2 = df_km.as<float4>();
+      ks.dx2 = df_dx.as<float2>();
+      ks.dy2 = df_dy.as<float2>();
+      launch_bvp_pack_df(ks, 0);
+      DPST_CUDA(cudaGetLastError());
+      size_t df_bytes = 0;
+      DPST_CUDA(bvp_df_plan(ks, nsm, &bvp_df_grid, &df_bytes));
+      bvp_df_scratch.alloc(df_bytes);
+      DPST_CUDA(cudaDeviceSynchronize());
+    }
     // particle buffers
     pos64.alloc(sizeof(double) * 3 * std::max<int64_t>(N, 1));
     flags.alloc(sizeof(int) * 8);
@@ -642,7 +677,10 @@ struct Engine : EngineBase {
 
   // per-wavenumber solve (+ k = 0) on the spectrum sp, in place
   void bvp_stage(CR *sp, cudaStream_t s) {
-    if (!use_static_scratch) {
+    if (!use_static_scratch && dfsolve) {
+      DPST_CUDA(launch_bvp_df<R>(ks, (R *)sp, corr.as<double2>(), bvp_df_scratch.as<float2>(), bvp_df_grid, s));
+      DPST_CUDA(launch_bvp_k0<R>(ks, (R *)sp, s));
+    } else if (!use_static_scratch) {
       DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
     } else {
       bool too_big = false;
@@ -1037,11 +1075,13 @@ struct Engine : EngineBase {
     // vorticity's forward z transform, curl and inverse z transform
     if (reg) o->kernels_per_mdot += (p.mode == DPST_MODE_NOWALL) ? 4 : 5;
     o->fused_particle_passes = fused ? 1 : 0;
+    o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
                            &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm,
-                           &corrf, &cmode, &znf, &gridT, &specT};
+                           &corrf, &cmode, &znf, &gridT, &specT, &df_mf, &df_bk, &df_ab, &df_gi, &df_km,
+                           &df_dx, &df_dy, &bvp_df_scratch};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;

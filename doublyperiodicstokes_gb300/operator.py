@@ -28,7 +28,9 @@ class StokesParams:
     Kernels: w points per axis, ES beta (the reference's beta_hat * w) and
     alpha (physical half width).  reg_kernel: torques and angular velocities
     with the regular ES kernel of (w_d, beta_d, alpha_d) and spectral curls
-    (the reference's useRegKernel=True) instead of the derivative kernels."""
+    (the reference's useRegKernel=True) instead of the derivative kernels.
+    solve: arithmetic of the per-wavenumber solve, 'default' (FP64 for the
+    FP64 operator, double-float for the mixed one), 'fp64' or 'df64'."""
     mode: str
     nx: int
     ny: int
@@ -47,13 +49,15 @@ class StokesParams:
     alpha_d: float = 3.0
     precision: str = "fp64"
     reg_kernel: bool = False
+    solve: str = "default"
 
     def to_c(self):
         return _lib.DpstParams(
             _lib.MODE[self.mode], int(self.nx), int(self.ny), int(self.nz), float(self.Lx),
             float(self.Ly), float(self.zmin), float(self.zmax), float(self.viscosity), int(self.w),
             float(self.beta), float(self.alpha), int(bool(self.has_torque)), int(self.w_d),
-            float(self.beta_d), float(self.alpha_d), _lib.PREC[self.precision], int(bool(self.reg_kernel)))
+            float(self.beta_d), float(self.alpha_d), _lib.PREC[self.precision], int(bool(self.reg_kernel)),
+            _lib.SOLVE[self.solve])
 
     def as_dict(self):
         return asdict(self)

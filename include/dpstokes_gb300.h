@@ -97,6 +97,16 @@ extern "C" {
                                427-439; useRegKernel = True).  dpst_create only: no batched
                                systems, no backward */
 
+/* arithmetic of the per-wavenumber solve (dpst_params.solve_arith) */
+#define DPST_SOLVE_DEFAULT 0 /* FP64 for DPST_PREC_FP64, double-float for DPST_PREC_MIXED */
+#define DPST_SOLVE_FP64 1    /* FP64 on the FP64 pipe */
+#define DPST_SOLVE_DF64 2    /* double-float: pairs of FP32 (about 48 significant bits, FP32's
+                                exponent range) on the FP32 pipe, the same algorithm and factors
+                                as the FP64 solve; the slit channel's wall-correction
+                                coefficients stay FP64.  Open and wall geometries of
+                                dpst_create handles; batched systems, multi-column Mdot and
+                                dpst_mdot_noalloc run the FP64 solve */
+
 /* element type of the particle arrays passed to mdot */
 #define DPST_F64 0
 #define DPST_F32 1
@@ -118,6 +128,7 @@ typedef struct dpst_params {
   double alpha_d;
   int precision;     /* DPST_PREC_* */
   int torque_kernel; /* DPST_TORQUE_* (0 when the initialiser stops before it) */
+  int solve_arith;   /* DPST_SOLVE_* (0 when the initialiser stops before it) */
 } dpst_params;
 
 typedef struct dpst_info {
@@ -149,6 +160,8 @@ typedef struct dpst_info {
   int z_fused;                     /* triply periodic: 1 when the z transform and the solve
                                       run in one kernel after 2-D x-y transforms (nz = 16,
                                       32, 64), 0 with cuFFT's 3-D transforms */
+  int solve_arith;                 /* arithmetic of the per-wavenumber solve dpst_mdot runs:
+                                      DPST_SOLVE_FP64 or DPST_SOLVE_DF64 (triply periodic: 0) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

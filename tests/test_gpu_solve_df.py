@@ -1,0 +1,90 @@
+"""The double-float per-wavenumber solve (DPST_SOLVE_DF64) against the FP64
+solve.
+
+The FP64 operator can run either solve with FP64 spectra in and out, which
+isolates the solve's arithmetic: per wavenumber (kx, ky), the velocity
+columns of the two runs (the velocity grid Fourier transformed in x and y,
+all nz levels and three components, wall correction included) agree to
+1e-12 relative to the column's own norm, and V, W to 1e-12; the FP64
+operator with the double-float solve still matches the reference's own
+outputs to 1e-10.  The mixed operator (double-float solve by default) stays
+within 1e-6 of the mixed operator with the FP64 solve and within 1e-5 of the
+FP64 operator."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import golden_io  # noqa: E402
+from conftest import rel_err  # noqa: E402
+from doublyperiodicstokes_gb300 import DPStokes, StokesParams, workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+CASES = [w.name for w in W.SMALL] + ["s_reg_dpbw_t", "s_dpbw_t_k3", "e_dpsc_t", "c0_dpbw_n2048",
+                                     "c2_dp_n65536@64"]
+
+
+def _wl(name):
+    return W.SMALL_BY_NAME.get(name) or W.by_name(name)
+
+
+def _run(w, precision, solve, X, F, T):
+    prm = StokesParams.from_workload(w, precision)
+    prm = StokesParams(**{**prm.as_dict(), "solve": solve})
+    op = DPStokes(prm, w.N)
+    d = op.device
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    op.set_positions(torch.tensor(X, device=d))
+    V, Wv = op.mdot(torch.tensor(F, dtype=dt, device=d), torch.tensor(T, dtype=dt, device=d) if T is not None else None)
+    torch.cuda.synchronize()
+    out = (V.double().cpu().numpy(), Wv.double().cpu().numpy() if Wv is not None else None,
+           op.velocity_grid().double().cpu(), op.info()["solve_arith"])
+    op.close()
+    return out
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_df64_solve_matches_fp64_solve_per_mode(name):
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    V1, W1, g1, a1 = _run(w, "fp64", "fp64", X, F, T)
+    V2, W2, g2, a2 = _run(w, "fp64", "df64", X, F, T)
+    assert (a1, a2) == (1, 2)
+    # per-wavenumber columns: [3][nz][ny][nx] -> x-y transform -> [ny][nxh][3 nz]
+    c1 = torch.fft.rfft2(g1).permute(2, 3, 0, 1).reshape(w.ny, w.nx // 2 + 1, -1)
+    c2 = torch.fft.rfft2(g2).permute(2, 3, 0, 1).reshape(w.ny, w.nx // 2 + 1, -1)
+    n1 = torch.linalg.vector_norm(c1, dim=2)
+    d = torch.linalg.vector_norm(c2 - c1, dim=2)
+    big = n1 > 1e-13 * n1.max()  # modes whose column is not at the rounding level of the grid
+    worst = float((d[big] / n1[big]).max())
+    ev, eg = rel_err(V2, V1), rel_err(g2.numpy(), g1.numpy())
+    print("%s per-mode max %.2e, grid %.2e, V %.2e" % (name, worst, eg, ev))
+    assert worst < 1e-12
+    assert ev < 1e-12
+    if T is not None:
+        assert rel_err(W2, W1) < 1e-12
+
+
+@pytest.mark.parametrize("name", [n for n in golden_io.names() if n.startswith(("s_d", "e_d", "c0", "c1"))])
+def test_fp64_operator_with_df64_solve_matches_reference(name):
+    w, X, F, T, g = golden_io.inputs(name)
+    V, Wv, _, _ = _run(w, "fp64", "df64", X, F, T)
+    assert rel_err(golden_io.restrict(g, V), g["V"]) < 1e-10
+    if w.has_torque:
+        assert rel_err(golden_io.restrict(g, Wv), g["W"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["s_dpbw_t", "s_dp_t", "s_dpsc_t", "c1_dpsc_n16384", "c2_dp_n65536@192"])
+def test_mixed_default_solve_is_df64(name):
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    Vd, Wd, _, ad = _run(w, "mixed", "default", X, F, T)
+    Vf, Wf, _, af = _run(w, "mixed", "fp64", X, F, T)
+    V6, W6, _, _ = _run(w, "fp64", "fp64", X, F, T)
+    assert (ad, af) == (2, 1)
+    e1, e2 = rel_err(Vd, Vf), rel_err(Vd, V6)
+    print("%s mixed df64 vs mixed fp64 solve %.2e, vs fp64 operator %.2e" % (name, e1, e2))
+    assert e1 < 1e-6 and e2 < 1e-5
+    if T is not None:
+        assert rel_err(Wd, Wf) < 1e-6 and rel_err(Wd, W6) < 1e-5
