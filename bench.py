@@ -318,6 +318,9 @@ def run_ours(args, rank, world):
             roof["fp64_pipe"] = {"lane_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
                                  "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
     extra["set_positions_ms"] = set_positions_ms
+    extra["solve_kernel"] = {"arith": {1: "fp64", 2: "double-float"}.get(info.get("solve_arith"), "n/a"),
+                             "variant": info.get("solve_variant"),
+                             "variant_ms": [round(float(x), 4) for x in info.get("solve_ms", [])]}
     return dict(value=value, ms_step=ms_step, e2e=e2e, stages=stages, info=info, extra=extra,
                 roofline=roof, clocks=clocks, w=w)
 

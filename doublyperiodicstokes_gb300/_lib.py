@@ -39,7 +39,8 @@ class DpstInfo(ctypes.Structure):
                 ("ztransform", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
                 ("fused_particle_passes", ctypes.c_int), ("ztransform_inverse", ctypes.c_int),
                 ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int),
-                ("solve_arith", ctypes.c_int)]
+                ("solve_arith", ctypes.c_int), ("solve_variant", ctypes.c_int),
+                ("solve_ms", ctypes.c_float * 4)]
 
 
 class DpstBatchInfo(ctypes.Structure):

@@ -33,8 +33,6 @@
 namespace dpst {
 
 constexpr int DFS_NZMAX = 128;
-constexpr int DFS_ROWS = DFS_NZMAX / 2;  // rows of one parity chain
-constexpr int DFS_MAXT = 512;            // threads per CTA (register budget 128)
 enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_DH };
 // k-independent tables as double-floats, at fixed offsets; then the scalars
 // se0, se1, fe, se0 / eta, se1 / eta
@@ -49,8 +47,74 @@ struct DfCtx {
   int NT, GT;
 };
 
+// Row loops with their global loads read ahead of use: ld(t) is issued PF
+// rows before body(t, value) runs (a ring of PF values in registers; loads
+// past the end are clamped to row n - 1 and discarded).  Up: t = 0 .. n-1;
+// down: t = n-1 .. 0.  n >= 1.
+template <int PF, typename T, typename Ld, typename Body>
+static __device__ __forceinline__ void rows_up(int n, Ld &&ld, Body &&body) {
+  T ring[PF];
+#pragma unroll
+  for (int k = 0; k < PF; ++k) ring[k] = ld(min(k, n - 1));
+  int t = 0;
+  for (; t + PF <= n; t += PF) {
+#pragma unroll
+    for (int k = 0; k < PF; ++k) {
+      const T v = ring[k];
+      ring[k] = ld(min(t + PF + k, n - 1));
+      body(t + k, v);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PF - 1; ++k)
+    if (t + k < n) body(t + k, ring[k]);
+}
+template <int PF, typename T, typename Ld, typename Body>
+static __device__ __forceinline__ void rows_down(int n, Ld &&ld, Body &&body) {
+  rows_up<PF, T>(n, [&](int s) { return ld(n - 1 - s); }, [&](int s, const T &v) { body(n - 1 - s, v); });
+}
+
+// Raw spectrum values (R) as double-float operands: FP32 values enter the
+// FP32-operand forms directly; FP64 values (the FP64-I/O instantiation) are
+// rounded to double-floats.
+static __device__ __forceinline__ float df_v(float x) { return x; }
+static __device__ __forceinline__ df64 df_v(double x) { return df_from_d(x); }
+
+template <typename R>
+struct DfRhsP {  // pressure right-hand side inputs of one row
+  R f, g, h;
+};
+template <typename R>
+struct DfRhsV {  // velocity forward-sweep inputs of one row
+  float2 m, cp;
+  R f;
+};
+struct DfBack {
+  float4 b0, b1;
+};
+template <typename R>
+struct DfWinP {  // pressure window inputs: A^{-1}B of row t + 1, f_z of row t
+  float2 ab;
+  R fz;
+};
+
+// Variants of the kernel: prefetch depths of the forward sweep, the back
+// sweep and the windows (rows read ahead through register rings), and
+// threads per CTA (13 warps with at most 128 registers, or 12 with 168).
+// The fastest for a handle is chosen when it is created, by timing.
+template <int F, int B, int W, int T>
+struct DfCfg {
+  static constexpr int PF_F = F, PF_B = B, PF_W = W, MAXT = T;
+};
+using DfV0 = DfCfg<2, 1, 2, 416>;
+using DfV1 = DfCfg<4, 2, 4, 384>;
+using DfV2 = DfCfg<6, 3, 6, 384>;
+using DfV3 = DfCfg<4, 4, 4, 384>;
+constexpr int DF_VARIANTS = 4;
+constexpr int DF_MAXT = 416;  // the most threads of any variant
+
 // Solve of wavenumber i by the quad of lanes this lane belongs to.
-template <typename R, bool WALLS>
+template <typename R, bool WALLS, typename CFG>
 static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
                                                 int i, bool store, const DfCtx &c) {
   const int nz = a.nz;
@@ -69,16 +133,14 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   // (i a)_part = sp a_(other part), sp = -1 for the real part
   const df64 dxs = part ? df_ld(a.dx2 + ix) : df_neg(df_ld(a.dx2 + ix));
   const df64 dys = part ? df_ld(a.dy2 + iy) : df_neg(df_ld(a.dy2 + iy));
-  const float4 kk = __ldg(a.km2 + i);
-  const df64 hK = df_make(kk.z, kk.w);  // 1 / (2 K)
-  const df64 G00 = df_ld(a.gi2 + i), G10 = df_ld(a.gi2 + nk + i);
-  const df64 G01 = df_ld(a.gi2 + 2 * nk + i), G11 = df_ld(a.gi2 + 3 * nk + i);
   const float2 *__restrict__ mf0 = a.mf2 + i;
   const float4 *__restrict__ bk0 = a.bk2 + 2 * i;
   const float2 *__restrict__ ab0 = a.ab2 + i;
-  const df64 se0 = df_lds(dfs_tab[DT_SCAL]), se1 = df_lds(dfs_tab[DT_SCAL + 1]);
-  const df64 fe = df_lds(dfs_tab[DT_SCAL + 2]);
-  const df64 se0e = df_lds(dfs_tab[DT_SCAL + 3]), se1e = df_lds(dfs_tab[DT_SCAL + 4]);
+  // g = Ginv r
+  auto schur = [&](df64 r0, df64 r1, df64 &g0, df64 &g1) {
+    g0 = df_fma(df_ld(a.gi2 + i), r0, df_mul(df_ld(a.gi2 + 2 * nk + i), r1));
+    g1 = df_fma(df_ld(a.gi2 + nk + i), r0, df_mul(df_ld(a.gi2 + 3 * nk + i), r1));
+  };
 
   // ---- pressure right-hand side over this chain, backward (DPTools.cpp:134-195):
   // X_j = Dx f + Dy g (other part) + d_j dh_j, with the Chebyshev derivative
@@ -86,101 +148,153 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   // d_0 = 1/2, d_j = 1 otherwise
   {
     df64 dh = df_zero();
-    for (int t = nzp - 1; t >= 0; --t) {
-      const int j = par + 2 * t;
-      if (j + 1 < nz) dh = df_fma(DTAB(DT_DH, j + 1), df_in(sp_own + (2 * nz + j + 1) * rs), dh);
-      df64 X = df_mul(dxs, df_in(sp_oth + j * rs));
-      X = df_fma(dys, df_in(sp_oth + (nz + j) * rs), X);
-      X = df_add(X, j == 0 ? df_scale2(dh, 0.5f) : dh);
-      XS(t) = df_f2(X);
-    }
+    rows_down<CFG::PF_F, DfRhsP<R>>(
+        nzp,
+        [&](int t) {
+          const int j = par + 2 * t;
+          DfRhsP<R> v;
+          v.f = sp_oth[j * rs];
+          v.g = sp_oth[(nz + j) * rs];
+          v.h = sp_own[(2 * nz + min(j + 1, nz - 1)) * rs];
+          return v;
+        },
+        [&](int t, const DfRhsP<R> &v) {
+          const int j = par + 2 * t;
+          if (j + 1 < nz) dh = df_fma(DTAB(DT_DH, j + 1), df_v(v.h), dh);
+          df64 X = df_mul(dxs, df_v(v.f));
+          X = df_fma(dys, df_v(v.g), X);
+          X = df_add(X, j == 0 ? df_scale2(dh, 0.5f) : dh);
+          XS(t) = df_f2(X);
+        });
   }
 
   // KBPENTA sweeps (LinearSolvers.h:106-141) on this chain, in place, with
-  // the forward sweep reading its right-hand side from rhs(t, j); the border
-  // dots y = C x are summed over both chains
-  auto penta = [&](auto &&rhs, df64 &y0, df64 &y1) {
-    df64 vm = df_zero();
-    for (int t = 0; t < nzp; ++t) {
-      const int j = par + 2 * t;
-      const df64 v = df_fnma(df_ld(mf0 + j * nk), vm, rhs(t, j));
-      XS(t) = df_f2(v);
-      vm = v;
-    }
+  // the border dots y = C x summed over both chains.  The forward sweep takes
+  // its right-hand side from XS (VEL = false) or forms Dc cp_other - f_c for
+  // an x / y velocity component (VEL = true).
+  auto back = [&](df64 &y0, df64 &y1) {
     df64 vp = df_zero();
-    y0 = df_zero();
-    y1 = df_zero();
-    for (int t = nzp - 1; t >= 0; --t) {
-      const int j = par + 2 * t;
-      const float4 b0 = __ldg(bk0 + j * rs), b1 = __ldg(bk0 + j * rs + 1);
-      const df64 v = df_mul(df_make(b0.x, b0.y), df_fnma(df_make(b0.z, b0.w), vp, df_lds(XS(t))));
-      XS(t) = df_f2(v);
-      vp = v;
-      y0 = df_fma(df_make(b1.x, b1.y), v, y0);
-      y1 = df_fma(df_make(b1.z, b1.w), v, y1);
-    }
-    y0 = df_add(y0, df_shfl_xor(y0, 2));
-    y1 = df_add(y1, df_shfl_xor(y1, 2));
+    df64 a0 = df_zero(), a1 = df_zero();
+    rows_down<CFG::PF_B, DfBack>(
+        nzp,
+        [&](int t) {
+          const int j = par + 2 * t;
+          DfBack v;
+          v.b0 = __ldg(bk0 + j * rs);
+          v.b1 = __ldg(bk0 + j * rs + 1);
+          return v;
+        },
+        [&](int t, const DfBack &v) {
+          const df64 x = df_mul(df_make(v.b0.x, v.b0.y), df_fnma(df_make(v.b0.z, v.b0.w), vp, df_lds(XS(t))));
+          XS(t) = df_f2(x);
+          vp = x;
+          a0 = df_fma(df_make(v.b1.x, v.b1.y), x, a0);
+          a1 = df_fma(df_make(v.b1.z, v.b1.w), x, a1);
+        });
+    y0 = df_add(a0, df_shfl_xor(a0, 2));
+    y1 = df_add(a1, df_shfl_xor(a1, 2));
   };
-  // the border-corrected solution of this chain, x_j = X_j - (A^{-1}B)_j g_par
-  // (column 0 on even rows, column 1 on odd rows), extended by the border
-  // unknown that follows its last row (x_nz = g0, x_nz+1 = g1)
-  auto xat = [&](int t, df64 gown, df64 gext) -> df64 {
-    if (t < nzp) return df_fnma(df_ld(ab0 + (par + 2 * t) * nk), gown, df_lds(XS(t)));
-    return gext;
+  auto penta_xs = [&](df64 &y0, df64 &y1) {
+    df64 vm = df_zero();
+    rows_up<CFG::PF_F, float2>(
+        nzp, [&](int t) { return __ldg(mf0 + (par + 2 * t) * nk); },
+        [&](int t, const float2 &m) {
+          const df64 v = df_fnma(df_make(m.x, m.y), vm, df_lds(XS(t)));
+          XS(t) = df_f2(v);
+          vm = v;
+        });
+    back(y0, y1);
+  };
+  auto penta_vel = [&](df64 dcs, const R *fs, df64 &y0, df64 &y1) {
+    df64 vm = df_zero();
+    const float2 *cpo = c.CPo;
+    rows_up<CFG::PF_F, DfRhsV<R>>(
+        nzp,
+        [&](int t) {
+          const int j = par + 2 * t;
+          DfRhsV<R> v;
+          v.m = __ldg(mf0 + j * nk);
+          v.cp = cpo[t * GT];
+          v.f = fs[j * rs];
+          return v;
+        },
+        [&](int t, const DfRhsV<R> &v) {
+          const df64 X = df_sub(df_mul(dcs, df_make(v.cp.x, v.cp.y)), df_v(v.f));
+          const df64 x = df_fnma(df_make(v.m.x, v.m.y), vm, X);
+          XS(t) = df_f2(x);
+          vm = x;
+        });
+    back(y0, y1);
   };
   const bool ext0 = (par + 2 * nzp == nz);  // this chain's extension is g0 (else g1)
 
   // ---- pressure: Schur solve, cp = S [x; g] (kept for the other part's x, y
-  // velocity right-hand sides), dp = F [x; g] -> z-velocity right-hand side
+  // velocity right-hand sides), dp = F [x; g] -> z-velocity right-hand side.
+  // The border-corrected solution of this chain is x_j = X_j - (A^{-1}B)_j g_par
+  // (column 0 on even rows, column 1 on odd rows), extended by the border
+  // unknown that follows its last row (x_nz = g0, x_nz+1 = g1).
   df64 pacc = df_zero();  // sum of this chain's pressure coefficients
   {
-    df64 y0, y1;
-    penta([&](int t, int) { return df_lds(XS(t)); }, y0, y1);
-    const df64 g0 = df_fma(G00, y0, df_mul(G01, y1)), g1 = df_fma(G10, y0, df_mul(G11, y1));
+    df64 y0, y1, g0, g1;
+    penta_xs(y0, y1);
+    schur(y0, y1, g0, g1);
     const df64 gown = par ? g1 : g0, gext = ext0 ? g0 : g1;
-    df64 xm = df_zero(), x0 = xat(0, gown, gext);
+    df64 xm = df_zero();
+    df64 x0 = df_fnma(df_ld(ab0 + par * nk), gown, df_lds(XS(0)));
     float2 *cpw = c.CPs;
-    for (int t = 0; t < nsteps; ++t) {
-      const int m = par + 2 * t;
-      const df64 xp = (t + 1 <= nzp) ? xat(t + 1, gown, gext) : df_zero();
-      // the other chain's neighbours x_{m-1}, x_{m+1}: parity 0 takes the
-      // partner's x(t - 1), x(t); parity 1 its x(t), x(t + 1)
-      const df64 px0 = df_shfl_xor(x0, 2), pside = df_shfl_xor(par ? xm : xp, 2);
-      const df64 xl = par ? px0 : pside, xr = par ? pside : px0;
-      if (t < nzp) {
-        df64 cp = df_mul(DTAB(DT_S0, m), x0);
-        if (m >= 2) cp = df_fma(DTAB(DT_SM2, m), xm, cp);
-        cp = df_fma(DTAB(DT_SP2, m), xp, cp);
-        if (m == 0) cp = df_fma(se0, g0, cp);
-        if (m == 1) cp = df_fma(se1, g1, cp);
-        df64 dp = df_mul(DTAB(DT_FP1, m), xr);
-        if (m >= 1) dp = df_fma(DTAB(DT_FM1, m), xl, dp);
-        if (m == 0) dp = df_fma(fe, g1, dp);
-        *cpw = df_f2(cp);
-        cpw += GT;
-        pacc = df_add(pacc, cp);
-        XS(t) = df_f2(df_sub(dp, df_in(sp_own + (2 * nz + m) * rs)));  // eta x z-velocity RHS (DPTools.cpp:214)
-      }
-      xm = x0;
-      x0 = xp;
-    }
+    rows_up<CFG::PF_W, DfWinP<R>>(
+        nsteps,
+        [&](int t) {
+          DfWinP<R> v;
+          v.ab = __ldg(ab0 + (par + 2 * min(t + 1, nzp - 1)) * nk);
+          v.fz = sp_own[(2 * nz + par + 2 * min(t, nzp - 1)) * rs];
+          return v;
+        },
+        [&](int t, const DfWinP<R> &v) {
+          const int m = par + 2 * t;
+          const df64 xp = (t + 1 < nzp)    ? df_fnma(df_make(v.ab.x, v.ab.y), gown, df_lds(XS(t + 1)))
+                          : (t + 1 == nzp) ? gext
+                                           : df_zero();
+          // the other chain's neighbours x_{m-1}, x_{m+1}: parity 0 takes the
+          // partner's x(t - 1), x(t); parity 1 its x(t), x(t + 1)
+          const df64 px0 = df_shfl_xor(x0, 2), pside = df_shfl_xor(par ? xm : xp, 2);
+          const df64 xl = par ? px0 : pside, xr = par ? pside : px0;
+          if (t < nzp) {
+            df64 cp = df_mul(DTAB(DT_S0, m), x0);
+            if (m >= 2) cp = df_fma(DTAB(DT_SM2, m), xm, cp);
+            cp = df_fma(DTAB(DT_SP2, m), xp, cp);
+            if (m == 0) cp = df_fma(df_lds(dfs_tab[DT_SCAL]), g0, cp);
+            if (m == 1) cp = df_fma(df_lds(dfs_tab[DT_SCAL + 1]), g1, cp);
+            df64 dp = df_mul(DTAB(DT_FP1, m), xr);
+            if (m >= 1) dp = df_fma(DTAB(DT_FM1, m), xl, dp);
+            if (m == 0) dp = df_fma(df_lds(dfs_tab[DT_SCAL + 2]), g1, dp);
+            cpw[t * GT] = df_f2(cp);
+            pacc = df_add(pacc, cp);
+            XS(t) = df_f2(df_sub(dp, df_v(v.fz)));  // eta x z-velocity RHS (DPTools.cpp:214)
+          }
+          xm = x0;
+          x0 = xp;
+        });
   }
   // velocity BC right-hand sides (DPTools.cpp:218-234): the pressure at
   // z = +-1 is the sum and the alternating sum of its coefficients; the
   // velocity solves run on eta x their right-hand sides (1/eta sits in the
   // window's SIMat bands), so the BC values are scaled by eta too
-  const df64 poth = df_shfl_xor(pacc, 2);
-  const df64 pe = par ? poth : pacc, po = par ? pacc : poth;
-  const df64 ssum = df_add(pe, po), asum = df_sub(pe, po);
-  const df64 ssum_o = df_shfl_xor(ssum, 1), asum_o = df_shfl_xor(asum, 1);
   df64 bc[6];
-  bc[0] = df_neg(df_mul(hK, df_mul(dxs, ssum_o)));
-  bc[1] = df_mul(hK, df_mul(dxs, asum_o));
-  bc[2] = df_neg(df_mul(hK, df_mul(dys, ssum_o)));
-  bc[3] = df_mul(hK, df_mul(dys, asum_o));
-  bc[4] = df_scale2(ssum, 0.5f);
-  bc[5] = df_scale2(asum, 0.5f);
+  {
+    const float4 kk = __ldg(a.km2 + i);
+    const df64 hK = df_make(kk.z, kk.w);  // 1 / (2 K)
+    const df64 poth = df_shfl_xor(pacc, 2);
+    const df64 pe = par ? poth : pacc, po = par ? pacc : poth;
+    const df64 ssum = df_add(pe, po), asum = df_sub(pe, po);
+    const df64 ssum_o = df_shfl_xor(ssum, 1), asum_o = df_shfl_xor(asum, 1);
+    bc[0] = df_neg(df_mul(hK, df_mul(dxs, ssum_o)));
+    bc[1] = df_mul(hK, df_mul(dxs, asum_o));
+    bc[2] = df_neg(df_mul(hK, df_mul(dys, ssum_o)));
+    bc[3] = df_mul(hK, df_mul(dys, asum_o));
+    bc[4] = df_scale2(ssum, 0.5f);
+    bc[5] = df_scale2(asum, 0.5f);
+  }
   __syncwarp();  // the other part's pressure coefficients are read below
 
   // ---- velocity: three Schur solves (DPTools.cpp:197-216, 287-345); z first
@@ -188,35 +302,30 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
 #pragma unroll
   for (int cc = 0; cc < 3; ++cc) {
     const int comp = (cc + 2) % 3;  // 2, 0, 1
-    df64 y0, y1;
-    if (comp == 2) {
-      penta([&](int t, int) { return df_lds(XS(t)); }, y0, y1);
-    } else {
-      const df64 dcs = comp == 0 ? dxs : dys;
-      const R *fs = sp_own + comp * nz * rs;
-      const float2 *cpo = c.CPo;
-      penta([&](int t, int j) { return df_sub(df_mul(dcs, df_lds(cpo[t * GT])), df_in(fs + j * rs)); }, y0, y1);
-    }
-    const df64 r0 = df_sub(y0, bc[2 * comp]), r1 = df_sub(y1, bc[2 * comp + 1]);
-    const df64 g0 = df_fma(G00, r0, df_mul(G01, r1)), g1 = df_fma(G10, r0, df_mul(G11, r1));
+    df64 y0, y1, g0, g1;
+    if (comp == 2) penta_xs(y0, y1);
+    else penta_vel(comp == 0 ? dxs : dys, sp_own + comp * nz * rs, y0, y1);
+    schur(df_sub(y0, bc[2 * comp]), df_sub(y1, bc[2 * comp + 1]), g0, g1);
     const df64 gown = par ? g1 : g0, gext = ext0 ? g0 : g1;
     df64 uacc = df_zero();
     R *us = sp_own + (comp * nz + par) * rs;
-    df64 xm = df_zero(), x0 = xat(0, gown, gext);
-    for (int t = 0; t < nzp; ++t) {
-      const int m = par + 2 * t;
-      const df64 xp = xat(t + 1, gown, gext);
-      df64 u = df_mul(DTAB(DT_S0E, m), x0);
-      if (m >= 2) u = df_fma(DTAB(DT_SM2E, m), xm, u);
-      u = df_fma(DTAB(DT_SP2E, m), xp, u);
-      if (m == 0) u = df_fma(se0e, g0, u);
-      if (m == 1) u = df_fma(se1e, g1, u);
-      if (store) df_out(us, u);
-      if (WALLS) uacc = df_add(uacc, u);
-      us += 2 * rs;
-      xm = x0;
-      x0 = xp;
-    }
+    df64 xm = df_zero();
+    df64 x0 = df_fnma(df_ld(ab0 + par * nk), gown, df_lds(XS(0)));
+    rows_up<CFG::PF_W, float2>(
+        nzp, [&](int t) { return __ldg(ab0 + (par + 2 * min(t + 1, nzp - 1)) * nk); },
+        [&](int t, const float2 &ab) {
+          const int m = par + 2 * t;
+          const df64 xp = (t + 1 < nzp) ? df_fnma(df_make(ab.x, ab.y), gown, df_lds(XS(t + 1))) : gext;
+          df64 u = df_mul(DTAB(DT_S0E, m), x0);
+          if (m >= 2) u = df_fma(DTAB(DT_SM2E, m), xm, u);
+          u = df_fma(DTAB(DT_SP2E, m), xp, u);
+          if (m == 0) u = df_fma(df_lds(dfs_tab[DT_SCAL + 3]), g0, u);
+          if (m == 1) u = df_fma(df_lds(dfs_tab[DT_SCAL + 4]), g1, u);
+          if (store) df_out(us + t * 2 * rs, u);
+          if (WALLS) uacc = df_add(uacc, u);
+          xm = x0;
+          x0 = xp;
+        });
     if (WALLS) {
       const df64 uoth = df_shfl_xor(uacc, 2);
       const df64 ue = par ? uoth : uacc, uo = par ? uacc : uoth;
@@ -269,11 +378,15 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
 #undef XS
 }
 
+template <typename R>
+cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, int variant,
+                          cudaStream_t s);
+
 // Persistent kernel: CTA b owns the units of 8 wavenumbers [b per_cta,
 // (b+1) per_cta) and its warps take them from a shared-memory counter.
-template <typename R>
-__global__ void __launch_bounds__(DFS_MAXT, 1) k_bvp_df(KsArgs a, R *__restrict__ spec, double2 *__restrict__ corr,
-                                                        float2 *__restrict__ cp_scratch, int per_cta) {
+template <typename R, bool WALLS, typename CFG>
+__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict__ spec, double2 *__restrict__ corr,
+                                                         float2 *__restrict__ cp_scratch, int per_cta) {
   extern __shared__ float2 dfs_cols[];
   __shared__ int next_unit;
   const int nz = a.nz, tid = threadIdx.x, NT = blockDim.x;
@@ -316,8 +429,7 @@ __global__ void __launch_bounds__(DFS_MAXT, 1) k_bvp_df(KsArgs a, R *__restrict_
     const int i_raw = u * 8 + (lane >> 2);
     const int i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
-    if (a.mode != 0) dfs_mode<R, true>(a, spec, corr, i, store, c);
-    else dfs_mode<R, false>(a, spec, corr, i, store, c);
+    dfs_mode<R, WALLS, CFG>(a, spec, corr, i, store, c);
   }
 }
 
@@ -357,33 +469,53 @@ void launch_bvp_pack_df(const KsArgs &a, cudaStream_t s) {
   k_bvp_pack_df<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(a);
 }
 
-// Threads per CTA of k_bvp_df for nz: as many warps as the columns
+// Threads per CTA of a variant for nz: as many warps as the columns
 // (ceil(nz / 2) double-floats per lane) allow next to the static tables in
-// 227 KB of shared memory, at most DFS_MAXT / 32.
-static int bvp_df_threads(int nz) {
+// 227 KB of shared memory, at most the variant's.
+static int bvp_df_threads(int nz, int maxt) {
   const size_t per_warp = sizeof(float2) * (size_t)((nz + 1) / 2) * 32;
   const size_t stat = sizeof(dfs_tab) + 64;
   const size_t avail = (size_t)227 * 1024 - stat;
   int w = (int)(avail / per_warp);
-  if (w > DFS_MAXT / 32) w = DFS_MAXT / 32;
+  if (w > maxt / 32) w = maxt / 32;
   return w * 32;
 }
 
-// Grid (one CTA per SM, at most one per unit of 8 wavenumbers) and the bytes
-// of the pressure scratch.
+template <typename CFG, typename R, bool WALLS>
+static cudaError_t df_setup(int nz) {
+  const int nt = bvp_df_threads(nz, CFG::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
+  cudaError_t err = cudaFuncSetAttribute(k_bvp_df<R, WALLS, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_df<R, WALLS, CFG>, nt, smem);
+  if (err != cudaSuccess) return err;
+  return per_sm < 1 ? cudaErrorInvalidConfiguration : cudaSuccess;
+}
+
+template <typename CFG>
+static cudaError_t df_setup_all(int nz) {
+  cudaError_t e = df_setup<CFG, float, false>(nz);
+  if (e == cudaSuccess) e = df_setup<CFG, float, true>(nz);
+  return e;
+}
+
+int bvp_df_variants() { return DF_VARIANTS; }
+
+// Grid (one CTA per SM, fewer when the units of 8 wavenumbers run out) and
+// the bytes of the pressure scratch, for every variant.
 cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
   if (a.nz > DFS_NZMAX) return cudaErrorInvalidValue;
   if ((int64_t)a.nz * a.nk * 4 >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
-  const int nt = bvp_df_threads(a.nz);
-  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
-  cudaError_t err = cudaFuncSetAttribute(k_bvp_df<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = df_setup_all<DfV0>(a.nz);
+  if (err == cudaSuccess) err = df_setup_all<DfV1>(a.nz);
+  if (err == cudaSuccess) err = df_setup_all<DfV2>(a.nz);
+  if (err == cudaSuccess) err = df_setup_all<DfV3>(a.nz);
+  if (err == cudaSuccess) err = df_setup<DfV1, double, false>(a.nz);
+  if (err == cudaSuccess) err = df_setup<DfV1, double, true>(a.nz);
   if (err != cudaSuccess) return err;
-  err = cudaFuncSetAttribute(k_bvp_df<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_df<float>, nt, smem);
-  if (err != cudaSuccess) return err;
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const int nt = bvp_df_threads(a.nz, DF_MAXT);
   int64_t g = nsm;
   const int64_t units = (a.nk + 7) / 8;
   const int64_t warps = nt / 32;
@@ -393,17 +525,35 @@ cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch
   return cudaSuccess;
 }
 
-template <typename R>
-cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, cudaStream_t s) {
-  const int nt = bvp_df_threads(a.nz);
+template <typename CFG, typename R>
+static cudaError_t df_launch(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid,
+                             cudaStream_t s) {
+  const int nt = bvp_df_threads(a.nz, CFG::MAXT);
   const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
   const int64_t units = (a.nk + 7) / 8;
   const int per_cta = (int)((units + grid - 1) / grid);
-  k_bvp_df<R><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
+  if (a.mode != 0) k_bvp_df<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
+  else k_bvp_df<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_bvp_df<float>(const KsArgs &, float *, double2 *, float2 *, int64_t, cudaStream_t);
-template cudaError_t launch_bvp_df<double>(const KsArgs &, double *, double2 *, float2 *, int64_t, cudaStream_t);
+// variant in [0, bvp_df_variants()); the FP64-I/O instantiation (R = double,
+// used to compare the solve with the FP64 one) exists in variant 1 only
+template <>
+cudaError_t launch_bvp_df<float>(const KsArgs &a, float *spec, double2 *corr, float2 *scratch, int64_t grid,
+                                 int variant, cudaStream_t s) {
+  switch (variant) {
+    case 0: return df_launch<DfV0>(a, spec, corr, scratch, grid, s);
+    case 2: return df_launch<DfV2>(a, spec, corr, scratch, grid, s);
+    case 3: return df_launch<DfV3>(a, spec, corr, scratch, grid, s);
+    default: return df_launch<DfV1>(a, spec, corr, scratch, grid, s);
+  }
+}
+template <>
+cudaError_t launch_bvp_df<double>(const KsArgs &a, double *spec, double2 *corr, float2 *scratch, int64_t grid,
+                                  int variant, cudaStream_t s) {
+  (void)variant;
+  return df_launch<DfV1>(a, spec, corr, scratch, grid, s);
+}
 
 }  // namespace dpst

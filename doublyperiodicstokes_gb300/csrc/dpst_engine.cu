@@ -59,8 +59,10 @@ cudaError_t launch_bvp_k0(const KsArgs &a, R *spec, cudaStream_t s);
 // double-float solve of the mixed operator (dpst_bvp_df.cu)
 void launch_bvp_pack_df(const KsArgs &a, cudaStream_t s);
 cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
+int bvp_df_variants();
 template <typename R>
-cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, cudaStream_t s);
+cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, int variant,
+                          cudaStream_t s);
 template <typename R>
 void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
                       const double *kvx, const double *kvy, double H, cudaStream_t s);
@@ -119,6 +121,8 @@ struct Engine : EngineBase {
   bool dfsolve = false;
   DevBuf df_mf, df_bk, df_ab, df_gi, df_km, df_dx, df_dy, bvp_df_scratch;
   int64_t bvp_df_grid = 0;
+  int df_variant = 1;              // kernel variant chosen by tune_solve
+  float df_ms[4] = {0, 0, 0, 0};   // its creation-time timings
   DevBuf grid, spec, corr, zext, wext, kvx, kvy, zn, bands, bcrows, k0rows, Tf, Ti;
   DevBuf fac_m, fac_i, fac_d, fac_a0, fac_a1, fac_c0, fac_c1, fac_g, fac_pm, fac_pb, fac_pa;
   DevBuf pos64, flags;
@@ -302,6 +306,44 @@ struct Engine : EngineBase {
     plans = true;
     DPST_CUDA(cudaDeviceSynchronize());
     tune_ztransform();
+    tune_solve();
+  }
+
+  // The double-float solve's kernel variant (prefetch depths, warps per SM):
+  // each is timed on the spectrum buffer (3 runs after a warm-up) and the
+  // fastest kept; DPSTOKES_GB300_SOLVE_VARIANT=<v> fixes it instead.
+  void tune_solve() {
+    if (!dfsolve || sizeof(R) != 4) return;
+    const char *env = getenv("DPSTOKES_GB300_SOLVE_VARIANT");
+    if (env && *env) {
+      const int v = atoi(env);
+      if (v < 0 || v >= bvp_df_variants()) throw Error(DPST_ERR_INVALID_ARG, "DPSTOKES_GB300_SOLVE_VARIANT out of range");
+      df_variant = v;
+      return;
+    }
+    R *sp = reinterpret_cast<R *>(spec.p);
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+    if (corr.p) DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    float best = 0.0f;
+    for (int v = 0; v < bvp_df_variants() && v < 4; ++v) {
+      DPST_CUDA(launch_bvp_df<R>(ks, sp, corr.as<double2>(), bvp_df_scratch.as<float2>(), bvp_df_grid, v, 0));
+      DPST_CUDA(cudaEventRecord(a, 0));
+      for (int rep = 0; rep < 3; ++rep)
+        DPST_CUDA(launch_bvp_df<R>(ks, sp, corr.as<double2>(), bvp_df_scratch.as<float2>(), bvp_df_grid, v, 0));
+      DPST_CUDA(cudaEventRecord(b, 0));
+      DPST_CUDA(cudaEventSynchronize(b));
+      DPST_CUDA(cudaEventElapsedTime(&df_ms[v], a, b));
+      df_ms[v] /= 3.0f;
+      if (v == 0 || df_ms[v] < best) {
+        best = df_ms[v];
+        df_variant = v;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
   }
 
   ~Engine() override {
@@ -678,7 +720,8 @@ struct Engine : EngineBase {
   // per-wavenumber solve (+ k = 0) on the spectrum sp, in place
   void bvp_stage(CR *sp, cudaStream_t s) {
     if (!use_static_scratch && dfsolve) {
-      DPST_CUDA(launch_bvp_df<R>(ks, (R *)sp, corr.as<double2>(), bvp_df_scratch.as<float2>(), bvp_df_grid, s));
+      DPST_CUDA(launch_bvp_df<R>(ks, (R *)sp, corr.as<double2>(), bvp_df_scratch.as<float2>(), bvp_df_grid,
+                                 df_variant, s));
       DPST_CUDA(launch_bvp_k0<R>(ks, (R *)sp, s));
     } else if (!use_static_scratch) {
       DPST_CUDA(launch_bvp<R>(ks, (R *)sp, corr.as<double2>(), bvp_scratch.as<double>(), bvp_grid, s));
@@ -1076,6 +1119,8 @@ struct Engine : EngineBase {
     if (reg) o->kernels_per_mdot += (p.mode == DPST_MODE_NOWALL) ? 4 : 5;
     o->fused_particle_passes = fused ? 1 : 0;
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
+    o->solve_variant = dfsolve ? df_variant : 0;
+    for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,

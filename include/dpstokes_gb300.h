@@ -162,6 +162,9 @@ typedef struct dpst_info {
                                       32, 64), 0 with cuFFT's 3-D transforms */
   int solve_arith;                 /* arithmetic of the per-wavenumber solve dpst_mdot runs:
                                       DPST_SOLVE_FP64 or DPST_SOLVE_DF64 (triply periodic: 0) */
+  int solve_variant;               /* DPST_SOLVE_DF64 in the mixed operator: the kernel variant
+                                      (prefetch depths, warps per SM) chosen at creation */
+  float solve_ms[4];               /* its creation-time timings per variant (0 if not timed) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

@@ -5,7 +5,9 @@ The FP64 operator can run either solve with FP64 spectra in and out, which
 isolates the solve's arithmetic: per wavenumber (kx, ky), the velocity
 columns of the two runs (the velocity grid Fourier transformed in x and y,
 all nz levels and three components, wall correction included) agree to
-1e-12 relative to the column's own norm, and V, W to 1e-12; the FP64
+1e-12 relative to the column's own norm for the columns within 1e-2 of the
+largest (5e-12 within 1e-3; every column within 5e-14 of the largest), and
+V, W to 1e-12; the FP64
 operator with the double-float solve still matches the reference's own
 outputs to 1e-10.  The mixed operator (double-float solve by default) stays
 within 1e-6 of the mixed operator with the FP64 solve and within 1e-5 of the
@@ -56,11 +58,26 @@ def test_df64_solve_matches_fp64_solve_per_mode(name):
     c2 = torch.fft.rfft2(g2).permute(2, 3, 0, 1).reshape(w.ny, w.nx // 2 + 1, -1)
     n1 = torch.linalg.vector_norm(c1, dim=2)
     d = torch.linalg.vector_norm(c2 - c1, dim=2)
-    big = n1 > 1e-13 * n1.max()  # modes whose column is not at the rounding level of the grid
+    nmax = float(n1.max())
+    # the grid carries FP64 rounding of ~1e-16 of its largest values, which the
+    # x-y transform spreads over every mode, and double-float rounds at 2^-48
+    # (32 times FP64's unit): per-mode relative errors are bounded on the modes
+    # within 1e-2 and 1e-3 of the largest, the rest against the largest
+    big = n1 >= 1e-2 * nmax
     worst = float((d[big] / n1[big]).max())
+    mid = n1 >= 1e-3 * nmax
+    worst_mid = float((d[mid] / n1[mid]).max())
+    worst_abs = float(d.max()) / nmax
+    for lo, hi in ((1e-1, 1.1), (1e-2, 1e-1), (1e-3, 1e-2), (1e-5, 1e-3), (1e-8, 1e-5)):
+        sel = (n1 >= lo * nmax) & (n1 < hi * nmax)
+        if bool(sel.any()):
+            print("  modes with norm in [%.0e, %.0e) of the largest: %5d, max rel err %.2e" %
+                  (lo, hi, int(sel.sum()), float((d[sel] / n1[sel]).max())))
     ev, eg = rel_err(V2, V1), rel_err(g2.numpy(), g1.numpy())
-    print("%s per-mode max %.2e, grid %.2e, V %.2e" % (name, worst, eg, ev))
+    print("%s per-mode max %.2e (abs %.2e of the largest), grid %.2e, V %.2e" % (name, worst, worst_abs, eg, ev))
     assert worst < 1e-12
+    assert worst_mid < 5e-12
+    assert worst_abs < 5e-14
     assert ev < 1e-12
     if T is not None:
         assert rel_err(W2, W1) < 1e-12
@@ -88,3 +105,20 @@ def test_mixed_default_solve_is_df64(name):
     assert e1 < 1e-6 and e2 < 1e-5
     if T is not None:
         assert rel_err(Wd, Wf) < 1e-6 and rel_err(Wd, W6) < 1e-5
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_every_solve_variant(variant, monkeypatch):
+    """Each kernel variant of the double-float solve (the creation-time tuner
+    picks one): the mixed operator against its FP64-solve form."""
+    monkeypatch.setenv("DPSTOKES_GB300_SOLVE_VARIANT", str(variant))
+    for name in ("s_dpsc_t", "s_dp_t", "c2_dp_n65536@64"):
+        w = _wl(name)
+        X, F, T = W.make_inputs(w)
+        prm = StokesParams.from_workload(w, "mixed")
+        op = DPStokes(prm, w.N)
+        assert op.info()["solve_variant"] == variant
+        op.close()
+        Vd, Wd, _, _ = _run(w, "mixed", "df64", X, F, T)
+        Vf, Wf, _, _ = _run(w, "mixed", "fp64", X, F, T)
+        assert rel_err(Vd, Vf) < 1e-6 and rel_err(Wd, Wf) < 1e-6
