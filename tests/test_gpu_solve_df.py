@@ -83,7 +83,7 @@ def test_df64_solve_matches_fp64_solve_per_mode(name):
         assert rel_err(W2, W1) < 1e-12
 
 
-@pytest.mark.parametrize("name", [n for n in golden_io.names() if n.startswith(("s_d", "e_d", "c0", "c1"))])
+@pytest.mark.parametrize("name", [n for n in golden_io.names() if n.startswith(("s_d", "e_d", "c0", "c1", "c2"))])
 def test_fp64_operator_with_df64_solve_matches_reference(name):
     w, X, F, T, g = golden_io.inputs(name)
     V, Wv, _, _ = _run(w, "fp64", "df64", X, F, T)
