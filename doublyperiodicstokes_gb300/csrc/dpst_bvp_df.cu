@@ -2,14 +2,27 @@
 // (the no-wall Schur/KBPENTA solve of DPTools.cpp:81-345 and the wall values
 // the corrections of DPTools.cpp:590-877 start from), on the FP32 pipe.
 //
-// Same algorithm, factors and operation order as the FP64 solve (dpst_bvp.cu,
-// bvp_mode): pressure right-hand side Dx f + Dy g + d/dz h, the KBPENTA
-// forward and back sweeps with the border dots, the Schur correction with
-// Ginv, the SIMat / FIMat window for the pressure coefficients and its z
-// derivative, then the three velocity solves (z first) with the BC values
-// from the pressure at z = +-1.  Every value is a double-float (dpst_df64.cuh,
-// about 48 significant bits); only the wall-correction coefficients of the
-// slit channel (an 8 x 8 complex solve per mode) stay FP64.
+// Same algorithm and factorisation as the FP64 solve (dpst_bvp.cu, bvp_mode):
+// pressure right-hand side Dx f + Dy g + d/dz h, the KBPENTA forward and back
+// sweeps with the border dots, the Schur correction with Ginv, the SIMat /
+// FIMat window for the pressure coefficients and its z derivative, then the
+// three velocity solves (z first) with the BC values from the pressure at
+// z = +-1.  Every value is a double-float (dpst_df64.cuh, about 48
+// significant bits); only the wall-correction coefficients of the slit
+// channel (an 8 x 8 complex solve per mode) stay FP64.
+//
+// Scaled unknowns.  The matrix is A = I - K^2 S (S the second-integral bands)
+// per parity chain, with pivots p_j and off-diagonals -K^2 sm2_j, -K^2 sp2_j.
+// The sweeps run on u~_j = K^2 v_j / p_j (forward) and x~_j = K^2 x_j (back):
+//   v_j = X_j + sm2_j u~_{j-2},  u~_j = kappa_j v_j,
+//   x~_j = u~_j + kappa_j (sp2_j x~_{j+2}),   kappa_j = K^2 / p_j,
+// so kappa is the only per-row factor the sweeps read (against the forward
+// multiplier, pivot, upper band and both border rows of the unscaled form),
+// the border rows C = h2k R2 + RA (H^2 K times one k-independent row plus
+// another) are dotted as two k-independent sums each, the Schur step takes
+// g^ = K^2 g = Ginv (C x~ - K^2 bc), and the window outputs carry a factor
+// K^2 that is removed once per output.  One wavenumber's factors shrink from
+// 6 to 2 values per row, which keeps the re-reads of the four solves in L2.
 //
 // Work decomposition: four lanes per wavenumber.  The banded matrix couples
 // row j with j +- 2 only, and its border columns act on rows of one parity
@@ -33,9 +46,10 @@
 namespace dpst {
 
 constexpr int DFS_NZMAX = 128;
-enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_DH };
-// k-independent tables as double-floats, at fixed offsets; then the scalars
-// se0, se1, fe, se0 / eta, se1 / eta
+enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_BR2, DT_BRA, DT_BL2, DT_BLA, DT_DH };
+// k-independent tables as double-floats, at fixed offsets (the BC rows as
+// C0 = H^2 K BR2 + BRA, C1 = H^2 K BL2 + BLA); then the scalars se0, se1,
+// fe, se0 / eta, se1 / eta
 __shared__ float2 dfs_tab[DT_DH * DFS_NZMAX + DFS_NZMAX + 1 + 5];
 #define DTAB(t, j) df_lds(dfs_tab[(t) * DFS_NZMAX + (j)])
 constexpr int DT_SCAL = DT_DH * DFS_NZMAX + DFS_NZMAX + 1;
@@ -86,11 +100,8 @@ struct DfRhsP {  // pressure right-hand side inputs of one row
 };
 template <typename R>
 struct DfRhsV {  // velocity forward-sweep inputs of one row
-  float2 m, cp;
+  float2 k, cp;
   R f;
-};
-struct DfBack {
-  float4 b0, b1;
 };
 template <typename R>
 struct DfWinP {  // pressure window inputs: A^{-1}B of row t + 1, f_z of row t
@@ -106,9 +117,9 @@ template <int F, int B, int W, int T>
 struct DfCfg {
   static constexpr int PF_F = F, PF_B = B, PF_W = W, MAXT = T;
 };
-using DfV0 = DfCfg<2, 1, 2, 416>;
-using DfV1 = DfCfg<4, 2, 4, 384>;
-using DfV2 = DfCfg<6, 3, 6, 384>;
+using DfV0 = DfCfg<4, 4, 4, 416>;
+using DfV1 = DfCfg<8, 8, 4, 384>;
+using DfV2 = DfCfg<8, 8, 8, 384>;
 using DfV3 = DfCfg<4, 4, 4, 384>;
 constexpr int DF_VARIANTS = 4;
 constexpr int DF_MAXT = 416;  // the most threads of any variant
@@ -133,10 +144,11 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   // (i a)_part = sp a_(other part), sp = -1 for the real part
   const df64 dxs = part ? df_ld(a.dx2 + ix) : df_neg(df_ld(a.dx2 + ix));
   const df64 dys = part ? df_ld(a.dy2 + iy) : df_neg(df_ld(a.dy2 + iy));
-  const float2 *__restrict__ mf0 = a.mf2 + i;
-  const float4 *__restrict__ bk0 = a.bk2 + 2 * i;
+  const float2 *__restrict__ kap0 = a.kap2 + i;
   const float2 *__restrict__ ab0 = a.ab2 + i;
-  // g = Ginv r
+  const float4 k2 = __ldg(a.km2 + i);
+  const df64 K2 = df_make(k2.x, k2.y), iK2 = df_make(k2.z, k2.w);  // K^2, 1/K^2
+  // g^ = Ginv r
   auto schur = [&](df64 r0, df64 r1, df64 &g0, df64 &g1) {
     g0 = df_fma(df_ld(a.gi2 + i), r0, df_mul(df_ld(a.gi2 + 2 * nk + i), r1));
     g1 = df_fma(df_ld(a.gi2 + nk + i), r0, df_mul(df_ld(a.gi2 + 3 * nk + i), r1));
@@ -168,72 +180,72 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
         });
   }
 
-  // KBPENTA sweeps (LinearSolvers.h:106-141) on this chain, in place, with
-  // the border dots y = C x summed over both chains.  The forward sweep takes
-  // its right-hand side from XS (VEL = false) or forms Dc cp_other - f_c for
-  // an x / y velocity component (VEL = true).
+  // KBPENTA sweeps (LinearSolvers.h:106-141) on this chain in the scaled
+  // unknowns, in place; returns y~ = C x~ summed over both chains.  The
+  // forward sweep takes its right-hand side from XS or (x / y velocity) forms
+  // Dc cp_other - f_c.
+  const float4 k3 = __ldg(a.km3 + i);
+  const df64 h2k = df_make(k3.x, k3.y);
   auto back = [&](df64 &y0, df64 &y1) {
-    df64 vp = df_zero();
-    df64 a0 = df_zero(), a1 = df_zero();
-    rows_down<CFG::PF_B, DfBack>(
-        nzp,
-        [&](int t) {
+    df64 xn = df_zero();
+    df_acc s1 = acc_zero(), s2 = acc_zero(), s3 = acc_zero(), s4 = acc_zero();
+    rows_down<CFG::PF_B, float2>(
+        nzp, [&](int t) { return __ldg(kap0 + (par + 2 * t) * nk); },
+        [&](int t, const float2 &k) {
           const int j = par + 2 * t;
-          DfBack v;
-          v.b0 = __ldg(bk0 + j * rs);
-          v.b1 = __ldg(bk0 + j * rs + 1);
-          return v;
-        },
-        [&](int t, const DfBack &v) {
-          const df64 x = df_mul(df_make(v.b0.x, v.b0.y), df_fnma(df_make(v.b0.z, v.b0.w), vp, df_lds(XS(t))));
+          const df64 x = df_fma(df_make(k.x, k.y), df_mul(DTAB(DT_SP2, j), xn), df_lds(XS(t)));
           XS(t) = df_f2(x);
-          vp = x;
-          a0 = df_fma(df_make(v.b1.x, v.b1.y), x, a0);
-          a1 = df_fma(df_make(v.b1.z, v.b1.w), x, a1);
+          xn = x;
+          acc_fma(s1, DTAB(DT_BR2, j), x);
+          acc_fma(s2, DTAB(DT_BRA, j), x);
+          acc_fma(s3, DTAB(DT_BL2, j), x);
+          acc_fma(s4, DTAB(DT_BLA, j), x);
         });
-    y0 = df_add(a0, df_shfl_xor(a0, 2));
-    y1 = df_add(a1, df_shfl_xor(a1, 2));
+    const df64 o0 = df_fma(h2k, acc_val(s1), acc_val(s2)), o1 = df_fma(h2k, acc_val(s3), acc_val(s4));
+    y0 = df_add(o0, df_shfl_xor(o0, 2));
+    y1 = df_add(o1, df_shfl_xor(o1, 2));
   };
   auto penta_xs = [&](df64 &y0, df64 &y1) {
-    df64 vm = df_zero();
+    df64 un = df_zero();
     rows_up<CFG::PF_F, float2>(
-        nzp, [&](int t) { return __ldg(mf0 + (par + 2 * t) * nk); },
-        [&](int t, const float2 &m) {
-          const df64 v = df_fnma(df_make(m.x, m.y), vm, df_lds(XS(t)));
-          XS(t) = df_f2(v);
-          vm = v;
+        nzp, [&](int t) { return __ldg(kap0 + (par + 2 * t) * nk); },
+        [&](int t, const float2 &k) {
+          const df64 u = df_mul(df_make(k.x, k.y), df_fma(DTAB(DT_SM2, par + 2 * t), un, df_lds(XS(t))));
+          XS(t) = df_f2(u);
+          un = u;
         });
     back(y0, y1);
   };
   auto penta_vel = [&](df64 dcs, const R *fs, df64 &y0, df64 &y1) {
-    df64 vm = df_zero();
+    df64 un = df_zero();
     const float2 *cpo = c.CPo;
     rows_up<CFG::PF_F, DfRhsV<R>>(
         nzp,
         [&](int t) {
           const int j = par + 2 * t;
           DfRhsV<R> v;
-          v.m = __ldg(mf0 + j * nk);
+          v.k = __ldg(kap0 + j * nk);
           v.cp = cpo[t * GT];
           v.f = fs[j * rs];
           return v;
         },
         [&](int t, const DfRhsV<R> &v) {
           const df64 X = df_sub(df_mul(dcs, df_make(v.cp.x, v.cp.y)), df_v(v.f));
-          const df64 x = df_fnma(df_make(v.m.x, v.m.y), vm, X);
-          XS(t) = df_f2(x);
-          vm = x;
+          const df64 u = df_mul(df_make(v.k.x, v.k.y), df_fma(DTAB(DT_SM2, par + 2 * t), un, X));
+          XS(t) = df_f2(u);
+          un = u;
         });
     back(y0, y1);
   };
   const bool ext0 = (par + 2 * nzp == nz);  // this chain's extension is g0 (else g1)
 
-  // ---- pressure: Schur solve, cp = S [x; g] (kept for the other part's x, y
-  // velocity right-hand sides), dp = F [x; g] -> z-velocity right-hand side.
-  // The border-corrected solution of this chain is x_j = X_j - (A^{-1}B)_j g_par
-  // (column 0 on even rows, column 1 on odd rows), extended by the border
-  // unknown that follows its last row (x_nz = g0, x_nz+1 = g1).
-  df64 pacc = df_zero();  // sum of this chain's pressure coefficients
+  // ---- pressure: Schur solve, cp = S [x; g] (kept, times K^2, for the other
+  // part's x, y velocity right-hand sides), dp = F [x; g] -> z-velocity
+  // right-hand side.  The border-corrected solution of this chain, times K^2,
+  // is x^_j = x~_j - (A^{-1}B)_j g^_par (column 0 on even rows, column 1 on
+  // odd rows), extended by the border unknown that follows its last row
+  // (x_nz = g0, x_nz+1 = g1).
+  df_acc pacc = acc_zero();  // sum of this chain's pressure coefficients (x K^2)
   {
     df64 y0, y1, g0, g1;
     penta_xs(y0, y1);
@@ -269,8 +281,9 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
             if (m >= 1) dp = df_fma(DTAB(DT_FM1, m), xl, dp);
             if (m == 0) dp = df_fma(df_lds(dfs_tab[DT_SCAL + 2]), g1, dp);
             cpw[t * GT] = df_f2(cp);
-            pacc = df_add(pacc, cp);
-            XS(t) = df_f2(df_sub(dp, df_v(v.fz)));  // eta x z-velocity RHS (DPTools.cpp:214)
+            acc_add(pacc, cp);
+            // eta x z-velocity RHS (DPTools.cpp:214)
+            XS(t) = df_f2(df_sub(df_mul(dp, iK2), df_v(v.fz)));
           }
           xm = x0;
           x0 = xp;
@@ -279,13 +292,14 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   // velocity BC right-hand sides (DPTools.cpp:218-234): the pressure at
   // z = +-1 is the sum and the alternating sum of its coefficients; the
   // velocity solves run on eta x their right-hand sides (1/eta sits in the
-  // window's SIMat bands), so the BC values are scaled by eta too
+  // window's SIMat bands), so the BC values are scaled by eta too; they enter
+  // the Schur step times K^2
   df64 bc[6];
   {
-    const float4 kk = __ldg(a.km2 + i);
-    const df64 hK = df_make(kk.z, kk.w);  // 1 / (2 K)
-    const df64 poth = df_shfl_xor(pacc, 2);
-    const df64 pe = par ? poth : pacc, po = par ? pacc : poth;
+    const df64 hK = df_make(k3.z, k3.w);  // 1 / (2 K)
+    const df64 pown = df_mul(acc_val(pacc), iK2);
+    const df64 poth = df_shfl_xor(pown, 2);
+    const df64 pe = par ? poth : pown, po = par ? pown : poth;
     const df64 ssum = df_add(pe, po), asum = df_sub(pe, po);
     const df64 ssum_o = df_shfl_xor(ssum, 1), asum_o = df_shfl_xor(asum, 1);
     bc[0] = df_neg(df_mul(hK, df_mul(dxs, ssum_o)));
@@ -304,10 +318,10 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
     const int comp = (cc + 2) % 3;  // 2, 0, 1
     df64 y0, y1, g0, g1;
     if (comp == 2) penta_xs(y0, y1);
-    else penta_vel(comp == 0 ? dxs : dys, sp_own + comp * nz * rs, y0, y1);
-    schur(df_sub(y0, bc[2 * comp]), df_sub(y1, bc[2 * comp + 1]), g0, g1);
+    else penta_vel(df_mul(comp == 0 ? dxs : dys, iK2), sp_own + comp * nz * rs, y0, y1);
+    schur(df_fnma(K2, bc[2 * comp], y0), df_fnma(K2, bc[2 * comp + 1], y1), g0, g1);
     const df64 gown = par ? g1 : g0, gext = ext0 ? g0 : g1;
-    df64 uacc = df_zero();
+    df_acc uacc = acc_zero();
     R *us = sp_own + (comp * nz + par) * rs;
     df64 xm = df_zero();
     df64 x0 = df_fnma(df_ld(ab0 + par * nk), gown, df_lds(XS(0)));
@@ -321,14 +335,15 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
           u = df_fma(DTAB(DT_SP2E, m), xp, u);
           if (m == 0) u = df_fma(df_lds(dfs_tab[DT_SCAL + 3]), g0, u);
           if (m == 1) u = df_fma(df_lds(dfs_tab[DT_SCAL + 4]), g1, u);
-          if (store) df_out(us + t * 2 * rs, u);
-          if (WALLS) uacc = df_add(uacc, u);
+          if (store) df_out(us + t * 2 * rs, df_mul(u, iK2));
+          if (WALLS) acc_add(uacc, u);
           xm = x0;
           x0 = xp;
         });
     if (WALLS) {
-      const df64 uoth = df_shfl_xor(uacc, 2);
-      const df64 ue = par ? uoth : uacc, uo = par ? uacc : uoth;
+      const df64 uown = df_mul(acc_val(uacc), iK2);
+      const df64 uoth = df_shfl_xor(uown, 2);
+      const df64 ue = par ? uoth : uown, uo = par ? uown : uoth;
       wt[comp] = df_add(ue, uo);  // u(z = 1), u(z = -1)
       wb[comp] = df_sub(ue, uo);
     }
@@ -401,6 +416,14 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
     dfs_tab[DT_SM2E * DFS_NZMAX + t] = df_f2(df_from_d(a.sm2[t] * inv_eta));
     dfs_tab[DT_SP2E * DFS_NZMAX + t] = df_f2(df_from_d(a.sp2[t] * inv_eta));
   }
+  for (int t = tid; t < nz; t += NT) {
+    // BC rows at k: C0 = bcr2 H^2 K + (bcr2 + (H bcr1 - bcr2)), C1 = bcl2 H^2 K +
+    // (-bcl2 + (H bcl1 + bcl2)) (Solvers.py:315-331, as k_bvp_factors forms them)
+    dfs_tab[DT_BR2 * DFS_NZMAX + t] = df_f2(df_from_d(a.bcr2[t]));
+    dfs_tab[DT_BRA * DFS_NZMAX + t] = df_f2(df_from_d(a.bcr2[t] + (a.H * a.bcr1[t] - a.bcr2[t])));
+    dfs_tab[DT_BL2 * DFS_NZMAX + t] = df_f2(df_from_d(a.bcl2[t]));
+    dfs_tab[DT_BLA * DFS_NZMAX + t] = df_f2(df_from_d(-a.bcl2[t] + (a.H * a.bcl1[t] + a.bcl2[t])));
+  }
   for (int t = tid; t <= nz; t += NT) dfs_tab[DT_DH * DFS_NZMAX + t] = df_f2(df_from_d((double)(2 * t) / a.H));
   if (tid == 0) {
     dfs_tab[DT_SCAL] = df_f2(df_from_d(a.se0));
@@ -433,25 +456,29 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
   }
 }
 
-// Double-float copies of the packed factors (one thread per table entry).
+// Per-wavenumber data of the double-float solve (one thread per entry):
+// kappa_j = K^2 / beta_{j+1} from the packed pivots, A^{-1}B, Ginv, the
+// per-mode scalars and Dx, Dy.
 __global__ void k_bvp_pack_df(KsArgs a) {
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nk = a.nk;
+  auto k2_of = [&](int64_t i) {
+    const int ix = (int)(i % a.nxh), iy = (int)(i / a.nxh);
+    const double kx = a.kvx[ix], ky = a.kvy[iy];
+    return kx * kx + ky * ky;
+  };
   if (t < (int64_t)a.nz * nk) {
-    a.mf2[t] = df_f2(df_from_d(a.mf[t]));
+    const int64_t i = t % nk;
+    a.kap2[t] = df_f2(df_from_d(k2_of(i) * a.bk[4 * t]));
     a.ab2[t] = df_f2(df_from_d(a.ab[t]));
-    const double *b = a.bk + 4 * t;
-    const df64 b0 = df_from_d(b[0]), b1 = df_from_d(b[1]), b2 = df_from_d(b[2]), b3 = df_from_d(b[3]);
-    a.bk2[2 * t] = make_float4(b0.hi, b0.lo, b1.hi, b1.lo);
-    a.bk2[2 * t + 1] = make_float4(b2.hi, b2.lo, b3.hi, b3.lo);
   }
   if (t < 4 * nk) a.gi2[t] = df_f2(df_from_d(a.ginv[t]));
   if (t < nk) {
-    const int ix = (int)(t % a.nxh), iy = (int)(t / a.nxh);
-    const double kx = a.kvx[ix], ky = a.kvy[iy];
-    const double K = sqrt(kx * kx + ky * ky);
-    const df64 k = df_from_d(K), h = df_from_d(K > 0.0 ? 0.5 / K : 0.0);
-    a.km2[t] = make_float4(k.hi, k.lo, h.hi, h.lo);
+    const double K2 = k2_of(t), K = sqrt(K2);
+    const df64 k2 = df_from_d(K2), ik2 = df_from_d(K2 > 0.0 ? 1.0 / K2 : 0.0);
+    const df64 h2k = df_from_d((a.H * a.H) * K), hk = df_from_d(K > 0.0 ? 0.5 / K : 0.0);
+    a.km2[t] = make_float4(k2.hi, k2.lo, ik2.hi, ik2.lo);
+    a.km3[t] = make_float4(h2k.hi, h2k.lo, hk.hi, hk.lo);
   }
   if (t < a.nxh) {
     const double kx = a.kvx[t];

@@ -119,6 +119,36 @@ static __device__ __forceinline__ df64 df_fma(df64 a, float b, df64 c) {
 // c - a * b
 static __device__ __forceinline__ df64 df_fnma(df64 a, df64 b, df64 c) { return df_fma(df_neg(a), b, c); }
 
+// Compensated accumulator of a sum of double-float terms or products (the
+// scheme of Ogita, Rump and Oishi's Dot2): the hi parts are summed with
+// TwoSum and every rounding error and lo part is collected in one FP32
+// correction, normalised once at the end; 8 (sum) or 12 (product)
+// operations per term instead of 10 or 15 for a renormalised double-float.
+struct df_acc {
+  float s, e;
+};
+static __device__ __forceinline__ df_acc acc_zero() {
+  df_acc a;
+  a.s = 0.0f;
+  a.e = 0.0f;
+  return a;
+}
+static __device__ __forceinline__ void acc_add(df_acc &a, df64 x) {
+  const df64 t = two_sum(a.s, x.hi);
+  a.s = t.hi;
+  a.e = __fadd_rn(a.e, __fadd_rn(t.lo, x.lo));
+}
+static __device__ __forceinline__ void acc_fma(df_acc &a, df64 x, df64 y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  const df64 t = two_sum(a.s, p);
+  a.s = t.hi;
+  a.e = __fadd_rn(a.e, __fadd_rn(t.lo, e));
+}
+static __device__ __forceinline__ df64 acc_val(df_acc a) { return two_sum(a.s, a.e); }
+
 static __device__ __forceinline__ df64 df_shfl_xor(df64 a, int m) {
   return df_make(__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m));
 }

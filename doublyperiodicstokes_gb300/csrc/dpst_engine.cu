@@ -260,14 +260,14 @@ struct Engine : EngineBase {
     if (dfsolve) {
       df_mf.alloc(sizeof(float2) * nz * nk);
       df_ab.alloc(sizeof(float2) * nz * nk);
-      df_bk.alloc(sizeof(float4) * 2 * nz * nk);
+      df_bk.alloc(sizeof(float4) * nk);
       df_gi.alloc(sizeof(float2) * 4 * nk);
       df_km.alloc(sizeof(float4) * nk);
       df_dx.alloc(sizeof(float2) * nxh);
       df_dy.alloc(sizeof(float2) * ny);
-      ks.mf2 = df_mf.as<float2>();
+      ks.kap2 = df_mf.as<float2>();
       ks.ab2 = df_ab.as<float2>();
-      ks.bk2 = df_bk.as<float4>();
+      ks.km3 = df_bk.as<float4>();
       ks.gi2 = df_gi.as<float2>();
       ks.km2 = df_km.as<float4>();
       ks.dx2 = df_dx.as<float2>();

@@ -133,16 +133,18 @@ struct KsArgs {
   // solve beside the FP64 ones for the mixed operator's epilogue (nullptr:
   // not wanted)
   float2 *corrf;
-  // double-float copies (hi, lo FP32 pairs) of the packed factors for the
-  // double-float solve k_bvp_df (nullptr when the handle does not use it):
-  //   mf2 [nz][nk], ab2 [nz][nk]  as mf, ab
-  //   bk2 [nz][nk][2]             {1/beta_{j+1}, dp2_j}, {C0_j, C1_j}
-  //   gi2 [4][nk]                 as ginv
-  //   km2 [nk]                    {K, 1/(2K)} (zero for k = 0)
-  //   dx2 [nxh], dy2 [ny]         the derivative wavenumbers Dx, Dy (kx, ky
-  //                               with the Nyquist entries of even sizes zeroed)
-  float2 *mf2, *ab2, *gi2, *dx2, *dy2;
-  float4 *bk2, *km2;
+  // per-wavenumber data of the double-float solve k_bvp_df, as hi, lo FP32
+  // pairs (nullptr when the handle does not use it):
+  //   kap2 [nz][nk]  kappa_j = K^2 / beta_{j+1} (K^2 times the reciprocal pivot
+  //                  of row j); the sweeps run on K^2-scaled unknowns, so this
+  //                  is the only per-row factor besides A^{-1}B
+  //   ab2 [nz][nk]   as ab
+  //   gi2 [4][nk]    as ginv
+  //   km2 [nk]       {K^2, 1/K^2}; km3 [nk] {H^2 K, 1/(2K)} (zero for k = 0)
+  //   dx2 [nxh], dy2 [ny]  the derivative wavenumbers Dx, Dy (kx, ky with the
+  //                  Nyquist entries of even sizes zeroed)
+  float2 *kap2, *ab2, *gi2, *dx2, *dy2;
+  float4 *km2, *km3;
 };
 
 // Epilogue of the z-transform GEMM.
