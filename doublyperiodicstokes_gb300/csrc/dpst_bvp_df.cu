@@ -19,7 +19,7 @@
 // so kappa is the only per-row factor the sweeps read (against the forward
 // multiplier, pivot, upper band and both border rows of the unscaled form),
 // the border rows C = h2k R2 + RA (H^2 K times one k-independent row plus
-// another) are dotted as two k-independent sums each, the Schur step takes
+// another) are dotted as two k-independent sums, the Schur step takes
 // g^ = K^2 g = Ginv (C x~ - K^2 bc), and the window outputs carry a factor
 // K^2 that is removed once per output.  One wavenumber's factors shrink from
 // 6 to 2 values per row, which keeps the re-reads of the four solves in L2.
@@ -46,10 +46,10 @@
 namespace dpst {
 
 constexpr int DFS_NZMAX = 128;
-enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_BR2, DT_BRA, DT_BL2, DT_BLA, DT_DH };
-// k-independent tables as double-floats, at fixed offsets (the BC rows as
-// C0 = H^2 K BR2 + BRA, C1 = H^2 K BL2 + BLA); then the scalars se0, se1,
-// fe, se0 / eta, se1 / eta
+enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_BR2, DT_BRA, DT_DH };
+// k-independent tables as double-floats, at fixed offsets (the first BC row
+// as C0 = H^2 K BR2 + BRA); then the scalars se0, se1, fe, se0 / eta,
+// se1 / eta
 __shared__ float2 dfs_tab[DT_DH * DFS_NZMAX + DFS_NZMAX + 1 + 5];
 #define DTAB(t, j) df_lds(dfs_tab[(t) * DFS_NZMAX + (j)])
 constexpr int DT_SCAL = DT_DH * DFS_NZMAX + DFS_NZMAX + 1;
@@ -186,9 +186,14 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   // Dc cp_other - f_c.
   const float4 k3 = __ldg(a.km3 + i);
   const df64 h2k = df_make(k3.x, k3.y);
+  // The two BC rows are mirror images: bcl_j = -(-1)^j bcr_j for j < nz
+  // (Solvers.py:603-643 builds them with the same magnitudes), so on one
+  // parity chain C1 = sg C0 with sg = -1 (even rows) or +1 (odd rows), up to
+  // the FP64 rounding of the reference's sums; one dot per chain gives both.
+  const float sg = par ? 1.0f : -1.0f;
   auto back = [&](df64 &y0, df64 &y1) {
     df64 xn = df_zero();
-    df_acc s1 = acc_zero(), s2 = acc_zero(), s3 = acc_zero(), s4 = acc_zero();
+    df_acc s1 = acc_zero(), s2 = acc_zero();
     rows_down<CFG::PF_B, float2>(
         nzp, [&](int t) { return __ldg(kap0 + (par + 2 * t) * nk); },
         [&](int t, const float2 &k) {
@@ -198,10 +203,8 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
           xn = x;
           acc_fma(s1, DTAB(DT_BR2, j), x);
           acc_fma(s2, DTAB(DT_BRA, j), x);
-          acc_fma(s3, DTAB(DT_BL2, j), x);
-          acc_fma(s4, DTAB(DT_BLA, j), x);
         });
-    const df64 o0 = df_fma(h2k, acc_val(s1), acc_val(s2)), o1 = df_fma(h2k, acc_val(s3), acc_val(s4));
+    const df64 o0 = df_fma(h2k, acc_val(s1), acc_val(s2)), o1 = df_scale2(o0, sg);
     y0 = df_add(o0, df_shfl_xor(o0, 2));
     y1 = df_add(o1, df_shfl_xor(o1, 2));
   };
@@ -230,7 +233,7 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
           return v;
         },
         [&](int t, const DfRhsV<R> &v) {
-          const df64 X = df_sub(df_mul(dcs, df_make(v.cp.x, v.cp.y)), df_v(v.f));
+          const df64 X = df_fms(dcs, df_make(v.cp.x, v.cp.y), df_v(v.f));
           const df64 u = df_mul(df_make(v.k.x, v.k.y), df_fma(DTAB(DT_SM2, par + 2 * t), un, X));
           XS(t) = df_f2(u);
           un = u;
@@ -283,7 +286,7 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
             cpw[t * GT] = df_f2(cp);
             acc_add(pacc, cp);
             // eta x z-velocity RHS (DPTools.cpp:214)
-            XS(t) = df_f2(df_sub(df_mul(dp, iK2), df_v(v.fz)));
+            XS(t) = df_f2(df_fms(dp, iK2, df_v(v.fz)));
           }
           xm = x0;
           x0 = xp;
@@ -417,12 +420,10 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
     dfs_tab[DT_SP2E * DFS_NZMAX + t] = df_f2(df_from_d(a.sp2[t] * inv_eta));
   }
   for (int t = tid; t < nz; t += NT) {
-    // BC rows at k: C0 = bcr2 H^2 K + (bcr2 + (H bcr1 - bcr2)), C1 = bcl2 H^2 K +
-    // (-bcl2 + (H bcl1 + bcl2)) (Solvers.py:315-331, as k_bvp_factors forms them)
+    // first BC row at k: C0 = bcr2 H^2 K + (bcr2 + (H bcr1 - bcr2))
+    // (Solvers.py:315-331, as k_bvp_factors forms it)
     dfs_tab[DT_BR2 * DFS_NZMAX + t] = df_f2(df_from_d(a.bcr2[t]));
     dfs_tab[DT_BRA * DFS_NZMAX + t] = df_f2(df_from_d(a.bcr2[t] + (a.H * a.bcr1[t] - a.bcr2[t])));
-    dfs_tab[DT_BL2 * DFS_NZMAX + t] = df_f2(df_from_d(a.bcl2[t]));
-    dfs_tab[DT_BLA * DFS_NZMAX + t] = df_f2(df_from_d(-a.bcl2[t] + (a.H * a.bcl1[t] + a.bcl2[t])));
   }
   for (int t = tid; t <= nz; t += NT) dfs_tab[DT_DH * DFS_NZMAX + t] = df_f2(df_from_d((double)(2 * t) / a.H));
   if (tid == 0) {

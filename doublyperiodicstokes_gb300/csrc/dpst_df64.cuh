@@ -118,6 +118,16 @@ static __device__ __forceinline__ df64 df_fma(df64 a, float b, df64 c) {
 }
 // c - a * b
 static __device__ __forceinline__ df64 df_fnma(df64 a, df64 b, df64 c) { return df_fma(df_neg(a), b, c); }
+// a * b - c for an FP32 or double-float c
+static __device__ __forceinline__ df64 df_fms(df64 a, df64 b, float c) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  const df64 s = two_sum(p, -c);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, e));
+}
+static __device__ __forceinline__ df64 df_fms(df64 a, df64 b, df64 c) { return df_fma(a, b, df_neg(c)); }
 
 // Compensated accumulator of a sum of double-float terms or products (the
 // scheme of Ogita, Rump and Oishi's Dot2): the hi parts are summed with
