@@ -43,6 +43,14 @@ void launch_interp_b(bool dipole, int64_t total, const SysP<R> *sys, const int64
                      bool dip_ghosts, cudaStream_t s);
 template <typename R>
 cudaError_t bvp_plan_b(int nz, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
+void launch_bvp_pack_df(const KsArgs &a, cudaStream_t s);
+int bvp_df_variants();
+cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
+template <typename R>
+cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
 template <typename R>
 cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, double *scratch,
                          int64_t grid, cudaStream_t s);
@@ -91,6 +99,10 @@ struct BatchEngine : BatchBase {
   DevBuf grid, spec, corr, zext, wext, zn, bands, bcrows, k0rows, Tf, Ti, kvs;
   DevBuf corrf, cmode, znf;  // FP32 correction tables (mixed operator, walls)
   DevBuf f_mf, f_bk, f_ab, f_g;
+  // double-float solve (default for the mixed operator): per-system tables
+  bool dfsolve = false;
+  int df_variant = 1;
+  DevBuf df_kap, df_ab, df_gi, df_km, df_km3, df_dxy;
   DevBuf st_cell_m, st_x_m, st_y_m, st_z_m, st_zw_m;
   DevBuf st_cell_d, st_x_d, st_y_d, st_z_d, st_zw_d, st_dx_d, st_dy_d, st_dz_d, st_dzw_d;
   DevBuf ghost_buf, pos64, bvp_scratch, fft_work;
@@ -109,6 +121,56 @@ struct BatchEngine : BatchBase {
   bool positioned = false;
   int kernels_per_mdot = 0;
 
+  // the per-wavenumber solve of every system (+ their k = 0 modes)
+  void solve(cudaStream_t s) {
+    if (dfsolve) {
+      DPST_CUDA(launch_bvp_df_b<R>(d_sysk.as<SysK<R>>(), S, d_mprefix.as<int64_t>(), K, nz, mode,
+                                   bvp_scratch.as<float2>(), bvp_grid, df_variant, s));
+      DPST_CUDA(launch_bvp_k0_b<R>(d_sysk.as<SysK<R>>(), S, s));
+    } else {
+      DPST_CUDA(launch_bvp_b<R>(d_sysk.as<SysK<R>>(), S, d_mprefix.as<int64_t>(), K, nz, bvp_scratch.as<double>(),
+                                bvp_grid, s));
+    }
+  }
+
+  // the double-float solve's kernel variant, timed on the spectrum buffer as
+  // the single-system engine does (DPSTOKES_GB300_SOLVE_VARIANT fixes it)
+  void tune_solve() {
+    const char *env = getenv("DPSTOKES_GB300_SOLVE_VARIANT");
+    if (env && *env) {
+      const int v = atoi(env);
+      if (v < 0 || v >= bvp_df_variants()) throw Error(DPST_ERR_INVALID_ARG, "DPSTOKES_GB300_SOLVE_VARIANT out of range");
+      df_variant = v;
+      return;
+    }
+    if (sizeof(R) != 4) return;
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+    if (corr.p) DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    float best = 0.0f;
+    for (int v = 0; v < bvp_df_variants(); ++v) {
+      auto run = [&] {
+        DPST_CUDA(launch_bvp_df_b<R>(d_sysk.as<SysK<R>>(), S, d_mprefix.as<int64_t>(), K, nz, mode,
+                                     bvp_scratch.as<float2>(), bvp_grid, v, 0));
+      };
+      run();
+      DPST_CUDA(cudaEventRecord(a, 0));
+      for (int rep = 0; rep < 3; ++rep) run();
+      DPST_CUDA(cudaEventRecord(b, 0));
+      DPST_CUDA(cudaEventSynchronize(b));
+      float ms = 0.0f;
+      DPST_CUDA(cudaEventElapsedTime(&ms, a, b));
+      if (v == 0 || ms < best) {
+        best = ms;
+        df_variant = v;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+
   BatchEngine(const dpst_params *prm, const int64_t *n, int count, int dev) {
     device = dev;
     S = count;
@@ -119,9 +181,10 @@ struct BatchEngine : BatchBase {
       validate(&prm[s], n[s]);
       const dpst_params &p = prm[s];
       if (p.nz != p0.nz || p.zmin != p0.zmin || p.zmax != p0.zmax || p.mode != p0.mode ||
-          p.viscosity != p0.viscosity || p.precision != p0.precision || p.has_torque != p0.has_torque)
-        throw Error(DPST_ERR_INVALID_ARG,
-                    "systems of a batch must share nz, zmin, zmax, mode, viscosity, precision and has_torque");
+          p.viscosity != p0.viscosity || p.precision != p0.precision || p.has_torque != p0.has_torque ||
+          p.solve_arith != p0.solve_arith)
+        throw Error(DPST_ERR_INVALID_ARG, "systems of a batch must share nz, zmin, zmax, mode, viscosity, "
+                                          "precision, has_torque and solve_arith");
     }
     nz = p0.nz;
     mode = p0.mode;
@@ -248,6 +311,15 @@ struct BatchEngine : BatchBase {
     f_bk.alloc(sizeof(double) * 4 * nz * K);
     f_ab.alloc(sizeof(double) * nz * K);
     f_g.alloc(sizeof(double) * 4 * K);
+    dfsolve = p0.solve_arith == DPST_SOLVE_DF64 || (p0.solve_arith == DPST_SOLVE_DEFAULT && sizeof(R) == 4);
+    if (dfsolve) {
+      df_kap.alloc(sizeof(float2) * nz * K);
+      df_ab.alloc(sizeof(float2) * nz * K);
+      df_gi.alloc(sizeof(float2) * 4 * K);
+      df_km.alloc(sizeof(float4) * K);
+      df_km3.alloc(sizeof(float4) * K);
+      df_dxy.alloc(sizeof(float2) * kvs.bytes / sizeof(double));
+    }
     std::vector<SysK<R>> sysk(S);
     {
       DevBuf w_m, w_i, w_d, w_a0, w_a1, w_c0, w_c1;
@@ -307,6 +379,17 @@ struct BatchEngine : BatchBase {
         launch_bvp_factors(ks, 0);
         DPST_CUDA(cudaGetLastError());
         ks.mfac = ks.invb = ks.dp2 = ks.ab0 = ks.ab1 = ks.c0 = ks.c1 = nullptr;
+        if (dfsolve) {
+          ks.kap2 = df_kap.as<float2>() + nz * moff[s];
+          ks.ab2 = df_ab.as<float2>() + nz * moff[s];
+          ks.gi2 = df_gi.as<float2>() + 4 * moff[s];
+          ks.km2 = df_km.as<float4>() + moff[s];
+          ks.km3 = df_km3.as<float4>() + moff[s];
+          ks.dx2 = df_dxy.as<float2>() + kvoff[s];
+          ks.dy2 = df_dxy.as<float2>() + kvoff[s] + p.nx;
+          launch_bvp_pack_df(ks, 0);
+          DPST_CUDA(cudaGetLastError());
+        }
         sysk[s].ks = ks;
         sysk[s].spec = reinterpret_cast<R *>(spec.as<CR>() + soff[s]);
         sysk[s].corr = (mode != DPST_MODE_NOWALL) ? corr.as<double2>() + 16 * moff[s] : nullptr;
@@ -347,8 +430,13 @@ struct BatchEngine : BatchBase {
     upload(d_segf, segf);
     upload(d_segi, segi);
     size_t bvp_bytes = 0;
-    DPST_CUDA(bvp_plan_b<R>(nz, K, nsm, &bvp_grid, &bvp_bytes));
+    if (dfsolve) {
+      DPST_CUDA(bvp_df_plan_b(sysk[0].ks, K, nsm, &bvp_grid, &bvp_bytes));
+    } else {
+      DPST_CUDA(bvp_plan_b<R>(nz, K, nsm, &bvp_grid, &bvp_bytes));
+    }
     bvp_scratch.alloc(bvp_bytes);
+    if (dfsolve) tune_solve();
 
     // ---- particles: stencils, ghost layers, per-system particle tables
     auto total = [&](const std::vector<KernelHost> &kk, int which) {
@@ -578,8 +666,7 @@ struct BatchEngine : BatchBase {
     }
     DPST_CUDA(launch_zgemm_b<R>(d_segf.as<ZSeg<R>>(), d_tprefix.as<int64_t>(), S, ntiles, nz, Tf.as<R>(), nsm, s,
                                 false));
-    DPST_CUDA(launch_bvp_b<R>(d_sysk.as<SysK<R>>(), S, d_mprefix.as<int64_t>(), K, nz, bvp_scratch.as<double>(),
-                              bvp_grid, s));
+    solve(s);
     DPST_CUDA(launch_zgemm_b<R>(d_segi.as<ZSeg<R>>(), d_tprefix.as<int64_t>(), S, ntiles, nz, Ti.as<R>(), nsm, s,
                                 true));
     for (FftClass &c : classes) {
@@ -659,6 +746,7 @@ struct BatchEngine : BatchBase {
                            &Tf, &Ti, &kvs, &f_mf, &f_bk, &f_ab, &f_g, &st_cell_m, &st_x_m, &st_y_m, &st_z_m,
                            &st_zw_m, &st_cell_d, &st_x_d, &st_y_d, &st_z_d, &st_zw_d, &st_dx_d, &st_dy_d,
                            &st_dz_d, &st_dzw_d, &ghost_buf, &pos64, &bvp_scratch, &fft_work, &sF, &sT, &sV, &sW,
+                           &df_kap, &df_ab, &df_gi, &df_km, &df_km3, &df_dxy,
                            &corrf, &cmode, &znf};
     for (const DevBuf *d : all) bytes += d->bytes;
     o->device_bytes = bytes;

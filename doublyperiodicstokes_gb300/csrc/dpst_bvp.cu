@@ -637,6 +637,15 @@ cudaError_t launch_bvp_k0(const KsArgs &a, R *spec, cudaStream_t s) {
 template cudaError_t launch_bvp_k0<float>(const KsArgs &, float *, cudaStream_t);
 template cudaError_t launch_bvp_k0<double>(const KsArgs &, double *, cudaStream_t);
 
+template <typename R>
+__global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restrict__ sys);
+// the k = 0 mode of every system of a batch (after the double-float solve)
+template <typename R>
+cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s) {
+  k_bvp_k0_b<R><<<S, 2 * K0_ROWS, 0, s>>>(sys);
+  return cudaGetLastError();
+}
+
 // Batched: one CTA per system.
 template <typename R>
 __global__ void __launch_bounds__(2 * K0_ROWS) k_bvp_k0_b(const SysK<R> *__restrict__ sys) {
@@ -885,6 +894,8 @@ cudaError_t launch_bvp_noalloc(const KsArgs &a, R *spec, double2 *corr, int64_t 
 
 size_t noalloc_scratch_bytes() { return NOALLOC_SCRATCH_DOUBLES * sizeof(double); }
 
+template cudaError_t launch_bvp_k0_b<float>(const SysK<float> *, int, cudaStream_t);
+template cudaError_t launch_bvp_k0_b<double>(const SysK<double> *, int, cudaStream_t);
 template cudaError_t launch_bvp_noalloc<float>(const KsArgs &, float *, double2 *, int64_t, cudaStream_t, bool *);
 template cudaError_t launch_bvp_noalloc<double>(const KsArgs &, double *, double2 *, int64_t, cudaStream_t, bool *);
 template cudaError_t bvp_plan<float>(const KsArgs &, int, int64_t *, size_t *);

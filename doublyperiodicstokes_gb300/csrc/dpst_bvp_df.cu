@@ -399,14 +399,15 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
 template <typename R>
 cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, int variant,
                           cudaStream_t s);
+template <typename R>
+cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
 
 // Persistent kernel: CTA b owns the units of 8 wavenumbers [b per_cta,
 // (b+1) per_cta) and its warps take them from a shared-memory counter.
-template <typename R, bool WALLS, typename CFG>
-__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict__ spec, double2 *__restrict__ corr,
-                                                         float2 *__restrict__ cp_scratch, int per_cta) {
-  extern __shared__ float2 dfs_cols[];
-  __shared__ int next_unit;
+// The k-independent tables (every system of a batch shares nz, H and the BC
+// rows) into static shared memory.
+static __device__ __forceinline__ void dfs_tables(const KsArgs &a) {
   const int nz = a.nz, tid = threadIdx.x, NT = blockDim.x;
   const double inv_eta = 1.0 / a.eta;
   for (int t = tid; t < nz; t += NT) {
@@ -432,19 +433,33 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
     dfs_tab[DT_SCAL + 2] = df_f2(df_from_d(a.fe));
     dfs_tab[DT_SCAL + 3] = df_f2(df_from_d(a.se0 * inv_eta));
     dfs_tab[DT_SCAL + 4] = df_f2(df_from_d(a.se1 * inv_eta));
-    next_unit = blockIdx.x * per_cta;
   }
-  __syncthreads();
+}
+
+static __device__ __forceinline__ DfCtx dfs_ctx(float2 *cols, float2 *cp_scratch) {
+  const int tid = threadIdx.x, NT = blockDim.x;
   DfCtx c;
   c.NT = NT;
   c.GT = gridDim.x * NT;
-  c.Xs = dfs_cols + tid;
+  c.Xs = cols + tid;
   c.CPs = cp_scratch + (size_t)blockIdx.x * NT + tid;
   c.CPo = cp_scratch + (size_t)blockIdx.x * NT + (tid ^ 1);
+  return c;
+}
+
+template <typename R, bool WALLS, typename CFG>
+__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict__ spec, double2 *__restrict__ corr,
+                                                         float2 *__restrict__ cp_scratch, int per_cta) {
+  extern __shared__ float2 dfs_cols[];
+  __shared__ int next_unit;
+  dfs_tables(a);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
+  __syncthreads();
+  const DfCtx c = dfs_ctx(dfs_cols, cp_scratch);
   const int nk = (int)a.nk;
   const int units = (nk + 7) / 8;
   const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
-  const int lane = tid & 31;
+  const int lane = threadIdx.x & 31;
   for (;;) {
     int u = 0;
     if (lane == 0) u = atomicAdd(&next_unit, 1);
@@ -454,6 +469,38 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
     const int i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
     dfs_mode<R, WALLS, CFG>(a, spec, corr, i, store, c);
+  }
+}
+
+// Batched systems (or the columns of a multi-RHS Mdot): units of 8
+// consecutive modes of the concatenated systems; a quad finds its system by
+// binary search (all systems share nz, H and the geometry).
+template <typename R, bool WALLS, typename CFG>
+__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df_b(const SysK<R> *__restrict__ sys, int S,
+                                                           const int64_t *__restrict__ mprefix,
+                                                           float2 *__restrict__ cp_scratch, int per_cta) {
+  extern __shared__ float2 dfs_cols[];
+  __shared__ int next_unit;
+  dfs_tables(sys[0].ks);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
+  __syncthreads();
+  const DfCtx c = dfs_ctx(dfs_cols, cp_scratch);
+  const int64_t K = mprefix[S];
+  const int units = (int)((K + 7) / 8);
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
+    const int64_t g_raw = (int64_t)u * 8 + (lane >> 2);
+    const int64_t g = g_raw < K ? g_raw : K - 1;
+    const int s = find_sys(mprefix, S, g);
+    const SysK<R> &y = sys[s];
+    const int i = (int)(g - mprefix[s]);
+    const bool store = (g_raw < K) && (i != 0);  // mode 0 of each system: k_bvp_k0_b
+    dfs_mode<R, WALLS, CFG>(y.ks, y.spec, y.corr, i, store, c);
   }
 }
 
@@ -522,10 +569,19 @@ static cudaError_t df_setup(int nz) {
   return per_sm < 1 ? cudaErrorInvalidConfiguration : cudaSuccess;
 }
 
+template <typename CFG, typename R, bool WALLS>
+static cudaError_t df_setup_b(int nz) {
+  const int nt = bvp_df_threads(nz, CFG::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
+  return cudaFuncSetAttribute(k_bvp_df_b<R, WALLS, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <typename CFG>
 static cudaError_t df_setup_all(int nz) {
   cudaError_t e = df_setup<CFG, float, false>(nz);
   if (e == cudaSuccess) e = df_setup<CFG, float, true>(nz);
+  if (e == cudaSuccess) e = df_setup_b<CFG, float, false>(nz);
+  if (e == cudaSuccess) e = df_setup_b<CFG, float, true>(nz);
   return e;
 }
 
@@ -542,6 +598,8 @@ cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch
   if (err == cudaSuccess) err = df_setup_all<DfV3>(a.nz);
   if (err == cudaSuccess) err = df_setup<DfV1, double, false>(a.nz);
   if (err == cudaSuccess) err = df_setup<DfV1, double, true>(a.nz);
+  if (err == cudaSuccess) err = df_setup_b<DfV1, double, false>(a.nz);
+  if (err == cudaSuccess) err = df_setup_b<DfV1, double, true>(a.nz);
   if (err != cudaSuccess) return err;
   const int nt = bvp_df_threads(a.nz, DF_MAXT);
   int64_t g = nsm;
@@ -551,6 +609,55 @@ cudaError_t bvp_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch
   *grid = g;
   *scratch_bytes = sizeof(float2) * (size_t)((a.nz + 1) / 2) * (size_t)g * nt;
   return cudaSuccess;
+}
+
+// Batched plan: the same for K modes in total with a shared nz (the tables
+// of the first system stand for all).
+cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  KsArgs a = a0;
+  a.nk = K;
+  if (a.nz > DFS_NZMAX) return cudaErrorInvalidValue;
+  if (K >= ((int64_t)1 << 31)) return cudaErrorInvalidValue;
+  a.nk = 1;  // the per-system bound is checked by each system's own plan
+  cudaError_t err = bvp_df_plan(a, nsm, grid, scratch_bytes);
+  if (err != cudaSuccess) return err;
+  const int nt = bvp_df_threads(a.nz, DF_MAXT);
+  int64_t g = nsm;
+  const int64_t units = (K + 7) / 8;
+  const int64_t warps = nt / 32;
+  if (g * warps > units) g = std::max<int64_t>(1, (units + warps - 1) / warps);
+  *grid = g;
+  *scratch_bytes = sizeof(float2) * (size_t)((a.nz + 1) / 2) * (size_t)g * nt;
+  return cudaSuccess;
+}
+
+template <typename CFG, typename R>
+static cudaError_t df_launch_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
+                               float2 *scratch, int64_t grid, cudaStream_t s) {
+  const int nt = bvp_df_threads(nz, CFG::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
+  const int64_t units = (K + 7) / 8;
+  const int per_cta = (int)((units + grid - 1) / grid);
+  if (mode != 0) k_bvp_df_b<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  else k_bvp_df_b<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_bvp_df_b<float>(const SysK<float> *sys, int S, const int64_t *mprefix, int64_t K, int nz,
+                                   int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s) {
+  switch (variant) {
+    case 0: return df_launch_b<DfV0>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+    case 2: return df_launch_b<DfV2>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+    case 3: return df_launch_b<DfV3>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+    default: return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+  }
+}
+template <>
+cudaError_t launch_bvp_df_b<double>(const SysK<double> *sys, int S, const int64_t *mprefix, int64_t K, int nz,
+                                    int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s) {
+  (void)variant;
+  return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
 }
 
 template <typename CFG, typename R>

@@ -63,6 +63,12 @@ int bvp_df_variants();
 template <typename R>
 cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid, int variant,
                           cudaStream_t s);
+cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
+template <typename R>
+cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
 template <typename R>
 void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
                       const double *kvx, const double *kvy, double H, cudaStream_t s);
@@ -814,7 +820,11 @@ struct Engine : EngineBase {
     upload(sysK, sk);
     upload(mprefK, mp);
     size_t bytes = 0;
-    DPST_CUDA(bvp_plan_b<R>(nz, (int64_t)K * nk, nsm, &bvpK_grid, &bytes));
+    if (dfsolve) {
+      DPST_CUDA(bvp_df_plan_b(ks, (int64_t)K * nk, nsm, &bvpK_grid, &bytes));
+    } else {
+      DPST_CUDA(bvp_plan_b<R>(nz, (int64_t)K * nk, nsm, &bvpK_grid, &bytes));
+    }
     bvpK_scratch.alloc(bytes);
     DPST_CUDA(cudaDeviceSynchronize());
     multi_k = K;
@@ -861,8 +871,14 @@ struct Engine : EngineBase {
     ef.scale = 1.0;
     ef.ks = ks;
     for (int k = 0; k < K; ++k) DPST_CUDA(zgemm((R *)(sK + k * scol), Tf.as<R>(), ef, false, s));
-    DPST_CUDA(launch_bvp_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz,
-                              bvpK_scratch.as<double>(), bvpK_grid, s));
+    if (dfsolve) {
+      DPST_CUDA(launch_bvp_df_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz, p.mode,
+                                   bvpK_scratch.as<float2>(), bvpK_grid, df_variant, s));
+      DPST_CUDA(launch_bvp_k0_b<R>(sysK.as<SysK<R>>(), K, s));
+    } else {
+      DPST_CUDA(launch_bvp_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz,
+                                bvpK_scratch.as<double>(), bvpK_grid, s));
+    }
     for (int k = 0; k < K; ++k) {
       EpiArgs eb = ef;
       eb.inverse = 1;

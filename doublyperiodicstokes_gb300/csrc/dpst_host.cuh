@@ -377,8 +377,6 @@ static void validate(const dpst_params *p, int64_t n, bool periodic_ok = false) 
     throw Error(DPST_ERR_INVALID_ARG, "torque_kernel must be DPST_TORQUE_DERIV or DPST_TORQUE_REG");
   if (p->solve_arith != DPST_SOLVE_DEFAULT && p->solve_arith != DPST_SOLVE_FP64 && p->solve_arith != DPST_SOLVE_DF64)
     throw Error(DPST_ERR_INVALID_ARG, "solve_arith must be DPST_SOLVE_DEFAULT, DPST_SOLVE_FP64 or DPST_SOLVE_DF64");
-  if (p->solve_arith == DPST_SOLVE_DF64 && !periodic_ok)
-    throw Error(DPST_ERR_UNSUPPORTED, "solve_arith DPST_SOLVE_DF64 is available through dpst_create only");
   if (p->torque_kernel == DPST_TORQUE_REG && !periodic_ok)
     throw Error(DPST_ERR_UNSUPPORTED, "torque_kernel DPST_TORQUE_REG is available through dpst_create only");
 }

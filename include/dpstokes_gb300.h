@@ -103,9 +103,10 @@ extern "C" {
 #define DPST_SOLVE_DF64 2    /* double-float: pairs of FP32 (about 48 significant bits, FP32's
                                 exponent range) on the FP32 pipe, the same algorithm and factors
                                 as the FP64 solve; the slit channel's wall-correction
-                                coefficients stay FP64.  Open and wall geometries of
-                                dpst_create handles; batched systems, multi-column Mdot and
-                                dpst_mdot_noalloc run the FP64 solve */
+                                coefficients stay FP64.  Open and wall geometries, single
+                                handles, batched systems and multi-column Mdot; the triply
+                                periodic mode has no such solve and dpst_mdot_noalloc runs
+                                the FP64 one */
 
 /* element type of the particle arrays passed to mdot */
 #define DPST_F64 0

@@ -122,3 +122,58 @@ def test_every_solve_variant(variant, monkeypatch):
         Vd, Wd, _, _ = _run(w, "mixed", "df64", X, F, T)
         Vf, Wf, _, _ = _run(w, "mixed", "fp64", X, F, T)
         assert rel_err(Vd, Vf) < 1e-6 and rel_err(Wd, Wf) < 1e-6
+
+
+@pytest.mark.parametrize("dom", ["DPBW", "DP", "DPSC"])
+def test_batched_systems_df64_solve(dom):
+    """The batched double-float solve (one launch over every system's modes):
+    FP64 systems with it against the FP64 solve to 1e-12, and the mixed batch
+    (double-float by default) against single mixed handles to 1e-6."""
+    from doublyperiodicstokes_gb300 import DPStokesBatch
+    ws = W.small_batch(dom, True)
+    Xs, Fs, Ts = zip(*[W.make_inputs(w) for w in ws])
+    cat = lambda a, dt: torch.tensor(np.concatenate(a), dtype=dt, device="cuda")  # noqa: E731
+
+    def batch(precision, solve):
+        prm = [StokesParams(**{**StokesParams.from_workload(w, precision).as_dict(), "solve": solve}) for w in ws]
+        b = DPStokesBatch(prm, [w.N for w in ws])
+        dt = torch.float64 if precision == "fp64" else torch.float32
+        b.set_positions(cat(Xs, torch.float64))
+        V, Wv = b.mdot(cat(Fs, dt), cat(Ts, dt))
+        torch.cuda.synchronize()
+        out = V.double().cpu().numpy(), Wv.double().cpu().numpy()
+        b.close()
+        return out
+
+    V1, W1 = batch("fp64", "fp64")
+    V2, W2 = batch("fp64", "df64")
+    assert rel_err(V2, V1) < 1e-12 and rel_err(W2, W1) < 1e-12
+    Vm, Wm = batch("mixed", "default")
+    Vs = np.concatenate([_run(w, "mixed", "default", X, F, T)[0] for w, X, F, T in zip(ws, Xs, Fs, Ts)])
+    assert rel_err(Vm, Vs) < 1e-6
+
+
+def test_multi_column_df64_solve():
+    """The multi-column Mdot with the batched double-float solve against
+    single-column calls (mixed, 1e-6) and against its FP64-solve form."""
+    w = _wl("c2_dp_n65536@64")
+    X, F, T = W.make_inputs(w)
+    rng = np.random.default_rng(5)
+    K = 3
+    Fk = rng.standard_normal((K, w.N, 3)).astype(np.float32)
+    Tk = rng.standard_normal((K, w.N, 3)).astype(np.float32)
+    res = {}
+    for solve in ("default", "fp64"):
+        prm = StokesParams(**{**StokesParams.from_workload(w, "mixed").as_dict(), "solve": solve})
+        op = DPStokes(prm, w.N)
+        op.set_positions(torch.tensor(X, device=op.device))
+        Vk, Wk = op.mdot_multi(torch.tensor(Fk, device=op.device), torch.tensor(Tk, device=op.device))
+        singles = [op.mdot(torch.tensor(Fk[k], device=op.device), torch.tensor(Tk[k], device=op.device))
+                   for k in range(K)]
+        torch.cuda.synchronize()
+        for k in range(K):
+            assert rel_err(Vk[k].double().cpu().numpy(), singles[k][0].double().cpu().numpy()) < 1e-6
+            assert rel_err(Wk[k].double().cpu().numpy(), singles[k][1].double().cpu().numpy()) < 1e-6
+        res[solve] = Vk.double().cpu().numpy()
+        op.close()
+    assert rel_err(res["default"], res["fp64"]) < 1e-6
