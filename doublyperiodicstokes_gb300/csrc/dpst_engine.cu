@@ -69,6 +69,13 @@ cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, i
                             float2 *scratch, int64_t grid, int variant, cudaStream_t s);
 template <typename R>
 cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
+// x-y transforms of the mixed operator (dpst_fft.cu)
+bool own_fft_supported(int nx, int ny);
+std::vector<float2> fft_twiddles(int n);
+cudaError_t fft_setup(int nx, int ny);
+cudaError_t fft_rows(bool inverse, const float *grid_in, float2 *spec_out, const float2 *spec_in, float *grid_out,
+                     int nx, int64_t rows, const float2 *twx, cudaStream_t s);
+cudaError_t fft_cols(bool inverse, float2 *spec, int ny, int nxh, int64_t planes, const float2 *twy, cudaStream_t s);
 template <typename R>
 void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
                       const double *kvx, const double *kvy, double H, cudaStream_t s);
@@ -143,6 +150,10 @@ struct Engine : EngineBase {
   bool positioned = false;
   cufftHandle plan_f = 0, plan_b = 0;
   bool plans = false;
+  // the library's own x-y transforms (mixed operator, power-of-two nx, ny);
+  // cuFFT otherwise
+  bool ownfft = false;
+  DevBuf twx, twy;
 
   Engine(const dpst_params &prm, int64_t n, int dev) {
     p = prm;
@@ -310,6 +321,16 @@ struct Engine : EngineBase {
     DPST_CUFFT(cufftPlanMany(&plan_b, 2, n2, onem, 1, (int)nk, inem, 1, ny * nx,
                              sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, batch));
     plans = true;
+    {
+      const char *env = getenv("DPSTOKES_GB300_XY_FFT");
+      const bool want_cufft = env && std::string(env) == "cufft";
+      if (sizeof(R) == 4 && !want_cufft && own_fft_supported(nx, ny)) {
+        ownfft = true;
+        upload(twx, fft_twiddles(nx));
+        upload(twy, fft_twiddles(ny));
+        DPST_CUDA(fft_setup(nx, ny));
+      }
+    }
     DPST_CUDA(cudaDeviceSynchronize());
     tune_ztransform();
     tune_solve();
@@ -581,11 +602,7 @@ struct Engine : EngineBase {
   void solve_stage(cudaStream_t s) {
     R *gr = grid.as<R>();
     CR *sp = spec.as<CR>();
-    DPST_CUFFT(cufftSetStream(plan_f, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
-    else
-      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
+    exec_fwd(gr, sp, s);
     mark(2, s);
     EpiArgs ef;
     memset(&ef, 0, sizeof(ef));
@@ -602,11 +619,7 @@ struct Engine : EngineBase {
     epi_corr(eb);
     DPST_CUDA(zgemm((R *)sp, Ti.as<R>(), eb, true, s));
     mark(5, s);
-    DPST_CUFFT(cufftSetStream(plan_b, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
-    else
-      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
+    exec_inv(sp, gr, s);
     mark(6, s);
   }
 
@@ -658,9 +671,8 @@ struct Engine : EngineBase {
       DPST_CUDA(cudaGetLastError());
     }
     mark(1, s);
-    DPST_CUFFT(cufftSetStream(plan_f, s));
-    exec_fwd(gr, sp);
-    if (torque) exec_fwd(gt, st);
+    exec_fwd(gr, sp, s);
+    if (torque) exec_fwd(gt, st, s);
     mark(2, s);
     EpiArgs ef;
     memset(&ef, 0, sizeof(ef));
@@ -704,9 +716,8 @@ struct Engine : EngineBase {
       DPST_CUDA(zgemm((R *)st, Ti.as<R>(), ew, true, s));
     }
     mark(5, s);
-    DPST_CUFFT(cufftSetStream(plan_b, s));
-    exec_inv(sp, gr);
-    exec_inv(st, gt);
+    exec_inv(sp, gr, s);
+    exec_inv(st, gt, s);
     mark(6, s);
     launch_interp<R, RF>(false, gr, N, km.d, g, stm, ghm, V, s, perm.as<int>());
     if (W != nullptr) {
@@ -743,17 +754,37 @@ struct Engine : EngineBase {
     }
   }
 
-  void exec_fwd(R *gr, CR *sp) {
+  // x-y transforms of `planes` grid planes (3 nz for one grid): the library's
+  // row and column passes, or the cuFFT plan given (made for that many planes)
+  void exec_fwd(R *gr, CR *sp, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
+    if (planes == 0) planes = 3 * (int64_t)nz;
+    if (plan == 0) plan = plan_f;
+    if (ownfft) {
+      DPST_CUDA(fft_rows(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr,
+                         nullptr, nx, planes * ny, twx.as<float2>(), s));
+      DPST_CUDA(fft_cols(false, reinterpret_cast<float2 *>(sp), ny, nxh, planes, twy.as<float2>(), s));
+      return;
+    }
+    DPST_CUFFT(cufftSetStream(plan, s));
     if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
+      DPST_CUFFT(cufftExecD2Z(plan, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
     else
-      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
+      DPST_CUFFT(cufftExecR2C(plan, (cufftReal *)gr, (cufftComplex *)sp));
   }
-  void exec_inv(CR *sp, R *gr) {
+  void exec_inv(CR *sp, R *gr, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
+    if (planes == 0) planes = 3 * (int64_t)nz;
+    if (plan == 0) plan = plan_b;
+    if (ownfft) {
+      DPST_CUDA(fft_cols(true, reinterpret_cast<float2 *>(sp), ny, nxh, planes, twy.as<float2>(), s));
+      DPST_CUDA(fft_rows(true, nullptr, nullptr, reinterpret_cast<const float2 *>(sp), reinterpret_cast<float *>(gr),
+                         nx, planes * ny, twx.as<float2>(), s));
+      return;
+    }
+    DPST_CUFFT(cufftSetStream(plan, s));
     if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
+      DPST_CUFFT(cufftExecZ2D(plan, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
     else
-      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)gr));
+      DPST_CUFFT(cufftExecC2R(plan, (cufftComplex *)sp, (cufftReal *)gr));
   }
 
   // interpolate V (and, with W, the angular velocities) from the grid gr with
@@ -860,11 +891,7 @@ struct Engine : EngineBase {
       gd[k] = p.has_torque ? ghosts_of(ghd, kd.d, ghostK + 2, k, K) : ghd;
       spread_into<RF>(F + k * col, torque ? T + k * col : nullptr, gK + k * gcol, gm[k], gd[k], s);
     }
-    DPST_CUFFT(cufftSetStream(planK_f, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecD2Z(planK_f, (cufftDoubleReal *)gK, (cufftDoubleComplex *)sK));
-    else
-      DPST_CUFFT(cufftExecR2C(planK_f, (cufftReal *)gK, (cufftComplex *)sK));
+    exec_fwd(gK, sK, s, 3 * (int64_t)nz * K, planK_f);
     EpiArgs ef;
     memset(&ef, 0, sizeof(ef));
     ef.inverse = 0;
@@ -888,11 +915,7 @@ struct Engine : EngineBase {
       if (eb.corrf) eb.corrf = corrfK.as<float2>() + (size_t)k * 16 * nk;
       DPST_CUDA(zgemm((R *)(sK + k * scol), Ti.as<R>(), eb, true, s));
     }
-    DPST_CUFFT(cufftSetStream(planK_b, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecZ2D(planK_b, (cufftDoubleComplex *)sK, (cufftDoubleReal *)gK));
-    else
-      DPST_CUFFT(cufftExecC2R(planK_b, (cufftComplex *)sK, (cufftReal *)gK));
+    exec_inv(sK, gK, s, 3 * (int64_t)nz * K, planK_b);
     for (int k = 0; k < K; ++k)
       interp_from<RF>(gK + k * gcol, gm[k], gd[k], torque, V + k * col, W ? W + k * col : nullptr, s);
   }
@@ -996,11 +1019,7 @@ struct Engine : EngineBase {
   void adjoint_solve_stage(cudaStream_t s) {
     R *g2 = grid2.as<R>();
     CR *sp = spec.as<CR>();
-    DPST_CUFFT(cufftSetStream(plan_f, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)g2, (cufftDoubleComplex *)sp));
-    else
-      DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)g2, (cufftComplex *)sp));
+    exec_fwd(g2, sp, s);
     if (p.mode != DPST_MODE_NOWALL) DPST_CUDA(launch_corr_adj<R>(ks, (const R *)sp, corr.as<double2>(), s));
     EpiArgs e;
     memset(&e, 0, sizeof(e));
@@ -1010,11 +1029,7 @@ struct Engine : EngineBase {
     DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s));
     DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
     DPST_CUDA(zgemm((R *)sp, TfTn.as<R>(), e, true, s));
-    DPST_CUFFT(cufftSetStream(plan_b, s));
-    if (sizeof(R) == 8)
-      DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)g2));
-    else
-      DPST_CUFFT(cufftExecC2R(plan_b, (cufftComplex *)sp, (cufftReal *)g2));
+    exec_inv(sp, g2, s);
   }
 
   template <typename RF>
@@ -1136,13 +1151,15 @@ struct Engine : EngineBase {
     o->fused_particle_passes = fused ? 1 : 0;
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     o->solve_variant = dfsolve ? df_variant : 0;
+    o->xy_transform = ownfft ? 1 : 0;
+    if (ownfft) o->kernels_per_mdot += 4 * (reg && p.has_torque ? 2 : 1);
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
                            &k0rows, &Tf, &Ti, &fac_m, &fac_i, &fac_d, &fac_a0, &fac_a1, &fac_c0, &fac_c1, &fac_pm, &fac_pb, &fac_pa,
                            &fac_g, &pos64, &flags, &dphzw_buf, &ord_count, &ord_start, &perm,
                            &corrf, &cmode, &znf, &gridT, &specT, &df_mf, &df_bk, &df_ab, &df_gi, &df_km,
-                           &df_dx, &df_dy, &bvp_df_scratch};
+                           &df_dx, &df_dy, &bvp_df_scratch, &twx, &twy};
     for (const DevBuf *d : all) b += d->bytes;
     for (int i = 0; i < 8; ++i) b += st_m[i].bytes + st_d[i].bytes;
     for (int i = 0; i < 2; ++i) b += gh_m[i].bytes + gh_d[i].bytes;
@@ -1344,6 +1361,32 @@ int dpst_get_info(dpst_handle h, dpst_info *out) {
   return guarded([&] {
     if (!h || !out) throw Error(DPST_ERR_INVALID_ARG, "NULL argument");
     h->e->info(out);
+  });
+}
+
+int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int device, void *stream) {
+  return guarded([&] {
+    if (!in || !out || planes < 1) throw Error(DPST_ERR_INVALID_ARG, "NULL argument or no planes");
+    if (!dpst::own_fft_supported(nx, ny))
+      throw Error(DPST_ERR_UNSUPPORTED, "the library's x-y transforms take powers of two, 64 <= nx <= 2048, "
+                                        "32 <= ny <= 1024");
+    DPST_CUDA(cudaSetDevice(device));
+    cudaStream_t s = (cudaStream_t)stream;
+    dpst::DevBuf twx, twy;
+    dpst::upload(twx, dpst::fft_twiddles(nx));
+    dpst::upload(twy, dpst::fft_twiddles(ny));
+    DPST_CUDA(dpst::fft_setup(nx, ny));
+    const int nxh = nx / 2 + 1;
+    if (!inverse) {
+      DPST_CUDA(dpst::fft_rows(false, (const float *)in, (float2 *)out, nullptr, nullptr, nx, planes * ny,
+                               twx.as<float2>(), s));
+      DPST_CUDA(dpst::fft_cols(false, (float2 *)out, ny, nxh, planes, twy.as<float2>(), s));
+    } else {
+      DPST_CUDA(dpst::fft_cols(true, (float2 *)in, ny, nxh, planes, twy.as<float2>(), s));
+      DPST_CUDA(dpst::fft_rows(true, nullptr, nullptr, (const float2 *)in, (float *)out, nx, planes * ny,
+                               twx.as<float2>(), s));
+    }
+    DPST_CUDA(cudaStreamSynchronize(s));
   });
 }
 

@@ -166,6 +166,9 @@ typedef struct dpst_info {
   int solve_variant;               /* DPST_SOLVE_DF64 in the mixed operator: the kernel variant
                                       (prefetch depths, warps per SM) chosen at creation */
   float solve_ms[4];               /* its creation-time timings per variant (0 if not timed) */
+  int xy_transform;                /* x-y transforms: 1 the library's own (mixed operator,
+                                      power-of-two nx and ny; DPSTOKES_GB300_XY_FFT=cufft
+                                      selects cuFFT), 0 cuFFT */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;
@@ -303,6 +306,19 @@ int dpst_batched_get_info(dpst_batch b, dpst_batch_info *out);
 
 /* Sizes and derived constants of a handle. */
 int dpst_get_info(dpst_handle h, dpst_info *out);
+
+/* Diagnostic: the mixed operator's own x-y transform on `planes` FP32 planes,
+ * unnormalised, as the operator applies it (no counterpart in the reference;
+ * it stands for the x-y part of Transform.cpp:215-304).  Forward
+ * (inverse = 0): in = real [planes][ny][nx], out = complex
+ * [planes][ny][nx/2 + 1] (cuFFT's R2C layout).  Inverse: in = the complex
+ * half spectrum, which is overwritten, out = real [planes][ny][nx], the
+ * imaginary parts of the kx = 0 and Nyquist columns after the y pass being
+ * dropped as a complex-to-real transform does.  Powers of two, 64 <= nx <=
+ * 2048, 32 <= ny <= 1024.  Allocates its twiddle tables and synchronises the
+ * stream. */
+int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int device,
+                      void *stream);
 
 /* Last error message of the calling thread ("" if none). */
 const char *dpst_last_error(void);

@@ -1,0 +1,84 @@
+"""The mixed operator's own x-y transforms (dpst_fft.cu) through the C ABI
+diagnostic dpst_xy_transform: the forward transform of random FP32 planes
+against torch's FP64 rfft2 (max error 2e-6 of the largest coefficient), the
+inverse of the forward giving back nx ny times the input (2e-6), and the
+inverse of a non-Hermitian spectrum against torch's irfft2 (which, like the
+operator, keeps the real-part convention of a complex-to-real transform);
+and the mixed operator with its own transforms against the same operator on
+cuFFT's (5e-6: two FP32 computations of the same transform)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from conftest import rel_err  # noqa: E402
+from doublyperiodicstokes_gb300 import DPStokes, StokesParams, _lib, workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+SIZES = [(64, 32), (128, 128), (256, 64), (512, 512), (1024, 256), (2048, 1024), (64, 1024)]
+
+
+def _xy(nx, ny, planes, src, dst, inverse):
+    L = _lib.lib()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(L.dpst_xy_transform(nx, ny, planes, ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(dst.data_ptr()),
+                                   int(inverse), torch.cuda.current_device(), stream))
+
+
+@pytest.mark.parametrize("nx,ny", SIZES)
+def test_forward_and_round_trip(nx, ny):
+    planes = 3
+    g = torch.Generator(device="cuda").manual_seed(nx + ny)
+    x = torch.randn(planes, ny, nx, device="cuda", generator=g, dtype=torch.float32)
+    spec = torch.empty(planes, ny, nx // 2 + 1, dtype=torch.complex64, device="cuda")
+    _xy(nx, ny, planes, x, spec, False)
+    ref = torch.fft.rfft2(x.double())
+    err = float((spec.to(torch.complex128) - ref).abs().max() / ref.abs().max())
+    print("%d x %d forward max err %.2e" % (nx, ny, err))
+    assert err < 2e-6
+    back = torch.empty_like(x)
+    _xy(nx, ny, planes, spec, back, True)
+    err2 = float((back.double() / (nx * ny) - x.double()).abs().max() / x.abs().max())
+    print("%d x %d round trip max err %.2e" % (nx, ny, err2))
+    assert err2 < 2e-6
+
+
+@pytest.mark.parametrize("nx,ny", [(128, 64), (512, 512)])
+def test_inverse_of_general_spectrum(nx, ny):
+    planes = 2
+    g = torch.Generator(device="cuda").manual_seed(7)
+    s = torch.randn(planes, ny, nx // 2 + 1, 2, device="cuda", generator=g)
+    spec = torch.view_as_complex(s.contiguous())
+    ref = torch.fft.irfft2(spec.to(torch.complex128), s=(ny, nx)) * (nx * ny)
+    out = torch.empty(planes, ny, nx, dtype=torch.float32, device="cuda")
+    _xy(nx, ny, planes, spec.clone(), out, True)
+    err = float((out.double() - ref).abs().max() / ref.abs().max())
+    print("%d x %d inverse max err %.2e" % (nx, ny, err))
+    assert err < 2e-6
+
+
+@pytest.mark.parametrize("name", ["s_dp_t", "c2_dp_n65536@128", "c1_dpsc_n16384", "c0_dpbw_n2048"])
+def test_operator_own_fft_matches_cufft(name, monkeypatch):
+    w = W.SMALL_BY_NAME.get(name) or W.by_name(name)
+    X, F, T = W.make_inputs(w)
+    out = {}
+    for which in ("own", "cufft"):
+        if which == "cufft":
+            monkeypatch.setenv("DPSTOKES_GB300_XY_FFT", "cufft")
+        op = DPStokes(StokesParams.from_workload(w, "mixed"), w.N)
+        own = op.info()["xy_transform"]
+        op.set_positions(torch.tensor(X, device=op.device))
+        V, Wv = op.mdot(torch.tensor(F, dtype=torch.float32, device=op.device),
+                        torch.tensor(T, dtype=torch.float32, device=op.device) if T is not None else None)
+        torch.cuda.synchronize()
+        out[which] = (own, V.double().cpu().numpy(), Wv.double().cpu().numpy() if Wv is not None else None)
+        op.close()
+    pow2 = (w.nx & (w.nx - 1)) == 0 and (w.ny & (w.ny - 1)) == 0 and w.nx >= 64 and w.ny >= 32
+    assert out["own"][0] == (1 if pow2 else 0) and out["cufft"][0] == 0
+    ev = rel_err(out["own"][1], out["cufft"][1])
+    print("%s own vs cuFFT V %.2e" % (name, ev))
+    assert ev < 5e-6
+    if T is not None:
+        assert rel_err(out["own"][2], out["cufft"][2]) < 5e-6
