@@ -150,7 +150,13 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
   const int64_t r = live ? row : rows - 1;
   float2 *sm = sbuf[g];
   const float2 *xr = in + r * (L + 1);
-  for (int k = p; k <= L; k += P) sm[k] = __ldg(xr + k);
+  // the kx = 0 and Nyquist terms enter through their real parts (the real
+  // part of the full complex inverse, as a complex-to-real transform takes it)
+  for (int k = p; k <= L; k += P) {
+    float2 xk = __ldg(xr + k);
+    if (k == 0 || k == L) xk.y = 0.0f;
+    sm[k] = xk;
+  }
   __syncwarp();
   float2 v[Q];
 #pragma unroll
