@@ -71,9 +71,15 @@ static __device__ __forceinline__ void dft_reg(float2 (&v)[S]) {
 // rows: real-to-complex (forward) and complex-to-real (inverse) along x
 // ---------------------------------------------------------------------------
 // rows per CTA: 256 threads' worth, at most 48 KB of rows in shared memory
+// Exchange layout of a group's shared memory: value (k1, p) at k1 (P + 1) + p,
+// so that the stage-2 reads (P values of one k1 per thread, threads P + 1
+// apart) fall in different banks; the natural-order pass uses the first
+// L + 1 entries.
 template <int L, int P>
 struct RowCfg {
-  static constexpr int cap = (48 * 1024) / ((L + 1) * 8);
+  static constexpr int Q = L / P;
+  static constexpr int BUF = (Q * (P + 1) > L + 1) ? Q * (P + 1) : L + 1;
+  static constexpr int cap = (48 * 1024) / (BUF * 8);
   static constexpr int RPC = (256 / P) <= cap ? (256 / P) : (cap >= 16 ? 16 : cap >= 8 ? 8 : cap >= 4 ? 4 : 2);
   static constexpr int T = RPC * P;
 };
@@ -83,7 +89,7 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
                                                                   float2 *__restrict__ out, int64_t rows,
                                                                   const float2 *__restrict__ twN) {
   constexpr int Q = L / P, RPC = RowCfg<L, P>::RPC, N = 2 * L, R = Q / P;
-  __shared__ float2 sbuf[RPC][L + 1];
+  __shared__ float2 sbuf[RPC][RowCfg<L, P>::BUF];
   const int g = threadIdx.x / P, p = threadIdx.x % P;
   const int64_t row = (int64_t)blockIdx.x * RPC + g;
   const bool live = row < rows;
@@ -101,14 +107,14 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
     for (int k1 = 1; k1 < Q; ++k1)
       if (p != 0) v[k1] = cmulf(v[k1], __ldg(twN + 2 * p * k1));
 #pragma unroll
-    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * P + p] = v[k1];
+    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k1 = p * R + i;
       float2 u[P];
 #pragma unroll
-      for (int q = 0; q < P; ++q) u[q] = sm[k1 * P + q];
+      for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
       dft_reg<P, DIR>(u);
 #pragma unroll
       for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[k2];
@@ -143,7 +149,7 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
                                                                   float *__restrict__ out, int64_t rows,
                                                                   const float2 *__restrict__ twN) {
   constexpr int Q = L / P, RPC = RowCfg<L, P>::RPC, N = 2 * L, R = Q / P;
-  __shared__ float2 sbuf[RPC][L + 1];
+  __shared__ float2 sbuf[RPC][RowCfg<L, P>::BUF];
   const int g = threadIdx.x / P, p = threadIdx.x % P;
   const int64_t row = (int64_t)blockIdx.x * RPC + g;
   const bool live = row < rows;
@@ -177,14 +183,14 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
     for (int k1 = 1; k1 < Q; ++k1)
       if (p != 0) v[k1] = cmulf(v[k1], conjf2(__ldg(twN + 2 * p * k1)));
 #pragma unroll
-    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * P + p] = v[k1];
+    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
       const int k1 = p * R + i;
       float2 u[P];
 #pragma unroll
-      for (int q = 0; q < P; ++q) u[q] = sm[k1 * P + q];
+      for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
       dft_reg<P, DIR>(u);
 #pragma unroll
       for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[k2];
@@ -207,11 +213,18 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
 // spectrum per CTA, in place
 // ---------------------------------------------------------------------------
 constexpr int FFT_CW = 16;
+// per-column exchange buffer: Q (P + 1) values, its stride odd so that the
+// 16 columns of a warp's access fall in different banks
+template <int L, int P>
+constexpr int col_stride() {
+  return ((L / P) * (P + 1)) | 1;
+}
+
 template <int L, int P, int DIR>
 __global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ data, int64_t planes, int nxh,
                                                          const float2 *__restrict__ twL) {
   constexpr int Q = L / P, R = Q / P;
-  extern __shared__ float2 cbuf[];  // [CW][L]
+  extern __shared__ float2 cbuf[];  // [CW][col_stride]
   const int c = threadIdx.x % FFT_CW, p = threadIdx.x / FFT_CW;
   const int tiles = (nxh + FFT_CW - 1) / FFT_CW;
   const int64_t t = blockIdx.x;
@@ -223,7 +236,7 @@ __global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ da
   float2 v[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) v[q] = base[(int64_t)(p + P * q) * nxh];
-  float2 *sm = cbuf + c * L;
+  float2 *sm = cbuf + c * col_stride<L, P>();
   dft_reg<Q, DIR>(v);
 #pragma unroll
   for (int k1 = 1; k1 < Q; ++k1) {
@@ -234,14 +247,14 @@ __global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ da
     }
   }
 #pragma unroll
-  for (int k1 = 0; k1 < Q; ++k1) sm[k1 * P + p] = v[k1];
+  for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int k1 = p * R + i;
     float2 u[P];
 #pragma unroll
-    for (int q = 0; q < P; ++q) u[q] = sm[k1 * P + q];
+    for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
     dft_reg<P, DIR>(u);
     if (live) {
 #pragma unroll
@@ -283,18 +296,22 @@ cudaError_t fft_setup(int nx, int ny) {
   (void)nx;
   cudaError_t e = upload_tw32();
   if (e != cudaSuccess) return e;
-  auto cols_smem = [](int L) { return (int)(sizeof(float2) * FFT_CW * L); };
+  auto cols_smem = [](int stride) { return (int)(sizeof(float2) * FFT_CW * stride); };
   // the column kernels' shared memory above 48 KB
   switch (ny) {
     case 512:
-      e = cudaFuncSetAttribute(k_fft_cols<512, 16, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem(512));
+      e = cudaFuncSetAttribute(k_fft_cols<512, 16, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               cols_smem(col_stride<512, 16>()));
       if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_fft_cols<512, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem(512));
+        e = cudaFuncSetAttribute(k_fft_cols<512, 16, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 cols_smem(col_stride<512, 16>()));
       break;
     case 1024:
-      e = cudaFuncSetAttribute(k_fft_cols<1024, 32, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem(1024));
+      e = cudaFuncSetAttribute(k_fft_cols<1024, 32, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               cols_smem(col_stride<1024, 32>()));
       if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_fft_cols<1024, 32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, cols_smem(1024));
+        e = cudaFuncSetAttribute(k_fft_cols<1024, 32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 cols_smem(col_stride<1024, 32>()));
       break;
     default:
       break;
@@ -315,7 +332,7 @@ static void rows_c2r(const float2 *in, float *out, int64_t rows, const float2 *t
 template <int L, int P, int DIR>
 static void cols(float2 *data, int64_t planes, int nxh, const float2 *tw, cudaStream_t s) {
   const int tiles = (nxh + FFT_CW - 1) / FFT_CW;
-  const size_t smem = sizeof(float2) * FFT_CW * L;
+  const size_t smem = sizeof(float2) * FFT_CW * col_stride<L, P>();
   k_fft_cols<L, P, DIR><<<(unsigned)(planes * tiles), FFT_CW * P, smem, s>>>(data, planes, nxh, tw);
 }
 
