@@ -39,32 +39,40 @@ static __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
 static __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
 // In place DFT of S values (S a power of two dividing 32): V_k = sum_j v_j
-// w^{jk}, w = e^{-2 pi i / S} (DIR = -1) or its conjugate (DIR = +1).
-// Recursive radix-2 decimation in time, written so that every array index is
-// a compile-time constant (the values stay in registers).
+// w^{jk}, w = e^{-2 pi i / S} (DIR = -1) or its conjugate (DIR = +1), left
+// in bit-reversed order: v[j] = V[brev(j)].  Radix-2 decimation in
+// frequency, in place (S values in registers, no copies); every index is a
+// compile-time constant after unrolling.
 template <int S, int DIR>
 static __device__ __forceinline__ void dft_reg(float2 (&v)[S]) {
-  if constexpr (S > 1) {
-    float2 e[S / 2], o[S / 2];
 #pragma unroll
-    for (int i = 0; i < S / 2; ++i) {
-      e[i] = v[2 * i];
-      o[i] = v[2 * i + 1];
-    }
-    dft_reg<S / 2, DIR>(e);
-    dft_reg<S / 2, DIR>(o);
+  for (int len = S; len >= 2; len >>= 1) {
 #pragma unroll
-    for (int k = 0; k < S / 2; ++k) {
-      float2 t = o[k];
-      if (k != 0) {
-        float2 w = c_tw32[k * (32 / S)];
-        if (DIR > 0) w = conjf2(w);
-        t = cmulf(t, w);
+    for (int i = 0; i < S; i += len) {
+#pragma unroll
+      for (int k = 0; k < len / 2; ++k) {
+        const float2 a = v[i + k], b = v[i + k + len / 2];
+        v[i + k] = make_float2(a.x + b.x, a.y + b.y);
+        const float2 d = make_float2(a.x - b.x, a.y - b.y);
+        if (k == 0) {
+          v[i + k + len / 2] = d;
+        } else {
+          float2 w = c_tw32[k * (32 / len)];
+          if (DIR > 0) w = conjf2(w);
+          v[i + k + len / 2] = cmulf(d, w);
+        }
       }
-      v[k] = make_float2(e[k].x + t.x, e[k].y + t.y);
-      v[k + S / 2] = make_float2(e[k].x - t.x, e[k].y - t.y);
     }
   }
+}
+
+// bit reversal of j within log2(S) bits
+template <int S>
+static __host__ __device__ constexpr int brev(int j) {
+  int r = 0;
+  for (int m = S >> 1, b = 1; m > 0; m >>= 1, b <<= 1)
+    if (j & m) r |= b;
+  return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -104,10 +112,11 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
     constexpr int DIR = -1;
     dft_reg<Q, DIR>(v);
 #pragma unroll
-    for (int k1 = 1; k1 < Q; ++k1)
-      if (p != 0) v[k1] = cmulf(v[k1], __ldg(twN + 2 * p * k1));
-#pragma unroll
-    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
+    for (int k1 = 0; k1 < Q; ++k1) {
+      float2 y = v[brev<Q>(k1)];
+      if (k1 != 0 && p != 0) y = cmulf(y, __ldg(twN + 2 * p * k1));
+      sm[k1 * (P + 1) + p] = y;
+    }
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
       for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
       dft_reg<P, DIR>(u);
 #pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[k2];
+      for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[brev<P>(k2)];
     }
     __syncwarp();
   }
@@ -158,10 +167,17 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
   const float2 *xr = in + r * (L + 1);
   // the kx = 0 and Nyquist terms enter through their real parts (the real
   // part of the full complex inverse, as a complex-to-real transform takes it)
-  for (int k = p; k <= L; k += P) {
-    float2 xk = __ldg(xr + k);
-    if (k == 0 || k == L) xk.y = 0.0f;
-    sm[k] = xk;
+  {
+    float2 t[Q];
+#pragma unroll
+    for (int m = 0; m < Q; ++m) t[m] = __ldg(xr + p + P * m);
+    const float2 last = __ldg(xr + L);
+#pragma unroll
+    for (int m = 0; m < Q; ++m) sm[p + P * m] = t[m];
+    if (p == 0) {
+      sm[0].y = 0.0f;
+      sm[L] = make_float2(last.x, 0.0f);
+    }
   }
   __syncwarp();
   float2 v[Q];
@@ -180,10 +196,11 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
     constexpr int DIR = 1;
     dft_reg<Q, DIR>(v);
 #pragma unroll
-    for (int k1 = 1; k1 < Q; ++k1)
-      if (p != 0) v[k1] = cmulf(v[k1], conjf2(__ldg(twN + 2 * p * k1)));
-#pragma unroll
-    for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
+    for (int k1 = 0; k1 < Q; ++k1) {
+      float2 y = v[brev<Q>(k1)];
+      if (k1 != 0 && p != 0) y = cmulf(y, conjf2(__ldg(twN + 2 * p * k1)));
+      sm[k1 * (P + 1) + p] = y;
+    }
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < R; ++i) {
@@ -193,7 +210,7 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
       for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
       dft_reg<P, DIR>(u);
 #pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[k2];
+      for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[brev<P>(k2)];
     }
     __syncwarp();
   }
@@ -221,7 +238,7 @@ constexpr int col_stride() {
 }
 
 template <int L, int P, int DIR>
-__global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ data, int64_t planes, int nxh,
+__global__ void __launch_bounds__(FFT_CW * P, (FFT_CW * P) <= 256 ? 3 : 1) k_fft_cols(float2 *__restrict__ data, int64_t planes, int nxh,
                                                          const float2 *__restrict__ twL) {
   constexpr int Q = L / P, R = Q / P;
   extern __shared__ float2 cbuf[];  // [CW][col_stride]
@@ -239,15 +256,15 @@ __global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ da
   float2 *sm = cbuf + c * col_stride<L, P>();
   dft_reg<Q, DIR>(v);
 #pragma unroll
-  for (int k1 = 1; k1 < Q; ++k1) {
-    if (p != 0) {
+  for (int k1 = 0; k1 < Q; ++k1) {
+    float2 y = v[brev<Q>(k1)];
+    if (k1 != 0 && p != 0) {
       float2 w = __ldg(twL + p * k1);
       if (DIR > 0) w = conjf2(w);
-      v[k1] = cmulf(v[k1], w);
+      y = cmulf(y, w);
     }
+    sm[k1 * (P + 1) + p] = y;
   }
-#pragma unroll
-  for (int k1 = 0; k1 < Q; ++k1) sm[k1 * (P + 1) + p] = v[k1];
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < R; ++i) {
@@ -258,7 +275,7 @@ __global__ void __launch_bounds__(FFT_CW * P) k_fft_cols(float2 *__restrict__ da
     dft_reg<P, DIR>(u);
     if (live) {
 #pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) base[(int64_t)(k1 + Q * k2) * nxh] = u[k2];
+      for (int k2 = 0; k2 < P; ++k2) base[(int64_t)(k1 + Q * k2) * nxh] = u[brev<P>(k2)];
     }
   }
 }
