@@ -639,6 +639,8 @@ def main():
     ap.add_argument("--skip-backward", action="store_true")
     ap.add_argument("--only-backward", action="store_true",
                     help="time only the backward pass of the differentiation configuration")
+    ap.add_argument("--only-backward-mixed", action="store_true",
+                    help="time only the mixed operator's backward pass of the differentiation configuration")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--only-batched", action="store_true",
                     help="time only the batched configuration (256 systems)")
@@ -671,6 +673,11 @@ def main():
         import torch
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
         print(json.dumps({"batched": run_batched(args, dev)}), flush=True)
+        return
+    if args.only_backward_mixed:
+        import torch
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"backward_mixed": run_backward(args, dev, "mixed")}), flush=True)
         return
     if args.only_backward:
         import torch
