@@ -507,6 +507,15 @@ cudaError_t launch_corr_adj(const KsArgs &a, const R *spec, double2 *cadj, cudaS
   return cudaGetLastError();
 }
 
+// the k = 0 mode alone (after the double-float adjoint of the other modes)
+template <typename R>
+cudaError_t launch_adj_k0(const KsArgs &a, R *spec, cudaStream_t s) {
+  k_bvp_adj_k0<R><<<1, 2 * ADJ_K0_ROWS, 0, s>>>(a, spec);
+  return cudaGetLastError();
+}
+template cudaError_t launch_adj_k0<float>(const KsArgs &, float *, cudaStream_t);
+template cudaError_t launch_adj_k0<double>(const KsArgs &, double *, cudaStream_t);
+
 template cudaError_t adj_plan<float>(const KsArgs &, int, int64_t *, size_t *);
 template cudaError_t adj_plan<double>(const KsArgs &, int, int64_t *, size_t *);
 template cudaError_t launch_adj_solve<float>(const KsArgs &, float *, const double2 *, double *, int64_t,

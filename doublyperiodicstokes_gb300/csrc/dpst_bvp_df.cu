@@ -49,8 +49,8 @@ constexpr int DFS_NZMAX = 128;
 enum DfTab { DT_S0, DT_SM2, DT_SP2, DT_FM1, DT_FP1, DT_S0E, DT_SM2E, DT_SP2E, DT_BR2, DT_BRA, DT_DH };
 // k-independent tables as double-floats, at fixed offsets (the first BC row
 // as C0 = H^2 K BR2 + BRA); then the scalars se0, se1, fe, se0 / eta,
-// se1 / eta
-__shared__ float2 dfs_tab[DT_DH * DFS_NZMAX + DFS_NZMAX + 1 + 5];
+// se1 / eta, 1 / eta
+__shared__ float2 dfs_tab[DT_DH * DFS_NZMAX + DFS_NZMAX + 1 + 6];
 #define DTAB(t, j) df_lds(dfs_tab[(t) * DFS_NZMAX + (j)])
 constexpr int DT_SCAL = DT_DH * DFS_NZMAX + DFS_NZMAX + 1;
 
@@ -93,6 +93,9 @@ static __device__ __forceinline__ void rows_down(int n, Ld &&ld, Body &&body) {
 // rounded to double-floats.
 static __device__ __forceinline__ float df_v(float x) { return x; }
 static __device__ __forceinline__ df64 df_v(double x) { return df_from_d(x); }
+// the same as double-float values
+static __device__ __forceinline__ df64 df_w(float x) { return df_from_f(x); }
+static __device__ __forceinline__ df64 df_w(double x) { return df_from_d(x); }
 
 template <typename R>
 struct DfRhsP {  // pressure right-hand side inputs of one row
@@ -433,6 +436,7 @@ static __device__ __forceinline__ void dfs_tables(const KsArgs &a) {
     dfs_tab[DT_SCAL + 2] = df_f2(df_from_d(a.fe));
     dfs_tab[DT_SCAL + 3] = df_f2(df_from_d(a.se0 * inv_eta));
     dfs_tab[DT_SCAL + 4] = df_f2(df_from_d(a.se1 * inv_eta));
+    dfs_tab[DT_SCAL + 5] = df_f2(df_from_d(inv_eta));
   }
 }
 
@@ -501,6 +505,232 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df_b(const SysK<R> *__rest
     const int i = (int)(g - mprefix[s]);
     const bool store = (g_raw < K) && (i != 0);  // mode 0 of each system: k_bvp_k0_b
     dfs_mode<R, WALLS, CFG>(y.ks, y.spec, y.corr, i, store, c);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the solve (the backward pass's N_i^H, as k_bvp_adj_pairs in
+// dpst_adjoint.cu computes it in FP64) in double-float arithmetic, with the
+// same lanes, columns and K^2-scaled sweeps as the forward kernel.  Per
+// velocity component (x, y, z): the transposed S window over the adjoint
+// velocity (wall terms W^T included), the border adjoints gb = S_border^T v -
+// (A^{-1}B)^T xbar, r = Ginv^T gb, then A^{-T} (xbar + C^T r) as
+//   U^T: z~_j = kappa_j (X_j + sp2_{j-2} z~_{j-2})   (increasing j)
+//   L^T: x~_j = z~_j + kappa_j sm2_{j+2} x~_{j+2}    (decreasing j)
+// (z~, x~ the K^2-scaled unknowns); the adjoint right-hand sides feed the
+// pressure's (i D_c cp -> the other part's rows) and the outputs -rhs/eta.
+// Then the pressure: S^T cp_bar + F^T dp_bar (the z-derivative band from the
+// other parity's rows), its border adjoints, A^{-T}, and the prhs adjoint
+// into f0, f1 (-i Dx, -i Dy of the other part) and f2 (the transposed
+// Chebyshev derivative recurrence, summed over the other parity's rows).
+// Scratch: cp_bar and dp_bar, [row][lane of the grid] each.
+// ---------------------------------------------------------------------------
+template <typename R, typename CFG>
+static __device__ __forceinline__ void dfs_adj_mode(const KsArgs &a, R *__restrict__ spec,
+                                                    const double2 *__restrict__ cadj, int i, bool store,
+                                                    const DfCtx &c, float2 *__restrict__ DPs,
+                                                    const float2 *__restrict__ DPp) {
+  const int nz = a.nz;
+  const int nk = (int)a.nk;
+  const int lane = threadIdx.x & 31;
+  const int part = lane & 1, par = (lane >> 1) & 1;
+  const int nzp = (nz + 1 - par) >> 1;
+  float2 *__restrict__ Xs = c.Xs;
+  const int NT = c.NT, GT = c.GT;
+#define XS(t) Xs[(t) * NT]
+#define XO(t) Xs[(t) * NT + (threadIdx.x ^ 1) - threadIdx.x]  // the other part, same row
+#define XP(t) Xs[(t) * NT + (threadIdx.x ^ 2) - threadIdx.x]  // the other parity
+  const int rs = 2 * nk;
+  R *__restrict__ own = spec + 2 * i + part;
+  const int ix = i % a.nxh, iy = i / a.nxh;
+  const df64 dxs = part ? df_ld(a.dx2 + ix) : df_neg(df_ld(a.dx2 + ix));  // sp Dx
+  const df64 dys = part ? df_ld(a.dy2 + iy) : df_neg(df_ld(a.dy2 + iy));
+  const float2 *__restrict__ kap0 = a.kap2 + i;
+  const float2 *__restrict__ ab0 = a.ab2 + i;
+  const float4 k2 = __ldg(a.km2 + i), k3 = __ldg(a.km3 + i);
+  const df64 iK2 = df_make(k2.z, k2.w), h2k = df_make(k3.x, k3.y), hK = df_make(k3.z, k3.w);
+  const df64 inv_eta = df_lds(dfs_tab[DT_SCAL + 5]);
+  const float sg = par ? 1.0f : -1.0f;    // C1 = sg C0 on this chain
+  const float psg = par ? -1.0f : 1.0f;   // (-1)^j on this chain
+  // r = Ginv^T gb
+  auto schur_t = [&](df64 gb0, df64 gb1, df64 &r0, df64 &r1) {
+    r0 = df_fma(df_ld(a.gi2 + i), gb0, df_mul(df_ld(a.gi2 + nk + i), gb1));
+    r1 = df_fma(df_ld(a.gi2 + 2 * nk + i), gb0, df_mul(df_ld(a.gi2 + 3 * nk + i), gb1));
+  };
+  // A^{-T} (XS + C^T r) in place, leaving rhs_bar = x~ / K^2 in XS
+  auto sweeps_t = [&](df64 rho) {
+    const df64 rh = df_mul(h2k, rho);
+    df64 zm = df_zero();
+    rows_up<CFG::PF_F, float2>(
+        nzp, [&](int t) { return __ldg(kap0 + (par + 2 * t) * nk); },
+        [&](int t, const float2 &k) {
+          const int j = par + 2 * t;
+          df64 X = df_fma(DTAB(DT_BR2, j), rh, df_lds(XS(t)));
+          X = df_fma(DTAB(DT_BRA, j), rho, X);
+          if (t > 0) X = df_fma(DTAB(DT_SP2, j - 2), zm, X);
+          const df64 z = df_mul(df_make(k.x, k.y), X);
+          XS(t) = df_f2(z);
+          zm = z;
+        });
+    df64 xn = df_zero();
+    rows_down<CFG::PF_B, float2>(
+        nzp, [&](int t) { return __ldg(kap0 + (par + 2 * t) * nk); },
+        [&](int t, const float2 &k) {
+          const int j = par + 2 * t;
+          df64 x = df_lds(XS(t));
+          if (t + 1 < nzp) x = df_fma(df_make(k.x, k.y), df_mul(DTAB(DT_SM2, j + 2), xn), x);
+          xn = x;
+          XS(t) = df_f2(df_mul(x, iK2));
+        });
+  };
+  // transposed window over this chain's rows: XS(t) = (S^T v)_j [+ (F^T d)_j],
+  // returning the border dot e = sum (A^{-1}B)_j xbar_j of this chain
+  auto window_t = [&](auto &&vat, auto &&dat, bool with_d) -> df64 {
+    df_acc e = acc_zero();
+    df64 vm = df_zero(), v0 = vat(0);
+    for (int t = 0; t < nzp; ++t) {
+      const int j = par + 2 * t;
+      const df64 vp = (t + 1 < nzp) ? vat(t + 1) : df_zero();
+      df64 x = df_mul(DTAB(DT_S0, j), v0);
+      if (j + 2 < nz) x = df_fma(DTAB(DT_SM2, j + 2), vp, x);
+      if (j >= 2) x = df_fma(DTAB(DT_SP2, j - 2), vm, x);
+      if (with_d) {
+        if (j + 1 < nz) x = df_fma(DTAB(DT_FM1, j + 1), dat(j + 1), x);
+        if (j >= 1) x = df_fma(DTAB(DT_FP1, j - 1), dat(j - 1), x);
+      }
+      XS(t) = df_f2(x);
+      acc_fma(e, df_ld(ab0 + j * nk), x);
+      vm = v0;
+      v0 = vp;
+    }
+    return acc_val(e);
+  };
+  double wbb[3] = {0, 0, 0}, wtb[3] = {0, 0, 0};
+  if (a.mode != 0 && i != 0) {
+    const double *cd = reinterpret_cast<const double *>(cadj + (size_t)i * 6);
+    for (int q = 0; q < 3; ++q) {
+      wbb[q] = cd[2 * q + part];
+      if (a.mode == 2) wtb[q] = cd[2 * (3 + q) + part];
+    }
+  }
+  const df64 se0 = df_lds(dfs_tab[DT_SCAL]), se1 = df_lds(dfs_tab[DT_SCAL + 1]), fe = df_lds(dfs_tab[DT_SCAL + 2]);
+  df64 bcbar[6];
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    R *us = own + comp * nz * rs;
+    const df64 wterm = df_from_d((par ? -wbb[comp] : wbb[comp]) + wtb[comp]);
+    auto vat = [&](int t) { return df_sub(df_w(us[(par + 2 * t) * rs]), wterm); };
+    const df64 e_own = window_t(vat, [&](int) { return df_zero(); }, false);
+    const df64 e_oth = df_shfl_xor(e_own, 2);
+    const df64 vf = vat(0), vfo = df_shfl_xor(vf, 2);
+    const df64 e0 = par ? e_oth : e_own, e1 = par ? e_own : e_oth;
+    const df64 v0r = par ? vfo : vf, v1r = par ? vf : vfo;
+    df64 r0, r1;
+    schur_t(df_fnma(df_from_f(1.0f), e0, df_mul(se0, v0r)), df_fnma(df_from_f(1.0f), e1, df_mul(se1, v1r)), r0, r1);
+    bcbar[2 * comp] = df_neg(r0);
+    bcbar[2 * comp + 1] = df_neg(r1);
+    sweeps_t(df_fma(df_from_f(sg), r1, r0));
+    __syncwarp();  // the other part's rhs_bar is read below
+    if (comp == 2) {
+      for (int t = 0; t < nzp; ++t) {
+        const df64 tj = df_mul(inv_eta, df_lds(XS(t)));
+        DPs[t * GT] = df_f2(tj);
+        if (store) df_out(us + (par + 2 * t) * rs, df_neg(tj));
+      }
+    } else {
+      const df64 coef = df_neg(df_mul(comp == 0 ? dxs : dys, inv_eta));  // -sp D_c / eta
+      for (int t = 0; t < nzp; ++t) {
+        const df64 add = df_mul(coef, df_lds(XO(t)));
+        float2 *cw = c.CPs + t * GT;
+        *cw = df_f2(comp == 0 ? add : df_add(df_lds(*cw), add));
+        if (store) df_out(us + (par + 2 * t) * rs, df_neg(df_mul(inv_eta, df_lds(XS(t)))));
+      }
+    }
+    __syncwarp();  // XS is rewritten by the next window; DP / CP reads below
+  }
+  // bc adjoints -> ssum / asum adjoints (DPTools.cpp:218-234): bc0 = -(i Dx
+  // ssum)/fac, bc1 = (i Dx asum)/fac, bc2, bc3 likewise with Dy, bc4 =
+  // ssum/fac1, bc5 = asum/fac1, fac1 = 2 eta, fac = fac1 K
+  const df64 ifac = df_mul(hK, inv_eta), ifac1 = df_scale2(inv_eta, 0.5f);
+  const df64 b0o = df_shfl_xor(bcbar[0], 1), b1o = df_shfl_xor(bcbar[1], 1);
+  const df64 b2o = df_shfl_xor(bcbar[2], 1), b3o = df_shfl_xor(bcbar[3], 1);
+  const df64 ssb = df_fma(df_mul(dxs, ifac), b0o, df_fma(df_mul(dys, ifac), b2o, df_mul(ifac1, bcbar[4])));
+  const df64 asb = df_fma(df_neg(df_mul(dxs, ifac)), b1o,
+                          df_fma(df_neg(df_mul(dys, ifac)), b3o, df_mul(ifac1, bcbar[5])));
+  const df64 cadd = df_fma(df_from_f(psg), asb, ssb);  // ssb + (-1)^j asb on this chain
+  // pressure: S^T cp_bar + F^T dp_bar, dp_bar of the other parity at rows j +- 1
+  {
+    const int nzpp = (nz + 1 - (par ^ 1)) >> 1;  // rows of the other parity
+    auto vat = [&](int t) { return df_add(df_lds(c.CPs[t * GT]), cadd); };
+    auto dat = [&](int jj) {
+      const int tp = (jj - (par ^ 1)) >> 1;  // row jj (other parity) in the other chain
+      return (tp >= 0 && tp < nzpp) ? df_lds(DPp[tp * GT]) : df_zero();
+    };
+    const df64 e_own = window_t(vat, dat, true);
+    const df64 e_oth = df_shfl_xor(e_own, 2);
+    const df64 vf = vat(0), vfo = df_shfl_xor(vf, 2);
+    const df64 e0 = par ? e_oth : e_own, e1 = par ? e_own : e_oth;
+    const df64 v0r = par ? vfo : vf, v1r = par ? vf : vfo;
+    const df64 d0 = par ? df_lds(DPp[0]) : df_lds(DPs[0]);
+    df64 r0, r1;
+    schur_t(df_fnma(df_from_f(1.0f), e0, df_mul(se0, v0r)),
+            df_fnma(df_from_f(1.0f), e1, df_fma(fe, d0, df_mul(se1, v1r))), r0, r1);
+    sweeps_t(df_fma(df_from_f(sg), r1, r0));  // XS = prhs_bar
+  }
+  __syncwarp();
+  // prhs adjoint -> f0 += -i Dx prhs_bar, f1 += -i Dy prhs_bar (the other
+  // part's rows), f2 += D^T of the derivative (DPTools.cpp:134-174): f2_j +=
+  // (2 j / H) e_j, e_j the sum of prhs_bar over the other parity's rows below
+  // j, the row-0 term halved
+  if (store) {
+    const df64 cx = df_neg(dxs), cy = df_neg(dys);
+    R *f0 = own, *f1 = own + nz * rs, *f2 = own + 2 * nz * rs;
+    df_acc e = acc_zero();
+    // parity 1 rows start with the other chain's row 0 (halved); parity 0
+    // rows sum the other chain's rows 1, 3, ... below them
+    for (int t = 0; t < nzp; ++t) {
+      const int j = par + 2 * t;
+      const df64 po = df_lds(XO(t));
+      df_out(f0 + j * rs, df_fma(cx, po, df_w(f0[j * rs])));
+      df_out(f1 + j * rs, df_fma(cy, po, df_w(f1[j * rs])));
+      if (par == 1) acc_add(e, t == 0 ? df_scale2(df_lds(XP(0)), 0.5f) : df_lds(XP(t)));
+      if (j >= 1) df_out(f2 + j * rs, df_fma(DTAB(DT_DH, j), acc_val(e), df_w(f2[j * rs])));
+      if (par == 0) acc_add(e, df_lds(XP(t)));
+    }
+  }
+  __syncwarp();
+#undef XS
+#undef XO
+#undef XP
+}
+
+template <typename R, typename CFG>
+__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_adj_df(KsArgs a, R *__restrict__ spec,
+                                                             const double2 *__restrict__ cadj,
+                                                             float2 *__restrict__ scratch, int per_cta) {
+  extern __shared__ float2 dfs_cols[];
+  __shared__ int next_unit;
+  dfs_tables(a);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
+  __syncthreads();
+  const DfCtx c = dfs_ctx(dfs_cols, scratch);
+  // dp_bar after cp_bar: [rows][lanes of the grid] each
+  float2 *dp_base = scratch + (size_t)((a.nz + 1) / 2) * c.GT;
+  float2 *DPs = dp_base + (size_t)blockIdx.x * c.NT + threadIdx.x;
+  const float2 *DPp = dp_base + (size_t)blockIdx.x * c.NT + (threadIdx.x ^ 2);
+  const int nk = (int)a.nk;
+  const int units = (nk + 7) / 8;
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
+    const int i_raw = u * 8 + (lane >> 2);
+    const int i = i_raw < nk ? i_raw : nk - 1;
+    const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_adj_k0
+    dfs_adj_mode<R, CFG>(a, spec, cadj, i, store, c, DPs, DPp);
   }
 }
 
@@ -659,6 +889,34 @@ cudaError_t launch_bvp_df_b<double>(const SysK<double> *sys, int S, const int64_
   (void)variant;
   return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
 }
+
+// The adjoint: the forward plan's grid, twice its scratch (cp_bar, dp_bar).
+cudaError_t bvp_adj_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
+  cudaError_t err = bvp_df_plan(a, nsm, grid, scratch_bytes);
+  if (err != cudaSuccess) return err;
+  const int nt = bvp_df_threads(a.nz, DfV1::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
+  err = cudaFuncSetAttribute(k_bvp_adj_df<float, DfV1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  err = cudaFuncSetAttribute(k_bvp_adj_df<double, DfV1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err != cudaSuccess) return err;
+  *scratch_bytes *= 2;
+  return cudaSuccess;
+}
+
+template <typename R>
+cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+                          cudaStream_t s) {
+  const int nt = bvp_df_threads(a.nz, DfV1::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
+  const int64_t units = (a.nk + 7) / 8;
+  const int per_cta = (int)((units + grid - 1) / grid);
+  k_bvp_adj_df<R, DfV1><<<(unsigned)grid, nt, smem, s>>>(a, spec, cadj, scratch, per_cta);
+  return cudaGetLastError();
+}
+template cudaError_t launch_adj_df<float>(const KsArgs &, float *, const double2 *, float2 *, int64_t, cudaStream_t);
+template cudaError_t launch_adj_df<double>(const KsArgs &, double *, const double2 *, float2 *, int64_t,
+                                           cudaStream_t);
 
 template <typename CFG, typename R>
 static cudaError_t df_launch(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid,

@@ -69,6 +69,13 @@ cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, i
                             float2 *scratch, int64_t grid, int variant, cudaStream_t s);
 template <typename R>
 cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
+// double-float adjoint solve (dpst_bvp_df.cu) and the FP64 k = 0 adjoint
+cudaError_t bvp_adj_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
+template <typename R>
+cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+                          cudaStream_t s);
+template <typename R>
+cudaError_t launch_adj_k0(const KsArgs &a, R *spec, cudaStream_t s);
 // x-y transforms of the mixed operator (dpst_fft.cu)
 bool own_fft_supported(int nx, int ny);
 std::vector<float2> fft_twiddles(int n);
@@ -958,7 +965,11 @@ struct Engine : EngineBase {
     if (!grad_ready) {
       grid2.alloc(grid.bytes);
       size_t bytes = 0;
-      DPST_CUDA(adj_plan<R>(ks, nsm, &adj_grid, &bytes));
+      if (dfsolve) {
+        DPST_CUDA(bvp_adj_df_plan(ks, nsm, &adj_grid, &bytes));
+      } else {
+        DPST_CUDA(adj_plan<R>(ks, nsm, &adj_grid, &bytes));
+      }
       adj_scratch.alloc(bytes);
       std::vector<double> tf, ti;
       dct_matrices(nz, tf, ti);
@@ -1027,7 +1038,12 @@ struct Engine : EngineBase {
     e.scale = 1.0;
     e.ks = ks;
     DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s));
-    DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
+    if (dfsolve) {
+      DPST_CUDA(launch_adj_df<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<float2>(), adj_grid, s));
+      DPST_CUDA(launch_adj_k0<R>(ks, (R *)sp, s));
+    } else {
+      DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));
+    }
     DPST_CUDA(zgemm((R *)sp, TfTn.as<R>(), e, true, s));
     exec_inv(sp, g2, s);
   }

@@ -180,3 +180,40 @@ def test_multi_column_df64_solve():
         res[solve] = Vk.double().cpu().numpy()
         op.close()
     assert rel_err(res["default"], res["fp64"]) < 5e-6
+
+
+@pytest.mark.parametrize("name", ["s_dpbw_t", "s_dp_t", "s_dpsc_t", "s_dpbw_t_odd", "s_dpsc_f_odd", "e_dp_t_shift",
+                                  "c2_dp_n65536@64"])
+def test_adjoint_df64_solve(name):
+    """The backward pass with the double-float adjoint solve (FP64 I/O)
+    against the FP64 adjoint (dl/dF, dl/dT, dl/dX to 1e-11), and its
+    transpose identity <gV, V> + <gW, W> = <dl/dF, F> + <dl/dT, T>."""
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    rng = np.random.default_rng(11)
+    gV = rng.standard_normal(F.shape)
+    gW = rng.standard_normal(F.shape) if T is not None else None
+    out = {}
+    for solve in ("fp64", "df64"):
+        prm = StokesParams(**{**StokesParams.from_workload(w, "fp64").as_dict(), "solve": solve})
+        op = DPStokes(prm, w.N)
+        d = op.device
+        op.set_positions(torch.tensor(X, device=d))
+        Ft = torch.tensor(F, device=d)
+        Tt = torch.tensor(T, device=d) if T is not None else None
+        V, Wv = op.mdot(Ft, Tt)
+        gF, gT, gX = op.mdot_backward(Ft, Tt, torch.tensor(gV, device=d),
+                                      torch.tensor(gW, device=d) if gW is not None else None,
+                                      need_F=True, need_T=T is not None, need_X=True)
+        torch.cuda.synchronize()
+        out[solve] = [None if a is None else a.cpu().numpy() for a in (V, Wv, gF, gT, gX)]
+        op.close()
+    V, Wv, gF, gT, gX = out["df64"]
+    for a, b in zip(out["df64"][2:], out["fp64"][2:]):
+        if a is not None:
+            assert rel_err(a, b) < 1e-11
+    lhs = np.sum(gV * V) + (np.sum(gW * Wv) if gW is not None else 0.0)
+    rhs = np.sum(gF * F) + (np.sum(gT * T) if T is not None else 0.0)
+    scale = np.sqrt(np.sum(gV * gV) * np.sum(V * V))
+    print("%s transpose identity %.2e" % (name, abs(lhs - rhs) / scale))
+    assert abs(lhs - rhs) < 1e-12 * scale
