@@ -105,11 +105,13 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def algorithmic_bytes(stage, w, prec):
+def algorithmic_bytes(stage, w, prec, arith=None):
     """Bytes a stage must move at minimum for one Mdot: the grid (3 nx ny nz
     values) and / or the spectrum (3 nz ny (nx/2+1) complex values) once in
     and once out, the per-wavenumber factors of the solve, and the particle
-    data."""
+    data.  `arith` "double-float" counts the double-float solve's factors
+    (kappa and A^-1 B per row, 2 nz float2, and 64 B of Ginv, K^2, H^2 K
+    scalars per wavenumber); otherwise the FP64 solve's 6 nz + 4 FP64 values."""
     s = 4 if prec == "mixed" else 8
     nxh = w.nx // 2 + 1
     nk = w.ny * nxh
@@ -118,6 +120,8 @@ def algorithmic_bytes(stage, w, prec):
     if stage == "solve" and w.domType == "TP":
         # triply periodic: the spectrum in and out (wavenumber tables are cached)
         return 2 * spec
+    if stage == "solve" and arith == "double-float":
+        return 2 * spec + nk * (2 * w.nz * 8 + 64)
     if stage == "solve":
         # spectrum in and out, per-wavenumber factors (6 nz + 4 FP64 values)
         return 2 * spec + nk * (6 * w.nz + 4) * 8
@@ -171,7 +175,10 @@ def run_ours(args, rank, world):
             torch.distributed.barrier()
             torch.cuda.synchronize()
 
-    op = DPStokes(StokesParams.from_workload(w, prec), w.N, device=dev)
+    prm = StokesParams.from_workload(w, prec)
+    if args.solve != "default":
+        prm = StokesParams(**{**prm.as_dict(), "solve": args.solve})
+    op = DPStokes(prm, w.N, device=dev)
     op.set_positions(torch.tensor(X, device=dev))
     Fd = torch.tensor(F, dtype=dt, device=dev)
     Td = torch.tensor(T, dtype=dt, device=dev) if T is not None else None
@@ -237,6 +244,22 @@ def run_ours(args, rank, world):
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
     nbytes = Fh.numel() * Fh.element_size()
+
+    # the allocation-free entry point on device arrays (static solve scratch,
+    # FP64-arithmetic solve on as many CTAs as the static array holds)
+    def noalloc_step():
+        _lib.check(L.dpst_mdot_noalloc(op._h, ptr(Fd), ptr(Td), ptr(V), ptr(Wd), code, stream))
+
+    for _ in range(2):
+        noalloc_step()
+    barrier()
+    k_na = max(3, min(args.steps, 10))
+    e0.record()
+    for _ in range(k_na):
+        noalloc_step()
+    e1.record()
+    barrier()
+    noalloc_ms = e0.elapsed_time(e1) / k_na
     e2e = {"value": replica_value(w.N, args.steps, e2e_s, world), "unit": "particles/s",
            "h2d_bytes_per_step": nbytes * (2 if T is not None else 1),
            "d2h_bytes_per_step": nbytes * (2 if w.has_torque else 1)}
@@ -270,7 +293,8 @@ def run_ours(args, rank, world):
     peaks, peak_kind = load_peaks()
     stage_names = [k for k in stages if k != "total"]
     dom = max(stage_names, key=lambda k: stages[k])
-    ab = algorithmic_bytes(dom, w, prec)
+    arith = {1: "fp64", 2: "double-float"}.get(info.get("solve_arith"), "n/a")
+    ab = algorithmic_bytes(dom, w, prec, arith)
     achieved = ab / (stages[dom] * 1e-3) / 1e9 if ab else None
     roof = {"bound": "hbm", "stage": dom, "achieved": achieved, "peak": peaks["hbm_gbs"],
             "unit": "GB/s", "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
@@ -278,7 +302,7 @@ def run_ours(args, rank, world):
     # every stage against HBM from the same CUDA-event stage times
     roof["stages"] = {}
     for k in stage_names:
-        b = algorithmic_bytes(k, w, prec)
+        b = algorithmic_bytes(k, w, prec, arith)
         if b and stages[k] > 0:
             gbs = b / (stages[k] * 1e-3) / 1e9
             roof["stages"][k] = {"ms": round(stages[k], 4), "algorithmic_bytes": b,
@@ -299,18 +323,41 @@ def run_ours(args, rank, world):
     roof["ztransform_kernel"] = "tcgen05 split-TF32" if info.get("ztransform") == 1 else "SIMT folded"
     roof["ztransform_inverse_kernel"] = ("tcgen05 split-TF32" if info.get("ztransform_inverse") == 1
                                          else "SIMT folded")
-    if dom == "solve":
+    if dom == "solve" and arith == "double-float":
+        # the double-float solve is issue bound (FP32 FMA chains of the
+        # compensated sweeps): its DRAM traffic is measured by ncu, and the
+        # issue rate is its warp instructions over the SMs' issue slots
+        roof["note"] = ("per-wavenumber double-float BVP: issue bound (FP32 FMA pipe); HBM fraction "
+                        "is of its algorithmic bytes; issue gives warp instructions per issue slot")
+        nk_solve = w.ny * (w.nx // 2 + 1)
+        if w.domType == "DP" and w.nz == 128:
+            # ncu launch list of the c2 Mdot (512^2 x 128 open box, 131,584 wavenumbers):
+            # k_bvp_df variant 3 read 1084.3 MB and wrote 616.7 MB per launch
+            roof["traffic"] = (1084.3e6 + 616.7e6) / 131584 * nk_solve
+            roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_bvp_df "
+                                      "(variant 3) on c2_dp_n65536, per launch, scaled by wavenumbers "
+                                      "(profiles/launches_c2_dp_n65536_mixed.md)")
+            # 636 M warp instructions for the 74,112 wavenumbers of c2_dp_n65536@384
+            # (ncu smsp__inst_executed.sum; profiles/k_bvp_df_c2_at384_dp_n36864_mixed.md)
+            nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = clocks.get("sm_mhz") or 2070.0
+            instr = 636e6 / 74112 * nk_solve
+            rate = instr / (stages["solve"] * 1e-3)
+            peak = nsm * 4 * mhz * 1e6
+            roof["issue"] = {"warp_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
+                             "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
+    elif dom == "solve":
         # FP64-pipe bound: report the FP64 arithmetic rate against the GB300 FP64 peak
         roof["note"] = ("per-wavenumber FP64 BVP: FP64-pipe bound; HBM fraction shown is of "
                         "its algorithmic bytes; fp64_pipe gives its FP64 issue rate")
         if w.domType == "DP" and w.nz == 128:
             # DRAM bytes of the hybrid solve per wavenumber from the ncu capture of
-            # k_bvp_hybrid on p4_dp_n36864_384 (same geometry and nz: 3.42 GB read +
+            # k_bvp_hybrid on c2_dp_n65536@384 (same geometry and nz: 3.42 GB read +
             # 1.32 GB written for 74,112 wavenumbers), scaled by this grid's wavenumbers
             nk_solve = w.ny * (w.nx // 2 + 1)
             roof["traffic"] = (3.42e9 + 1.32e9) / 74112 * nk_solve
-            roof["traffic_source"] = ("ncu k_bvp_hybrid on p4_dp_n36864_384, scaled by wavenumbers "
-                                      "(profiles/k_bvp_hybrid_p4_dp_n36864_384.md)")
+            roof["traffic_source"] = ("ncu k_bvp_hybrid on c2_dp_n65536@384, scaled by wavenumbers "
+                                      "(profiles/k_bvp_hybrid_c2_at384_dp_n36864_mixed.md)")
         if w.domType != "TP":
             # ~46 FP64 instructions per row per lane (2 lanes x nz rows per wavenumber;
             # ncu's FP64 instruction count of the solve), at 2 FP64 lane-operations
@@ -323,7 +370,8 @@ def run_ours(args, rank, world):
             roof["fp64_pipe"] = {"lane_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
                                  "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
     extra["set_positions_ms"] = set_positions_ms
-    extra["solve_kernel"] = {"arith": {1: "fp64", 2: "double-float"}.get(info.get("solve_arith"), "n/a"),
+    extra["noalloc_ms_per_step"] = noalloc_ms
+    extra["solve_kernel"] = {"arith": arith,
                              "variant": info.get("solve_variant"),
                              "variant_ms": [round(float(x), 4) for x in info.get("solve_ms", [])]}
     return dict(value=value, ms_step=ms_step, e2e=e2e, stages=stages, info=info, extra=extra,
@@ -634,6 +682,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2_dp_n65536")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--solve", default="default", choices=["default", "fp64", "df64"],
+                    help="arithmetic of the per-wavenumber solve of the timed operator")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-backward", action="store_true")

@@ -111,16 +111,3 @@ def test_edge_positions_inside_the_cell():
             assert (X[:, 2] < w.z0 + w.Lz).all()
         else:
             assert (X[:, 2] == w.z0 + w.Lz).any()
-
-
-def test_cpu_sample_all_cores_runs():
-    """The reference arm's CPU sample on several processes (spawned) returns a
-    positive estimate per stage and reports its process count."""
-    import cpu_sample
-    from doublyperiodicstokes_gb300 import workloads as W
-    w = W.SMALL_BY_NAME["s_dpsc_t"]
-    X, F, T = W.make_inputs(w)
-    tot, stages, sample, cores = cpu_sample.sample_mdot_seconds_parallel(O.Params(**w.oracle_params()), X, F, T,
-                                                                         workers=2, pfrac=2, mfrac=4)
-    assert cores == 2 and tot > 0 and all(v >= 0 for v in stages.values())
-    assert "2 processes" in sample
