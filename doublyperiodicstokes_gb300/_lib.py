@@ -40,7 +40,8 @@ class DpstInfo(ctypes.Structure):
                 ("fused_particle_passes", ctypes.c_int), ("ztransform_inverse", ctypes.c_int),
                 ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int),
                 ("solve_arith", ctypes.c_int), ("solve_variant", ctypes.c_int),
-                ("solve_ms", ctypes.c_float * 4), ("xy_transform", ctypes.c_int)]
+                ("solve_ms", ctypes.c_float * 4), ("xy_transform", ctypes.c_int),
+                ("xy_ms", ctypes.c_float * 2)]
 
 
 class DpstBatchInfo(ctypes.Structure):
@@ -87,7 +88,8 @@ SIGNATURES = {
     "dpst_batched_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DpstBatchInfo)]),
     "dpst_get_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DpstInfo)]),
     "dpst_xy_transform": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p,
-                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_void_p]),
     "dpst_last_error": (ctypes.c_char_p, []),
     "dpst_version": (ctypes.c_char_p, []),
 }

@@ -83,6 +83,19 @@ cudaError_t fft_setup(int nx, int ny);
 cudaError_t fft_rows(bool inverse, const float *grid_in, float2 *spec_out, const float2 *spec_in, float *grid_out,
                      int nx, int64_t rows, const float2 *twx, cudaStream_t s);
 cudaError_t fft_cols(bool inverse, float2 *spec, int ny, int nxh, int64_t planes, const float2 *twy, cudaStream_t s);
+bool fft_xy_fused_supported(int nx, int ny);
+int64_t fft_xy_counter_ints(int64_t planes);
+// planes between the one-launch transform's two passes: 16, or
+// DPSTOKES_GB300_XY_LAG (1 ... 4096)
+static int xy_lag_setting() {
+  const char *env = getenv("DPSTOKES_GB300_XY_LAG");
+  const int v = env ? atoi(env) : 16;
+  return (v >= 1 && v <= 4096) ? v : 16;
+}
+cudaError_t fft_xy_setup(int nx, int ny, int *grid);
+cudaError_t fft_xy_fused(bool inverse, const float *grid_in, float2 *spec, float *grid_out, int nx, int ny,
+                         int64_t planes, const float2 *twx, const float2 *twy, int *ctr, int grid, int lag,
+                         cudaStream_t s);
 template <typename R>
 void launch_spec_curl(const R *src, R *dst, bool accumulate, int nz, int64_t nk, int nx, int ny, int nxh,
                       const double *kvx, const double *kvy, double H, cudaStream_t s);
@@ -161,6 +174,15 @@ struct Engine : EngineBase {
   // cuFFT otherwise
   bool ownfft = false;
   DevBuf twx, twy;
+  // one-launch x-y transforms (both passes, the intermediate in L2): per-plane
+  // counters for up to xy_planes planes, the persistent grid, the plane lag,
+  // and the creation-time timings {two-pass, one-launch} of a forward +
+  // inverse pair
+  bool xyfused = false;
+  DevBuf xyctr;
+  int64_t xy_planes = 0;
+  int xy_grid = 0, xy_lag = xy_lag_setting();
+  float xy_ms[2] = {0.0f, 0.0f};
 
   Engine(const dpst_params &prm, int64_t n, int dev) {
     p = prm;
@@ -330,17 +352,67 @@ struct Engine : EngineBase {
     plans = true;
     {
       const char *env = getenv("DPSTOKES_GB300_XY_FFT");
-      const bool want_cufft = env && std::string(env) == "cufft";
+      const bool want_cufft = env && std::string(env) == "cufft";  // or "twopass" / "fused"
       if (sizeof(R) == 4 && !want_cufft && own_fft_supported(nx, ny)) {
         ownfft = true;
         upload(twx, fft_twiddles(nx));
         upload(twy, fft_twiddles(ny));
         DPST_CUDA(fft_setup(nx, ny));
+        if (fft_xy_fused_supported(nx, ny) && !(env && std::string(env) == "twopass")) {
+          DPST_CUDA(fft_xy_setup(nx, ny, &xy_grid));
+          grow_xy_counters(3 * (int64_t)nz);
+        }
       }
     }
     DPST_CUDA(cudaDeviceSynchronize());
+    tune_xy();
     tune_ztransform();
     tune_solve();
+  }
+
+  void grow_xy_counters(int64_t planes) {
+    if (planes <= xy_planes) return;
+    xyctr.alloc(sizeof(int) * fft_xy_counter_ints(planes));
+    DPST_CUDA(cudaMemset(xyctr.p, 0, sizeof(int) * fft_xy_counter_ints(planes)));
+    xy_planes = planes;
+  }
+
+  // The x-y transform's form: the two-pass kernels and the one-launch kernel
+  // each run a forward + inverse pair on the grid and spectrum buffers (one
+  // warm-up, best of three), and the faster is kept; a one-launch run whose
+  // waits gave up (error word set) is never kept.  DPSTOKES_GB300_XY_FFT=
+  // fused | twopass fixes the choice.
+  void tune_xy() {
+    if (!ownfft || xy_planes == 0) return;
+    const char *env = getenv("DPSTOKES_GB300_XY_FFT");
+    const std::string want = env ? std::string(env) : std::string();
+    cudaStream_t s = 0;
+    cudaEvent_t e0, e1;
+    DPST_CUDA(cudaEventCreate(&e0));
+    DPST_CUDA(cudaEventCreate(&e1));
+    for (int form = 0; form < 2; ++form) {
+      xyfused = form == 1;
+      float best = 1e30f;
+      for (int r = 0; r < 4; ++r) {
+        DPST_CUDA(cudaEventRecord(e0, s));
+        exec_fwd(grid.as<R>(), spec.as<CR>(), s);
+        exec_inv(spec.as<CR>(), grid.as<R>(), s);
+        DPST_CUDA(cudaEventRecord(e1, s));
+        DPST_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        DPST_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0) best = std::min(best, ms);
+      }
+      xy_ms[form] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int err = 0;
+    DPST_CUDA(cudaMemcpy(&err, xyctr.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    if (want == "fused") xyfused = true;
+    else xyfused = err == 0 && xy_ms[1] < xy_ms[0];
+    if (err != 0) xyfused = false;
+    DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
   }
 
   // The double-float solve's kernel variant (prefetch depths, warps per SM):
@@ -766,6 +838,11 @@ struct Engine : EngineBase {
   void exec_fwd(R *gr, CR *sp, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
     if (planes == 0) planes = 3 * (int64_t)nz;
     if (plan == 0) plan = plan_f;
+    if (ownfft && xyfused && planes <= xy_planes) {
+      DPST_CUDA(fft_xy_fused(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr, nx,
+                             ny, planes, twx.as<float2>(), twy.as<float2>(), xyctr.as<int>(), xy_grid, xy_lag, s));
+      return;
+    }
     if (ownfft) {
       DPST_CUDA(fft_rows(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr,
                          nullptr, nx, planes * ny, twx.as<float2>(), s));
@@ -781,6 +858,11 @@ struct Engine : EngineBase {
   void exec_inv(CR *sp, R *gr, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
     if (planes == 0) planes = 3 * (int64_t)nz;
     if (plan == 0) plan = plan_b;
+    if (ownfft && xyfused && planes <= xy_planes) {
+      DPST_CUDA(fft_xy_fused(true, nullptr, reinterpret_cast<float2 *>(sp), reinterpret_cast<float *>(gr), nx, ny,
+                             planes, twx.as<float2>(), twy.as<float2>(), xyctr.as<int>(), xy_grid, xy_lag, s));
+      return;
+    }
     if (ownfft) {
       DPST_CUDA(fft_cols(true, reinterpret_cast<float2 *>(sp), ny, nxh, planes, twy.as<float2>(), s));
       DPST_CUDA(fft_rows(true, nullptr, nullptr, reinterpret_cast<const float2 *>(sp), reinterpret_cast<float *>(gr),
@@ -864,6 +946,7 @@ struct Engine : EngineBase {
       DPST_CUDA(bvp_plan_b<R>(nz, (int64_t)K * nk, nsm, &bvpK_grid, &bytes));
     }
     bvpK_scratch.alloc(bytes);
+    if (xy_planes > 0) grow_xy_counters(3 * (int64_t)nz * K);
     DPST_CUDA(cudaDeviceSynchronize());
     multi_k = K;
   }
@@ -1167,8 +1250,10 @@ struct Engine : EngineBase {
     o->fused_particle_passes = fused ? 1 : 0;
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     o->solve_variant = dfsolve ? df_variant : 0;
-    o->xy_transform = ownfft ? 1 : 0;
-    if (ownfft) o->kernels_per_mdot += 4 * (reg && p.has_torque ? 2 : 1);
+    o->xy_transform = ownfft ? (xyfused ? 2 : 1) : 0;
+    o->xy_ms[0] = xy_ms[0];
+    o->xy_ms[1] = xy_ms[1];
+    if (ownfft) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,
@@ -1380,12 +1465,16 @@ int dpst_get_info(dpst_handle h, dpst_info *out) {
   });
 }
 
-int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int device, void *stream) {
+int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int form, int device,
+                      void *stream) {
   return guarded([&] {
     if (!in || !out || planes < 1) throw Error(DPST_ERR_INVALID_ARG, "NULL argument or no planes");
+    if (form != 0 && form != 1) throw Error(DPST_ERR_INVALID_ARG, "form must be 0 (two passes) or 1 (one launch)");
     if (!dpst::own_fft_supported(nx, ny))
       throw Error(DPST_ERR_UNSUPPORTED, "the library's x-y transforms take powers of two, 64 <= nx <= 2048, "
                                         "32 <= ny <= 1024");
+    if (form == 1 && !dpst::fft_xy_fused_supported(nx, ny))
+      throw Error(DPST_ERR_UNSUPPORTED, "the one-launch x-y transform takes nx = ny in 128, 256, 512, 1024");
     DPST_CUDA(cudaSetDevice(device));
     cudaStream_t s = (cudaStream_t)stream;
     dpst::DevBuf twx, twy;
@@ -1393,6 +1482,26 @@ int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int i
     dpst::upload(twy, dpst::fft_twiddles(ny));
     DPST_CUDA(dpst::fft_setup(nx, ny));
     const int nxh = nx / 2 + 1;
+    if (form == 1) {
+      int grid = 0;
+      DPST_CUDA(dpst::fft_xy_setup(nx, ny, &grid));
+      dpst::DevBuf ctr;
+      ctr.alloc(sizeof(int) * dpst::fft_xy_counter_ints(planes));
+      DPST_CUDA(cudaMemsetAsync(ctr.p, 0, sizeof(int) * dpst::fft_xy_counter_ints(planes), s));
+      const int lag = dpst::xy_lag_setting();
+      if (!inverse)
+        DPST_CUDA(dpst::fft_xy_fused(false, (const float *)in, (float2 *)out, nullptr, nx, ny, planes,
+                                     twx.as<float2>(), twy.as<float2>(), ctr.as<int>(), grid, lag, s));
+      else
+        DPST_CUDA(dpst::fft_xy_fused(true, nullptr, (float2 *)in, (float *)out, nx, ny, planes, twx.as<float2>(),
+                                     twy.as<float2>(), ctr.as<int>(), grid, lag, s));
+      int word[2] = {0, 0};
+      DPST_CUDA(cudaMemcpyAsync(word, ctr.as<int>() + 1, sizeof(word), cudaMemcpyDeviceToHost, s));
+      DPST_CUDA(cudaStreamSynchronize(s));
+      if (word[1] != 0) throw Error(DPST_ERR_CUDA, "one-launch x-y transform: a wait gave up");
+      if (word[0] != 0) throw Error(DPST_ERR_CUDA, "one-launch x-y transform: counters not reset");
+      return;
+    }
     if (!inverse) {
       DPST_CUDA(dpst::fft_rows(false, (const float *)in, (float2 *)out, nullptr, nullptr, nx, planes * ny,
                                twx.as<float2>(), s));

@@ -92,21 +92,24 @@ struct RowCfg {
   static constexpr int T = RPC * P;
 };
 
+// One CTA's rows [row0, row0 + RPC) (threads beyond RowCfg::T idle); sbuf:
+// RPC x BUF values.  Data loads bypass L1 (another CTA of the same launch may
+// have written them).
 template <int L, int P>
-__global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *__restrict__ in,
-                                                                  float2 *__restrict__ out, int64_t rows,
-                                                                  const float2 *__restrict__ twN) {
-  constexpr int Q = L / P, RPC = RowCfg<L, P>::RPC, N = 2 * L, R = Q / P;
-  __shared__ float2 sbuf[RPC][RowCfg<L, P>::BUF];
+static __device__ __forceinline__ void rows_r2c_body(const float *__restrict__ in, float2 *__restrict__ out,
+                                                     int64_t rows, int64_t row0, const float2 *__restrict__ twN,
+                                                     float2 *sbuf) {
+  constexpr int Q = L / P, N = 2 * L, R = Q / P;
+  if (threadIdx.x >= RowCfg<L, P>::T) return;
   const int g = threadIdx.x / P, p = threadIdx.x % P;
-  const int64_t row = (int64_t)blockIdx.x * RPC + g;
+  const int64_t row = row0 + g;
   const bool live = row < rows;
   const int64_t r = live ? row : rows - 1;
   const float2 *x = reinterpret_cast<const float2 *>(in + r * N);
   float2 v[Q];
 #pragma unroll
-  for (int q = 0; q < Q; ++q) v[q] = __ldg(x + p + P * q);
-  float2 *sm = sbuf[g];
+  for (int q = 0; q < Q; ++q) v[q] = __ldcg(x + p + P * q);
+  float2 *sm = sbuf + g * RowCfg<L, P>::BUF;
   {
     // stage 1 / exchange / stage 2, w_L^j = w_N^{2j} from the w_N table
     constexpr int DIR = -1;
@@ -154,24 +157,32 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
 }
 
 template <int L, int P>
-__global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *__restrict__ in,
-                                                                  float *__restrict__ out, int64_t rows,
+__global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *__restrict__ in,
+                                                                  float2 *__restrict__ out, int64_t rows,
                                                                   const float2 *__restrict__ twN) {
-  constexpr int Q = L / P, RPC = RowCfg<L, P>::RPC, N = 2 * L, R = Q / P;
-  __shared__ float2 sbuf[RPC][RowCfg<L, P>::BUF];
+  __shared__ float2 sbuf[RowCfg<L, P>::RPC * RowCfg<L, P>::BUF];
+  rows_r2c_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf);
+}
+
+template <int L, int P>
+static __device__ __forceinline__ void rows_c2r_body(const float2 *__restrict__ in, float *__restrict__ out,
+                                                     int64_t rows, int64_t row0, const float2 *__restrict__ twN,
+                                                     float2 *sbuf) {
+  constexpr int Q = L / P, N = 2 * L, R = Q / P;
+  if (threadIdx.x >= RowCfg<L, P>::T) return;
   const int g = threadIdx.x / P, p = threadIdx.x % P;
-  const int64_t row = (int64_t)blockIdx.x * RPC + g;
+  const int64_t row = row0 + g;
   const bool live = row < rows;
   const int64_t r = live ? row : rows - 1;
-  float2 *sm = sbuf[g];
+  float2 *sm = sbuf + g * RowCfg<L, P>::BUF;
   const float2 *xr = in + r * (L + 1);
   // the kx = 0 and Nyquist terms enter through their real parts (the real
   // part of the full complex inverse, as a complex-to-real transform takes it)
   {
     float2 t[Q];
 #pragma unroll
-    for (int m = 0; m < Q; ++m) t[m] = __ldg(xr + p + P * m);
-    const float2 last = __ldg(xr + L);
+    for (int m = 0; m < Q; ++m) t[m] = __ldcg(xr + p + P * m);
+    const float2 last = __ldcg(xr + L);
 #pragma unroll
     for (int m = 0; m < Q; ++m) sm[p + P * m] = t[m];
     if (p == 0) {
@@ -225,6 +236,14 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
   }
 }
 
+template <int L, int P>
+__global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *__restrict__ in,
+                                                                  float *__restrict__ out, int64_t rows,
+                                                                  const float2 *__restrict__ twN) {
+  __shared__ float2 sbuf[RowCfg<L, P>::RPC * RowCfg<L, P>::BUF];
+  rows_c2r_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf);
+}
+
 // ---------------------------------------------------------------------------
 // columns: complex FFT of length L along y for CW columns of the half
 // spectrum per CTA, in place
@@ -233,49 +252,200 @@ constexpr int FFT_CW = 16;
 // per-column exchange buffer: Q (P + 1) values, its stride odd so that the
 // 16 columns of a warp's access fall in different banks
 template <int L, int P>
-constexpr int col_stride() {
+__host__ __device__ constexpr int col_stride() {
   return ((L / P) * (P + 1)) | 1;
+}
+
+// Column tile `tile` (FFT_CW columns from kx = tile FFT_CW) of plane `plane`,
+// in place; every thread of the CTA reaches the one barrier, threads beyond
+// FFT_CW P idle.  cbuf: FFT_CW x col_stride values.
+template <int L, int P, int DIR>
+static __device__ __forceinline__ void cols_body(float2 *__restrict__ data, int64_t plane, int tile, int nxh,
+                                                 const float2 *__restrict__ twL, float2 *cbuf) {
+  constexpr int Q = L / P, R = Q / P;
+  const bool act = threadIdx.x < FFT_CW * P;
+  const int c = threadIdx.x % FFT_CW, p = threadIdx.x / FFT_CW;
+  const int kx = tile * FFT_CW + c;
+  const bool live = act && kx < nxh;
+  float2 *base = data + plane * (int64_t)L * nxh + (kx < nxh ? kx : nxh - 1);
+  float2 *sm = cbuf + c * col_stride<L, P>();
+  if (act) {
+    float2 v[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) v[q] = __ldcg(base + (int64_t)(p + P * q) * nxh);
+    dft_reg<Q, DIR>(v);
+#pragma unroll
+    for (int k1 = 0; k1 < Q; ++k1) {
+      float2 y = v[brev<Q>(k1)];
+      if (k1 != 0 && p != 0) {
+        float2 w = __ldg(twL + p * k1);
+        if (DIR > 0) w = conjf2(w);
+        y = cmulf(y, w);
+      }
+      sm[k1 * (P + 1) + p] = y;
+    }
+  }
+  __syncthreads();
+  if (act) {
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int k1 = p * R + i;
+      float2 u[P];
+#pragma unroll
+      for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
+      dft_reg<P, DIR>(u);
+      if (live) {
+#pragma unroll
+        for (int k2 = 0; k2 < P; ++k2) base[(int64_t)(k1 + Q * k2) * nxh] = u[brev<P>(k2)];
+      }
+    }
+  }
 }
 
 template <int L, int P, int DIR>
 __global__ void __launch_bounds__(FFT_CW * P, (FFT_CW * P) <= 256 ? 3 : 1) k_fft_cols(float2 *__restrict__ data, int64_t planes, int nxh,
                                                          const float2 *__restrict__ twL) {
-  constexpr int Q = L / P, R = Q / P;
   extern __shared__ float2 cbuf[];  // [CW][col_stride]
-  const int c = threadIdx.x % FFT_CW, p = threadIdx.x / FFT_CW;
   const int tiles = (nxh + FFT_CW - 1) / FFT_CW;
   const int64_t t = blockIdx.x;
   const int64_t plane = t / tiles;
-  const int kx = (int)(t % tiles) * FFT_CW + c;
   if (plane >= planes) return;
-  const bool live = kx < nxh;
-  float2 *base = data + plane * (int64_t)L * nxh + (live ? kx : nxh - 1);
-  float2 v[Q];
-#pragma unroll
-  for (int q = 0; q < Q; ++q) v[q] = base[(int64_t)(p + P * q) * nxh];
-  float2 *sm = cbuf + c * col_stride<L, P>();
-  dft_reg<Q, DIR>(v);
-#pragma unroll
-  for (int k1 = 0; k1 < Q; ++k1) {
-    float2 y = v[brev<Q>(k1)];
-    if (k1 != 0 && p != 0) {
-      float2 w = __ldg(twL + p * k1);
-      if (DIR > 0) w = conjf2(w);
-      y = cmulf(y, w);
+  cols_body<L, P, DIR>(data, plane, (int)(t % tiles), nxh, twL, cbuf);
+}
+
+// ---------------------------------------------------------------------------
+// both passes in one persistent launch, the intermediate kept in L2
+// ---------------------------------------------------------------------------
+// The two-pass form reads and writes the whole spectrum twice per direction
+// (0.8 GB each way on a 512 x 512 x 384-plane grid, four times L2).  Here the
+// CTAs take tasks from one counter in an order that runs the first pass of
+// plane j beside the second pass of plane j - lag: rows (forward) or columns
+// (inverse) of a plane are written to L2, and the other pass reads them back
+// from L2 lag planes later, so DRAM sees one read and one write per direction.
+// A second-pass task waits until every first-pass task of its plane has
+// published (per-plane counter, release / acquire).  Those tasks were taken
+// from the counter before it and never wait themselves, so every wait ends
+// however many CTAs are resident; each wait still gives up after
+// FFT_WAIT_NS, records the error in ctr[2] and skips its task.  The last CTA
+// to finish resets the counters for the next launch (ctr[2] is sticky).
+// ctr (ints): [1] CTAs finished, [2] error, [4..5] next task (64-bit),
+// [6 + plane] first-pass tasks done.
+constexpr unsigned long long FFT_WAIT_NS = 1000000000ull;
+
+static __device__ __forceinline__ unsigned long long fft_clock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+static __device__ __forceinline__ int ld_acquire_gpu(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <int NX>
+struct RowP {
+  static constexpr int P = NX <= 64 ? 4 : NX <= 256 ? 8 : NX <= 1024 ? 16 : 32;
+};
+template <int NY>
+struct ColP {
+  static constexpr int P = NY <= 32 ? 4 : NY <= 128 ? 8 : NY <= 512 ? 16 : 32;
+};
+
+template <int NX, int NY>
+struct XyCfg {
+  static constexpr int L = NX / 2, P = RowP<NX>::P, PY = ColP<NY>::P;
+  static constexpr int TR = RowCfg<L, P>::T, TC = FFT_CW * PY;
+  static constexpr int T = TR > TC ? TR : TC;
+  static constexpr int MINB = T <= 256 ? 3 : 1;  // CTAs per SM the registers are sized for
+  static constexpr int SR = RowCfg<L, P>::RPC * RowCfg<L, P>::BUF, SC = FFT_CW * col_stride<NY, PY>();
+  static constexpr int SMEM = (SR > SC ? SR : SC) * (int)sizeof(float2);
+  static constexpr int RT = NY / RowCfg<L, P>::RPC;          // row tasks per plane
+  static constexpr int CT = (L + 1 + FFT_CW - 1) / FFT_CW;   // column tasks per plane
+};
+
+// INV = false: forward, grid -> spectrum (rows first); true: inverse,
+// spectrum -> grid (columns first, in place on the spectrum).
+template <int NX, int NY, bool INV>
+__global__ void __launch_bounds__(XyCfg<NX, NY>::T, XyCfg<NX, NY>::MINB) k_fft_xy(const float *__restrict__ gin, float2 *spec,
+                                                             float *__restrict__ gout, int64_t planes,
+                                                             const float2 *__restrict__ twx,
+                                                             const float2 *__restrict__ twy, int *ctr, int lag) {
+  using C = XyCfg<NX, NY>;
+  constexpr int NA = INV ? C::CT : C::RT, NB = INV ? C::RT : C::CT;
+  constexpr int L = C::L, RPC = RowCfg<L, C::P>::RPC;
+  extern __shared__ float2 xsm[];
+  __shared__ int64_t s_task;
+  __shared__ int s_ok;
+  const int64_t D = lag < planes ? lag : planes;
+  const int64_t s1 = D * NA, s2 = s1 + (planes - D) * (NA + NB), total = planes * (NA + NB);
+  const int64_t rows = planes * NY;
+  for (;;) {
+    __syncthreads();  // the previous task's shared-memory reads are done
+    if (threadIdx.x == 0) s_task = atomicAdd(reinterpret_cast<unsigned long long *>(ctr + 4), 1ull);
+    __syncthreads();
+    const int64_t t = s_task;
+    if (t >= total) break;
+    bool first;
+    int64_t plane;
+    int idx;
+    if (t < s1) {
+      first = true, plane = t / NA, idx = (int)(t % NA);
+    } else if (t < s2) {
+      const int64_t u = t - s1, j = D + u / (NA + NB);
+      const int r = (int)(u % (NA + NB));
+      first = r < NA;
+      plane = first ? j : j - D;
+      idx = first ? r : r - NA;
+    } else {
+      const int64_t u = t - s2;
+      first = false, plane = planes + u / NB - D, idx = (int)(u % NB);
     }
-    sm[k1 * (P + 1) + p] = y;
+    if (!first) {
+      if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned long long t0 = fft_clock_ns();
+        for (int spin = 0; ld_acquire_gpu(ctr + 6 + plane) < NA; ++spin) {
+          if ((spin & 15) == 15 && fft_clock_ns() - t0 > FFT_WAIT_NS) {
+            atomicOr(ctr + 2, 1);
+            ok = 0;
+            break;
+          }
+          __nanosleep(100);
+        }
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (!s_ok) continue;
+    }
+    const bool rowtask = (first != INV);
+    if (rowtask) {
+      if (!INV) rows_r2c_body<L, C::P>(gin, spec, rows, plane * NY + (int64_t)idx * RPC, twx, xsm);
+      else rows_c2r_body<L, C::P>(spec, gout, rows, plane * NY + (int64_t)idx * RPC, twx, xsm);
+    } else {
+      cols_body<NY, C::PY, INV ? 1 : -1>(spec, plane, idx, L + 1, twy, xsm);
+    }
+    if (first) {
+      __syncthreads();  // every thread's stores precede the release
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr + 6 + plane, 1);
+      }
+    }
+  }
+  // the last CTA out resets the counters
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(ctr + 1, 1) == (int)gridDim.x - 1;
   }
   __syncthreads();
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int k1 = p * R + i;
-    float2 u[P];
-#pragma unroll
-    for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
-    dft_reg<P, DIR>(u);
-    if (live) {
-#pragma unroll
-      for (int k2 = 0; k2 < P; ++k2) base[(int64_t)(k1 + Q * k2) * nxh] = u[brev<P>(k2)];
+  if (s_last) {
+    for (int64_t p = threadIdx.x; p < planes; p += blockDim.x) ctr[6 + p] = 0;
+    if (threadIdx.x == 0) {
+      *reinterpret_cast<unsigned long long *>(ctr + 4) = 0ull;
+      ctr[1] = 0;
+      __threadfence();
     }
   }
 }
@@ -394,6 +564,66 @@ cudaError_t fft_cols(bool inverse, float2 *spec, int ny, int nxh, int64_t planes
 #undef COLS_CASE
     default:
       return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// the one-launch form: sizes, counters, launch
+// ---------------------------------------------------------------------------
+bool fft_xy_fused_supported(int nx, int ny) {
+  return nx == ny && (nx == 128 || nx == 256 || nx == 512 || nx == 1024);
+}
+int64_t fft_xy_counter_ints(int64_t planes) { return 6 + planes; }
+
+template <int NX, int NY>
+static cudaError_t xy_setup(int *grid) {
+  using C = XyCfg<NX, NY>;
+  cudaError_t e = cudaFuncSetAttribute(k_fft_xy<NX, NY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_fft_xy<NX, NY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM);
+  int per_sm = 0, nsm = 0, dev = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_xy<NX, NY, false>, C::T, C::SMEM);
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) *grid = (per_sm > 0 ? per_sm : 1) * nsm;
+  return e;
+}
+
+// Shared-memory attributes and the persistent grid (CTAs resident at once).
+cudaError_t fft_xy_setup(int nx, int ny, int *grid) {
+  if (!fft_xy_fused_supported(nx, ny)) return cudaErrorInvalidValue;
+  cudaError_t e = upload_tw32();
+  if (e != cudaSuccess) return e;
+  switch (nx) {
+    case 128: return xy_setup<128, 128>(grid);
+    case 256: return xy_setup<256, 256>(grid);
+    case 512: return xy_setup<512, 512>(grid);
+    case 1024: return xy_setup<1024, 1024>(grid);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <int NX, int NY>
+static void xy_launch(bool inverse, const float *gin, float2 *spec, float *gout, int64_t planes, const float2 *twx,
+                      const float2 *twy, int *ctr, int grid, int lag, cudaStream_t s) {
+  using C = XyCfg<NX, NY>;
+  if (inverse) k_fft_xy<NX, NY, true><<<grid, C::T, C::SMEM, s>>>(gin, spec, gout, planes, twx, twy, ctr, lag);
+  else k_fft_xy<NX, NY, false><<<grid, C::T, C::SMEM, s>>>(gin, spec, gout, planes, twx, twy, ctr, lag);
+}
+
+// Forward (grid_in -> spec) or inverse (spec -> grid_out, spec overwritten)
+// x-y transform of `planes` planes in one launch; ctr: fft_xy_counter_ints
+// (planes) zeroed ints (left zeroed, but for the sticky error at ctr[2]).
+cudaError_t fft_xy_fused(bool inverse, const float *grid_in, float2 *spec, float *grid_out, int nx, int ny,
+                         int64_t planes, const float2 *twx, const float2 *twy, int *ctr, int grid, int lag,
+                         cudaStream_t s) {
+  if (!fft_xy_fused_supported(nx, ny) || grid <= 0 || planes <= 0) return cudaErrorInvalidValue;
+  switch (nx) {
+    case 128: xy_launch<128, 128>(inverse, grid_in, spec, grid_out, planes, twx, twy, ctr, grid, lag, s); break;
+    case 256: xy_launch<256, 256>(inverse, grid_in, spec, grid_out, planes, twx, twy, ctr, grid, lag, s); break;
+    case 512: xy_launch<512, 512>(inverse, grid_in, spec, grid_out, planes, twx, twy, ctr, grid, lag, s); break;
+    case 1024: xy_launch<1024, 1024>(inverse, grid_in, spec, grid_out, planes, twx, twy, ctr, grid, lag, s); break;
   }
   return cudaGetLastError();
 }

@@ -166,9 +166,14 @@ typedef struct dpst_info {
   int solve_variant;               /* DPST_SOLVE_DF64 in the mixed operator: the kernel variant
                                       (prefetch depths, warps per SM) chosen at creation */
   float solve_ms[4];               /* its creation-time timings per variant (0 if not timed) */
-  int xy_transform;                /* x-y transforms: 1 the library's own (mixed operator,
-                                      power-of-two nx and ny; DPSTOKES_GB300_XY_FFT=cufft
-                                      selects cuFFT), 0 cuFFT */
+  int xy_transform;                /* x-y transforms: the library's own in the mixed operator
+                                      with power-of-two nx and ny, 1 as two passes (rows,
+                                      columns), 2 as one launch of both passes (nx = ny in
+                                      128, 256, 512, 1024, when faster at creation);
+                                      0 cuFFT.  DPSTOKES_GB300_XY_FFT=cufft | twopass |
+                                      fused forces one */
+  float xy_ms[2];                  /* creation-time timings of a forward + inverse pair:
+                                      two-pass, one-launch (0 if not timed) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;
@@ -315,9 +320,11 @@ int dpst_get_info(dpst_handle h, dpst_info *out);
  * half spectrum, which is overwritten, out = real [planes][ny][nx], the
  * imaginary parts of the kx = 0 and Nyquist columns after the y pass being
  * dropped as a complex-to-real transform does.  Powers of two, 64 <= nx <=
- * 2048, 32 <= ny <= 1024.  Allocates its twiddle tables and synchronises the
- * stream. */
-int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int device,
+ * 2048, 32 <= ny <= 1024.  form 0: two launches (rows, columns); form 1:
+ * one persistent launch of both passes (nx = ny in 128, 256, 512, 1024,
+ * else DPST_ERR_UNSUPPORTED), whose bounded waits report DPST_ERR_CUDA if
+ * one gave up.  Allocates its tables and synchronises the stream. */
+int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int form, int device,
                       void *stream);
 
 /* Last error message of the calling thread ("" if none). */
