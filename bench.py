@@ -412,11 +412,23 @@ def run_backward(args, dev, precision="fp64"):
         return e0.elapsed_time(e1) / k
 
     fwd = timed(lambda: op.mdot(Fd, None, out=(V, None)))
-    bwd = timed(lambda: op.mdot_backward(Fd, None, gd, need_F=True, need_X=True))
+
+    def step():
+        # a training step: the forward, then the backward on the forward's
+        # velocity grid (dpst_mdot_backward_saved)
+        op.mdot(Fd, None, out=(V, None))
+        op.mdot_backward(Fd, None, gd, need_F=True, need_X=True, forward_serial=op.forward_serial())
+
+    pair = timed(step)
+    reused = op.last_backward_reused
+    bwd_re = timed(lambda: op.mdot_backward(Fd, None, gd, need_F=True, need_X=True))
     op.close()
+    bwd = pair - fwd
     return {"workload": w.name, "precision": precision, "grads": ["F", "X"], "calls": k,
-            "fwd_ms": fwd, "bwd_ms": bwd, "bwd_fwd_ratio": bwd / fwd,
-            "note": "backward recomputes the forward's spread and velocity grid"}
+            "fwd_ms": fwd, "bwd_ms": bwd, "bwd_fwd_ratio": bwd / fwd, "fwd_bwd_pair_ms": pair,
+            "forward_grid_reused": reused, "bwd_recompute_ms": bwd_re, "bwd_recompute_fwd_ratio": bwd_re / fwd,
+            "note": "bwd_ms = (forward + backward on the forward's velocity grid) - forward; "
+                    "bwd_recompute_ms: a backward that recomputes the forward's spread and velocity grid"}
 
 
 def run_batched(args, dev):
@@ -570,19 +582,33 @@ def run_periodic(args, dev):
         # backward: dl/dF, dl/dT, dl/dX of l = <gV, V> + <gW, W>
         gVd = torch.tensor(np.random.default_rng(12).standard_normal(F.shape), dtype=dt, device=dev)
         gWd = torch.tensor(np.random.default_rng(13).standard_normal(F.shape), dtype=dt, device=dev)
-        for _ in range(max(3, args.warmup)):
-            op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(reps):
-            op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True)
-        e1.record()
-        torch.cuda.synchronize()
-        bms = e0.elapsed_time(e1) / reps
+        def timed_loop(fn):
+            for _ in range(max(3, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) / reps
+
+        def step():
+            # forward, then the backward on the forward's velocity grid
+            op.mdot(Fd, Td, out=(V, Wd))
+            op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True,
+                             forward_serial=op.forward_serial())
+
+        pair = timed_loop(step)
+        reused = op.last_backward_reused
+        bre = timed_loop(lambda: op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=True, need_X=True))
+        bms = pair - ms
         out[precision] = {"ms_per_mdot": ms, "particles_per_s": w.N / (ms / 1e3),
                           "stages_ms": {k: round(v, 4) for k, v in st.items()}, "stage_hbm": roof,
                           "kernels_per_mdot": op.info()["kernels_per_mdot"],
-                          "backward_ms": bms, "bwd_fwd_ratio": bms / ms, "backward_grads": ["F", "T", "X"]}
+                          "backward_ms": bms, "bwd_fwd_ratio": bms / ms, "backward_grads": ["F", "T", "X"],
+                          "fwd_bwd_pair_ms": pair, "forward_grid_reused": reused,
+                          "backward_recompute_ms": bre, "bwd_recompute_fwd_ratio": bre / ms}
         op.close()
     rel = lambda a, b: float(torch.linalg.norm(a - b) / torch.linalg.norm(b))  # noqa: E731
     out["rel_err_V_mixed_vs_fp64"] = rel(res["mixed"][0], res["fp64"][0])

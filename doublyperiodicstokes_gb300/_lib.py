@@ -78,6 +78,9 @@ SIGNATURES = {
                                          ctypes.c_void_p]),
     "dpst_mdot_backward": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_void_p] * 7
                            + [ctypes.c_int, ctypes.c_void_p]),
+    "dpst_forward_serial": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "dpst_mdot_backward_saved": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64] + [ctypes.c_void_p] * 7
+                                 + [ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "dpst_batched_create": (ctypes.c_int, [ctypes.POINTER(DpstParams), ctypes.POINTER(ctypes.c_int64),
                                            ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "dpst_batched_destroy": (ctypes.c_int, [ctypes.c_void_p]),

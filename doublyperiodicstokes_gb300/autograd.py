@@ -9,8 +9,9 @@ operator applied to the incoming gradients (the adjoint of every stage:
 interpolation, x-y FFT, z transform, per-wavenumber solve, wall correction,
 spreading; in the triply periodic box the grid-to-grid map is self-adjoint)
 for dl/dF and dl/dT, and the ES-kernel derivatives in the spreading and
-interpolation weights for dl/dX.  The forward's velocity grid is recomputed
-in the backward rather than kept.  Second derivatives and the
+interpolation weights for dl/dX.  The forward's velocity grid is taken from
+the handle when it still holds it (no other Mdot or position update on the
+handle since the forward), else recomputed.  Second derivatives and the
 regular-kernel torque coupling are not provided."""
 import torch
 from torch.autograd.function import once_differentiable
@@ -24,6 +25,7 @@ class _Mdot(torch.autograd.Function):
         T = T.detach().contiguous() if T is not None else None
         op.set_positions(X)
         V, W = op.mdot(F, T)
+        ctx.serial = op.forward_serial()
         ctx.op = op
         ctx.has_T = T is not None
         ctx.save_for_backward(X, F, T if T is not None else torch.empty(0, device=F.device))
@@ -45,9 +47,11 @@ class _Mdot(torch.autograd.Function):
             gW = gW.contiguous()
         else:
             gW = None
-        op.set_positions(X)  # the handle may have moved on since the forward
+        serial = ctx.serial if op.forward_serial() == ctx.serial else 0
+        if serial == 0:
+            op.set_positions(X)  # the handle has moved on since the forward
         gF, gT, gX = op.mdot_backward(F if need_X else None, T, gV, gW, need_F=need_F,
-                                      need_T=need_T and T is not None, need_X=need_X)
+                                      need_T=need_T and T is not None, need_X=need_X, forward_serial=serial)
         return None, gX, gF, gT
 
 

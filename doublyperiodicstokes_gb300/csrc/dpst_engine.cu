@@ -1149,9 +1149,12 @@ struct Engine : EngineBase {
       if (p.has_torque)
         launch_locate_grad<R>(true, pos64.as<double>(), N, kd.d, zext.as<double>(), wext.as<double>(), g, std_,
                               gsd, s);
-      // velocity grid and ghost layers of the forward, recomputed
-      spread_stage<RF>(F, T, s);
-      solve_stage(s);
+      // velocity grid and ghost layers of the forward, recomputed unless the
+      // handle still holds that forward's
+      if (!reuse_forward) {
+        spread_stage<RF>(F, T, s);
+        solve_stage(s);
+      }
     }
     // adjoint source J^T (gV, gW) on grid2 and the adjoint ghost layers
     DPST_CUDA(cudaMemsetAsync(g2, 0, grid2.bytes, s));
@@ -1334,10 +1337,21 @@ int dpst_destroy(dpst_handle h) {
   return guarded([&] { delete h; });
 }
 
+// Forward bookkeeping (EngineBase::serial, grid_serial): a call that moves
+// the particles or overwrites the velocity grid with anything but a
+// single-column Mdot's result forgets the held grid; a single-column Mdot
+// records itself as the holder once it has completed its launches.
+static void grid_forget(dpst::EngineBase *e) {
+  ++e->serial;
+  e->grid_serial = 0;
+}
+static void grid_hold(dpst::EngineBase *e) { e->grid_serial = ++e->serial; }
+
 int dpst_set_positions(dpst_handle h, const void *pos, int dtype, void *stream) {
   return guarded([&] {
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
+    grid_forget(h->e.get());
     h->e->set_positions(pos, dtype, (cudaStream_t)stream);
   });
 }
@@ -1346,7 +1360,16 @@ int dpst_mdot(dpst_handle h, const void *F, const void *T, void *V, void *W, int
   return guarded([&] {
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
+    grid_forget(h->e.get());
     h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
+    grid_hold(h->e.get());
+  });
+}
+
+int dpst_forward_serial(dpst_handle h, uint64_t *out) {
+  return guarded([&] {
+    if (!h || !out) throw Error(DPST_ERR_INVALID_ARG, "NULL argument");
+    *out = h->e->grid_serial;
   });
 }
 
@@ -1355,6 +1378,7 @@ int dpst_mdot_multi(dpst_handle h, int K, const void *F, const void *T, void *V,
   return guarded([&] {
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
+    grid_forget(h->e.get());
     h->e->mdot_multi(K, F, T, V, W, dtype, (cudaStream_t)stream);
   });
 }
@@ -1375,6 +1399,7 @@ int dpst_set_positions_host(dpst_handle h, const void *pos, int dtype, void *str
     cudaStream_t s = (cudaStream_t)stream;
     const size_t b = 3 * (size_t)h->e->N * elem_size(dtype);
     if (b) DPST_CUDA(cudaMemcpyAsync(h->dpos, pos, b, cudaMemcpyHostToDevice, s));
+    grid_forget(h->e.get());
     h->e->set_positions(h->dpos, dtype, s);
   });
 }
@@ -1393,7 +1418,9 @@ int dpst_mdot_host(dpst_handle h, const void *F, const void *T, void *V, void *W
       DPST_CUDA(cudaMemcpyAsync(h->dF, F, b, cudaMemcpyHostToDevice, s));
       if (T) DPST_CUDA(cudaMemcpyAsync(h->dT, T, b, cudaMemcpyHostToDevice, s));
     }
+    grid_forget(h->e.get());
     h->e->mdot(h->dF, T ? h->dT : nullptr, h->dV, W ? h->dW : nullptr, dtype, s);
+    grid_hold(h->e.get());
     if (cap) {
       DPST_CUDA(cudaMemcpyAsync(V, h->dV, b, cudaMemcpyDeviceToHost, s));
       if (W) DPST_CUDA(cudaMemcpyAsync(W, h->dW, b, cudaMemcpyDeviceToHost, s));
@@ -1406,6 +1433,7 @@ int dpst_spread_grid(dpst_handle h, const void *F, const void *T, int dtype, voi
   return guarded([&] {
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
+    grid_forget(h->e.get());
     h->e->spread_grid(F, T, dtype, grid_out, (cudaStream_t)stream);
   });
 }
@@ -1424,6 +1452,7 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
     if (!h || !stage_ms) throw Error(DPST_ERR_INVALID_ARG, "NULL argument");
     DPST_CUDA(cudaSetDevice(h->e->device));
     h->e->stage_ms = stage_ms;
+    grid_forget(h->e.get());
     try {
       h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
     } catch (...) {
@@ -1431,6 +1460,7 @@ int dpst_mdot_timed(dpst_handle h, const void *F, const void *T, void *V, void *
       throw;
     }
     h->e->stage_ms = nullptr;
+    grid_hold(h->e.get());
   });
 }
 
@@ -1439,6 +1469,7 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
     h->e->use_static_scratch = true;
+    grid_forget(h->e.get());
     try {
       h->e->mdot(F, T, V, W, dtype, (cudaStream_t)stream);
     } catch (...) {
@@ -1446,6 +1477,7 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
       throw;
     }
     h->e->use_static_scratch = false;
+    grid_hold(h->e.get());
   });
 }
 
@@ -1454,7 +1486,28 @@ int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *
   return guarded([&] {
     if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
     DPST_CUDA(cudaSetDevice(h->e->device));
+    grid_forget(h->e.get());  // a position gradient recomputes the velocity grid from these F, T
     h->e->backward(F, T, gV, gW, gF, gT, gX, dtype, (cudaStream_t)stream);
+  });
+}
+
+int dpst_mdot_backward_saved(dpst_handle h, uint64_t forward_serial, const void *F, const void *T, const void *gV,
+                             const void *gW, void *gF, void *gT, void *gX, int dtype, void *stream, int *reused) {
+  return guarded([&] {
+    if (!h) throw Error(DPST_ERR_INVALID_ARG, "handle is NULL");
+    DPST_CUDA(cudaSetDevice(h->e->device));
+    const bool reuse = forward_serial != 0 && forward_serial == h->e->grid_serial;
+    if (reused) *reused = reuse ? 1 : 0;
+    if (!reuse) grid_forget(h->e.get());
+    h->e->reuse_forward = reuse;
+    try {
+      h->e->backward(F, T, gV, gW, gF, gT, gX, dtype, (cudaStream_t)stream);
+    } catch (...) {
+      h->e->reuse_forward = false;
+      grid_forget(h->e.get());
+      throw;
+    }
+    h->e->reuse_forward = false;
   });
 }
 

@@ -35,7 +35,7 @@ static __device__ __forceinline__ void pos_derivs(double o, const KernelDesc &kd
     es_pos_derivs(o, kd.beta, kd.alpha2, g1, g2);
   } else {
     float f1, f2;
-    es_pos_derivs_f(o, kd.beta, kd.alpha2, f1, f2);
+    es_pos_derivs_f(o, kd.beta, kd.alpha2, kd.inv_alpha2, f1, f2);
     g1 = f1;
     g2 = f2;
   }
@@ -214,6 +214,34 @@ __global__ void k_ghost_fold_y_t(R *buf, int levels, int ny, KernelDesc kd) {
   else lev[((int64_t)(tbeg + j) * kd.nxeff + i) * 3 + d] += lev[((int64_t)(tbeg + j - ny) * kd.nxeff + i) * 3 + d];
 }
 
+// A lane's walk over a particle's stencil items t = lane, lane + 32, ...
+// (t = (k wy + j) wx + i: column (i, j), window level k) without a division
+// per item: two divisions up front, then steps of 32 = qa wx + ra.
+struct StencilWalk {
+  int i, j, k, qa, ra;
+  __device__ __forceinline__ StencilWalk(int lane, int wx, int wy) {
+    const int cols = wx * wy;
+    k = lane / cols;
+    const int c = lane - k * cols;
+    j = c / wx;
+    i = c - j * wx;
+    qa = 32 / wx;
+    ra = 32 - qa * wx;
+  }
+  __device__ __forceinline__ void next(int wx, int wy) {
+    i += ra;
+    j += qa;
+    if (i >= wx) {
+      i -= wx;
+      ++j;
+    }
+    while (j >= wy) {
+      j -= wy;
+      ++k;
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Monopole gather: dl/dF_p = sum phx phy phz psi (S^T, ghost layers from the
 // adjoint ghost buffers) and, with gX, the position gradient
@@ -221,7 +249,7 @@ __global__ void k_ghost_fold_y_t(R *buf, int levels, int ny, KernelDesc kd) {
 // One warp per particle; u is not read without gX.
 // ---------------------------------------------------------------------------
 template <typename R, typename RF>
-__global__ void k_gather_mono(const R *__restrict__ u, const R *__restrict__ psi, int64_t N, KernelDesc kd,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) k_gather_mono(const R *__restrict__ u, const R *__restrict__ psi, int64_t N, KernelDesc kd,
                               GridArgs g, Stencils<R> st, GradStencils<R> gs, Ghosts<R> ghu, Ghosts<R> ghp,
                               const RF *__restrict__ F, const RF *__restrict__ gV, RF *__restrict__ gF,
                               RF *__restrict__ gX) {
@@ -241,13 +269,10 @@ __global__ void k_gather_mono(const R *__restrict__ u, const R *__restrict__ psi
   }
   R s0 = 0, s1 = 0, s2 = 0, x0 = 0, x1 = 0, x2 = 0;
   if (cl.w > 0) {
-    const int cols = kd.wx * kd.wy;
-    const int tot = cols * cl.w;
     const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
-    for (int t = lane; t < tot; t += 32) {
-      const int k = t / cols;
-      const int c = t - k * cols;
-      const int i = c % kd.wx, j = c / kd.wx;
+    StencilWalk sw(lane, kd.wx, kd.wy);
+    for (; sw.k < cl.w; sw.next(kd.wx, kd.wy)) {
+      const int i = sw.i, j = sw.j, k = sw.k;
       const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
       const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
       const int64_t col = (int64_t)wrapi(oy, g.ny) * g.nx + wrapi(ox, g.nx);
@@ -312,7 +337,7 @@ __global__ void k_gather_mono(const R *__restrict__ u, const R *__restrict__ psi
 // first).
 // ---------------------------------------------------------------------------
 template <typename R, typename RF>
-__global__ void k_gather_dip(const R *__restrict__ u, const R *__restrict__ psi, int64_t N, KernelDesc kd,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) k_gather_dip(const R *__restrict__ u, const R *__restrict__ psi, int64_t N, KernelDesc kd,
                              GridArgs g, Stencils<R> st, GradStencils<R> gs, Ghosts<R> ghu, Ghosts<R> ghp,
                              const RF *__restrict__ T, const RF *__restrict__ gW, RF *__restrict__ gT,
                              RF *__restrict__ gX) {
@@ -337,13 +362,10 @@ __global__ void k_gather_dip(const R *__restrict__ u, const R *__restrict__ psi,
   const R half = (R)0.5;
   R s0 = 0, s1 = 0, s2 = 0, x0 = 0, x1 = 0, x2 = 0;
   if (cl.w > 0) {
-    const int cols = kd.wx * kd.wy;
-    const int tot = cols * cl.w;
     const int64_t plane = (int64_t)g.nx * g.ny, comp = plane * g.nz;
-    for (int t = lane; t < tot; t += 32) {
-      const int k = t / cols;
-      const int c = t - k * cols;
-      const int i = c % kd.wx, j = c / kd.wx;
+    StencilWalk sw(lane, kd.wx, kd.wy);
+    for (; sw.k < cl.w; sw.next(kd.wx, kd.wy)) {
+      const int i = sw.i, j = sw.j, k = sw.k;
       const int ox = cl.x + i - kd.wx / 2 + kd.evenx;
       const int oy = cl.y + j - kd.wy / 2 + kd.eveny;
       const int ie = ox + kd.lend, je = oy + kd.bend;

@@ -129,6 +129,7 @@ static KernelHost make_kernel(int w, double beta, double alpha, bool dipole, dou
   d.beta = beta;
   d.alpha = alpha;
   d.alpha2 = alpha * alpha;
+  d.inv_alpha2 = 1.0 / d.alpha2;
   d.norm = es_norm(beta, alpha);
   d.inv_norm3 = 1.0 / (d.norm * d.norm * d.norm);
   d.thr = dipole ? dipole_threshold(beta, alpha) : alpha;
@@ -196,6 +197,7 @@ static KernelHost make_kernel_tp(int w, double beta, double alpha, bool dipole, 
   d.beta = beta;
   d.alpha = alpha;
   d.alpha2 = alpha * alpha;
+  d.inv_alpha2 = 1.0 / d.alpha2;
   d.norm = es_norm(beta, alpha);
   d.inv_norm3 = 1.0 / (d.norm * d.norm * d.norm);
   d.thr = dipole ? dipole_threshold(beta, alpha) : alpha;

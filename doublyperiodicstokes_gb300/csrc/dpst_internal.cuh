@@ -23,6 +23,7 @@ struct KernelDesc {
   int evenz;          // uniform z: 1 for an even z width
   double hz;          // uniform z: grid spacing
   double beta, alpha, alpha2, thr, inv_norm3, norm;
+  double inv_alpha2;  // 1 / alpha2
 };
 
 // Boundary handling of the z ends for one BC set (reference BCs / BCst_z,

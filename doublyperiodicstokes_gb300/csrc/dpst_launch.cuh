@@ -23,6 +23,13 @@ struct EngineBase {
   virtual void backward(const void *F, const void *T, const void *gV, const void *gW, void *gF, void *gT,
                         void *gX, int dtype, cudaStream_t s) = 0;
   float *stage_ms = nullptr;  // set by dpst_mdot_timed for one call
+  // Forward bookkeeping for dpst_mdot_backward_saved: `serial` counts the
+  // calls that change positions or the velocity grid; `grid_serial` is the
+  // serial of the single-column Mdot whose velocity grid (and open-end ghost
+  // layers) the handle still holds, 0 if none; `reuse_forward` is set for
+  // one backward call that takes that grid instead of recomputing it.
+  uint64_t serial = 0, grid_serial = 0;
+  bool reuse_forward = false;
   int device = 0;
   int64_t N = 0;
   dpst_params p;

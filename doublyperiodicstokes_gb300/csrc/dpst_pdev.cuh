@@ -52,10 +52,12 @@ static __device__ __forceinline__ R des1r(double o, const KernelDesc &kd) {
 }
 
 // es_pos_derivs for the mixed operator's FP32 stencils: 1 - o^2/alpha^2 in
-// FP64 (it cancels near the support's edge), the square root, exponential
-// and quotients in FP32.
-static __device__ __forceinline__ void es_pos_derivs_f(double o, double beta, double alpha2, float &g1, float &g2) {
-  const double qd = o * o / alpha2;
+// FP64 (it cancels near the support's edge; o^2 times the FP64 reciprocal
+// 1/alpha^2 rather than an FP64 division, which costs dozens of FP64-pipe
+// instructions), the square root, exponential and quotients in FP32.
+static __device__ __forceinline__ void es_pos_derivs_f(double o, double beta, double alpha2, double inv_alpha2,
+                                                       float &g1, float &g2) {
+  const double qd = o * o * inv_alpha2;
   const double s2d = 1.0 - qd;
   if (!(s2d > 0.0)) {
     g1 = 0.0f;

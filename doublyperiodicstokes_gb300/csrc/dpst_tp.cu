@@ -756,14 +756,26 @@ struct EngineTP : EngineBase {
     if (want_x) {
       launch_locate_grad<R>(false, pos64.as<double>(), N, km.d, nullptr, nullptr, g, stm, gsm, s);
       if (p.has_torque) launch_locate_grad<R>(true, pos64.as<double>(), N, kd.d, nullptr, nullptr, g, std_, gsd, s);
-      spread_stage<RF>(F, T, s);  // the forward's velocity grid, recomputed
-      solve_stage(false, s);
+      if (!reuse_forward) {  // the forward's velocity grid, unless the handle still holds it
+        spread_stage<RF>(F, T, s);
+        solve_stage(false, s);
+      }
     }
     DPST_CUDA(cudaMemsetAsync(g2, 0, grid2.bytes, s));
     Stencils<R> sw = stm;
     sw.phz = stm.phzw;  // the interpolation's weights
-    launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, none, s, perm.as<int>());
-    if (gW) launch_adj_spread_dip<R, RF>(gW, N, kd.d, g, std_, g2, none, s);
+    if (gW && fused) {
+      // J_dip^T gW = 1/2 grad(w) x gW at the interpolation's weights: the
+      // form of the torque spread, and the periodic z map has no ghost
+      // layers, so the fused spread applies it with gW in place of T
+      Stencils<R> swd = std_;
+      swd.phz = std_.phzw;
+      swd.dphz = std_.dphzw;
+      launch_spread_fused<R, RF>(gV, gW, N, km.d, kd.d, g, sw, swd, g2, none, none, s, perm.as<int>());
+    } else {
+      launch_spread<R, RF>(false, gV, N, km.d, g, sw, g2, none, s, perm.as<int>());
+      if (gW) launch_adj_spread_dip<R, RF>(gW, N, kd.d, g, std_, g2, none, s);
+    }
     DPST_CUDA(cudaGetLastError());
     solve_stage(false, s, g2);  // psi
     if (gF || want_x)

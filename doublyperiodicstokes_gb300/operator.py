@@ -237,13 +237,22 @@ class DPStokes:
         return V, W, dict(zip(self.STAGES, list(ms)))
 
     # ---- backward pass -----------------------------------------------------
-    def mdot_backward(self, F, T, gV, gW=None, need_F=True, need_T=False, need_X=True):
+    def forward_serial(self):
+        """Serial of the last single-column mdot whose velocity grid the
+        handle still holds (0 if none); pass it to mdot_backward."""
+        v = ctypes.c_uint64()
+        _lib.check(self.L.dpst_forward_serial(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def mdot_backward(self, F, T, gV, gW=None, need_F=True, need_T=False, need_X=True, forward_serial=0):
         """Vector-Jacobian product of mdot at the current positions.
 
         For l = <gV, V> + <gW, W> with (V, W) = mdot(F, T), returns
         (dl/dF, dl/dT, dl/dX), each [N, 3] or None when not requested.  T is
         the forward call's torques (None if it had none); F is needed only for
-        dl/dX.  The forward's velocity grid is recomputed, not stored."""
+        dl/dX.  The forward's velocity grid is recomputed, unless
+        forward_serial is forward_serial() read right after that mdot and the
+        handle still holds its grid (then F, T must be unchanged since)."""
         gV = self._check_arr(gV, "gV")
         dt = gV.dtype
         args = {}
@@ -262,9 +271,12 @@ class DPStokes:
         def ptr(t):
             return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
 
-        _lib.check(self.L.dpst_mdot_backward(self._h, ptr(args["F"]), ptr(args["T"]), ptr(gV),
-                                             ptr(args["gW"]), ptr(gF), ptr(gT), ptr(gX),
-                                             _dtype_code(gV), _stream_ptr(self.device)))
+        reused = ctypes.c_int(0)
+        _lib.check(self.L.dpst_mdot_backward_saved(self._h, int(forward_serial), ptr(args["F"]), ptr(args["T"]),
+                                                   ptr(gV), ptr(args["gW"]), ptr(gF), ptr(gT), ptr(gX),
+                                                   _dtype_code(gV), _stream_ptr(self.device),
+                                                   ctypes.byref(reused)))
+        self.last_backward_reused = bool(reused.value)
         return gF, gT, gX
 
 

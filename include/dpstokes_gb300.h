@@ -269,7 +269,8 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
  *     created with torques.
  *   - gF, gT, gX may each be NULL (not computed); gT needs T.
  * The velocity grid of the forward is recomputed (spread + solve), not kept
- * from dpst_mdot.  Offsets the forward clamps to the kernel threshold and
+ * from dpst_mdot (dpst_mdot_backward_saved below takes it when the handle
+ * still holds it).  Offsets the forward clamps to the kernel threshold and
  * the stencil's discrete choices (nearest node, z window) have zero
  * derivative; dl/dX is the gradient of the operator between those events.
  * Buffers for the backward pass are allocated on its first call.
@@ -278,6 +279,25 @@ int dpst_mdot_noalloc(dpst_handle h, const void *F, const void *T, void *V, void
  * returns DPST_ERR_UNSUPPORTED. */
 int dpst_mdot_backward(dpst_handle h, const void *F, const void *T, const void *gV, const void *gW,
                        void *gF, void *gT, void *gX, int dtype, void *stream);
+
+/* The serial of the single-column Mdot (dpst_mdot, _host, _timed, _noalloc)
+ * whose velocity grid the handle still holds, 0 if none: every position
+ * update, multi-column Mdot, dpst_spread_grid and recomputing backward call
+ * forgets it.  Read it right after the forward call. */
+int dpst_forward_serial(dpst_handle h, uint64_t *out);
+
+/* dpst_mdot_backward after a known forward: when forward_serial is the
+ * value dpst_forward_serial gave right after the Mdot whose F, T these are,
+ * and the handle still holds that Mdot's velocity grid (no position update
+ * or other grid-writing call since), the position gradient takes that grid
+ * and its open-end ghost layers instead of recomputing them (the spread and
+ * the solve of the forward are skipped); otherwise it recomputes them, as
+ * dpst_mdot_backward does.  *reused (may be NULL) tells which.  The caller
+ * guarantees that F and T are unchanged since that Mdot (autograd's saved
+ * tensors do). */
+int dpst_mdot_backward_saved(dpst_handle h, uint64_t forward_serial, const void *F, const void *T,
+                             const void *gV, const void *gW, void *gF, void *gT, void *gX, int dtype,
+                             void *stream, int *reused);
 
 /* ---- Batched systems (no counterpart in the reference, which runs one
  * system per FCM / DPStokes instance) ------------------------------------

@@ -10,7 +10,12 @@ For l = <gV, V> + <gW, W> with (V, W) = M(X) (F, T):
     the oracle's own forward (which matches the reference to ~1e-15), 1e-10;
   * dl/dX against central differences of the oracle's forward (step 1e-6),
     1e-6 relative (2-norm);
-  * the autograd wrapper against the direct call;
+  * the autograd wrapper against the direct call, taking the forward's
+    velocity grid from the handle (dpst_mdot_backward_saved);
+  * the backward on a held forward grid against the recomputing backward
+    (FP64 1e-13, mixed 5e-6: two runs of FP32 atomics), in every geometry
+    and the triply periodic mode, and the serial's invalidation by position
+    updates and multi-column Mdots;
   * the mixed-precision backward against the FP64 one;
   * the differentiation configuration (bottom wall, N = 8192, 192^2 x 64):
     transpose identity, sampled entries of M^T g from the FP64 forward and
@@ -145,6 +150,7 @@ def test_autograd_matches_direct():
     V, Wv = mdot(op, Xt, Ft, Tt)
     l = (V * _dev(gV)).sum() + (Wv * _dev(gW)).sum()
     l.backward()
+    assert op.last_backward_reused
     dF, dT, dX = _grads(op, X, F, T, gV, gW)
     # equal up to the order of the spreading's atomic sums
     assert rel_err(_np(Ft.grad), dF) < 1e-12
@@ -204,3 +210,47 @@ def test_differentiation_config():
         fd = (vals[0] - vals[1]) / (2 * FD_STEP)
         print("c3 dX[%d,%d] %.10e fd %.10e" % (p, d, gX[p, d], fd))
         assert abs(gX[p, d] - fd) <= 1e-6 * np.abs(gX).max()
+
+
+@pytest.mark.parametrize("name,precision", [("s_dpbw_t", "fp64"), ("s_dp_t", "fp64"), ("s_dpsc_t", "fp64"),
+                                            ("s_dpbw_f_top", "fp64"), ("s_tp_t", "fp64"), ("s_dpbw_t", "mixed"),
+                                            ("s_tp_t", "mixed")])
+def test_backward_on_held_forward_grid(name, precision):
+    w = W.SMALL_BY_NAME[name]
+    X, F, T = W.make_inputs(w)
+    gV, gW = _cotangents(w)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    op = _op(w, precision)
+    op.set_positions(_dev(X))
+    assert op.forward_serial() == 0
+    Fd, Td, gVd, gWd = _dev(F, dt), _dev(T, dt), _dev(gV, dt), _dev(gW, dt)
+    ref = [_np(a) for a in op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=T is not None, need_X=True)]
+    assert not op.last_backward_reused
+    op.mdot(Fd, Td)
+    serial = op.forward_serial()
+    assert serial != 0
+    for _ in range(2):  # the held grid stays valid across backward calls
+        got = [_np(a) for a in op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=T is not None, need_X=True,
+                                                forward_serial=serial)]
+        assert op.last_backward_reused
+        tol = 1e-13 if precision == "fp64" else 5e-6
+        for a, b in zip(got, ref):
+            if b is not None:
+                assert rel_err(a, b) < tol
+    # a position update forgets the held grid; a stale serial recomputes
+    op.set_positions(_dev(X))
+    assert op.forward_serial() == 0
+    got = [_np(a) for a in op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_T=T is not None, need_X=True,
+                                            forward_serial=serial)]
+    assert not op.last_backward_reused
+    assert rel_err(got[-1], ref[-1]) < (1e-13 if precision == "fp64" else 5e-6)
+    # a multi-column Mdot forgets it too
+    op.mdot(Fd, Td)
+    s2 = op.forward_serial()
+    assert s2 > serial
+    Fk = Fd.reshape(1, w.N, 3).repeat(2, 1, 1).contiguous()
+    op.mdot_multi(Fk, Td.reshape(1, w.N, 3).repeat(2, 1, 1).contiguous() if Td is not None else None)
+    assert op.forward_serial() == 0
+    op.mdot_backward(Fd, Td, gVd, gWd, need_F=True, need_X=True, forward_serial=s2)
+    assert not op.last_backward_reused
+    op.close()
