@@ -23,6 +23,7 @@
 #include <map>
 #include <memory>
 #include <numeric>
+#include <string>
 
 #include "dpst_host.cuh"
 
@@ -48,7 +49,7 @@ int bvp_df_variants();
 cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
 template <typename R>
 cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
-                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s, int ncol = 0);
 template <typename R>
 cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
 template <typename R>
@@ -57,6 +58,11 @@ cudaError_t launch_bvp_b(const SysK<R> *sys, int S, const int64_t *mprefix, int6
 template <typename R>
 cudaError_t launch_zgemm_b(const ZSeg<R> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz, const R *Tm,
                            int nsm, cudaStream_t s, bool fold_out);
+int64_t ztc_tiles(int64_t ncols);
+cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                              const float *Tm, bool inverse, int nsm, int *err, cudaStream_t s);
+cudaError_t launch_corr_add_b(const ZSeg<float> *segs, const int64_t *mprefix, int S, int64_t K, int nz, int wall,
+                              cudaStream_t s);
 
 template <typename RP>
 __global__ void k_prep_pos_b(const RP *pos, int64_t N, double zmin, double *out) {
@@ -91,6 +97,13 @@ struct BatchEngine : BatchBase {
   std::vector<int> order;  // systems sorted by (nx, ny)
   // device tables
   DevBuf d_sysp, d_sysk, d_segf, d_segi, d_pprefix, d_ipm, d_ipd, d_mprefix, d_tprefix;
+  // tcgen05 z transform over every system (mixed operator): its tile prefix,
+  // tile count, error word, the choice per direction {forward, inverse} and
+  // the creation-time timings {SIMT, tcgen05} per direction
+  DevBuf d_tprefix_tc, ztc_err, d_segi_nc;  // d_segi_nc: the inverse segments without the wall correction
+  int64_t ntiles_tc = 0;
+  bool ztc_use[2] = {false, false};
+  float ztc_ms[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
   DevBuf d_jobs_m, d_jobs_d, d_jpx_m, d_jpy_m, d_jpx_d, d_jpy_d, d_reach, d_flags;
   int64_t items_m = 0, items_d = 0, ntiles = 0;
   int njobs_m = 0, njobs_d = 0;
@@ -131,6 +144,69 @@ struct BatchEngine : BatchBase {
       DPST_CUDA(launch_bvp_b<R>(d_sysk.as<SysK<R>>(), S, d_mprefix.as<int64_t>(), K, nz, bvp_scratch.as<double>(),
                                 bvp_grid, s));
     }
+  }
+
+  // z transforms of every system in one launch: SIMT (folded) or tcgen05
+  void ztrans(bool inverse, cudaStream_t s) {
+    const ZSeg<R> *segs = (inverse ? d_segi : d_segf).template as<ZSeg<R>>();
+    const R *Tm = (inverse ? Ti : Tf).template as<R>();
+    if constexpr (sizeof(R) == 4) {
+      if (ztc_use[inverse ? 1 : 0]) {
+        // the inverse's wall correction as its own pass (the tcgen05
+        // epilogue's four warps are too few for its arithmetic)
+        const bool walls = inverse && mode != DPST_MODE_NOWALL;
+        const ZSeg<R> *tsegs = walls ? d_segi_nc.template as<ZSeg<R>>() : segs;
+        DPST_CUDA(launch_zgemm_tc_b(reinterpret_cast<const ZSeg<float> *>(tsegs), d_tprefix_tc.as<int64_t>(), S,
+                                    ntiles_tc, nz, reinterpret_cast<const float *>(Tm), inverse, nsm,
+                                    ztc_err.as<int>(), s));
+        if (walls)
+          DPST_CUDA(launch_corr_add_b(reinterpret_cast<const ZSeg<float> *>(segs), d_mprefix.as<int64_t>(), S, K, nz,
+                                      mode, s));
+        return;
+      }
+    }
+    DPST_CUDA(launch_zgemm_b<R>(segs, d_tprefix.as<int64_t>(), S, ntiles, nz, Tm, nsm, s, inverse));
+  }
+
+  // Per direction, the SIMT and tcgen05 transforms are timed on the spectrum
+  // buffer (one warm-up, three runs) and the faster kept; a tcgen05 run whose
+  // waits timed out is never kept.  DPSTOKES_GB300_ZTRANSFORM=simt|tcgen05
+  // forces one.
+  void tune_ztransform() {
+    if (sizeof(R) != 4 || nz > 128) return;
+    ztc_err.alloc(sizeof(int));
+    DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
+    const char *env = getenv("DPSTOKES_GB300_ZTRANSFORM");
+    const std::string want = env ? std::string(env) : std::string();
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+    if (corr.p) DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
+    if (corrf.p) DPST_CUDA(cudaMemset(corrf.p, 0, corrf.bytes));
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    for (int dir = 0; dir < 2; ++dir) {
+      for (int k = 0; k < 2; ++k) {
+        ztc_use[dir] = k == 1;
+        ztrans(dir == 1, 0);
+        DPST_CUDA(cudaEventRecord(a, 0));
+        for (int rep = 0; rep < 3; ++rep) ztrans(dir == 1, 0);
+        DPST_CUDA(cudaEventRecord(b, 0));
+        DPST_CUDA(cudaEventSynchronize(b));
+        DPST_CUDA(cudaEventElapsedTime(&ztc_ms[dir][k], a, b));
+        ztc_ms[dir][k] /= 3.0f;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    int err = 0;
+    DPST_CUDA(cudaMemcpy(&err, ztc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    for (int dir = 0; dir < 2; ++dir) {
+      if (want == "tcgen05") ztc_use[dir] = true;
+      else if (want == "simt") ztc_use[dir] = false;
+      else ztc_use[dir] = ztc_ms[dir][1] < ztc_ms[dir][0];
+      if (err != 0) ztc_use[dir] = false;
+    }
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
   }
 
   // the double-float solve's kernel variant, timed on the spectrum buffer as
@@ -427,8 +503,22 @@ struct BatchEngine : BatchBase {
     upload(d_sysk, sysk_sorted);
     upload(d_mprefix, mprefix);
     upload(d_tprefix, tprefix);
+    {
+      std::vector<int64_t> tp(S + 1, 0);
+      for (int oi = 0; oi < S; ++oi) tp[oi + 1] = tp[oi] + ztc_tiles(segf[oi].ncols);
+      ntiles_tc = tp[S];
+      upload(d_tprefix_tc, tp);
+    }
     upload(d_segf, segf);
     upload(d_segi, segi);
+    {
+      std::vector<ZSeg<R>> nc = segi;
+      for (ZSeg<R> &g : nc) {
+        g.e.corr = nullptr;
+        g.e.corrf = nullptr;
+      }
+      upload(d_segi_nc, nc);
+    }
     size_t bvp_bytes = 0;
     if (dfsolve) {
       DPST_CUDA(bvp_df_plan_b(sysk[0].ks, K, nsm, &bvp_grid, &bvp_bytes));
@@ -437,6 +527,7 @@ struct BatchEngine : BatchBase {
     }
     bvp_scratch.alloc(bvp_bytes);
     if (dfsolve) tune_solve();
+    tune_ztransform();
 
     // ---- particles: stencils, ghost layers, per-system particle tables
     auto total = [&](const std::vector<KernelHost> &kk, int which) {
@@ -664,11 +755,9 @@ struct BatchEngine : BatchBase {
                                        std::to_string(c.grid - grid.as<R>()) + "): cuFFT error " +
                                        std::to_string((int)r));
     }
-    DPST_CUDA(launch_zgemm_b<R>(d_segf.as<ZSeg<R>>(), d_tprefix.as<int64_t>(), S, ntiles, nz, Tf.as<R>(), nsm, s,
-                                false));
+    ztrans(false, s);
     solve(s);
-    DPST_CUDA(launch_zgemm_b<R>(d_segi.as<ZSeg<R>>(), d_tprefix.as<int64_t>(), S, ntiles, nz, Ti.as<R>(), nsm, s,
-                                true));
+    ztrans(true, s);
     for (FftClass &c : classes) {
       DPST_CUFFT(cufftSetStream(c.b, s));
       if (sizeof(R) == 8)
@@ -740,8 +829,15 @@ struct BatchEngine : BatchBase {
     o->n_modes = K;
     o->kernels_per_mdot = kernels_per_mdot;
     o->fft_plans = 2 * (int)classes.size();
+    o->ztransform = ztc_use[0] ? 1 : 0;
+    o->ztransform_inverse = ztc_use[1] ? 1 : 0;
+    for (int k = 0; k < 2; ++k) {
+      o->ztransform_ms[k] = ztc_ms[0][k];
+      o->ztransform_inverse_ms[k] = ztc_ms[1][k];
+    }
     int64_t bytes = 0;
     const DevBuf *all[] = {&d_sysp, &d_sysk, &d_segf, &d_segi, &d_pprefix, &d_ipm, &d_ipd, &d_mprefix, &d_tprefix,
+                           &d_tprefix_tc, &ztc_err, &d_segi_nc,
                            &d_jobs_m, &d_jobs_d, &grid, &spec, &corr, &zext, &wext, &zn, &bands, &bcrows, &k0rows,
                            &Tf, &Ti, &kvs, &f_mf, &f_bk, &f_ab, &f_g, &st_cell_m, &st_x_m, &st_y_m, &st_z_m,
                            &st_zw_m, &st_cell_d, &st_x_d, &st_y_d, &st_z_d, &st_zw_d, &st_dx_d, &st_dy_d,

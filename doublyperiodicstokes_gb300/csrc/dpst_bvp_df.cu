@@ -130,7 +130,7 @@ constexpr int DF_MAXT = 416;  // the most threads of any variant
 // Solve of wavenumber i by the quad of lanes this lane belongs to.
 template <typename R, bool WALLS, typename CFG>
 static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__ spec, double2 *__restrict__ corr,
-                                                int i, bool store, const DfCtx &c) {
+                                                float2 *__restrict__ corrf, int i, bool store, const DfCtx &c) {
   const int nz = a.nz;
   const int nk = (int)a.nk;  // nz * nk * 4 < 2^31 is checked at creation
   const int lane = threadIdx.x & 31;
@@ -371,8 +371,8 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
   double *crd = reinterpret_cast<double *>(corr + i * 16);
   if (a.mode == 1) {
     for (int q = 0; q < 3; ++q) crd[2 * q + part] = -wbd[q];
-    if (a.corrf)
-      for (int q = 0; q < 3; ++q) reinterpret_cast<float *>(a.corrf + i * 16)[2 * q + part] = (float)(-wbd[q]);
+    if (corrf)
+      for (int q = 0; q < 3; ++q) reinterpret_cast<float *>(corrf + i * 16)[2 * q + part] = (float)(-wbd[q]);
   } else if (a.mode == 2 && part == 0) {
     const double kx = __ldg(a.kvx + ix), ky = __ldg(a.kvy + iy);
     double2 fb[3], ft[3], cf[8];
@@ -382,8 +382,8 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
     }
     slit_coeffs(kx, ky, a.Lz, a.eta, fb, ft, cf);
     for (int r = 0; r < 8; ++r) corr[i * 16 + r] = cf[r];
-    if (a.corrf)
-      for (int r = 0; r < 8; ++r) a.corrf[i * 16 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
+    if (corrf)
+      for (int r = 0; r < 8; ++r) corrf[i * 16 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
     double kxp, kyp;
     if (!mode_is_hermitian(a, ix, iy, kx, ky, kxp, kyp)) {
       for (int q = 0; q < 3; ++q) {
@@ -392,8 +392,8 @@ static __device__ __forceinline__ void dfs_mode(const KsArgs &a, R *__restrict__
       }
       slit_coeffs(kxp, kyp, a.Lz, a.eta, fb, ft, cf);
       for (int r = 0; r < 8; ++r) corr[i * 16 + 8 + r] = cf[r];
-      if (a.corrf)
-        for (int r = 0; r < 8; ++r) a.corrf[i * 16 + 8 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
+      if (corrf)
+        for (int r = 0; r < 8; ++r) corrf[i * 16 + 8 + r] = make_float2((float)cf[r].x, (float)cf[r].y);
     }
   }
 #undef XS
@@ -404,7 +404,11 @@ cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scrat
                           cudaStream_t s);
 template <typename R>
 cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
-                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s, int ncol = 0);
+template <typename R>
+cudaError_t launch_bvp_df_cols(const KsArgs &a, R *spec0, int64_t sstride, double2 *corr0, float2 *corrf0,
+                               int64_t cstride, int ncol, float2 *scratch, int64_t grid, int variant,
+                               cudaStream_t s);
 
 // Persistent kernel: CTA b owns the units of 8 wavenumbers [b per_cta,
 // (b+1) per_cta) and its warps take them from a shared-memory counter.
@@ -472,17 +476,19 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df(KsArgs a, R *__restrict
     const int i_raw = u * 8 + (lane >> 2);
     const int i = i_raw < nk ? i_raw : nk - 1;
     const bool store = (i_raw < nk) && (i != 0);  // mode 0: k_bvp_k0
-    dfs_mode<R, WALLS, CFG>(a, spec, corr, i, store, c);
+    dfs_mode<R, WALLS, CFG>(a, spec, corr, a.corrf, i, store, c);
   }
 }
 
-// Batched systems (or the columns of a multi-RHS Mdot): units of 8
-// consecutive modes of the concatenated systems; a quad finds its system by
-// binary search (all systems share nz, H and the geometry).
+// Batched systems: units of 8 consecutive modes of the concatenated
+// systems; a quad finds its system by binary search (all systems share nz,
+// H and the geometry).  ncol > 0: the S systems are columns of one system,
+// their modes interleaved wavenumber-major (k_bvp_df_cols does this with the
+// system's arguments in the parameter space, which is faster).
 template <typename R, bool WALLS, typename CFG>
 __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df_b(const SysK<R> *__restrict__ sys, int S,
                                                            const int64_t *__restrict__ mprefix,
-                                                           float2 *__restrict__ cp_scratch, int per_cta) {
+                                                           float2 *__restrict__ cp_scratch, int per_cta, int ncol) {
   extern __shared__ float2 dfs_cols[];
   __shared__ int next_unit;
   dfs_tables(sys[0].ks);
@@ -500,11 +506,53 @@ __global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df_b(const SysK<R> *__rest
     if (u >= u_end) break;
     const int64_t g_raw = (int64_t)u * 8 + (lane >> 2);
     const int64_t g = g_raw < K ? g_raw : K - 1;
-    const int s = find_sys(mprefix, S, g);
+    int s, i;
+    if (ncol > 0) {
+      s = (int)(g % ncol);
+      i = (int)(g / ncol);
+    } else {
+      s = find_sys(mprefix, S, g);
+      i = (int)(g - mprefix[s]);
+    }
     const SysK<R> &y = sys[s];
-    const int i = (int)(g - mprefix[s]);
     const bool store = (g_raw < K) && (i != 0);  // mode 0 of each system: k_bvp_k0_b
-    dfs_mode<R, WALLS, CFG>(y.ks, y.spec, y.corr, i, store, c);
+    dfs_mode<R, WALLS, CFG>(y.ks, y.spec, y.corr, y.ks.corrf, i, store, c);
+  }
+}
+
+// The K columns of a multi-RHS Mdot (one system: the same wavenumbers and
+// factors; spectra, wall coefficients and their FP32 copies at fixed
+// strides per column): mode g is column g % ncol of wavenumber g / ncol, so
+// the quads of one warp that solve one wavenumber's columns share its factor
+// reads, and the system's arguments stay in the parameter space.
+template <typename R, bool WALLS, typename CFG>
+__global__ void __launch_bounds__(CFG::MAXT, 1) k_bvp_df_cols(KsArgs a, R *__restrict__ spec0, int64_t sstride,
+                                                              double2 *__restrict__ corr0,
+                                                              float2 *__restrict__ corrf0, int64_t cstride,
+                                                              int ncol, float2 *__restrict__ cp_scratch,
+                                                              int per_cta) {
+  extern __shared__ float2 dfs_cols[];
+  __shared__ int next_unit;
+  dfs_tables(a);
+  if (threadIdx.x == 0) next_unit = blockIdx.x * per_cta;
+  __syncthreads();
+  const DfCtx c = dfs_ctx(dfs_cols, cp_scratch);
+  const int64_t K = a.nk * ncol;
+  const int units = (int)((K + 7) / 8);
+  const int u_end = min((int)(blockIdx.x + 1) * per_cta, units);
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&next_unit, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= u_end) break;
+    const int64_t g_raw = (int64_t)u * 8 + (lane >> 2);
+    const int64_t g = g_raw < K ? g_raw : K - 1;
+    const int col = (int)(g % ncol);
+    const int i = (int)(g / ncol);
+    const bool store = (g_raw < K) && (i != 0);  // mode 0 of each column: k_bvp_k0_b
+    dfs_mode<R, WALLS, CFG>(a, spec0 + col * sstride, corr0 ? corr0 + col * cstride : nullptr,
+                            corrf0 ? corrf0 + col * cstride : nullptr, i, store, c);
   }
 }
 
@@ -792,6 +840,8 @@ static cudaError_t df_setup(int nz) {
   const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
   cudaError_t err = cudaFuncSetAttribute(k_bvp_df<R, WALLS, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
+  if (err == cudaSuccess)
+    err = cudaFuncSetAttribute(k_bvp_df_cols<R, WALLS, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   int per_sm = 0;
   err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bvp_df<R, WALLS, CFG>, nt, smem);
@@ -863,31 +913,33 @@ cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, s
 
 template <typename CFG, typename R>
 static cudaError_t df_launch_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
-                               float2 *scratch, int64_t grid, cudaStream_t s) {
+                               float2 *scratch, int64_t grid, int ncol, cudaStream_t s) {
   const int nt = bvp_df_threads(nz, CFG::MAXT);
   const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
   const int64_t units = (K + 7) / 8;
   const int per_cta = (int)((units + grid - 1) / grid);
-  if (mode != 0) k_bvp_df_b<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta);
-  else k_bvp_df_b<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta);
+  if (mode != 0)
+    k_bvp_df_b<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta, ncol);
+  else k_bvp_df_b<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(sys, S, mprefix, scratch, per_cta, ncol);
   return cudaGetLastError();
 }
 
 template <>
 cudaError_t launch_bvp_df_b<float>(const SysK<float> *sys, int S, const int64_t *mprefix, int64_t K, int nz,
-                                   int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s) {
+                                   int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s, int ncol) {
   switch (variant) {
-    case 0: return df_launch_b<DfV0>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
-    case 2: return df_launch_b<DfV2>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
-    case 3: return df_launch_b<DfV3>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
-    default: return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+    case 0: return df_launch_b<DfV0>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
+    case 2: return df_launch_b<DfV2>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
+    case 3: return df_launch_b<DfV3>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
+    default: return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
   }
 }
 template <>
 cudaError_t launch_bvp_df_b<double>(const SysK<double> *sys, int S, const int64_t *mprefix, int64_t K, int nz,
-                                    int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s) {
+                                    int mode, float2 *scratch, int64_t grid, int variant, cudaStream_t s,
+                                    int ncol) {
   (void)variant;
-  return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, s);
+  return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
 }
 
 // The adjoint: the forward plan's grid, twice its scratch (cp_bar, dp_bar).
@@ -928,6 +980,44 @@ static cudaError_t df_launch(const KsArgs &a, R *spec, double2 *corr, float2 *sc
   if (a.mode != 0) k_bvp_df<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
   else k_bvp_df<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec, corr, scratch, per_cta);
   return cudaGetLastError();
+}
+
+template <typename CFG, typename R>
+static cudaError_t df_launch_cols(const KsArgs &a, R *spec0, int64_t sstride, double2 *corr0, float2 *corrf0,
+                                  int64_t cstride, int ncol, float2 *scratch, int64_t grid, cudaStream_t s) {
+  const int nt = bvp_df_threads(a.nz, CFG::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
+  const int64_t units = (a.nk * ncol + 7) / 8;
+  const int per_cta = (int)((units + grid - 1) / grid);
+  if (a.mode != 0)
+    k_bvp_df_cols<R, true, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec0, sstride, corr0, corrf0, cstride, ncol,
+                                                                   scratch, per_cta);
+  else
+    k_bvp_df_cols<R, false, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec0, sstride, corr0, corrf0, cstride, ncol,
+                                                                    scratch, per_cta);
+  return cudaGetLastError();
+}
+
+// ncol columns of one system (multi-RHS): spectra spec0 + c sstride (R
+// elements), wall coefficients corr0 / corrf0 + c cstride; grid and scratch
+// from bvp_df_plan_b over ncol nk modes.
+template <>
+cudaError_t launch_bvp_df_cols<float>(const KsArgs &a, float *spec0, int64_t sstride, double2 *corr0, float2 *corrf0,
+                                      int64_t cstride, int ncol, float2 *scratch, int64_t grid, int variant,
+                                      cudaStream_t s) {
+  switch (variant) {
+    case 0: return df_launch_cols<DfV0>(a, spec0, sstride, corr0, corrf0, cstride, ncol, scratch, grid, s);
+    case 2: return df_launch_cols<DfV2>(a, spec0, sstride, corr0, corrf0, cstride, ncol, scratch, grid, s);
+    case 3: return df_launch_cols<DfV3>(a, spec0, sstride, corr0, corrf0, cstride, ncol, scratch, grid, s);
+    default: return df_launch_cols<DfV1>(a, spec0, sstride, corr0, corrf0, cstride, ncol, scratch, grid, s);
+  }
+}
+template <>
+cudaError_t launch_bvp_df_cols<double>(const KsArgs &a, double *spec0, int64_t sstride, double2 *corr0,
+                                       float2 *corrf0, int64_t cstride, int ncol, float2 *scratch, int64_t grid,
+                                       int variant, cudaStream_t s) {
+  (void)variant;
+  return df_launch_cols<DfV1>(a, spec0, sstride, corr0, corrf0, cstride, ncol, scratch, grid, s);
 }
 
 // variant in [0, bvp_df_variants()); the FP64-I/O instantiation (R = double,

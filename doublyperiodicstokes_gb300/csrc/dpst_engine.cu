@@ -66,7 +66,11 @@ cudaError_t launch_bvp_df(const KsArgs &a, R *spec, double2 *corr, float2 *scrat
 cudaError_t bvp_df_plan_b(const KsArgs &a0, int64_t K, int nsm, int64_t *grid, size_t *scratch_bytes);
 template <typename R>
 cudaError_t launch_bvp_df_b(const SysK<R> *sys, int S, const int64_t *mprefix, int64_t K, int nz, int mode,
-                            float2 *scratch, int64_t grid, int variant, cudaStream_t s);
+                            float2 *scratch, int64_t grid, int variant, cudaStream_t s, int ncol = 0);
+template <typename R>
+cudaError_t launch_bvp_df_cols(const KsArgs &a, R *spec0, int64_t sstride, double2 *corr0, float2 *corrf0,
+                               int64_t cstride, int ncol, float2 *scratch, int64_t grid, int variant,
+                               cudaStream_t s);
 template <typename R>
 cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
 // double-float adjoint solve (dpst_bvp_df.cu) and the FP64 k = 0 adjoint
@@ -105,6 +109,7 @@ cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiA
 // tensor-core z transform of the mixed operator (dpst_ztc.cu)
 cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
                             int *err, cudaStream_t s);
+cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s);
 // backward pass (dpst_adjoint.cu, dpst_grad.cu)
 template <typename R>
 cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
@@ -628,9 +633,21 @@ struct Engine : EngineBase {
   // impl < 0: the tuned kernel for e's direction
   cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl = -1) {
     if (impl < 0) impl = ztc[e.inverse ? 1 : 0];
-    if (impl == 1 && sizeof(R) == 4)
+    if (impl == 1 && sizeof(R) == 4) {
+      if (e.inverse && e.ks.mode != 0 && e.corr != nullptr) {
+        // the wall correction as its own pass: the tcgen05 epilogue's four
+        // warps are too few for its arithmetic
+        EpiArgs e2 = e;
+        e2.corr = nullptr;
+        e2.corrf = nullptr;
+        cudaError_t r = launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk,
+                                        reinterpret_cast<const float *>(T), e2, nsm, ztc_err.as<int>(), s);
+        if (r == cudaSuccess) r = launch_corr_add(reinterpret_cast<float *>(sp), nz, nk, e, s);
+        return r;
+      }
       return launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk, reinterpret_cast<const float *>(T), e, nsm,
                              ztc_err.as<int>(), s);
+    }
     return launch_zgemm<R>(sp, nz, 2 * nk, T, e, nsm, s, fold_out);
   }
 
@@ -989,8 +1006,11 @@ struct Engine : EngineBase {
     ef.ks = ks;
     for (int k = 0; k < K; ++k) DPST_CUDA(zgemm((R *)(sK + k * scol), Tf.as<R>(), ef, false, s));
     if (dfsolve) {
-      DPST_CUDA(launch_bvp_df_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz, p.mode,
-                                   bvpK_scratch.as<float2>(), bvpK_grid, df_variant, s));
+      // the K columns' modes interleaved wavenumber-major (shared factor reads)
+      DPST_CUDA(launch_bvp_df_cols<R>(ks, reinterpret_cast<R *>(sK), 2 * (int64_t)scol,
+                                      corr.p ? corrK.as<double2>() : nullptr,
+                                      corrf.p ? corrfK.as<float2>() : nullptr, 16 * (int64_t)nk, K,
+                                      bvpK_scratch.as<float2>(), bvpK_grid, df_variant, s));
       DPST_CUDA(launch_bvp_k0_b<R>(sysK.as<SysK<R>>(), K, s));
     } else {
       DPST_CUDA(launch_bvp_b<R>(sysK.as<SysK<R>>(), K, mprefK.as<int64_t>(), (int64_t)K * nk, nz,
@@ -1257,6 +1277,7 @@ struct Engine : EngineBase {
     o->xy_ms[0] = xy_ms[0];
     o->xy_ms[1] = xy_ms[1];
     if (ownfft) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
+    if (sizeof(R) == 4 && ztc[1] && p.mode != DPST_MODE_NOWALL) o->kernels_per_mdot += 1;  // correction pass
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;
     const DevBuf *all[] = {&bvp_scratch, &grid, &spec, &corr, &zext, &wext, &kvx, &kvy, &zn, &bands, &bcrows,

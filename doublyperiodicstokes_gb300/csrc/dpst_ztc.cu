@@ -157,10 +157,59 @@ size_t ztc_smem_bytes(int nz) {
   const int kp = (nz + 7) & ~7;
   return ztc_off_bar(kp) + ZTC_NBARS * 8 + 16;
 }
+// batched: after the single-system layout, one EpiArgs per epilogue warp
+// (the tile's segment's epilogue arguments, copied from global memory)
+static __host__ __device__ constexpr size_t ztc_off_epi(int kp) {
+  return (ztc_off_bar(kp) + ZTC_NBARS * 8 + 16 + 15) & ~(size_t)15;
+}
+static size_t ztc_smem_bytes_b(int nz) {
+  const int kp = (nz + 7) & ~7;
+  return ztc_off_epi(kp) + ZTC_EPI_WARPS * sizeof(EpiArgs);
+}
 
-template <bool INVERSE>
+// A tile's data: its spectrum component block B ([nz][ncols] real columns),
+// the component d, the first column, and the epilogue arguments.  BATCH: the
+// tiles of the S segments (systems) are numbered by the prefix `tprefix` of
+// 3 ceil(ncols_s / ZTC_N) tiles each; the segment is found by binary search.
+struct ZtcTile {
+  float *B;
+  int64_t ncols, col0;
+  int d, seg;
+};
+
+template <bool BATCH>
+static __device__ __forceinline__ ZtcTile ztc_tile(int64_t t, float *spec, int nz, int64_t ncols,
+                                                   const ZSeg<float> *__restrict__ segs,
+                                                   const int64_t *__restrict__ tprefix, int S) {
+  ZtcTile z;
+  int64_t tl = t;
+  z.seg = 0;
+  if (BATCH) {
+    int lo = 0, hi = S - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tprefix[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    z.seg = lo;
+    tl = t - tprefix[lo];
+    spec = segs[lo].spec;
+    ncols = segs[lo].ncols;
+  }
+  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;
+  z.d = (int)(tl / tpc);
+  z.col0 = (tl % tpc) * ZTC_N;
+  z.ncols = ncols;
+  z.B = spec + (int64_t)z.d * nz * ncols;
+  return z;
+}
+
+template <bool INVERSE, bool BATCH>
 __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz, int64_t ncols,
-                                                             const float *__restrict__ Tm, EpiArgs e, int *err) {
+                                                             const float *__restrict__ Tm, EpiArgs e, int *err,
+                                                             const ZSeg<float> *__restrict__ segs,
+                                                             const int64_t *__restrict__ tprefix, int S,
+                                                             int64_t ntiles_b) {
   extern __shared__ __align__(1024) unsigned char ztc_sm[];
   const int kp = (nz + 7) & ~7;  // K padded to the MMA step
   const int kq = kp / 4;         // core matrices along K
@@ -211,8 +260,7 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  const int64_t tiles_per_comp = (ncols + ZTC_N - 1) / ZTC_N;
-  const int64_t ntiles = 3 * tiles_per_comp;
+  const int64_t ntiles = BATCH ? ntiles_b : 3 * ((ncols + ZTC_N - 1) / ZTC_N);
   const int64_t G = gridDim.x;
   const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
   const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
@@ -223,20 +271,28 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
     // ---- producers: column n, row quads q = qg + ZTC_PGROUPS i of the chunk
     const int n = tid % ZTC_N, qg = tid / ZTC_N;
     float b0[ZTC_QPT][4], b1[ZTC_QPT][4], b2[ZTC_QPT][4];
+    int cur_j = -1;  // the tile whose data `cur` holds (steps come in increasing order)
+    ZtcTile cur;
+    cur.B = spec;
+    cur.ncols = ncols;
+    cur.col0 = 0;
     auto load_step = [&](int u, float (&br)[ZTC_QPT][4]) {
       const bool valid = u < my_steps;
       const int j = valid ? u / nkc : 0, c = valid ? u - j * nkc : 0;
-      const int64_t t = blockIdx.x + (int64_t)j * G;
-      const int d = valid ? (int)(t / tiles_per_comp) : 0;
-      const int64_t col = valid ? (t % tiles_per_comp) * ZTC_N + n : 0;
-      const float *B = spec + (int64_t)d * nz * ncols;
+      if (valid && j != cur_j) {
+        cur = ztc_tile<BATCH>(blockIdx.x + (int64_t)j * G, spec, nz, ncols, segs, tprefix, S);
+        cur_j = j;
+      }
+      const int64_t col = valid ? cur.col0 + n : 0;
+      const float *B = cur.B;
+      const int64_t nc = cur.ncols;
 #pragma unroll
       for (int i = 0; i < ZTC_QPT; ++i) {
         const int q = qg + ZTC_PGROUPS * i;
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
           const int k = ZTC_KC * c + 4 * q + jj;
-          br[i][jj] = (valid && k < nz && col < ncols) ? __ldcs(B + (int64_t)k * ncols + col) : 0.0f;
+          br[i][jj] = (valid && k < nz && col < nc) ? __ldcs(B + (int64_t)k * nc + col) : 0.0f;
         }
       }
     };
@@ -281,9 +337,8 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
     // tcgen05.ld is in flight while the current block is stored.
     const int qd = warp & 3;
     float *st = stg + (size_t)(warp - ZTC_PROD_WARPS) * 32 * ZTC_STG;
-    const bool v4 = (ncols & 3) == 0;  // 16-byte aligned rows
-    const bool corr = INVERSE && e.ks.mode != 0 && e.corr != nullptr;
-    const float scale = INVERSE ? (float)e.scale : 1.0f;
+    EpiArgs *eslot = reinterpret_cast<EpiArgs *>(ztc_sm + ztc_off_epi(kp)) + (warp - ZTC_PROD_WARPS);
+    int eseg = -1;  // the segment whose arguments eslot holds
     uint32_t v[32];
     auto tmem_ld = [&](uint32_t taddr) {
       asm volatile(
@@ -303,7 +358,21 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
       if (!__all_sync(0xffffffffu, ok)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
       const int64_t t = blockIdx.x + (int64_t)j * G;
-      const int d = (int)(t / tiles_per_comp);
+      const ZtcTile zt = ztc_tile<BATCH>(t, spec, nz, ncols, segs, tprefix, S);
+      const int d = zt.d;
+      const int64_t ncols_t = zt.ncols;
+      if (BATCH && zt.seg != eseg) {
+        // the segment's epilogue arguments into this warp's shared slot
+        const int *src = reinterpret_cast<const int *>(&segs[zt.seg].e);
+        int *dst = reinterpret_cast<int *>(eslot);
+        for (int w = lane; w < (int)(sizeof(EpiArgs) / 4); w += 32) dst[w] = src[w];
+        __syncwarp();
+        eseg = zt.seg;
+      }
+      const EpiArgs &et = BATCH ? *eslot : e;
+      const bool v4 = (ncols_t & 3) == 0;  // 16-byte aligned rows
+      const bool corr = INVERSE && et.ks.mode != 0 && et.corr != nullptr;
+      const float scale = INVERSE ? (float)et.scale : 1.0f;
       const uint32_t tbase = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * ZTC_N);
       tmem_ld(tbase);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -317,17 +386,17 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
         __syncwarp();
         if (sb + 1 < ZTC_N / 32) tmem_ld(tbase + (uint32_t)(32 * (sb + 1)));
         // 4 rows x 128 B per store instruction
-        const int64_t col = (t % tiles_per_comp) * ZTC_N + 32 * sb + 4 * (lane & 7);
+        const int64_t col = zt.col0 + 32 * sb + 4 * (lane & 7);
 #pragma unroll 4
         for (int i = 0; i < 8; ++i) {
           const int rl = 4 * i + (lane >> 3);
           const int r = 32 * qd + rl;
-          if (r < nz && col < ncols) {
+          if (r < nz && col < ncols_t) {
             float4 q = *reinterpret_cast<const float4 *>(st + rl * ZTC_STG + 4 * (lane & 7));
             if (corr) {
               float c0r, c0i, c1r, c1i;
-              corr_any<float>(e, d, r, col >> 1, c0r, c0i);
-              if (col + 2 < ncols) corr_any<float>(e, d, r, (col >> 1) + 1, c1r, c1i);
+              corr_any<float>(et, d, r, col >> 1, c0r, c0i);
+              if (col + 2 < ncols_t) corr_any<float>(et, d, r, (col >> 1) + 1, c1r, c1i);
               else c1r = c1i = 0.0f;
               q.x += c0r;
               q.y += c0i;
@@ -340,12 +409,12 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
               q.z *= scale;
               q.w *= scale;
             }
-            float *g = spec + ((int64_t)d * nz + r) * ncols + col;
+            float *g = zt.B + (int64_t)r * ncols_t + col;
             if (v4) {
               __stcs(reinterpret_cast<float4 *>(g), q);
             } else {
               __stcs(reinterpret_cast<float2 *>(g), make_float2(q.x, q.y));
-              if (col + 2 < ncols) __stcs(reinterpret_cast<float2 *>(g + 2), make_float2(q.z, q.w));
+              if (col + 2 < ncols_t) __stcs(reinterpret_cast<float2 *>(g + 2), make_float2(q.z, q.w));
             }
           }
         }
@@ -406,26 +475,205 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
   }
 }
 
-cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
-                            int *err, cudaStream_t s) {
+template <bool BATCH>
+static cudaError_t ztc_launch(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
+                              const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, bool inverse,
+                              cudaStream_t s) {
   if (nz > 128) return cudaErrorInvalidValue;
-  const size_t smem = ztc_smem_bytes(nz);
+  const size_t smem = BATCH ? ztc_smem_bytes_b(nz) : ztc_smem_bytes(nz);
   cudaError_t r;
-  if (e.inverse) r = cudaFuncSetAttribute(k_zgemm_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  else r = cudaFuncSetAttribute(k_zgemm_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (inverse)
+    r = cudaFuncSetAttribute(k_zgemm_tc<true, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  else r = cudaFuncSetAttribute(k_zgemm_tc<false, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (r != cudaSuccess) return r;
-  const int64_t ntiles = 3 * ((ncols + ZTC_N - 1) / ZTC_N);
   int per_sm = 0;
-  if (e.inverse) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<true>, ZTC_THREADS, smem);
-  else r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<false>, ZTC_THREADS, smem);
+  if (inverse)
+    r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<true, BATCH>, ZTC_THREADS, smem);
+  else r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<false, BATCH>, ZTC_THREADS, smem);
   if (r != cudaSuccess) return r;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (per_sm > 2) per_sm = 2;  // 2 x 256 tensor-memory columns: allocation never waits
   int64_t grid = (int64_t)nsm * per_sm;
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return cudaSuccess;
-  if (e.inverse) k_zgemm_tc<true><<<(unsigned)grid, ZTC_THREADS, smem, s>>>(spec, nz, ncols, Tm, e, err);
-  else k_zgemm_tc<false><<<(unsigned)grid, ZTC_THREADS, smem, s>>>(spec, nz, ncols, Tm, e, err);
+  if (inverse)
+    k_zgemm_tc<true, BATCH><<<(unsigned)grid, ZTC_THREADS, smem, s>>>(spec, nz, ncols, Tm, e, err, segs, tprefix, S,
+                                                                      ntiles);
+  else
+    k_zgemm_tc<false, BATCH><<<(unsigned)grid, ZTC_THREADS, smem, s>>>(spec, nz, ncols, Tm, e, err, segs, tprefix, S,
+                                                                       ntiles);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
+                            int *err, cudaStream_t s) {
+  const int64_t ntiles = 3 * ((ncols + ZTC_N - 1) / ZTC_N);
+  return ztc_launch<false>(spec, nz, ncols, Tm, e, nsm, err, nullptr, nullptr, 0, ntiles, e.inverse != 0, s);
+}
+
+// Batched systems: one launch over the tiles of every segment (system);
+// tprefix: S + 1 prefix counts of 3 ceil(ncols_s / 128) tiles, in device
+// memory, ntiles = tprefix[S].  Segments share nz and T.
+int64_t ztc_tiles(int64_t ncols) { return 3 * ((ncols + ZTC_N - 1) / ZTC_N); }
+cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                              const float *Tm, bool inverse, int nsm, int *err, cudaStream_t s) {
+  EpiArgs e;
+  memset(&e, 0, sizeof(e));
+  e.inverse = inverse ? 1 : 0;
+  return ztc_launch<true>(nullptr, nz, 0, Tm, e, nsm, err, segs, tprefix, S, ntiles, inverse, s);
+}
+
+// ---------------------------------------------------------------------------
+// The wall correction as its own pass after an inverse z transform run
+// without it: spec[d][m][mode] += corr_d(z_m, mode) scale for every
+// component d and node m, one thread per mode (its coefficients read once,
+// the node loop in the thread; consecutive threads take consecutive modes,
+// so every access of a node row is coalesced).  The tcgen05 kernel's
+// epilogue has only four warps per CTA for this arithmetic; the pass
+// spreads it over the whole GPU.  BATCH: modes of the S segments by their
+// prefix mprefix (nk_s each); ks.mode == 0 or corr == nullptr: nothing.
+// ---------------------------------------------------------------------------
+// WM: 1 bottom wall (three coefficients per mode), 2 slit (eight per pass).
+// Threads: K modes x ceil(nz / CORR_NODES) node blocks (consecutive threads,
+// consecutive modes of one node block).
+constexpr int CORR_NODES = 16;
+template <bool BATCH, int WM>
+__global__ void __launch_bounds__(128) k_corr_add(float *spec, int nz, int64_t nk, EpiArgs e,
+                                                  const ZSeg<float> *__restrict__ segs,
+                                                  const int64_t *__restrict__ mprefix, int S, int64_t K) {
+  const int64_t tt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int nblk = (nz + CORR_NODES - 1) / CORR_NODES;
+  if (tt >= K * nblk) return;
+  const int64_t t = tt % K;
+  const int m_beg = (int)(tt / K) * CORR_NODES, m_end = min(m_beg + CORR_NODES, nz);
+  int64_t mode = t;
+  const EpiArgs *ep = &e;
+  if (BATCH) {
+    int lo = 0, hi = S - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (mprefix[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    mode = t - mprefix[lo];
+    ep = &segs[lo].e;
+    spec = segs[lo].spec;
+    nk = segs[lo].ncols / 2;
+  }
+  const EpiArgs &ea = *ep;
+  if (ea.corr == nullptr || mode == 0) return;
+  const float scale = (float)ea.scale;
+  float2 *__restrict__ g0 = reinterpret_cast<float2 *>(spec) + mode;
+  if (ea.corrf == nullptr) {  // no FP32 tables: the general per-value form
+    for (int d = 0; d < 3; ++d)
+      for (int m = m_beg; m < m_end; ++m) {
+        float re, im;
+        corr_any<float>(ea, d, m, mode, re, im);
+        float2 *g = g0 + ((int64_t)d * nz + m) * nk;
+        float2 v = *g;
+        v.x += re * scale;
+        v.y += im * scale;
+        *g = v;
+      }
+    return;
+  }
+  // corr_value_f for the three components at once, the mode's table entries
+  // read once into registers, four nodes' values loaded ahead of their update
+  typedef float CT;
+  constexpr int NC = WM == 1 ? 3 : 16;
+  const float4 m0 = ea.cmode[2 * mode];
+  const CT k = m0.x;
+  const int npass = m0.w != 0.0f ? 1 : 2;
+  const float4 m1 = npass == 2 ? ea.cmode[2 * mode + 1] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float2 *cr = ea.corrf + mode * 16;
+  const int ncoef = WM == 1 ? 3 : 8 * npass;
+  cplx<CT> c[NC];
+#pragma unroll
+  for (int r = 0; r < NC; ++r) c[r] = r < ncoef ? mk<CT>(cr[r].x, cr[r].y) : mk<CT>(0, 0);
+  const CT fac = ea.fac, Lz = (CT)ea.ks.Lz;
+  const float *__restrict__ znf = ea.znf;
+  const int64_t dstride = (int64_t)nz * nk;
+  constexpr int U = 4;
+  for (int mb = m_beg; mb < m_end; mb += U) {
+    float2 vin[U][3];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        vin[u][d] = (mb + u < m_end) ? g0[d * dstride + (int64_t)(mb + u) * nk] : make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int m = mb + u;
+      if (m >= m_end) break;
+      const CT z = znf[m];
+      const CT enkz = expf(-k * z);
+      const CT zenkz = z * enkz;
+      CT ekzmh = 0, zekzmh = 0;
+      if constexpr (WM != 1) {
+        ekzmh = expf(k * (z - Lz));
+        zekzmh = z * ekzmh;
+      }
+      cplx<CT> acc[3] = {mk<CT>(0, 0), mk<CT>(0, 0), mk<CT>(0, 0)};
+#pragma unroll
+      for (int pass = 0; pass < 2; ++pass) {
+        if (pass >= npass) break;
+        const CT qx = pass ? m1.x : m0.y, qy = pass ? m1.y : m0.z;
+        cplx<CT> v[3];
+        if constexpr (WM == 1) {
+          cplx<CT> f0 = c[0], f1 = c[1], f2 = c[2];
+          if (pass) {
+            f0 = conj(f0);
+            f1 = conj(f1);
+            f2 = conj(f2);
+          }
+          const cplx<CT> al = (qx * f0 + qy * f1) + ik(k, f2);
+          v[0] = (-qx * zenkz / k) * al + enkz * f0;
+          v[1] = (-qy * zenkz / k) * al + enkz * f1;
+          v[2] = ik(-zenkz, al) + enkz * f2;
+        } else {
+          const int o = 8 * pass;
+          v[0] = (ik(-qx * zenkz * fac / k, c[o + 0]) + ik(qx * zekzmh * fac / k, c[o + 1])) +
+                 (enkz * c[o + 2] + ekzmh * c[o + 3]);
+          v[1] = (ik(-qy * zenkz * fac / k, c[o + 0]) + ik(qy * zekzmh * fac / k, c[o + 1])) +
+                 (enkz * c[o + 4] + ekzmh * c[o + 5]);
+          v[2] = ((zenkz * fac) * c[o + 0] + (zekzmh * fac) * c[o + 1]) + (enkz * c[o + 6] + ekzmh * c[o + 7]);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[d] = acc[d] + (pass ? conj(v[d]) : v[d]);
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        if (npass == 2) acc[d] = (CT)0.5 * acc[d];
+        float2 vv = vin[u][d];
+        vv.x += acc[d].x * scale;
+        vv.y += acc[d].y * scale;
+        g0[d * dstride + (int64_t)m * nk] = vv;
+      }
+    }
+  }
+}
+
+cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s) {
+  if (nk <= 0 || e.ks.mode == 0) return cudaSuccess;
+  const int bs = 128;
+  const int64_t nt = nk * ((nz + CORR_NODES - 1) / CORR_NODES);
+  const unsigned nb = (unsigned)((nt + bs - 1) / bs);
+  if (e.ks.mode == 1) k_corr_add<false, 1><<<nb, bs, 0, s>>>(spec, nz, nk, e, nullptr, nullptr, 0, nk);
+  else k_corr_add<false, 2><<<nb, bs, 0, s>>>(spec, nz, nk, e, nullptr, nullptr, 0, nk);
+  return cudaGetLastError();
+}
+
+// wall: the systems' common geometry (1 bottom wall, 2 slit)
+cudaError_t launch_corr_add_b(const ZSeg<float> *segs, const int64_t *mprefix, int S, int64_t K, int nz, int wall,
+                              cudaStream_t s) {
+  if (K <= 0 || wall == 0) return cudaSuccess;
+  EpiArgs e;
+  memset(&e, 0, sizeof(e));
+  const int bs = 128;
+  const int64_t nt = K * ((nz + CORR_NODES - 1) / CORR_NODES);
+  const unsigned nb = (unsigned)((nt + bs - 1) / bs);
+  if (wall == 1) k_corr_add<true, 1><<<nb, bs, 0, s>>>(nullptr, nz, 0, e, segs, mprefix, S, K);
+  else k_corr_add<true, 2><<<nb, bs, 0, s>>>(nullptr, nz, 0, e, segs, mprefix, S, K);
   return cudaGetLastError();
 }
 

@@ -26,19 +26,31 @@ def _inputs(ws, dtype):
     return Xs, Fs, Ts, cat(Xs).double(), cat(Fs), (cat(Ts) if Ts[0] is not None else None)
 
 
-def _single(w, X, F, T, precision, dtype):
-    # the batch's z transform is the SIMT one: compare like with like (the
-    # tensor-core transform differs from it by ~1e-6, covered elsewhere)
-    import os
-    old = os.environ.get("DPSTOKES_GB300_ZTRANSFORM")
-    os.environ["DPSTOKES_GB300_ZTRANSFORM"] = "simt"
-    try:
-        op = DPStokes(StokesParams.from_workload(w, precision), w.N)
-    finally:
-        if old is None:
-            del os.environ["DPSTOKES_GB300_ZTRANSFORM"]
+class _ZTransform:
+    """DPSTOKES_GB300_ZTRANSFORM for the handles created inside: batch and
+    single handles compare like with like (the tensor-core transform differs
+    from the SIMT one by ~1e-6, covered elsewhere)."""
+
+    def __init__(self, which):
+        self.which = which
+
+    def __enter__(self):
+        import os
+        self.old = os.environ.get("DPSTOKES_GB300_ZTRANSFORM")
+        if self.which:
+            os.environ["DPSTOKES_GB300_ZTRANSFORM"] = self.which
+
+    def __exit__(self, *exc):
+        import os
+        if self.old is None:
+            os.environ.pop("DPSTOKES_GB300_ZTRANSFORM", None)
         else:
-            os.environ["DPSTOKES_GB300_ZTRANSFORM"] = old
+            os.environ["DPSTOKES_GB300_ZTRANSFORM"] = self.old
+
+
+def _single(w, X, F, T, precision, dtype, zt="simt"):
+    with _ZTransform(zt):
+        op = DPStokes(StokesParams.from_workload(w, precision), w.N)
     op.set_positions(torch.tensor(X, device="cuda"))
     V, Wv = op.mdot(torch.tensor(F, dtype=dtype, device="cuda"),
                     torch.tensor(T, dtype=dtype, device="cuda") if T is not None else None)
@@ -48,8 +60,9 @@ def _single(w, X, F, T, precision, dtype):
     return out
 
 
-def _run_batch(ws, precision, dtype):
-    b = DPStokesBatch([StokesParams.from_workload(w, precision) for w in ws], [w.N for w in ws])
+def _run_batch(ws, precision, dtype, zt="simt"):
+    with _ZTransform(zt):
+        b = DPStokesBatch([StokesParams.from_workload(w, precision) for w in ws], [w.N for w in ws])
     Xs, Fs, Ts, X, F, T = _inputs(ws, dtype)
     b.set_positions(X)
     V, Wv = b.mdot(F, T)
@@ -112,3 +125,31 @@ def test_batched_c4_sample():
         print("%s N %d n %d: %.2e" % (ws[k].name, ws[k].N, ws[k].nx, e))
         assert e < 1e-6
     b.close()
+
+
+@pytest.mark.parametrize("dom,torque", [("DPBW", True), ("DP", True), ("DPSC", False)])
+def test_batched_tensor_core_ztransform(dom, torque):
+    """The batch's tcgen05 z transform over all systems (one launch, tiles of
+    every system): against single handles on the tcgen05 transform (1e-6),
+    and against the FP64 batch (1e-5); the creation-time choice is reported."""
+    ws = W.small_batch(dom, torque)
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, "mixed", torch.float32, zt="tcgen05")
+    info = b.info()
+    assert info["ztransform"] == 1 and info["ztransform_inverse"] == 1
+    b64, _, _, _, V64, W64 = _run_batch(ws, "fp64", torch.float64)
+    for k, w in enumerate(ws):
+        V1, W1 = _single(w, Xs[k], Fs[k], Ts[k], "mixed", torch.float32, zt="tcgen05")
+        ev = rel_err(Vs[k], V1)
+        ew = rel_err(Ws[k], W1) if torque else 0.0
+        e64 = rel_err(Vs[k], V64[k])
+        print("%s tcgen05 V %.2e W %.2e vs fp64 %.2e" % (w.name, ev, ew, e64))
+        assert ev < 1e-6 and ew < 1e-6 and e64 < 1e-5
+    b.close()
+    b64.close()
+    b2, _, _, _, Va, _ = _run_batch(ws, "mixed", torch.float32, zt=None)
+    info = b2.info()
+    print("auto choice", info["ztransform"], info["ztransform_inverse"], list(info["ztransform_ms"]),
+          list(info["ztransform_inverse_ms"]))
+    for k in range(len(ws)):
+        assert rel_err(Va[k], V64[k]) < 1e-5
+    b2.close()
