@@ -110,6 +110,16 @@ cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiA
 cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
                             int *err, cudaStream_t s);
 cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s);
+bool tile_spread_supported(const KernelDesc &km, const KernelDesc &kd, int nx, int ny, int nz);
+cudaError_t tile_spread_setup(int nz);
+template <typename R>
+void launch_edge_list(int64_t N, const Stencils<R> &sm, const KernelDesc &km, int nz, int *count, int *list,
+                      cudaStream_t s);
+template <typename RF>
+void launch_spread_tiles(const RF *F, const RF *T, const KernelDesc &km, const KernelDesc &kd, const GridArgs &g,
+                         const Stencils<float> &sm, const Stencils<float> &sd, float *grid, const Ghosts<float> &ghm,
+                         const Ghosts<float> &ghd, const int *perm, const int *tstart, const int *edge,
+                         int64_t n_edge, cudaStream_t s);
 // backward pass (dpst_adjoint.cu, dpst_grad.cu)
 template <typename R>
 cudaError_t adj_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
@@ -148,6 +158,12 @@ struct Engine : EngineBase {
   double hx, hy, Lz, H;
   KernelHost km, kd;
   bool fused = false;  // monopole and dipole share one spread and one interpolation pass
+  // tile-owner spread (mixed operator, fused pair): the grid written once per
+  // tile, no clearing, no HBM atomics; edge particles (windows not interior)
+  // from their list with atomics afterwards
+  bool tile_spread = false;
+  DevBuf edge_list;
+  int64_t n_edge = 0;
   bool reg = false;    // torques with the regular kernel and spectral curls (DPST_TORQUE_REG)
   DevBuf gridT, specT; // reg: torque grid and spectrum, then the vorticity's
   GridArgs g;
@@ -209,6 +225,14 @@ struct Engine : EngineBase {
     reg = p.has_torque && p.torque_kernel == DPST_TORQUE_REG;
     if (p.has_torque) kd = make_kernel(p.w_d, p.beta_d, p.alpha_d, !reg, hx, hy, nx, ny, zG, zW, "dipole kernel");
     fused = p.has_torque && !reg && fused_supports(km.d, kd.d);
+    {
+      // measured on c2: 0.45 ms against 0.25 ms for the clear-and-atomics
+      // spread (latency-bound gather phase at two CTAs per SM), so it runs
+      // only when asked for
+      const char *env = getenv("DPSTOKES_GB300_SPREAD");
+      const bool want_tiles = env && std::string(env) == "tiles";
+      tile_spread = sizeof(R) == 4 && fused && want_tiles && tile_spread_supported(km.d, kd.d, nx, ny, nz);
+    }
     km.d.zext_off = 0;
     kd.d.zext_off = (int)km.zext.size();
     std::vector<double> ze = km.zext, we = km.wext;
@@ -341,6 +365,10 @@ struct Engine : EngineBase {
     }
     // particle order by grid tile (set_positions), used by the spread and
     // interpolation kernels
+    if (tile_spread) {
+      DPST_CUDA(tile_spread_setup(nz));
+      edge_list.alloc(sizeof(int) * std::max<int64_t>(N, 1));
+    }
     ord_count.alloc(sizeof(int) * tile_order_tiles(nx, ny));
     ord_start.alloc(sizeof(int) * (tile_order_tiles(nx, ny) + 1));
     perm.alloc(sizeof(int) * std::max<int64_t>(N, 1));
@@ -531,6 +559,7 @@ struct Engine : EngineBase {
     DPST_CUDA(cudaGetLastError());
     int out[8];
     launch_tile_order<R>(N, g, stm, ord_count.as<int>(), ord_start.as<int>(), perm.as<int>(), s);
+    if (tile_spread) launch_edge_list<R>(N, stm, km.d, nz, fl + 5, edge_list.as<int>(), s);
     DPST_CUDA(cudaGetLastError());
     DPST_CUDA(cudaMemcpyAsync(out, fl, sizeof(out), cudaMemcpyDeviceToHost, s));
     DPST_CUDA(cudaStreamSynchronize(s));
@@ -542,6 +571,7 @@ struct Engine : EngineBase {
       positioned = false;
       throw Error(DPST_ERR_CUDA, "internal: z window longer than its bound");
     }
+    n_edge = tile_spread ? out[5] : 0;
     reach_m[0] = out[1]; reach_m[1] = out[2];
     reach_d[0] = out[3]; reach_d[1] = out[4];
     setup_ghosts(km.d, g.bcA, reach_m, gh_m, ghm);
@@ -572,14 +602,19 @@ struct Engine : EngineBase {
   template <typename RF>
   void spread_into(const RF *F, const RF *T, R *gr, const Ghosts<R> &gm, const Ghosts<R> &gd, cudaStream_t s) {
     const bool torque = p.has_torque && T != nullptr;
-    DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
+    const bool tiles = tile_spread && torque;
+    if (!tiles) DPST_CUDA(cudaMemsetAsync(gr, 0, grid.bytes, s));
     for (const Ghosts<R> *gh : {&gm, &gd}) {
       const KernelDesc &d = (gh == &gm) ? km.d : kd.d;
       const size_t lev = (size_t)d.nyeff * d.nxeff * 3 * sizeof(R);
       if (gh->top) DPST_CUDA(cudaMemsetAsync(gh->top, 0, lev * gh->ntop, s));
       if (gh->bot) DPST_CUDA(cudaMemsetAsync(gh->bot, 0, lev * gh->nbot, s));
     }
-    if (torque && fused) {
+    if (tiles) {
+      if constexpr (sizeof(R) == 4)
+        launch_spread_tiles<RF>(F, T, km.d, kd.d, g, stm, std_, gr, gm, gd, perm.as<int>(), ord_start.as<int>(),
+                                edge_list.as<int>(), n_edge, s);
+    } else if (torque && fused) {
       launch_spread_fused<R, RF>(F, T, N, km.d, kd.d, g, stm, std_, gr, gm, gd, s, perm.as<int>());
     } else {
       launch_spread<R, RF>(false, F, N, km.d, g, stm, gr, gm, s, perm.as<int>());
@@ -1274,6 +1309,7 @@ struct Engine : EngineBase {
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     o->solve_variant = dfsolve ? df_variant : 0;
     o->xy_transform = ownfft ? (xyfused ? 2 : 1) : 0;
+    o->spread_tiles = (tile_spread && p.has_torque) ? 1 : 0;
     o->xy_ms[0] = xy_ms[0];
     o->xy_ms[1] = xy_ms[1];
     if (ownfft) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);

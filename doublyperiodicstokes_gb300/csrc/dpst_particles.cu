@@ -403,6 +403,219 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 1) k_spread_fused(co
 }
 
 // ---------------------------------------------------------------------------
+// Tile-owner spread (mixed operator, fused kernel pair): one CTA per
+// ORDER_TILE x ORDER_TILE tile of grid columns holds the tile's whole grid
+// block [3][nz][8][8] in shared memory, gathers the contributions of the
+// particles of the 3 x 3 neighbouring tiles (every stencil reaching the tile
+// starts there: wx, wy <= 14) to its own cells with shared-memory atomics,
+// and writes the block once with plain stores.  Every grid value is written
+// exactly once, zeros included, so the grid needs no clearing and HBM sees
+// no atomics.  Particles whose window is not interior under both BC sets
+// (spread_fused_item's general path: folds, ghost layers) are skipped here
+// and spread afterwards from their list by k_spread_fused.
+// ---------------------------------------------------------------------------
+constexpr int ORDER_TILE = 8;  // columns per side of the particle-order tile (k_tile_order)
+constexpr int TILE_SPREAD_THREADS = 256;
+
+template <typename R, typename RF>
+void launch_spread_fused(const RF *F, const RF *T, int64_t N, const KernelDesc &km, const KernelDesc &kd,
+                         const GridArgs &g, const Stencils<R> &sm, const Stencils<R> &sd, R *grid,
+                         const Ghosts<R> &ghm, const Ghosts<R> &ghd, cudaStream_t s, const int *perm);
+
+static __device__ __forceinline__ bool fused_interior(const int4 &cm, int dend, int nz) {
+  const int m0 = cm.z - dend;
+  return cm.w == 0 || (m0 >= 1 && m0 + cm.w <= nz - 1);
+}
+
+template <typename RF>
+__global__ void __launch_bounds__(TILE_SPREAD_THREADS, 2)
+    k_spread_tiles(const RF *__restrict__ F, const RF *__restrict__ T, KernelDesc km, KernelDesc kd, GridArgs g,
+                   Stencils<float> sm, Stencils<float> sd, float *__restrict__ grid, const int *__restrict__ perm,
+                   const int *__restrict__ tstart, int ntx, int nty) {
+  extern __shared__ float tb[];  // [3][nz][ORDER_TILE][ORDER_TILE]
+  __shared__ int list[TILE_SPREAD_THREADS];
+  __shared__ int nlist, rng[10];
+  constexpr int TT = ORDER_TILE * ORDER_TILE;
+  const int nz = g.nz;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = TILE_SPREAD_THREADS / 32;
+  const int bx = blockIdx.x % ntx, by = blockIdx.x / ntx;
+  const int x0 = bx * ORDER_TILE, y0 = by * ORDER_TILE;
+  const int cells = 3 * nz * TT;
+  for (int i = tid; i < cells; i += TILE_SPREAD_THREADS) tb[i] = 0.0f;
+  // the candidates: the particles of the 3 x 3 neighbouring tiles, as one
+  // range [0, rng[9]) with the tiles' offsets in rng
+  if (tid == 0) {
+    int acc = 0;
+    for (int nb = 0; nb < 9; ++nb) {
+      const int t = wrapi(by + nb / 3 - 1, nty) * ntx + wrapi(bx + nb % 3 - 1, ntx);
+      rng[nb] = acc;
+      acc += tstart[t + 1] - tstart[t];
+    }
+    rng[9] = acc;
+  }
+  __syncthreads();
+  const int ncand = rng[9];
+  const float half = 0.5f;
+  const int comp = nz * TT;
+  for (int c0 = 0; c0 < ncand; c0 += TILE_SPREAD_THREADS) {
+    // one candidate per thread: keep the interior particles whose stencil
+    // reaches this tile
+    if (tid == 0) nlist = 0;
+    __syncthreads();
+    const int c = c0 + tid;
+    if (c < ncand) {
+      int nb = 0;
+      while (c >= rng[nb + 1]) ++nb;
+      const int t = wrapi(by + nb / 3 - 1, nty) * ntx + wrapi(bx + nb % 3 - 1, ntx);
+      const int p = perm[tstart[t] + c - rng[nb]];
+      const int4 cm = sm.cell[p];
+      if (cm.w > 0 && fused_interior(cm, km.dend, nz)) {
+        const int sx = wrapi(cm.x - km.wx / 2 + km.evenx - x0, g.nx), sy = wrapi(cm.y - km.wy / 2 + km.eveny - y0, g.ny);
+        // the stencil's first column relative to the tile, modulo nx: it
+        // reaches the tile when it starts inside or ends past the tile's start
+        const bool hx = sx < ORDER_TILE || sx + km.wx > g.nx;
+        const bool hy = sy < ORDER_TILE || sy + km.wy > g.ny;
+        if (hx && hy) list[atomicAdd(&nlist, 1)] = p;
+      }
+    }
+    __syncthreads();
+    const int nl = nlist;
+    for (int e = warp; e < nl; e += nw) {
+      const int p = list[e];
+      const int4 cm = sm.cell[p];
+      const int4 cd = sd.cell[p];
+      const int dk = cm.z - cd.z;
+      const int k0 = max(-dk, 0), k1 = min(cd.w - dk, cm.w);
+      const int m0 = cm.z - km.dend;
+      // the stencil's columns inside the tile: i in [i0, i1), j in [j0, j1)
+      int sx = cm.x - km.wx / 2 + km.evenx - x0, sy = cm.y - km.wy / 2 + km.eveny - y0;
+      sx = wrapi(sx, g.nx);
+      sy = wrapi(sy, g.ny);
+      if (sx >= ORDER_TILE) sx -= g.nx;  // started left of the tile (wrapped)
+      if (sy >= ORDER_TILE) sy -= g.ny;
+      const int i0 = max(0, -sx), i1 = min(km.wx, ORDER_TILE - sx);
+      const int j0 = max(0, -sy), j1 = min(km.wy, ORDER_TILE - sy);
+      const int ni = i1 - i0, nj = j1 - j0;
+      if (ni <= 0 || nj <= 0) continue;
+      // the particle's factors in lanes: lane l holds entry l of each table
+      const float lphx = lane < km.wx ? sm.phx[p * km.wx + lane] : 0.0f;
+      const float lphy = lane < km.wy ? sm.phy[p * km.wy + lane] : 0.0f;
+      const float lfx = lane < kd.wx ? sd.phx[p * kd.wx + lane] : 0.0f;
+      const float lfy = lane < kd.wy ? sd.phy[p * kd.wy + lane] : 0.0f;
+      const float ldfx = lane < kd.wx ? sd.dphx[p * kd.wx + lane] : 0.0f;
+      const float ldfy = lane < kd.wy ? sd.dphy[p * kd.wy + lane] : 0.0f;
+      // z factors of window entries lane and lane + 32
+      float lpz[2], lpzd[2], ldpzd[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int kk = lane + 32 * h;
+        lpz[h] = kk < cm.w ? sm.phz[p * km.wz_max + kk] : 0.0f;
+        const bool dz = kk >= k0 && kk < k1;
+        lpzd[h] = dz ? sd.phz[p * kd.wz_max + dk + kk] : 0.0f;
+        ldpzd[h] = dz ? sd.dphz[p * kd.wz_max + dk + kk] : 0.0f;
+      }
+      const float f0 = (float)F[3 * p], f1 = (float)F[3 * p + 1], f2 = (float)F[3 * p + 2];
+      const float tx_ = (float)T[3 * p], ty_ = (float)T[3 * p + 1], tz_ = (float)T[3 * p + 2];
+      const int items = ni * nj * cm.w;
+      for (int b = 0; b < items; b += 32) {
+        const int it = b + lane;
+        const bool live = it < items;
+        const int k = live ? it / (ni * nj) : 0;
+        const int r = live ? it - k * (ni * nj) : 0;
+        const int jj = r / ni, ii = r - jj * ni;
+        const int i = i0 + ii, j = j0 + jj;
+        const float px = __shfl_sync(0xffffffffu, lphx, i), py = __shfl_sync(0xffffffffu, lphy, j);
+        const float fx = __shfl_sync(0xffffffffu, lfx, i), fy = __shfl_sync(0xffffffffu, lfy, j);
+        const float dfx = __shfl_sync(0xffffffffu, ldfx, i), dfy = __shfl_sync(0xffffffffu, ldfy, j);
+        const int kh = k >> 5;
+        const float pz0 = __shfl_sync(0xffffffffu, lpz[0], k), pz1 = __shfl_sync(0xffffffffu, lpz[1], k);
+        const float pd0 = __shfl_sync(0xffffffffu, lpzd[0], k), pd1 = __shfl_sync(0xffffffffu, lpzd[1], k);
+        const float dd0 = __shfl_sync(0xffffffffu, ldpzd[0], k), dd1 = __shfl_sync(0xffffffffu, ldpzd[1], k);
+        const float pz = kh ? pz1 : pz0, phz = kh ? pd1 : pd0, dphz = kh ? dd1 : dd0;
+        if (!live) continue;
+        const float v = (px * py) * pz;
+        float gx = v * f0, gy = v * f1, gz = v * f2;
+        if (k >= k0 && k < k1) {
+          const float ax = (dfx * fy) * phz, ay = (fx * dfy) * phz, az = (fx * fy) * dphz;
+          gx += half * (ay * tz_) + (-half) * (az * ty_);
+          gy += -half * (ax * tz_) + half * (az * tx_);
+          gz += half * (ax * ty_ - ay * tx_);
+        }
+        float *dst = tb + ((m0 + k) * ORDER_TILE + sy + j) * ORDER_TILE + sx + i;
+        atomicAdd(dst, gx);
+        atomicAdd(dst + comp, gy);
+        atomicAdd(dst + 2 * comp, gz);
+      }
+    }
+    __syncthreads();
+  }
+  // the block to the grid: rows of ORDER_TILE values, two float4 per row
+  const int64_t plane = (int64_t)g.nx * g.ny;
+  const int rows = 3 * nz * ORDER_TILE;
+  const bool full = x0 + ORDER_TILE <= g.nx && y0 + ORDER_TILE <= g.ny && (g.nx & 3) == 0;
+  for (int r2 = tid; r2 < 2 * rows; r2 += TILE_SPREAD_THREADS) {
+    const int r = r2 >> 1, h = r2 & 1;
+    const int yl = r % ORDER_TILE, dm = r / ORDER_TILE;  // dm = d nz + m
+    const int y = y0 + yl;
+    const float *src = tb + r * ORDER_TILE + 4 * h;
+    float *dst = grid + (int64_t)dm * plane + (int64_t)y * g.nx + x0 + 4 * h;
+    if (full) {
+      *reinterpret_cast<float4 *>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+    } else if (y < g.ny) {
+      for (int e = 0; e < 4; ++e)
+        if (x0 + 4 * h + e < g.nx) dst[e] = src[e];
+    }
+  }
+}
+
+// Particles whose fused window is not interior: list[0..count) (count at *count).
+template <typename R>
+__global__ void k_edge_list(int64_t N, Stencils<R> sm, int dend, int nz, int *count, int *list) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  if (!fused_interior(sm.cell[p], dend, nz)) list[atomicAdd(count, 1)] = (int)p;
+}
+
+template <typename R>
+void launch_edge_list(int64_t N, const Stencils<R> &sm, const KernelDesc &km, int nz, int *count, int *list,
+                      cudaStream_t s) {
+  if (N == 0) return;
+  k_edge_list<R><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(N, sm, km.dend, nz, count, list);
+}
+
+// nz <= 128: the block fits in shared memory; wx, wy <= 14: stencils reach
+// one tile at most; z windows of at most 64 nodes (two per lane); more than
+// two tiles per axis: the 3 x 3 neighbourhood holds nine distinct tiles.
+bool tile_spread_supported(const KernelDesc &km, const KernelDesc &kd, int nx, int ny, int nz) {
+  return nz <= 128 && km.wx <= 14 && km.wy <= 14 && km.wz_max <= 64 && kd.wz_max <= 64 &&
+         nx > 2 * ORDER_TILE && ny > 2 * ORDER_TILE;
+}
+
+size_t tile_spread_smem(int nz) { return sizeof(float) * 3 * (size_t)nz * ORDER_TILE * ORDER_TILE; }
+
+cudaError_t tile_spread_setup(int nz) {
+  cudaError_t e = cudaFuncSetAttribute(k_spread_tiles<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tile_spread_smem(nz));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_spread_tiles<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tile_spread_smem(nz));
+  return e;
+}
+
+// The whole grid written by the tiles (no clearing needed); then the edge
+// particles' contributions added with atomics (ghost layers, folds).
+template <typename RF>
+void launch_spread_tiles(const RF *F, const RF *T, const KernelDesc &km, const KernelDesc &kd, const GridArgs &g,
+                         const Stencils<float> &sm, const Stencils<float> &sd, float *grid, const Ghosts<float> &ghm,
+                         const Ghosts<float> &ghd, const int *perm, const int *tstart, const int *edge,
+                         int64_t n_edge, cudaStream_t s) {
+  const int ntx = (g.nx + ORDER_TILE - 1) / ORDER_TILE, nty = (g.ny + ORDER_TILE - 1) / ORDER_TILE;
+  k_spread_tiles<RF><<<(unsigned)(ntx * nty), TILE_SPREAD_THREADS, tile_spread_smem(g.nz), s>>>(
+      F, T, km, kd, g, sm, sd, grid, perm, tstart, ntx, nty);
+  if (n_edge > 0) launch_spread_fused<float, RF>(F, T, n_edge, km, kd, g, sm, sd, grid, ghm, ghd, s, edge);
+}
+
+// ---------------------------------------------------------------------------
 // Periodic x then y fold of the ghost-layer buffers, applied to every stored
 // level exactly as the reference folds its whole extended grid
 // (BoundaryConditions.h:43-84 then 143-184): x ghosts are added into the
@@ -918,7 +1131,6 @@ void launch_spread(bool dipole, const RF *FT, int64_t N, const KernelDesc &kd, c
 // that the spread's and the interpolation's neighbouring threads touch
 // neighbouring grid cells.  count holds ntiles ints, start ntiles + 1.
 // ---------------------------------------------------------------------------
-constexpr int ORDER_TILE = 8;
 
 template <typename R, bool FILL>
 __global__ void k_tile_order(int64_t N, GridArgs g, Stencils<R> st, int ntx, int *count, const int *start,
@@ -1062,5 +1274,18 @@ void launch_interp(bool dipole, const R *grid, int64_t N, const KernelDesc &kd, 
 
 DPST_INST(float)
 DPST_INST(double)
+
+template void launch_spread_tiles<float>(const float *, const float *, const KernelDesc &, const KernelDesc &,
+                                         const GridArgs &, const Stencils<float> &, const Stencils<float> &, float *,
+                                         const Ghosts<float> &, const Ghosts<float> &, const int *, const int *,
+                                         const int *, int64_t, cudaStream_t);
+template void launch_spread_tiles<double>(const double *, const double *, const KernelDesc &, const KernelDesc &,
+                                          const GridArgs &, const Stencils<float> &, const Stencils<float> &,
+                                          float *, const Ghosts<float> &, const Ghosts<float> &, const int *,
+                                          const int *, const int *, int64_t, cudaStream_t);
+template void launch_edge_list<float>(int64_t, const Stencils<float> &, const KernelDesc &, int, int *, int *,
+                                      cudaStream_t);
+template void launch_edge_list<double>(int64_t, const Stencils<double> &, const KernelDesc &, int, int *, int *,
+                                       cudaStream_t);
 
 }  // namespace dpst

@@ -174,6 +174,11 @@ typedef struct dpst_info {
                                       fused forces one */
   float xy_ms[2];                  /* creation-time timings of a forward + inverse pair:
                                       two-pass, one-launch (0 if not timed) */
+  int spread_tiles;                /* 1: the spread of forces and torques writes the grid once
+                                      per 8 x 8-column tile from shared memory (mixed operator,
+                                      fused kernel pair, DPSTOKES_GB300_SPREAD=tiles); 0: the grid
+                                      is cleared and the contributions added with atomics (default,
+                                      faster on the measured configurations) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;
