@@ -109,6 +109,8 @@ cudaError_t launch_zgemm(R *spec, int nz, int64_t ncols, const R *Tm, const EpiA
 // tensor-core z transform of the mixed operator (dpst_ztc.cu)
 cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
                             int *err, cudaStream_t s);
+cudaError_t launch_zgemm_df(double *spec, int nz, int64_t ncols, const double *Tm, const EpiArgs &e, int nsm,
+                            cudaStream_t s, bool fold_out);
 cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s);
 bool tile_spread_supported(const KernelDesc &km, const KernelDesc &kd, int nx, int ny, int nz);
 cudaError_t tile_spread_setup(int nz);
@@ -665,9 +667,16 @@ struct Engine : EngineBase {
     }
   }
 
-  // impl < 0: the tuned kernel for e's direction
+  // impl < 0: the tuned kernel for e's direction; 0 SIMT in the operator's
+  // arithmetic, 1 tcgen05 split-TF32 (FP32 spectra), 2 double-float SIMT
+  // (FP64 spectra)
   cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl = -1) {
     if (impl < 0) impl = ztc[e.inverse ? 1 : 0];
+    if constexpr (sizeof(R) == 8) {
+      if (impl == 2)
+        return launch_zgemm_df(reinterpret_cast<double *>(sp), nz, 2 * nk, reinterpret_cast<const double *>(T), e,
+                               nsm, s, fold_out);
+    }
     if (impl == 1 && sizeof(R) == 4) {
       if (e.inverse && e.ks.mode != 0 && e.corr != nullptr) {
         // the wall correction as its own pass: the tcgen05 epilogue's four
@@ -686,12 +695,52 @@ struct Engine : EngineBase {
     return launch_zgemm<R>(sp, nz, 2 * nk, T, e, nsm, s, fold_out);
   }
 
+  // The FP64 operator: the FP64 and the double-float SIMT transforms per
+  // direction, timed like the FP32 pair (one warm-up, three runs), the faster
+  // kept; DPSTOKES_GB300_ZTRANSFORM=simt | df64 fixes one.
+  void tune_ztransform_fp64(const std::string &want) {
+    if (want == "simt") return;
+    R *sp = reinterpret_cast<R *>(spec.p);
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+    DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    for (int dir = 0; dir < 2; ++dir) {
+      EpiArgs e;
+      memset(&e, 0, sizeof(e));
+      e.ks = ks;
+      e.inverse = dir;
+      e.scale = dir ? 1.0 / ((double)nx * (double)ny) : 1.0;
+      if (dir) epi_corr(e);
+      const R *T = dir ? Ti.as<R>() : Tf.as<R>();
+      for (int k = 0; k < 2; ++k) {
+        const int impl = k ? 2 : 0;
+        DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));  // warm-up
+        DPST_CUDA(cudaEventRecord(a, 0));
+        for (int rep = 0; rep < 3; ++rep) DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));
+        DPST_CUDA(cudaEventRecord(b, 0));
+        DPST_CUDA(cudaEventSynchronize(b));
+        DPST_CUDA(cudaEventElapsedTime(&ztc_ms[dir][k], a, b));
+        ztc_ms[dir][k] /= 3.0f;
+      }
+      ztc[dir] = (want == "df64" || ztc_ms[dir][1] < ztc_ms[dir][0]) ? 2 : 0;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
+  }
+
   void tune_ztransform() {
     ztc_err.alloc(sizeof(int));
     DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
     const char *env = getenv("DPSTOKES_GB300_ZTRANSFORM");
     const std::string want = env ? env : "auto";
-    if (sizeof(R) != 4 || nz > 128 || want == "simt") return;
+    if (sizeof(R) == 8) {
+      tune_ztransform_fp64(want);
+      return;
+    }
+    if (nz > 128 || want == "simt") return;
     R *sp = reinterpret_cast<R *>(spec.p);
     DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
     DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));

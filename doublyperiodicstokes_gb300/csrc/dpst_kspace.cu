@@ -25,6 +25,7 @@
 // the reference computes at its partner index.
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
+#include "dpst_df64.cuh"
 #include <cuComplex.h>
 #include <type_traits>
 
@@ -351,6 +352,214 @@ __global__ void __launch_bounds__(256) k_zgemm_b(const ZSeg<R> *__restrict__ seg
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// The FP64 operator's z transform in double-float arithmetic on the FP32
+// pipes (FP64 runs at 1/64 of the FP32 rate on this GPU): the folded GEMM of
+// zgemm_tile with the matrix and the staged tile held as double-float pairs
+// in shared memory and every sum accumulated with the compensated
+// (Ogita-Rump-Oishi Dot2) scheme, 12 FP32 operations per multiply-add.  The
+// folds (P, Q) are formed in FP64 before the rounding to double-float, and
+// the epilogue (wall correction, scale) runs in FP64.  Error ~ 2^-48 times
+// the sum of the terms' magnitudes plus the double-float rounding of the
+// inputs: about 1e-14 relative against the FP64 GEMM.
+// ---------------------------------------------------------------------------
+template <int RPT, int FOLD>
+__global__ void __launch_bounds__(256) k_zgemm_df(double *spec, int nz, int64_t ncols, const double *__restrict__ Tm,
+                                                 EpiArgs e) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int h = nz / 2, odd_n = nz & 1;
+  const int kf = h + odd_n;
+  const int tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const int tstride = tcols + 1;
+  const int trows = (FOLD == ZFOLD_IN) ? nz : kf;
+  float2 *Ts = reinterpret_cast<float2 *>(smem_raw);  // [16 RPT][tcols + 1]
+  float2 *Bs = Ts + 16 * RPT * tstride;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  for (int idx = tid; idx < 16 * RPT * tstride; idx += 256) {
+    const int r = idx / tstride, m = idx % tstride;
+    const df64 v = df_from_d((r < trows && m < tcols) ? Tm[r * nz + m] : 0.0);
+    Ts[idx] = make_float2(v.hi, v.lo);
+  }
+  const int64_t tiles_per_comp = (ncols + 63) / 64;
+  const int64_t ntiles = 3 * tiles_per_comp;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int d = (int)(t / tiles_per_comp);
+    const int64_t c0 = (t % tiles_per_comp) * 64;
+    double *B = spec + (int64_t)d * nz * ncols;
+    __syncthreads();
+    if (FOLD == ZFOLD_IN) {
+      for (int idx = tid; idx < kf * 64; idx += 256) {
+        const int m = idx >> 6, c = idx & 63;
+        double pv = 0.0, qv = 0.0;
+        if (c0 + c < ncols) {
+          const double xa = B[(int64_t)m * ncols + c0 + c];
+          if (m < h) {
+            const double xb = B[(int64_t)(nz - 1 - m) * ncols + c0 + c];
+            pv = xa + xb;
+            qv = xa - xb;
+          } else {
+            pv = xa;  // middle node (odd nz)
+          }
+        }
+        const df64 dp = df_from_d(pv), dq = df_from_d(qv);
+        Bs[idx] = make_float2(dp.hi, dp.lo);
+        Bs[kf * 64 + idx] = make_float2(dq.hi, dq.lo);
+      }
+    } else {
+      for (int idx = tid; idx < nz * 64; idx += 256) {
+        const int m = idx >> 6, c = idx & 63;
+        const df64 v = df_from_d((c0 + c < ncols) ? B[(int64_t)m * ncols + c0 + c] : 0.0);
+        Bs[idx] = make_float2(v.hi, v.lo);
+      }
+    }
+    __syncthreads();
+    auto store = [&](int r, int64_t col, df64 re_, df64 im_) {
+      double vr = df_to_d(re_), vi = df_to_d(im_);
+      if (e.inverse) {
+        double cre, cim;
+        corr_any<double>(e, d, r, col >> 1, cre, cim);
+        vr = (vr + cre) * e.scale;
+        vi = (vi + cim) * e.scale;
+      }
+      B[(int64_t)r * ncols + col] = vr;
+      B[(int64_t)r * ncols + col + 1] = vi;
+    };
+    if (FOLD == ZFOLD_IN) {
+      df_acc acc[RPT][4];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[q][c] = acc_zero();
+      const float2 *Bp = Bs + ((ty & 1) ? kf * 64 : 0);  // odd rows read Q
+      for (int m = 0; m < kf; ++m) {
+        df64 b[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = df_lds(Bp[m * 64 + tx * 4 + c]);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const df64 av = df_lds(Ts[(ty + 16 * q) * tstride + m]);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc_fma(acc[q][c], av, b[c]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int r = ty + 16 * q;
+        if (r >= nz) continue;
+#pragma unroll
+        for (int cp = 0; cp < 2; ++cp) {
+          const int64_t col = c0 + tx * 4 + 2 * cp;
+          if (col >= ncols) continue;
+          store(r, col, acc_val(acc[q][2 * cp]), acc_val(acc[q][2 * cp + 1]));
+        }
+      }
+    } else {
+      df_acc ae[RPT][4], ao[RPT][4];
+#pragma unroll
+      for (int q = 0; q < RPT; ++q)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ae[q][c] = ao[q][c] = acc_zero();
+      int j = 0;
+      for (; j + 1 < nz; j += 2) {
+        df64 be[4], bo[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          be[c] = df_lds(Bs[j * 64 + tx * 4 + c]);
+          bo[c] = df_lds(Bs[(j + 1) * 64 + tx * 4 + c]);
+        }
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const df64 te = df_lds(Ts[(ty + 16 * q) * tstride + j]), to = df_lds(Ts[(ty + 16 * q) * tstride + j + 1]);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            acc_fma(ae[q][c], te, be[c]);
+            acc_fma(ao[q][c], to, bo[c]);
+          }
+        }
+      }
+      if (j < nz) {  // odd nz: last (even) coefficient
+        df64 be[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) be[c] = df_lds(Bs[j * 64 + tx * 4 + c]);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+          const df64 te = df_lds(Ts[(ty + 16 * q) * tstride + j]);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc_fma(ae[q][c], te, be[c]);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < RPT; ++q) {
+        const int m = ty + 16 * q;
+        if (m >= kf) continue;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const df64 E = acc_val(ae[q][c]), O = acc_val(ao[q][c]);
+          ae[q][c].s = E.hi;  // keep E and O as value pairs for the store below
+          ae[q][c].e = E.lo;
+          ao[q][c].s = O.hi;
+          ao[q][c].e = O.lo;
+        }
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+          const int r = half ? nz - 1 - m : m;
+          if (half && r == m) continue;  // middle node
+#pragma unroll
+          for (int cp = 0; cp < 2; ++cp) {
+            const int64_t col = c0 + tx * 4 + 2 * cp;
+            if (col >= ncols) continue;
+            const df64 er = df_make(ae[q][2 * cp].s, ae[q][2 * cp].e), orr = df_make(ao[q][2 * cp].s, ao[q][2 * cp].e);
+            const df64 ei = df_make(ae[q][2 * cp + 1].s, ae[q][2 * cp + 1].e);
+            const df64 oi = df_make(ao[q][2 * cp + 1].s, ao[q][2 * cp + 1].e);
+            store(r, col, half ? df_sub(er, orr) : df_add(er, orr), half ? df_sub(ei, oi) : df_add(ei, oi));
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int RPT, int FOLD>
+static cudaError_t zgemm_df_rpt(double *spec, int nz, int64_t ncols, const double *Tm, const EpiArgs &e, int nsm,
+                                cudaStream_t s) {
+  const int kf = nz / 2 + (nz & 1);
+  const size_t tcols = (FOLD == ZFOLD_IN) ? kf : nz;
+  const size_t bs = (FOLD == ZFOLD_IN) ? 2 * (size_t)kf * 64 : (size_t)nz * 64;
+  const size_t smem = (16 * RPT * (tcols + 1) + bs) * sizeof(float2);
+  cudaError_t err = cudaFuncSetAttribute(k_zgemm_df<RPT, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+  if (err != cudaSuccess) return err;
+  int blocks_per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_zgemm_df<RPT, FOLD>, 256, smem);
+  if (err != cudaSuccess) return err;
+  if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
+  int64_t ntiles = 3 * ((ncols + 63) / 64);
+  int64_t grid = (int64_t)nsm * blocks_per_sm;
+  if (grid > ntiles) grid = ntiles;
+  k_zgemm_df<RPT, FOLD><<<(unsigned)grid, 256, smem, s>>>(spec, nz, ncols, Tm, e);
+  return cudaGetLastError();
+}
+
+template <int FOLD>
+static cudaError_t zgemm_df_fold(double *spec, int nz, int64_t ncols, const double *Tm, const EpiArgs &e, int nsm,
+                                 cudaStream_t s) {
+  const int rows = (FOLD == ZFOLD_IN) ? nz : nz / 2 + (nz & 1);
+  const int rpt = (rows + 15) / 16;
+  if (rpt <= 2) return zgemm_df_rpt<2, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 4) return zgemm_df_rpt<4, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 6) return zgemm_df_rpt<6, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  if (rpt <= 8) return zgemm_df_rpt<8, FOLD>(spec, nz, ncols, Tm, e, nsm, s);
+  return cudaErrorInvalidValue;
+}
+
+// The double-float z transform of an FP64 spectrum (same arguments as
+// launch_zgemm<double>).
+cudaError_t launch_zgemm_df(double *spec, int nz, int64_t ncols, const double *Tm, const EpiArgs &e, int nsm,
+                            cudaStream_t s, bool fold_out) {
+  return fold_out ? zgemm_df_fold<ZFOLD_OUT>(spec, nz, ncols, Tm, e, nsm, s)
+                  : zgemm_df_fold<ZFOLD_IN>(spec, nz, ncols, Tm, e, nsm, s);
+}
 
 // ---------------------------------------------------------------------------
 // Host launchers

@@ -2,7 +2,9 @@
 transform and the FP64 operator (forced with DPSTOKES_GB300_ZTRANSFORM at
 creation): Mdot outputs within 5e-6 of each other and 1e-5 of FP64, on the
 small cases (odd and even nz, every geometry) and the open-domain c2
-geometry on a 192^2 x 128 grid; the backward pass likewise."""
+geometry on a 192^2 x 128 grid; the backward pass likewise.  The FP64
+operator's double-float z transform against its FP64 one (1e-12) and the
+reference fixtures (1e-10)."""
 import numpy as np
 import pytest
 
@@ -78,3 +80,39 @@ def test_tcgen05_backward(name, monkeypatch):
     for a, b in zip(out["tc"], out["d"]):
         if a is not None:
             assert rel_err(a, b) < 1e-4
+
+
+@pytest.mark.parametrize("name", [w.name for w in W.SMALL] + ["c2_dp_n65536@192", "c0_dpbw_n2048"])
+def test_fp64_double_float_ztransform(name, monkeypatch):
+    """The FP64 operator's double-float z transform (FP32 pipes, compensated
+    sums) against its FP64 transform: V, W to 1e-12; the backward pass too;
+    and the reference fixtures (where one exists) to 1e-10."""
+    import golden_io
+    w = _wl(name)
+    X, F, T = W.make_inputs(w)
+    df = _op(w, "fp64", "df64", monkeypatch)
+    info = df.info()
+    assert info["ztransform"] == 2 and info["ztransform_inverse"] == 2, info
+    fp = _op(w, "fp64", "simt", monkeypatch)
+    assert fp.info()["ztransform"] == 0
+    Va, Wa = _mdot(df, X, F, T, torch.float64)
+    Vb, Wb = _mdot(fp, X, F, T, torch.float64)
+    ev = rel_err(Va, Vb)
+    print("%s df64-fp64 V %.2e (ms fp64 %.3f df64 %.3f)" % (name, ev, info["ztransform_ms"][0],
+                                                           info["ztransform_ms"][1]))
+    assert ev < 1e-12
+    if T is not None:
+        assert rel_err(Wa, Wb) < 1e-12
+    g = np.random.default_rng(5).standard_normal(F.shape)
+    grads = []
+    for op in (df, fp):
+        gF, _, gX = op.mdot_backward(torch.tensor(F, device="cuda"), torch.tensor(T, device="cuda") if T is not None
+                                     else None, torch.tensor(g, device="cuda"), need_F=True, need_X=True)
+        torch.cuda.synchronize()
+        grads.append((gF.cpu().numpy(), gX.cpu().numpy()))
+    assert rel_err(grads[0][0], grads[1][0]) < 1e-12 and rel_err(grads[0][1], grads[1][1]) < 1e-11
+    if name in golden_io.names():
+        _, _, _, _, gd = golden_io.inputs(name)
+        er = rel_err(golden_io.restrict(gd, Va), gd["V"])
+        print("%s df64 vs reference %.2e" % (name, er))
+        assert er < 1e-10
