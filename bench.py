@@ -369,7 +369,8 @@ def run_ours(args, rank, world):
             peak = nsm * 2 * mhz * 1e6
             roof["fp64_pipe"] = {"lane_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
                                  "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
-    extra["xy_transform"] = {"form": {0: "cuFFT", 1: "own, two passes", 2: "own, one launch"}.get(
+    extra["xy_transform"] = {"form": {0: "cuFFT", 1: "own, two passes", 2: "own, one launch",
+                                      3: "own double-float, two passes"}.get(
         info.get("xy_transform"), "n/a"), "pair_ms_two_pass_one_launch": [round(float(x), 4) for x in
                                                                         info.get("xy_ms", [])]}
     extra["set_positions_ms"] = set_positions_ms

@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libdpstokes_gb300.so"
 SOURCES = ["dpst_engine.cu", "dpst_particles.cu", "dpst_kspace.cu", "dpst_bvp.cu", "dpst_adjoint.cu",
            "dpst_grad.cu", "dpst_batch.cu", "dpst_ztc.cu", "dpst_tp.cu", "dpst_bvp_df.cu",
-           "dpst_fft.cu"]
+           "dpst_fft.cu", "dpst_fft_df.cu"]
 HEADERS = ["dpst_internal.cuh", "dpst_kdev.cuh", "dpst_pdev.cuh", "dpst_host.cuh", "dpst_launch.cuh",
            "dpst_df64.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

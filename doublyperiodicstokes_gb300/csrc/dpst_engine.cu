@@ -89,6 +89,13 @@ cudaError_t fft_rows(bool inverse, const float *grid_in, float2 *spec_out, const
 cudaError_t fft_cols(bool inverse, float2 *spec, int ny, int nxh, int64_t planes, const float2 *twy, cudaStream_t s);
 bool fft_xy_fused_supported(int nx, int ny);
 int64_t fft_xy_counter_ints(int64_t planes);
+bool own_fft_df_supported(int nx, int ny);
+std::vector<float4> fft_twiddles_df(int n);
+cudaError_t fft_setup_df(int nx, int ny);
+cudaError_t fft_rows_df(bool inverse, const double *grid_in, double2 *spec_out, const double2 *spec_in,
+                        double *grid_out, int nx, int64_t rows, const float4 *twx, cudaStream_t s);
+cudaError_t fft_cols_df(bool inverse, double2 *spec, int ny, int nxh, int64_t planes, const float4 *twy,
+                        cudaStream_t s);
 // planes between the one-launch transform's two passes: 16, or
 // DPSTOKES_GB300_XY_LAG (1 ... 4096)
 static int xy_lag_setting() {
@@ -202,6 +209,11 @@ struct Engine : EngineBase {
   // and the creation-time timings {two-pass, one-launch} of a forward +
   // inverse pair
   bool xyfused = false;
+  // FP64 operator: the library's double-float x-y transforms (when faster
+  // than cuFFT's FP64 ones at creation) and their timings {cuFFT, own}
+  bool ownfft_d = false;
+  DevBuf twxd, twyd;
+  float xyd_ms[2] = {0.0f, 0.0f};
   DevBuf xyctr;
   int64_t xy_planes = 0;
   int xy_grid = 0, xy_lag = xy_lag_setting();
@@ -398,11 +410,46 @@ struct Engine : EngineBase {
           grow_xy_counters(3 * (int64_t)nz);
         }
       }
+      if (sizeof(R) == 8 && !want_cufft && own_fft_df_supported(nx, ny)) {
+        upload(twxd, fft_twiddles_df(nx));
+        upload(twyd, fft_twiddles_df(ny));
+        DPST_CUDA(fft_setup_df(nx, ny));
+        tune_xy_d(env && std::string(env) == "own");
+      }
     }
     DPST_CUDA(cudaDeviceSynchronize());
     tune_xy();
     tune_ztransform();
     tune_solve();
+  }
+
+  // FP64 operator: cuFFT's FP64 pair against the double-float kernels' pair
+  // on the grid and spectrum buffers (one warm-up, best of three); force:
+  // DPSTOKES_GB300_XY_FFT=own (or =cufft, which skips this).
+  void tune_xy_d(bool force) {
+    cudaEvent_t e0, e1;
+    DPST_CUDA(cudaEventCreate(&e0));
+    DPST_CUDA(cudaEventCreate(&e1));
+    DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
+    for (int form = 0; form < 2; ++form) {
+      ownfft_d = form == 1;
+      float best = 1e30f;
+      for (int r = 0; r < 4; ++r) {
+        DPST_CUDA(cudaEventRecord(e0, 0));
+        exec_fwd(grid.as<R>(), spec.as<CR>(), 0);
+        exec_inv(spec.as<CR>(), grid.as<R>(), 0);
+        DPST_CUDA(cudaEventRecord(e1, 0));
+        DPST_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        DPST_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0) best = std::min(best, ms);
+      }
+      xyd_ms[form] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ownfft_d = force || xyd_ms[1] < xyd_ms[0];
+    DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
   }
 
   void grow_xy_counters(int64_t planes) {
@@ -939,6 +986,14 @@ struct Engine : EngineBase {
   void exec_fwd(R *gr, CR *sp, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
     if (planes == 0) planes = 3 * (int64_t)nz;
     if (plan == 0) plan = plan_f;
+    if constexpr (sizeof(R) == 8) {
+      if (ownfft_d) {
+        DPST_CUDA(fft_rows_df(false, reinterpret_cast<const double *>(gr), reinterpret_cast<double2 *>(sp), nullptr,
+                              nullptr, nx, planes * ny, twxd.as<float4>(), s));
+        DPST_CUDA(fft_cols_df(false, reinterpret_cast<double2 *>(sp), ny, nxh, planes, twyd.as<float4>(), s));
+        return;
+      }
+    }
     if (ownfft && xyfused && planes <= xy_planes) {
       DPST_CUDA(fft_xy_fused(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr, nx,
                              ny, planes, twx.as<float2>(), twy.as<float2>(), xyctr.as<int>(), xy_grid, xy_lag, s));
@@ -959,6 +1014,14 @@ struct Engine : EngineBase {
   void exec_inv(CR *sp, R *gr, cudaStream_t s, int64_t planes = 0, cufftHandle plan = 0) {
     if (planes == 0) planes = 3 * (int64_t)nz;
     if (plan == 0) plan = plan_b;
+    if constexpr (sizeof(R) == 8) {
+      if (ownfft_d) {
+        DPST_CUDA(fft_cols_df(true, reinterpret_cast<double2 *>(sp), ny, nxh, planes, twyd.as<float4>(), s));
+        DPST_CUDA(fft_rows_df(true, nullptr, nullptr, reinterpret_cast<const double2 *>(sp),
+                              reinterpret_cast<double *>(gr), nx, planes * ny, twxd.as<float4>(), s));
+        return;
+      }
+    }
     if (ownfft && xyfused && planes <= xy_planes) {
       DPST_CUDA(fft_xy_fused(true, nullptr, reinterpret_cast<float2 *>(sp), reinterpret_cast<float *>(gr), nx, ny,
                              planes, twx.as<float2>(), twy.as<float2>(), xyctr.as<int>(), xy_grid, xy_lag, s));
@@ -1357,11 +1420,11 @@ struct Engine : EngineBase {
     o->fused_particle_passes = fused ? 1 : 0;
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     o->solve_variant = dfsolve ? df_variant : 0;
-    o->xy_transform = ownfft ? (xyfused ? 2 : 1) : 0;
+    o->xy_transform = ownfft ? (xyfused ? 2 : 1) : (ownfft_d ? 3 : 0);
     o->spread_tiles = (tile_spread && p.has_torque) ? 1 : 0;
-    o->xy_ms[0] = xy_ms[0];
-    o->xy_ms[1] = xy_ms[1];
-    if (ownfft) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
+    o->xy_ms[0] = sizeof(R) == 8 ? xyd_ms[0] : xy_ms[0];
+    o->xy_ms[1] = sizeof(R) == 8 ? xyd_ms[1] : xy_ms[1];
+    if (ownfft || ownfft_d) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
     if (sizeof(R) == 4 && ztc[1] && p.mode != DPST_MODE_NOWALL) o->kernels_per_mdot += 1;  // correction pass
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;

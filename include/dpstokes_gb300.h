@@ -170,11 +170,14 @@ typedef struct dpst_info {
   int xy_transform;                /* x-y transforms: the library's own in the mixed operator
                                       with power-of-two nx and ny, 1 as two passes (rows,
                                       columns), 2 as one launch of both passes (nx = ny in
-                                      128, 256, 512, 1024, when faster at creation);
+                                      128, 256, 512, 1024, when faster at creation); 3 the
+                                      FP64 operator's own double-float two passes (powers of
+                                      two, nx <= 1024, ny <= 512, when faster than cuFFT);
                                       0 cuFFT.  DPSTOKES_GB300_XY_FFT=cufft | twopass |
-                                      fused forces one */
+                                      fused | own forces one */
   float xy_ms[2];                  /* creation-time timings of a forward + inverse pair:
-                                      two-pass, one-launch (0 if not timed) */
+                                      mixed: two-pass, one-launch; FP64: cuFFT, own
+                                      double-float (0 if not timed) */
   int spread_tiles;                /* 1: the spread of forces and torques writes the grid once
                                       per 8 x 8-column tile from shared memory (mixed operator,
                                       fused kernel pair, DPSTOKES_GB300_SPREAD=tiles); 0: the grid

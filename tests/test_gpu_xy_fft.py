@@ -145,3 +145,33 @@ def test_operator_one_launch_matches_two_pass(name, monkeypatch):
         op.close()
     for a, b in zip(out["fused"], out["twopass"]):
         assert rel_err(a, b) < 5e-6
+
+
+@pytest.mark.parametrize("name", ["c0_dpbw_n2048", "c2_dp_n65536@128", "c1_dpsc_n16384@128"])
+def test_fp64_operator_double_float_xy_transform(name, monkeypatch):
+    """The FP64 operator on the library's double-float x-y transforms against
+    the same operator on cuFFT's FP64 transforms (1e-12), and against the
+    reference fixture where one exists (1e-10)."""
+    import golden_io
+    w = W.by_name(name)
+    X, F, T = W.make_inputs(w)
+    out = {}
+    for which in ("own", "cufft"):
+        monkeypatch.setenv("DPSTOKES_GB300_XY_FFT", which)
+        op = DPStokes(StokesParams.from_workload(w, "fp64"), w.N)
+        form = op.info()["xy_transform"]
+        op.set_positions(torch.tensor(X, device=op.device))
+        V, Wv = op.mdot(torch.tensor(F, device=op.device),
+                        torch.tensor(T, device=op.device) if T is not None else None)
+        torch.cuda.synchronize()
+        out[which] = (form, V.cpu().numpy(), Wv.cpu().numpy() if Wv is not None else None)
+        op.close()
+    assert out["own"][0] == 3 and out["cufft"][0] == 0
+    ev = rel_err(out["own"][1], out["cufft"][1])
+    print("%s FP64 own double-float vs cuFFT V %.2e" % (name, ev))
+    assert ev < 1e-12
+    if T is not None:
+        assert rel_err(out["own"][2], out["cufft"][2]) < 1e-12
+    if name in golden_io.names():
+        _, _, _, _, gd = golden_io.inputs(name)
+        assert rel_err(golden_io.restrict(gd, out["own"][1]), gd["V"]) < 1e-10
