@@ -23,7 +23,7 @@ from conftest import rel_err  # noqa: E402
 from doublyperiodicstokes_gb300 import DPStokes, StokesParams, _lib, workloads as W  # noqa: E402
 
 pytestmark = pytest.mark.gpu
-SIZES = [(64, 32), (128, 128), (256, 64), (512, 512), (1024, 256), (2048, 1024), (64, 1024)]
+SIZES = [(64, 32), (128, 128), (256, 64), (512, 512), (1024, 256), (2048, 1024), (64, 1024), (256, 512), (128, 512)]
 FUSED = [(128, 128), (256, 256), (512, 512), (1024, 1024)]
 
 
