@@ -39,6 +39,16 @@
 #include "dpst_launch.cuh"
 
 namespace dpst {
+bool own_fft_df_supported(int nx, int ny);
+std::vector<float4> fft_twiddles_df(int n);
+cudaError_t fft_setup_df(int nx, int ny);
+cudaError_t fft_rows_df(bool inverse, const double *grid_in, double2 *spec_out, const double2 *spec_in,
+                        double *grid_out, int nx, int64_t rows, const float4 *twx, cudaStream_t s);
+cudaError_t fft_cols_df(bool inverse, double2 *spec, int ny, int nxh, int64_t planes, const float4 *twy,
+                        cudaStream_t s);
+}  // namespace dpst
+
+namespace dpst {
 
 // backward-pass kernels (dpst_grad.cu)
 template <typename R>
@@ -413,6 +423,13 @@ struct EngineTP : EngineBase {
   // (default) overrides the choice.
   bool zfused = false;
   DevBuf twz;  // exp(-2 pi i m / nz), m < nz, in R
+  // FP64 operator on the 3-D path: the library's double-float transforms
+  // (x rows, y columns, z columns) when faster than cuFFT's FP64 3-D ones at
+  // creation; timings {cuFFT, own} of a forward + inverse pair
+  bool own3d = false;
+  DevBuf twxd, twyd, twzd;
+  float own3d_ms[2] = {0.0f, 0.0f};
+  cudaStream_t cur_stream = 0;
 
   EngineTP(const dpst_params &prm, int64_t n, int dev) {
     p = prm;
@@ -480,7 +497,48 @@ struct EngineTP : EngineBase {
                                sizeof(R) == 8 ? CUFFT_Z2D : CUFFT_C2R, 3));
     }
     plans = true;
+    if (sizeof(R) == 8 && !zfused && own_fft_df_supported(nx, ny) && own_fft_df_supported(nx, nz) &&
+        !(getenv("DPSTOKES_GB300_XY_FFT") && std::string(getenv("DPSTOKES_GB300_XY_FFT")) == "cufft")) {
+      upload(twxd, fft_twiddles_df(nx));
+      upload(twyd, fft_twiddles_df(ny));
+      upload(twzd, fft_twiddles_df(nz));
+      DPST_CUDA(fft_setup_df(nx, ny));
+      DPST_CUDA(fft_setup_df(nx, nz));
+      const char *env = getenv("DPSTOKES_GB300_XY_FFT");
+      tune_own3d(env && std::string(env) == "own");
+    }
     DPST_CUDA(cudaDeviceSynchronize());
+  }
+
+  // cuFFT's FP64 3-D pair against the double-float kernels' pair on the
+  // grid and spectrum buffers (one warm-up, best of three)
+  void tune_own3d(bool force) {
+    cudaEvent_t e0, e1;
+    DPST_CUDA(cudaEventCreate(&e0));
+    DPST_CUDA(cudaEventCreate(&e1));
+    DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
+    cur_stream = 0;
+    DPST_CUFFT(cufftSetStream(plan_f, 0));
+    DPST_CUFFT(cufftSetStream(plan_b, 0));
+    for (int form = 0; form < 2; ++form) {
+      own3d = form == 1;
+      float best = 1e30f;
+      for (int r = 0; r < 4; ++r) {
+        DPST_CUDA(cudaEventRecord(e0, 0));
+        exec_fwd(grid.as<R>(), spec.as<CR>());
+        exec_inv(spec.as<CR>(), grid.as<R>());
+        DPST_CUDA(cudaEventRecord(e1, 0));
+        DPST_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        DPST_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0) best = std::min(best, ms);
+      }
+      own3d_ms[form] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    own3d = force || own3d_ms[1] < own3d_ms[0];
+    DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
   }
 
   ~EngineTP() override {
@@ -571,12 +629,35 @@ struct EngineTP : EngineBase {
   }
 
   void exec_fwd(R *gr, CR *sp) {
+    if constexpr (sizeof(R) == 8) {
+      if (own3d) {  // x rows, y columns over every (component, z) plane, then z columns per component
+        DPST_CUDA(fft_rows_df(false, reinterpret_cast<const double *>(gr), reinterpret_cast<double2 *>(sp), nullptr,
+                              nullptr, nx, 3 * (int64_t)nz * ny, twxd.as<float4>(), cur_stream));
+        DPST_CUDA(fft_cols_df(false, reinterpret_cast<double2 *>(sp), ny, nxh, 3 * (int64_t)nz, twyd.as<float4>(),
+                              cur_stream));
+        DPST_CUDA(fft_cols_df(false, reinterpret_cast<double2 *>(sp), nz, ny * nxh, 3, twzd.as<float4>(),
+                              cur_stream));
+        return;
+      }
+    }
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecD2Z(plan_f, (cufftDoubleReal *)gr, (cufftDoubleComplex *)sp));
     else
       DPST_CUFFT(cufftExecR2C(plan_f, (cufftReal *)gr, (cufftComplex *)sp));
   }
   void exec_inv(CR *sp, R *gr) {
+    if constexpr (sizeof(R) == 8) {
+      if (own3d) {
+        DPST_CUDA(fft_cols_df(true, reinterpret_cast<double2 *>(sp), nz, ny * nxh, 3, twzd.as<float4>(),
+                              cur_stream));
+        DPST_CUDA(fft_cols_df(true, reinterpret_cast<double2 *>(sp), ny, nxh, 3 * (int64_t)nz, twyd.as<float4>(),
+                              cur_stream));
+        DPST_CUDA(fft_rows_df(true, nullptr, nullptr, reinterpret_cast<const double2 *>(sp),
+                              reinterpret_cast<double *>(gr), nx, 3 * (int64_t)nz * ny, twxd.as<float4>(),
+                              cur_stream));
+        return;
+      }
+    }
     if (sizeof(R) == 8)
       DPST_CUFFT(cufftExecZ2D(plan_b, (cufftDoubleComplex *)sp, (cufftDoubleReal *)gr));
     else
@@ -588,6 +669,7 @@ struct EngineTP : EngineBase {
   void solve_stage(bool torque, cudaStream_t s, R *on = nullptr) {
     R *gr = on ? on : grid.as<R>();
     CR *sp = spec.as<CR>();
+    cur_stream = s;
     DPST_CUFFT(cufftSetStream(plan_f, s));
     exec_fwd(gr, sp);
     if (reg && torque) exec_fwd(gridT.as<R>(), specT.as<CR>());
@@ -828,6 +910,9 @@ struct EngineTP : EngineBase {
     o->kernels_per_mdot = particle_passes + 1 + particle_passes;
     o->fused_particle_passes = fused ? 1 : 0;
     o->z_fused = zfused ? 1 : 0;
+    o->xy_transform = own3d ? 3 : 0;
+    o->xy_ms[0] = own3d_ms[0];
+    o->xy_ms[1] = own3d_ms[1];
     int64_t b = 0;
     const DevBuf *all[] = {&grid, &spec, &kvx, &kvy, &kvz, &pos64, &flags, &ord_count, &ord_start, &perm, &dphzw_buf,
                            &gridT, &specT, &twz, &grid2};

@@ -288,3 +288,33 @@ def test_backward_forces_torques(name):
     if T is not None:
         assert rel_err(gT, Wo) < TOL_FP64
     op.close()
+
+
+@pytest.mark.parametrize("name", ["t0_tp_n2048", "t1_tp_n65536@128"])
+def test_fp64_periodic_double_float_transforms(name, monkeypatch):
+    """The triply periodic FP64 operator on the library's double-float 3-D
+    transforms (x rows, y and z columns) against cuFFT's FP64 3-D transforms
+    (1e-12), and the reference fixture where one exists (1e-10)."""
+    import golden_io
+    w = W.by_name(name)
+    X, F, T = W.make_inputs(w)
+    out = {}
+    for which in ("own", "cufft"):
+        monkeypatch.setenv("DPSTOKES_GB300_XY_FFT", which)
+        op = DPStokes(StokesParams.from_workload(w, "fp64"), w.N)
+        form = op.info()["xy_transform"]
+        op.set_positions(torch.tensor(X, device=op.device))
+        V, Wv = op.mdot(torch.tensor(F, device=op.device),
+                        torch.tensor(T, device=op.device) if T is not None else None)
+        torch.cuda.synchronize()
+        out[which] = (form, V.cpu().numpy(), Wv.cpu().numpy() if Wv is not None else None)
+        op.close()
+    assert out["own"][0] == 3 and out["cufft"][0] == 0
+    ev = rel_err(out["own"][1], out["cufft"][1])
+    print("%s TP FP64 own double-float vs cuFFT V %.2e" % (name, ev))
+    assert ev < 1e-12
+    if T is not None:
+        assert rel_err(out["own"][2], out["cufft"][2]) < 1e-12
+    if name in golden_io.names():
+        _, _, _, _, gd = golden_io.inputs(name)
+        assert rel_err(golden_io.restrict(gd, out["own"][1]), gd["V"]) < 1e-10
