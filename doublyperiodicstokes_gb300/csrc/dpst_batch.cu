@@ -60,7 +60,7 @@ cudaError_t launch_zgemm_b(const ZSeg<R> *segs, const int64_t *tprefix, int S, i
                            int nsm, cudaStream_t s, bool fold_out);
 int64_t ztc_tiles(int64_t ncols);
 cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
-                              const float *Tm, bool inverse, int nsm, int *err, cudaStream_t s);
+                              const float *Tm, bool corr, int nsm, int *err, cudaStream_t s);
 cudaError_t launch_corr_add_b(const ZSeg<float> *segs, const int64_t *mprefix, int S, int64_t K, int nz, int wall,
                               cudaStream_t s);
 
@@ -156,8 +156,9 @@ struct BatchEngine : BatchBase {
         // epilogue's four warps are too few for its arithmetic)
         const bool walls = inverse && mode != DPST_MODE_NOWALL;
         const ZSeg<R> *tsegs = walls ? d_segi_nc.template as<ZSeg<R>>() : segs;
+        // no segment's epilogue corrects (the correction is its own pass)
         DPST_CUDA(launch_zgemm_tc_b(reinterpret_cast<const ZSeg<float> *>(tsegs), d_tprefix_tc.as<int64_t>(), S,
-                                    ntiles_tc, nz, reinterpret_cast<const float *>(Tm), inverse, nsm,
+                                    ntiles_tc, nz, reinterpret_cast<const float *>(Tm), false, nsm,
                                     ztc_err.as<int>(), s));
         if (walls)
           DPST_CUDA(launch_corr_add_b(reinterpret_cast<const ZSeg<float> *>(segs), d_mprefix.as<int64_t>(), S, K, nz,

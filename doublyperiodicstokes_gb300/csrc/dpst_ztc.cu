@@ -204,7 +204,9 @@ static __device__ __forceinline__ ZtcTile ztc_tile(int64_t t, float *spec, int n
   return z;
 }
 
-template <bool INVERSE, bool BATCH>
+// CORR: the epilogue may add the wall correction (inverse with walls); the
+// inverse's 1/(nx ny) scale is applied in either instantiation.
+template <bool CORR, bool BATCH>
 __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz, int64_t ncols,
                                                              const float *__restrict__ Tm, EpiArgs e, int *err,
                                                              const ZSeg<float> *__restrict__ segs,
@@ -371,8 +373,8 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
       }
       const EpiArgs &et = BATCH ? *eslot : e;
       const bool v4 = (ncols_t & 3) == 0;  // 16-byte aligned rows
-      const bool corr = INVERSE && et.ks.mode != 0 && et.corr != nullptr;
-      const float scale = INVERSE ? (float)et.scale : 1.0f;
+      const bool corr = CORR && et.inverse && et.ks.mode != 0 && et.corr != nullptr;
+      const float scale = et.inverse ? (float)et.scale : 1.0f;
       const uint32_t tbase = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * ZTC_N);
       tmem_ld(tbase);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -403,12 +405,10 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
               q.z += c1r;
               q.w += c1i;
             }
-            if (INVERSE) {
-              q.x *= scale;
-              q.y *= scale;
-              q.z *= scale;
-              q.w *= scale;
-            }
+            q.x *= scale;
+            q.y *= scale;
+            q.z *= scale;
+            q.w *= scale;
             float *g = zt.B + (int64_t)r * ncols_t + col;
             if (v4) {
               __stcs(reinterpret_cast<float4 *>(g), q);
@@ -477,17 +477,17 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
 
 template <bool BATCH>
 static cudaError_t ztc_launch(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
-                              const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, bool inverse,
+                              const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, bool corr,
                               cudaStream_t s) {
   if (nz > 128) return cudaErrorInvalidValue;
   const size_t smem = BATCH ? ztc_smem_bytes_b(nz) : ztc_smem_bytes(nz);
   cudaError_t r;
-  if (inverse)
+  if (corr)
     r = cudaFuncSetAttribute(k_zgemm_tc<true, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   else r = cudaFuncSetAttribute(k_zgemm_tc<false, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (r != cudaSuccess) return r;
   int per_sm = 0;
-  if (inverse)
+  if (corr)
     r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<true, BATCH>, ZTC_THREADS, smem);
   else r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zgemm_tc<false, BATCH>, ZTC_THREADS, smem);
   if (r != cudaSuccess) return r;
@@ -496,7 +496,7 @@ static cudaError_t ztc_launch(float *spec, int nz, int64_t ncols, const float *T
   int64_t grid = (int64_t)nsm * per_sm;
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return cudaSuccess;
-  if (inverse)
+  if (corr)
     k_zgemm_tc<true, BATCH><<<(unsigned)grid, ZTC_THREADS, smem, s>>>(spec, nz, ncols, Tm, e, err, segs, tprefix, S,
                                                                       ntiles);
   else
@@ -508,19 +508,21 @@ static cudaError_t ztc_launch(float *spec, int nz, int64_t ncols, const float *T
 cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm,
                             int *err, cudaStream_t s) {
   const int64_t ntiles = 3 * ((ncols + ZTC_N - 1) / ZTC_N);
-  return ztc_launch<false>(spec, nz, ncols, Tm, e, nsm, err, nullptr, nullptr, 0, ntiles, e.inverse != 0, s);
+  const bool corr = e.inverse != 0 && e.ks.mode != 0 && e.corr != nullptr;
+  return ztc_launch<false>(spec, nz, ncols, Tm, e, nsm, err, nullptr, nullptr, 0, ntiles, corr, s);
 }
 
 // Batched systems: one launch over the tiles of every segment (system);
 // tprefix: S + 1 prefix counts of 3 ceil(ncols_s / 128) tiles, in device
 // memory, ntiles = tprefix[S].  Segments share nz and T.
 int64_t ztc_tiles(int64_t ncols) { return 3 * ((ncols + ZTC_N - 1) / ZTC_N); }
+// corr: some segment's epilogue adds a wall correction (else the lighter
+// instantiation runs; each segment's EpiArgs says whether it is an inverse).
 cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
-                              const float *Tm, bool inverse, int nsm, int *err, cudaStream_t s) {
+                              const float *Tm, bool corr, int nsm, int *err, cudaStream_t s) {
   EpiArgs e;
   memset(&e, 0, sizeof(e));
-  e.inverse = inverse ? 1 : 0;
-  return ztc_launch<true>(nullptr, nz, 0, Tm, e, nsm, err, segs, tprefix, S, ntiles, inverse, s);
+  return ztc_launch<true>(nullptr, nz, 0, Tm, e, nsm, err, segs, tprefix, S, ntiles, corr, s);
 }
 
 // ---------------------------------------------------------------------------
