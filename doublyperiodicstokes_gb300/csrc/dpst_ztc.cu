@@ -278,16 +278,28 @@ __global__ void __launch_bounds__(ZTC_THREADS, 1) k_zgemm_tc(float *spec, int nz
     cur.B = spec;
     cur.ncols = ncols;
     cur.col0 = 0;
+    const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;  // single system: tiles per component
     auto load_step = [&](int u, float (&br)[ZTC_QPT][4]) {
       const bool valid = u < my_steps;
       const int j = valid ? u / nkc : 0, c = valid ? u - j * nkc : 0;
-      if (valid && j != cur_j) {
-        cur = ztc_tile<BATCH>(blockIdx.x + (int64_t)j * G, spec, nz, ncols, segs, tprefix, S);
-        cur_j = j;
+      int64_t col;
+      const float *B;
+      int64_t nc;
+      if constexpr (BATCH) {
+        if (valid && j != cur_j) {
+          cur = ztc_tile<BATCH>(blockIdx.x + (int64_t)j * G, spec, nz, ncols, segs, tprefix, S);
+          cur_j = j;
+        }
+        col = valid ? cur.col0 + n : 0;
+        B = cur.B;
+        nc = cur.ncols;
+      } else {
+        const int64_t t = blockIdx.x + (int64_t)j * G;
+        const int d = valid ? (int)(t / tpc) : 0;
+        col = valid ? (t % tpc) * ZTC_N + n : 0;
+        B = spec + (int64_t)d * nz * ncols;
+        nc = ncols;
       }
-      const int64_t col = valid ? cur.col0 + n : 0;
-      const float *B = cur.B;
-      const int64_t nc = cur.ncols;
 #pragma unroll
       for (int i = 0; i < ZTC_QPT; ++i) {
         const int q = qg + ZTC_PGROUPS * i;
