@@ -409,6 +409,9 @@ template <typename R>
 cudaError_t launch_bvp_df_cols(const KsArgs &a, R *spec0, int64_t sstride, double2 *corr0, float2 *corrf0,
                                int64_t cstride, int ncol, float2 *scratch, int64_t grid, int variant,
                                cudaStream_t s);
+template <typename R>
+cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid, int variant,
+                          cudaStream_t s);
 
 // Persistent kernel: CTA b owns the units of 8 wavenumbers [b per_cta,
 // (b+1) per_cta) and its warps take them from a shared-memory counter.
@@ -942,33 +945,55 @@ cudaError_t launch_bvp_df_b<double>(const SysK<double> *sys, int S, const int64_
   return df_launch_b<DfV1>(sys, S, mprefix, K, nz, mode, scratch, grid, ncol, s);
 }
 
-// The adjoint: the forward plan's grid, twice its scratch (cp_bar, dp_bar).
+template <typename CFG, typename R>
+static cudaError_t adj_setup(int nz) {
+  const int nt = bvp_df_threads(nz, CFG::MAXT);
+  const size_t smem = sizeof(float2) * (size_t)((nz + 1) / 2) * nt;
+  return cudaFuncSetAttribute(k_bvp_adj_df<R, CFG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+// The adjoint: the forward plan's grid, twice its scratch (cp_bar, dp_bar),
+// sized for the largest variant.
 cudaError_t bvp_adj_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes) {
   cudaError_t err = bvp_df_plan(a, nsm, grid, scratch_bytes);
-  if (err != cudaSuccess) return err;
-  const int nt = bvp_df_threads(a.nz, DfV1::MAXT);
-  const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
-  err = cudaFuncSetAttribute(k_bvp_adj_df<float, DfV1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  err = cudaFuncSetAttribute(k_bvp_adj_df<double, DfV1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (err == cudaSuccess) err = adj_setup<DfV0, float>(a.nz);
+  if (err == cudaSuccess) err = adj_setup<DfV1, float>(a.nz);
+  if (err == cudaSuccess) err = adj_setup<DfV2, float>(a.nz);
+  if (err == cudaSuccess) err = adj_setup<DfV3, float>(a.nz);
+  if (err == cudaSuccess) err = adj_setup<DfV1, double>(a.nz);
   if (err != cudaSuccess) return err;
   *scratch_bytes *= 2;
   return cudaSuccess;
 }
 
-template <typename R>
-cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid,
-                          cudaStream_t s) {
-  const int nt = bvp_df_threads(a.nz, DfV1::MAXT);
+template <typename CFG, typename R>
+static cudaError_t adj_launch(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+                              cudaStream_t s) {
+  const int nt = bvp_df_threads(a.nz, CFG::MAXT);
   const size_t smem = sizeof(float2) * (size_t)((a.nz + 1) / 2) * nt;
   const int64_t units = (a.nk + 7) / 8;
   const int per_cta = (int)((units + grid - 1) / grid);
-  k_bvp_adj_df<R, DfV1><<<(unsigned)grid, nt, smem, s>>>(a, spec, cadj, scratch, per_cta);
+  k_bvp_adj_df<R, CFG><<<(unsigned)grid, nt, smem, s>>>(a, spec, cadj, scratch, per_cta);
   return cudaGetLastError();
 }
-template cudaError_t launch_adj_df<float>(const KsArgs &, float *, const double2 *, float2 *, int64_t, cudaStream_t);
-template cudaError_t launch_adj_df<double>(const KsArgs &, double *, const double2 *, float2 *, int64_t,
-                                           cudaStream_t);
+
+// variant as for the forward solve (the FP64-I/O instantiation: variant 1)
+template <>
+cudaError_t launch_adj_df<float>(const KsArgs &a, float *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+                                 int variant, cudaStream_t s) {
+  switch (variant) {
+    case 0: return adj_launch<DfV0>(a, spec, cadj, scratch, grid, s);
+    case 2: return adj_launch<DfV2>(a, spec, cadj, scratch, grid, s);
+    case 3: return adj_launch<DfV3>(a, spec, cadj, scratch, grid, s);
+    default: return adj_launch<DfV1>(a, spec, cadj, scratch, grid, s);
+  }
+}
+template <>
+cudaError_t launch_adj_df<double>(const KsArgs &a, double *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+                                  int variant, cudaStream_t s) {
+  (void)variant;
+  return adj_launch<DfV1>(a, spec, cadj, scratch, grid, s);
+}
 
 template <typename CFG, typename R>
 static cudaError_t df_launch(const KsArgs &a, R *spec, double2 *corr, float2 *scratch, int64_t grid,

@@ -76,7 +76,7 @@ cudaError_t launch_bvp_k0_b(const SysK<R> *sys, int S, cudaStream_t s);
 // double-float adjoint solve (dpst_bvp_df.cu) and the FP64 k = 0 adjoint
 cudaError_t bvp_adj_df_plan(const KsArgs &a, int nsm, int64_t *grid, size_t *scratch_bytes);
 template <typename R>
-cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid,
+cudaError_t launch_adj_df(const KsArgs &a, R *spec, const double2 *cadj, float2 *scratch, int64_t grid, int variant,
                           cudaStream_t s);
 template <typename R>
 cudaError_t launch_adj_k0(const KsArgs &a, R *spec, cudaStream_t s);
@@ -1211,6 +1211,41 @@ struct Engine : EngineBase {
   Ghosts<R> gham, ghad;
   bool grad_ready = false;
 
+  // The double-float adjoint's kernel variant, timed like the forward's on
+  // the spectrum buffer (FP32 spectra; DPSTOKES_GB300_SOLVE_VARIANT fixes it)
+  int adj_variant = 1;
+  float adj_ms[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  void tune_adjoint() {
+    if (sizeof(R) != 4) return;
+    const char *env = getenv("DPSTOKES_GB300_SOLVE_VARIANT");
+    if (env && *env) {
+      adj_variant = atoi(env);
+      return;
+    }
+    cudaEvent_t a, b;
+    DPST_CUDA(cudaEventCreate(&a));
+    DPST_CUDA(cudaEventCreate(&b));
+    float best = 0.0f;
+    for (int v = 0; v < bvp_df_variants(); ++v) {
+      auto run = [&] {
+        DPST_CUDA(launch_adj_df<R>(ks, spec.as<R>(), corr.as<double2>(), adj_scratch.as<float2>(), adj_grid, v, 0));
+      };
+      run();
+      DPST_CUDA(cudaEventRecord(a, 0));
+      for (int rep = 0; rep < 3; ++rep) run();
+      DPST_CUDA(cudaEventRecord(b, 0));
+      DPST_CUDA(cudaEventSynchronize(b));
+      DPST_CUDA(cudaEventElapsedTime(&adj_ms[v], a, b));
+      adj_ms[v] /= 3.0f;
+      if (v == 0 || adj_ms[v] < best) {
+        best = adj_ms[v];
+        adj_variant = v;
+      }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+
   void ensure_grad() {
     if (!grad_ready) {
       grid2.alloc(grid.bytes);
@@ -1221,6 +1256,7 @@ struct Engine : EngineBase {
         DPST_CUDA(adj_plan<R>(ks, nsm, &adj_grid, &bytes));
       }
       adj_scratch.alloc(bytes);
+      if (dfsolve) tune_adjoint();
       std::vector<double> tf, ti;
       dct_matrices(nz, tf, ti);
       const double sc = 1.0 / ((double)nx * (double)ny);
@@ -1289,7 +1325,8 @@ struct Engine : EngineBase {
     e.ks = ks;
     DPST_CUDA(zgemm((R *)sp, TiT.as<R>(), e, false, s));
     if (dfsolve) {
-      DPST_CUDA(launch_adj_df<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<float2>(), adj_grid, s));
+      DPST_CUDA(launch_adj_df<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<float2>(), adj_grid, adj_variant,
+                                 s));
       DPST_CUDA(launch_adj_k0<R>(ks, (R *)sp, s));
     } else {
       DPST_CUDA(launch_adj_solve<R>(ks, (R *)sp, corr.as<double2>(), adj_scratch.as<double>(), adj_grid, s));

@@ -217,3 +217,33 @@ def test_adjoint_df64_solve(name):
     scale = np.sqrt(np.sum(gV * gV) * np.sum(V * V))
     print("%s transpose identity %.2e" % (name, abs(lhs - rhs) / scale))
     assert abs(lhs - rhs) < 1e-12 * scale
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_mixed_adjoint_every_variant(variant, monkeypatch):
+    """The mixed operator's backward with each double-float adjoint variant
+    (DPSTOKES_GB300_SOLVE_VARIANT) against the FP64 backward: dl/dF 1e-5,
+    dl/dX 1e-4, on a bottom-wall case with torques."""
+    w = _wl("c2_dp_n65536@64")
+    X, F, T = W.make_inputs(w)
+    rng = np.random.default_rng(21)
+    gV = rng.standard_normal(F.shape)
+    gW = rng.standard_normal(F.shape)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        if prec == "mixed":
+            monkeypatch.setenv("DPSTOKES_GB300_SOLVE_VARIANT", str(variant))
+        op = DPStokes(StokesParams.from_workload(w, prec), w.N)
+        dt = torch.float64 if prec == "fp64" else torch.float32
+        d = op.device
+        op.set_positions(torch.tensor(X, device=d))
+        out = op.mdot_backward(torch.tensor(F, dtype=dt, device=d), torch.tensor(T, dtype=dt, device=d),
+                               torch.tensor(gV, dtype=dt, device=d), torch.tensor(gW, dtype=dt, device=d),
+                               need_F=True, need_T=True, need_X=True)
+        torch.cuda.synchronize()
+        res[prec] = [a.double().cpu().numpy() for a in out]
+        op.close()
+        monkeypatch.delenv("DPSTOKES_GB300_SOLVE_VARIANT", raising=False)
+    e = [rel_err(a, b) for a, b in zip(res["mixed"], res["fp64"])]
+    print("variant %d mixed vs fp64 backward %s" % (variant, " ".join("%.2e" % x for x in e)))
+    assert e[0] < 1e-5 and e[1] < 1e-5 and e[2] < 1e-4
