@@ -310,7 +310,7 @@ def run_ours(args, rank, world):
     # the z transform as a dense contraction: 2 nz^2 flops per real column (3 x 2 nk columns) per
     # product, three TF32 products (split TF32) on the tensor pipe; TF32 dense rate taken as half
     # the measured BF16 rate
-    if w.domType != "TP" and info.get("ztransform") == 1 and stages.get("ztrans_fwd", 0) > 0:
+    if w.domType != "TP" and info.get("ztransform") in (1, 3) and stages.get("ztrans_fwd", 0) > 0:
         nk = w.ny * (w.nx // 2 + 1)
         flops = 3 * 2.0 * w.nz * w.nz * 3 * 2 * nk
         tf32_peak = peaks["bf16_tflops"] / 2.0
@@ -320,9 +320,18 @@ def run_ours(args, rank, world):
             "achieved_tflops_inv": flops / (stages["ztrans_inv"] * 1e-3) / 1e12,
             "peak_tflops": tf32_peak, "peak_source": peak_kind + " bf16_tflops / 2 (TF32 dense)",
             "frac_fwd": flops / (stages["ztrans_fwd"] * 1e-3) / 1e12 / tf32_peak}
-    roof["ztransform_kernel"] = "tcgen05 split-TF32" if info.get("ztransform") == 1 else "SIMT folded"
-    roof["ztransform_inverse_kernel"] = ("tcgen05 split-TF32" if info.get("ztransform_inverse") == 1
-                                         else "SIMT folded")
+    znames = {0: "SIMT folded", 1: "tcgen05 split-TF32", 2: "double-float SIMT",
+              3: "tcgen05 split-TF32, TMA-fed"}
+    roof["ztransform_kernel"] = znames.get(info.get("ztransform"), "SIMT folded")
+    roof["ztransform_inverse_kernel"] = znames.get(info.get("ztransform_inverse"), "SIMT folded")
+    if info.get("ztransform_tma_ms") and info["ztransform_tma_ms"][0] > 0:
+        roof["ztransform_creation_ms"] = {
+            "forward": {"simt": round(float(info["ztransform_ms"][0]), 4),
+                        "tcgen05": round(float(info["ztransform_ms"][1]), 4),
+                        "tcgen05_tma": round(float(info["ztransform_tma_ms"][0]), 4)},
+            "inverse": {"simt": round(float(info["ztransform_inverse_ms"][0]), 4),
+                        "tcgen05": round(float(info["ztransform_inverse_ms"][1]), 4),
+                        "tcgen05_tma": round(float(info["ztransform_tma_ms"][1]), 4)}}
     if dom == "solve" and arith == "double-float":
         # the double-float solve is issue bound (FP32 FMA chains of the
         # compensated sweeps): its DRAM traffic is measured by ncu, and the

@@ -41,7 +41,8 @@ class DpstInfo(ctypes.Structure):
                 ("ztransform_inverse_ms", ctypes.c_float * 2), ("z_fused", ctypes.c_int),
                 ("solve_arith", ctypes.c_int), ("solve_variant", ctypes.c_int),
                 ("solve_ms", ctypes.c_float * 4), ("xy_transform", ctypes.c_int),
-                ("xy_ms", ctypes.c_float * 2), ("spread_tiles", ctypes.c_int)]
+                ("xy_ms", ctypes.c_float * 2), ("spread_tiles", ctypes.c_int),
+                ("ztransform_tma_ms", ctypes.c_float * 2)]
 
 
 class DpstBatchInfo(ctypes.Structure):

@@ -119,6 +119,9 @@ cudaError_t launch_zgemm_tc(float *spec, int nz, int64_t ncols, const float *Tm,
 cudaError_t launch_zgemm_df(double *spec, int nz, int64_t ncols, const double *Tm, const EpiArgs &e, int nsm,
                             cudaStream_t s, bool fold_out);
 cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s);
+bool ztm_supported(const float *spec, int nz, int64_t ncols);
+cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
+                             cudaStream_t s);
 bool tile_spread_supported(const KernelDesc &km, const KernelDesc &kd, int nx, int ny, int nz);
 cudaError_t tile_spread_setup(int nz);
 template <typename R>
@@ -694,13 +697,15 @@ struct Engine : EngineBase {
 
   // ---- z transform kernel choice (creation-time autotuner) -----------------
   // 0: SIMT even/odd-folded GEMM (FP32 or FP64); 1: tcgen05 split-TF32 (FP32
-  // data only, nz <= 128).  Chosen separately for the plain transforms
-  // (ztc[0]: forward, and the backward's adjoint transforms) and for the
-  // inverse with its wall-correction epilogue (ztc[1]), each timed on this
-  // handle's buffers.  DPSTOKES_GB300_ZTRANSFORM = simt | tcgen05 | auto
-  // (default) overrides the choice.
+  // data only, nz <= 128), operands staged through registers; 3: the same
+  // fed by TMA (nz >= 32, an even number of modes).  Chosen separately for
+  // the plain transforms (ztc[0]: forward, and the backward's adjoint
+  // transforms) and for the inverse with its wall correction (ztc[1]), each
+  // timed on this handle's buffers.  DPSTOKES_GB300_ZTRANSFORM = simt |
+  // tcgen05 | tma | auto (default) overrides the choice.
   int ztc[2] = {0, 0};
   float ztc_ms[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [direction][impl]
+  float ztm_ms[2] = {0.f, 0.f};                   // [direction]: the TMA-fed form
   DevBuf ztc_err;
 
   // the wall-correction inputs of the inverse transform's epilogue
@@ -716,7 +721,7 @@ struct Engine : EngineBase {
 
   // impl < 0: the tuned kernel for e's direction; 0 SIMT in the operator's
   // arithmetic, 1 tcgen05 split-TF32 (FP32 spectra), 2 double-float SIMT
-  // (FP64 spectra)
+  // (FP64 spectra), 3 tcgen05 split-TF32 fed by TMA (FP32 spectra)
   cudaError_t zgemm(R *sp, const R *T, const EpiArgs &e, bool fold_out, cudaStream_t s, int impl = -1) {
     if (impl < 0) impl = ztc[e.inverse ? 1 : 0];
     if constexpr (sizeof(R) == 8) {
@@ -724,20 +729,23 @@ struct Engine : EngineBase {
         return launch_zgemm_df(reinterpret_cast<double *>(sp), nz, 2 * nk, reinterpret_cast<const double *>(T), e,
                                nsm, s, fold_out);
     }
-    if (impl == 1 && sizeof(R) == 4) {
+    if ((impl == 1 || impl == 3) && sizeof(R) == 4) {
+      float *fs = reinterpret_cast<float *>(sp);
+      const float *fT = reinterpret_cast<const float *>(T);
+      const bool tma = impl == 3 && ztm_supported(fs, nz, 2 * nk);
       if (e.inverse && e.ks.mode != 0 && e.corr != nullptr) {
         // the wall correction as its own pass: the tcgen05 epilogue's four
         // warps are too few for its arithmetic
         EpiArgs e2 = e;
         e2.corr = nullptr;
         e2.corrf = nullptr;
-        cudaError_t r = launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk,
-                                        reinterpret_cast<const float *>(T), e2, nsm, ztc_err.as<int>(), s);
-        if (r == cudaSuccess) r = launch_corr_add(reinterpret_cast<float *>(sp), nz, nk, e, s);
+        cudaError_t r = tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e2, nsm, ztc_err.as<int>(), s)
+                            : launch_zgemm_tc(fs, nz, 2 * nk, fT, e2, nsm, ztc_err.as<int>(), s);
+        if (r == cudaSuccess) r = launch_corr_add(fs, nz, nk, e, s);
         return r;
       }
-      return launch_zgemm_tc(reinterpret_cast<float *>(sp), nz, 2 * nk, reinterpret_cast<const float *>(T), e, nsm,
-                             ztc_err.as<int>(), s);
+      return tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e, nsm, ztc_err.as<int>(), s)
+                 : launch_zgemm_tc(fs, nz, 2 * nk, fT, e, nsm, ztc_err.as<int>(), s);
     }
     return launch_zgemm<R>(sp, nz, 2 * nk, T, e, nsm, s, fold_out);
   }
@@ -789,6 +797,7 @@ struct Engine : EngineBase {
     }
     if (nz > 128 || want == "simt") return;
     R *sp = reinterpret_cast<R *>(spec.p);
+    const bool tma_ok = want != "tcgen05" && ztm_supported(reinterpret_cast<const float *>(sp), nz, 2 * nk);
     DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
     DPST_CUDA(cudaMemset(corr.p, 0, corr.bytes));
     cudaEvent_t a, b;
@@ -802,14 +811,17 @@ struct Engine : EngineBase {
       e.scale = dir ? 1.0 / ((double)nx * (double)ny) : 1.0;
       if (dir) epi_corr(e);
       const R *T = dir ? Ti.as<R>() : Tf.as<R>();
-      for (int impl = 0; impl < 2; ++impl) {
+      for (int k = 0; k < 3; ++k) {
+        const int impl = k == 2 ? 3 : k;
+        if (impl == 3 && !tma_ok) continue;
+        float ms = 0.0f;
         DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));  // warm-up
         DPST_CUDA(cudaEventRecord(a, 0));
         for (int rep = 0; rep < 3; ++rep) DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));
         DPST_CUDA(cudaEventRecord(b, 0));
         DPST_CUDA(cudaEventSynchronize(b));
-        DPST_CUDA(cudaEventElapsedTime(&ztc_ms[dir][impl], a, b));
-        ztc_ms[dir][impl] /= 3.0f;
+        DPST_CUDA(cudaEventElapsedTime(&ms, a, b));
+        (impl == 3 ? ztm_ms[dir] : ztc_ms[dir][impl]) = ms / 3.0f;
       }
     }
     cudaEventDestroy(a);
@@ -821,7 +833,19 @@ struct Engine : EngineBase {
       DPST_CUDA(cudaMemset(ztc_err.p, 0, sizeof(int)));
       return;
     }
-    for (int dir = 0; dir < 2; ++dir) ztc[dir] = (want == "tcgen05" || ztc_ms[dir][1] < ztc_ms[dir][0]) ? 1 : 0;
+    for (int dir = 0; dir < 2; ++dir) {
+      if (want == "tma" && tma_ok) ztc[dir] = 3;
+      else if (want == "tcgen05") ztc[dir] = 1;
+      else {
+        float best = ztc_ms[dir][0];
+        ztc[dir] = 0;
+        if (ztc_ms[dir][1] < best) {
+          best = ztc_ms[dir][1];
+          ztc[dir] = 1;
+        }
+        if (tma_ok && ztm_ms[dir] < best) ztc[dir] = 3;
+      }
+    }
   }
 
   // grid (spread forces) -> grid (velocities): x-y FFT, z transform, per-k
@@ -1461,6 +1485,8 @@ struct Engine : EngineBase {
     o->spread_tiles = (tile_spread && p.has_torque) ? 1 : 0;
     o->xy_ms[0] = sizeof(R) == 8 ? xyd_ms[0] : xy_ms[0];
     o->xy_ms[1] = sizeof(R) == 8 ? xyd_ms[1] : xy_ms[1];
+    o->ztransform_tma_ms[0] = ztm_ms[0];
+    o->ztransform_tma_ms[1] = ztm_ms[1];
     if (ownfft || ownfft_d) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
     if (sizeof(R) == 4 && ztc[1] && p.mode != DPST_MODE_NOWALL) o->kernels_per_mdot += 1;  // correction pass
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];

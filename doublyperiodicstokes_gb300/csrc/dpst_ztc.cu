@@ -32,6 +32,10 @@
 // an iteration deadline: on expiry the waiting thread records the error and
 // raises a shared abort flag that ends every role; the MMA thread then waits
 // (bounded) for its issued products before the tensor memory is freed.
+#include <cuda.h>
+
+#include <mutex>
+
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
 
@@ -535,6 +539,398 @@ cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, i
   EpiArgs e;
   memset(&e, 0, sizeof(e));
   return ztc_launch<true>(nullptr, nz, 0, Tm, e, nsm, err, segs, tprefix, S, ntiles, corr, s);
+}
+
+// ---------------------------------------------------------------------------
+// The same transform fed by the tensor memory accelerator (TMA).
+//
+// Differences from k_zgemm_tc:
+//   * T (hi, lo) is the MMA's A operand in tensor memory (columns 256-383
+//     hi, 384-511 lo; lane = row), written once with tcgen05.st, so shared
+//     memory holds only the streamed B operand and staging;
+//   * one thread issues cp.async.bulk.tensor loads of 32-row x 128-column
+//     FP32 blocks ([32][128] row-major, zero-filled past nz and ncols) into
+//     a ring of ZTM_RS stages, each completing on its mbarrier with the
+//     block's byte count; no register holds a load in flight;
+//   * 8 converter warps read a block from the ring, split it into TF32
+//     hi / lo and write the canonical K-major stages the MMAs read;
+//   * 4 epilogue warps scale the accumulator's 32 x 32 blocks into
+//     128-byte-swizzled staging (two buffers per warp) and store each block
+//     with one cp.async.bulk.tensor store (rows >= nz and columns >= ncols
+//     clipped by the tensor map).
+// The spectrum is one 3-D tensor [3][nz][ncols] (ncols a multiple of 4, so
+// that its rows start on 16-byte boundaries; every x coordinate is a
+// multiple of 32 columns).  No wall-correction epilogue: the inverse with
+// walls runs k_corr_add afterwards, as for the other tcgen05 form.
+// ---------------------------------------------------------------------------
+constexpr int ZTM_RS = 6;                                     // TMA ring stages
+constexpr int ZTM_CONV_WARPS = 8;
+constexpr int ZTM_EPI_WARPS = 4;
+constexpr int ZTM_MMA_WARP = ZTM_CONV_WARPS + ZTM_EPI_WARPS;  // warp 12
+constexpr int ZTM_TMA_WARP = ZTM_MMA_WARP + 1;                // warp 13
+constexpr int ZTM_THREADS = 32 * (ZTM_TMA_WARP + 1);
+constexpr int ZTM_TMEM_COLS = 512;                            // 2 accumulators, T hi, T lo
+constexpr uint32_t ZTM_COL_AHI = 2 * ZTC_N, ZTM_COL_ALO = 3 * ZTC_N;
+constexpr uint32_t ZTM_RAW_BYTES = ZTC_KC * ZTC_N * 4;        // 16 KB
+constexpr uint32_t ZTM_HL_BYTES = 2 * ZTC_N * ZTC_KC * 4;     // hi + lo, 32 KB
+constexpr uint32_t ZTM_STG_BYTES = 32 * 32 * 4;               // one 32 x 32 block, 4 KB
+constexpr size_t ZTM_OFF_HL = (size_t)ZTM_RS * ZTM_RAW_BYTES;
+constexpr size_t ZTM_OFF_STG = ZTM_OFF_HL + (size_t)ZTC_STAGES * ZTM_HL_BYTES;
+constexpr size_t ZTM_OFF_BAR = ZTM_OFF_STG + (size_t)ZTM_EPI_WARPS * 2 * ZTM_STG_BYTES;
+constexpr int ZTM_NBARS = 2 * ZTM_RS + 2 * ZTC_STAGES + 2 * ZTC_ACC + 1;
+constexpr size_t ZTM_SMEM = ZTM_OFF_BAR + ZTM_NBARS * 8 + 16 + 1024;  // + alignment slack
+static_assert(ZTM_SMEM <= 227 * 1024, "TMA z transform: shared memory");
+static_assert(ZTM_OFF_HL % 1024 == 0 && ZTM_OFF_STG % 1024 == 0, "1024-byte aligned regions");
+
+static __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+static __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
+                                                   uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+static __device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int x, int y, int z) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(src), "r"(x), "r"(y), "r"(z)
+               : "memory");
+}
+
+// D += A B with A (128 x 8 TF32) in tensor memory, B by descriptor
+static __device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t bd, uint32_t idesc,
+                                                   uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__global__ void __launch_bounds__(ZTM_THREADS, 1)
+    k_zgemm_tma(const __grid_constant__ CUtensorMap map_ld, const __grid_constant__ CUtensorMap map_st, int nz,
+                int64_t ncols, const float *__restrict__ Tm, float scale, int *err) {
+  extern __shared__ unsigned char ztm_raw_sm[];
+  // 1024-byte alignment of the swizzled staging (the dynamic window's base
+  // alignment is not guaranteed beyond 16 bytes)
+  unsigned char *sm = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(ztm_raw_sm) + 1023) & ~static_cast<uintptr_t>(1023));
+  const int kp = (nz + 7) & ~7;
+  const uint32_t raw0 = smem_u32(sm);
+  uint32_t *Hst = reinterpret_cast<uint32_t *>(sm + ZTM_OFF_HL);
+  const float *rawf = reinterpret_cast<const float *>(sm);
+  float *stg = reinterpret_cast<float *>(sm + ZTM_OFF_STG);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + ZTM_OFF_BAR);
+  const uint32_t bar0 = smem_u32(bars);
+  auto rfull_bar = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+  auto rempty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(ZTM_RS + s); };
+  auto full_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + s); };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + ZTC_STAGES + s); };
+  auto accf_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + 2 * ZTC_STAGES + a); };
+  auto acce_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + 2 * ZTC_STAGES + ZTC_ACC + a); };
+  const uint32_t drain_bar = bar0 + 8u * (uint32_t)(ZTM_NBARS - 1);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + ZTM_NBARS);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(ZTM_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < ZTM_RS; ++s) {
+      mbar_init(rfull_bar(s), 1);
+      mbar_init(rempty_bar(s), ZTM_CONV_WARPS);
+    }
+    for (int s = 0; s < ZTC_STAGES; ++s) {
+      mbar_init(full_bar(s), ZTM_CONV_WARPS);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int a = 0; a < ZTC_ACC; ++a) {
+      mbar_init(accf_bar(a), 1);
+      mbar_init(acce_bar(a), ZTM_EPI_WARPS);
+    }
+    mbar_init(drain_bar, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  if (warp == ZTM_TMA_WARP && lane == 0) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_ld)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_st)) : "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp >= ZTM_CONV_WARPS && warp < ZTM_MMA_WARP) {
+    // T split into tf32 hi / lo, row r = 32 (warp & 3) + lane of this warp's
+    // lane quadrant, 8 columns per tcgen05.st; rows and columns >= nz zero
+    const int r = 32 * (warp & 3) + lane;
+    const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    for (int k0 = 0; k0 < kp; k0 += 8) {
+      uint32_t h[8], l[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int k = k0 + i;
+        const float v = (r < nz && k < nz) ? Tm[r * nz + k] : 0.0f;
+        h[i] = to_tf32(v);
+        l[i] = to_tf32(v - __uint_as_float(h[i]));
+      }
+      asm volatile(
+          "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(
+              trow + ZTM_COL_AHI + (uint32_t)k0),
+          "r"(h[0]), "r"(h[1]), "r"(h[2]), "r"(h[3]), "r"(h[4]), "r"(h[5]), "r"(h[6]), "r"(h[7])
+          : "memory");
+      asm volatile(
+          "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(
+              trow + ZTM_COL_ALO + (uint32_t)k0),
+          "r"(l[0]), "r"(l[1]), "r"(l[2]), "r"(l[3]), "r"(l[4]), "r"(l[5]), "r"(l[6]), "r"(l[7])
+          : "memory");
+    }
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+
+  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;  // tiles per component
+  const int64_t ntiles = 3 * tpc;
+  const int64_t G = gridDim.x;
+  const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
+  const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
+  const int my_steps = my_tiles * nkc;         // step u = (tile u / nkc, K chunk u % nkc)
+  constexpr int SKQ = ZTC_KC / 4;
+
+  if (warp < ZTM_CONV_WARPS) {
+    // ---- converters: column n, row quads q = qg + ZTC_PGROUPS i of the chunk
+    const int n = tid % ZTC_N, qg = tid / ZTC_N;
+    for (int u = 0; u < my_steps; ++u) {
+      const int rs = u % ZTM_RS;
+      bool ok = ztc_wait(rfull_bar(rs), (uint32_t)((u / ZTM_RS) & 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      const float *rb = rawf + (size_t)rs * (ZTC_KC * ZTC_N);
+      float br[ZTC_QPT][4];
+#pragma unroll
+      for (int i = 0; i < ZTC_QPT; ++i) {
+        const int q = qg + ZTC_PGROUPS * i;
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) br[i][jj] = rb[(4 * q + jj) * ZTC_N + n];
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(rempty_bar(rs));
+      const int s = u % ZTC_STAGES;
+      ok = ztc_wait(empty_bar(s), (uint32_t)(((u / ZTC_STAGES) & 1) ^ 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      uint32_t *Bhi = Hst + (size_t)s * 2 * ZTC_N * ZTC_KC, *Blo = Bhi + ZTC_N * ZTC_KC;
+#pragma unroll
+      for (int i = 0; i < ZTC_QPT; ++i) {
+        const int q = qg + ZTC_PGROUPS * i;
+        uint4 h, l;
+        h.x = to_tf32(br[i][0]);
+        h.y = to_tf32(br[i][1]);
+        h.z = to_tf32(br[i][2]);
+        h.w = to_tf32(br[i][3]);
+        l.x = to_tf32(br[i][0] - __uint_as_float(h.x));
+        l.y = to_tf32(br[i][1] - __uint_as_float(h.y));
+        l.z = to_tf32(br[i][2] - __uint_as_float(h.z));
+        l.w = to_tf32(br[i][3] - __uint_as_float(h.w));
+        const int o = cm_off(n, 4 * q, SKQ);
+        *reinterpret_cast<uint4 *>(Bhi + o) = h;
+        *reinterpret_cast<uint4 *>(Blo + o) = l;
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(full_bar(s));
+    }
+  } else if (warp < ZTM_MMA_WARP) {
+    // ---- epilogue: warp owns lane quadrant qd = rows 32 qd .. 32 qd + 31
+    const int qd = warp & 3;
+    float *st0 = stg + (size_t)(warp - ZTM_CONV_WARPS) * 2 * (ZTM_STG_BYTES / 4);
+    uint32_t v[32];
+    auto tmem_ld = [&](uint32_t taddr) {
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+            "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+            "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr)
+          : "memory");
+    };
+    const bool rows_live = 32 * qd < nz;
+    int nst = 0;  // blocks stored by this warp (staging buffer nst & 1)
+    for (int j = 0; j < my_tiles; ++j) {
+      const int a = j % ZTC_ACC;
+      bool ok = ztc_wait(accf_bar(a), (uint32_t)((j / ZTC_ACC) & 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int64_t t = blockIdx.x + (int64_t)j * G;
+      const int d = (int)(t / tpc);
+      const int64_t col0 = (t % tpc) * ZTC_N;
+      const uint32_t tbase = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * ZTC_N);
+      tmem_ld(tbase);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int sb = 0; sb < ZTC_N / 32; ++sb) {
+        const bool live = rows_live && col0 + 32 * sb < ncols;
+        float *st = st0 + (size_t)(nst & 1) * (ZTM_STG_BYTES / 4);
+        if (live) {
+          // the buffer's store of two blocks ago has read its source
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+          __syncwarp();
+          // row `lane`: 16-byte chunk c at chunk position c ^ (lane & 7)
+          // (the 128-byte swizzle of the store's tensor map)
+          float4 *srow = reinterpret_cast<float4 *>(st + lane * 32);
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            srow[c ^ (lane & 7)] =
+                make_float4(__uint_as_float(v[4 * c]) * scale, __uint_as_float(v[4 * c + 1]) * scale,
+                            __uint_as_float(v[4 * c + 2]) * scale, __uint_as_float(v[4 * c + 3]) * scale);
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+        }
+        if (sb + 1 < ZTC_N / 32) tmem_ld(tbase + (uint32_t)(32 * (sb + 1)));
+        if (live) {
+          if (lane == 0) {
+            tma_store_3d(&map_st, smem_u32(st), (int)(col0 + 32 * sb), 32 * qd, d);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          }
+          ++nst;
+        }
+        if (sb + 1 < ZTC_N / 32) {
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (sb + 2 == ZTC_N / 32) {  // the last block is in registers: release the accumulator
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acce_bar(a));
+          }
+        }
+      }
+    }
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncwarp();
+  } else if (warp == ZTM_MMA_WARP) {
+    // ---- MMA warp: every lane takes the waits (warp vote), lane 0 issues
+    const uint32_t idesc = ztc_idesc(128, ZTC_N);
+    const uint32_t sbo_b = SKQ * 128;
+    for (int u = 0; u < my_steps; ++u) {
+      const int j = u / nkc, c = u - j * nkc;
+      const int s = u % ZTC_STAGES, a = j % ZTC_ACC;
+      bool ok = ztc_wait(full_bar(s), (uint32_t)((u / ZTC_STAGES) & 1), abort_flag, err);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      if (c == 0) {
+        ok = ztc_wait(acce_bar(a), (uint32_t)(((j / ZTC_ACC) & 1) ^ 1), abort_flag, err);
+        if (!__all_sync(0xffffffffu, ok)) break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (lane == 0) {
+        const uint32_t b_hi = smem_u32(Hst + (size_t)s * 2 * ZTC_N * ZTC_KC);
+        const uint32_t b_lo = b_hi + (uint32_t)(ZTC_N * ZTC_KC * 4);
+        const uint32_t dt = tmem + (uint32_t)(a * ZTC_N);
+        const int ksteps = min(ZTC_KC, kp - ZTC_KC * c) / 8;
+        for (int ks = 0; ks < ksteps; ++ks) {
+          const uint32_t acol = (uint32_t)(ZTC_KC * c + 8 * ks), offb = (uint32_t)ks * 256u;
+          const uint64_t bh = smem_desc(b_hi + offb, 128, sbo_b), bl = smem_desc(b_lo + offb, 128, sbo_b);
+          mma_tf32_ta(dt, tmem + ZTM_COL_AHI + acol, bh, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+          mma_tf32_ta(dt, tmem + ZTM_COL_AHI + acol, bl, idesc, 1u);
+          mma_tf32_ta(dt, tmem + ZTM_COL_ALO + acol, bh, idesc, 1u);
+        }
+        tc_commit(empty_bar(s));
+        if (c == nkc - 1) tc_commit(accf_bar(a));
+      }
+      __syncwarp();
+    }
+    if (lane == 0) tc_commit(drain_bar);
+    __syncwarp();
+    ztc_wait(drain_bar, 0u, abort_flag, err, false);
+    __syncwarp();
+  } else {
+    // ---- TMA warp: lane 0 streams the blocks of this CTA's tiles
+    if (lane == 0) {
+      int issued = 0;
+      for (int u = 0; u < my_steps; ++u) {
+        const int rs = u % ZTM_RS;
+        if (!ztc_wait(rempty_bar(rs), (uint32_t)(((u / ZTM_RS) & 1) ^ 1), abort_flag, err)) break;
+        const int j = u / nkc, c = u - j * nkc;
+        const int64_t t = blockIdx.x + (int64_t)j * G;
+        mbar_expect_tx(rfull_bar(rs), ZTM_RAW_BYTES);
+        tma_load_3d(raw0 + (uint32_t)rs * ZTM_RAW_BYTES, &map_ld, (int)((t % tpc) * ZTC_N), ZTC_KC * c,
+                    (int)(t / tpc), rfull_bar(rs));
+        issued = u + 1;
+      }
+      // every issued load has landed before the shared memory is released
+      for (int u = max(0, issued - ZTM_RS); u < issued; ++u)
+        ztc_wait(rfull_bar(u % ZTM_RS), (uint32_t)((u / ZTM_RS) & 1), abort_flag, err, false);
+    }
+    __syncwarp();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ZTM_TMEM_COLS));
+  }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*ztm_encode_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static ztm_encode_fn ztm_encoder() {
+  static ztm_encode_fn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<ztm_encode_fn>(p);
+  });
+  return fn;
+}
+
+// The spectrum qualifies: 16-byte aligned base, 4 | ncols (16-byte row
+// pitch), 32 <= nz <= 128, an encoder available.
+bool ztm_supported(const float *spec, int nz, int64_t ncols) {
+  return nz >= 32 && nz <= 128 && ncols > 0 && (ncols & 3) == 0 && ncols < (int64_t(1) << 31) &&
+         (reinterpret_cast<uintptr_t>(spec) & 15) == 0 && ztm_encoder() != nullptr;
+}
+
+cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
+                             cudaStream_t s) {
+  if (!ztm_supported(spec, nz, ncols)) return cudaErrorNotSupported;
+  CUtensorMap mld, mst;
+  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)nz, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)ncols * 4, (cuuint64_t)ncols * 4 * (cuuint64_t)nz};
+  const cuuint32_t box_ld[3] = {ZTC_N, ZTC_KC, 1}, box_st[3] = {32, 32, 1}, es[3] = {1, 1, 1};
+  ztm_encode_fn enc = ztm_encoder();
+  if (enc(&mld, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_ld, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  if (enc(&mst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_st, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  cudaError_t r = cudaFuncSetAttribute(k_zgemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZTM_SMEM);
+  if (r != cudaSuccess) return r;
+  const int64_t ntiles = 3 * ((ncols + ZTC_N - 1) / ZTC_N);
+  int64_t grid = nsm;  // one CTA per SM: all 512 tensor-memory columns
+  if (grid > ntiles) grid = ntiles;
+  const float scale = e.inverse ? (float)e.scale : 1.0f;
+  k_zgemm_tma<<<(unsigned)grid, ZTM_THREADS, ZTM_SMEM, s>>>(mld, mst, nz, ncols, Tm, scale, err);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

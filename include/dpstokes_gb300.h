@@ -148,16 +148,19 @@ typedef struct dpst_info {
   int ztransform;          /* z-transform kernel chosen at creation for the forward
                               transform (and the backward's adjoint transforms): 0
                               FP32/FP64 SIMT (even/odd folded), 1 tcgen05 split-TF32
-                              (mixed only), 2 double-float SIMT (FP64 operator) */
+                              (mixed only), 2 double-float SIMT (FP64 operator), 3
+                              tcgen05 split-TF32 fed by TMA (mixed, 32 <= nz <= 128,
+                              an even number of modes) */
   float ztransform_ms[2];  /* creation-time timings of one transform: SIMT and the
-                              alternative (tcgen05 for the mixed operator, double-float
-                              for the FP64 one); 0 if not timed */
+                              alternative (tcgen05 with register-staged operands for
+                              the mixed operator, double-float for the FP64 one); 0 if
+                              not timed */
   int fused_particle_passes; /* 1: torques spread and interpolate in the same pass as
                                 the forces (the dipole kernel's stencil columns and z
                                 ghost extension equal the monopole's and its threshold
                                 is not larger); 0: separate monopole / dipole passes */
   int ztransform_inverse;          /* kernel of the inverse z transform (with the wall-
-                                      correction epilogue), chosen separately: 0 / 1 / 2 */
+                                      correction), chosen separately: 0 / 1 / 2 / 3 */
   float ztransform_inverse_ms[2];  /* its creation-time timings, as ztransform_ms */
   int z_fused;                     /* triply periodic: 1 when the z transform and the solve
                                       run in one kernel after 2-D x-y transforms (nz = 16,
@@ -183,6 +186,8 @@ typedef struct dpst_info {
                                       fused kernel pair, DPSTOKES_GB300_SPREAD=tiles); 0: the grid
                                       is cleared and the contributions added with atomics (default,
                                       faster on the measured configurations) */
+  float ztransform_tma_ms[2];      /* creation-time timings of the TMA-fed tcgen05 z transform,
+                                      forward and inverse (0 if not timed) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

@@ -116,3 +116,72 @@ def test_fp64_double_float_ztransform(name, monkeypatch):
         er = rel_err(golden_io.restrict(gd, Va), gd["V"])
         print("%s df64 vs reference %.2e" % (name, er))
         assert er < 1e-10
+
+
+def _variant(base, nz=None, nx=None, ny=None):
+    from dataclasses import replace
+    w = _wl(base)
+    kw = {}
+    if nz is not None:
+        kw["nz"] = nz
+    if nx is not None:
+        kw.update(nx=nx, Lx=w.Lx * nx / w.nx)
+    if ny is not None:
+        kw.update(ny=ny, Ly=w.Ly * ny / w.ny)
+    return replace(w, name="%s_nz%s" % (base, nz), **kw)
+
+
+# (workload, nz): nz a multiple of 32, of 8, and neither (K padded, the last
+# TMA block partly past nz); every geometry; partial last column tiles
+TMA_CASES = [("c2_dp_n65536@192", None), ("c3_dpbw_n8192", None), ("s_dpsc_t", 37), ("s_dpbw_t_odd", 45),
+             ("s_dp_t", 64), ("s_dpbw_t", 40)]
+
+
+@pytest.mark.parametrize("base,nz", TMA_CASES)
+def test_tma_ztransform_matches(base, nz, monkeypatch):
+    """The TMA-fed tcgen05 z transform (T in tensor memory, blocks loaded and
+    stored by cp.async.bulk.tensor) against the register-staged tcgen05
+    transform (the same split products in the same order: 1e-6) and the FP64
+    operator (1e-5), forward and backward."""
+    w = _variant(base, nz) if nz else _wl(base)
+    X, F, T = W.make_inputs(w)
+    tm = _op(w, "mixed", "tma", monkeypatch)
+    info = tm.info()
+    assert info["ztransform"] == 3 and info["ztransform_inverse"] == 3, info
+    tc = _op(w, "mixed", "tcgen05", monkeypatch)
+    assert tc.info()["ztransform"] == 1
+    f64 = _op(w, "fp64", "auto", monkeypatch)
+    Vm, Wm = _mdot(tm, X, F, T, torch.float32)
+    Vt, Wt = _mdot(tc, X, F, T, torch.float32)
+    Vd, Wd = _mdot(f64, X, F, T, torch.float64)
+    e_mt, e_md = rel_err(Vm, Vt), rel_err(Vm, Vd)
+    print("%s nz %d tma-tc %.2e tma-fp64 %.2e (ms fwd tc %.3f tma %.3f, inv tc %.3f tma %.3f)" %
+          (w.name, w.nz, e_mt, e_md, info["ztransform_ms"][1], info["ztransform_tma_ms"][0],
+           info["ztransform_inverse_ms"][1], info["ztransform_tma_ms"][1]))
+    assert e_mt < 1e-6 and e_md < 1e-5
+    if T is not None:
+        assert rel_err(Wm, Wt) < 1e-6 and rel_err(Wm, Wd) < 1e-5
+    g = np.random.default_rng(7).standard_normal(F.shape)
+    grads = []
+    for op, dt in ((tm, torch.float32), (f64, torch.float64)):
+        gF, _, gX = op.mdot_backward(torch.tensor(F, dtype=dt, device="cuda"),
+                                     torch.tensor(T, dtype=dt, device="cuda") if T is not None else None,
+                                     torch.tensor(g, dtype=dt, device="cuda"), need_F=True, need_X=True)
+        torch.cuda.synchronize()
+        grads.append((gF.double().cpu().numpy(), gX.double().cpu().numpy()))
+    assert rel_err(grads[0][0], grads[1][0]) < 1e-5 and rel_err(grads[0][1], grads[1][1]) < 1e-4
+
+
+def test_tma_ztransform_unsupported_shape_falls_back(monkeypatch):
+    """An odd number of modes (nx = 16, ny = 15: 9 x 15 = 135) gives rows that
+    do not start on 16-byte boundaries: the TMA form is not chosen even when
+    asked for, and the operator still matches FP64."""
+    w = _variant("s_dp_t", 48, ny=15)
+    X, F, T = W.make_inputs(w)
+    tm = _op(w, "mixed", "tma", monkeypatch)
+    info = tm.info()
+    assert info["ztransform"] != 3 and info["ztransform_tma_ms"][0] == 0.0, info
+    f64 = _op(w, "fp64", "auto", monkeypatch)
+    Vm, _ = _mdot(tm, X, F, T, torch.float32)
+    Vd, _ = _mdot(f64, X, F, T, torch.float64)
+    assert rel_err(Vm, Vd) < 1e-5
