@@ -331,7 +331,9 @@ def run_ours(args, rank, world):
                         "tcgen05_tma": round(float(info["ztransform_tma_ms"][0]), 4)},
             "inverse": {"simt": round(float(info["ztransform_inverse_ms"][0]), 4),
                         "tcgen05": round(float(info["ztransform_inverse_ms"][1]), 4),
-                        "tcgen05_tma": round(float(info["ztransform_tma_ms"][1]), 4)}}
+                        "tcgen05_tma": round(float(info["ztransform_tma_ms"][1]), 4)},
+            "tma_variant": list(info["ztransform_tma_variant"]),
+            "tma_variants_ms": [round(float(x), 4) for x in info["ztransform_tma_variant_ms"]]}
     if dom == "solve" and arith == "double-float":
         # the double-float solve is issue bound (FP32 FMA chains of the
         # compensated sweeps): its DRAM traffic is measured by ncu, and the

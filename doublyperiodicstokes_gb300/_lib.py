@@ -42,7 +42,8 @@ class DpstInfo(ctypes.Structure):
                 ("solve_arith", ctypes.c_int), ("solve_variant", ctypes.c_int),
                 ("solve_ms", ctypes.c_float * 4), ("xy_transform", ctypes.c_int),
                 ("xy_ms", ctypes.c_float * 2), ("spread_tiles", ctypes.c_int),
-                ("ztransform_tma_ms", ctypes.c_float * 2)]
+                ("ztransform_tma_ms", ctypes.c_float * 2), ("ztransform_tma_variant", ctypes.c_int * 2),
+                ("ztransform_tma_variant_ms", ctypes.c_float * 6)]
 
 
 class DpstBatchInfo(ctypes.Structure):

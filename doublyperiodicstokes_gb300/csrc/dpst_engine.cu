@@ -120,8 +120,9 @@ cudaError_t launch_zgemm_df(double *spec, int nz, int64_t ncols, const double *T
                             cudaStream_t s, bool fold_out);
 cudaError_t launch_corr_add(float *spec, int nz, int64_t nk, const EpiArgs &e, cudaStream_t s);
 bool ztm_supported(const float *spec, int nz, int64_t ncols);
+int ztm_variants();
 cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
-                             cudaStream_t s);
+                             int variant, cudaStream_t s);
 bool tile_spread_supported(const KernelDesc &km, const KernelDesc &kd, int nx, int ny, int nz);
 cudaError_t tile_spread_setup(int nz);
 template <typename R>
@@ -702,10 +703,13 @@ struct Engine : EngineBase {
   // the plain transforms (ztc[0]: forward, and the backward's adjoint
   // transforms) and for the inverse with its wall correction (ztc[1]), each
   // timed on this handle's buffers.  DPSTOKES_GB300_ZTRANSFORM = simt |
-  // tcgen05 | tma | auto (default) overrides the choice.
+  // tcgen05 | tma | auto (default) overrides the choice, and
+  // DPSTOKES_GB300_ZTMA_VARIANT = 0 | 1 | 2 the TMA-fed form's variant.
   int ztc[2] = {0, 0};
   float ztc_ms[2][2] = {{0.f, 0.f}, {0.f, 0.f}};  // [direction][impl]
-  float ztm_ms[2] = {0.f, 0.f};                   // [direction]: the TMA-fed form
+  float ztm_ms[2] = {0.f, 0.f};                   // [direction]: the TMA-fed form, its best variant
+  int ztm_var[2] = {0, 0};                        // [direction]: that variant (ring and converted stages)
+  float ztm_vms[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // [direction][variant]
   DevBuf ztc_err;
 
   // the wall-correction inputs of the inverse transform's epilogue
@@ -739,12 +743,12 @@ struct Engine : EngineBase {
         EpiArgs e2 = e;
         e2.corr = nullptr;
         e2.corrf = nullptr;
-        cudaError_t r = tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e2, nsm, ztc_err.as<int>(), s)
+        cudaError_t r = tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e2, nsm, ztc_err.as<int>(), ztm_var[1], s)
                             : launch_zgemm_tc(fs, nz, 2 * nk, fT, e2, nsm, ztc_err.as<int>(), s);
         if (r == cudaSuccess) r = launch_corr_add(fs, nz, nk, e, s);
         return r;
       }
-      return tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e, nsm, ztc_err.as<int>(), s)
+      return tma ? launch_zgemm_tma(fs, nz, 2 * nk, fT, e, nsm, ztc_err.as<int>(), ztm_var[e.inverse ? 1 : 0], s)
                  : launch_zgemm_tc(fs, nz, 2 * nk, fT, e, nsm, ztc_err.as<int>(), s);
     }
     return launch_zgemm<R>(sp, nz, 2 * nk, T, e, nsm, s, fold_out);
@@ -811,9 +815,12 @@ struct Engine : EngineBase {
       e.scale = dir ? 1.0 / ((double)nx * (double)ny) : 1.0;
       if (dir) epi_corr(e);
       const R *T = dir ? Ti.as<R>() : Tf.as<R>();
-      for (int k = 0; k < 3; ++k) {
-        const int impl = k == 2 ? 3 : k;
-        if (impl == 3 && !tma_ok) continue;
+      // SIMT, tcgen05, then each variant of the TMA-fed form
+      const int nv = tma_ok ? ztm_variants() : 0;
+      int best_var = 0;
+      for (int k = 0; k < 2 + nv; ++k) {
+        const int impl = k >= 2 ? 3 : k;
+        if (impl == 3) ztm_var[dir] = k - 2;
         float ms = 0.0f;
         DPST_CUDA(zgemm(sp, T, e, dir == 1, 0, impl));  // warm-up
         DPST_CUDA(cudaEventRecord(a, 0));
@@ -821,7 +828,18 @@ struct Engine : EngineBase {
         DPST_CUDA(cudaEventRecord(b, 0));
         DPST_CUDA(cudaEventSynchronize(b));
         DPST_CUDA(cudaEventElapsedTime(&ms, a, b));
-        (impl == 3 ? ztm_ms[dir] : ztc_ms[dir][impl]) = ms / 3.0f;
+        ms /= 3.0f;
+        if (impl != 3) ztc_ms[dir][impl] = ms;
+        else ztm_vms[dir][k - 2] = ms;
+        if (impl == 3 && (k == 2 || ms < ztm_ms[dir])) {
+          ztm_ms[dir] = ms;
+          best_var = k - 2;
+        }
+      }
+      ztm_var[dir] = best_var;
+      if (const char *ev = getenv("DPSTOKES_GB300_ZTMA_VARIANT")) {
+        const int v = atoi(ev);
+        if (v >= 0 && v < nv) ztm_var[dir] = v;
       }
     }
     cudaEventDestroy(a);
@@ -1487,6 +1505,10 @@ struct Engine : EngineBase {
     o->xy_ms[1] = sizeof(R) == 8 ? xyd_ms[1] : xy_ms[1];
     o->ztransform_tma_ms[0] = ztm_ms[0];
     o->ztransform_tma_ms[1] = ztm_ms[1];
+    for (int d = 0; d < 2; ++d) {
+      o->ztransform_tma_variant[d] = ztm_var[d];
+      for (int v = 0; v < 3; ++v) o->ztransform_tma_variant_ms[3 * d + v] = ztm_vms[d][v];
+    }
     if (ownfft || ownfft_d) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
     if (sizeof(R) == 4 && ztc[1] && p.mode != DPST_MODE_NOWALL) o->kernels_per_mdot += 1;  // correction pass
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];

@@ -550,7 +550,7 @@ cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, i
 //     memory holds only the streamed B operand and staging;
 //   * one thread issues cp.async.bulk.tensor loads of 32-row x 128-column
 //     FP32 blocks ([32][128] row-major, zero-filled past nz and ncols) into
-//     a ring of ZTM_RS stages, each completing on its mbarrier with the
+//     a ring of RS stages, each completing on its mbarrier with the
 //     block's byte count; no register holds a load in flight;
 //   * 8 converter warps read a block from the ring, split it into TF32
 //     hi / lo and write the canonical K-major stages the MMAs read;
@@ -563,7 +563,6 @@ cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, i
 // multiple of 32 columns).  No wall-correction epilogue: the inverse with
 // walls runs k_corr_add afterwards, as for the other tcgen05 form.
 // ---------------------------------------------------------------------------
-constexpr int ZTM_RS = 6;                                     // TMA ring stages
 constexpr int ZTM_CONV_WARPS = 8;
 constexpr int ZTM_EPI_WARPS = 4;
 constexpr int ZTM_MMA_WARP = ZTM_CONV_WARPS + ZTM_EPI_WARPS;  // warp 12
@@ -574,13 +573,20 @@ constexpr uint32_t ZTM_COL_AHI = 2 * ZTC_N, ZTM_COL_ALO = 3 * ZTC_N;
 constexpr uint32_t ZTM_RAW_BYTES = ZTC_KC * ZTC_N * 4;        // 16 KB
 constexpr uint32_t ZTM_HL_BYTES = 2 * ZTC_N * ZTC_KC * 4;     // hi + lo, 32 KB
 constexpr uint32_t ZTM_STG_BYTES = 32 * 32 * 4;               // one 32 x 32 block, 4 KB
-constexpr size_t ZTM_OFF_HL = (size_t)ZTM_RS * ZTM_RAW_BYTES;
-constexpr size_t ZTM_OFF_STG = ZTM_OFF_HL + (size_t)ZTC_STAGES * ZTM_HL_BYTES;
-constexpr size_t ZTM_OFF_BAR = ZTM_OFF_STG + (size_t)ZTM_EPI_WARPS * 2 * ZTM_STG_BYTES;
-constexpr int ZTM_NBARS = 2 * ZTM_RS + 2 * ZTC_STAGES + 2 * ZTC_ACC + 1;
-constexpr size_t ZTM_SMEM = ZTM_OFF_BAR + ZTM_NBARS * 8 + 16 + 1024;  // + alignment slack
-static_assert(ZTM_SMEM <= 227 * 1024, "TMA z transform: shared memory");
-static_assert(ZTM_OFF_HL % 1024 == 0 && ZTM_OFF_STG % 1024 == 0, "1024-byte aligned regions");
+constexpr int ZTM_TP = 128 + 4;                               // T's row pitch in shared memory (floats)
+// Shared-memory layout of a variant: RS ring stages of raw blocks, HL
+// converted (hi, lo) stages, the epilogue's staging, the mbarriers.
+template <int RS, int HL>
+struct ZtmCfg {
+  static constexpr size_t off_hl = (size_t)RS * ZTM_RAW_BYTES;
+  static constexpr size_t off_stg = off_hl + (size_t)HL * ZTM_HL_BYTES;
+  static constexpr size_t off_bar = off_stg + (size_t)ZTM_EPI_WARPS * 2 * ZTM_STG_BYTES;
+  static constexpr int nbars = 2 * RS + 2 * HL + 2 * ZTC_ACC + 1;
+  static constexpr size_t smem = off_bar + nbars * 8 + 16 + 1024;  // + alignment slack
+  static_assert(smem <= 227 * 1024, "TMA z transform: shared memory");
+  static_assert(off_hl % 1024 == 0 && off_stg % 1024 == 0, "1024-byte aligned regions");
+  static_assert(off_bar - off_hl >= (size_t)128 * ZTM_TP * 4, "T staged over the converted stages and staging");
+};
 
 static __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
@@ -612,9 +618,11 @@ static __device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atme
       "r"(atmem), "l"(bd), "r"(idesc), "r"(acc));
 }
 
+template <int RS, int HL>
 __global__ void __launch_bounds__(ZTM_THREADS, 1)
     k_zgemm_tma(const __grid_constant__ CUtensorMap map_ld, const __grid_constant__ CUtensorMap map_st, int nz,
                 int64_t ncols, const float *__restrict__ Tm, float scale, int *err) {
+  using Cfg = ZtmCfg<RS, HL>;
   extern __shared__ unsigned char ztm_raw_sm[];
   // 1024-byte alignment of the swizzled staging (the dynamic window's base
   // alignment is not guaranteed beyond 16 bytes)
@@ -622,19 +630,19 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
       (reinterpret_cast<uintptr_t>(ztm_raw_sm) + 1023) & ~static_cast<uintptr_t>(1023));
   const int kp = (nz + 7) & ~7;
   const uint32_t raw0 = smem_u32(sm);
-  uint32_t *Hst = reinterpret_cast<uint32_t *>(sm + ZTM_OFF_HL);
+  uint32_t *Hst = reinterpret_cast<uint32_t *>(sm + Cfg::off_hl);
   const float *rawf = reinterpret_cast<const float *>(sm);
-  float *stg = reinterpret_cast<float *>(sm + ZTM_OFF_STG);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + ZTM_OFF_BAR);
+  float *stg = reinterpret_cast<float *>(sm + Cfg::off_stg);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Cfg::off_bar);
   const uint32_t bar0 = smem_u32(bars);
   auto rfull_bar = [&](int s) { return bar0 + 8u * (uint32_t)s; };
-  auto rempty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(ZTM_RS + s); };
-  auto full_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + s); };
-  auto empty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + ZTC_STAGES + s); };
-  auto accf_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + 2 * ZTC_STAGES + a); };
-  auto acce_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * ZTM_RS + 2 * ZTC_STAGES + ZTC_ACC + a); };
-  const uint32_t drain_bar = bar0 + 8u * (uint32_t)(ZTM_NBARS - 1);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + ZTM_NBARS);
+  auto rempty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(RS + s); };
+  auto full_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * RS + s); };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (uint32_t)(2 * RS + HL + s); };
+  auto accf_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * RS + 2 * HL + a); };
+  auto acce_bar = [&](int a) { return bar0 + 8u * (uint32_t)(2 * RS + 2 * HL + ZTC_ACC + a); };
+  const uint32_t drain_bar = bar0 + 8u * (uint32_t)(Cfg::nbars - 1);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + Cfg::nbars);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -644,11 +652,11 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    for (int s = 0; s < ZTM_RS; ++s) {
+    for (int s = 0; s < RS; ++s) {
       mbar_init(rfull_bar(s), 1);
       mbar_init(rempty_bar(s), ZTM_CONV_WARPS);
     }
-    for (int s = 0; s < ZTC_STAGES; ++s) {
+    for (int s = 0; s < HL; ++s) {
       mbar_init(full_bar(s), ZTM_CONV_WARPS);
       mbar_init(empty_bar(s), 1);
     }
@@ -670,19 +678,54 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
+  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;  // tiles per component
+  const int64_t ntiles = 3 * tpc;
+  const int64_t G = gridDim.x;
+  const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
+  const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
+  const int my_steps = my_tiles * nkc;         // step u = (tile u / nkc, K chunk u % nkc)
+  constexpr int SKQ = ZTC_KC / 4;
+
+  // TMA: step u's block into ring stage u % RS once the stage is free
+  int issued = 0;
+  auto tma_issue = [&](int u) -> bool {
+    const int rs = u % RS;
+    if (!ztc_wait(rempty_bar(rs), (uint32_t)(((u / RS) & 1) ^ 1), abort_flag, err)) return false;
+    const int j = u / nkc, c = u - j * nkc;
+    const int64_t t = blockIdx.x + (int64_t)j * G;
+    mbar_expect_tx(rfull_bar(rs), ZTM_RAW_BYTES);
+    tma_load_3d(raw0 + (uint32_t)rs * ZTM_RAW_BYTES, &map_ld, (int)((t % tpc) * ZTC_N), ZTC_KC * c, (int)(t / tpc),
+                rfull_bar(rs));
+    issued = u + 1;
+    return true;
+  };
+  // the first ring stages are filled while T is set up
+  if (warp == ZTM_TMA_WARP && lane == 0)
+    for (int u = 0; u < min(RS, my_steps); ++u)
+      if (!tma_issue(u)) break;
+
+  // T through shared memory ([128][ZTM_TP] floats over the converted stages
+  // and the staging, not yet in use): coalesced loads by every thread, then
+  // each epilogue warp splits its lane quadrant's rows into tf32 hi / lo,
+  // 8 columns per tcgen05.st; rows and columns >= nz zero
+  float *tsm = reinterpret_cast<float *>(sm + Cfg::off_hl);
+  for (int idx = tid; idx < 128 * kp; idx += ZTM_THREADS) {
+    const int r = idx / kp, k = idx - (idx / kp) * kp;
+    tsm[r * ZTM_TP + k] = (r < nz && k < nz) ? Tm[r * nz + k] : 0.0f;
+  }
+  __syncthreads();
   if (warp >= ZTM_CONV_WARPS && warp < ZTM_MMA_WARP) {
-    // T split into tf32 hi / lo, row r = 32 (warp & 3) + lane of this warp's
-    // lane quadrant, 8 columns per tcgen05.st; rows and columns >= nz zero
     const int r = 32 * (warp & 3) + lane;
     const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     for (int k0 = 0; k0 < kp; k0 += 8) {
       uint32_t h[8], l[8];
+      const float4 va = *reinterpret_cast<const float4 *>(tsm + r * ZTM_TP + k0);
+      const float4 vb = *reinterpret_cast<const float4 *>(tsm + r * ZTM_TP + k0 + 4);
+      const float tv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
-        const int k = k0 + i;
-        const float v = (r < nz && k < nz) ? Tm[r * nz + k] : 0.0f;
-        h[i] = to_tf32(v);
-        l[i] = to_tf32(v - __uint_as_float(h[i]));
+        h[i] = to_tf32(tv[i]);
+        l[i] = to_tf32(tv[i] - __uint_as_float(h[i]));
       }
       asm volatile(
           "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(
@@ -701,20 +744,12 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
 
-  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;  // tiles per component
-  const int64_t ntiles = 3 * tpc;
-  const int64_t G = gridDim.x;
-  const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
-  const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
-  const int my_steps = my_tiles * nkc;         // step u = (tile u / nkc, K chunk u % nkc)
-  constexpr int SKQ = ZTC_KC / 4;
-
   if (warp < ZTM_CONV_WARPS) {
     // ---- converters: column n, row quads q = qg + ZTC_PGROUPS i of the chunk
     const int n = tid % ZTC_N, qg = tid / ZTC_N;
     for (int u = 0; u < my_steps; ++u) {
-      const int rs = u % ZTM_RS;
-      bool ok = ztc_wait(rfull_bar(rs), (uint32_t)((u / ZTM_RS) & 1), abort_flag, err);
+      const int rs = u % RS;
+      bool ok = ztc_wait(rfull_bar(rs), (uint32_t)((u / RS) & 1), abort_flag, err);
       if (!__all_sync(0xffffffffu, ok)) break;
       const float *rb = rawf + (size_t)rs * (ZTC_KC * ZTC_N);
       float br[ZTC_QPT][4];
@@ -726,8 +761,8 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(rempty_bar(rs));
-      const int s = u % ZTC_STAGES;
-      ok = ztc_wait(empty_bar(s), (uint32_t)(((u / ZTC_STAGES) & 1) ^ 1), abort_flag, err);
+      const int s = u % HL;
+      ok = ztc_wait(empty_bar(s), (uint32_t)(((u / HL) & 1) ^ 1), abort_flag, err);
       if (!__all_sync(0xffffffffu, ok)) break;
       uint32_t *Bhi = Hst + (size_t)s * 2 * ZTC_N * ZTC_KC, *Blo = Bhi + ZTC_N * ZTC_KC;
 #pragma unroll
@@ -824,8 +859,8 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
     const uint32_t sbo_b = SKQ * 128;
     for (int u = 0; u < my_steps; ++u) {
       const int j = u / nkc, c = u - j * nkc;
-      const int s = u % ZTC_STAGES, a = j % ZTC_ACC;
-      bool ok = ztc_wait(full_bar(s), (uint32_t)((u / ZTC_STAGES) & 1), abort_flag, err);
+      const int s = u % HL, a = j % ZTC_ACC;
+      bool ok = ztc_wait(full_bar(s), (uint32_t)((u / HL) & 1), abort_flag, err);
       if (!__all_sync(0xffffffffu, ok)) break;
       if (c == 0) {
         ok = ztc_wait(acce_bar(a), (uint32_t)(((j / ZTC_ACC) & 1) ^ 1), abort_flag, err);
@@ -856,20 +891,12 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
   } else {
     // ---- TMA warp: lane 0 streams the blocks of this CTA's tiles
     if (lane == 0) {
-      int issued = 0;
-      for (int u = 0; u < my_steps; ++u) {
-        const int rs = u % ZTM_RS;
-        if (!ztc_wait(rempty_bar(rs), (uint32_t)(((u / ZTM_RS) & 1) ^ 1), abort_flag, err)) break;
-        const int j = u / nkc, c = u - j * nkc;
-        const int64_t t = blockIdx.x + (int64_t)j * G;
-        mbar_expect_tx(rfull_bar(rs), ZTM_RAW_BYTES);
-        tma_load_3d(raw0 + (uint32_t)rs * ZTM_RAW_BYTES, &map_ld, (int)((t % tpc) * ZTC_N), ZTC_KC * c,
-                    (int)(t / tpc), rfull_bar(rs));
-        issued = u + 1;
-      }
+      if (issued == min(RS, my_steps))
+        for (int u = issued; u < my_steps; ++u)
+          if (!tma_issue(u)) break;
       // every issued load has landed before the shared memory is released
-      for (int u = max(0, issued - ZTM_RS); u < issued; ++u)
-        ztc_wait(rfull_bar(u % ZTM_RS), (uint32_t)((u / ZTM_RS) & 1), abort_flag, err, false);
+      for (int u = max(0, issued - RS); u < issued; ++u)
+        ztc_wait(rfull_bar(u % RS), (uint32_t)((u / RS) & 1), abort_flag, err, false);
     }
     __syncwarp();
   }
@@ -900,17 +927,29 @@ static ztm_encode_fn ztm_encoder() {
   return fn;
 }
 
-// The spectrum qualifies: 16-byte aligned base, 4 | ncols (16-byte row
-// pitch), 32 <= nz <= 128, an encoder available.
-bool ztm_supported(const float *spec, int nz, int64_t ncols) {
-  return nz >= 32 && nz <= 128 && ncols > 0 && (ncols & 3) == 0 && ncols < (int64_t(1) << 31) &&
-         (reinterpret_cast<uintptr_t>(spec) & 15) == 0 && ztm_encoder() != nullptr;
-}
-
-cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
-                             cudaStream_t s) {
-  if (!ztm_supported(spec, nz, ncols)) return cudaErrorNotSupported;
-  CUtensorMap mld, mst;
+// The load (128 x 32 blocks, no swizzle) and store (32 x 32 blocks, 128-byte
+// swizzle) maps of the tensor [3][nz][ncols] at spec, encoded once per
+// (device, spec, nz, ncols) and kept in a small cache (a launch then costs
+// no driver call beyond the launch itself).
+struct ZtmMaps {
+  CUtensorMap ld, st;
+  const void *p;
+  int64_t ncols;
+  int nz, dev;
+};
+static bool ztm_maps(float *spec, int nz, int64_t ncols, CUtensorMap &mld, CUtensorMap &mst) {
+  static std::mutex mu;
+  static ZtmMaps cache[8];
+  static int used = 0, next = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < used; ++i)
+    if (cache[i].p == spec && cache[i].nz == nz && cache[i].ncols == ncols && cache[i].dev == dev) {
+      mld = cache[i].ld;
+      mst = cache[i].st;
+      return true;
+    }
   const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)nz, 3};
   const cuuint64_t strides[2] = {(cuuint64_t)ncols * 4, (cuuint64_t)ncols * 4 * (cuuint64_t)nz};
   const cuuint32_t box_ld[3] = {ZTC_N, ZTC_KC, 1}, box_st[3] = {32, 32, 1}, es[3] = {1, 1, 1};
@@ -918,19 +957,57 @@ cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm
   if (enc(&mld, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_ld, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
+    return false;
   if (enc(&mst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_st, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
           CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
-  cudaError_t r = cudaFuncSetAttribute(k_zgemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZTM_SMEM);
+    return false;
+  ZtmMaps &c = cache[next];
+  next = (next + 1) % 8;
+  if (used < 8) ++used;
+  c.ld = mld;
+  c.st = mst;
+  c.p = spec;
+  c.nz = nz;
+  c.ncols = ncols;
+  c.dev = dev;
+  return true;
+}
+
+// The spectrum qualifies: 16-byte aligned base, 4 | ncols (16-byte row
+// pitch), 32 <= nz <= 128, an encoder available.
+bool ztm_supported(const float *spec, int nz, int64_t ncols) {
+  return nz >= 32 && nz <= 128 && ncols > 0 && (ncols & 3) == 0 && ncols < (int64_t(1) << 31) &&
+         (reinterpret_cast<uintptr_t>(spec) & 15) == 0 && ztm_encoder() != nullptr;
+}
+
+template <int RS, int HL>
+static cudaError_t ztm_launch(const CUtensorMap &mld, const CUtensorMap &mst, int nz, int64_t ncols, const float *Tm,
+                              float scale, int64_t grid, int *err, cudaStream_t s) {
+  cudaError_t r =
+      cudaFuncSetAttribute(k_zgemm_tma<RS, HL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZtmCfg<RS, HL>::smem);
   if (r != cudaSuccess) return r;
+  k_zgemm_tma<RS, HL><<<(unsigned)grid, ZTM_THREADS, ZtmCfg<RS, HL>::smem, s>>>(mld, mst, nz, ncols, Tm, scale, err);
+  return cudaGetLastError();
+}
+
+// variant: (ring stages, converted stages) = (6, 2), (4, 3), (7, 2)
+int ztm_variants() { return 3; }
+
+cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm, const EpiArgs &e, int nsm, int *err,
+                             int variant, cudaStream_t s) {
+  if (!ztm_supported(spec, nz, ncols)) return cudaErrorNotSupported;
+  CUtensorMap mld, mst;
+  if (!ztm_maps(spec, nz, ncols, mld, mst)) return cudaErrorInvalidValue;
   const int64_t ntiles = 3 * ((ncols + ZTC_N - 1) / ZTC_N);
   int64_t grid = nsm;  // one CTA per SM: all 512 tensor-memory columns
   if (grid > ntiles) grid = ntiles;
   const float scale = e.inverse ? (float)e.scale : 1.0f;
-  k_zgemm_tma<<<(unsigned)grid, ZTM_THREADS, ZTM_SMEM, s>>>(mld, mst, nz, ncols, Tm, scale, err);
-  return cudaGetLastError();
+  switch (variant) {
+    case 1: return ztm_launch<4, 3>(mld, mst, nz, ncols, Tm, scale, grid, err, s);
+    case 2: return ztm_launch<7, 2>(mld, mst, nz, ncols, Tm, scale, grid, err, s);
+    default: return ztm_launch<6, 2>(mld, mst, nz, ncols, Tm, scale, grid, err, s);
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -187,7 +187,10 @@ typedef struct dpst_info {
                                       is cleared and the contributions added with atomics (default,
                                       faster on the measured configurations) */
   float ztransform_tma_ms[2];      /* creation-time timings of the TMA-fed tcgen05 z transform,
-                                      forward and inverse (0 if not timed) */
+                                      forward and inverse, its fastest variant (0 if not timed) */
+  int ztransform_tma_variant[2];   /* that variant per direction: 0, 1, 2 = (TMA ring stages,
+                                      converted operand stages) (6, 2), (4, 3), (7, 2) */
+  float ztransform_tma_variant_ms[6]; /* every variant's timing, [direction][variant] */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;

@@ -158,6 +158,8 @@ def test_tma_ztransform_matches(base, nz, monkeypatch):
     print("%s nz %d tma-tc %.2e tma-fp64 %.2e (ms fwd tc %.3f tma %.3f, inv tc %.3f tma %.3f)" %
           (w.name, w.nz, e_mt, e_md, info["ztransform_ms"][1], info["ztransform_tma_ms"][0],
            info["ztransform_inverse_ms"][1], info["ztransform_tma_ms"][1]))
+    print("  TMA variants (fwd 0-2, inv 0-2) ms", [round(x, 4) for x in info["ztransform_tma_variant_ms"]],
+          "chosen", list(info["ztransform_tma_variant"]))
     assert e_mt < 1e-6 and e_md < 1e-5
     if T is not None:
         assert rel_err(Wm, Wt) < 1e-6 and rel_err(Wm, Wd) < 1e-5
@@ -170,6 +172,23 @@ def test_tma_ztransform_matches(base, nz, monkeypatch):
         torch.cuda.synchronize()
         grads.append((gF.double().cpu().numpy(), gX.double().cpu().numpy()))
     assert rel_err(grads[0][0], grads[1][0]) < 1e-5 and rel_err(grads[0][1], grads[1][1]) < 1e-4
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_tma_ztransform_every_variant(variant, monkeypatch):
+    """Each variant of the TMA-fed transform (ring and converted-stage
+    counts), forced, against the register-staged tcgen05 transform."""
+    w = _variant("s_dpbw_t", 45)
+    X, F, T = W.make_inputs(w)
+    monkeypatch.setenv("DPSTOKES_GB300_ZTMA_VARIANT", str(variant))
+    tm = _op(w, "mixed", "tma", monkeypatch)
+    monkeypatch.delenv("DPSTOKES_GB300_ZTMA_VARIANT")
+    info = tm.info()
+    assert info["ztransform"] == 3 and list(info["ztransform_tma_variant"]) == [variant, variant], info
+    tc = _op(w, "mixed", "tcgen05", monkeypatch)
+    Vm, Wm = _mdot(tm, X, F, T, torch.float32)
+    Vt, Wt = _mdot(tc, X, F, T, torch.float32)
+    assert rel_err(Vm, Vt) < 1e-6 and rel_err(Wm, Wt) < 1e-6
 
 
 def test_tma_ztransform_unsupported_shape_falls_back(monkeypatch):
