@@ -381,9 +381,11 @@ def run_ours(args, rank, world):
             roof["fp64_pipe"] = {"lane_instructions": instr, "achieved_per_s": rate, "peak_per_s": peak,
                                  "frac": rate / peak, "sm_mhz": mhz, "sms": nsm}
     extra["xy_transform"] = {"form": {0: "cuFFT", 1: "own, two passes", 2: "own, one launch",
-                                      3: "own double-float, two passes"}.get(
+                                      3: "own double-float, two passes",
+                                      4: "own, one launch of 8-CTA clusters"}.get(
         info.get("xy_transform"), "n/a"), "pair_ms_two_pass_one_launch": [round(float(x), 4) for x in
-                                                                        info.get("xy_ms", [])]}
+                                                                        info.get("xy_ms", [])],
+        "pair_ms_cluster": round(float(info.get("xy_cluster_ms", 0.0)), 4)}
     extra["set_positions_ms"] = set_positions_ms
     extra["noalloc_ms_per_step"] = noalloc_ms
     extra["solve_kernel"] = {"arith": arith,

@@ -43,7 +43,7 @@ class DpstInfo(ctypes.Structure):
                 ("solve_ms", ctypes.c_float * 4), ("xy_transform", ctypes.c_int),
                 ("xy_ms", ctypes.c_float * 2), ("spread_tiles", ctypes.c_int),
                 ("ztransform_tma_ms", ctypes.c_float * 2), ("ztransform_tma_variant", ctypes.c_int * 2),
-                ("ztransform_tma_variant_ms", ctypes.c_float * 6)]
+                ("ztransform_tma_variant_ms", ctypes.c_float * 6), ("xy_cluster_ms", ctypes.c_float)]
 
 
 class DpstBatchInfo(ctypes.Structure):

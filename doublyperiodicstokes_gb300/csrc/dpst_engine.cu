@@ -88,6 +88,10 @@ cudaError_t fft_rows(bool inverse, const float *grid_in, float2 *spec_out, const
                      int nx, int64_t rows, const float2 *twx, cudaStream_t s);
 cudaError_t fft_cols(bool inverse, float2 *spec, int ny, int nxh, int64_t planes, const float2 *twy, cudaStream_t s);
 bool fft_xy_fused_supported(int nx, int ny);
+bool fft_xy_cluster_supported(int nx, int ny);
+cudaError_t fft_xy_cluster_setup(int nx, int ny, int *grid);
+cudaError_t fft_xy_cluster(bool inverse, const float *grid_in, float2 *spec, float *grid_out, int nx, int ny,
+                           int64_t planes, const float2 *twx, const float2 *twy, int *err, int grid, cudaStream_t s);
 int64_t fft_xy_counter_ints(int64_t planes);
 bool own_fft_df_supported(int nx, int ny);
 std::vector<float4> fft_twiddles_df(int n);
@@ -213,6 +217,12 @@ struct Engine : EngineBase {
   // and the creation-time timings {two-pass, one-launch} of a forward +
   // inverse pair
   bool xyfused = false;
+  // the cluster form (one launch per direction, a plane across a cluster's
+  // shared memory): chosen when faster at creation; its grid and error word
+  bool xycl = false;
+  int xycl_grid = 0;
+  DevBuf xycl_err;
+  float xycl_ms = 0.0f;
   // FP64 operator: the library's double-float x-y transforms (when faster
   // than cuFFT's FP64 ones at creation) and their timings {cuFFT, own}
   bool ownfft_d = false;
@@ -413,6 +423,13 @@ struct Engine : EngineBase {
           DPST_CUDA(fft_xy_setup(nx, ny, &xy_grid));
           grow_xy_counters(3 * (int64_t)nz);
         }
+        if (fft_xy_cluster_supported(nx, ny) && !(env && std::string(env) == "twopass")) {
+          DPST_CUDA(fft_xy_cluster_setup(nx, ny, &xycl_grid));
+          if (xycl_grid > 0) {
+            xycl_err.alloc(sizeof(int));
+            DPST_CUDA(cudaMemset(xycl_err.p, 0, sizeof(int)));
+          }
+        }
       }
       if (sizeof(R) == 8 && !want_cufft && own_fft_df_supported(nx, ny)) {
         upload(twxd, fft_twiddles_df(nx));
@@ -463,21 +480,24 @@ struct Engine : EngineBase {
     xy_planes = planes;
   }
 
-  // The x-y transform's form: the two-pass kernels and the one-launch kernel
-  // each run a forward + inverse pair on the grid and spectrum buffers (one
-  // warm-up, best of three), and the faster is kept; a one-launch run whose
-  // waits gave up (error word set) is never kept.  DPSTOKES_GB300_XY_FFT=
-  // fused | twopass fixes the choice.
+  // The x-y transform's form: the two-pass kernels, the one-launch kernel and
+  // the cluster kernel each run a forward + inverse pair on the grid and
+  // spectrum buffers (one warm-up, best of three), and the fastest is kept;
+  // a one-launch or cluster run whose waits gave up (error word set) is never
+  // kept.  DPSTOKES_GB300_XY_FFT= fused | cluster | twopass fixes the choice.
   void tune_xy() {
-    if (!ownfft || xy_planes == 0) return;
+    if (!ownfft || (xy_planes == 0 && xycl_grid == 0)) return;
     const char *env = getenv("DPSTOKES_GB300_XY_FFT");
     const std::string want = env ? std::string(env) : std::string();
     cudaStream_t s = 0;
     cudaEvent_t e0, e1;
     DPST_CUDA(cudaEventCreate(&e0));
     DPST_CUDA(cudaEventCreate(&e1));
-    for (int form = 0; form < 2; ++form) {
+    for (int form = 0; form < 3; ++form) {
+      if (form == 1 && xy_planes == 0) continue;
+      if (form == 2 && xycl_grid == 0) continue;
       xyfused = form == 1;
+      xycl = form == 2;
       float best = 1e30f;
       for (int r = 0; r < 4; ++r) {
         DPST_CUDA(cudaEventRecord(e0, s));
@@ -489,15 +509,28 @@ struct Engine : EngineBase {
         DPST_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         if (r > 0) best = std::min(best, ms);
       }
-      xy_ms[form] = best;
+      (form == 2 ? xycl_ms : xy_ms[form]) = best;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int err = 0;
-    DPST_CUDA(cudaMemcpy(&err, xyctr.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost));
-    if (want == "fused") xyfused = true;
-    else xyfused = err == 0 && xy_ms[1] < xy_ms[0];
-    if (err != 0) xyfused = false;
+    int err = 0, errc = 0;
+    if (xy_planes > 0) DPST_CUDA(cudaMemcpy(&err, xyctr.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost));
+    if (xycl_grid > 0) DPST_CUDA(cudaMemcpy(&errc, xycl_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    const bool ok1 = xy_planes > 0 && err == 0, ok2 = xycl_grid > 0 && errc == 0;
+    xyfused = xycl = false;
+    if (want == "fused" && ok1) xyfused = true;
+    else if (want == "cluster" && ok2) xycl = true;
+    else if (want != "twopass") {
+      float best = xy_ms[0];
+      if (ok1 && xy_ms[1] < best) {
+        best = xy_ms[1];
+        xyfused = true;
+      }
+      if (ok2 && xycl_ms < best) {
+        xyfused = false;
+        xycl = true;
+      }
+    }
     DPST_CUDA(cudaMemset(grid.p, 0, grid.bytes));
   }
 
@@ -1036,6 +1069,11 @@ struct Engine : EngineBase {
         return;
       }
     }
+    if (ownfft && xycl) {
+      DPST_CUDA(fft_xy_cluster(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr, nx,
+                               ny, planes, twx.as<float2>(), twy.as<float2>(), xycl_err.as<int>(), xycl_grid, s));
+      return;
+    }
     if (ownfft && xyfused && planes <= xy_planes) {
       DPST_CUDA(fft_xy_fused(false, reinterpret_cast<const float *>(gr), reinterpret_cast<float2 *>(sp), nullptr, nx,
                              ny, planes, twx.as<float2>(), twy.as<float2>(), xyctr.as<int>(), xy_grid, xy_lag, s));
@@ -1063,6 +1101,11 @@ struct Engine : EngineBase {
                               reinterpret_cast<double *>(gr), nx, planes * ny, twxd.as<float4>(), s));
         return;
       }
+    }
+    if (ownfft && xycl) {
+      DPST_CUDA(fft_xy_cluster(true, nullptr, reinterpret_cast<float2 *>(sp), reinterpret_cast<float *>(gr), nx, ny,
+                               planes, twx.as<float2>(), twy.as<float2>(), xycl_err.as<int>(), xycl_grid, s));
+      return;
     }
     if (ownfft && xyfused && planes <= xy_planes) {
       DPST_CUDA(fft_xy_fused(true, nullptr, reinterpret_cast<float2 *>(sp), reinterpret_cast<float *>(gr), nx, ny,
@@ -1499,7 +1542,8 @@ struct Engine : EngineBase {
     o->fused_particle_passes = fused ? 1 : 0;
     o->solve_arith = dfsolve ? DPST_SOLVE_DF64 : DPST_SOLVE_FP64;
     o->solve_variant = dfsolve ? df_variant : 0;
-    o->xy_transform = ownfft ? (xyfused ? 2 : 1) : (ownfft_d ? 3 : 0);
+    o->xy_transform = ownfft ? (xycl ? 4 : xyfused ? 2 : 1) : (ownfft_d ? 3 : 0);
+    o->xy_cluster_ms = xycl_ms;
     o->spread_tiles = (tile_spread && p.has_torque) ? 1 : 0;
     o->xy_ms[0] = sizeof(R) == 8 ? xyd_ms[0] : xy_ms[0];
     o->xy_ms[1] = sizeof(R) == 8 ? xyd_ms[1] : xy_ms[1];
@@ -1509,7 +1553,7 @@ struct Engine : EngineBase {
       o->ztransform_tma_variant[d] = ztm_var[d];
       for (int v = 0; v < 3; ++v) o->ztransform_tma_variant_ms[3 * d + v] = ztm_vms[d][v];
     }
-    if (ownfft || ownfft_d) o->kernels_per_mdot += (xyfused ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
+    if (ownfft || ownfft_d) o->kernels_per_mdot += (xyfused || xycl ? 2 : 4) * (reg && p.has_torque ? 2 : 1);
     if (sizeof(R) == 4 && ztc[1] && p.mode != DPST_MODE_NOWALL) o->kernels_per_mdot += 1;  // correction pass
     for (int v = 0; v < 4; ++v) o->solve_ms[v] = df_ms[v];
     int64_t b = 0;
@@ -1776,12 +1820,15 @@ int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int i
                       void *stream) {
   return guarded([&] {
     if (!in || !out || planes < 1) throw Error(DPST_ERR_INVALID_ARG, "NULL argument or no planes");
-    if (form != 0 && form != 1) throw Error(DPST_ERR_INVALID_ARG, "form must be 0 (two passes) or 1 (one launch)");
+    if (form != 0 && form != 1 && form != 2)
+      throw Error(DPST_ERR_INVALID_ARG, "form must be 0 (two passes), 1 (one launch) or 2 (clusters)");
     if (!dpst::own_fft_supported(nx, ny))
       throw Error(DPST_ERR_UNSUPPORTED, "the library's x-y transforms take powers of two, 64 <= nx <= 2048, "
                                         "32 <= ny <= 1024");
     if (form == 1 && !dpst::fft_xy_fused_supported(nx, ny))
       throw Error(DPST_ERR_UNSUPPORTED, "the one-launch x-y transform takes nx = ny in 128, 256, 512, 1024");
+    if (form == 2 && !dpst::fft_xy_cluster_supported(nx, ny))
+      throw Error(DPST_ERR_UNSUPPORTED, "the cluster x-y transform takes nx = ny in 256, 512");
     DPST_CUDA(cudaSetDevice(device));
     cudaStream_t s = (cudaStream_t)stream;
     dpst::DevBuf twx, twy;
@@ -1789,6 +1836,25 @@ int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int i
     dpst::upload(twy, dpst::fft_twiddles(ny));
     DPST_CUDA(dpst::fft_setup(nx, ny));
     const int nxh = nx / 2 + 1;
+    if (form == 2) {
+      int grid = 0;
+      DPST_CUDA(dpst::fft_xy_cluster_setup(nx, ny, &grid));
+      if (grid <= 0) throw Error(DPST_ERR_UNSUPPORTED, "the cluster x-y transform cannot be resident on this device");
+      dpst::DevBuf err;
+      err.alloc(sizeof(int));
+      DPST_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+      if (!inverse)
+        DPST_CUDA(dpst::fft_xy_cluster(false, (const float *)in, (float2 *)out, nullptr, nx, ny, planes,
+                                       twx.as<float2>(), twy.as<float2>(), err.as<int>(), grid, s));
+      else
+        DPST_CUDA(dpst::fft_xy_cluster(true, nullptr, (float2 *)in, (float *)out, nx, ny, planes, twx.as<float2>(),
+                                       twy.as<float2>(), err.as<int>(), grid, s));
+      int word = 0;
+      DPST_CUDA(cudaMemcpyAsync(&word, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      DPST_CUDA(cudaStreamSynchronize(s));
+      if (word != 0) throw Error(DPST_ERR_CUDA, "cluster x-y transform: a wait gave up");
+      return;
+    }
     if (form == 1) {
       int grid = 0;
       DPST_CUDA(dpst::fft_xy_setup(nx, ny, &grid));

@@ -451,6 +451,317 @@ __global__ void __launch_bounds__(XyCfg<NX, NY>::T, XyCfg<NX, NY>::MINB) k_fft_x
 }
 
 // ---------------------------------------------------------------------------
+// both passes in one launch, the plane held across a thread-block cluster
+// ---------------------------------------------------------------------------
+// A cluster of FFT_CL CTAs transforms one (component, level) plane at a time,
+// the plane's rows split evenly among its CTAs (RC = ny / FFT_CL rows each,
+// in shared memory with a 16-byte row pitch), so that HBM sees one read of
+// the input and one write of the output per direction:
+//   forward: the CTA's RC real rows arrive by bulk asynchronous copies (one
+//     mbarrier, the rows' byte count); each row's real-to-complex transform
+//     runs in place; after a cluster barrier each CTA takes column tiles
+//     rank, rank + FFT_CL, ... (FFT_CW columns each), gathers the tile's ny
+//     rows from the owning CTAs' shared memory (distributed shared memory),
+//     transforms along y and stores the tile to the spectrum;
+//   inverse: each CTA loads its column tiles from the spectrum, transforms
+//     along y and stores every row of the tile into the owning CTA's shared
+//     memory; after a cluster barrier each CTA runs the complex-to-real
+//     transform of its rows and stores them to the grid.
+// A cluster barrier closes every plane, so no CTA writes a row buffer that
+// another is still reading, and none exits while its memory may be read.
+// Every CTA of a cluster takes the same planes, so all reach the same
+// barriers; the one mbarrier wait gives up after FFT_WAIT_NS (error word set,
+// the plane's results undefined) and the CTA still takes every barrier.
+constexpr int FFT_CL = 8;
+
+template <int NX, int NY>
+struct XcCfg {
+  static constexpr int L = NX / 2, NXH = L + 1;
+  static constexpr int PITCH = (NXH + 1) & ~1;  // float2 per row in shared memory
+  static constexpr int RC = NY / FFT_CL;        // rows per CTA
+  static constexpr int PR = (L >= 256) ? 16 : 8;  // row transform: threads per row
+  static constexpr int PC = 16;                 // column transform: threads per column
+  static constexpr int T = 256;
+  static constexpr int RPP = T / PR;            // rows per row pass
+  static constexpr int BUF = RowCfg<L, PR>::BUF;
+  static constexpr size_t ROWB = (size_t)RC * PITCH * 8;
+  static constexpr size_t CB = (size_t)FFT_CW * col_stride<NY, PC>() * 8;
+  static constexpr size_t SB = (size_t)RPP * BUF * 8;
+  static constexpr size_t XB = CB > SB ? CB : SB;
+  static constexpr size_t SMEM = ROWB + XB + 16;
+  static_assert(RC % RPP == 0 && (L / PR) >= PR && (NY / PC) >= PC && FFT_CW * PC == T, "cluster x-y transform");
+  static_assert(ROWB % 16 == 0 && (NX * 4) % 16 == 0, "16-byte rows");
+};
+
+static __device__ __forceinline__ uint32_t xc_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+static __device__ __forceinline__ void xc_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+static __device__ __forceinline__ uint32_t xc_mapa(uint32_t a, uint32_t rank) {
+  uint32_t d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
+static __device__ __forceinline__ float2 xc_ld_remote(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+static __device__ __forceinline__ void xc_st_remote(uint32_t a, float2 v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+
+// In-place real-to-complex transform of one row in shared memory: L float2
+// (the 2L reals) in, L + 1 values out; the P threads of the row (lane p of
+// the row's group, all in one warp) exchange through sm (BUF values).
+template <int L, int P>
+static __device__ __forceinline__ void row_r2c_sm(float2 *row, const float2 *__restrict__ twN, float2 *sm, int p) {
+  constexpr int Q = L / P, R = Q / P;
+  float2 v[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) v[q] = row[p + P * q];
+  constexpr int DIR = -1;
+  dft_reg<Q, DIR>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < Q; ++k1) {
+    float2 y = v[brev<Q>(k1)];
+    if (k1 != 0 && p != 0) y = cmulf(y, __ldg(twN + 2 * p * k1));
+    sm[k1 * (P + 1) + p] = y;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k1 = p * R + i;
+    float2 u[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
+    dft_reg<P, DIR>(u);
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[brev<P>(k2)];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) sm[(p * R + i) + Q * k2] = v[i * P + k2];
+  __syncwarp();
+  if (p == 0) sm[L] = sm[0];
+  __syncwarp();
+  for (int k = p; k <= L; k += P) {
+    const float2 zk = sm[k], zm = conjf2(sm[L - k]);
+    const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y + zm.y));
+    const float2 d = make_float2(0.5f * (zk.x - zm.x), 0.5f * (zk.y - zm.y));
+    const float2 od = make_float2(d.y, -d.x);
+    const float2 w = __ldg(twN + (k == L ? 0 : k));
+    const float2 wo = (k == L) ? make_float2(-od.x, -od.y) : cmulf(w, od);
+    row[k] = make_float2(e.x + wo.x, e.y + wo.y);
+  }
+  __syncwarp();
+}
+
+// Complex-to-real transform of one row in shared memory (L + 1 values) to
+// the 2L reals at out (global).
+template <int L, int P>
+static __device__ __forceinline__ void row_c2r_sm(const float2 *row, float *__restrict__ out,
+                                                  const float2 *__restrict__ twN, float2 *sm, int p) {
+  constexpr int Q = L / P, R = Q / P;
+  {
+    float2 t[Q];
+#pragma unroll
+    for (int m = 0; m < Q; ++m) t[m] = row[p + P * m];
+    const float2 last = row[L];
+    __syncwarp();
+#pragma unroll
+    for (int m = 0; m < Q; ++m) sm[p + P * m] = t[m];
+    if (p == 0) {
+      sm[0].y = 0.0f;
+      sm[L] = make_float2(last.x, 0.0f);
+    }
+  }
+  __syncwarp();
+  float2 v[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int k = p + P * q;
+    const float2 xk = sm[k], xm = conjf2(sm[L - k]);
+    const float2 e = make_float2(xk.x + xm.x, xk.y + xm.y);
+    const float2 d = make_float2(xk.x - xm.x, xk.y - xm.y);
+    const float2 o = (k == 0) ? d : cmulf(d, conjf2(__ldg(twN + k)));
+    v[q] = make_float2(e.x - o.y, e.y + o.x);
+  }
+  __syncwarp();
+  constexpr int DIR = 1;
+  dft_reg<Q, DIR>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < Q; ++k1) {
+    float2 y = v[brev<Q>(k1)];
+    if (k1 != 0 && p != 0) y = cmulf(y, conjf2(__ldg(twN + 2 * p * k1)));
+    sm[k1 * (P + 1) + p] = y;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k1 = p * R + i;
+    float2 u[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
+    dft_reg<P, DIR>(u);
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) v[i * P + k2] = u[brev<P>(k2)];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < R; ++i)
+#pragma unroll
+    for (int k2 = 0; k2 < P; ++k2) sm[(p * R + i) + Q * k2] = v[i * P + k2];
+  __syncwarp();
+  float2 *o = reinterpret_cast<float2 *>(out);
+  for (int n = p; n < L; n += P) __stcs(o + n, sm[n]);  // (x_2n, x_2n+1)
+  __syncwarp();
+}
+
+// Column tile `tile` of one plane: rows gathered from (INV = false) or
+// scattered to (INV = true) the cluster's row buffers (rows_sa: this CTA's
+// row buffer, shared-memory address; row y in CTA y / RC at row y % RC);
+// the spectrum plane sp [NY][nxh] is written (forward) or read (inverse).
+// Every thread of the CTA takes the one barrier.
+template <int NX, int NY, bool INV>
+static __device__ __forceinline__ void col_tile_cl(float2 *__restrict__ sp, int tile, uint32_t rows_sa,
+                                                   const float2 *__restrict__ twL, float2 *cbuf) {
+  using C = XcCfg<NX, NY>;
+  constexpr int L = NY, P = C::PC, Q = L / P, R = Q / P, DIR = INV ? 1 : -1;
+  constexpr int nxh = C::NXH;
+  const int c = threadIdx.x % FFT_CW, p = threadIdx.x / FFT_CW;
+  const int kx = tile * FFT_CW + c;
+  const bool live = kx < nxh;
+  const int kxc = live ? kx : nxh - 1;
+  float2 *sm = cbuf + c * col_stride<L, P>();
+  float2 v[Q];
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int y = p + P * q;
+    if (INV) {
+      v[q] = __ldcg(sp + (int64_t)y * nxh + kxc);
+    } else {
+      const uint32_t a = rows_sa + (uint32_t)(((y % C::RC) * C::PITCH + kxc) * 8);
+      v[q] = xc_ld_remote(xc_mapa(a, (uint32_t)(y / C::RC)));
+    }
+  }
+  dft_reg<Q, DIR>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < Q; ++k1) {
+    float2 y = v[brev<Q>(k1)];
+    if (k1 != 0 && p != 0) {
+      float2 w = __ldg(twL + p * k1);
+      if (DIR > 0) w = conjf2(w);
+      y = cmulf(y, w);
+    }
+    sm[k1 * (P + 1) + p] = y;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    const int k1 = p * R + i;
+    float2 u[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) u[q] = sm[k1 * (P + 1) + q];
+    dft_reg<P, DIR>(u);
+    if (live) {
+#pragma unroll
+      for (int k2 = 0; k2 < P; ++k2) {
+        const int y = k1 + Q * k2;
+        if (INV) {
+          const uint32_t a = rows_sa + (uint32_t)(((y % C::RC) * C::PITCH + kx) * 8);
+          xc_st_remote(xc_mapa(a, (uint32_t)(y / C::RC)), u[brev<P>(k2)]);
+        } else {
+          __stcs(sp + (int64_t)y * nxh + kx, u[brev<P>(k2)]);
+        }
+      }
+    }
+  }
+  __syncthreads();  // cbuf reused by the next tile
+}
+
+template <int NX, int NY, bool INV>
+__global__ void __cluster_dims__(FFT_CL, 1, 1) __launch_bounds__(256, 1)
+    k_fft_xy_cl(const float *__restrict__ gin, float2 *spec, float *__restrict__ gout, int64_t planes,
+                const float2 *__restrict__ twx, const float2 *__restrict__ twy, int *err) {
+  using C = XcCfg<NX, NY>;
+  extern __shared__ __align__(16) unsigned char xc_sm[];
+  float2 *rows = reinterpret_cast<float2 *>(xc_sm);
+  float2 *xb = reinterpret_cast<float2 *>(xc_sm + C::ROWB);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(xc_sm + C::ROWB + C::XB);
+  const uint32_t rows_sa = (uint32_t)__cvta_generic_to_shared(rows);
+  const uint32_t bar_sa = (uint32_t)__cvta_generic_to_shared(bar);
+  const uint32_t rank = xc_rank();
+  const int64_t cl = blockIdx.x / FFT_CL, ncl = gridDim.x / FFT_CL;
+  constexpr int ntiles = (C::NXH + FFT_CW - 1) / FFT_CW;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_sa));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  xc_cluster_sync();  // every CTA of the cluster runs before any remote access
+  int it = 0;
+  for (int64_t pl = cl; pl < planes; pl += ncl, ++it) {
+    const int64_t row0 = pl * NY + (int64_t)rank * C::RC;  // this CTA's first row of the plane
+    if (!INV) {
+      if (tid == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_sa),
+                     "r"((uint32_t)(C::RC * NX * 4))
+                     : "memory");
+        for (int i = 0; i < C::RC; ++i)
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                  rows_sa + (uint32_t)(i * C::PITCH * 8)),
+              "l"(gin + (row0 + i) * NX), "r"((uint32_t)(NX * 4)), "r"(bar_sa)
+              : "memory");
+      }
+      {
+        const unsigned long long t0 = fft_clock_ns();
+        for (int spin = 0;; ++spin) {
+          uint32_t done;
+          asm volatile(
+              "{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.b32 %0, 1, 0, "
+              "q;\n\t}"
+              : "=r"(done)
+              : "r"(bar_sa), "r"((uint32_t)(it & 1))
+              : "memory");
+          if (done) break;
+          if ((spin & 63) == 63 && fft_clock_ns() - t0 > FFT_WAIT_NS) {
+            if (tid == 0) atomicOr(err, 1);
+            break;
+          }
+        }
+      }
+      for (int r0 = 0; r0 < C::RC; r0 += C::RPP)
+        row_r2c_sm<C::L, C::PR>(rows + (r0 + tid / C::PR) * C::PITCH, twx, xb + (tid / C::PR) * C::BUF,
+                                tid % C::PR);
+      xc_cluster_sync();
+      for (int tile = (int)rank; tile < ntiles; tile += FFT_CL)
+        col_tile_cl<NX, NY, false>(spec + pl * (int64_t)NY * C::NXH, tile, rows_sa, twy, xb);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // row writes before the next copies
+      xc_cluster_sync();
+    } else {
+      for (int tile = (int)rank; tile < ntiles; tile += FFT_CL)
+        col_tile_cl<NX, NY, true>(spec + pl * (int64_t)NY * C::NXH, tile, rows_sa, twy, xb);
+      xc_cluster_sync();
+      for (int r0 = 0; r0 < C::RC; r0 += C::RPP) {
+        const int r = r0 + tid / C::PR;
+        row_c2r_sm<C::L, C::PR>(rows + r * C::PITCH, gout + (row0 + r) * NX, twx, xb + (tid / C::PR) * C::BUF,
+                                tid % C::PR);
+      }
+      xc_cluster_sync();
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
@@ -588,6 +899,63 @@ static cudaError_t xy_setup(int *grid) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) *grid = (per_sm > 0 ? per_sm : 1) * nsm;
   return e;
+}
+
+// ---- the cluster form ----
+bool fft_xy_cluster_supported(int nx, int ny) { return nx == ny && (nx == 256 || nx == 512); }
+
+template <int NX, int NY>
+static cudaError_t xc_setup(int *grid) {
+  using C = XcCfg<NX, NY>;
+  cudaError_t e = cudaFuncSetAttribute(k_fft_xy_cl<NX, NY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)C::SMEM);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_fft_xy_cl<NX, NY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(FFT_CL * 64, 1, 1);
+  cfg.blockDim = dim3(C::T, 1, 1);
+  cfg.dynamicSmemBytes = C::SMEM;
+  int ncl = 0;
+  e = cudaOccupancyMaxActiveClusters(&ncl, (void *)k_fft_xy_cl<NX, NY, false>, &cfg);
+  if (e != cudaSuccess) return e;
+  *grid = ncl * FFT_CL;
+  return cudaSuccess;
+}
+
+// Shared-memory attributes and the grid (clusters resident at once x FFT_CL
+// CTAs); grid 0: the cluster form cannot run here.
+cudaError_t fft_xy_cluster_setup(int nx, int ny, int *grid) {
+  *grid = 0;
+  if (!fft_xy_cluster_supported(nx, ny)) return cudaErrorInvalidValue;
+  cudaError_t e = upload_tw32();
+  if (e != cudaSuccess) return e;
+  if (nx == 256) return xc_setup<256, 256>(grid);
+  return xc_setup<512, 512>(grid);
+}
+
+// Forward (grid_in -> spec) or inverse (spec -> grid_out, spec overwritten)
+// x-y transform of `planes` planes in one launch of clusters; err: an int
+// set (never cleared) when a wait gave up.
+cudaError_t fft_xy_cluster(bool inverse, const float *grid_in, float2 *spec, float *grid_out, int nx, int ny,
+                           int64_t planes, const float2 *twx, const float2 *twy, int *err, int grid, cudaStream_t s) {
+  if (!fft_xy_cluster_supported(nx, ny) || grid < FFT_CL || planes <= 0) return cudaErrorInvalidValue;
+  int64_t g = (int64_t)(grid / FFT_CL) * FFT_CL;
+  if (g > planes * FFT_CL) g = planes * FFT_CL;
+#define XC_LAUNCH(N)                                                                                            \
+  if (inverse)                                                                                                 \
+    k_fft_xy_cl<N, N, true><<<(unsigned)g, XcCfg<N, N>::T, XcCfg<N, N>::SMEM, s>>>(grid_in, spec, grid_out, planes, \
+                                                                                 twx, twy, err);               \
+  else                                                                                                         \
+    k_fft_xy_cl<N, N, false><<<(unsigned)g, XcCfg<N, N>::T, XcCfg<N, N>::SMEM, s>>>(grid_in, spec, grid_out,     \
+                                                                                  planes, twx, twy, err);
+  if (nx == 256) {
+    XC_LAUNCH(256)
+  } else {
+    XC_LAUNCH(512)
+  }
+#undef XC_LAUNCH
+  return cudaGetLastError();
 }
 
 // Shared-memory attributes and the persistent grid (CTAs resident at once).

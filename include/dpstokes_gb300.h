@@ -176,8 +176,11 @@ typedef struct dpst_info {
                                       128, 256, 512, 1024, when faster at creation); 3 the
                                       FP64 operator's own double-float two passes (powers of
                                       two, nx <= 1024, ny <= 512, when faster than cuFFT);
-                                      0 cuFFT.  DPSTOKES_GB300_XY_FFT=cufft | twopass |
-                                      fused | own forces one */
+                                      4 one launch of thread-block clusters, each plane held
+                                      in the shared memory of 8 CTAs (nx = ny in 256, 512,
+                                      when faster at creation); 0 cuFFT.
+                                      DPSTOKES_GB300_XY_FFT=cufft | twopass | fused |
+                                      cluster | own forces one */
   float xy_ms[2];                  /* creation-time timings of a forward + inverse pair:
                                       mixed: two-pass, one-launch; FP64: cuFFT, own
                                       double-float (0 if not timed) */
@@ -191,6 +194,8 @@ typedef struct dpst_info {
   int ztransform_tma_variant[2];   /* that variant per direction: 0, 1, 2 = (TMA ring stages,
                                       converted operand stages) (6, 2), (4, 3), (7, 2) */
   float ztransform_tma_variant_ms[6]; /* every variant's timing, [direction][variant] */
+  float xy_cluster_ms;             /* creation-time timing of the cluster form's forward +
+                                      inverse pair (0 if not timed) */
 } dpst_info;
 
 typedef struct dpst_engine *dpst_handle;
@@ -365,7 +370,10 @@ int dpst_get_info(dpst_handle h, dpst_info *out);
  * 2048, 32 <= ny <= 1024.  form 0: two launches (rows, columns); form 1:
  * one persistent launch of both passes (nx = ny in 128, 256, 512, 1024,
  * else DPST_ERR_UNSUPPORTED), whose bounded waits report DPST_ERR_CUDA if
- * one gave up.  Allocates its tables and synchronises the stream. */
+ * one gave up; form 2: one launch of 8-CTA thread-block clusters, a plane
+ * held in a cluster's shared memory (nx = ny in 256, 512, else
+ * DPST_ERR_UNSUPPORTED; a bounded wait that gave up reports DPST_ERR_CUDA).
+ * Allocates its tables and synchronises the stream. */
 int dpst_xy_transform(int nx, int ny, int64_t planes, void *in, void *out, int inverse, int form, int device,
                       void *stream);
 

@@ -25,6 +25,7 @@ from doublyperiodicstokes_gb300 import DPStokes, StokesParams, _lib, workloads a
 pytestmark = pytest.mark.gpu
 SIZES = [(64, 32), (128, 128), (256, 64), (512, 512), (1024, 256), (2048, 1024), (64, 1024), (256, 512), (128, 512)]
 FUSED = [(128, 128), (256, 256), (512, 512), (1024, 1024)]
+CLUSTER = [(256, 256), (512, 512)]
 
 
 def _xy(nx, ny, planes, src, dst, inverse, form=0):
@@ -83,7 +84,7 @@ def test_operator_own_fft_matches_cufft(name, monkeypatch):
         out[which] = (own, V.double().cpu().numpy(), Wv.double().cpu().numpy() if Wv is not None else None)
         op.close()
     pow2 = (w.nx & (w.nx - 1)) == 0 and (w.ny & (w.ny - 1)) == 0 and w.nx >= 64 and w.ny >= 32
-    assert (out["own"][0] in (1, 2)) == pow2 and out["cufft"][0] == 0
+    assert (out["own"][0] in (1, 2, 4)) == pow2 and out["cufft"][0] == 0
     ev = rel_err(out["own"][1], out["cufft"][1])
     print("%s own vs cuFFT V %.2e" % (name, ev))
     assert ev < 5e-6
@@ -116,6 +117,42 @@ def test_one_launch_equals_two_pass(nx, ny, planes):
         assert d < 1e-6
 
 
+@pytest.mark.parametrize("nx,ny", CLUSTER)
+@pytest.mark.parametrize("planes", [1, 5, 40, 390])
+def test_cluster_form_equals_two_pass(nx, ny, planes):
+    """The cluster form (a plane across 8 CTAs' shared memory, the column
+    pass through distributed shared memory): the two-pass results (same
+    arithmetic per value), forward and inverse, on repeated launches, for
+    fewer planes than clusters and for several planes per cluster."""
+    g = torch.Generator(device="cuda").manual_seed(nx + planes + 1)
+    x = torch.randn(planes, ny, nx, device="cuda", generator=g, dtype=torch.float32)
+    s2 = torch.empty(planes, ny, nx // 2 + 1, dtype=torch.complex64, device="cuda")
+    s1 = torch.empty_like(s2)
+    _xy(nx, ny, planes, x, s2, False, form=0)
+    for _ in range(2):
+        s1.fill_(float("nan"))
+        _xy(nx, ny, planes, x, s1, False, form=2)
+        d = float((s1 - s2).abs().max() / s2.abs().max())
+        print("%d x %d x %d forward cluster vs two-pass %.2e" % (nx, ny, planes, d))
+        assert d < 1e-6
+    b2 = torch.empty_like(x)
+    b1 = torch.empty_like(x)
+    _xy(nx, ny, planes, s2.clone(), b2, True, form=0)
+    for _ in range(2):
+        b1.fill_(float("nan"))
+        _xy(nx, ny, planes, s2.clone(), b1, True, form=2)
+        d = float((b1 - b2).abs().max() / b2.abs().max())
+        print("%d x %d x %d inverse cluster vs two-pass %.2e" % (nx, ny, planes, d))
+        assert d < 1e-6
+
+
+def test_cluster_form_rejects_other_sizes():
+    x = torch.zeros(1, 128, 128, device="cuda")
+    s = torch.zeros(1, 128, 65, dtype=torch.complex64, device="cuda")
+    with pytest.raises(_lib.DPStokesError):
+        _xy(128, 128, 1, x, s, False, form=2)
+
+
 def test_one_launch_rejects_other_sizes():
     x = torch.zeros(1, 64, 128, device="cuda")
     s = torch.zeros(1, 64, 65, dtype=torch.complex64, device="cuda")
@@ -132,10 +169,12 @@ def test_operator_one_launch_matches_two_pass(name, monkeypatch):
     Fk = rng.standard_normal((K, w.N, 3)).astype(np.float32)
     Tk = rng.standard_normal((K, w.N, 3)).astype(np.float32)
     out = {}
-    for form in ("twopass", "fused"):
+    for form in ("twopass", "fused", "cluster"):
+        if form == "cluster" and w.nx not in (256, 512):
+            continue
         monkeypatch.setenv("DPSTOKES_GB300_XY_FFT", form)
         op = DPStokes(StokesParams.from_workload(w, "mixed"), w.N)
-        assert op.info()["xy_transform"] == (2 if form == "fused" else 1)
+        assert op.info()["xy_transform"] == {"fused": 2, "twopass": 1, "cluster": 4}[form]
         op.set_positions(torch.tensor(X, device=op.device))
         V, Wv = op.mdot(torch.tensor(F, dtype=torch.float32, device=op.device),
                         torch.tensor(T, dtype=torch.float32, device=op.device))
@@ -145,6 +184,9 @@ def test_operator_one_launch_matches_two_pass(name, monkeypatch):
         op.close()
     for a, b in zip(out["fused"], out["twopass"]):
         assert rel_err(a, b) < 5e-6
+    if "cluster" in out:
+        for a, b in zip(out["cluster"], out["twopass"]):
+            assert rel_err(a, b) < 5e-6
 
 
 @pytest.mark.parametrize("name", ["c0_dpbw_n2048", "c2_dp_n65536@128", "c1_dpsc_n16384@128"])
