@@ -56,6 +56,8 @@ static __device__ __forceinline__ void dft_reg(float2 (&v)[S]) {
         const float2 d = make_float2(a.x - b.x, a.y - b.y);
         if (k == 0) {
           v[i + k + len / 2] = d;
+        } else if (4 * k == len) {  // w = -i (forward) or +i: exact, no multiply
+          v[i + k + len / 2] = DIR < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
         } else {
           float2 w = c_tw32[k * (32 / len)];
           if (DIR > 0) w = conjf2(w);

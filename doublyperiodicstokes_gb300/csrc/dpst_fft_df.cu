@@ -66,6 +66,8 @@ static __device__ __forceinline__ void dft_reg_d(dcx (&v)[S]) {
         const dcx d = dc_sub(a, b);
         if (k == 0) {
           v[i + k + len / 2] = d;
+        } else if (4 * k == len) {  // w = -i (forward) or +i: exact, no multiply
+          v[i + k + len / 2] = DIR < 0 ? dc_make(d.y, df_neg(d.x)) : dc_make(df_neg(d.y), d.x);
         } else {
           const float4 t = c_tw32d[k * (32 / len)];
           dcx w = dc_make(df_make(t.x, t.y), df_make(t.z, t.w));
