@@ -500,10 +500,11 @@ def run_batched(args, dev):
             "batched_ms": batched, "loop_ms": looped, "speedup_vs_loop": looped / batched,
             "batched_particles_per_s": n / (batched / 1e3), "loop_particles_per_s": n / (looped / 1e3),
             "kernels_per_batched_mdot": info["kernels_per_mdot"], "fft_plans": info["fft_plans"],
-            "ztransform": {1: "tcgen05", 0: "SIMT"}.get(info["ztransform"]),
-            "ztransform_inverse": {1: "tcgen05", 0: "SIMT"}.get(info["ztransform_inverse"]),
+            "ztransform": {1: "tcgen05", 3: "tcgen05, TMA-fed", 0: "SIMT"}.get(info["ztransform"]),
+            "ztransform_inverse": {1: "tcgen05", 3: "tcgen05, TMA-fed", 0: "SIMT"}.get(info["ztransform_inverse"]),
             "ztransform_ms_simt_tcgen05": [round(float(x), 3) for x in info["ztransform_ms"]],
             "ztransform_inverse_ms_simt_tcgen05": [round(float(x), 3) for x in info["ztransform_inverse_ms"]],
+            "ztransform_tma_ms_fwd_inv": [round(float(x), 3) for x in info["ztransform_tma_ms"]],
             "precision": "mixed", "note": "one CUDA graph launch per batched Mdot"}
 
 

@@ -52,7 +52,7 @@ class DpstBatchInfo(ctypes.Structure):
                 ("kernels_per_mdot", ctypes.c_int), ("fft_plans", ctypes.c_int),
                 ("device_bytes", ctypes.c_int64), ("ztransform", ctypes.c_int),
                 ("ztransform_inverse", ctypes.c_int), ("ztransform_ms", ctypes.c_float * 2),
-                ("ztransform_inverse_ms", ctypes.c_float * 2)]
+                ("ztransform_inverse_ms", ctypes.c_float * 2), ("ztransform_tma_ms", ctypes.c_float * 2)]
 
 
 # every entry point of include/dpstokes_gb300.h with its signature

@@ -15,6 +15,7 @@
 // batched Mdot.
 // Shared across the batch (checked at creation): nz, zmin, zmax, geometry,
 // viscosity, precision, torque flag.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 
@@ -63,6 +64,9 @@ cudaError_t launch_zgemm_tc_b(const ZSeg<float> *segs, const int64_t *tprefix, i
                               const float *Tm, bool corr, int nsm, int *err, cudaStream_t s);
 cudaError_t launch_corr_add_b(const ZSeg<float> *segs, const int64_t *mprefix, int S, int64_t K, int nz, int wall,
                               cudaStream_t s);
+bool ztm_maps_b(const ZSeg<float> *segs, int S, int nz, std::vector<CUtensorMap> &out);
+cudaError_t launch_zgemm_tma_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                               const float *Tm, const CUtensorMap *gmaps, int nsm, int *err, cudaStream_t s);
 
 template <typename RP>
 __global__ void k_prep_pos_b(const RP *pos, int64_t N, double zmin, double *out) {
@@ -102,8 +106,19 @@ struct BatchEngine : BatchBase {
   // the creation-time timings {SIMT, tcgen05} per direction
   DevBuf d_tprefix_tc, ztc_err, d_segi_nc;  // d_segi_nc: the inverse segments without the wall correction
   int64_t ntiles_tc = 0;
-  bool ztc_use[2] = {false, false};
+  // per direction: 0 SIMT, 1 tcgen05 (register-staged operands), 3 tcgen05
+  // fed by TMA (every system's spectrum through its own tensor maps, d_tmaps)
+  int ztc_use[2] = {0, 0};
   float ztc_ms[2][2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+  float ztm_ms[2] = {0.0f, 0.0f};
+  // the TMA form runs over the systems whose spectrum rows start on 16-byte
+  // boundaries (an even mode count; "a" tables: forward segments, inverse
+  // segments without the correction, tile prefix, the tensor maps) and the
+  // register-staged form over the others ("b" tables)
+  DevBuf d_tmaps, d_segf_a, d_segi_a, d_tp_a, d_segf_b, d_segi_b, d_tp_b;
+  int S_a = 0, S_b = 0;
+  int64_t ntiles_a = 0, ntiles_b = 0;
+  bool tma_ok = false;
   DevBuf d_jobs_m, d_jobs_d, d_jpx_m, d_jpy_m, d_jpx_d, d_jpy_d, d_reach, d_flags;
   int64_t items_m = 0, items_d = 0, ntiles = 0;
   int njobs_m = 0, njobs_d = 0;
@@ -157,9 +172,18 @@ struct BatchEngine : BatchBase {
         const bool walls = inverse && mode != DPST_MODE_NOWALL;
         const ZSeg<R> *tsegs = walls ? d_segi_nc.template as<ZSeg<R>>() : segs;
         // no segment's epilogue corrects (the correction is its own pass)
-        DPST_CUDA(launch_zgemm_tc_b(reinterpret_cast<const ZSeg<float> *>(tsegs), d_tprefix_tc.as<int64_t>(), S,
-                                    ntiles_tc, nz, reinterpret_cast<const float *>(Tm), false, nsm,
-                                    ztc_err.as<int>(), s));
+        if (ztc_use[inverse ? 1 : 0] == 3 && tma_ok) {
+          DPST_CUDA(launch_zgemm_tma_b((inverse ? d_segi_a : d_segf_a).as<ZSeg<float>>(), d_tp_a.as<int64_t>(), S_a,
+                                       ntiles_a, nz, reinterpret_cast<const float *>(Tm),
+                                       d_tmaps.as<CUtensorMap>(), nsm, ztc_err.as<int>(), s));
+          if (S_b > 0)
+            DPST_CUDA(launch_zgemm_tc_b((inverse ? d_segi_b : d_segf_b).as<ZSeg<float>>(), d_tp_b.as<int64_t>(), S_b,
+                                        ntiles_b, nz, reinterpret_cast<const float *>(Tm), false, nsm,
+                                        ztc_err.as<int>(), s));
+        } else
+          DPST_CUDA(launch_zgemm_tc_b(reinterpret_cast<const ZSeg<float> *>(tsegs), d_tprefix_tc.as<int64_t>(), S,
+                                      ntiles_tc, nz, reinterpret_cast<const float *>(Tm), false, nsm,
+                                      ztc_err.as<int>(), s));
         if (walls)
           DPST_CUDA(launch_corr_add_b(reinterpret_cast<const ZSeg<float> *>(segs), d_mprefix.as<int64_t>(), S, K, nz,
                                       mode, s));
@@ -169,10 +193,10 @@ struct BatchEngine : BatchBase {
     DPST_CUDA(launch_zgemm_b<R>(segs, d_tprefix.as<int64_t>(), S, ntiles, nz, Tm, nsm, s, inverse));
   }
 
-  // Per direction, the SIMT and tcgen05 transforms are timed on the spectrum
-  // buffer (one warm-up, three runs) and the faster kept; a tcgen05 run whose
-  // waits timed out is never kept.  DPSTOKES_GB300_ZTRANSFORM=simt|tcgen05
-  // forces one.
+  // Per direction, the SIMT, tcgen05 and TMA-fed tcgen05 transforms are
+  // timed on the spectrum buffer (one warm-up, three runs) and the fastest
+  // kept; a tensor-core run whose waits timed out is never kept.
+  // DPSTOKES_GB300_ZTRANSFORM=simt|tcgen05|tma forces one.
   void tune_ztransform() {
     if (sizeof(R) != 4 || nz > 128) return;
     ztc_err.alloc(sizeof(int));
@@ -186,15 +210,17 @@ struct BatchEngine : BatchBase {
     DPST_CUDA(cudaEventCreate(&a));
     DPST_CUDA(cudaEventCreate(&b));
     for (int dir = 0; dir < 2; ++dir) {
-      for (int k = 0; k < 2; ++k) {
-        ztc_use[dir] = k == 1;
+      for (int k = 0; k < 3; ++k) {
+        if (k == 2 && !tma_ok) continue;
+        ztc_use[dir] = k == 2 ? 3 : k;
         ztrans(dir == 1, 0);
         DPST_CUDA(cudaEventRecord(a, 0));
         for (int rep = 0; rep < 3; ++rep) ztrans(dir == 1, 0);
         DPST_CUDA(cudaEventRecord(b, 0));
         DPST_CUDA(cudaEventSynchronize(b));
-        DPST_CUDA(cudaEventElapsedTime(&ztc_ms[dir][k], a, b));
-        ztc_ms[dir][k] /= 3.0f;
+        float ms = 0.0f;
+        DPST_CUDA(cudaEventElapsedTime(&ms, a, b));
+        (k == 2 ? ztm_ms[dir] : ztc_ms[dir][k]) = ms / 3.0f;
       }
     }
     cudaEventDestroy(a);
@@ -202,10 +228,19 @@ struct BatchEngine : BatchBase {
     int err = 0;
     DPST_CUDA(cudaMemcpy(&err, ztc_err.p, sizeof(int), cudaMemcpyDeviceToHost));
     for (int dir = 0; dir < 2; ++dir) {
-      if (want == "tcgen05") ztc_use[dir] = true;
-      else if (want == "simt") ztc_use[dir] = false;
-      else ztc_use[dir] = ztc_ms[dir][1] < ztc_ms[dir][0];
-      if (err != 0) ztc_use[dir] = false;
+      if (want == "tma" && tma_ok) ztc_use[dir] = 3;
+      else if (want == "tcgen05") ztc_use[dir] = 1;
+      else if (want == "simt") ztc_use[dir] = 0;
+      else {
+        float best = ztc_ms[dir][0];
+        ztc_use[dir] = 0;
+        if (ztc_ms[dir][1] < best) {
+          best = ztc_ms[dir][1];
+          ztc_use[dir] = 1;
+        }
+        if (tma_ok && ztm_ms[dir] < best) ztc_use[dir] = 3;
+      }
+      if (err != 0) ztc_use[dir] = 0;
     }
     DPST_CUDA(cudaMemset(spec.p, 0, spec.bytes));
   }
@@ -520,6 +555,40 @@ struct BatchEngine : BatchBase {
       }
       upload(d_segi_nc, nc);
     }
+    if (sizeof(R) == 4 && nz >= 32 && nz <= 128) {
+      // the systems the TMA form takes and their tensor maps (the same
+      // spectra in both directions); the others keep the register-staged form
+      std::vector<ZSeg<R>> fa, ia, fb, ib;
+      std::vector<int64_t> pa(1, 0), pb(1, 0);
+      for (int oi = 0; oi < S; ++oi) {
+        ZSeg<R> inc = segi[oi];
+        inc.e.corr = nullptr;
+        inc.e.corrf = nullptr;
+        std::vector<CUtensorMap> one;
+        const bool a = ztm_maps_b(reinterpret_cast<const ZSeg<float> *>(&segf[oi]), 1, nz, one);
+        (a ? fa : fb).push_back(segf[oi]);
+        (a ? ia : ib).push_back(inc);
+        std::vector<int64_t> &pp = a ? pa : pb;
+        pp.push_back(pp.back() + ztc_tiles(segf[oi].ncols));
+      }
+      S_a = (int)fa.size();
+      S_b = (int)fb.size();
+      std::vector<CUtensorMap> maps;
+      tma_ok = S_a > 0 && ztm_maps_b(reinterpret_cast<const ZSeg<float> *>(fa.data()), S_a, nz, maps);
+      if (tma_ok) {
+        upload(d_tmaps, maps);
+        upload(d_segf_a, fa);
+        upload(d_segi_a, ia);
+        upload(d_tp_a, pa);
+        ntiles_a = pa.back();
+        if (S_b > 0) {
+          upload(d_segf_b, fb);
+          upload(d_segi_b, ib);
+          upload(d_tp_b, pb);
+          ntiles_b = pb.back();
+        }
+      }
+    }
     size_t bvp_bytes = 0;
     if (dfsolve) {
       DPST_CUDA(bvp_df_plan_b(sysk[0].ks, K, nsm, &bvp_grid, &bvp_bytes));
@@ -829,16 +898,21 @@ struct BatchEngine : BatchBase {
     o->n_particles = Ntot;
     o->n_modes = K;
     o->kernels_per_mdot = kernels_per_mdot;
+    // the TMA form's second launch over the systems it does not take
+    for (int d = 0; d < 2; ++d)
+      if (kernels_per_mdot > 0 && ztc_use[d] == 3 && tma_ok && S_b > 0) o->kernels_per_mdot += 1;
     o->fft_plans = 2 * (int)classes.size();
-    o->ztransform = ztc_use[0] ? 1 : 0;
-    o->ztransform_inverse = ztc_use[1] ? 1 : 0;
+    o->ztransform = ztc_use[0];
+    o->ztransform_inverse = ztc_use[1];
     for (int k = 0; k < 2; ++k) {
       o->ztransform_ms[k] = ztc_ms[0][k];
       o->ztransform_inverse_ms[k] = ztc_ms[1][k];
+      o->ztransform_tma_ms[k] = ztm_ms[k];
     }
     int64_t bytes = 0;
     const DevBuf *all[] = {&d_sysp, &d_sysk, &d_segf, &d_segi, &d_pprefix, &d_ipm, &d_ipd, &d_mprefix, &d_tprefix,
-                           &d_tprefix_tc, &ztc_err, &d_segi_nc,
+                           &d_tprefix_tc, &ztc_err, &d_segi_nc, &d_tmaps, &d_segf_a, &d_segi_a, &d_tp_a,
+                           &d_segf_b, &d_segi_b, &d_tp_b,
                            &d_jobs_m, &d_jobs_d, &grid, &spec, &corr, &zext, &wext, &zn, &bands, &bcrows, &k0rows,
                            &Tf, &Ti, &kvs, &f_mf, &f_bk, &f_ab, &f_g, &st_cell_m, &st_x_m, &st_y_m, &st_z_m,
                            &st_zw_m, &st_cell_d, &st_x_d, &st_y_d, &st_z_d, &st_zw_d, &st_dx_d, &st_dy_d,

@@ -35,6 +35,7 @@
 #include <cuda.h>
 
 #include <mutex>
+#include <vector>
 
 #include "dpst_internal.cuh"
 #include "dpst_kdev.cuh"
@@ -618,10 +619,45 @@ static __device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atme
       "r"(atmem), "l"(bd), "r"(idesc), "r"(acc));
 }
 
-template <int RS, int HL>
+// BATCH: the tiles of S segments (systems) numbered by the prefix tprefix of
+// 3 ceil(ncols_s / 128) tiles each; segment s's load and store maps are
+// gmaps[2 s], gmaps[2 s + 1] (global memory) and its scale is its EpiArgs'.
+struct ZtmTile {
+  int64_t col0;
+  int d, seg;
+};
+template <bool BATCH>
+static __device__ __forceinline__ ZtmTile ztm_tile(int64_t t, int64_t ncols, const ZSeg<float> *__restrict__ segs,
+                                                   const int64_t *__restrict__ tprefix, int S) {
+  ZtmTile z;
+  z.seg = 0;
+  if (BATCH) {
+    int lo = 0, hi = S - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tprefix[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    z.seg = lo;
+    t -= tprefix[lo];
+    ncols = segs[lo].ncols;
+  }
+  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;
+  z.d = (int)(t / tpc);
+  z.col0 = (t % tpc) * ZTC_N;
+  return z;
+}
+
+static __device__ __forceinline__ void tmap_acquire(const CUtensorMap *m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(m))
+               : "memory");
+}
+
+template <int RS, int HL, bool BATCH>
 __global__ void __launch_bounds__(ZTM_THREADS, 1)
     k_zgemm_tma(const __grid_constant__ CUtensorMap map_ld, const __grid_constant__ CUtensorMap map_st, int nz,
-                int64_t ncols, const float *__restrict__ Tm, float scale, int *err) {
+                int64_t ncols, const float *__restrict__ Tm, float scale, int *err, const CUtensorMap *gmaps,
+                const ZSeg<float> *__restrict__ segs, const int64_t *__restrict__ tprefix, int S, int64_t ntiles_b) {
   using Cfg = ZtmCfg<RS, HL>;
   extern __shared__ unsigned char ztm_raw_sm[];
   // 1024-byte alignment of the swizzled staging (the dynamic window's base
@@ -668,7 +704,7 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  if (warp == ZTM_TMA_WARP && lane == 0) {
+  if (!BATCH && warp == ZTM_TMA_WARP && lane == 0) {  // (BATCH: the parameter maps are unused)
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_ld)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_st)) : "memory");
   }
@@ -678,8 +714,7 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
 
-  const int64_t tpc = (ncols + ZTC_N - 1) / ZTC_N;  // tiles per component
-  const int64_t ntiles = 3 * tpc;
+  const int64_t ntiles = BATCH ? ntiles_b : 3 * ((ncols + ZTC_N - 1) / ZTC_N);
   const int64_t G = gridDim.x;
   const int my_tiles = (blockIdx.x < ntiles) ? (int)((ntiles - 1 - blockIdx.x) / G + 1) : 0;
   const int nkc = (kp + ZTC_KC - 1) / ZTC_KC;  // stages per tile
@@ -687,15 +722,28 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
   constexpr int SKQ = ZTC_KC / 4;
 
   // TMA: step u's block into ring stage u % RS once the stage is free
-  int issued = 0;
+  int issued = 0, ld_j = -1, ld_seg = -1;
+  ZtmTile ld_t;
+  ld_t.col0 = 0;
+  ld_t.d = ld_t.seg = 0;
   auto tma_issue = [&](int u) -> bool {
     const int rs = u % RS;
     if (!ztc_wait(rempty_bar(rs), (uint32_t)(((u / RS) & 1) ^ 1), abort_flag, err)) return false;
     const int j = u / nkc, c = u - j * nkc;
-    const int64_t t = blockIdx.x + (int64_t)j * G;
+    if (j != ld_j) {
+      ld_t = ztm_tile<BATCH>(blockIdx.x + (int64_t)j * G, ncols, segs, tprefix, S);
+      ld_j = j;
+    }
+    const CUtensorMap *m = &map_ld;
+    if (BATCH) {
+      m = gmaps + 2 * ld_t.seg;
+      if (ld_t.seg != ld_seg) {
+        tmap_acquire(m);
+        ld_seg = ld_t.seg;
+      }
+    }
     mbar_expect_tx(rfull_bar(rs), ZTM_RAW_BYTES);
-    tma_load_3d(raw0 + (uint32_t)rs * ZTM_RAW_BYTES, &map_ld, (int)((t % tpc) * ZTC_N), ZTC_KC * c, (int)(t / tpc),
-                rfull_bar(rs));
+    tma_load_3d(raw0 + (uint32_t)rs * ZTM_RAW_BYTES, m, (int)ld_t.col0, ZTC_KC * c, ld_t.d, rfull_bar(rs));
     issued = u + 1;
     return true;
   };
@@ -804,19 +852,30 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
     };
     const bool rows_live = 32 * qd < nz;
     int nst = 0;  // blocks stored by this warp (staging buffer nst & 1)
+    int st_seg = -1;
+    const CUtensorMap *mst = &map_st;
+    int64_t ncols_t = ncols;
     for (int j = 0; j < my_tiles; ++j) {
       const int a = j % ZTC_ACC;
       bool ok = ztc_wait(accf_bar(a), (uint32_t)((j / ZTC_ACC) & 1), abort_flag, err);
       if (!__all_sync(0xffffffffu, ok)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const int64_t t = blockIdx.x + (int64_t)j * G;
-      const int d = (int)(t / tpc);
-      const int64_t col0 = (t % tpc) * ZTC_N;
+      const ZtmTile zt = ztm_tile<BATCH>(blockIdx.x + (int64_t)j * G, ncols, segs, tprefix, S);
+      const int d = zt.d;
+      const int64_t col0 = zt.col0;
+      if (BATCH && zt.seg != st_seg) {
+        st_seg = zt.seg;
+        mst = gmaps + 2 * st_seg + 1;
+        ncols_t = segs[st_seg].ncols;
+        scale = segs[st_seg].e.inverse ? (float)segs[st_seg].e.scale : 1.0f;
+        if (lane == 0) tmap_acquire(mst);
+        __syncwarp();
+      }
       const uint32_t tbase = tmem + ((uint32_t)(32 * qd) << 16) + (uint32_t)(a * ZTC_N);
       tmem_ld(tbase);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       for (int sb = 0; sb < ZTC_N / 32; ++sb) {
-        const bool live = rows_live && col0 + 32 * sb < ncols;
+        const bool live = rows_live && col0 + 32 * sb < ncols_t;
         float *st = st0 + (size_t)(nst & 1) * (ZTM_STG_BYTES / 4);
         if (live) {
           // the buffer's store of two blocks ago has read its source
@@ -836,7 +895,7 @@ __global__ void __launch_bounds__(ZTM_THREADS, 1)
         if (sb + 1 < ZTC_N / 32) tmem_ld(tbase + (uint32_t)(32 * (sb + 1)));
         if (live) {
           if (lane == 0) {
-            tma_store_3d(&map_st, smem_u32(st), (int)(col0 + 32 * sb), 32 * qd, d);
+            tma_store_3d(mst, smem_u32(st), (int)(col0 + 32 * sb), 32 * qd, d);
             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
           }
           ++nst;
@@ -931,6 +990,20 @@ static ztm_encode_fn ztm_encoder() {
 // swizzle) maps of the tensor [3][nz][ncols] at spec, encoded once per
 // (device, spec, nz, ncols) and kept in a small cache (a launch then costs
 // no driver call beyond the launch itself).
+static bool ztm_encode(float *spec, int nz, int64_t ncols, CUtensorMap &mld, CUtensorMap &mst) {
+  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)nz, 3};
+  const cuuint64_t strides[2] = {(cuuint64_t)ncols * 4, (cuuint64_t)ncols * 4 * (cuuint64_t)nz};
+  const cuuint32_t box_ld[3] = {ZTC_N, ZTC_KC, 1}, box_st[3] = {32, 32, 1}, es[3] = {1, 1, 1};
+  ztm_encode_fn enc = ztm_encoder();
+  if (enc == nullptr) return false;
+  if (enc(&mld, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_ld, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  return enc(&mst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_st, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 struct ZtmMaps {
   CUtensorMap ld, st;
   const void *p;
@@ -950,18 +1023,7 @@ static bool ztm_maps(float *spec, int nz, int64_t ncols, CUtensorMap &mld, CUten
       mst = cache[i].st;
       return true;
     }
-  const cuuint64_t dims[3] = {(cuuint64_t)ncols, (cuuint64_t)nz, 3};
-  const cuuint64_t strides[2] = {(cuuint64_t)ncols * 4, (cuuint64_t)ncols * 4 * (cuuint64_t)nz};
-  const cuuint32_t box_ld[3] = {ZTC_N, ZTC_KC, 1}, box_st[3] = {32, 32, 1}, es[3] = {1, 1, 1};
-  ztm_encode_fn enc = ztm_encoder();
-  if (enc(&mld, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_ld, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return false;
-  if (enc(&mst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box_st, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return false;
+  if (!ztm_encode(spec, nz, ncols, mld, mst)) return false;
   ZtmMaps &c = cache[next];
   next = (next + 1) % 8;
   if (used < 8) ++used;
@@ -981,13 +1043,16 @@ bool ztm_supported(const float *spec, int nz, int64_t ncols) {
          (reinterpret_cast<uintptr_t>(spec) & 15) == 0 && ztm_encoder() != nullptr;
 }
 
-template <int RS, int HL>
+template <int RS, int HL, bool BATCH = false>
 static cudaError_t ztm_launch(const CUtensorMap &mld, const CUtensorMap &mst, int nz, int64_t ncols, const float *Tm,
-                              float scale, int64_t grid, int *err, cudaStream_t s) {
-  cudaError_t r =
-      cudaFuncSetAttribute(k_zgemm_tma<RS, HL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZtmCfg<RS, HL>::smem);
+                              float scale, int64_t grid, int *err, cudaStream_t s, const CUtensorMap *gmaps = nullptr,
+                              const ZSeg<float> *segs = nullptr, const int64_t *tprefix = nullptr, int S = 0,
+                              int64_t ntiles_b = 0) {
+  cudaError_t r = cudaFuncSetAttribute(k_zgemm_tma<RS, HL, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)ZtmCfg<RS, HL>::smem);
   if (r != cudaSuccess) return r;
-  k_zgemm_tma<RS, HL><<<(unsigned)grid, ZTM_THREADS, ZtmCfg<RS, HL>::smem, s>>>(mld, mst, nz, ncols, Tm, scale, err);
+  k_zgemm_tma<RS, HL, BATCH><<<(unsigned)grid, ZTM_THREADS, ZtmCfg<RS, HL>::smem, s>>>(
+      mld, mst, nz, ncols, Tm, scale, err, gmaps, segs, tprefix, S, ntiles_b);
   return cudaGetLastError();
 }
 
@@ -1008,6 +1073,31 @@ cudaError_t launch_zgemm_tma(float *spec, int nz, int64_t ncols, const float *Tm
     case 2: return ztm_launch<7, 2>(mld, mst, nz, ncols, Tm, scale, grid, err, s);
     default: return ztm_launch<6, 2>(mld, mst, nz, ncols, Tm, scale, grid, err, s);
   }
+}
+
+// Batched systems: every segment's load and store maps, in segment order
+// (2 S maps, for device memory), when every segment qualifies.
+bool ztm_maps_b(const ZSeg<float> *segs, int S, int nz, std::vector<CUtensorMap> &out) {
+  out.assign(2 * (size_t)S, CUtensorMap{});
+  for (int i = 0; i < S; ++i) {
+    if (!ztm_supported(segs[i].spec, nz, segs[i].ncols)) return false;
+    if (!ztm_encode(segs[i].spec, nz, segs[i].ncols, out[2 * i], out[2 * i + 1])) return false;
+  }
+  return true;
+}
+
+// One launch over the tiles of every segment (tprefix as launch_zgemm_tc_b,
+// device memory); gmaps: ztm_maps_b's maps in device memory.  The epilogue
+// only scales (each segment's EpiArgs); the inverse's wall correction is the
+// caller's separate pass.
+cudaError_t launch_zgemm_tma_b(const ZSeg<float> *segs, const int64_t *tprefix, int S, int64_t ntiles, int nz,
+                               const float *Tm, const CUtensorMap *gmaps, int nsm, int *err, cudaStream_t s) {
+  if (nz < 32 || nz > 128 || ntiles <= 0) return cudaErrorInvalidValue;
+  CUtensorMap unused;
+  memset(&unused, 0, sizeof(unused));
+  int64_t grid = nsm;
+  if (grid > ntiles) grid = ntiles;
+  return ztm_launch<6, 2, true>(unused, unused, nz, 0, Tm, 1.0f, grid, err, s, gmaps, segs, tprefix, S, ntiles);
 }
 
 // ---------------------------------------------------------------------------

@@ -342,11 +342,13 @@ typedef struct {
   int kernels_per_mdot; /* kernels of this library in one batched Mdot (cuFFT excluded) */
   int fft_plans;
   int64_t device_bytes;
-  int ztransform, ztransform_inverse; /* z transforms over all systems: 1 tcgen05, 0 SIMT (chosen at
+  int ztransform, ztransform_inverse; /* z transforms over all systems: 1 tcgen05, 3 tcgen05 fed by
+                                         TMA (every system's own tensor maps), 0 SIMT (chosen at
                                          creation by timing, mixed operator; DPSTOKES_GB300_ZTRANSFORM
                                          forces one) */
   float ztransform_ms[2];             /* creation-time timings, forward: SIMT, tcgen05 */
   float ztransform_inverse_ms[2];     /* inverse (with the wall correction): SIMT, tcgen05 */
+  float ztransform_tma_ms[2];         /* the TMA-fed form's: forward, inverse (0 if not timed) */
 } dpst_batch_info;
 
 int dpst_batched_create(const dpst_params *params, const int64_t *n_particles, int n_systems, int device,

@@ -155,3 +155,43 @@ def test_batched_tensor_core_ztransform(dom, torque):
     for k in range(len(ws)):
         assert rel_err(Va[k], V64[k]) < 1e-5
     b2.close()
+
+
+@pytest.mark.parametrize("dom,torque,nz", [("DPBW", True, 40), ("DP", True, 64), ("DPSC", False, 45)])
+def test_batched_tma_ztransform(dom, torque, nz):
+    """The batch's TMA-fed tcgen05 z transform (every system's spectrum
+    through its own tensor maps, one launch): against single handles on the
+    register-staged tcgen05 transform (1e-6 for V, 2e-6 for the vorticity)
+    and against the FP64 batch (1e-5)."""
+    from dataclasses import replace
+    ws = [replace(w, nz=nz) for w in W.small_batch(dom, torque)]
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, "mixed", torch.float32, zt="tma")
+    info = b.info()
+    assert info["ztransform"] == 3 and info["ztransform_inverse"] == 3, info
+    b64, _, _, _, V64, _ = _run_batch(ws, "fp64", torch.float64)
+    for k, w in enumerate(ws):
+        V1, W1 = _single(w, Xs[k], Fs[k], Ts[k], "mixed", torch.float32, zt="tcgen05")
+        ev = rel_err(Vs[k], V1)
+        ew = rel_err(Ws[k], W1) if torque else 0.0
+        e64 = rel_err(Vs[k], V64[k])
+        print("%s nz %d tma V %.2e W %.2e vs fp64 %.2e" % (w.name, nz, ev, ew, e64))
+        assert ev < 1e-6 and ew < 2e-6 and e64 < 1e-5
+    b.close()
+    b64.close()
+
+
+def test_batched_tma_ztransform_mixed_alignment():
+    """Systems whose spectrum rows do not start on 16-byte boundaries (an odd
+    mode count: nx = 16, ny = 15 gives 9 x 15) beside ones that do: the TMA
+    launch takes the latter, the register-staged launch the former, and
+    every system matches its single handle."""
+    from dataclasses import replace
+    ws = [replace(w, nz=48) for w in W.small_batch("DPBW", True)]
+    ws[1] = replace(ws[1], nx=16, ny=15, Lx=16.0, Ly=15.0)
+    b, Xs, Fs, Ts, Vs, Ws = _run_batch(ws, "mixed", torch.float32, zt="tma")
+    info = b.info()
+    assert info["ztransform"] == 3 and info["ztransform_inverse"] == 3, info
+    for k, w in enumerate(ws):
+        V1, W1 = _single(w, Xs[k], Fs[k], Ts[k], "mixed", torch.float32, zt="tcgen05")
+        assert rel_err(Vs[k], V1) < 1e-6 and rel_err(Ws[k], W1) < 2e-6
+    b.close()
