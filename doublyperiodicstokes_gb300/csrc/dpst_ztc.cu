@@ -1170,6 +1170,28 @@ __global__ void __launch_bounds__(128) k_corr_add(float *spec, int nz, int64_t n
   const CT fac = ea.fac, Lz = (CT)ea.ks.Lz;
   const float *__restrict__ znf = ea.znf;
   const int64_t dstride = (int64_t)nz * nk;
+  // the node-independent parts of each pass, hoisted out of the node loop:
+  //   bottom wall: v_x = (-qx/k) z e^{-kz} al + e^{-kz} f0, v_y likewise,
+  //     v_z = -i z e^{-kz} al + e^{-kz} f2, al = qx f0 + qy f1 + i k f2
+  //     (f conjugated in the Nyquist partner's pass);
+  //   slit: the same with fac / k and the top wall's e^{k(z - Lz)} terms.
+  cplx<CT> al[2], f[2][3];
+  CT ax[2], ay[2];
+#pragma unroll
+  for (int pass = 0; pass < 2; ++pass) {
+    const CT qx = pass ? m1.x : m0.y, qy = pass ? m1.y : m0.z;
+    if constexpr (WM == 1) {
+      f[pass][0] = pass ? conj(c[0]) : c[0];
+      f[pass][1] = pass ? conj(c[1]) : c[1];
+      f[pass][2] = pass ? conj(c[2]) : c[2];
+      al[pass] = (qx * f[pass][0] + qy * f[pass][1]) + ik(k, f[pass][2]);
+      ax[pass] = -qx / k;
+      ay[pass] = -qy / k;
+    } else {
+      ax[pass] = qx * fac / k;
+      ay[pass] = qy * fac / k;
+    }
+  }
   constexpr int U = 4;
   for (int mb = m_beg; mb < m_end; mb += U) {
     float2 vin[U][3];
@@ -1194,24 +1216,16 @@ __global__ void __launch_bounds__(128) k_corr_add(float *spec, int nz, int64_t n
 #pragma unroll
       for (int pass = 0; pass < 2; ++pass) {
         if (pass >= npass) break;
-        const CT qx = pass ? m1.x : m0.y, qy = pass ? m1.y : m0.z;
         cplx<CT> v[3];
         if constexpr (WM == 1) {
-          cplx<CT> f0 = c[0], f1 = c[1], f2 = c[2];
-          if (pass) {
-            f0 = conj(f0);
-            f1 = conj(f1);
-            f2 = conj(f2);
-          }
-          const cplx<CT> al = (qx * f0 + qy * f1) + ik(k, f2);
-          v[0] = (-qx * zenkz / k) * al + enkz * f0;
-          v[1] = (-qy * zenkz / k) * al + enkz * f1;
-          v[2] = ik(-zenkz, al) + enkz * f2;
+          v[0] = (ax[pass] * zenkz) * al[pass] + enkz * f[pass][0];
+          v[1] = (ay[pass] * zenkz) * al[pass] + enkz * f[pass][1];
+          v[2] = ik(-zenkz, al[pass]) + enkz * f[pass][2];
         } else {
           const int o = 8 * pass;
-          v[0] = (ik(-qx * zenkz * fac / k, c[o + 0]) + ik(qx * zekzmh * fac / k, c[o + 1])) +
+          v[0] = (ik(-ax[pass] * zenkz, c[o + 0]) + ik(ax[pass] * zekzmh, c[o + 1])) +
                  (enkz * c[o + 2] + ekzmh * c[o + 3]);
-          v[1] = (ik(-qy * zenkz * fac / k, c[o + 0]) + ik(qy * zekzmh * fac / k, c[o + 1])) +
+          v[1] = (ik(-ay[pass] * zenkz, c[o + 0]) + ik(ay[pass] * zekzmh, c[o + 1])) +
                  (enkz * c[o + 4] + ekzmh * c[o + 5]);
           v[2] = ((zenkz * fac) * c[o + 0] + (zekzmh * fac) * c[o + 1]) + (enkz * c[o + 6] + ekzmh * c[o + 7]);
         }
