@@ -32,6 +32,12 @@ namespace dpst {
 
 // e^{-2 pi i m / 32}: the twiddles of the in-register DFTs (sizes dividing 32)
 __constant__ float2 c_tw32[32];
+// e^{-2 pi i m / 1024}: the column passes' stage twiddles for every length L
+// <= 1024 (w_L^j = entry j 1024 / L, the same FP32 values as a length-L
+// table).  A warp of a column pass reads two distinct entries per access (its
+// two thread rows), which the constant cache serves without the load pipe.
+constexpr int FFT_TWC = 1024;
+__constant__ float2 c_twc[FFT_TWC];
 
 static __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(__fmaf_rn(a.x, b.x, -a.y * b.y), __fmaf_rn(a.x, b.y, a.y * b.x));
@@ -280,7 +286,7 @@ static __device__ __forceinline__ void cols_body(float2 *__restrict__ data, int6
     for (int k1 = 0; k1 < Q; ++k1) {
       float2 y = v[brev<Q>(k1)];
       if (k1 != 0 && p != 0) {
-        float2 w = __ldg(twL + p * k1);
+        float2 w = c_twc[p * k1 * (FFT_TWC / L)];
         if (DIR > 0) w = conjf2(w);
         y = cmulf(y, w);
       }
@@ -658,7 +664,7 @@ static __device__ __forceinline__ void col_tile_cl(float2 *__restrict__ sp, int 
   for (int k1 = 0; k1 < Q; ++k1) {
     float2 y = v[brev<Q>(k1)];
     if (k1 != 0 && p != 0) {
-      float2 w = __ldg(twL + p * k1);
+      float2 w = c_twc[p * k1 * (FFT_TWC / L)];
       if (DIR > 0) w = conjf2(w);
       y = cmulf(y, w);
     }
@@ -788,6 +794,10 @@ static cudaError_t upload_tw32() {
   if (dev >= 0 && dev < 256 && done[dev]) return cudaSuccess;
   const std::vector<float2> t = fft_twiddles(32);
   e = cudaMemcpyToSymbol(c_tw32, t.data(), sizeof(float2) * 32);
+  if (e == cudaSuccess) {
+    const std::vector<float2> tc = fft_twiddles(FFT_TWC);
+    e = cudaMemcpyToSymbol(c_twc, tc.data(), sizeof(float2) * FFT_TWC);
+  }
   if (e == cudaSuccess && dev >= 0 && dev < 256) done[dev] = true;
   return e;
 }
