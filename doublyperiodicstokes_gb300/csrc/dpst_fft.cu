@@ -106,7 +106,7 @@ struct RowCfg {
 template <int L, int P>
 static __device__ __forceinline__ void rows_r2c_body(const float *__restrict__ in, float2 *__restrict__ out,
                                                      int64_t rows, int64_t row0, const float2 *__restrict__ twN,
-                                                     float2 *sbuf) {
+                                                     float2 *sbuf, const float2 *tws, int tss) {
   constexpr int Q = L / P, N = 2 * L, R = Q / P;
   if (threadIdx.x >= RowCfg<L, P>::T) return;
   const int g = threadIdx.x / P, p = threadIdx.x % P;
@@ -125,7 +125,7 @@ static __device__ __forceinline__ void rows_r2c_body(const float *__restrict__ i
 #pragma unroll
     for (int k1 = 0; k1 < Q; ++k1) {
       float2 y = v[brev<Q>(k1)];
-      if (k1 != 0 && p != 0) y = cmulf(y, __ldg(twN + 2 * p * k1));
+      if (k1 != 0 && p != 0) y = cmulf(y, tws[p * k1 * tss]);
       sm[k1 * (P + 1) + p] = y;
     }
     __syncwarp();
@@ -169,13 +169,16 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_r2c(const float *_
                                                                   float2 *__restrict__ out, int64_t rows,
                                                                   const float2 *__restrict__ twN) {
   __shared__ float2 sbuf[RowCfg<L, P>::RPC * RowCfg<L, P>::BUF];
-  rows_r2c_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf);
+  __shared__ float2 tws[L];  // w_L^j = w_N^{2j}: the stage twiddles, read at 16 distinct entries per warp
+  for (int j = threadIdx.x; j < L; j += blockDim.x) tws[j] = __ldg(twN + 2 * j);
+  __syncthreads();
+  rows_r2c_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf, tws, 1);
 }
 
 template <int L, int P>
 static __device__ __forceinline__ void rows_c2r_body(const float2 *__restrict__ in, float *__restrict__ out,
                                                      int64_t rows, int64_t row0, const float2 *__restrict__ twN,
-                                                     float2 *sbuf) {
+                                                     float2 *sbuf, const float2 *tws, int tss) {
   constexpr int Q = L / P, N = 2 * L, R = Q / P;
   if (threadIdx.x >= RowCfg<L, P>::T) return;
   const int g = threadIdx.x / P, p = threadIdx.x % P;
@@ -217,7 +220,7 @@ static __device__ __forceinline__ void rows_c2r_body(const float2 *__restrict__ 
 #pragma unroll
     for (int k1 = 0; k1 < Q; ++k1) {
       float2 y = v[brev<Q>(k1)];
-      if (k1 != 0 && p != 0) y = cmulf(y, conjf2(__ldg(twN + 2 * p * k1)));
+      if (k1 != 0 && p != 0) y = cmulf(y, conjf2(tws[p * k1 * tss]));
       sm[k1 * (P + 1) + p] = y;
     }
     __syncwarp();
@@ -249,7 +252,10 @@ __global__ void __launch_bounds__(RowCfg<L, P>::T) k_fft_rows_c2r(const float2 *
                                                                   float *__restrict__ out, int64_t rows,
                                                                   const float2 *__restrict__ twN) {
   __shared__ float2 sbuf[RowCfg<L, P>::RPC * RowCfg<L, P>::BUF];
-  rows_c2r_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf);
+  __shared__ float2 tws[L];  // w_L^j = w_N^{2j}, as in k_fft_rows_r2c
+  for (int j = threadIdx.x; j < L; j += blockDim.x) tws[j] = __ldg(twN + 2 * j);
+  __syncthreads();
+  rows_c2r_body<L, P>(in, out, rows, (int64_t)blockIdx.x * RowCfg<L, P>::RPC, twN, sbuf, tws, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -428,8 +434,8 @@ __global__ void __launch_bounds__(XyCfg<NX, NY>::T, XyCfg<NX, NY>::MINB) k_fft_x
     }
     const bool rowtask = (first != INV);
     if (rowtask) {
-      if (!INV) rows_r2c_body<L, C::P>(gin, spec, rows, plane * NY + (int64_t)idx * RPC, twx, xsm);
-      else rows_c2r_body<L, C::P>(spec, gout, rows, plane * NY + (int64_t)idx * RPC, twx, xsm);
+      if (!INV) rows_r2c_body<L, C::P>(gin, spec, rows, plane * NY + (int64_t)idx * RPC, twx, xsm, twx, 2);
+      else rows_c2r_body<L, C::P>(spec, gout, rows, plane * NY + (int64_t)idx * RPC, twx, xsm, twx, 2);
     } else {
       cols_body<NY, C::PY, INV ? 1 : -1>(spec, plane, idx, L + 1, twy, xsm);
     }
