@@ -343,8 +343,8 @@ def run_ours(args, rank, world):
         nk_solve = w.ny * (w.nx // 2 + 1)
         if w.domType == "DP" and w.nz == 128:
             # ncu launch list of the c2 Mdot (512^2 x 128 open box, 131,584 wavenumbers):
-            # k_bvp_df variant 3 read 1063.1 MB and wrote 614.9 MB per launch
-            roof["traffic"] = (1063.1e6 + 614.9e6) / 131584 * nk_solve
+            # k_bvp_df variant 3 read 1065.8 MB and wrote 615.5 MB per launch
+            roof["traffic"] = (1065.8e6 + 615.5e6) / 131584 * nk_solve
             roof["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_bvp_df "
                                       "(variant 3) on c2_dp_n65536, per launch, scaled by wavenumbers "
                                       "(profiles/launches_c2_dp_n65536_mixed.md)")
